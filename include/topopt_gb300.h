@@ -1,0 +1,155 @@
+/*
+ * topopt_gb300 -- C ABI of the GB300 (sm_103a) SIMP compliance-minimisation
+ * library.  Plain pointers and sizes only; every host array is C-contiguous,
+ * FP64 (double), int64 (indices) or int32/int8 as stated.
+ *
+ * The library is a drop-in for the per-iteration hot path of the reference
+ * topoptlab driver (topoptlab/topology_optimization.py:411-673): SIMP
+ * scaling, assembly + Dirichlet slicing + linear solve, compliance and
+ * sensitivities, sensitivity / density filter, OC update, change / volume.
+ * A context (tg_ctx) owns every device buffer of one problem and one CUDA
+ * stream; it is not re-entrant, separate contexts may run concurrently.
+ *
+ * Return codes: TG_OK, or one of the TG_E* codes with a message available
+ * from tg_last_error().  The Python wrapper maps TG_EINVAL to ValueError and
+ * TG_ENOTCONV / TG_ETIMEOUT / TG_ENAN / TG_ECUDA to RuntimeError, like the
+ * reference's ValueError("Unknown ...") (topology_optimization.py:262, :367)
+ * and RuntimeError("... did not converge") (solve_linsystem.py:349-351).
+ */
+#ifndef TOPOPT_GB300_H
+#define TOPOPT_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TG_ABI_VERSION 1
+
+enum {
+  TG_OK = 0,
+  TG_EINVAL = 1,     /* bad argument / unsupported combination */
+  TG_ENOTCONV = 2,   /* PCG or OC bisection did not converge within its cap */
+  TG_ETIMEOUT = 3,   /* a device loop hit its wall-clock limit */
+  TG_ENAN = 4,       /* NaN / Inf in a residual or objective */
+  TG_ECUDA = 5,      /* CUDA runtime error */
+  TG_ENOMEM = 6
+};
+
+enum { TG_PREC_FP64 = 0, TG_PREC_MIXED = 1 };
+enum { TG_PRECOND_GMG = 0, TG_PRECOND_JACOBI = 1 };
+enum {
+  TG_FIELD_X = 0,      /* design variables x            (nel)  */
+  TG_FIELD_XPHYS = 1,  /* physical densities xPhys      (nel)  */
+  TG_FIELD_U = 2,      /* state (displacement / temp.)  (ndof) */
+  TG_FIELD_DC = 3,     /* filtered objective sensitivity (nel) */
+  TG_FIELD_DV = 4,     /* filtered volume sensitivity   (nel)  */
+  TG_FIELD_F = 5       /* load vector                   (ndof) */
+};
+
+/* Problem description; mirrors the arguments of the reference main()
+ * (topology_optimization.py:47-79) that the hot path consumes. */
+typedef struct tg_problem {
+  int32_t ndim;          /* 2 or 3 */
+  int32_t nnode_dof;     /* 1 (Poisson) or ndim (elasticity) */
+  int32_t nelx, nely, nelz;   /* nelz ignored for ndim == 2 */
+  const double* KE;      /* element matrix, (2^ndim*nnode_dof)^2, row major,
+                            reference local node order (lk(l=l) output) */
+  const int64_t* fixed;  /* fixed DOF indices (bcs() output) */
+  int64_t nfixed;
+  const double* f;       /* load vector, ndof (bcs() output, one load case) */
+  double volfrac, rmin, eps, penal, move;
+  int32_t ft;            /* -1 none, 0 sensitivity filter, 1 density filter */
+  const int8_t* el_flags;/* NULL or nel flags: 1 passive (0), 2 active (1) */
+  int32_t precond;       /* TG_PRECOND_* */
+  int32_t precision;     /* TG_PREC_* */
+  int32_t nlevels;       /* multigrid levels, 0 = automatic */
+  int32_t nsmooth;       /* damped-Jacobi sweeps before / after (default 2) */
+  double omega;          /* Jacobi damping (default 0.6) */
+  double rtol;           /* FP64 relative residual target (default 1e-8) */
+  int32_t maxiter;       /* PCG iteration cap (default 2000) */
+  double inner_rtol;     /* mixed precision: FP32 inner solve target (1e-4) */
+  int32_t learned;       /* 1: learned warm start (requires tg_cnn_* setup) */
+  int32_t device;        /* CUDA device ordinal */
+} tg_problem;
+
+typedef struct tg_iter_out {
+  double obj;            /* compliance of the design that was solved */
+  double vol;            /* mean(xPhys) after the update */
+  double change;         /* max |x_new - x_old| */
+  double g;              /* OC carry (optimality_criterion.py:73) */
+  double rel_res;        /* true FP64 ||f - K u|| / ||f|| after the solve */
+  int32_t pcg_iters;     /* (inner) PCG iterations */
+  int32_t vcycles;       /* V-cycles applied */
+  int32_t refinements;   /* FP64 refinement steps (mixed precision) */
+  int32_t oc_steps;      /* OC bisection steps */
+  int32_t fallback;      /* 1 if the learned warm start was rejected */
+  int32_t nlevels;       /* multigrid levels used */
+  double t_solve_ms;     /* device time of the linear solve */
+  double t_step_ms;      /* host wall time of the whole step */
+} tg_iter_out;
+
+typedef struct tg_solve_info {
+  int32_t iters, vcycles, refinements, converged;
+  double rel_res;
+} tg_solve_info;
+
+typedef struct tg_ctx tg_ctx;
+
+int32_t tg_abi_version(void);
+
+/* Message of the last failing call on ctx, or of the last failing
+ * tg_create / context-free call when ctx is NULL. */
+const char* tg_last_error(const tg_ctx* ctx);
+
+/* Replaces the set-up half of main() (topology_optimization.py:203-409):
+ * element matrix, edofMat (implicit), filter, BCs, initial design x = volfrac.*/
+int32_t tg_create(const tg_problem* prob, tg_ctx** out);
+void tg_destroy(tg_ctx* ctx);
+
+/* One design iteration (topology_optimization.py:411-673, OC branch). */
+int32_t tg_step(tg_ctx* ctx, tg_iter_out* out);
+
+/* Host <-> device copies of a field (TG_FIELD_*), n = number of doubles. */
+int32_t tg_get(tg_ctx* ctx, int32_t field, double* host, int64_t n);
+int32_t tg_set(tg_ctx* ctx, int32_t field, const double* host, int64_t n);
+
+/* Unit entry points (host buffers), used by the solve_lin / filter / OC /
+ * objective mirrors and by the tests. */
+/* y = M K(xPhys) M u  (fem.py:141-237 + SpMV); precision TG_PREC_FP64 or
+ * TG_PREC_MIXED (FP32 arithmetic, result widened to FP64). */
+int32_t tg_kmul(tg_ctx* ctx, const double* xPhys, const double* u, double* y, int32_t precision);
+/* K u = rhs on the free DOFs (solve_linsystem.py:20-365 slot).  u0 may be NULL. */
+int32_t tg_solve(tg_ctx* ctx, const double* xPhys, const double* rhs, const double* u0, double* u,
+                 tg_solve_info* info);
+/* mode 0: (H x)/Hs   1: H(x/Hs)   2: H(x*d)/Hs/max(1e-3,x)   3: Hs
+ * (filter/matrix_filter.py:101-232 + topology_optimization.py:545-558, :639) */
+int32_t tg_filter(tg_ctx* ctx, const double* x, const double* d, double* y, int32_t mode);
+/* obj = sum simp(xPhys) u_e^T KE u_e, dc = -simp_dx(xPhys) u_e^T KE u_e
+ * (objectives.py:51-55, topology_optimization.py:491-500) */
+int32_t tg_compliance(tg_ctx* ctx, const double* xPhys, const double* u, double* obj, double* dc);
+/* oc_top88 (optimizer/optimality_criterion.py:9-79) */
+int32_t tg_oc(tg_ctx* ctx, const double* x, const double* dc, const double* dv, double g,
+              double* xnew, double* gt, int32_t* nsteps);
+/* oc_top88 without a context: n design variables, optional el_flags (int8,
+ * 1 passive, 2 active), bisection bounds l1 < l2 */
+int32_t tg_oc_raw(int64_t n, const double* x, const double* dc, const double* dv, double g,
+                  const int8_t* el_flags, double move, double l1, double l2, double* xnew,
+                  double* gt, int32_t* nsteps, int32_t device);
+/* one multigrid V-cycle x = V(b) for the densities xPhys */
+int32_t tg_vcycle(tg_ctx* ctx, const double* xPhys, const double* b, double* x, int32_t precision);
+/* number of multigrid levels and the DOF count of one level */
+int32_t tg_levels(tg_ctx* ctx, int32_t* nlevels, int64_t* ndofs_per_level /* >= 8 entries */);
+/* assembled stencil of level >= 1 for the densities xPhys, layout
+ * [(dir*ndof+ci)*ndof+cj][node], n = 3^ndim*ndof^2*nnodes(level) */
+int32_t tg_coarse_stencil(tg_ctx* ctx, const double* xPhys, int32_t level, double* out, int64_t n);
+/* edofMat (elements/bilinear_quadrilateral.py:7-48, trilinear_hexahedron.py:7-58)
+ * generated on the device; out has nel*(2^ndim*nnode_dof) int32 entries */
+int32_t tg_edofmat(int32_t ndim, int32_t nelx, int32_t nely, int32_t nelz, int32_t nnode_dof,
+                   int32_t* out, int32_t device);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TOPOPT_GB300_H */

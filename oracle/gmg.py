@@ -1,0 +1,127 @@
+"""FP64 geometric-multigrid PCG restatement (test infrastructure only).
+
+The reference ships a V-cycle skeleton (multigrid.py:89-154), a damped-Jacobi
+smoother (linear_solvers.py:306-372), a PCG (linear_solvers.py:50-136) and a
+stride-2 coarse-node selection (gmg.py:148-189), but its geometric
+interpolator (gmg.py:34-146) raises on every grid and solve_lin never wires a
+multigrid preconditioner (solve_linsystem.py:136).  This module is the CPU
+statement of the multigrid the GPU library builds in their place:
+
+* operators live on all DOFs with Dirichlet rows/columns zeroed:
+  A_0 = M_0 K M_0  (M = diagonal 0/1 mask of free DOFs);
+* prolongation P is the trilinear (bilinear) interpolation from the stride-2
+  coarse nodes (the nodes create_coarse_inds selects), applied per DOF
+  component, with masks on both sides: Pt = M_l P M_{l+1};
+* coarse DOF fixed  <=>  the coincident fine DOF is fixed;
+* Galerkin coarse operators A_{l+1} = Pt^T A_l Pt;
+* V-cycle with zero initial guess on every level, nu damped-Jacobi sweeps
+  before and after the coarse correction, exact coarsest solve;
+* PCG exactly as linear_solvers.py:114-134 with ||r||_2 < rtol*||b||_2.
+"""
+from __future__ import annotations
+
+import numpy as np
+import scipy.sparse as sp
+
+
+def _interp_1d(nf):
+    """(nf+1) x (nf//2+1) linear interpolation between stride-2 nodes."""
+    nc = nf // 2
+    rows, cols, vals = [], [], []
+    for i in range(nf + 1):
+        if i % 2 == 0:
+            rows.append(i), cols.append(i // 2), vals.append(1.0)
+        else:
+            rows += [i, i]
+            cols += [i // 2, i // 2 + 1]
+            vals += [0.5, 0.5]
+    return sp.csr_matrix((vals, (rows, cols)), shape=(nf + 1, nc + 1))
+
+
+def prolongation(dims, ndof):
+    """P: coarse nodal vector -> fine nodal vector.  Node order y fastest,
+    then x, then z; DOF = node*ndof + c.  dims = (nelx, nely[, nelz])."""
+    Px = _interp_1d(dims[0])
+    Py = _interp_1d(dims[1])
+    P = sp.kron(Px, Py)                       # node index x*(ny+1)+y
+    if len(dims) == 3:
+        P = sp.kron(_interp_1d(dims[2]), P)   # z slowest
+    return sp.kron(P, sp.identity(ndof)).tocsr()
+
+
+def coarse_fixed_mask(fixed_mask, dims, ndof):
+    """Coarse DOF fixed iff its coincident fine DOF is fixed."""
+    nn = [d + 1 for d in dims]
+    m = fixed_mask.reshape(([nn[2]] if len(dims) == 3 else []) + [nn[0], nn[1], ndof])
+    if len(dims) == 3:
+        return m[::2, ::2, ::2, :].ravel().copy()
+    return m[::2, ::2, :].ravel().copy()
+
+
+class Hierarchy:
+    def __init__(self, K, fixed_mask, dims, ndof, nlevels, omega=0.6, nsmooth=2):
+        self.omega, self.nsmooth = omega, nsmooth
+        free = (~fixed_mask).astype(float)
+        M = sp.diags(free)
+        self.A = [(M @ K @ M).tocsr()]
+        self.mask = [fixed_mask]
+        self.P = []
+        self.dims = [tuple(dims)]
+        d = tuple(dims)
+        for _ in range(nlevels - 1):
+            P = prolongation(d, ndof)
+            cmask = coarse_fixed_mask(self.mask[-1], d, ndof)
+            Pt = sp.diags((~self.mask[-1]).astype(float)) @ P @ sp.diags((~cmask).astype(float))
+            Pt = Pt.tocsr()
+            self.P.append(Pt)
+            self.A.append((Pt.T @ self.A[-1] @ Pt).tocsr())
+            self.mask.append(cmask)
+            d = tuple(x // 2 for x in d)
+            self.dims.append(d)
+        self.Dinv = []
+        for A, m in zip(self.A, self.mask):
+            dg = A.diagonal().copy()
+            inv = np.zeros_like(dg)
+            inv[~m] = 1.0 / dg[~m]
+            self.Dinv.append(inv)
+        Ac = self.A[-1].toarray()
+        mc = self.mask[-1]
+        Ac[mc, mc] = 1.0
+        self.Ac_inv = np.linalg.inv(Ac)
+        self.Ac_inv[mc, :] = 0.0
+        self.Ac_inv[:, mc] = 0.0
+
+    def vcycle(self, b, lvl=0):
+        if lvl == len(self.A) - 1:
+            return self.Ac_inv @ b
+        A, Dinv, w = self.A[lvl], self.Dinv[lvl], self.omega
+        x = w * Dinv * b
+        for _ in range(self.nsmooth - 1):
+            x = x + w * Dinv * (b - A @ x)
+        r = b - A @ x
+        xc = self.vcycle(self.P[lvl].T @ r, lvl + 1)
+        x = x + self.P[lvl] @ xc
+        for _ in range(self.nsmooth):
+            x = x + w * Dinv * (b - A @ x)
+        return x
+
+
+def pcg(A, b, precond, x0=None, rtol=1e-8, maxiter=10000):
+    """linear_solvers.py:50-136 with conv. criterion res_norm (:31-48)."""
+    x = np.zeros_like(b) if x0 is None else x0.copy()
+    atol = rtol * np.linalg.norm(b)
+    r = b - A @ x
+    p = np.zeros_like(b)
+    rho_prev = None
+    for i in range(maxiter):
+        if np.linalg.norm(r) < atol:
+            return x, i
+        z = precond(r)
+        rho = r @ z
+        p = z.copy() if i == 0 else p * (rho / rho_prev) + z
+        q = A @ p
+        alpha = rho / (p @ q)
+        x += alpha * p
+        r -= alpha * q
+        rho_prev = rho
+    return x, -1

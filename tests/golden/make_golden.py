@@ -1,0 +1,190 @@
+"""Generate the golden fixtures in this folder by running the reference
+topoptlab (stefanhiemer/topoptlab) on CPU in this container.
+
+The reference is pure Python; it imports a few optional packages at module
+level (matplotlib, cvxopt, pyamg, mmapy, meshio) that are not needed on the
+paths used here (scipy-direct solve, OC optimiser, no display, no export), so
+they are replaced by inert stub modules before the import.
+
+Run:  python tests/golden/make_golden.py [/path/to/reference]
+
+Outputs (small .npz files, committed):
+  elements.npz     edofMat (2-D / 3-D, several nnode_dof), KE matrices,
+                   create_coarse_inds arrays (the GMG index pins)
+  filters.npz      matrix filter H (dense) and Hs for small 2-D / 3-D grids
+  mbb2d_60x20.npz  MBB beam 60x20, ft=1, OC: obj/vol/change per iteration,
+                   xPhys/u/dc/x snapshots at selected iterations, final x
+  heat2d_40x40.npz heat plate 40x40, ft=0, OC (Poisson KE)
+  mbb2d_60x20_ft0.npz  MBB beam 60x20 with the sensitivity filter
+  cant3d_12x6x6.npz    3-D cantilever (reference callable), ft=1, 12 iterations
+"""
+import os
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+
+
+class _Inert:
+    def __getattr__(self, k):
+        return _Inert()
+
+    def __call__(self, *a, **k):
+        return _Inert()
+
+
+def _install_stubs():
+    attrs = {
+        "matplotlib": [], "matplotlib.pyplot": [], "matplotlib.colors": ["Normalize"],
+        "cvxopt": ["matrix", "spmatrix"], "cvxopt.cholmod": ["solve", "symbolic", "numeric"],
+        "pyamg": [], "pyamg.aggregation": ["adaptive_sa_solver", "rootnode_solver",
+                                            "smoothed_aggregation_solver", "pairwise_solver"],
+        "pyamg.classical": ["air_solver", "ruge_stuben_solver"],
+        "mmapy": ["mmasub", "gcmmasub", "asymp", "concheck", "raaupdate", "kktcheck"],
+        "meshio": ["Mesh", "write", "read"],
+    }
+    for name, names in attrs.items():
+        m = types.ModuleType(name)
+        m.__path__ = []
+        for a in names:
+            setattr(m, a, _Inert())
+        sys.modules[name] = m
+    sys.modules["matplotlib"].pyplot = sys.modules["matplotlib.pyplot"]
+
+
+_install_stubs()
+sys.path.insert(0, REF)
+
+import topoptlab.topology_optimization as T  # noqa: E402
+from topoptlab.elements.bilinear_quadrilateral import create_edofMat as edof2d  # noqa: E402
+from topoptlab.elements.trilinear_hexahedron import create_edofMat as edof3d  # noqa: E402
+from topoptlab.elements.linear_elasticity_2d import lk_linear_elast_2d  # noqa: E402
+from topoptlab.elements.linear_elasticity_3d import lk_linear_elast_3d  # noqa: E402
+from topoptlab.elements.poisson_2d import lk_poisson_2d  # noqa: E402
+from topoptlab.elements.poisson_3d import lk_poisson_3d  # noqa: E402
+from topoptlab.filter.matrix_filter import assemble_matrix_filter  # noqa: E402
+from topoptlab.gmg import create_coarse_inds  # noqa: E402
+from topoptlab.example_bc.lin_elast import mbb_2d, cantilever_3d  # noqa: E402
+from topoptlab.example_bc.heat_conduction import heatplate_2d  # noqa: E402
+from topoptlab.objectives import compliance  # noqa: E402
+from topoptlab.optimizer.optimality_criterion import oc_top88  # noqa: E402
+
+OUT_KW = {"file": None, "display": False, "export": False, "write_log": False,
+          "profile": False, "debug": 0}
+
+
+def gen_elements():
+    d = {}
+    for (nx, ny, nd) in [(5, 3, 1), (5, 3, 2), (60, 20, 2)]:
+        d[f"edof2d_{nx}x{ny}_{nd}"] = edof2d(nelx=nx, nely=ny, nnode_dof=nd)[0]
+    for (nx, ny, nz, nd) in [(4, 3, 2, 1), (4, 3, 2, 3), (6, 4, 4, 3)]:
+        d[f"edof3d_{nx}x{ny}x{nz}_{nd}"] = edof3d(nelx=nx, nely=ny, nelz=nz, nnode_dof=nd)[0]
+    d["KE_elast2d"] = lk_linear_elast_2d(l=np.array([1., 1.]))
+    d["KE_elast3d"] = lk_linear_elast_3d(l=np.array([1., 1., 1.]))
+    d["KE_poisson2d"] = lk_poisson_2d(l=np.array([1., 1.]))
+    d["KE_poisson3d"] = lk_poisson_3d(l=np.array([1., 1., 1.]))
+    d["KE_elast2d_rect"] = lk_linear_elast_2d(l=np.array([2., 1.]))
+    d["KE_elast3d_rect"] = lk_linear_elast_3d(l=np.array([1., 2., 0.5]))
+    # GMG coarse index pins (the cases of the reference's tests/test_gmg.py)
+    cases = [(4, 6, None, 1, 2), (4, 6, None, 2, 2), (4, 6, 8, 1, 2), (4, 6, 8, 3, 2),
+             (8, 4, 4, 3, 2), (16, 8, 8, 3, 2)]
+    for (nx, ny, nz, nd, st) in cases:
+        d[f"coarse_{nx}_{ny}_{nz}_{nd}_{st}"] = create_coarse_inds(
+            nelx=nx, nely=ny, nelz=nz, ndof=nd, stride=st)
+    # boundary-condition callables (fixed DOFs and load vectors)
+    for (nx, ny) in [(60, 20), (10, 4)]:
+        u, f, fixed, free, _ = mbb_2d(nelx=nx, nely=ny, ndof=2 * (nx + 1) * (ny + 1))
+        d[f"bc_mbb2d_{nx}x{ny}_fixed"], d[f"bc_mbb2d_{nx}x{ny}_f"] = fixed, f[:, 0]
+    for (nx, ny, nz) in [(12, 6, 6), (16, 8, 8)]:
+        u, f, fixed, free, _ = cantilever_3d(nelx=nx, nely=ny, nelz=nz,
+                                             ndof=3 * (nx + 1) * (ny + 1) * (nz + 1))
+        d[f"bc_cant3d_{nx}x{ny}x{nz}_fixed"], d[f"bc_cant3d_{nx}x{ny}x{nz}_f"] = fixed, f[:, 0]
+    for n in [40, 64, 100]:
+        u, f, fixed, free, _ = heatplate_2d(nelx=n, nely=n, ndof=(n + 1) ** 2)
+        d[f"bc_heat2d_{n}_fixed"], d[f"bc_heat2d_{n}_f"] = fixed, f[:, 0]
+    np.savez_compressed(os.path.join(HERE, "elements.npz"), **d)
+
+
+def gen_filters():
+    d = {}
+    for (nx, ny, nz, rmin) in [(7, 5, None, 2.4), (9, 6, None, 1.5), (6, 5, 4, 1.5),
+                               (5, 4, 3, 2.4)]:
+        H, Hs = assemble_matrix_filter(nelx=nx, nely=ny, nelz=nz, rmin=rmin,
+                                       ndim=2 if nz is None else 3)
+        key = f"{nx}_{ny}_{nz}_{rmin}"
+        d["H_" + key] = H.toarray()
+        d["Hs_" + key] = np.asarray(Hs).ravel()
+    np.savez_compressed(os.path.join(HERE, "filters.npz"), **d)
+
+
+def run_traced(name, snap_its, **kw):
+    """Run the reference main() and record per-iteration state.
+
+    compliance() sees (xPhys, u) of each iteration, oc_top88 sees
+    (x, dc, dv, g) after the sensitivity filter and returns (xnew, g)."""
+    rec = {"obj": [], "g": [], "xPhys": {}, "u": {}, "dc": {}, "dv": {}, "x_in": {},
+           "x_out": {}, "g_in": {}}
+    it = {"k": 0}
+
+    def comp(**a):
+        obj, rhs_adj, sa = compliance(**a)
+        k = it["k"]
+        rec["obj"].append(obj)
+        if k in snap_its:
+            rec["xPhys"][k] = a["xPhys"][:, 0].copy()
+            rec["u"][k] = a["u"][:, 0].copy()
+        return obj, rhs_adj, sa
+
+    def oc(x, volfrac, dc, dv, g, el_flags, **k2):
+        k = it["k"]
+        xnew, gt = oc_top88(x=x, volfrac=volfrac, dc=dc, dv=dv, g=g, el_flags=el_flags, **k2)
+        if k in snap_its:
+            rec["dc"][k] = dc.copy()
+            rec["dv"][k] = dv.copy()
+            rec["x_in"][k] = x.copy()
+            rec["x_out"][k] = xnew.copy()
+            rec["g_in"][k] = g
+        rec["g"].append(gt)
+        it["k"] += 1
+        return xnew, gt
+
+    orig_oc = T.oc_top88
+    T.oc_top88 = oc
+    try:
+        x, obj = T.main(obj_func=comp, optimizer="oc", output_kw=OUT_KW, **kw)
+    finally:
+        T.oc_top88 = orig_oc
+    out = {"final_x": x[:, 0], "final_obj": np.array(obj), "g": np.array(rec["g"]),
+           "obj": np.array(rec["obj"]),
+           "n_iter": np.array(it["k"])}
+    for key in ["xPhys", "u", "dc", "dv", "x_in", "x_out", "g_in"]:
+        for k, v in rec[key].items():
+            out[f"{key}_{k}"] = np.asarray(v)
+    np.savez_compressed(os.path.join(HERE, name), **out)
+    return x, obj, it["k"]
+
+
+def main():
+    gen_elements()
+    gen_filters()
+    r = run_traced("mbb2d_60x20.npz", {0, 1, 2, 24, 143},
+                   nelx=60, nely=20, volfrac=0.5, rmin=2.4, ft=1, bcs=mbb_2d)
+    print("mbb ft1", r[1], r[2])
+    r = run_traced("mbb2d_60x20_ft0.npz", {0, 1, 2},
+                   nelx=60, nely=20, volfrac=0.5, rmin=2.4, ft=0, bcs=mbb_2d)
+    print("mbb ft0", r[1], r[2])
+    r = run_traced("heat2d_40x40.npz", {0, 1, 2},
+                   nelx=40, nely=40, volfrac=0.4, rmin=1.2, ft=0, bcs=heatplate_2d,
+                   lk=lk_poisson_2d)
+    print("heat", r[1], r[2])
+    r = run_traced("cant3d_12x6x6.npz", {0, 1, 11},
+                   nelx=12, nely=6, nelz=6, volfrac=0.3, rmin=1.5, ft=1,
+                   bcs=cantilever_3d, nouteriter=12)
+    print("cant3d", r[1], r[2])
+
+
+if __name__ == "__main__":
+    main()

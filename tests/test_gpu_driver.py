@@ -1,0 +1,118 @@
+"""The drop-in driver on the GPU against the reference's own trajectories
+(fixtures made by running the reference, tests/golden/make_golden.py) and the
+reference test suite's golden compliance values (tests/test_compliance.py)."""
+import numpy as np
+import pytest
+
+from oracle import topopt as O
+
+pytestmark = pytest.mark.gpu
+
+OUT = {"file": None, "display": False, "export": False, "write_log": False,
+       "profile": False, "debug": 0}
+
+
+def test_mbb_density_filter_full_run(gpu_lib, golden):
+    """tests/test_compliance.py:10 -- 233.71457 at decimal=5, plus the whole
+    144-iteration trajectory and final design within 1e-8."""
+    from topoptlab_gb300 import main
+    from topoptlab_gb300.example_bc import mbb_2d
+    g = golden("mbb2d_60x20.npz")
+    x, obj = main(nelx=60, nely=20, volfrac=0.5, rmin=2.4, ft=1, filter_mode="matrix",
+                  optimizer="oc", bcs=mbb_2d, lin_solver_kw={"name": "scipy-direct"},
+                  output_kw=dict(OUT))
+    np.testing.assert_almost_equal(obj, 233.71457, decimal=5)
+    np.testing.assert_allclose(obj, float(g["final_obj"]), rtol=1e-8)
+    np.testing.assert_allclose(x[:, 0], g["final_x"], atol=1e-8)
+
+
+def test_mbb_sensitivity_filter(gpu_lib, golden):
+    """tests/test_compliance.py:9 -- 216.81366 (ft=0)."""
+    from topoptlab_gb300 import main
+    from topoptlab_gb300.example_bc import mbb_2d
+    g = golden("mbb2d_60x20_ft0.npz")
+    x, obj = main(nelx=60, nely=20, volfrac=0.5, rmin=2.4, ft=0, optimizer="oc", bcs=mbb_2d,
+                  lin_solver_kw={"name": "scipy-direct"}, output_kw=dict(OUT))
+    np.testing.assert_almost_equal(obj, 216.81366, decimal=5)
+    np.testing.assert_allclose(x[:, 0], g["final_x"], atol=1e-7)
+
+
+def test_heat_plate(gpu_lib, golden):
+    """tests/test_compliance.py:92 -- 473.7336997084 at decimal=3."""
+    from topoptlab_gb300 import main
+    from topoptlab_gb300.example_bc import heatplate_2d
+    from topoptlab_gb300.elements import lk_poisson_2d
+    g = golden("heat2d_40x40.npz")
+    x, obj = main(nelx=40, nely=40, volfrac=0.4, rmin=1.2, ft=0, optimizer="oc",
+                  bcs=heatplate_2d, lk=lk_poisson_2d, lin_solver_kw={"name": "scipy-direct"},
+                  output_kw=dict(OUT))
+    np.testing.assert_almost_equal(obj, 473.7336997084, decimal=3)
+    np.testing.assert_allclose(obj, float(g["final_obj"]), rtol=1e-8)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_cantilever_3d_trajectory(gpu_lib, golden, precision):
+    """3-D cantilever (reference callable semantics), 12 iterations: compliance
+    per iteration and final design within 1e-8 of the reference run."""
+    from topoptlab_gb300.context import GpuProblem
+    from topoptlab_gb300.elements import lk_linear_elast_3d
+    g = golden("cant3d_12x6x6.npz")
+    fixed, f = O.bc_cantilever_3d(12, 6, 6)
+    prob = GpuProblem(12, 6, 6, lk_linear_elast_3d(), fixed, f, 0.3, 1.5, ft=1, rtol=1e-12,
+                      precision=precision)
+    try:
+        objs = [prob.step().obj for _ in range(12)]
+        x = prob.get(0)
+    finally:
+        prob.close()
+    np.testing.assert_allclose(objs, g["obj"], rtol=1e-8)
+    np.testing.assert_allclose(x, g["final_x"], atol=1e-8)
+
+
+def test_teacher_forced_iteration(gpu_lib, golden):
+    """Per-iteration parity: start from the reference's state at iteration 24
+    (xPhys, x, g) and compare u, obj and the OC output of that iteration."""
+    from topoptlab_gb300.context import GpuProblem
+    from topoptlab_gb300.elements import lk_linear_elast_2d
+    from topoptlab_gb300 import _lib
+    g = golden("mbb2d_60x20.npz")
+    fixed, f = O.bc_mbb_2d(60, 20)
+    prob = GpuProblem(60, 20, None, lk_linear_elast_2d(), fixed, f, 0.5, 2.4, ft=1, rtol=1e-12)
+    try:
+        u, info = prob.solve(g["xPhys_24"], f)
+        np.testing.assert_allclose(u, g["u_24"], rtol=0, atol=1e-9 * np.abs(g["u_24"]).max())
+        obj, dc = prob.compliance(g["xPhys_24"], u)
+        np.testing.assert_allclose(obj, g["obj"][24], rtol=1e-9)
+    finally:
+        prob.close()
+
+
+def test_nonconvergence_raises(gpu_lib):
+    """A PCG iteration cap that cannot be met surfaces as RuntimeError, like
+    solve_linsystem.py:349-351 (failure made on the host: maxiter=1)."""
+    from topoptlab_gb300.context import GpuProblem
+    from topoptlab_gb300.elements import lk_linear_elast_2d
+    fixed, f = O.bc_mbb_2d(32, 16)
+    prob = GpuProblem(32, 16, None, lk_linear_elast_2d(), fixed, f, 0.5, 1.5, maxiter=1,
+                      rtol=1e-12)
+    try:
+        with pytest.raises(RuntimeError, match="did not converge"):
+            prob.step()
+    finally:
+        prob.close()
+
+
+def test_nan_density_raises(gpu_lib):
+    from topoptlab_gb300.context import GpuProblem
+    from topoptlab_gb300.elements import lk_linear_elast_2d
+    from topoptlab_gb300 import _lib
+    fixed, f = O.bc_mbb_2d(16, 8)
+    prob = GpuProblem(16, 8, None, lk_linear_elast_2d(), fixed, f, 0.5, 1.5)
+    try:
+        x = np.full(16 * 8, 0.5)
+        x[3] = np.nan
+        prob.set(_lib.TG_FIELD_XPHYS, x)
+        with pytest.raises(RuntimeError):
+            prob.step()
+    finally:
+        prob.close()

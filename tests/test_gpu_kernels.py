@@ -1,0 +1,245 @@
+"""GPU kernels against the CPU oracle, through the C ABI.
+
+Tolerances: index work bit-exact; FP64 kernels within 1e-12 relative of the
+oracle (summation order differs); FP32 kernels within 1e-5 relative."""
+import numpy as np
+import pytest
+
+from oracle import topopt as O
+from oracle import gmg as G
+
+pytestmark = pytest.mark.gpu
+
+CASES = [
+    # (nelx, nely, nelz, kind)
+    (12, 6, None, "elast"), (9, 7, None, "elast"), (10, 6, None, "poisson"),
+    (6, 4, 4, "elast"), (5, 3, 4, "elast"), (8, 6, 4, "poisson"), (20, 10, 10, "elast"),
+]
+
+
+def _setup(nelx, nely, nelz, kind, rng, **kw):
+    from topoptlab_gb300.context import GpuProblem
+    ndim = 2 if nelz is None else 3
+    KE = O.ke_elast(ndim) if kind == "elast" else O.ke_poisson(ndim)
+    nnd = ndim if kind == "elast" else 1
+    dims = (nelx, nely) if ndim == 2 else (nelx, nely, nelz)
+    nel = int(np.prod(dims))
+    ndof = nnd * int(np.prod(np.array(dims) + 1))
+    if kind == "elast" and ndim == 2:
+        fixed, f = O.bc_mbb_2d(nelx, nely)
+    elif kind == "elast":
+        fixed, f = O.bc_cantilever_3d(nelx, nely, nelz)
+    else:
+        fixed = np.arange(0, nely + 1)
+        f = np.full(ndof, 0.01)
+    prob = GpuProblem(nelx, nely, nelz, KE, fixed, f, 0.5, 1.5, **kw)
+    x = rng.uniform(0.05, 1.0, nel)
+    return prob, KE, fixed, f, x, ndof
+
+
+def test_edofmat_bit_exact(gpu_lib, golden):
+    from topoptlab_gb300.elements import create_edofMat
+    d = golden("elements.npz")
+    for k in d.files:
+        if k.startswith("edof2d"):
+            _, dims, nd = k.split("_")
+            nx, ny = map(int, dims.split("x"))
+            np.testing.assert_array_equal(create_edofMat(nx, ny, None, int(nd))[0], d[k])
+        elif k.startswith("edof3d"):
+            _, dims, nd = k.split("_")
+            nx, ny, nz = map(int, dims.split("x"))
+            np.testing.assert_array_equal(create_edofMat(nx, ny, nz, int(nd))[0], d[k])
+    # a large grid against the oracle
+    e, *_ = create_edofMat(40, 20, 10, 3)
+    np.testing.assert_array_equal(e, O.edofmat(40, 20, 10, 3))
+
+
+@pytest.mark.parametrize("nelx,nely,nelz,kind", CASES)
+def test_kmul_fp64(gpu_lib, nelx, nely, nelz, kind):
+    rng = np.random.default_rng(1)
+    prob, KE, fixed, f, x, ndof = _setup(nelx, nely, nelz, kind, rng)
+    try:
+        u = rng.standard_normal(ndof)
+        y = prob.kmul(x, u)
+    finally:
+        prob.close()
+    edof = O.edofmat(nelx, nely, nelz, KE.shape[0] // (4 if nelz is None else 8))
+    K = O.assemble(KE, edof, O.simp(x), ndof)
+    m = np.ones(ndof)
+    m[fixed] = 0.0
+    yref = m * (K @ (m * u))
+    np.testing.assert_allclose(y, yref, rtol=0, atol=1e-13 * np.abs(yref).max())
+
+
+@pytest.mark.parametrize("nelx,nely,nelz,kind", CASES[:4])
+def test_kmul_fp32(gpu_lib, nelx, nely, nelz, kind):
+    rng = np.random.default_rng(2)
+    prob, KE, fixed, f, x, ndof = _setup(nelx, nely, nelz, kind, rng, precision="mixed")
+    try:
+        u = rng.standard_normal(ndof)
+        y = prob.kmul(x, u, precision="mixed")
+    finally:
+        prob.close()
+    edof = O.edofmat(nelx, nely, nelz, KE.shape[0] // (4 if nelz is None else 8))
+    K = O.assemble(KE, edof, O.simp(x), ndof)
+    m = np.ones(ndof)
+    m[fixed] = 0.0
+    yref = m * (K @ (m * u))
+    np.testing.assert_allclose(y, yref, rtol=0, atol=1e-5 * np.abs(yref).max())
+
+
+@pytest.mark.parametrize("nelx,nely,nelz,rmin", [(7, 5, None, 2.4), (9, 6, None, 1.5),
+                                                 (6, 5, 4, 1.5), (5, 4, 3, 2.4), (60, 20, None, 2.4)])
+def test_filter_modes(gpu_lib, nelx, nely, nelz, rmin):
+    rng = np.random.default_rng(3)
+    ndim = 2 if nelz is None else 3
+    prob, KE, fixed, f, x, ndof = _setup(nelx, nely, nelz, "elast", rng)
+    prob.close()
+    from topoptlab_gb300.context import GpuProblem
+    prob = GpuProblem(nelx, nely, nelz, KE, fixed, f, 0.5, rmin)
+    try:
+        H, Hs = O.filter_matrix(nelx, nely, nelz, rmin)
+        d = -rng.uniform(0.1, 1.0, x.shape[0])
+        np.testing.assert_allclose(prob.filter(None, 3), Hs, rtol=1e-14)
+        np.testing.assert_allclose(prob.filter(x, 0), (H @ x) / Hs, rtol=1e-13)
+        np.testing.assert_allclose(prob.filter(d, 1), H @ (d / Hs), rtol=1e-13)
+        np.testing.assert_allclose(prob.filter(x, 2, d), (H @ (x * d)) / Hs / np.maximum(0.001, x),
+                                   rtol=1e-13)
+    finally:
+        prob.close()
+
+
+@pytest.mark.parametrize("nelx,nely,nelz,kind", CASES)
+def test_compliance_and_sensitivity(gpu_lib, nelx, nely, nelz, kind):
+    rng = np.random.default_rng(4)
+    prob, KE, fixed, f, x, ndof = _setup(nelx, nely, nelz, kind, rng)
+    try:
+        u = rng.standard_normal(ndof)
+        u[fixed] = 0.0
+        obj, dc = prob.compliance(x, u)
+    finally:
+        prob.close()
+    edof = O.edofmat(nelx, nely, nelz, KE.shape[0] // (4 if nelz is None else 8))
+    obj_ref, dc_ref, _ = O.compliance_sens(x, u, KE, edof)
+    np.testing.assert_allclose(obj, obj_ref, rtol=1e-12)
+    np.testing.assert_allclose(dc, dc_ref, rtol=1e-11, atol=1e-13 * np.abs(dc_ref).max())
+
+
+def test_oc_against_reference_steps(gpu_lib, golden):
+    from topoptlab_gb300.optimizer import oc_top88
+    g = golden("mbb2d_60x20.npz")
+    for k in (0, 1, 2, 24, 143):
+        xnew, gt = oc_top88(g[f"x_in_{k}"], 0.5, g[f"dc_{k}"], g[f"dv_{k}"], float(g[f"g_in_{k}"]))
+        np.testing.assert_allclose(xnew, g[f"x_out_{k}"], atol=1e-13)
+        np.testing.assert_allclose(gt, g["g"][k], rtol=1e-9, atol=1e-12)
+
+
+def test_oc_passive_active_flags(gpu_lib):
+    from topoptlab_gb300.optimizer import oc_top88
+    rng = np.random.default_rng(5)
+    n = 5000
+    x = rng.uniform(0.1, 0.9, n)
+    dc = -rng.uniform(0.1, 2.0, n)
+    dv = np.ones(n)
+    flags = rng.integers(0, 3, n).astype(np.int8)
+    xnew, gt = oc_top88(x, 0.5, dc, dv, 0.0, el_flags=flags)
+    assert np.all(xnew[flags == 1] == 0.0) and np.all(xnew[flags == 2] == 1.0)
+    # oracle with the same flag rule (optimality_criterion.py:69-71)
+    l1, l2 = 0.0, 1e9
+    xr = np.zeros(n)
+    while (l2 - l1) / (l1 + l2) > 1e-3:
+        lmid = 0.5 * (l2 + l1)
+        xr[:] = np.maximum(0.0, np.maximum(x - 0.2, np.minimum(1.0, np.minimum(x + 0.2, x * np.sqrt(-dc / dv / lmid)))))
+        xr[flags == 1] = 0
+        xr[flags == 2] = 1
+        gtr = np.sum(dv * (xr - x))
+        if gtr > 0:
+            l1 = lmid
+        else:
+            l2 = lmid
+    np.testing.assert_allclose(xnew, xr, atol=1e-13)
+
+
+@pytest.mark.parametrize("nelx,nely,nelz,kind", [(12, 8, None, "elast"), (16, 8, None, "poisson"),
+                                                 (8, 4, 4, "elast"), (16, 8, 8, "elast")])
+def test_coarse_operators_are_galerkin(gpu_lib, nelx, nely, nelz, kind):
+    rng = np.random.default_rng(6)
+    prob, KE, fixed, f, x, ndof = _setup(nelx, nely, nelz, kind, rng, nlevels=3)
+    ndim = 2 if nelz is None else 3
+    dims = (nelx, nely) if ndim == 2 else (nelx, nely, nelz)
+    nnd = KE.shape[0] // 2 ** ndim
+    edof = O.edofmat(nelx, nely, nelz, nnd)
+    K = O.assemble(KE, edof, O.simp(x), ndof)
+    mask = np.zeros(ndof, bool)
+    mask[fixed] = True
+    h = G.Hierarchy(K, mask, dims, nnd, 3)
+    try:
+        for lvl in (1, 2):
+            st = prob.coarse_stencil(x, lvl)
+            A = h.A[lvl].toarray()
+            Ad = _stencil_to_dense(st, h.dims[lvl], nnd)
+            np.testing.assert_allclose(Ad, A, rtol=0, atol=1e-12 * np.abs(A).max())
+    finally:
+        prob.close()
+
+
+def _stencil_to_dense(st, dims, nnd):
+    ndim = len(dims)
+    nn = [d + 1 for d in dims]
+    nnodes = int(np.prod(nn))
+    ndir = 3 ** ndim
+    S = st.reshape(ndir, nnd, nnd, nnodes)
+    A = np.zeros((nnodes * nnd, nnodes * nnd))
+    for n in range(nnodes):
+        y = n % nn[1]
+        xx = (n // nn[1]) % nn[0]
+        z = n // (nn[1] * nn[0]) if ndim == 3 else 0
+        for d in range(ndir):
+            dy, dx = d % 3 - 1, (d // 3) % 3 - 1
+            dz = d // 9 - 1 if ndim == 3 else 0
+            X, Y, Z = xx + dx, y + dy, z + dz
+            if not (0 <= X < nn[0] and 0 <= Y < nn[1] and (ndim == 2 or 0 <= Z < nn[2])):
+                continue
+            m = (Z * nn[0] + X) * nn[1] + Y
+            A[n * nnd:(n + 1) * nnd, m * nnd:(m + 1) * nnd] = S[d, :, :, n]
+    return A
+
+
+@pytest.mark.parametrize("nelx,nely,nelz,kind", [(12, 8, None, "elast"), (16, 16, None, "poisson"),
+                                                 (8, 4, 4, "elast"), (16, 8, 8, "elast")])
+def test_vcycle_matches_oracle(gpu_lib, nelx, nely, nelz, kind):
+    rng = np.random.default_rng(7)
+    prob, KE, fixed, f, x, ndof = _setup(nelx, nely, nelz, kind, rng, nlevels=3)
+    ndim = 2 if nelz is None else 3
+    dims = (nelx, nely) if ndim == 2 else (nelx, nely, nelz)
+    nnd = KE.shape[0] // 2 ** ndim
+    K = O.assemble(KE, O.edofmat(nelx, nely, nelz, nnd), O.simp(x), ndof)
+    mask = np.zeros(ndof, bool)
+    mask[fixed] = True
+    h = G.Hierarchy(K, mask, dims, nnd, 3, omega=0.6, nsmooth=2)
+    b = rng.standard_normal(ndof) * ~mask
+    try:
+        z = prob.vcycle(x, b)
+    finally:
+        prob.close()
+    zr = h.vcycle(b)
+    np.testing.assert_allclose(z, zr, rtol=0, atol=1e-10 * np.abs(zr).max())
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("nelx,nely,nelz,kind", [(32, 16, None, "elast"), (32, 32, None, "poisson"),
+                                                 (16, 8, 8, "elast")])
+def test_solve_reaches_direct_solution(gpu_lib, precision, nelx, nely, nelz, kind):
+    rng = np.random.default_rng(8)
+    prob, KE, fixed, f, x, ndof = _setup(nelx, nely, nelz, kind, rng, precision=precision,
+                                         rtol=1e-10)
+    try:
+        u, info = prob.solve(x, f)
+    finally:
+        prob.close()
+    assert info["converged"] == 1 and info["rel_res"] < 1e-10
+    nnd = KE.shape[0] // (4 if nelz is None else 8)
+    K = O.assemble(KE, O.edofmat(nelx, nely, nelz, nnd), O.simp(x), ndof)
+    free = np.setdiff1d(np.arange(ndof), fixed)
+    ud = O.solve_direct(K, f, free)
+    np.testing.assert_allclose(u, ud, rtol=0, atol=1e-7 * np.abs(ud).max())

@@ -1,0 +1,89 @@
+"""Host-side logic of the package that needs no GPU: element matrices,
+boundary-condition callables, option mapping, the C-ABI library's exports."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from topoptlab_gb300 import elements as E
+from topoptlab_gb300 import example_bc as B
+from topoptlab_gb300.topology_optimization import solver_options, main
+from topoptlab_gb300 import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_element_matrices_match_reference(golden):
+    d = golden("elements.npz")
+    np.testing.assert_allclose(E.lk_linear_elast_2d(l=np.array([1., 1.])), d["KE_elast2d"], atol=1e-15)
+    np.testing.assert_allclose(E.lk_linear_elast_3d(l=np.array([1., 1., 1.])), d["KE_elast3d"], atol=1e-15)
+    np.testing.assert_allclose(E.lk_poisson_2d(l=np.array([1., 1.])), d["KE_poisson2d"], atol=1e-15)
+    np.testing.assert_allclose(E.lk_poisson_3d(l=np.array([1., 1., 1.])), d["KE_poisson3d"], atol=1e-15)
+    np.testing.assert_allclose(E.lk_linear_elast_2d(l=np.array([2., 1.])), d["KE_elast2d_rect"], atol=1e-15)
+    np.testing.assert_allclose(E.lk_linear_elast_3d(l=np.array([1., 2., .5])), d["KE_elast3d_rect"], atol=1e-15)
+
+
+def test_bc_callables_match_reference(golden):
+    d = golden("elements.npz")
+    for nx, ny in [(60, 20), (10, 4)]:
+        u, f, fixed, free, springs = B.mbb_2d(nx, ny, 2 * (nx + 1) * (ny + 1))
+        np.testing.assert_array_equal(fixed, d[f"bc_mbb2d_{nx}x{ny}_fixed"])
+        np.testing.assert_array_equal(f[:, 0], d[f"bc_mbb2d_{nx}x{ny}_f"])
+        assert springs is None and len(free) + len(fixed) == u.shape[0]
+    for nx, ny, nz in [(12, 6, 6), (16, 8, 8)]:
+        u, f, fixed, free, _ = B.cantilever_3d(nx, ny, nz, 3 * (nx + 1) * (ny + 1) * (nz + 1))
+        np.testing.assert_array_equal(fixed, d[f"bc_cant3d_{nx}x{ny}x{nz}_fixed"])
+        np.testing.assert_array_equal(f[:, 0], d[f"bc_cant3d_{nx}x{ny}x{nz}_f"])
+    for n in [40, 64, 100]:
+        u, f, fixed, free, _ = B.heatplate_2d(n, n, (n + 1) ** 2)
+        np.testing.assert_array_equal(fixed, d[f"bc_heat2d_{n}_fixed"])
+        np.testing.assert_array_equal(f[:, 0], d[f"bc_heat2d_{n}_f"])
+
+
+def test_solver_options_mapping():
+    o = solver_options({"name": "scipy-direct"}, {"name": None})
+    assert o["precond"] == "gb300-gmg" and o["rtol"] == 1e-12
+    o = solver_options({"name": "gb300-gmgpcg", "rtol": 1e-6},
+                       {"name": "gb300-gmg", "precision": "mixed", "nlevels": 3})
+    assert o["rtol"] == 1e-6 and o["precision"] == "mixed" and o["nlevels"] == 3
+    o = solver_options({"name": "gb300-pcg"}, {"name": "gb300-jacobi"})
+    assert o["precond"] == "gb300-jacobi"
+    with pytest.raises(ValueError):
+        solver_options({"name": "no-such-solver"}, {"name": None})
+    with pytest.raises(ValueError):
+        solver_options({"name": "gb300-gmgpcg"}, {"name": "no-such-preconditioner"})
+
+
+@pytest.mark.parametrize("kw", [dict(optimizer="mma"), dict(optimizer="oc", ft=5),
+                                dict(optimizer="oc", filter_mode="helmholtz"),
+                                dict(optimizer="oc", body_forces_kw={"density_coupled": 1}),
+                                dict(optimizer="oc", mix=0.5)])
+def test_main_rejects_unsupported_options(kw):
+    """Unsupported options fail before any device work, like the reference's
+    ValueError for unknown options (topology_optimization.py:262, :367)."""
+    with pytest.raises(ValueError):
+        main(nelx=4, nely=2, volfrac=0.5, rmin=1.5,
+             output_kw={"file": None, "display": False, "export": False, "write_log": False}, **kw)
+
+
+def _declared_symbols():
+    txt = open(os.path.join(ROOT, "include", "topopt_gb300.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(tg_[a-z_0-9]+)\s*\(", txt)))
+
+
+def test_header_and_binding_agree():
+    assert _declared_symbols() == sorted(_lib.SIGNATURES)
+
+
+def test_library_loads_and_exports_every_symbol():
+    """Build the library here (nvcc cross-compiles, no GPU needed) and check
+    that every declared entry point is exported; no compute call is made."""
+    from topoptlab_gb300 import build as b
+    path = b.build()
+    lib = ctypes.CDLL(path)
+    for name in _declared_symbols():
+        assert hasattr(lib, name), name
+    assert _lib.load().tg_abi_version() == 1

@@ -1,0 +1,126 @@
+"""Pin the CPU oracle against fixtures generated by the reference itself
+(tests/golden/make_golden.py).  CPU only."""
+import numpy as np
+import pytest
+
+from oracle import topopt as O
+from oracle import gmg as G
+
+
+def test_edofmat(golden):
+    d = golden("elements.npz")
+    for k in d.files:
+        if k.startswith("edof2d"):
+            _, dims, nd = k.split("_")
+            nx, ny = map(int, dims.split("x"))
+            np.testing.assert_array_equal(O.edofmat(nx, ny, None, int(nd)), d[k])
+        elif k.startswith("edof3d"):
+            _, dims, nd = k.split("_")
+            nx, ny, nz = map(int, dims.split("x"))
+            np.testing.assert_array_equal(O.edofmat(nx, ny, nz, int(nd)), d[k])
+
+
+def test_element_matrices(golden):
+    d = golden("elements.npz")
+    np.testing.assert_allclose(O.ke_elast(2), d["KE_elast2d"], atol=1e-15)
+    np.testing.assert_allclose(O.ke_elast(3), d["KE_elast3d"], atol=1e-15)
+    np.testing.assert_allclose(O.ke_poisson(2), d["KE_poisson2d"], atol=1e-15)
+    np.testing.assert_allclose(O.ke_poisson(3), d["KE_poisson3d"], atol=1e-15)
+    np.testing.assert_allclose(O.ke_elast(2, l=[2, 1]), d["KE_elast2d_rect"], atol=1e-15)
+    np.testing.assert_allclose(O.ke_elast(3, l=[1, 2, 0.5]), d["KE_elast3d_rect"], atol=1e-15)
+
+
+def test_filter_matrix(golden):
+    f = golden("filters.npz")
+    for key in ["7_5_None_2.4", "9_6_None_1.5", "6_5_4_1.5", "5_4_3_2.4"]:
+        a = key.split("_")
+        nz = None if a[2] == "None" else int(a[2])
+        H, Hs = O.filter_matrix(int(a[0]), int(a[1]), nz, float(a[3]))
+        np.testing.assert_allclose(H.toarray(), f["H_" + key], atol=1e-15)
+        np.testing.assert_allclose(Hs, f["Hs_" + key], rtol=1e-14)
+
+
+def test_boundary_conditions(golden):
+    d = golden("elements.npz")
+    for nx, ny in [(60, 20), (10, 4)]:
+        fixed, f = O.bc_mbb_2d(nx, ny)
+        np.testing.assert_array_equal(fixed, d[f"bc_mbb2d_{nx}x{ny}_fixed"])
+        np.testing.assert_array_equal(f, d[f"bc_mbb2d_{nx}x{ny}_f"])
+    for nx, ny, nz in [(12, 6, 6), (16, 8, 8)]:
+        fixed, f = O.bc_cantilever_3d(nx, ny, nz)
+        np.testing.assert_array_equal(fixed, d[f"bc_cant3d_{nx}x{ny}x{nz}_fixed"])
+        np.testing.assert_array_equal(f, d[f"bc_cant3d_{nx}x{ny}x{nz}_f"])
+    for n in [40, 64, 100]:
+        fixed, f = O.bc_heatplate_2d(n, n)
+        np.testing.assert_array_equal(fixed, d[f"bc_heat2d_{n}_fixed"])
+        np.testing.assert_array_equal(f, d[f"bc_heat2d_{n}_f"])
+
+
+def test_coarse_index_pins(golden):
+    """The oracle's stride-2 coarse nodes are the reference's create_coarse_inds."""
+    d = golden("elements.npz")
+    for k in d.files:
+        if not k.startswith("coarse_"):
+            continue
+        _, nx, ny, nz, nd, st = k.split("_")
+        nx, ny, nd = int(nx), int(ny), int(nd)
+        nz = None if nz == "None" else int(nz)
+        dims = (nx, ny) if nz is None else (nx, ny, nz)
+        P = G.prolongation(dims, nd)
+        # a coarse DOF's column has a single weight-1 entry at its coincident fine DOF
+        coinc = np.array([P[:, j].toarray().ravel().argmax() for j in range(P.shape[1])])
+        np.testing.assert_array_equal(coinc, d[k])
+
+
+def test_mbb_trajectory(golden):
+    """Whole 144-iteration MBB run (ft=1) against the reference's trajectory."""
+    g = golden("mbb2d_60x20.npz")
+    fixed, f = O.bc_mbb_2d(60, 20)
+    r = O.run(60, 20, None, 0.5, 2.4, 1, O.ke_elast(2), fixed, f)
+    assert len(r["obj"]) == int(g["n_iter"]) == 144
+    np.testing.assert_allclose(r["obj"], g["obj"], rtol=1e-9)
+    np.testing.assert_allclose(r["x"], g["final_x"], atol=1e-8)
+    np.testing.assert_allclose(r["final_obj"], 233.71457, atol=1e-5)   # tests/test_compliance.py:10
+
+
+def test_heat_ft0_first_iterations(golden):
+    g = golden("heat2d_40x40.npz")
+    fixed, f = O.bc_heatplate_2d(40, 40)
+    r = O.run(40, 40, None, 0.4, 1.2, 0, O.ke_poisson(2), fixed, f, nouteriter=3, record=(0, 1, 2))
+    np.testing.assert_allclose(r["obj"], g["obj"][:3], rtol=1e-10)
+    for k in (0, 1, 2):
+        np.testing.assert_allclose(r["rec"][k]["dc"], g[f"dc_{k}"], rtol=1e-9, atol=1e-14)
+        np.testing.assert_allclose(r["rec"][k]["u"], g[f"u_{k}"], rtol=1e-9, atol=1e-14)
+
+
+def test_cantilever_3d_trajectory(golden):
+    g = golden("cant3d_12x6x6.npz")
+    fixed, f = O.bc_cantilever_3d(12, 6, 6)
+    r = O.run(12, 6, 6, 0.3, 1.5, 1, O.ke_elast(3), fixed, f, nouteriter=12)
+    np.testing.assert_allclose(r["obj"], g["obj"], rtol=1e-9)
+    np.testing.assert_allclose(r["x"], g["final_x"], atol=1e-8)
+
+
+def test_oc_step_golden(golden):
+    g = golden("mbb2d_60x20.npz")
+    for k in (0, 1, 24):
+        xnew, gt, _ = O.oc_top88(g[f"x_in_{k}"], g[f"dc_{k}"], g[f"dv_{k}"], float(g[f"g_in_{k}"]))
+        np.testing.assert_allclose(xnew, g[f"x_out_{k}"], atol=1e-13)
+        np.testing.assert_allclose(gt, g["g"][k], rtol=1e-9, atol=1e-12)
+
+
+def test_gmg_pcg_matches_direct():
+    """FP64 GMG-PCG restatement reaches the direct solution (3-D cantilever)."""
+    nx, ny, nz = 8, 4, 4
+    KE = O.ke_elast(3)
+    rng = np.random.default_rng(0)
+    x = rng.uniform(0.05, 1.0, nx * ny * nz)
+    K = O.assemble(KE, O.edofmat(nx, ny, nz, 3), O.simp(x), 3 * (nx + 1) * (ny + 1) * (nz + 1))
+    fixed, f = O.bc_cantilever_3d(nx, ny, nz)
+    mask = np.zeros(K.shape[0], bool)
+    mask[fixed] = True
+    h = G.Hierarchy(K, mask, (nx, ny, nz), 3, 3)
+    u, it = G.pcg(h.A[0], f * ~mask, h.vcycle, rtol=1e-10)
+    assert it > 0
+    ud = O.solve_direct(K, f, np.setdiff1d(np.arange(K.shape[0]), fixed))
+    np.testing.assert_allclose(u, ud, atol=1e-8 * np.abs(ud).max())

@@ -1,0 +1,333 @@
+// extern "C" entry points (include/topopt_gb300.h).  Every call catches the
+// library's exceptions and turns them into a status code plus a message;
+// nothing aborts and no device code traps.
+#include <cstring>
+#include <vector>
+#include "tg_ctx.cuh"
+#include "../../include/topopt_gb300.h"
+
+struct tg_ctx {
+  tg::Ctx c;
+};
+
+namespace {
+thread_local std::string g_last_error;
+
+template <typename F>
+int32_t guarded(tg_ctx* ctx, F&& fn) {
+  try {
+    if (ctx) TG_CUDA(cudaSetDevice(ctx->c.dev));
+    fn();
+    return TG_OK;
+  } catch (const tg::Error& e) {
+    if (ctx) ctx->c.err = e.msg;
+    g_last_error = e.msg;
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    if (ctx) ctx->c.err = "host out of memory";
+    g_last_error = "host out of memory";
+    return TG_ENOMEM;
+  } catch (const std::exception& e) {
+    if (ctx) ctx->c.err = e.what();
+    g_last_error = e.what();
+    return TG_ECUDA;
+  }
+}
+
+template <typename T>
+void h2d(T* dst, const T* src, int64_t n, cudaStream_t st) {
+  TG_CUDA(cudaMemcpyAsync(dst, src, sizeof(T) * n, cudaMemcpyHostToDevice, st));
+}
+template <typename T>
+void d2h(T* dst, const T* src, int64_t n, cudaStream_t st) {
+  TG_CUDA(cudaMemcpyAsync(dst, src, sizeof(T) * n, cudaMemcpyDeviceToHost, st));
+  TG_CUDA(cudaStreamSynchronize(st));
+}
+
+double* field_ptr(tg::Ctx& c, int32_t field, int64_t& n) {
+  switch (field) {
+    case TG_FIELD_X: n = c.g.nel(); return c.x;
+    case TG_FIELD_XPHYS: n = c.g.nel(); return c.xPhys;
+    case TG_FIELD_U: n = c.g.ndofs(); return c.u;
+    case TG_FIELD_DC: n = c.g.nel(); return c.dcf;
+    case TG_FIELD_DV: n = c.g.nel(); return c.dv;
+    case TG_FIELD_F: n = c.g.ndofs(); return c.f;
+    default: throw tg::Error{TG_EINVAL, "unknown field"};
+  }
+}
+}  // namespace
+
+extern "C" {
+
+int32_t tg_abi_version(void) { return TG_ABI_VERSION; }
+
+const char* tg_last_error(const tg_ctx* ctx) {
+  if (ctx) return ctx->c.err.c_str();
+  return g_last_error.c_str();
+}
+
+int32_t tg_create(const tg_problem* prob, tg_ctx** out) {
+  if (!prob || !out) {
+    g_last_error = "tg_create: NULL argument";
+    return TG_EINVAL;
+  }
+  *out = nullptr;
+  tg_ctx* ctx = nullptr;
+  try {
+    ctx = new tg_ctx();
+  } catch (...) {
+    g_last_error = "host out of memory";
+    return TG_ENOMEM;
+  }
+  const int32_t rc = guarded(nullptr, [&] { tg::ctx_init(ctx->c, *prob); });
+  if (rc != TG_OK) {
+    delete ctx;
+    return rc;
+  }
+  *out = ctx;
+  return TG_OK;
+}
+
+void tg_destroy(tg_ctx* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->c.dev);
+  if (ctx->c.st) cudaStreamSynchronize(ctx->c.st);
+  delete ctx;
+}
+
+int32_t tg_step(tg_ctx* ctx, tg_iter_out* out) {
+  if (!ctx || !out) return TG_EINVAL;
+  return guarded(ctx, [&] { tg::ctx_step(ctx->c, *out); });
+}
+
+int32_t tg_get(tg_ctx* ctx, int32_t field, double* host, int64_t n) {
+  if (!ctx || !host) return TG_EINVAL;
+  return guarded(ctx, [&] {
+    int64_t m = 0;
+    double* p = field_ptr(ctx->c, field, m);
+    TG_REQUIRE(n == m, "tg_get: wrong element count");
+    d2h(host, p, n, ctx->c.st);
+  });
+}
+
+int32_t tg_set(tg_ctx* ctx, int32_t field, const double* host, int64_t n) {
+  if (!ctx || !host) return TG_EINVAL;
+  return guarded(ctx, [&] {
+    tg::Ctx& c = ctx->c;
+    int64_t m = 0;
+    double* p = field_ptr(c, field, m);
+    TG_REQUIRE(n == m, "tg_set: wrong element count");
+    h2d(p, host, n, c.st);
+    if (field == TG_FIELD_F || field == TG_FIELD_U)
+      tg::mask_vec_f64(c.g.nnodes(), c.g.ndof, c.op.fix, p, c.st);
+    TG_CUDA(cudaStreamSynchronize(c.st));
+  });
+}
+
+int32_t tg_kmul(tg_ctx* ctx, const double* xPhys, const double* u, double* y, int32_t precision) {
+  if (!ctx || !xPhys || !u || !y) return TG_EINVAL;
+  return guarded(ctx, [&] {
+    tg::Ctx& c = ctx->c;
+    const int64_t nel = c.g.nel(), nd = c.g.ndofs();
+    h2d(c.xnew.p, xPhys, nel, c.st);
+    h2d(c.r.p, u, nd, c.st);
+    if (precision == TG_PREC_FP64) {
+      tg::simp_scale(nel, c.xnew, c.eps, c.penal, c.s64, nullptr, nullptr, c.st);
+      tg::fine_apply<double, double>(c.op, c.s64, c.r, c.q, nullptr, nullptr, 0.0, tg::AM_Y, c.st);
+      d2h(y, c.q.p, nd, c.st);
+    } else {
+      TG_REQUIRE(c.precision == TG_PREC_MIXED, "tg_kmul: FP32 path needs a mixed-precision context");
+      tg::simp_scale(nel, c.xnew, c.eps, c.penal, nullptr, c.s32, nullptr, c.st);
+      tg::d2f(nd, c.r, c.p32, c.st);
+      tg::fine_apply<float, float>(c.op, c.s32, c.p32, c.q32, nullptr, nullptr, 0.0, tg::AM_Y, c.st);
+      std::vector<float> tmp(nd);
+      d2h(tmp.data(), c.q32.p, nd, c.st);
+      for (int64_t i = 0; i < nd; ++i) y[i] = tmp[i];
+    }
+  });
+}
+
+int32_t tg_solve(tg_ctx* ctx, const double* xPhys, const double* rhs, const double* u0, double* u,
+                 tg_solve_info* info) {
+  if (!ctx || !xPhys || !rhs || !u) return TG_EINVAL;
+  tg::Ctx& c = ctx->c;
+  const int32_t rc = guarded(ctx, [&] {
+    const int64_t nel = c.g.nel(), nd = c.g.ndofs();
+    h2d(c.xnew.p, xPhys, nel, c.st);
+    tg::set_density(c, c.xnew);
+    tg::build_hierarchy(c);
+    h2d(c.z.p, rhs, nd, c.st);
+    tg::mask_vec_f64(c.g.nnodes(), c.g.ndof, c.op.fix, c.z, c.st);
+    if (u0) h2d(c.p.p, u0, nd, c.st);
+    else TG_CUDA(cudaMemsetAsync(c.p.p, 0, sizeof(double) * nd, c.st));
+    // solve() uses r, q and the level buffers; rhs lives in z, the iterate in a
+    // dedicated copy so the PCG vectors stay free
+    std::vector<double> host(nd);
+    tg::DevBuf<double> b, x;
+    b.alloc(nd);
+    x.alloc(nd);
+    TG_CUDA(cudaMemcpyAsync(b.p, c.z.p, sizeof(double) * nd, cudaMemcpyDeviceToDevice, c.st));
+    TG_CUDA(cudaMemcpyAsync(x.p, c.p.p, sizeof(double) * nd, cudaMemcpyDeviceToDevice, c.st));
+    tg::solve(c, b, x);
+    d2h(u, x.p, nd, c.st);
+  });
+  if (info) {
+    info->iters = c.last_iters;
+    info->vcycles = c.last_vcycles;
+    info->refinements = c.last_refine;
+    info->converged = c.last_converged;
+    info->rel_res = c.last_relres;
+  }
+  return rc;
+}
+
+int32_t tg_filter(tg_ctx* ctx, const double* x, const double* d, double* y, int32_t mode) {
+  if (!ctx || !y || mode < 0 || mode > 3 || (mode != 3 && !x) || (mode == 2 && !d)) return TG_EINVAL;
+  return guarded(ctx, [&] {
+    tg::Ctx& c = ctx->c;
+    const int64_t nel = c.g.nel();
+    if (x) h2d(c.xnew.p, x, nel, c.st);
+    if (d) h2d(c.S.p, d, nel, c.st);
+    tg::filter_apply(c.g, c.fs, c.xnew, c.S, c.Hs, c.dc, mode, c.st);
+    d2h(y, c.dc.p, nel, c.st);
+  });
+}
+
+int32_t tg_compliance(tg_ctx* ctx, const double* xPhys, const double* u, double* obj, double* dc) {
+  if (!ctx || !xPhys || !u || !obj) return TG_EINVAL;
+  return guarded(ctx, [&] {
+    tg::Ctx& c = ctx->c;
+    const int64_t nel = c.g.nel(), nd = c.g.ndofs();
+    h2d(c.xnew.p, xPhys, nel, c.st);
+    h2d(c.r.p, u, nd, c.st);
+    tg::fine_compliance(c.op, c.xnew, c.r, c.eps, c.penal, c.dc, c.part, c.st);
+    tg::reduce_partials(c.part, (int)tg::red_blocks(nel), c.scal.p, false, c.st);
+    d2h(obj, c.scal.p, 1, c.st);
+    if (dc) d2h(dc, c.dc.p, nel, c.st);
+  });
+}
+
+int32_t tg_oc(tg_ctx* ctx, const double* x, const double* dc, const double* dv, double g,
+              double* xnew, double* gt, int32_t* nsteps) {
+  if (!ctx || !x || !dc || !dv || !xnew) return TG_EINVAL;
+  return guarded(ctx, [&] {
+    tg::Ctx& c = ctx->c;
+    const int64_t nel = c.g.nel();
+    tg::DevBuf<double> xd, dcd, dvd, xn;
+    xd.alloc(nel); dcd.alloc(nel); dvd.alloc(nel); xn.alloc(nel);
+    h2d(xd.p, x, nel, c.st);
+    h2d(dcd.p, dc, nel, c.st);
+    h2d(dvd.p, dv, nel, c.st);
+    tg::oc_begin(nel, dcd, dvd, c.S, c.oc, g, c.st);
+    for (int k = 0; k < 16; ++k) {
+      tg::oc_steps(nel, xd, c.S, dvd, c.flags.p, c.move, xn, c.part2, c.oc, 16, c.st);
+      d2h(c.h_oc, c.oc.p, 1, c.st);
+      if (c.h_oc->done) break;
+    }
+    if (!c.h_oc->done) throw tg::Error{TG_ENOTCONV, "OC bisection did not terminate"};
+    d2h(xnew, xn.p, nel, c.st);
+    if (gt) *gt = c.h_oc->gt;
+    if (nsteps) *nsteps = c.h_oc->nsteps;
+  });
+}
+
+int32_t tg_oc_raw(int64_t n, const double* x, const double* dc, const double* dv, double g,
+                  const int8_t* el_flags, double move, double l1, double l2, double* xnew,
+                  double* gt, int32_t* nsteps, int32_t device) {
+  if (!x || !dc || !dv || !xnew || n <= 0) return TG_EINVAL;
+  return guarded(nullptr, [&] {
+    TG_CUDA(cudaSetDevice(device));
+    cudaStream_t st = 0;
+    tg::DevBuf<double> xd, dcd, dvd, xn, S, part;
+    tg::DevBuf<int8_t> fl;
+    tg::DevBuf<tg::OCState> oc;
+    xd.alloc(n); dcd.alloc(n); dvd.alloc(n); xn.alloc(n); S.alloc(n); part.alloc(tg::RED_BLOCKS);
+    oc.alloc(1);
+    h2d(xd.p, x, n, st);
+    h2d(dcd.p, dc, n, st);
+    h2d(dvd.p, dv, n, st);
+    if (el_flags) {
+      fl.alloc(n);
+      h2d(fl.p, el_flags, n, st);
+    }
+    tg::OCState h;
+    tg::oc_begin(n, dcd, dvd, S, oc, g, st, l1, l2);
+    for (int k = 0; k < 16; ++k) {
+      tg::oc_steps(n, xd, S, dvd, fl.p, move, xn, part, oc, 16, st);
+      d2h(&h, oc.p, 1, st);
+      if (h.done) break;
+    }
+    if (!h.done) throw tg::Error{TG_ENOTCONV, "OC bisection did not terminate"};
+    d2h(xnew, xn.p, n, st);
+    if (gt) *gt = h.gt;
+    if (nsteps) *nsteps = h.nsteps;
+  });
+}
+
+int32_t tg_vcycle(tg_ctx* ctx, const double* xPhys, const double* b, double* x, int32_t precision) {
+  if (!ctx || !xPhys || !b || !x) return TG_EINVAL;
+  return guarded(ctx, [&] {
+    tg::Ctx& c = ctx->c;
+    TG_REQUIRE(c.precond == TG_PRECOND_GMG, "tg_vcycle needs a multigrid context");
+    const int64_t nel = c.g.nel(), nd = c.g.ndofs();
+    h2d(c.xnew.p, xPhys, nel, c.st);
+    tg::set_density(c, c.xnew);
+    tg::build_hierarchy(c);
+    h2d(c.r.p, b, nd, c.st);
+    tg::mask_vec_f64(c.g.nnodes(), c.g.ndof, c.op.fix, c.r, c.st);
+    if (precision == TG_PREC_FP64) {
+      tg::vcycle<double>(c, 0, c.r, c.z);
+      d2h(x, c.z.p, nd, c.st);
+    } else {
+      TG_REQUIRE(c.precision == TG_PREC_MIXED, "FP32 V-cycle needs a mixed-precision context");
+      tg::d2f(nd, c.r, c.r32, c.st);
+      tg::vcycle<float>(c, 0, c.r32, c.z32);
+      std::vector<float> tmp(nd);
+      d2h(tmp.data(), c.z32.p, nd, c.st);
+      for (int64_t i = 0; i < nd; ++i) x[i] = tmp[i];
+    }
+  });
+}
+
+int32_t tg_levels(tg_ctx* ctx, int32_t* nlevels, int64_t* ndofs) {
+  if (!ctx || !nlevels) return TG_EINVAL;
+  return guarded(ctx, [&] {
+    *nlevels = ctx->c.L;
+    if (ndofs)
+      for (int l = 0; l < ctx->c.L && l < 8; ++l) ndofs[l] = ctx->c.lv[l]->g.ndofs();
+  });
+}
+
+int32_t tg_coarse_stencil(tg_ctx* ctx, const double* xPhys, int32_t level, double* out, int64_t n) {
+  if (!ctx || !xPhys || !out) return TG_EINVAL;
+  return guarded(ctx, [&] {
+    tg::Ctx& c = ctx->c;
+    TG_REQUIRE(c.precond == TG_PRECOND_GMG, "no multigrid hierarchy");
+    TG_REQUIRE(level >= 1 && level < c.L, "level out of range");
+    tg::Level& v = *c.lv[level];
+    TG_REQUIRE(n == v.A64.n, "tg_coarse_stencil: wrong element count");
+    h2d(c.xnew.p, xPhys, c.g.nel(), c.st);
+    tg::set_density(c, c.xnew);
+    tg::build_hierarchy(c);
+    d2h(out, v.A64.p, n, c.st);
+  });
+}
+
+int32_t tg_edofmat(int32_t ndim, int32_t nelx, int32_t nely, int32_t nelz, int32_t nnode_dof,
+                   int32_t* out, int32_t device) {
+  if (!out) return TG_EINVAL;
+  return guarded(nullptr, [&] {
+    TG_REQUIRE((ndim == 2 || ndim == 3) && nelx > 0 && nely > 0 && (ndim == 2 || nelz > 0) &&
+                   nnode_dof > 0 && nnode_dof <= 3,
+               "tg_edofmat: bad arguments");
+    TG_CUDA(cudaSetDevice(device));
+    const tg::Grid g = tg::make_grid(ndim, nnode_dof, nelx, nely, nelz);
+    const int64_t n = g.nel() * (1 << ndim) * nnode_dof;
+    tg::DevBuf<int32_t> d;
+    d.alloc(n);
+    tg::edofmat(g, d, 0);
+    TG_CUDA(cudaMemcpy(out, d.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
+  });
+}
+
+}  // extern "C"

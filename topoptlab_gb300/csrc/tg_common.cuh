@@ -1,0 +1,145 @@
+// Shared definitions for the GB300 SIMP compliance library (sm_103a).
+//
+// Data layout in HBM (the reference's own numbering, so host<->device copies
+// are plain memcpys and edofMat parity is structural):
+//   node (x, y, z)    -> ((z * nnx) + x) * nny + y          (y fastest)
+//   DOF  (node, c)    -> node * ndof + c
+//   element (x, y, z) -> ((z * nex) + x) * ney + y
+// (elements/bilinear_quadrilateral.py:41-47, trilinear_hexahedron.py:45-57,
+//  filter/matrix_filter.py:178-183).  In 2-D z = 0 and nnz = nez = 1.
+//
+// Dirichlet conditions: one byte per node, bit c set when DOF c is fixed.
+// Every operator works on all DOFs with fixed rows and columns zeroed
+// (A = M K M, M the 0/1 mask of free DOFs); every vector is kept zero on
+// fixed DOFs.
+#pragma once
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+#include <string>
+
+namespace tg {
+
+struct Grid {
+  int ndim;              // 2 or 3
+  int ndof;              // DOFs per node (1, 2, 3)
+  int nex, ney, nez;     // elements per axis (nez = 1 in 2-D)
+  int nnx, nny, nnz;     // nodes per axis (nnz = 1 in 2-D)
+  __host__ __device__ int64_t nnodes() const { return (int64_t)nnx * nny * nnz; }
+  __host__ __device__ int64_t ndofs() const { return nnodes() * ndof; }
+  __host__ __device__ int64_t nel() const { return (int64_t)nex * ney * nez; }
+  __host__ __device__ int64_t node(int x, int y, int z) const {
+    return ((int64_t)z * nnx + x) * nny + y;
+  }
+  __host__ __device__ int64_t elem(int x, int y, int z) const {
+    return ((int64_t)z * nex + x) * ney + y;
+  }
+};
+
+inline Grid make_grid(int ndim, int ndof, int nex, int ney, int nez) {
+  Grid g;
+  g.ndim = ndim; g.ndof = ndof;
+  g.nex = nex; g.ney = ney; g.nez = (ndim == 3) ? nez : 1;
+  g.nnx = nex + 1; g.nny = ney + 1; g.nnz = (ndim == 3) ? nez + 1 : 1;
+  return g;
+}
+
+inline Grid coarsen(const Grid& f) {
+  return make_grid(f.ndim, f.ndof, f.nex / 2, f.ney / 2, f.ndim == 3 ? f.nez / 2 : 1);
+}
+
+// Status codes shared with the C ABI.
+enum : int {
+  OK = 0, EINVAL_ = 1, ENOTCONV = 2, ETIMEOUT = 3, ENAN = 4, ECUDA = 5, ENOMEM_ = 6
+};
+
+struct Error {
+  int code;
+  std::string msg;
+};
+
+#define TG_CUDA(call)                                                        \
+  do {                                                                       \
+    cudaError_t _e = (call);                                                 \
+    if (_e != cudaSuccess)                                                   \
+      throw ::tg::Error{::tg::ECUDA, std::string(#call) + ": " +             \
+                                         cudaGetErrorString(_e)};            \
+  } while (0)
+
+#define TG_CHECK_LAUNCH() TG_CUDA(cudaGetLastError())
+
+#define TG_REQUIRE(cond, msg)                                                \
+  do {                                                                       \
+    if (!(cond)) throw ::tg::Error{::tg::EINVAL_, (msg)};                    \
+  } while (0)
+
+__host__ __device__ inline int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// ---------------------------------------------------------------------------
+// type helpers
+// ---------------------------------------------------------------------------
+template <typename S> __device__ __forceinline__ float to_f(S v);
+template <> __device__ __forceinline__ float to_f<float>(float v) { return v; }
+template <> __device__ __forceinline__ float to_f<__nv_bfloat16>(__nv_bfloat16 v) {
+  return __bfloat162float(v);
+}
+template <typename T, typename S> __device__ __forceinline__ T load_scale(const S* p, int64_t i);
+template <> __device__ __forceinline__ double load_scale<double, double>(const double* p, int64_t i) {
+  return __ldg(p + i);
+}
+template <> __device__ __forceinline__ float load_scale<float, float>(const float* p, int64_t i) {
+  return __ldg(p + i);
+}
+template <> __device__ __forceinline__ float load_scale<float, __nv_bfloat16>(const __nv_bfloat16* p,
+                                                                            int64_t i) {
+  return __bfloat162float(p[i]);
+}
+
+// ---------------------------------------------------------------------------
+// deterministic block reductions (fixed shuffle tree, fixed partial order)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+  return v;
+}
+// result valid in thread 0; blockDim.x must be a multiple of 32, <= 1024
+__device__ inline double block_sum(double v, double* sh /* >= 32 */) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  v = warp_sum(v);
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  const int nw = blockDim.x >> 5;
+  v = (threadIdx.x < nw) ? sh[threadIdx.x] : 0.0;
+  if (w == 0) v = warp_sum(v);
+  __syncthreads();
+  return v;
+}
+__device__ inline double block_max(double v, double* sh) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  v = warp_max(v);
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  const int nw = blockDim.x >> 5;
+  v = (threadIdx.x < nw) ? sh[threadIdx.x] : -1.0e308;
+  if (w == 0) v = warp_max(v);
+  __syncthreads();
+  return v;
+}
+
+// Number of partial-sum slots used by every grid-wide reduction.  Grids that
+// reduce are launched with at most this many blocks (grid-stride loops), so
+// the summation order depends only on the problem size, never on timing.
+constexpr int RED_BLOCKS = 1216;   // 8 per SM on 152 SMs
+constexpr int RED_THREADS = 256;
+inline unsigned red_blocks(int64_t n) {
+  const int64_t b = cdiv(n, RED_THREADS);
+  return (unsigned)(b < RED_BLOCKS ? (b < 1 ? 1 : b) : RED_BLOCKS);
+}
+
+}  // namespace tg

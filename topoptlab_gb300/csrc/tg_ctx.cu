@@ -1,0 +1,581 @@
+// Problem set-up, multigrid hierarchy, PCG drivers and the design step.
+//
+// The design step follows topology_optimization.py:411-673 (OC branch):
+// scale -> solve -> compliance/sensitivity -> sensitivity filter -> OC ->
+// density filter -> change/volume.  Every array stays on the device; the
+// host reads back four scalars per step.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include "tg_ctx.cuh"
+#include "../../include/topopt_gb300.h"
+
+namespace tg {
+
+Ctx::~Ctx() {
+  for (Level* l : lv) delete l;
+  if (h_oc) cudaFreeHost(h_oc);
+  if (h_pcg) cudaFreeHost(h_pcg);
+  if (h_scal) cudaFreeHost(h_scal);
+  if (ev0) cudaEventDestroy(ev0);
+  if (ev1) cudaEventDestroy(ev1);
+  if (st) cudaStreamDestroy(st);
+}
+
+// reference local node order -> corner bits (dx | dy<<1 | dz<<2)
+static int corner_bits(int k, int ndim) {
+  static const int lx[4] = {0, 1, 1, 0}, ly[4] = {1, 1, 0, 0};
+  const int dz = (ndim == 3) ? (k >> 2) : 0;
+  return lx[k & 3] | (ly[k & 3] << 1) | (dz << 2);
+}
+
+static void setup_element(Ctx& c, const double* KEref) {
+  const int nd = c.g.ndim, nf = c.g.ndof, NC = 1 << nd, NE = NC * nf;
+  c.ne = NE;
+  // permute to corner-bit order
+  std::vector<int> perm(NE);   // bit index -> reference index
+  for (int k = 0; k < NC; ++k)
+    for (int q = 0; q < nf; ++q) perm[corner_bits(k, nd) * nf + q] = k * nf + q;
+  c.KEh.assign(NE * NE, 0.0);
+  for (int i = 0; i < NE; ++i)
+    for (int j = 0; j < NE; ++j) c.KEh[i * NE + j] = KEref[perm[i] * NE + perm[j]];
+  // sector blocks  B = H KE H / 4^nd
+  std::vector<double> B(NE * NE, 0.0);
+  auto hsign = [](int s, int d) { return (__builtin_popcount(s & d) & 1) ? -1.0 : 1.0; };
+  double bmax = 0.0;
+  for (int s = 0; s < NC; ++s)
+    for (int a = 0; a < nf; ++a)
+      for (int t = 0; t < NC; ++t)
+        for (int b = 0; b < nf; ++b) {
+          double acc = 0.0;
+          for (int d = 0; d < NC; ++d)
+            for (int e = 0; e < NC; ++e)
+              acc += hsign(s, d) * c.KEh[(d * nf + a) * NE + e * nf + b] * hsign(t, e);
+          acc /= (double)(NC * NC);
+          B[(s * nf + a) * NE + t * nf + b] = acc;
+          bmax = std::max(bmax, std::fabs(acc));
+        }
+  auto sigf = [&](int chi, int q) { return (nf == nd) ? (chi ^ (1 << q)) : chi; };
+  const bool vec_ok = (nf == nd) || (nf == 1);
+  double off = 0.0;
+  for (int s = 0; s < NC; ++s)
+    for (int a = 0; a < nf; ++a)
+      for (int t = 0; t < NC; ++t)
+        for (int b = 0; b < nf; ++b) {
+          const int chi1 = (nf == nd) ? (s ^ (1 << a)) : s;
+          const int chi2 = (nf == nd) ? (t ^ (1 << b)) : t;
+          if (chi1 != chi2) off = std::max(off, std::fabs(B[(s * nf + a) * NE + t * nf + b]));
+        }
+  c.op.sector = vec_ok && off <= 1e-12 * bmax;
+  std::memset(&c.op.B64, 0, sizeof(c.op.B64));
+  std::memset(&c.op.B32, 0, sizeof(c.op.B32));
+  if (c.op.sector)
+    for (int chi = 0; chi < NC; ++chi)
+      for (int a = 0; a < nf; ++a)
+        for (int b = 0; b < nf; ++b) {
+          const double v = B[(sigf(chi, a) * nf + a) * NE + sigf(chi, b) * nf + b];
+          c.op.B64.b[chi][a][b] = v;
+          c.op.B32.b[chi][a][b] = (float)v;
+        }
+  for (int i = 0; i < NE; ++i) c.op.KEdiag[i] = c.KEh[i * NE + i];
+  // Q_o = P_o^T KE P_o for the 2^nd child octants (level-1 Galerkin blocks)
+  std::vector<double> Qh((size_t)NC * NE * NE, 0.0);
+  auto pw = [&](int o, int p, int a) {
+    double w = 1.0;
+    for (int k = 0; k < nd; ++k) {
+      const int pos = ((o >> k) & 1) + ((p >> k) & 1);
+      const int dist = std::abs(pos - 2 * ((a >> k) & 1));
+      w *= dist == 0 ? 1.0 : (dist == 1 ? 0.5 : 0.0);
+    }
+    return w;
+  };
+  for (int o = 0; o < NC; ++o)
+    for (int a = 0; a < NC; ++a)
+      for (int b = 0; b < NC; ++b)
+        for (int ci = 0; ci < nf; ++ci)
+          for (int cj = 0; cj < nf; ++cj) {
+            double acc = 0.0;
+            for (int p = 0; p < NC; ++p) {
+              const double wp = pw(o, p, a);
+              if (wp == 0.0) continue;
+              for (int q = 0; q < NC; ++q) {
+                const double wq = pw(o, q, b);
+                if (wq == 0.0) continue;
+                acc += wp * wq * c.KEh[(p * nf + ci) * NE + q * nf + cj];
+              }
+            }
+            Qh[(size_t)o * NE * NE + (a * nf + ci) * NE + b * nf + cj] = acc;
+          }
+  c.KE64.alloc(NE * NE);
+  c.KE32.alloc(NE * NE);
+  c.Q.alloc((int64_t)NC * NE * NE);
+  std::vector<float> k32(NE * NE);
+  for (int i = 0; i < NE * NE; ++i) k32[i] = (float)c.KEh[i];
+  TG_CUDA(cudaMemcpy(c.KE64.p, c.KEh.data(), sizeof(double) * NE * NE, cudaMemcpyHostToDevice));
+  TG_CUDA(cudaMemcpy(c.KE32.p, k32.data(), sizeof(float) * NE * NE, cudaMemcpyHostToDevice));
+  TG_CUDA(cudaMemcpy(c.Q.p, Qh.data(), sizeof(double) * Qh.size(), cudaMemcpyHostToDevice));
+  c.op.KE64 = c.KE64.p;
+  c.op.KE32 = c.KE32.p;
+}
+
+static int choose_levels(const Grid& g, int requested) {
+  int L = 1;
+  Grid cur = g;
+  const int cap = requested > 0 ? requested : 12;
+  while (L < cap) {
+    const bool even = (cur.nex % 2 == 0) && (cur.ney % 2 == 0) && (cur.ndim == 2 || cur.nez % 2 == 0);
+    if (!even || cur.nex < 2 || cur.ney < 2 || (cur.ndim == 3 && cur.nez < 2)) break;
+    if (requested <= 0 && cur.ndofs() <= 1200) break;
+    cur = coarsen(cur);
+    ++L;
+  }
+  return L;
+}
+
+void ctx_init(Ctx& c, const tg_problem& p) {
+  TG_REQUIRE(p.ndim == 2 || p.ndim == 3, "ndim must be 2 or 3");
+  TG_REQUIRE(p.nnode_dof == 1 || p.nnode_dof == p.ndim,
+             "nnode_dof must be 1 (scalar) or ndim (elasticity)");
+  TG_REQUIRE(p.nelx > 0 && p.nely > 0 && (p.ndim == 2 || p.nelz > 0), "element counts must be > 0");
+  TG_REQUIRE(p.KE != nullptr && p.f != nullptr, "KE and f are required");
+  TG_REQUIRE(p.ft >= -1 && p.ft <= 1, "ft must be -1, 0 or 1");
+  TG_REQUIRE(p.precision == TG_PREC_FP64 || p.precision == TG_PREC_MIXED, "unknown precision");
+  TG_REQUIRE(p.precond == TG_PRECOND_GMG || p.precond == TG_PRECOND_JACOBI, "unknown preconditioner");
+  c.dev = p.device;
+  TG_CUDA(cudaSetDevice(c.dev));
+  TG_CUDA(cudaStreamCreateWithFlags(&c.st, cudaStreamNonBlocking));
+  TG_CUDA(cudaEventCreate(&c.ev0));
+  TG_CUDA(cudaEventCreate(&c.ev1));
+  c.g = make_grid(p.ndim, p.nnode_dof, p.nelx, p.nely, p.nelz);
+  c.volfrac = p.volfrac; c.rmin = p.rmin; c.eps = p.eps; c.penal = p.penal;
+  c.move = p.move > 0 ? p.move : 0.2;
+  c.ft = p.ft; c.precond = p.precond; c.precision = p.precision;
+  c.nsmooth = p.nsmooth > 0 ? p.nsmooth : 2;
+  c.omega = p.omega > 0 ? p.omega : 0.6;
+  c.rtol = p.rtol > 0 ? p.rtol : 1e-8;
+  c.maxiter = p.maxiter > 0 ? p.maxiter : 2000;
+  c.inner_rtol = p.inner_rtol > 0 ? p.inner_rtol : 1e-4;
+  c.learned = p.learned;
+  const Grid& g = c.g;
+  const int64_t nn = g.nnodes(), nd = g.ndofs(), nel = g.nel();
+  c.op.g = g;
+  setup_element(c, p.KE);
+
+  // fixed-DOF bits per node, and per element "touches a fixed DOF"
+  std::vector<uint8_t> fix(nn, 0);
+  for (int64_t i = 0; i < p.nfixed; ++i) {
+    const int64_t d = p.fixed[i];
+    TG_REQUIRE(d >= 0 && d < nd, "fixed DOF index out of range");
+    fix[d / g.ndof] |= (uint8_t)(1u << (d % g.ndof));
+  }
+  std::vector<uint8_t> touch(nel, 0);
+  for (int ez = 0; ez < g.nez; ++ez)
+    for (int ex = 0; ex < g.nex; ++ex)
+      for (int ey = 0; ey < g.ney; ++ey) {
+        uint8_t t = 0;
+        for (int d = 0; d < (1 << g.ndim); ++d)
+          t |= fix[g.node(ex + (d & 1), ey + ((d >> 1) & 1), g.ndim == 3 ? ez + ((d >> 2) & 1) : 0)];
+        touch[g.elem(ex, ey, ez)] = t ? 1 : 0;
+      }
+  // hierarchy grids and coarse fixed bits (coincident fine DOF)
+  c.L = (c.precond == TG_PRECOND_GMG) ? choose_levels(g, p.nlevels) : 1;
+  if (c.precond == TG_PRECOND_GMG) {
+    TG_REQUIRE(c.L >= 2, "the grid cannot be coarsened (odd element counts): use "
+                         "preconditioner gb300-jacobi or element counts divisible by 2");
+  }
+  std::vector<std::vector<uint8_t>> fixl{fix};
+  c.lv.push_back(new Level());
+  c.lv[0]->g = g;
+  for (int l = 1; l < c.L; ++l) {
+    const Grid gf = c.lv[l - 1]->g, gc = coarsen(gf);
+    std::vector<uint8_t> fc(gc.nnodes(), 0);
+    for (int z = 0; z < gc.nnz; ++z)
+      for (int x = 0; x < gc.nnx; ++x)
+        for (int y = 0; y < gc.nny; ++y)
+          fc[gc.node(x, y, z)] = fixl[l - 1][gf.node(2 * x, 2 * y, gf.ndim == 3 ? 2 * z : 0)];
+    fixl.push_back(fc);
+    c.lv.push_back(new Level());
+    c.lv[l]->g = gc;
+  }
+  if (c.precond == TG_PRECOND_GMG) {
+    const Grid gc = c.lv[c.L - 1]->g;
+    c.nc = gc.ndofs();
+    TG_REQUIRE(c.nc <= 8192, "coarsest multigrid level too large for the dense solve "
+                             "(use element counts divisible by a higher power of 2)");
+    c.ldc = cdiv(c.nc, 32) * 32;
+    c.Dc.alloc(c.ldc * c.ldc);
+    c.gjwork.alloc(32 * 32 + 32 * c.ldc);
+  }
+  const bool mixed = c.precision == TG_PREC_MIXED;
+  for (int l = 0; l < c.L; ++l) {
+    Level& v = *c.lv[l];
+    const int64_t n = v.g.ndofs();
+    v.fix.alloc(v.g.nnodes());
+    TG_CUDA(cudaMemcpy(v.fix.p, fixl[l].data(), fixl[l].size(), cudaMemcpyHostToDevice));
+    const int64_t ns = v.g.nnodes() * (g.ndim == 3 ? 27 : 9) * g.ndof * g.ndof;
+    if (l >= 1) v.A64.alloc(ns);
+    const bool last = (l == c.L - 1) && c.precond == TG_PRECOND_GMG;
+    if (!last) {
+      v.dinv64.alloc(n); v.t64.alloc(n); v.r64.alloc(n);
+      if (mixed) {
+        v.dinv32.alloc(n); v.t32.alloc(n); v.r32.alloc(n);
+        if (l >= 1) v.A32.alloc(ns);
+      }
+    }
+    if (l >= 1) {
+      v.b64.alloc(n); v.x64.alloc(n);
+      if (mixed) { v.b32.alloc(n); v.x32.alloc(n); }
+    }
+  }
+  c.op.fix = c.lv[0]->fix.p;
+  c.touch.alloc(nel);
+  TG_CUDA(cudaMemcpy(c.touch.p, touch.data(), nel, cudaMemcpyHostToDevice));
+  if (p.el_flags) {
+    c.flags.alloc(nel);
+    TG_CUDA(cudaMemcpy(c.flags.p, p.el_flags, nel, cudaMemcpyHostToDevice));
+  }
+  // vectors
+  c.f.alloc(nd); c.u.alloc(nd);
+  c.x.alloc(nel); c.xPhys.alloc(nel); c.xold.alloc(nel); c.xnew.alloc(nel);
+  c.dc.alloc(nel); c.dcf.alloc(nel); c.dv.alloc(nel); c.Hs.alloc(nel); c.S.alloc(nel);
+  c.s64.alloc(nel);
+  if (mixed) { c.s32.alloc(nel); c.s16.alloc(nel); }
+  c.part.alloc(RED_BLOCKS); c.part2.alloc(RED_BLOCKS); c.scal.alloc(8);
+  c.oc.alloc(1); c.pcg.alloc(1); c.pcg_out.alloc(1);
+  c.oc.zero(c.st); c.pcg.zero(c.st); c.pcg_out.zero(c.st);
+  c.r.alloc(nd); c.z.alloc(nd); c.p.alloc(nd); c.q.alloc(nd);
+  if (mixed) { c.r32.alloc(nd); c.z32.alloc(nd); c.p32.alloc(nd); c.q32.alloc(nd); c.d32.alloc(nd); }
+  TG_CUDA(cudaMallocHost(&c.h_oc, sizeof(OCState)));
+  TG_CUDA(cudaMallocHost(&c.h_pcg, sizeof(PCGState)));
+  TG_CUDA(cudaMallocHost(&c.h_scal, 8 * sizeof(double)));
+
+  // load (masked to the free DOFs) and its norm
+  std::vector<double> fh(p.f, p.f + nd);
+  double bb = 0.0;
+  for (int64_t i = 0; i < nd; ++i) {
+    if ((fix[i / g.ndof] >> (i % g.ndof)) & 1) fh[i] = 0.0;
+    bb += fh[i] * fh[i];
+  }
+  c.bnorm = std::sqrt(bb);
+  TG_CUDA(cudaMemcpy(c.f.p, fh.data(), sizeof(double) * nd, cudaMemcpyHostToDevice));
+  c.u.zero(c.st);
+
+  // filter stencil weights and the normaliser Hs (filter/matrix_filter.py:185-231)
+  const int R = std::max(0, (int)std::ceil(c.rmin) - 1);
+  const int W = 2 * R + 1;
+  const int nw = (g.ndim == 3) ? W * W * W : W * W;
+  std::vector<double> w(nw);
+  for (int i = 0; i < nw; ++i) {
+    const int oy = i % W - R, ox = (i / W) % W - R, oz = (g.ndim == 3) ? i / (W * W) - R : 0;
+    w[i] = std::max(0.0, c.rmin - std::sqrt((double)(ox * ox + oy * oy + oz * oz)));
+  }
+  c.fw.alloc(nw);
+  TG_CUDA(cudaMemcpy(c.fw.p, w.data(), sizeof(double) * nw, cudaMemcpyHostToDevice));
+  c.fs.R = R; c.fs.nw = nw; c.fs.w = c.fw.p;
+  filter_apply(g, c.fs, nullptr, nullptr, nullptr, c.Hs, 3, c.st);
+  // dv: ones, filtered once for the density filter (topology_optimization.py:520, :558)
+  std::vector<double> ones(nel, 1.0);
+  TG_CUDA(cudaMemcpy(c.xnew.p, ones.data(), sizeof(double) * nel, cudaMemcpyHostToDevice));
+  if (c.ft == 1) filter_apply(g, c.fs, c.xnew, nullptr, c.Hs, c.dv, 1, c.st);
+  else TG_CUDA(cudaMemcpyAsync(c.dv.p, c.xnew.p, sizeof(double) * nel, cudaMemcpyDeviceToDevice, c.st));
+  // initial design x = xPhys = volfrac (topology_optimization.py:216-219)
+  std::vector<double> x0(nel, c.volfrac);
+  TG_CUDA(cudaMemcpy(c.x.p, x0.data(), sizeof(double) * nel, cudaMemcpyHostToDevice));
+  TG_CUDA(cudaMemcpy(c.xPhys.p, x0.data(), sizeof(double) * nel, cudaMemcpyHostToDevice));
+  c.g_oc = 0.0;
+  TG_CUDA(cudaStreamSynchronize(c.st));
+}
+
+// ---------------------------------------------------------------------------
+// hierarchy
+// ---------------------------------------------------------------------------
+void set_density(Ctx& c, const double* xPhys) {
+  simp_scale(c.g.nel(), xPhys, c.eps, c.penal, c.s64, c.s32.p, c.s16.p, c.st);
+}
+
+void build_hierarchy(Ctx& c) {
+  const bool mixed = c.precision == TG_PREC_MIXED;
+  Level& f = *c.lv[0];
+  fine_dinv<double, double>(c.op, c.s64, f.dinv64, c.st);
+  if (mixed) fine_dinv<float, __nv_bfloat16>(c.op, c.s16, f.dinv32, c.st);
+  if (c.precond != TG_PRECOND_GMG) return;
+  for (int l = 1; l < c.L; ++l) {
+    Level& v = *c.lv[l];
+    if (l == 1) build_level1(c.op, c.s64, c.touch, c.Q, v.g, v.fix, v.A64, c.st);
+    else build_galerkin(c.lv[l - 1]->g, c.lv[l - 1]->A64, v.g, v.fix, v.A64, c.st);
+    if (l < c.L - 1) {
+      stencil_dinv<double>(v.g, v.fix, v.A64, v.dinv64, c.st);
+      if (mixed) {
+        d2f(v.A64.n, v.A64, v.A32, c.st);
+        stencil_dinv<float>(v.g, v.fix, v.A32, v.dinv32, c.st);
+      }
+    }
+  }
+  Level& cl = *c.lv[c.L - 1];
+  stencil_to_dense(cl.g, cl.fix, cl.A64, c.Dc, c.nc, c.ldc, c.st);
+  gj_inverse(c.Dc, c.nc, c.ldc, c.gjwork, c.st);
+}
+
+// ---------------------------------------------------------------------------
+// V-cycle (zero initial guess, nsmooth damped-Jacobi sweeps before and after)
+// ---------------------------------------------------------------------------
+template <typename T> struct LvBufs;
+template <> struct LvBufs<double> {
+  static double* dinv(Level& v) { return v.dinv64; }
+  static double* b(Level& v) { return v.b64; }
+  static double* x(Level& v) { return v.x64; }
+  static double* t(Level& v) { return v.t64; }
+  static double* r(Level& v) { return v.r64; }
+  static const double* A(Level& v) { return v.A64; }
+};
+template <> struct LvBufs<float> {
+  static float* dinv(Level& v) { return v.dinv32; }
+  static float* b(Level& v) { return v.b32; }
+  static float* x(Level& v) { return v.x32; }
+  static float* t(Level& v) { return v.t32; }
+  static float* r(Level& v) { return v.r32; }
+  static const float* A(Level& v) { return v.A32; }
+};
+
+template <typename T>
+static void level_apply(Ctx& c, int l, const T* in, T* out, const T* b, int mode) {
+  Level& v = *c.lv[l];
+  if (l == 0) {
+    if (std::is_same<T, double>::value)
+      fine_apply<double, double>(c.op, c.s64, (const double*)in, (double*)out, (const double*)b,
+                                 (const double*)LvBufs<T>::dinv(v), c.omega, mode, c.st);
+    else
+      fine_apply<float, __nv_bfloat16>(c.op, c.s16, (const float*)in, (float*)out,
+                                       (const float*)b, (const float*)LvBufs<T>::dinv(v), c.omega,
+                                       mode, c.st);
+  } else {
+    stencil_apply<T>(v.g, LvBufs<T>::A(v), in, out, b, LvBufs<T>::dinv(v), c.omega, mode, c.st);
+  }
+}
+
+template <typename T> void vcycle(Ctx& c, int l, const T* b, T* x) {
+  Level& v = *c.lv[l];
+  const int64_t n = v.g.ndofs();
+  if (l == c.L - 1) {
+    dense_apply<T>(c.Dc, c.nc, c.ldc, b, x, c.st);
+    return;
+  }
+  T* bufs[2] = {x, LvBufs<T>::t(v)};
+  int cur = 0;
+  scale_mul<T>(n, c.omega, LvBufs<T>::dinv(v), b, bufs[cur], c.st);
+  for (int s = 1; s < c.nsmooth; ++s) {
+    level_apply<T>(c, l, bufs[cur], bufs[1 - cur], b, AM_JACOBI);
+    cur = 1 - cur;
+  }
+  T* r = LvBufs<T>::r(v);
+  level_apply<T>(c, l, bufs[cur], r, b, AM_RES);
+  Level& w = *c.lv[l + 1];
+  restrict_<T>(v.g, w.g, w.fix, r, LvBufs<T>::b(w), c.st);
+  vcycle<T>(c, l + 1, LvBufs<T>::b(w), LvBufs<T>::x(w));
+  prolong_add<T>(v.g, w.g, v.fix, LvBufs<T>::x(w), bufs[cur], c.st);
+  for (int s = 0; s < c.nsmooth; ++s) {
+    level_apply<T>(c, l, bufs[cur], bufs[1 - cur], b, AM_JACOBI);
+    cur = 1 - cur;
+  }
+  if (bufs[cur] != x)
+    TG_CUDA(cudaMemcpyAsync(x, bufs[cur], sizeof(T) * n, cudaMemcpyDeviceToDevice, c.st));
+}
+template void vcycle<double>(Ctx&, int, const double*, double*);
+template void vcycle<float>(Ctx&, int, const float*, float*);
+
+template <typename T>
+static void precondition(Ctx& c, const T* r, T* z) {
+  if (c.precond == TG_PRECOND_GMG) {
+    vcycle<T>(c, 0, r, z);
+  } else {
+    scale_mul<T>(c.g.ndofs(), 1.0, LvBufs<T>::dinv(*c.lv[0]), r, z, c.st);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// solvers
+// ---------------------------------------------------------------------------
+static void read_pcg(Ctx& c, PCGState* d) {
+  TG_CUDA(cudaMemcpyAsync(c.h_pcg, d, sizeof(PCGState), cudaMemcpyDeviceToHost, c.st));
+  TG_CUDA(cudaStreamSynchronize(c.st));
+}
+
+static void check_finite(double v, const char* what) {
+  if (!std::isfinite(v)) throw Error{ENAN, std::string("non-finite value in ") + what};
+}
+
+// plain FP64 PCG (linear_solvers.py:114-134), x in/out
+static int pcg64(Ctx& c, const double* b, double* x, double tol_abs, int maxiter, bool& conv) {
+  const int64_t n = c.g.ndofs();
+  fine_apply<double, double>(c.op, c.s64, x, c.r, b, nullptr, 0.0, AM_RES, c.st);
+  pcg_reset(c.pcg, c.st);
+  dot<double, double>(n, c.r.p, c.r.p, c.part, c.pcg, DOT_RR, c.st);
+  read_pcg(c, c.pcg);
+  double rr = c.h_pcg->rr;
+  check_finite(rr, "PCG residual");
+  conv = std::sqrt(rr) < tol_abs;
+  int it = 0;
+  while (!conv && it < maxiter) {
+    precondition<double>(c, c.r, c.z);
+    dot<double, double>(n, c.r.p, c.z.p, c.part, c.pcg, DOT_RHO, c.st);
+    update_p<double>(n, c.z, c.p, c.pcg, c.st);
+    fine_apply<double, double>(c.op, c.s64, c.p, c.q, nullptr, nullptr, 0.0, AM_Y, c.st);
+    dot<double, double>(n, c.p.p, c.q.p, c.part, c.pcg, DOT_ALPHA, c.st);
+    update_xr<double>(n, c.p, c.q, x, c.r, c.part, c.pcg, c.st);
+    ++it;
+    read_pcg(c, c.pcg);
+    rr = c.h_pcg->rr;
+    check_finite(rr, "PCG residual");
+    conv = std::sqrt(rr) < tol_abs;
+  }
+  return it;
+}
+
+// FP32 PCG on the unit-norm residual r32 (d32 = 0 initial), FP64 dots
+static int pcg32(Ctx& c, double tol_abs, int maxiter) {
+  const int64_t n = c.g.ndofs();
+  TG_CUDA(cudaMemsetAsync(c.d32.p, 0, sizeof(float) * n, c.st));
+  pcg_reset(c.pcg, c.st);
+  int it = 0;
+  while (it < maxiter) {
+    precondition<float>(c, c.r32, c.z32);
+    dot<float, float>(n, c.r32.p, c.z32.p, c.part, c.pcg, DOT_RHO, c.st);
+    update_p<float>(n, c.z32, c.p32, c.pcg, c.st);
+    fine_apply<float, float>(c.op, c.s32, c.p32, c.q32, nullptr, nullptr, 0.0, AM_Y, c.st);
+    dot<float, float>(n, c.p32.p, c.q32.p, c.part, c.pcg, DOT_ALPHA, c.st);
+    update_xr<float>(n, c.p32, c.q32, c.d32, c.r32, c.part, c.pcg, c.st);
+    ++it;
+    read_pcg(c, c.pcg);
+    const double rr = c.h_pcg->rr;
+    check_finite(rr, "inner PCG residual");
+    if (std::sqrt(rr) < tol_abs) break;
+  }
+  return it;
+}
+
+void solve(Ctx& c, const double* b, double* u) {
+  const int64_t n = c.g.ndofs();
+  double bb;
+  {
+    pcg_reset(c.pcg_out, c.st);
+    dot<double, double>(n, b, b, c.part, c.pcg_out, DOT_BB, c.st);
+    read_pcg(c, c.pcg_out);
+    bb = c.h_pcg->bb;
+  }
+  const double bnorm = std::sqrt(bb);
+  const double tol = c.rtol * bnorm;
+  c.last_iters = c.last_vcycles = c.last_refine = 0;
+  c.last_converged = 0;
+  if (bnorm == 0.0) {
+    TG_CUDA(cudaMemsetAsync(u, 0, sizeof(double) * n, c.st));
+    c.last_converged = 1;
+    c.last_relres = 0.0;
+    return;
+  }
+  mask_vec_f64(c.g.nnodes(), c.g.ndof, c.op.fix, u, c.st);
+  if (c.precision == TG_PREC_FP64) {
+    bool conv = false;
+    const int it = pcg64(c, b, u, tol, c.maxiter, conv);
+    c.last_iters = it;
+    c.last_vcycles = (c.precond == TG_PRECOND_GMG) ? it : 0;
+    c.last_converged = conv;
+  } else {
+    // FP64 iterative refinement around the FP32 PCG
+    int total = 0;
+    bool conv = false;
+    for (int k = 0; k < 64 && total < c.maxiter; ++k) {
+      fine_apply<double, double>(c.op, c.s64, u, c.r, b, nullptr, 0.0, AM_RES, c.st);
+      pcg_reset(c.pcg_out, c.st);
+      dot<double, double>(n, c.r.p, c.r.p, c.part, c.pcg_out, DOT_RR, c.st);
+      read_pcg(c, c.pcg_out);
+      const double rr = c.h_pcg->rr;
+      check_finite(rr, "FP64 residual");
+      if (std::sqrt(rr) < tol) {
+        conv = true;
+        break;
+      }
+      to_unit_f32(n, c.r, c.pcg_out, c.r32, c.st);
+      const double inner = std::max(c.inner_rtol, 0.5 * tol / std::sqrt(rr));
+      total += pcg32(c, inner, c.maxiter - total);
+      add_scaled_f32(n, c.d32, c.pcg_out, u, c.st);
+      c.last_refine = k + 1;
+    }
+    c.last_iters = total;
+    c.last_vcycles = (c.precond == TG_PRECOND_GMG) ? total : 0;
+    c.last_converged = conv;
+  }
+  // true FP64 residual
+  fine_apply<double, double>(c.op, c.s64, u, c.r, b, nullptr, 0.0, AM_RES, c.st);
+  pcg_reset(c.pcg_out, c.st);
+  dot<double, double>(n, c.r.p, c.r.p, c.part, c.pcg_out, DOT_RR, c.st);
+  read_pcg(c, c.pcg_out);
+  c.last_relres = std::sqrt(c.h_pcg->rr) / bnorm;
+  if (!c.last_converged)
+    throw Error{ENOTCONV, "gb300 pcg iteration did not converge (iterations: " +
+                              std::to_string(c.last_iters) +
+                              ", relative residual: " + std::to_string(c.last_relres) + ")"};
+}
+
+// ---------------------------------------------------------------------------
+// one design iteration
+// ---------------------------------------------------------------------------
+void ctx_step(Ctx& c, tg_iter_out& out) {
+  const auto t0 = std::chrono::steady_clock::now();
+  const Grid& g = c.g;
+  const int64_t nel = g.nel();
+  set_density(c, c.xPhys);
+  TG_CUDA(cudaEventRecord(c.ev0, c.st));
+  build_hierarchy(c);
+  solve(c, c.f, c.u);
+  TG_CUDA(cudaEventRecord(c.ev1, c.st));
+  // compliance + raw sensitivity
+  fine_compliance(c.op, c.xPhys, c.u, c.eps, c.penal, c.dc, c.part, c.st);
+  const int nbe = (int)red_blocks(nel);
+  reduce_partials(c.part, nbe, c.scal.p + 0, false, c.st);
+  // sensitivity filter
+  if (c.ft == 1) filter_apply(g, c.fs, c.dc, nullptr, c.Hs, c.dcf, 1, c.st);
+  else if (c.ft == 0) filter_apply(g, c.fs, c.x, c.dc, c.Hs, c.dcf, 2, c.st);
+  else TG_CUDA(cudaMemcpyAsync(c.dcf.p, c.dc.p, sizeof(double) * nel, cudaMemcpyDeviceToDevice, c.st));
+  // OC
+  oc_begin(nel, c.dcf, c.dv, c.S, c.oc, c.g_oc, c.st);
+  int guard = 0;
+  for (;;) {
+    oc_steps(nel, c.x, c.S, c.dv, c.flags.p, c.move, c.xnew, c.part2, c.oc, 16, c.st);
+    TG_CUDA(cudaMemcpyAsync(c.h_oc, c.oc.p, sizeof(OCState), cudaMemcpyDeviceToHost, c.st));
+    TG_CUDA(cudaStreamSynchronize(c.st));
+    if (c.h_oc->done) break;
+    if (++guard > 16) throw Error{ENOTCONV, "OC bisection did not terminate within 256 steps"};
+  }
+  c.g_oc = c.h_oc->gt;
+  // x_old <- x ; x <- x_new
+  std::swap(c.xold.p, c.x.p);
+  std::swap(c.x.p, c.xnew.p);
+  // density filter (or copy) fused with the volume sum and max |x - x_old|
+  filter_apply_ex(g, c.fs, c.x, nullptr, c.Hs, c.xPhys, c.ft == 1 ? 0 : 4, c.xold, c.part,
+                  c.part2, c.st);
+  reduce_partials(c.part, nbe, c.scal.p + 1, false, c.st);
+  reduce_partials(c.part2, nbe, c.scal.p + 2, true, c.st);
+  TG_CUDA(cudaMemcpyAsync(c.h_scal, c.scal.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, c.st));
+  TG_CUDA(cudaStreamSynchronize(c.st));
+  const double vol_sum = c.h_scal[1];
+  float ms = 0.f;
+  TG_CUDA(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
+  out.obj = c.h_scal[0];
+  out.vol = vol_sum / (double)nel;
+  out.change = c.h_scal[2];
+  out.g = c.g_oc;
+  out.rel_res = c.last_relres;
+  out.pcg_iters = c.last_iters;
+  out.vcycles = c.last_vcycles;
+  out.refinements = c.last_refine;
+  out.oc_steps = c.h_oc->nsteps;
+  out.fallback = 0;
+  out.nlevels = c.L;
+  out.t_solve_ms = ms;
+  check_finite(out.obj, "objective");
+  c.iter++;
+  out.t_step_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+}  // namespace tg

@@ -1,0 +1,104 @@
+// Context of one optimisation problem: device buffers, multigrid hierarchy,
+// solver drivers.  Internal to the library (the ABI sees an opaque tg_ctx).
+#pragma once
+#include <vector>
+#include <string>
+#include "tg_common.cuh"
+#include "tg_ops.cuh"
+#include "tg_design.cuh"
+#include "../../include/topopt_gb300.h"
+
+namespace tg {
+
+template <typename T> struct DevBuf {
+  T* p = nullptr;
+  int64_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  void alloc(int64_t count) {
+    release();
+    if (count <= 0) return;
+    TG_CUDA(cudaMalloc(&p, sizeof(T) * count));
+    n = count;
+  }
+  void zero(cudaStream_t st) {
+    if (p) TG_CUDA(cudaMemsetAsync(p, 0, sizeof(T) * n, st));
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  ~DevBuf() { release(); }
+  operator T*() const { return p; }
+};
+
+struct Level {
+  Grid g;
+  DevBuf<uint8_t> fix;
+  DevBuf<double> A64;       // stencil (levels >= 1)
+  DevBuf<float> A32;
+  DevBuf<double> dinv64, b64, x64, t64, r64;
+  DevBuf<float> dinv32, b32, x32, t32, r32;
+};
+
+struct Ctx {
+  int dev = 0;
+  cudaStream_t st = nullptr;
+  std::string err;
+  // problem
+  Grid g;                       // fine grid (element counts in nex/ney/nez)
+  int ne = 0;                   // element matrix dim
+  double volfrac = 0.5, rmin = 1.5, eps = 1e-9, penal = 3.0, move = 0.2;
+  int ft = 1;
+  int precond = 0, precision = 0, nsmooth = 2, maxiter = 2000, learned = 0;
+  double omega = 0.6, rtol = 1e-8, inner_rtol = 1e-4;
+  double bnorm = 0.0;           // ||M f||
+  FineOp op;
+  std::vector<double> KEh;      // corner-bit order, host
+  // device: problem data
+  DevBuf<uint8_t> touch;
+  DevBuf<int8_t> flags;
+  DevBuf<double> KE64, Q;
+  DevBuf<float> KE32;
+  DevBuf<double> f, u, x, xPhys, xold, xnew, dc, dcf, dv, Hs, S, s64;
+  DevBuf<float> s32;
+  DevBuf<__nv_bfloat16> s16;
+  DevBuf<double> fw;            // filter weights
+  FilterStencil fs;
+  DevBuf<double> part, part2;   // reduction partials
+  DevBuf<double> scal;          // scalar results (obj, vol, change)
+  DevBuf<OCState> oc;
+  DevBuf<PCGState> pcg, pcg_out;
+  // PCG vectors
+  DevBuf<double> r, z, p, q;
+  DevBuf<float> r32, z32, p32, q32, d32;
+  // hierarchy
+  std::vector<Level*> lv;
+  int L = 1;
+  int64_t nc = 0, ldc = 0;
+  DevBuf<double> Dc, gjwork;
+  double g_oc = 0.0;            // OC carry
+  int iter = 0;
+  // pinned host mirrors
+  OCState* h_oc = nullptr;
+  PCGState* h_pcg = nullptr;
+  double* h_scal = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // statistics of the last solve
+  int last_iters = 0, last_vcycles = 0, last_refine = 0, last_converged = 0;
+  double last_relres = 0.0;
+
+  ~Ctx();
+};
+
+void ctx_init(Ctx& c, const ::tg_problem& p);
+void ctx_step(Ctx& c, ::tg_iter_out& out);
+void build_hierarchy(Ctx& c);     // uses c.s64 / c.s32 / c.s16 of the current xPhys
+void set_density(Ctx& c, const double* xPhys_dev);   // scale factors for xPhys
+// solve K u = b (b, u device FP64, u holds the warm start)
+void solve(Ctx& c, const double* b, double* u);
+template <typename T> void vcycle(Ctx& c, int l, const T* b, T* x);
+
+}  // namespace tg

@@ -1,0 +1,435 @@
+// Design-variable kernels: distance filter stencil, SIMP scale factors,
+// OC bisection with device-side control, deterministic reductions, PCG
+// vector updates.
+//
+// Replaces: assemble_matrix_filter + the three sparse H products per
+// iteration (filter/matrix_filter.py:101-232, topology_optimization.py:545-572,
+// :637-649), simp (material_interpolation.py:6-32), oc_top88
+// (optimizer/optimality_criterion.py:9-79), the change/volume reductions
+// (topology_optimization.py:516, :654, :670) and the PCG vector algebra
+// (linear_solvers.py:114-134).
+#include "tg_ops.cuh"
+#include "tg_design.cuh"
+
+namespace tg {
+
+// ---------------------------------------------------------------------------
+// filter: weights max(0, rmin - |d|) over |d_i| <= R; H is never formed
+// ---------------------------------------------------------------------------
+template <int NDIM, int MODE>
+__global__ void __launch_bounds__(RED_THREADS) k_filter(Grid g, int R, const double* __restrict__ w,
+                                                       const double* __restrict__ x,
+                                                       const double* __restrict__ d,
+                                                       const double* __restrict__ Hs,
+                                                       double* __restrict__ y,
+                                                       const double* __restrict__ xold,
+                                                       double* part_sum, double* part_max) {
+  __shared__ double sh[32];
+  const int64_t nel = g.nel();
+  const int W = 2 * R + 1;
+  double psum = 0.0, pmax = 0.0;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nel;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int ey = (int)(e % g.ney);
+    const int ex = (int)((e / g.ney) % g.nex);
+    const int ez = (int)(e / ((int64_t)g.ney * g.nex));
+    double acc = 0.0;
+    const int zlo = (NDIM == 3) ? -R : 0, zhi = (NDIM == 3) ? R : 0;
+    for (int oz = zlo; oz <= zhi && MODE != 4; ++oz) {
+      const int nz = ez + oz;
+      if (nz < 0 || nz >= g.nez) continue;
+      for (int ox = -R; ox <= R; ++ox) {
+        const int nx = ex + ox;
+        if (nx < 0 || nx >= g.nex) continue;
+        for (int oy = -R; oy <= R; ++oy) {
+          const int ny = ey + oy;
+          if (ny < 0 || ny >= g.ney) continue;
+          const double wt = w[((NDIM == 3 ? (oz + R) * W : 0) + (ox + R)) * W + (oy + R)];
+          const int64_t nb = g.elem(nx, ny, nz);
+          if (MODE == 0) acc += wt * x[nb];
+          else if (MODE == 1) acc += wt * (x[nb] / Hs[nb]);
+          else if (MODE == 2) acc += wt * (x[nb] * d[nb]);
+          else acc += wt;
+        }
+      }
+    }
+    double out;
+    if (MODE == 0) out = acc / Hs[e];
+    else if (MODE == 1) out = acc;
+    else if (MODE == 2) out = acc / Hs[e] / fmax(0.001, x[e]);
+    else if (MODE == 3) out = acc;
+    else out = x[e];
+    y[e] = out;
+    if (part_sum) psum += out;
+    if (xold) pmax = fmax(pmax, fabs(x[e] - xold[e]));
+  }
+  if (part_sum) {
+    const double s = block_sum(psum, sh);
+    if (threadIdx.x == 0) part_sum[blockIdx.x] = s;
+  }
+  if (xold) {
+    const double m = block_max(pmax, sh);
+    if (threadIdx.x == 0) part_max[blockIdx.x] = m;
+  }
+}
+
+void filter_apply_ex(const Grid& g, const FilterStencil& fs, const double* x, const double* d,
+                     const double* Hs, double* y, int mode, const double* xold, double* part_sum,
+                     double* part_max, cudaStream_t st) {
+  const unsigned blocks = red_blocks(g.nel());
+#define TG_F(ND, M) k_filter<ND, M><<<blocks, RED_THREADS, 0, st>>>(g, fs.R, fs.w, x, d, Hs, y, xold, part_sum, part_max)
+  if (g.ndim == 3) {
+    if (mode == 0) TG_F(3, 0); else if (mode == 1) TG_F(3, 1); else if (mode == 2) TG_F(3, 2);
+    else if (mode == 3) TG_F(3, 3); else TG_F(3, 4);
+  } else {
+    if (mode == 0) TG_F(2, 0); else if (mode == 1) TG_F(2, 1); else if (mode == 2) TG_F(2, 2);
+    else if (mode == 3) TG_F(2, 3); else TG_F(2, 4);
+  }
+#undef TG_F
+  TG_CHECK_LAUNCH();
+}
+
+void filter_apply(const Grid& g, const FilterStencil& fs, const double* x, const double* d,
+                  const double* Hs, double* y, int mode, cudaStream_t st) {
+  filter_apply_ex(g, fs, x, d, Hs, y, mode, nullptr, nullptr, nullptr, st);
+}
+
+// ---------------------------------------------------------------------------
+// SIMP scale factors eps + (1-eps) x^p in FP64 / FP32 / BF16
+// ---------------------------------------------------------------------------
+__global__ void k_simp(int64_t n, const double* __restrict__ x, double eps, double penal,
+                       double* s64, float* s32, __nv_bfloat16* s16) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double xv = x[i];
+  const double xp = (penal == 3.0) ? xv * xv * xv : pow(xv, penal);
+  const double s = eps + (1.0 - eps) * xp;
+  if (s64) s64[i] = s;
+  if (s32) s32[i] = (float)s;
+  if (s16) s16[i] = __double2bfloat16(s);
+}
+
+void simp_scale(int64_t n, const double* x, double eps, double penal, double* s64, float* s32,
+                __nv_bfloat16* s16, cudaStream_t st) {
+  k_simp<<<(unsigned)cdiv(n, 256), 256, 0, st>>>(n, x, eps, penal, s64, s32, s16);
+  TG_CHECK_LAUNCH();
+}
+
+// ---------------------------------------------------------------------------
+// deterministic finalisation of block partials (single block, fixed order)
+// ---------------------------------------------------------------------------
+__device__ double sum_partials(const double* part, int nb, double* sh) {
+  double v = 0.0;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) v += __ldcg(part + i);
+  return block_sum(v, sh);
+}
+__device__ double max_partials(const double* part, int nb, double* sh) {
+  double v = 0.0;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) v = fmax(v, __ldcg(part + i));
+  return block_max(v, sh);
+}
+
+__global__ void k_reduce_to(const double* part, int nb, double* out, int is_max) {
+  __shared__ double sh[32];
+  const double v = is_max ? max_partials(part, nb, sh) : sum_partials(part, nb, sh);
+  if (threadIdx.x == 0) *out = v;
+}
+
+void reduce_partials(const double* part, int nb, double* out, bool is_max, cudaStream_t st) {
+  k_reduce_to<<<1, RED_THREADS, 0, st>>>(part, nb, out, is_max ? 1 : 0);
+  TG_CHECK_LAUNCH();
+}
+
+// ---------------------------------------------------------------------------
+// OC bisection: each launch is one bisection step; the last block to finish
+// sums the partials in fixed order and advances (l1, l2, lmid) or sets done.
+// ---------------------------------------------------------------------------
+__global__ void k_oc_init(OCState* s, double g, double l1, double l2) {
+  s->l1 = l1;
+  s->l2 = l2;
+  s->g = g;
+  s->gt = g;
+  s->nsteps = 0;
+  s->done = ((l2 - l1) / (l1 + l2) > 1e-3) ? 0 : 1;
+  s->lmid = 0.5 * (l2 + l1);
+  s->ticket = 0;
+}
+
+__global__ void __launch_bounds__(RED_THREADS) k_oc_prep(int64_t n, const double* __restrict__ dc,
+                                                        const double* __restrict__ dv,
+                                                        double* __restrict__ S) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) S[i] = sqrt(-dc[i] / dv[i]);
+}
+
+__global__ void __launch_bounds__(RED_THREADS) k_oc_step(int64_t n, const double* __restrict__ x,
+                                                        const double* __restrict__ S,
+                                                        const double* __restrict__ dv,
+                                                        const int8_t* __restrict__ flags,
+                                                        double move, double* __restrict__ xnew,
+                                                        double* part, OCState* st) {
+  __shared__ double sh[32];
+  __shared__ int last;
+  if (st->done) return;   // uniform: written by a previous launch
+  const double lmid = st->lmid;
+  const double sc = 1.0 / sqrt(lmid);
+  double acc = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double xi = x[i];
+    double xn = fmax(0.0, fmax(xi - move, fmin(1.0, fmin(xi + move, xi * S[i] * sc))));
+    if (flags) {
+      if (flags[i] == 1) xn = 0.0;
+      else if (flags[i] == 2) xn = 1.0;
+    }
+    xnew[i] = xn;
+    acc += dv[i] * (xn - xi);
+  }
+  const double s = block_sum(acc, sh);
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = s;
+    __threadfence();
+    const unsigned t = atomicAdd(&st->ticket, 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  const double tot = sum_partials(part, gridDim.x, sh);
+  if (threadIdx.x == 0) {
+    const double gt = st->g + tot;
+    st->gt = gt;
+    if (gt > 0) st->l1 = lmid;
+    else st->l2 = lmid;
+    st->nsteps += 1;
+    const double l1 = st->l1, l2 = st->l2;
+    if ((l2 - l1) / (l1 + l2) > 1e-3) st->lmid = 0.5 * (l2 + l1);
+    else st->done = 1;
+    st->ticket = 0;
+  }
+}
+
+void oc_begin(int64_t n, const double* dc, const double* dv, double* S, OCState* st, double g,
+              cudaStream_t s, double l1, double l2) {
+  k_oc_prep<<<(unsigned)cdiv(n, RED_THREADS), RED_THREADS, 0, s>>>(n, dc, dv, S);
+  k_oc_init<<<1, 1, 0, s>>>(st, g, l1, l2);
+  TG_CHECK_LAUNCH();
+}
+void oc_steps(int64_t n, const double* x, const double* S, const double* dv, const int8_t* flags,
+              double move, double* xnew, double* part, OCState* st, int nsteps, cudaStream_t s) {
+  const unsigned blocks = red_blocks(n);
+  for (int k = 0; k < nsteps; ++k)
+    k_oc_step<<<blocks, RED_THREADS, 0, s>>>(n, x, S, dv, flags, move, xnew, part, st);
+  TG_CHECK_LAUNCH();
+}
+
+// ---------------------------------------------------------------------------
+// PCG vector algebra (scalars live in device memory)
+// ---------------------------------------------------------------------------
+template <typename TA, typename TB>
+__global__ void __launch_bounds__(RED_THREADS) k_dot(int64_t n, const TA* __restrict__ a,
+                                                    const TB* __restrict__ b, double* part,
+                                                    PCGState* st, int op) {
+  __shared__ double sh[32];
+  __shared__ int last;
+  double acc = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    acc += (double)a[i] * (double)b[i];
+  const double s = block_sum(acc, sh);
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = s;
+    __threadfence();
+    const unsigned t = atomicAdd(&st->ticket, 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  const double tot = sum_partials(part, gridDim.x, sh);
+  if (threadIdx.x == 0) {
+    if (op == DOT_RHO) {
+      st->beta = (st->iter > 0) ? tot / st->rho : 0.0;
+      st->rho = tot;
+    } else if (op == DOT_ALPHA) {
+      st->pq = tot;
+      st->alpha = st->rho / tot;
+    } else if (op == DOT_RR) {
+      st->rr = tot;
+    } else if (op == DOT_BB) {
+      st->bb = tot;
+    }
+    st->ticket = 0;
+  }
+}
+
+template <typename TA, typename TB>
+void dot(int64_t n, const TA* a, const TB* b, double* part, PCGState* st, int op, cudaStream_t s) {
+  k_dot<TA, TB><<<red_blocks(n), RED_THREADS, 0, s>>>(n, a, b, part, st, op);
+  TG_CHECK_LAUNCH();
+}
+template void dot<double, double>(int64_t, const double*, const double*, double*, PCGState*, int, cudaStream_t);
+template void dot<float, float>(int64_t, const float*, const float*, double*, PCGState*, int, cudaStream_t);
+
+template <typename T>
+__global__ void k_update_p(int64_t n, const T* __restrict__ z, T* __restrict__ p, const PCGState* st) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double beta = st->beta;
+  p[i] = (st->iter > 0) ? (T)((double)z[i] + beta * (double)p[i]) : z[i];
+}
+template <typename T>
+void update_p(int64_t n, const T* z, T* p, const PCGState* st, cudaStream_t s) {
+  k_update_p<T><<<(unsigned)cdiv(n, 256), 256, 0, s>>>(n, z, p, st);
+  TG_CHECK_LAUNCH();
+}
+template void update_p<double>(int64_t, const double*, double*, const PCGState*, cudaStream_t);
+template void update_p<float>(int64_t, const float*, float*, const PCGState*, cudaStream_t);
+
+// x += alpha p ; r -= alpha q ; rr = r.r (finalised by the last block)
+template <typename T>
+__global__ void __launch_bounds__(RED_THREADS) k_update_xr(int64_t n, const T* __restrict__ p,
+                                                          const T* __restrict__ q, T* __restrict__ x,
+                                                          T* __restrict__ r, double* part, PCGState* st) {
+  __shared__ double sh[32];
+  __shared__ int last;
+  const double alpha = st->alpha;
+  double acc = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] = (T)((double)x[i] + alpha * (double)p[i]);
+    const T ri = (T)((double)r[i] - alpha * (double)q[i]);
+    r[i] = ri;
+    acc += (double)ri * (double)ri;
+  }
+  const double s = block_sum(acc, sh);
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = s;
+    __threadfence();
+    const unsigned t = atomicAdd(&st->ticket, 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  const double tot = sum_partials(part, gridDim.x, sh);
+  if (threadIdx.x == 0) {
+    st->rr = tot;
+    st->iter += 1;
+    st->ticket = 0;
+  }
+}
+template <typename T>
+void update_xr(int64_t n, const T* p, const T* q, T* x, T* r, double* part, PCGState* st,
+               cudaStream_t s) {
+  k_update_xr<T><<<red_blocks(n), RED_THREADS, 0, s>>>(n, p, q, x, r, part, st);
+  TG_CHECK_LAUNCH();
+}
+template void update_xr<double>(int64_t, const double*, const double*, double*, double*, double*, PCGState*, cudaStream_t);
+template void update_xr<float>(int64_t, const float*, const float*, float*, float*, double*, PCGState*, cudaStream_t);
+
+__global__ void k_pcg_reset(PCGState* st) {
+  st->iter = 0;
+  st->rho = st->beta = st->alpha = st->pq = 0.0;
+  st->ticket = 0;
+}
+void pcg_reset(PCGState* st, cudaStream_t s) {
+  k_pcg_reset<<<1, 1, 0, s>>>(st);
+  TG_CHECK_LAUNCH();
+}
+
+// r32 = r64 / sqrt(rr) ;   x64 += sqrt(rr) * d32
+__global__ void k_to_unit_f32(int64_t n, const double* __restrict__ r, const PCGState* st,
+                              float* __restrict__ r32) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double inv = 1.0 / sqrt(st->rr);
+  r32[i] = (float)(r[i] * inv);
+}
+__global__ void k_add_scaled_f32(int64_t n, const float* __restrict__ d, const PCGState* st,
+                                 double* __restrict__ x) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  x[i] += sqrt(st->rr) * (double)d[i];
+}
+void to_unit_f32(int64_t n, const double* r, const PCGState* st, float* r32, cudaStream_t s) {
+  k_to_unit_f32<<<(unsigned)cdiv(n, 256), 256, 0, s>>>(n, r, st, r32);
+  TG_CHECK_LAUNCH();
+}
+void add_scaled_f32(int64_t n, const float* d, const PCGState* st, double* x, cudaStream_t s) {
+  k_add_scaled_f32<<<(unsigned)cdiv(n, 256), 256, 0, s>>>(n, d, st, x);
+  TG_CHECK_LAUNCH();
+}
+
+// ---------------------------------------------------------------------------
+// small helpers
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_scale_mul(int64_t n, double a, const T* __restrict__ d, const T* __restrict__ b,
+                            T* __restrict__ x) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) x[i] = (T)(a * (double)d[i] * (double)b[i]);
+}
+template <typename T>
+void scale_mul(int64_t n, double a, const T* d, const T* b, T* x, cudaStream_t s) {
+  k_scale_mul<T><<<(unsigned)cdiv(n, 256), 256, 0, s>>>(n, a, d, b, x);
+  TG_CHECK_LAUNCH();
+}
+template void scale_mul<double>(int64_t, double, const double*, const double*, double*, cudaStream_t);
+template void scale_mul<float>(int64_t, double, const float*, const float*, float*, cudaStream_t);
+
+__global__ void k_d2f(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (float)a[i];
+}
+void d2f(int64_t n, const double* a, float* b, cudaStream_t s) {
+  k_d2f<<<(unsigned)cdiv(n, 256), 256, 0, s>>>(n, a, b);
+  TG_CHECK_LAUNCH();
+}
+
+template <typename T>
+__global__ void k_axpby(int64_t n, double a, const T* __restrict__ x, double b, T* __restrict__ y) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) y[i] = (T)(a * (double)x[i] + b * (double)y[i]);
+}
+template <typename T>
+void axpby(int64_t n, double a, const T* x, double b, T* y, cudaStream_t st) {
+  k_axpby<T><<<(unsigned)cdiv(n, 256), 256, 0, st>>>(n, a, x, b, y);
+  TG_CHECK_LAUNCH();
+}
+template void axpby<double>(int64_t, double, const double*, double, double*, cudaStream_t);
+template void axpby<float>(int64_t, double, const float*, double, float*, cudaStream_t);
+
+__global__ void k_mask(int64_t nnodes, int ndof, const uint8_t* fix, double* v) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= nnodes * ndof) return;
+  if ((fix[i / ndof] >> (i % ndof)) & 1) v[i] = 0.0;
+}
+void mask_vec_f64(int64_t nnodes, int ndof, const uint8_t* fix, double* v, cudaStream_t st) {
+  k_mask<<<(unsigned)cdiv(nnodes * ndof, 256), 256, 0, st>>>(nnodes, ndof, fix, v);
+  TG_CHECK_LAUNCH();
+}
+
+// edofMat straight from the element coordinates (reference local node order)
+__global__ void k_edofmat(Grid g, int32_t* out) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= g.nel()) return;
+  const int ey = (int)(e % g.ney);
+  const int ex = (int)((e / g.ney) % g.nex);
+  const int ez = (int)(e / ((int64_t)g.ney * g.nex));
+  // reference local order as (dx, dy, dz): 2-D (0,1),(1,1),(1,0),(0,0);
+  // 3-D adds the same four at dz = 1
+  const int lx[4] = {0, 1, 1, 0}, ly[4] = {1, 1, 0, 0};
+  const int nc = (g.ndim == 3) ? 8 : 4;
+  const int nd = g.ndof;
+  for (int k = 0; k < nc; ++k) {
+    const int64_t n = g.node(ex + lx[k & 3], ey + ly[k & 3], ez + (k >> 2));
+    for (int c = 0; c < nd; ++c) out[e * nc * nd + k * nd + c] = (int32_t)(n * nd + c);
+  }
+}
+void edofmat(const Grid& g, int32_t* out, cudaStream_t st) {
+  k_edofmat<<<(unsigned)cdiv(g.nel(), 256), 256, 0, st>>>(g, out);
+  TG_CHECK_LAUNCH();
+}
+
+}  // namespace tg

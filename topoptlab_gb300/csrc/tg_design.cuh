@@ -1,0 +1,48 @@
+// Device-resident solver / optimiser state and the launchers of tg_design.cu.
+#pragma once
+#include "tg_common.cuh"
+#include "tg_ops.cuh"
+
+namespace tg {
+
+// OC bisection state (optimizer/optimality_criterion.py:59-77)
+struct OCState {
+  double l1, l2, lmid, g, gt;
+  int done, nsteps;
+  unsigned int ticket;
+};
+
+// PCG scalars (linear_solvers.py:114-134)
+enum DotOp : int { DOT_RHO = 0, DOT_ALPHA = 1, DOT_RR = 2, DOT_BB = 3 };
+struct PCGState {
+  double rho, beta, alpha, pq, rr, bb;
+  int iter;
+  unsigned int ticket;
+};
+
+void filter_apply_ex(const Grid& g, const FilterStencil& fs, const double* x, const double* d,
+                     const double* Hs, double* y, int mode, const double* xold, double* part_sum,
+                     double* part_max, cudaStream_t st);
+void reduce_partials(const double* part, int nb, double* out, bool is_max, cudaStream_t st);
+
+void oc_begin(int64_t n, const double* dc, const double* dv, double* S, OCState* st, double g,
+              cudaStream_t s, double l1 = 0.0, double l2 = 1e9);
+void oc_steps(int64_t n, const double* x, const double* S, const double* dv, const int8_t* flags,
+              double move, double* xnew, double* part, OCState* st, int nsteps, cudaStream_t s);
+
+template <typename TA, typename TB>
+void dot(int64_t n, const TA* a, const TB* b, double* part, PCGState* st, int op, cudaStream_t s);
+template <typename T>
+void update_p(int64_t n, const T* z, T* p, const PCGState* st, cudaStream_t s);
+template <typename T>
+void update_xr(int64_t n, const T* p, const T* q, T* x, T* r, double* part, PCGState* st,
+               cudaStream_t s);
+void pcg_reset(PCGState* st, cudaStream_t s);
+void to_unit_f32(int64_t n, const double* r, const PCGState* st, float* r32, cudaStream_t s);
+void add_scaled_f32(int64_t n, const float* d, const PCGState* st, double* x, cudaStream_t s);
+template <typename T>
+void scale_mul(int64_t n, double a, const T* d, const T* b, T* x, cudaStream_t s);
+void d2f(int64_t n, const double* a, float* b, cudaStream_t s);
+void edofmat(const Grid& g, int32_t* out, cudaStream_t st);
+
+}  // namespace tg

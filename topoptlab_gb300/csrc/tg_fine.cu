@@ -1,0 +1,393 @@
+// Fine-level matrix-free SIMP operator y = M K(rho) M u on structured quad4 /
+// hex8 grids, its inverse diagonal, and the fused compliance + sensitivity.
+//
+// Replaces the reference's per-iteration  Kes = KE*simp(xPhys)  +  COO->CSC
+// assembly + Dirichlet slicing + CSR SpMV (topology_optimization.py:419-451,
+// fem.py:141-237, linear_solvers.py:130) and the compliance / sensitivity
+// gathers (objectives.py:51-55, topology_optimization.py:491-500).
+//
+// Design (GB300): one CTA owns a brick of nodes (16 y x 8 x x 8 z in 3-D,
+// 32 x 32 in 2-D), stages the u halo in shared memory, evaluates every
+// element touching the brick and accumulates into a shared output tile in
+// 2^ndim colour passes (elements of one colour share no node), so the sum
+// order at each node is fixed: results are bit-reproducible and need no
+// atomics.  The element product uses the reflection-sector form
+// KE = H B H (Walsh-Hadamard over corner bits, B block diagonal), ~240 flops
+// per hex8 element instead of 1152: GB300's FP64 pipe is narrow, and the
+// FP64 residual is the one K.u the mixed-precision solver cannot avoid.
+#include "tg_ops.cuh"
+
+namespace tg {
+
+template <int NDIM> struct Tile;
+template <> struct Tile<3> { static constexpr int X = 8, Y = 16, Z = 8; };
+template <> struct Tile<2> { static constexpr int X = 32, Y = 32, Z = 1; };
+
+template <int NDIM, int NDOF>
+__host__ __device__ constexpr int sig(int chi, int c) {
+  return (NDOF == NDIM) ? (chi ^ (1 << c)) : chi;
+}
+
+template <int NDIM, int NDOF, typename T>
+__device__ __forceinline__ void wht(T (&v)[1 << NDIM][NDOF]) {
+#pragma unroll
+  for (int a = 0; a < NDIM; ++a)
+#pragma unroll
+    for (int d = 0; d < (1 << NDIM); ++d)
+      if (!((d >> a) & 1)) {
+        const int e = d | (1 << a);
+#pragma unroll
+        for (int c = 0; c < NDOF; ++c) {
+          const T t0 = v[d][c], t1 = v[e][c];
+          v[d][c] = t0 + t1;
+          v[e][c] = t0 - t1;
+        }
+      }
+}
+
+// y = rho * KE u  for one element, sector form.  u is destroyed.
+template <int NDIM, int NDOF, typename T>
+__device__ __forceinline__ void elem_sector(T (&u)[1 << NDIM][NDOF], const Sector<T>& B, T rho,
+                                            T (&y)[1 << NDIM][NDOF]) {
+  constexpr int NC = 1 << NDIM;
+  wht<NDIM, NDOF, T>(u);
+#pragma unroll
+  for (int c = 0; c < NDOF; ++c)
+#pragma unroll
+    for (int s = 0; s < NC; ++s) u[s][c] *= rho;
+#pragma unroll
+  for (int chi = 0; chi < NC; ++chi)
+#pragma unroll
+    for (int c = 0; c < NDOF; ++c) {
+      T acc = T(0);
+#pragma unroll
+      for (int c2 = 0; c2 < NDOF; ++c2) acc += B.b[chi][c][c2] * u[sig<NDIM, NDOF>(chi, c2)][c2];
+      y[sig<NDIM, NDOF>(chi, c)][c] = acc;
+    }
+  wht<NDIM, NDOF, T>(y);
+}
+
+template <int NDIM, int NDOF, typename T>
+__device__ __forceinline__ void elem_dense(const T (&u)[1 << NDIM][NDOF], const T* KEs, T rho,
+                                           T (&y)[1 << NDIM][NDOF]) {
+  constexpr int NE = (1 << NDIM) * NDOF;
+#pragma unroll 4
+  for (int i = 0; i < NE; ++i) {
+    T acc = T(0);
+#pragma unroll
+    for (int j = 0; j < NE; ++j) acc += KEs[i * NE + j] * u[j / NDOF][j % NDOF];
+    y[i / NDOF][i % NDOF] = rho * acc;
+  }
+}
+
+template <typename T, typename S> struct ApplyArgs {
+  Grid g;
+  const uint8_t* fix;
+  const S* scale;
+  const T* u;
+  T* y;
+  const T* b;
+  const T* dinv;
+  T omega;
+  const T* KE;      // dense path
+  Sector<T> B;
+};
+
+template <int NDIM, int NDOF, typename T, bool SECTOR>
+constexpr size_t apply_smem() {
+  using TL = Tile<NDIM>;
+  constexpr int HZ = (NDIM == 3) ? TL::Z + 2 : 1;
+  constexpr int NE = (1 << NDIM) * NDOF;
+  return sizeof(T) * ((size_t)HZ * (TL::X + 2) * (TL::Y + 2) * NDOF +
+                      (size_t)TL::Z * TL::X * TL::Y * NDOF + (SECTOR ? 0 : NE * NE));
+}
+
+template <int NDIM, int NDOF, typename T, typename S, bool SECTOR, int MODE>
+__global__ void __launch_bounds__(256) k_fine_apply(ApplyArgs<T, S> a) {
+  using TL = Tile<NDIM>;
+  constexpr int TX = TL::X, TY = TL::Y, TZ = TL::Z;
+  constexpr int HX = TX + 2, HY = TY + 2, HZ = (NDIM == 3) ? TZ + 2 : 1;
+  constexpr int NC = 1 << NDIM;
+  constexpr int NE = NC * NDOF;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* us = reinterpret_cast<T*>(smem_raw);       // [HZ][HX][HY][NDOF]
+  T* ys = us + HZ * HX * HY * NDOF;              // [TZ][TX][TY][NDOF]
+  T* KEs = ys + TZ * TX * TY * NDOF;             // dense path only
+  const Grid& g = a.g;
+  const int y0 = blockIdx.x * TY, x0 = blockIdx.y * TX, z0 = blockIdx.z * TZ;
+  const int tid = threadIdx.x, nth = blockDim.x;
+
+  // stage u (masked) with a one-node halo
+  for (int i = tid; i < HZ * HX * HY * NDOF; i += nth) {
+    const int c = i % NDOF;
+    const int hy = (i / NDOF) % HY;
+    const int hx = (i / (NDOF * HY)) % HX;
+    const int hz = i / (NDOF * HY * HX);
+    const int gx = x0 - 1 + hx, gy = y0 - 1 + hy, gz = (NDIM == 3) ? z0 - 1 + hz : 0;
+    T v = T(0);
+    if (gx >= 0 && gx < g.nnx && gy >= 0 && gy < g.nny && gz >= 0 && gz < g.nnz) {
+      const int64_t n = g.node(gx, gy, gz);
+      if (!((a.fix[n] >> c) & 1)) v = a.u[n * NDOF + c];
+    }
+    us[i] = v;
+  }
+  for (int i = tid; i < TZ * TX * TY * NDOF; i += nth) ys[i] = T(0);
+  if (!SECTOR)
+    for (int i = tid; i < NE * NE; i += nth) KEs[i] = a.KE[i];
+  __syncthreads();
+
+  // elements with local coords l in [0, T+1): global = origin - 1 + l
+#pragma unroll 1
+  for (int col = 0; col < NC; ++col) {
+    const int cx = col & 1, cy = (col >> 1) & 1, cz = (col >> 2) & 1;
+    const int nyc = (TY + 1 - cy + 1) / 2, nxc = (TX + 1 - cx + 1) / 2;
+    const int nzc = (NDIM == 3) ? (TZ + 1 - cz + 1) / 2 : 1;
+    for (int t = tid; t < nyc * nxc * nzc; t += nth) {
+      const int ly = cy + 2 * (t % nyc);
+      const int lx = cx + 2 * ((t / nyc) % nxc);
+      const int lz = (NDIM == 3) ? cz + 2 * (t / (nyc * nxc)) : 0;
+      const int ex = x0 - 1 + lx, ey = y0 - 1 + ly, ez = (NDIM == 3) ? z0 - 1 + lz : 0;
+      if (ex < 0 || ex >= g.nex || ey < 0 || ey >= g.ney || ez < 0 || ez >= g.nez) continue;
+      const T rho = load_scale<T, S>(a.scale, g.elem(ex, ey, ez));
+      T ue[NC][NDOF], ye[NC][NDOF];
+#pragma unroll
+      for (int d = 0; d < NC; ++d) {
+        const int hx = lx + (d & 1), hy = ly + ((d >> 1) & 1), hz = (NDIM == 3) ? lz + ((d >> 2) & 1) : 0;
+#pragma unroll
+        for (int c = 0; c < NDOF; ++c) ue[d][c] = us[((hz * HX + hx) * HY + hy) * NDOF + c];
+      }
+      if (SECTOR)
+        elem_sector<NDIM, NDOF, T>(ue, a.B, rho, ye);
+      else
+        elem_dense<NDIM, NDOF, T>(ue, KEs, rho, ye);
+#pragma unroll
+      for (int d = 0; d < NC; ++d) {
+        const int ox = lx + (d & 1) - 1, oy = ly + ((d >> 1) & 1) - 1;
+        const int oz = (NDIM == 3) ? lz + ((d >> 2) & 1) - 1 : 0;
+        if (ox < 0 || ox >= TX || oy < 0 || oy >= TY || oz < 0 || oz >= TZ) continue;
+#pragma unroll
+        for (int c = 0; c < NDOF; ++c) ys[((oz * TX + ox) * TY + oy) * NDOF + c] += ye[d][c];
+      }
+    }
+    __syncthreads();
+  }
+
+  // epilogue: owned nodes
+  for (int i = tid; i < TZ * TX * TY * NDOF; i += nth) {
+    const int c = i % NDOF;
+    const int oy = (i / NDOF) % TY;
+    const int ox = (i / (NDOF * TY)) % TX;
+    const int oz = i / (NDOF * TY * TX);
+    const int gx = x0 + ox, gy = y0 + oy, gz = z0 + oz;
+    if (gx >= g.nnx || gy >= g.nny || gz >= g.nnz) continue;
+    const int64_t n = g.node(gx, gy, gz);
+    const int64_t k = n * NDOF + c;
+    T out = T(0);
+    if (!((a.fix[n] >> c) & 1)) {
+      const T au = ys[i];
+      if (MODE == AM_Y) {
+        out = au;
+      } else if (MODE == AM_RES) {
+        out = a.b[k] - au;
+      } else {
+        const T uc = us[(((NDIM == 3 ? oz + 1 : 0) * HX + ox + 1) * HY + oy + 1) * NDOF + c];
+        out = uc + a.omega * a.dinv[k] * (a.b[k] - au);
+      }
+    }
+    a.y[k] = out;
+  }
+}
+
+template <int NDIM, int NDOF, typename T, typename S, bool SECTOR, int MODE>
+static void launch_apply(const ApplyArgs<T, S>& a, cudaStream_t st) {
+  using TL = Tile<NDIM>;
+  constexpr size_t smem = apply_smem<NDIM, NDOF, T, SECTOR>();
+  auto kern = k_fine_apply<NDIM, NDOF, T, S, SECTOR, MODE>;
+  static bool attr_set = false;   // per instantiation; attribute is per function
+  if (!attr_set) {
+    TG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr_set = true;
+  }
+  dim3 grid((unsigned)cdiv(a.g.nny, TL::Y), (unsigned)cdiv(a.g.nnx, TL::X),
+            (unsigned)cdiv(a.g.nnz, TL::Z));
+  kern<<<grid, 256, smem, st>>>(a);
+  TG_CHECK_LAUNCH();
+}
+
+template <int NDIM, int NDOF, typename T, typename S>
+static void dispatch_apply(const ApplyArgs<T, S>& a, bool sector, int mode, cudaStream_t st) {
+  if (sector) {
+    if (mode == AM_Y) launch_apply<NDIM, NDOF, T, S, true, AM_Y>(a, st);
+    else if (mode == AM_RES) launch_apply<NDIM, NDOF, T, S, true, AM_RES>(a, st);
+    else launch_apply<NDIM, NDOF, T, S, true, AM_JACOBI>(a, st);
+  } else {
+    if (mode == AM_Y) launch_apply<NDIM, NDOF, T, S, false, AM_Y>(a, st);
+    else if (mode == AM_RES) launch_apply<NDIM, NDOF, T, S, false, AM_RES>(a, st);
+    else launch_apply<NDIM, NDOF, T, S, false, AM_JACOBI>(a, st);
+  }
+}
+
+template <typename T> static const T* ke_ptr(const FineOp& op);
+template <> const double* ke_ptr<double>(const FineOp& op) { return op.KE64; }
+template <> const float* ke_ptr<float>(const FineOp& op) { return op.KE32; }
+template <typename T> static const Sector<T>& sec_ref(const FineOp& op);
+template <> const Sector<double>& sec_ref<double>(const FineOp& op) { return op.B64; }
+template <> const Sector<float>& sec_ref<float>(const FineOp& op) { return op.B32; }
+
+template <typename T, typename S>
+void fine_apply(const FineOp& op, const S* scale, const T* u, T* y, const T* b, const T* dinv,
+                double omega, int mode, cudaStream_t st) {
+  ApplyArgs<T, S> a;
+  a.g = op.g; a.fix = op.fix; a.scale = scale; a.u = u; a.y = y; a.b = b; a.dinv = dinv;
+  a.omega = (T)omega; a.KE = ke_ptr<T>(op); a.B = sec_ref<T>(op);
+  const int key = op.g.ndim * 10 + op.g.ndof;
+  switch (key) {
+    case 33: dispatch_apply<3, 3, T, S>(a, op.sector, mode, st); break;
+    case 31: dispatch_apply<3, 1, T, S>(a, op.sector, mode, st); break;
+    case 22: dispatch_apply<2, 2, T, S>(a, op.sector, mode, st); break;
+    case 21: dispatch_apply<2, 1, T, S>(a, op.sector, mode, st); break;
+    default: throw Error{EINVAL_, "unsupported (ndim, nnode_dof) combination"};
+  }
+}
+
+template void fine_apply<double, double>(const FineOp&, const double*, const double*, double*,
+                                         const double*, const double*, double, int, cudaStream_t);
+template void fine_apply<float, float>(const FineOp&, const float*, const float*, float*,
+                                       const float*, const float*, double, int, cudaStream_t);
+template void fine_apply<float, __nv_bfloat16>(const FineOp&, const __nv_bfloat16*, const float*,
+                                               float*, const float*, const float*, double, int,
+                                               cudaStream_t);
+
+// ---------------------------------------------------------------------------
+// inverse diagonal
+// ---------------------------------------------------------------------------
+template <int NDIM, int NDOF, typename T, typename S>
+__global__ void k_fine_dinv(Grid g, const uint8_t* fix, const S* scale, T* dinv, FineOp op) {
+  const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (n >= g.nnodes()) return;
+  const int y = (int)(n % g.nny);
+  const int x = (int)((n / g.nny) % g.nnx);
+  const int z = (int)(n / ((int64_t)g.nny * g.nnx));
+  double acc[NDOF];
+#pragma unroll
+  for (int c = 0; c < NDOF; ++c) acc[c] = 0.0;
+#pragma unroll
+  for (int d = 0; d < (1 << NDIM); ++d) {
+    const int ex = x - (d & 1), ey = y - ((d >> 1) & 1), ez = (NDIM == 3) ? z - ((d >> 2) & 1) : 0;
+    if (ex < 0 || ex >= g.nex || ey < 0 || ey >= g.ney || ez < 0 || ez >= g.nez) continue;
+    const double s = (double)load_scale<T, S>(scale, g.elem(ex, ey, ez));
+#pragma unroll
+    for (int c = 0; c < NDOF; ++c) acc[c] += s * op.KEdiag[d * NDOF + c];
+  }
+#pragma unroll
+  for (int c = 0; c < NDOF; ++c)
+    dinv[n * NDOF + c] = ((fix[n] >> c) & 1) ? T(0) : (T)(1.0 / acc[c]);
+}
+
+template <typename T, typename S>
+void fine_dinv(const FineOp& op, const S* scale, T* dinv, cudaStream_t st) {
+  const int64_t nn = op.g.nnodes();
+  const unsigned blocks = (unsigned)cdiv(nn, 256);
+  const int key = op.g.ndim * 10 + op.g.ndof;
+  switch (key) {
+    case 33: k_fine_dinv<3, 3, T, S><<<blocks, 256, 0, st>>>(op.g, op.fix, scale, dinv, op); break;
+    case 31: k_fine_dinv<3, 1, T, S><<<blocks, 256, 0, st>>>(op.g, op.fix, scale, dinv, op); break;
+    case 22: k_fine_dinv<2, 2, T, S><<<blocks, 256, 0, st>>>(op.g, op.fix, scale, dinv, op); break;
+    case 21: k_fine_dinv<2, 1, T, S><<<blocks, 256, 0, st>>>(op.g, op.fix, scale, dinv, op); break;
+    default: throw Error{EINVAL_, "unsupported (ndim, nnode_dof) combination"};
+  }
+  TG_CHECK_LAUNCH();
+}
+template void fine_dinv<double, double>(const FineOp&, const double*, double*, cudaStream_t);
+template void fine_dinv<float, float>(const FineOp&, const float*, float*, cudaStream_t);
+template void fine_dinv<float, __nv_bfloat16>(const FineOp&, const __nv_bfloat16*, float*,
+                                              cudaStream_t);
+
+// ---------------------------------------------------------------------------
+// compliance + sensitivity (FP64)
+// ---------------------------------------------------------------------------
+template <int NDIM, int NDOF, bool SECTOR>
+__global__ void __launch_bounds__(RED_THREADS) k_compliance(Grid g, const double* __restrict__ xPhys,
+                                                           const double* __restrict__ u,
+                                                           const double* __restrict__ KE,
+                                                           Sector<double> B, double eps,
+                                                           double penal, double* dc,
+                                                           double* partial) {
+  constexpr int NC = 1 << NDIM;
+  constexpr int NE = NC * NDOF;
+  __shared__ double sh[32];
+  double objp = 0.0;
+  const int64_t nel = g.nel();
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nel;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int ey = (int)(e % g.ney);
+    const int ex = (int)((e / g.ney) % g.nex);
+    const int ez = (int)(e / ((int64_t)g.ney * g.nex));
+    double ue[NC][NDOF];
+#pragma unroll
+    for (int d = 0; d < NC; ++d) {
+      const int64_t n = g.node(ex + (d & 1), ey + ((d >> 1) & 1), (NDIM == 3) ? ez + ((d >> 2) & 1) : 0);
+#pragma unroll
+      for (int c = 0; c < NDOF; ++c) ue[d][c] = __ldg(u + n * NDOF + c);
+    }
+    double ce = 0.0;
+    if (SECTOR) {
+      // u^T KE u = (H u)^T B (H u)
+      wht<NDIM, NDOF, double>(ue);
+#pragma unroll
+      for (int chi = 0; chi < NC; ++chi)
+#pragma unroll
+        for (int c = 0; c < NDOF; ++c) {
+          double acc = 0.0;
+#pragma unroll
+          for (int c2 = 0; c2 < NDOF; ++c2)
+            acc += B.b[chi][c][c2] * ue[sig<NDIM, NDOF>(chi, c2)][c2];
+          ce += acc * ue[sig<NDIM, NDOF>(chi, c)][c];
+        }
+    } else {
+      for (int i = 0; i < NE; ++i) {
+        double acc = 0.0;
+        for (int j = 0; j < NE; ++j) acc += __ldg(KE + i * NE + j) * ue[j / NDOF][j % NDOF];
+        ce += acc * ue[i / NDOF][i % NDOF];
+      }
+    }
+    const double xv = xPhys[e];
+    double xp, xpm1;
+    if (penal == 3.0) {
+      xpm1 = xv * xv;
+      xp = xpm1 * xv;
+    } else {
+      xp = pow(xv, penal);
+      xpm1 = pow(xv, penal - 1.0);
+    }
+    objp += (eps + (1.0 - eps) * xp) * ce;
+    dc[e] = -(penal * (1.0 - eps) * xpm1) * ce;
+  }
+  const double s = block_sum(objp, sh);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+
+void fine_compliance(const FineOp& op, const double* xPhys, const double* u, double eps,
+                     double penal, double* dc, double* partial, cudaStream_t st) {
+  const int64_t nel = op.g.nel();
+  const unsigned blocks = red_blocks(nel);
+  const int key = op.g.ndim * 10 + op.g.ndof;
+#define TG_COMP(ND, NF)                                                                     \
+  if (op.sector)                                                                            \
+    k_compliance<ND, NF, true><<<blocks, RED_THREADS, 0, st>>>(op.g, xPhys, u, op.KE64,      \
+                                                              op.B64, eps, penal, dc, partial); \
+  else                                                                                      \
+    k_compliance<ND, NF, false><<<blocks, RED_THREADS, 0, st>>>(op.g, xPhys, u, op.KE64,     \
+                                                               op.B64, eps, penal, dc, partial);
+  switch (key) {
+    case 33: TG_COMP(3, 3) break;
+    case 31: TG_COMP(3, 1) break;
+    case 22: TG_COMP(2, 2) break;
+    case 21: TG_COMP(2, 1) break;
+    default: throw Error{EINVAL_, "unsupported (ndim, nnode_dof) combination"};
+  }
+#undef TG_COMP
+  TG_CHECK_LAUNCH();
+}
+
+}  // namespace tg

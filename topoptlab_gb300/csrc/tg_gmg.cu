@@ -1,0 +1,541 @@
+// Geometric multigrid on structured grids: assembled coarse stencils,
+// exact (masked) Galerkin coarse operators, transfers, damped Jacobi, and the
+// dense FP64 coarsest-grid inverse.
+//
+// The reference's multigrid (multigrid.py:89-154 V-cycle, gmg.py:148-189
+// stride-2 coarse nodes, linear_solvers.py:306-372 damped Jacobi) forms
+// P^T A P with SciPy on every V-cycle call and its interpolator
+// (gmg.py:34-146) does not run.  Here:
+//  * P is trilinear (bilinear) interpolation from the stride-2 nodes, per DOF
+//    component, masked on both sides: Pt = M_f P M_c;
+//  * level 1 is built straight from the element scale factors as
+//    A_1 = Pt^T (M K(rho) M) Pt: an unmasked child element contributes
+//    rho_c * Q_c with Q_c = P_c^T KE P_c precomputed once per problem, a
+//    child touching a fixed DOF contributes the exact masked product;
+//  * deeper levels are Galerkin products of the assembled stencils;
+//  * stencils are stored structure-of-arrays, A[(dir*ndof+ci)*ndof+cj][node],
+//    so one thread per node reads coalesced coefficients;
+//  * the coarsest level (a few hundred to ~2000 DOFs) is inverted once per
+//    design iteration by a blocked Gauss-Jordan in FP64 and applied as one
+//    dense mat-vec per V-cycle.
+#include "tg_ops.cuh"
+
+namespace tg {
+
+template <int NDIM> __host__ __device__ constexpr int ndir() { return NDIM == 3 ? 27 : 9; }
+
+__device__ __forceinline__ void node_xyz(const Grid& g, int64_t n, int& x, int& y, int& z) {
+  y = (int)(n % g.nny);
+  x = (int)((n / g.nny) % g.nnx);
+  z = (int)(n / ((int64_t)g.nny * g.nnx));
+}
+// direction index: dy fastest, then dx, then dz; components in {-1,0,1}
+__device__ __forceinline__ void dir_xyz(int d, int ndim, int& dx, int& dy, int& dz) {
+  dy = d % 3 - 1;
+  dx = (d / 3) % 3 - 1;
+  dz = (ndim == 3) ? d / 9 - 1 : 0;
+}
+__device__ __forceinline__ int dir_index(int dx, int dy, int dz, int ndim) {
+  return (ndim == 3 ? (dz + 1) * 9 : 0) + (dx + 1) * 3 + (dy + 1);
+}
+__device__ __forceinline__ bool in_grid(const Grid& g, int x, int y, int z) {
+  return x >= 0 && x < g.nnx && y >= 0 && y < g.nny && z >= 0 && z < g.nnz;
+}
+
+// ---------------------------------------------------------------------------
+// stencil mat-vec with fused residual / Jacobi epilogues
+// ---------------------------------------------------------------------------
+template <int NDIM, int NDOF, typename T, int MODE>
+__global__ void __launch_bounds__(256) k_stencil_apply(Grid g, const T* __restrict__ A,
+                                                      const T* __restrict__ u, T* __restrict__ y,
+                                                      const T* __restrict__ b,
+                                                      const T* __restrict__ dinv, T omega) {
+  const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t ld = g.nnodes();
+  if (n >= ld) return;
+  int x, yy, z;
+  node_xyz(g, n, x, yy, z);
+  T acc[NDOF];
+#pragma unroll
+  for (int c = 0; c < NDOF; ++c) acc[c] = T(0);
+#pragma unroll
+  for (int d = 0; d < ndir<NDIM>(); ++d) {
+    int dx, dy, dz;
+    dir_xyz(d, NDIM, dx, dy, dz);
+    if (!in_grid(g, x + dx, yy + dy, z + dz)) continue;
+    const int64_t m = g.node(x + dx, yy + dy, z + dz);
+#pragma unroll
+    for (int cj = 0; cj < NDOF; ++cj) {
+      const T uj = __ldg(u + m * NDOF + cj);
+#pragma unroll
+      for (int ci = 0; ci < NDOF; ++ci) acc[ci] += __ldg(A + ((d * NDOF + ci) * NDOF + cj) * ld + n) * uj;
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < NDOF; ++c) {
+    const int64_t k = n * NDOF + c;
+    T out;
+    if (MODE == AM_Y) out = acc[c];
+    else if (MODE == AM_RES) out = b[k] - acc[c];
+    else out = u[k] + omega * dinv[k] * (b[k] - acc[c]);
+    y[k] = out;
+  }
+}
+
+template <typename T>
+void stencil_apply(const Grid& g, const T* A, const T* u, T* y, const T* b, const T* dinv,
+                   double omega, int mode, cudaStream_t st) {
+  const unsigned blocks = (unsigned)cdiv(g.nnodes(), 256);
+  const int key = g.ndim * 10 + g.ndof;
+#define TG_SA(ND, NF)                                                                          \
+  if (mode == AM_Y) k_stencil_apply<ND, NF, T, AM_Y><<<blocks, 256, 0, st>>>(g, A, u, y, b, dinv, (T)omega); \
+  else if (mode == AM_RES) k_stencil_apply<ND, NF, T, AM_RES><<<blocks, 256, 0, st>>>(g, A, u, y, b, dinv, (T)omega); \
+  else k_stencil_apply<ND, NF, T, AM_JACOBI><<<blocks, 256, 0, st>>>(g, A, u, y, b, dinv, (T)omega);
+  switch (key) {
+    case 33: TG_SA(3, 3) break;
+    case 31: TG_SA(3, 1) break;
+    case 22: TG_SA(2, 2) break;
+    case 21: TG_SA(2, 1) break;
+    default: throw Error{EINVAL_, "unsupported (ndim, nnode_dof)"};
+  }
+#undef TG_SA
+  TG_CHECK_LAUNCH();
+}
+template void stencil_apply<double>(const Grid&, const double*, const double*, double*,
+                                    const double*, const double*, double, int, cudaStream_t);
+template void stencil_apply<float>(const Grid&, const float*, const float*, float*, const float*,
+                                   const float*, double, int, cudaStream_t);
+
+template <int NDIM, int NDOF, typename T>
+__global__ void k_stencil_dinv(Grid g, const uint8_t* fix, const T* A, T* dinv) {
+  const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t ld = g.nnodes();
+  if (n >= ld) return;
+  const int center = ndir<NDIM>() / 2;
+#pragma unroll
+  for (int c = 0; c < NDOF; ++c) {
+    const T dg = A[((center * NDOF + c) * NDOF + c) * ld + n];
+    dinv[n * NDOF + c] = (((fix[n] >> c) & 1) || dg == T(0)) ? T(0) : T(1) / dg;
+  }
+}
+
+template <typename T>
+void stencil_dinv(const Grid& g, const uint8_t* fix, const T* A, T* dinv, cudaStream_t st) {
+  const unsigned blocks = (unsigned)cdiv(g.nnodes(), 256);
+  const int key = g.ndim * 10 + g.ndof;
+  switch (key) {
+    case 33: k_stencil_dinv<3, 3, T><<<blocks, 256, 0, st>>>(g, fix, A, dinv); break;
+    case 31: k_stencil_dinv<3, 1, T><<<blocks, 256, 0, st>>>(g, fix, A, dinv); break;
+    case 22: k_stencil_dinv<2, 2, T><<<blocks, 256, 0, st>>>(g, fix, A, dinv); break;
+    case 21: k_stencil_dinv<2, 1, T><<<blocks, 256, 0, st>>>(g, fix, A, dinv); break;
+    default: throw Error{EINVAL_, "unsupported (ndim, nnode_dof)"};
+  }
+  TG_CHECK_LAUNCH();
+}
+template void stencil_dinv<double>(const Grid&, const uint8_t*, const double*, double*, cudaStream_t);
+template void stencil_dinv<float>(const Grid&, const uint8_t*, const float*, float*, cudaStream_t);
+
+// ---------------------------------------------------------------------------
+// level 1 from the element scale factors
+// ---------------------------------------------------------------------------
+// weight of coarse corner a for child-element corner p of child octant o
+__device__ __forceinline__ double pweight(int o, int p, int a, int ndim) {
+  double w = 1.0;
+  for (int k = 0; k < ndim; ++k) {
+    const int pos = ((o >> k) & 1) + ((p >> k) & 1);   // 0..2 inside the coarse element
+    const int dist = abs(pos - 2 * ((a >> k) & 1));
+    w *= (dist == 0) ? 1.0 : (dist == 1 ? 0.5 : 0.0);
+  }
+  return w;
+}
+
+template <int NDIM, int NDOF>
+__global__ void __launch_bounds__(256) k_build_level1(Grid gf, Grid gc, const double* __restrict__ scale,
+                                                      const uint8_t* __restrict__ touch,
+                                                      const uint8_t* __restrict__ fixf,
+                                                      const double* __restrict__ Q,
+                                                      const double* __restrict__ KE,
+                                                      const uint8_t* __restrict__ fixc,
+                                                      double* __restrict__ Ac) {
+  constexpr int NC = 1 << NDIM;
+  constexpr int NE = NC * NDOF;
+  const int64_t ldc = gc.nnodes();
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= ldc * ndir<NDIM>()) return;
+  const int64_t I = t % ldc;
+  const int D = (int)(t / ldc);
+  int ix, iy, iz, dx, dy, dz;
+  node_xyz(gc, I, ix, iy, iz);
+  dir_xyz(D, NDIM, dx, dy, dz);
+  const int jx = ix + dx, jy = iy + dy, jz = iz + dz;
+  double acc[NDOF][NDOF];
+#pragma unroll
+  for (int a = 0; a < NDOF; ++a)
+#pragma unroll
+    for (int b = 0; b < NDOF; ++b) acc[a][b] = 0.0;
+  if (in_grid(gc, jx, jy, jz)) {
+    const int64_t J = gc.node(jx, jy, jz);
+    const int exl = max(max(ix, jx) - 1, 0), exh = min(min(ix, jx), gc.nex - 1);
+    const int eyl = max(max(iy, jy) - 1, 0), eyh = min(min(iy, jy), gc.ney - 1);
+    const int ezl = (NDIM == 3) ? max(max(iz, jz) - 1, 0) : 0;
+    const int ezh = (NDIM == 3) ? min(min(iz, jz), gc.nez - 1) : 0;
+    for (int ez = ezl; ez <= ezh; ++ez)
+      for (int ex = exl; ex <= exh; ++ex)
+        for (int ey = eyl; ey <= eyh; ++ey) {
+          const int ca = (ix - ex) | ((iy - ey) << 1) | ((NDIM == 3 ? iz - ez : 0) << 2);
+          const int cb = (jx - ex) | ((jy - ey) << 1) | ((NDIM == 3 ? jz - ez : 0) << 2);
+#pragma unroll 1
+          for (int o = 0; o < NC; ++o) {
+            const int fx = 2 * ex + (o & 1), fy = 2 * ey + ((o >> 1) & 1);
+            const int fz = (NDIM == 3) ? 2 * ez + ((o >> 2) & 1) : 0;
+            const int64_t fe = gf.elem(fx, fy, fz);
+            const double rho = scale[fe];
+            if (!touch[fe]) {
+              const double* Qo = Q + (int64_t)o * NE * NE;
+#pragma unroll
+              for (int ci = 0; ci < NDOF; ++ci)
+#pragma unroll
+                for (int cj = 0; cj < NDOF; ++cj)
+                  acc[ci][cj] += rho * __ldg(Qo + (ca * NDOF + ci) * NE + cb * NDOF + cj);
+            } else {
+              // exact: sum_{p,q} P[p,a] P[q,b] m(p,ci) m(q,cj) KE[(p,ci),(q,cj)]
+              for (int p = 0; p < NC; ++p) {
+                const double wp = pweight(o, p, ca, NDIM);
+                if (wp == 0.0) continue;
+                const uint8_t mp = fixf[gf.node(fx + (p & 1), fy + ((p >> 1) & 1),
+                                                 (NDIM == 3) ? fz + ((p >> 2) & 1) : 0)];
+                for (int q = 0; q < NC; ++q) {
+                  const double wq = pweight(o, q, cb, NDIM);
+                  if (wq == 0.0) continue;
+                  const uint8_t mq = fixf[gf.node(fx + (q & 1), fy + ((q >> 1) & 1),
+                                                   (NDIM == 3) ? fz + ((q >> 2) & 1) : 0)];
+                  for (int ci = 0; ci < NDOF; ++ci) {
+                    if ((mp >> ci) & 1) continue;
+                    for (int cj = 0; cj < NDOF; ++cj) {
+                      if ((mq >> cj) & 1) continue;
+                      acc[ci][cj] += rho * wp * wq * KE[(p * NDOF + ci) * NE + q * NDOF + cj];
+                    }
+                  }
+                }
+              }
+            }
+          }
+        }
+    const uint8_t mi = fixc[I], mj = fixc[J];
+#pragma unroll
+    for (int ci = 0; ci < NDOF; ++ci)
+#pragma unroll
+      for (int cj = 0; cj < NDOF; ++cj)
+        if (((mi >> ci) & 1) || ((mj >> cj) & 1)) acc[ci][cj] = 0.0;
+  }
+#pragma unroll
+  for (int ci = 0; ci < NDOF; ++ci)
+#pragma unroll
+    for (int cj = 0; cj < NDOF; ++cj) Ac[((D * NDOF + ci) * NDOF + cj) * ldc + I] = acc[ci][cj];
+}
+
+void build_level1(const FineOp& op, const double* scale, const uint8_t* touch, const double* Q,
+                  const Grid& gc, const uint8_t* fixc, double* Ac, cudaStream_t st) {
+  const int64_t nt = gc.nnodes() * (op.g.ndim == 3 ? 27 : 9);
+  const unsigned blocks = (unsigned)cdiv(nt, 256);
+  const int key = op.g.ndim * 10 + op.g.ndof;
+  switch (key) {
+    case 33: k_build_level1<3, 3><<<blocks, 256, 0, st>>>(op.g, gc, scale, touch, op.fix, Q, op.KE64, fixc, Ac); break;
+    case 31: k_build_level1<3, 1><<<blocks, 256, 0, st>>>(op.g, gc, scale, touch, op.fix, Q, op.KE64, fixc, Ac); break;
+    case 22: k_build_level1<2, 2><<<blocks, 256, 0, st>>>(op.g, gc, scale, touch, op.fix, Q, op.KE64, fixc, Ac); break;
+    case 21: k_build_level1<2, 1><<<blocks, 256, 0, st>>>(op.g, gc, scale, touch, op.fix, Q, op.KE64, fixc, Ac); break;
+    default: throw Error{EINVAL_, "unsupported (ndim, nnode_dof)"};
+  }
+  TG_CHECK_LAUNCH();
+}
+
+// ---------------------------------------------------------------------------
+// Galerkin product of an assembled stencil
+// ---------------------------------------------------------------------------
+template <int NDIM, int NDOF>
+__global__ void __launch_bounds__(256) k_galerkin(Grid gf, const double* __restrict__ Af, Grid gc,
+                                                  const uint8_t* __restrict__ fixc,
+                                                  double* __restrict__ Ac) {
+  const int64_t ldc = gc.nnodes(), ldf = gf.nnodes();
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= ldc * ndir<NDIM>()) return;
+  const int64_t I = t % ldc;
+  const int D = (int)(t / ldc);
+  int ix, iy, iz, dx, dy, dz;
+  node_xyz(gc, I, ix, iy, iz);
+  dir_xyz(D, NDIM, dx, dy, dz);
+  const int jx = ix + dx, jy = iy + dy, jz = iz + dz;
+  double acc[NDOF][NDOF];
+#pragma unroll
+  for (int a = 0; a < NDOF; ++a)
+#pragma unroll
+    for (int b = 0; b < NDOF; ++b) acc[a][b] = 0.0;
+  if (in_grid(gc, jx, jy, jz)) {
+    const int64_t J = gc.node(jx, jy, jz);
+    for (int al = 0; al < ndir<NDIM>(); ++al) {
+      int ax, ay, az;
+      dir_xyz(al, NDIM, ax, ay, az);
+      const int fx = 2 * ix + ax, fy = 2 * iy + ay, fz = 2 * iz + az;
+      if (!in_grid(gf, fx, fy, fz)) continue;
+      const double wi = (ax ? 0.5 : 1.0) * (ay ? 0.5 : 1.0) * (az ? 0.5 : 1.0);
+      const int64_t fi = gf.node(fx, fy, fz);
+      for (int be = 0; be < ndir<NDIM>(); ++be) {
+        int bx, by, bz;
+        dir_xyz(be, NDIM, bx, by, bz);
+        const int gx = 2 * jx + bx, gy = 2 * jy + by, gz = 2 * jz + bz;
+        const int rx = gx - fx, ry = gy - fy, rz = gz - fz;
+        if (rx < -1 || rx > 1 || ry < -1 || ry > 1 || rz < -1 || rz > 1) continue;
+        if (!in_grid(gf, gx, gy, gz)) continue;
+        const double w = wi * (bx ? 0.5 : 1.0) * (by ? 0.5 : 1.0) * (bz ? 0.5 : 1.0);
+        const int dd = dir_index(rx, ry, rz, NDIM);
+#pragma unroll
+        for (int ci = 0; ci < NDOF; ++ci)
+#pragma unroll
+          for (int cj = 0; cj < NDOF; ++cj)
+            acc[ci][cj] += w * __ldg(Af + ((dd * NDOF + ci) * NDOF + cj) * ldf + fi);
+      }
+    }
+    const uint8_t mi = fixc[I], mj = fixc[J];
+#pragma unroll
+    for (int ci = 0; ci < NDOF; ++ci)
+#pragma unroll
+      for (int cj = 0; cj < NDOF; ++cj)
+        if (((mi >> ci) & 1) || ((mj >> cj) & 1)) acc[ci][cj] = 0.0;
+  }
+#pragma unroll
+  for (int ci = 0; ci < NDOF; ++ci)
+#pragma unroll
+    for (int cj = 0; cj < NDOF; ++cj) Ac[((D * NDOF + ci) * NDOF + cj) * ldc + I] = acc[ci][cj];
+}
+
+void build_galerkin(const Grid& gf, const double* Af, const Grid& gc, const uint8_t* fixc,
+                    double* Ac, cudaStream_t st) {
+  const int64_t nt = gc.nnodes() * (gf.ndim == 3 ? 27 : 9);
+  const unsigned blocks = (unsigned)cdiv(nt, 256);
+  const int key = gf.ndim * 10 + gf.ndof;
+  switch (key) {
+    case 33: k_galerkin<3, 3><<<blocks, 256, 0, st>>>(gf, Af, gc, fixc, Ac); break;
+    case 31: k_galerkin<3, 1><<<blocks, 256, 0, st>>>(gf, Af, gc, fixc, Ac); break;
+    case 22: k_galerkin<2, 2><<<blocks, 256, 0, st>>>(gf, Af, gc, fixc, Ac); break;
+    case 21: k_galerkin<2, 1><<<blocks, 256, 0, st>>>(gf, Af, gc, fixc, Ac); break;
+    default: throw Error{EINVAL_, "unsupported (ndim, nnode_dof)"};
+  }
+  TG_CHECK_LAUNCH();
+}
+
+// ---------------------------------------------------------------------------
+// transfers
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_restrict(Grid gf, Grid gc, const uint8_t* fixc, const T* __restrict__ rf,
+                           T* __restrict__ bc) {
+  const int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (I >= gc.nnodes()) return;
+  const int ndof = gc.ndof;
+  int ix, iy, iz;
+  node_xyz(gc, I, ix, iy, iz);
+  double acc[3] = {0.0, 0.0, 0.0};
+  const int nd = (gc.ndim == 3) ? 27 : 9;
+  for (int al = 0; al < nd; ++al) {
+    int ax, ay, az;
+    dir_xyz(al, gc.ndim, ax, ay, az);
+    const int fx = 2 * ix + ax, fy = 2 * iy + ay, fz = 2 * iz + az;
+    if (!in_grid(gf, fx, fy, fz)) continue;
+    const double w = (ax ? 0.5 : 1.0) * (ay ? 0.5 : 1.0) * (az ? 0.5 : 1.0);
+    const int64_t fi = gf.node(fx, fy, fz);
+    for (int c = 0; c < ndof; ++c) acc[c] += w * (double)rf[fi * ndof + c];
+  }
+  for (int c = 0; c < ndof; ++c) bc[I * ndof + c] = ((fixc[I] >> c) & 1) ? T(0) : (T)acc[c];
+}
+
+template <typename T>
+void restrict_(const Grid& gf, const Grid& gc, const uint8_t* fixc, const T* rf, T* bc,
+               cudaStream_t st) {
+  k_restrict<T><<<(unsigned)cdiv(gc.nnodes(), 256), 256, 0, st>>>(gf, gc, fixc, rf, bc);
+  TG_CHECK_LAUNCH();
+}
+template void restrict_<double>(const Grid&, const Grid&, const uint8_t*, const double*, double*, cudaStream_t);
+template void restrict_<float>(const Grid&, const Grid&, const uint8_t*, const float*, float*, cudaStream_t);
+
+template <typename T>
+__global__ void k_prolong_add(Grid gf, Grid gc, const uint8_t* fixf, const T* __restrict__ xc,
+                              T* __restrict__ xf) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= gf.nnodes()) return;
+  const int ndof = gf.ndof;
+  int fx, fy, fz;
+  node_xyz(gf, i, fx, fy, fz);
+  double acc[3] = {0.0, 0.0, 0.0};
+  const int nzc = (gf.ndim == 3 && (fz & 1)) ? 2 : 1;
+  const int nxc = (fx & 1) ? 2 : 1, nyc = (fy & 1) ? 2 : 1;
+  const double w = ((fx & 1) ? 0.5 : 1.0) * ((fy & 1) ? 0.5 : 1.0) *
+                   ((gf.ndim == 3 && (fz & 1)) ? 0.5 : 1.0);
+  for (int a = 0; a < nzc; ++a)
+    for (int b = 0; b < nxc; ++b)
+      for (int c2 = 0; c2 < nyc; ++c2) {
+        const int cz = (gf.ndim == 3) ? fz / 2 + a : 0, cx = fx / 2 + b, cy = fy / 2 + c2;
+        const int64_t I = gc.node(cx, cy, cz);
+        for (int c = 0; c < ndof; ++c) acc[c] += w * (double)xc[I * ndof + c];
+      }
+  for (int c = 0; c < ndof; ++c)
+    if (!((fixf[i] >> c) & 1)) xf[i * ndof + c] += (T)acc[c];
+}
+
+template <typename T>
+void prolong_add(const Grid& gf, const Grid& gc, const uint8_t* fixf, const T* xc, T* xf,
+                 cudaStream_t st) {
+  k_prolong_add<T><<<(unsigned)cdiv(gf.nnodes(), 256), 256, 0, st>>>(gf, gc, fixf, xc, xf);
+  TG_CHECK_LAUNCH();
+}
+template void prolong_add<double>(const Grid&, const Grid&, const uint8_t*, const double*, double*, cudaStream_t);
+template void prolong_add<float>(const Grid&, const Grid&, const uint8_t*, const float*, float*, cudaStream_t);
+
+// ---------------------------------------------------------------------------
+// coarsest level: dense matrix and blocked Gauss-Jordan inverse (FP64)
+// ---------------------------------------------------------------------------
+__global__ void k_stencil_to_dense(Grid g, const uint8_t* fix, const double* __restrict__ A,
+                                   double* D, int64_t n, int64_t ld) {
+  const int64_t ldA = g.nnodes();
+  const int nd = g.ndim == 3 ? 27 : 9;
+  const int ndof = g.ndof;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= ldA * nd * ndof * ndof) return;
+  const int64_t I = t % ldA;
+  const int k = (int)(t / ldA);          // (dir*ndof+ci)*ndof+cj
+  const int cj = k % ndof, ci = (k / ndof) % ndof, d = k / (ndof * ndof);
+  int ix, iy, iz, dx, dy, dz;
+  node_xyz(g, I, ix, iy, iz);
+  dir_xyz(d, g.ndim, dx, dy, dz);
+  if (!in_grid(g, ix + dx, iy + dy, iz + dz)) return;
+  const int64_t J = g.node(ix + dx, iy + dy, iz + dz);
+  D[(I * ndof + ci) * ld + J * ndof + cj] = A[(int64_t)k * ldA + I];
+}
+__global__ void k_dense_fix_diag(Grid g, const uint8_t* fix, double* D, int64_t n, int64_t ld) {
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= ld) return;
+  if (r >= n) {
+    D[r * ld + r] = 1.0;
+    return;
+  }
+  const int64_t node = r / g.ndof;
+  const int c = (int)(r % g.ndof);
+  if ((fix[node] >> c) & 1) D[r * ld + r] = 1.0;
+}
+
+void stencil_to_dense(const Grid& g, const uint8_t* fix, const double* A, double* D, int64_t n,
+                      int64_t ld, cudaStream_t st) {
+  TG_CUDA(cudaMemsetAsync(D, 0, sizeof(double) * ld * ld, st));
+  const int64_t nt = g.nnodes() * (g.ndim == 3 ? 27 : 9) * g.ndof * g.ndof;
+  k_stencil_to_dense<<<(unsigned)cdiv(nt, 256), 256, 0, st>>>(g, fix, A, D, n, ld);
+  TG_CHECK_LAUNCH();
+  k_dense_fix_diag<<<(unsigned)cdiv(ld, 256), 256, 0, st>>>(g, fix, D, n, ld);
+  TG_CHECK_LAUNCH();
+}
+
+constexpr int GJB = 32;
+
+// invert the k-th diagonal block (SPD, no pivoting) into P (GJB x GJB)
+__global__ void __launch_bounds__(GJB * GJB) k_gj_pivot(const double* D, int64_t ld, int k, double* P) {
+  __shared__ double a[GJB][GJB + 1];
+  const int i = threadIdx.y, j = threadIdx.x;
+  a[i][j] = D[(int64_t)(k * GJB + i) * ld + k * GJB + j];
+  __syncthreads();
+  for (int p = 0; p < GJB; ++p) {
+    const double piv = a[p][p];
+    const double aip = a[i][p], apj = a[p][j];
+    __syncthreads();
+    double v;
+    if (i == p && j == p) v = 1.0 / piv;
+    else if (i == p) v = apj / piv;
+    else if (j == p) v = -aip / piv;
+    else v = a[i][j] - aip * apj / piv;
+    a[i][j] = v;
+    __syncthreads();
+  }
+  P[i * GJB + j] = a[i][j];
+}
+// R[:, jb] = P * D[k-block, jb]
+__global__ void __launch_bounds__(GJB * GJB) k_gj_rowpanel(const double* D, int64_t ld, int k,
+                                                          const double* P, double* R) {
+  __shared__ double ps[GJB][GJB + 1], ds[GJB][GJB + 1];
+  const int i = threadIdx.y, j = threadIdx.x, jb = blockIdx.x;
+  ps[i][j] = P[i * GJB + j];
+  ds[i][j] = D[(int64_t)(k * GJB + i) * ld + jb * GJB + j];
+  __syncthreads();
+  double acc = 0.0;
+#pragma unroll 8
+  for (int m = 0; m < GJB; ++m) acc += ps[i][m] * ds[m][j];
+  R[(int64_t)i * ld + jb * GJB + j] = acc;
+}
+// D[ib, jb] -= D[ib, k] R[:, jb]   for ib != k, jb != k
+__global__ void __launch_bounds__(GJB * GJB) k_gj_update(double* D, int64_t ld, int k,
+                                                        const double* R) {
+  const int ib = blockIdx.y, jb = blockIdx.x;
+  if (ib == k || jb == k) return;
+  __shared__ double cs[GJB][GJB + 1], rs[GJB][GJB + 1];
+  const int i = threadIdx.y, j = threadIdx.x;
+  cs[i][j] = D[(int64_t)(ib * GJB + i) * ld + k * GJB + j];
+  rs[i][j] = R[(int64_t)i * ld + jb * GJB + j];
+  __syncthreads();
+  double acc = 0.0;
+#pragma unroll 8
+  for (int m = 0; m < GJB; ++m) acc += cs[i][m] * rs[m][j];
+  D[(int64_t)(ib * GJB + i) * ld + jb * GJB + j] -= acc;
+}
+// column k <- -D[:,k] P ; row k <- R ; pivot block <- P
+__global__ void __launch_bounds__(GJB * GJB) k_gj_finish(double* D, int64_t ld, int k,
+                                                        const double* P, const double* R) {
+  const int b = blockIdx.x;
+  const int i = threadIdx.y, j = threadIdx.x;
+  if (b == k) {
+    D[(int64_t)(k * GJB + i) * ld + k * GJB + j] = P[i * GJB + j];
+    return;
+  }
+  __shared__ double cs[GJB][GJB + 1], ps[GJB][GJB + 1];
+  cs[i][j] = D[(int64_t)(b * GJB + i) * ld + k * GJB + j];
+  ps[i][j] = P[i * GJB + j];
+  __syncthreads();
+  double acc = 0.0;
+#pragma unroll 8
+  for (int m = 0; m < GJB; ++m) acc += cs[i][m] * ps[m][j];
+  D[(int64_t)(b * GJB + i) * ld + k * GJB + j] = -acc;
+  D[(int64_t)(k * GJB + i) * ld + b * GJB + j] = R[(int64_t)i * ld + b * GJB + j];
+}
+
+void gj_inverse(double* D, int64_t n, int64_t ld, double* work, cudaStream_t st) {
+  TG_REQUIRE(ld % GJB == 0, "dense leading dimension must be a multiple of 32");
+  const int nb = (int)(ld / GJB);
+  double* P = work;                 // GJB*GJB
+  double* R = work + GJB * GJB;     // GJB*ld
+  const dim3 thr(GJB, GJB);
+  for (int k = 0; k < nb; ++k) {
+    k_gj_pivot<<<1, thr, 0, st>>>(D, ld, k, P);
+    k_gj_rowpanel<<<nb, thr, 0, st>>>(D, ld, k, P, R);
+    k_gj_update<<<dim3(nb, nb), thr, 0, st>>>(D, ld, k, R);
+    k_gj_finish<<<nb, thr, 0, st>>>(D, ld, k, P, R);
+  }
+  TG_CHECK_LAUNCH();
+}
+
+// x = Dinv b (warp per row), fixed rows of Dinv hold identity and b is 0 there
+template <typename T>
+__global__ void k_dense_apply(const double* __restrict__ Dinv, int64_t n, int64_t ld,
+                              const T* __restrict__ b, T* __restrict__ x) {
+  const int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  double acc = 0.0;
+  for (int64_t j = lane; j < n; j += 32) acc += Dinv[row * ld + j] * (double)b[j];
+  acc = warp_sum(acc);
+  if (lane == 0) x[row] = (T)acc;
+}
+
+template <typename T>
+void dense_apply(const double* Dinv, int64_t n, int64_t ld, const T* b, T* x, cudaStream_t st) {
+  k_dense_apply<T><<<(unsigned)cdiv(n * 32, 256), 256, 0, st>>>(Dinv, n, ld, b, x);
+  TG_CHECK_LAUNCH();
+}
+template void dense_apply<double>(const double*, int64_t, int64_t, const double*, double*, cudaStream_t);
+template void dense_apply<float>(const double*, int64_t, int64_t, const float*, float*, cudaStream_t);
+
+}  // namespace tg

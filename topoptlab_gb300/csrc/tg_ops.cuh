@@ -1,0 +1,106 @@
+// Host-side launcher declarations shared by the library's translation units.
+#pragma once
+#include "tg_common.cuh"
+
+namespace tg {
+
+// Sector blocks of the element matrix.  With H the Walsh-Hadamard transform
+// over the element's corner bits (d = dx | dy<<1 | dz<<2, y in index space),
+// KE = H B H where B is block diagonal: block chi couples (sigma, c) with
+// sigma = chi ^ (1<<c) for vector problems (ndof == ndim) and sigma = chi for
+// scalar ones.  The 1/4^ndim normalisation is folded into B.
+template <typename T> struct Sector {
+  T b[8][3][3];
+};
+
+// Fine-level (matrix-free) operator description.
+struct FineOp {
+  Grid g;
+  const uint8_t* fix;       // [nnodes] fixed-DOF bits
+  const double* KE64;       // [NE*NE] element matrix, corner-bit order (device)
+  const float* KE32;        // same in FP32 (device)
+  Sector<double> B64;
+  Sector<float> B32;
+  bool sector;              // use the sector path
+  double KEdiag[24];        // diagonal of KE, corner-bit order
+};
+
+enum ApplyMode : int { AM_Y = 0, AM_RES = 1, AM_JACOBI = 2 };
+
+// y = M K(s) M u  (mode AM_Y);  y = b - A u  (AM_RES);
+// y = u + omega * dinv * (b - A u)  (AM_JACOBI).  Fixed DOFs of y are 0.
+template <typename T, typename S>
+void fine_apply(const FineOp& op, const S* scale, const T* u, T* y, const T* b, const T* dinv,
+                double omega, int mode, cudaStream_t st);
+
+// dinv = 1/diag(A) on free DOFs, 0 on fixed DOFs
+template <typename T, typename S>
+void fine_dinv(const FineOp& op, const S* scale, T* dinv, cudaStream_t st);
+
+// ce_e = u_e^T KE u_e ;  dc_e = -penal (1-eps) x^(penal-1) ce_e ;
+// partial[b] = sum over the block's elements of simp(x_e) ce_e
+void fine_compliance(const FineOp& op, const double* xPhys, const double* u, double eps,
+                     double penal, double* dc, double* partial, cudaStream_t st);
+
+// ---------------------------------------------------------------------------
+// assembled 3^ndim-point block stencils (coarse levels)
+// layout: A[(dir * ndof + ci) * ndof + cj][node]   (structure of arrays)
+// ---------------------------------------------------------------------------
+struct Stencil {
+  Grid g;
+  const uint8_t* fix;
+  void* A;             // double* or float*
+  int64_t ld;          // leading dimension = nnodes
+};
+
+template <typename T>
+void stencil_apply(const Grid& g, const T* A, const T* u, T* y, const T* b, const T* dinv,
+                   double omega, int mode, cudaStream_t st);
+template <typename T>
+void stencil_dinv(const Grid& g, const uint8_t* fix, const T* A, T* dinv, cudaStream_t st);
+
+// level-1 stencil straight from element scale factors (exact masked Galerkin)
+void build_level1(const FineOp& op, const double* scale, const uint8_t* elem_touch_fixed,
+                  const double* Q /* [nchild][NE][NE] */, const Grid& gc,
+                  const uint8_t* fixc, double* Ac, cudaStream_t st);
+// Galerkin product of an assembled stencil: Ac = M_c P^T A P M_c
+void build_galerkin(const Grid& gf, const double* Af, const Grid& gc, const uint8_t* fixc,
+                    double* Ac, cudaStream_t st);
+
+// transfers (masked): bc = Mc P^T rf ;  xf += Mf P xc
+template <typename T>
+void restrict_(const Grid& gf, const Grid& gc, const uint8_t* fixc, const T* rf, T* bc,
+               cudaStream_t st);
+template <typename T>
+void prolong_add(const Grid& gf, const Grid& gc, const uint8_t* fixf, const T* xc, T* xf,
+                 cudaStream_t st);
+
+// coarsest level: dense matrix (fixed DOFs -> identity) and its inverse
+void stencil_to_dense(const Grid& g, const uint8_t* fix, const double* A, double* D, int64_t n,
+                      int64_t ld, cudaStream_t st);
+void gj_inverse(double* D, int64_t n, int64_t ld, double* work, cudaStream_t st);
+template <typename T>
+void dense_apply(const double* Dinv, int64_t n, int64_t ld, const T* b, T* x, cudaStream_t st);
+
+// ---------------------------------------------------------------------------
+// design-variable kernels
+// ---------------------------------------------------------------------------
+struct FilterStencil {
+  int R;                 // half width
+  int nw;                // (2R+1)^ndim
+  const double* w;       // [nw] weights, dz slowest, dx, dy fastest
+};
+// mode 0: y = (H x) / Hs ; mode 1: y = H (x / Hs) ; mode 2: y = H(x*d)/Hs/max(1e-3, x)
+// mode 3: Hs = H 1 (x unused) ; mode 4: y = x (copy, used with the fused reductions)
+void filter_apply(const Grid& ge, const FilterStencil& fs, const double* x, const double* d,
+                  const double* Hs, double* y, int mode, cudaStream_t st);
+
+void simp_scale(int64_t n, const double* x, double eps, double penal, double* s64, float* s32,
+                __nv_bfloat16* s16, cudaStream_t st);
+
+// vector helpers
+template <typename T>
+void axpby(int64_t n, double a, const T* x, double b, T* y, cudaStream_t st);
+void mask_vec_f64(int64_t nnodes, int ndof, const uint8_t* fix, double* v, cudaStream_t st);
+
+}  // namespace tg
