@@ -144,6 +144,17 @@ int32_t tg_levels(tg_ctx* ctx, int32_t* nlevels, int64_t* ndofs_per_level /* >= 
 /* assembled stencil of level >= 1 for the densities xPhys, layout
  * [(dir*ndof+ci)*ndof+cj][node], n = 3^ndim*ndof^2*nnodes(level) */
 int32_t tg_coarse_stencil(tg_ctx* ctx, const double* xPhys, int32_t level, double* out, int64_t n);
+/* Device time between two calls on the context's stream: op 0 records the
+ * start event, op 1 records the stop event, synchronises and writes the
+ * elapsed milliseconds to *ms. */
+int32_t tg_timer(tg_ctx* ctx, int32_t op, double* ms);
+/* Event timing of one kernel family (0 off, 1 fine FP64 K.u, 2 fine FP32
+ * K.u, 3 fine FP32 K.u with BF16 densities, 4 FP32 coarse stencil, 5 FP64
+ * coarse stencil, 6 filter, 7 OC step); resets the accumulated time. */
+int32_t tg_profile_kernel(int32_t kind);
+/* Kernel launches made by the library (all contexts) and the accumulated
+ * device time / launch count of the profiled family; reset != 0 zeroes them. */
+int32_t tg_stats(int32_t reset, int64_t* launches, double* prof_ms, int64_t* prof_launches);
 /* edofMat (elements/bilinear_quadrilateral.py:7-48, trilinear_hexahedron.py:7-58)
  * generated on the device; out has nel*(2^ndim*nnode_dof) int32 entries */
 int32_t tg_edofmat(int32_t ndim, int32_t nelx, int32_t nely, int32_t nelz, int32_t nnode_dof,

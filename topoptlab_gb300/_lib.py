@@ -74,6 +74,9 @@ SIGNATURES = {
     "tg_vcycle": (C.c_int32, [C.c_void_p, _dp, _dp, _dp, C.c_int32]),
     "tg_levels": (C.c_int32, [C.c_void_p, _i32p, _i64p]),
     "tg_coarse_stencil": (C.c_int32, [C.c_void_p, _dp, C.c_int32, _dp, C.c_int64]),
+    "tg_timer": (C.c_int32, [C.c_void_p, C.c_int32, _dp]),
+    "tg_profile_kernel": (C.c_int32, [C.c_int32]),
+    "tg_stats": (C.c_int32, [C.c_int32, _i64p, _dp, _i64p]),
     "tg_edofmat": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _i32p,
                                C.c_int32]),
 }

@@ -313,6 +313,22 @@ int32_t tg_coarse_stencil(tg_ctx* ctx, const double* xPhys, int32_t level, doubl
   });
 }
 
+int32_t tg_timer(tg_ctx* ctx, int32_t op, double* ms) {
+  if (!ctx) return TG_EINVAL;
+  return guarded(ctx, [&] {
+    tg::Ctx& c = ctx->c;
+    if (op == 0) {
+      TG_CUDA(cudaEventRecord(c.tev0, c.st));
+    } else {
+      TG_CUDA(cudaEventRecord(c.tev1, c.st));
+      TG_CUDA(cudaEventSynchronize(c.tev1));
+      float t = 0.f;
+      TG_CUDA(cudaEventElapsedTime(&t, c.tev0, c.tev1));
+      if (ms) *ms = t;
+    }
+  });
+}
+
 int32_t tg_edofmat(int32_t ndim, int32_t nelx, int32_t nely, int32_t nelz, int32_t nnode_dof,
                    int32_t* out, int32_t device) {
   if (!out) return TG_EINVAL;

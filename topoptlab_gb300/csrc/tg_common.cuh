@@ -66,7 +66,24 @@ struct Error {
                                          cudaGetErrorString(_e)};            \
   } while (0)
 
-#define TG_CHECK_LAUNCH() TG_CUDA(cudaGetLastError())
+// Every kernel launch of the library goes through TG_CHECK_LAUNCH (or
+// count_launches for loops), which also counts launches for the bench's
+// gpu_launches figure.
+void count_launches(int64_t n);
+#define TG_CHECK_LAUNCH()                 \
+  do {                                    \
+    ::tg::count_launches(1);              \
+    TG_CUDA(cudaGetLastError());          \
+  } while (0)
+
+// Optional event timing of one kernel family (see tg_profile_kernel):
+// prof_begin/prof_end bracket the launches of family `kind` on stream st.
+enum ProfKind : int {
+  PK_NONE = 0, PK_FINE_F64 = 1, PK_FINE_F32 = 2, PK_FINE_BF16 = 3, PK_STENCIL_F32 = 4,
+  PK_STENCIL_F64 = 5, PK_FILTER = 6, PK_OC = 7
+};
+void prof_begin(int kind, cudaStream_t st);
+void prof_end(int kind, cudaStream_t st);
 
 #define TG_REQUIRE(cond, msg)                                                \
   do {                                                                       \

@@ -20,6 +20,8 @@ Ctx::~Ctx() {
   if (h_scal) cudaFreeHost(h_scal);
   if (ev0) cudaEventDestroy(ev0);
   if (ev1) cudaEventDestroy(ev1);
+  if (tev0) cudaEventDestroy(tev0);
+  if (tev1) cudaEventDestroy(tev1);
   if (st) cudaStreamDestroy(st);
 }
 
@@ -147,6 +149,8 @@ void ctx_init(Ctx& c, const tg_problem& p) {
   TG_CUDA(cudaStreamCreateWithFlags(&c.st, cudaStreamNonBlocking));
   TG_CUDA(cudaEventCreate(&c.ev0));
   TG_CUDA(cudaEventCreate(&c.ev1));
+  TG_CUDA(cudaEventCreate(&c.tev0));
+  TG_CUDA(cudaEventCreate(&c.tev1));
   c.g = make_grid(p.ndim, p.nnode_dof, p.nelx, p.nely, p.nelz);
   c.volfrac = p.volfrac; c.rmin = p.rmin; c.eps = p.eps; c.penal = p.penal;
   c.move = p.move > 0 ? p.move : 0.2;
@@ -179,11 +183,9 @@ void ctx_init(Ctx& c, const tg_problem& p) {
         touch[g.elem(ex, ey, ez)] = t ? 1 : 0;
       }
   // hierarchy grids and coarse fixed bits (coincident fine DOF)
+  // L == 1 with multigrid: the fine grid is the coarsest level and the
+  // "V-cycle" is the dense direct solve of the fine operator
   c.L = (c.precond == TG_PRECOND_GMG) ? choose_levels(g, p.nlevels) : 1;
-  if (c.precond == TG_PRECOND_GMG) {
-    TG_REQUIRE(c.L >= 2, "the grid cannot be coarsened (odd element counts): use "
-                         "preconditioner gb300-jacobi or element counts divisible by 2");
-  }
   std::vector<std::vector<uint8_t>> fixl{fix};
   c.lv.push_back(new Level());
   c.lv[0]->g = g;
@@ -202,7 +204,8 @@ void ctx_init(Ctx& c, const tg_problem& p) {
     const Grid gc = c.lv[c.L - 1]->g;
     c.nc = gc.ndofs();
     TG_REQUIRE(c.nc <= 8192, "coarsest multigrid level too large for the dense solve "
-                             "(use element counts divisible by a higher power of 2)");
+                             "(use element counts divisible by a higher power of 2, or "
+                             "preconditioner gb300-jacobi)");
     c.ldc = cdiv(c.nc, 32) * 32;
     c.Dc.alloc(c.ldc * c.ldc);
     c.gjwork.alloc(32 * 32 + 32 * c.ldc);
@@ -214,9 +217,9 @@ void ctx_init(Ctx& c, const tg_problem& p) {
     v.fix.alloc(v.g.nnodes());
     TG_CUDA(cudaMemcpy(v.fix.p, fixl[l].data(), fixl[l].size(), cudaMemcpyHostToDevice));
     const int64_t ns = v.g.nnodes() * (g.ndim == 3 ? 27 : 9) * g.ndof * g.ndof;
-    if (l >= 1) v.A64.alloc(ns);
     const bool last = (l == c.L - 1) && c.precond == TG_PRECOND_GMG;
-    if (!last) {
+    if (l >= 1 || last) v.A64.alloc(ns);
+    if (!last || l == 0) {
       v.dinv64.alloc(n); v.t64.alloc(n); v.r64.alloc(n);
       if (mixed) {
         v.dinv32.alloc(n); v.t32.alloc(n); v.r32.alloc(n);
@@ -313,6 +316,7 @@ void build_hierarchy(Ctx& c) {
     }
   }
   Level& cl = *c.lv[c.L - 1];
+  if (c.L == 1) build_fine_stencil(c.op, c.s64, cl.A64, c.st);
   stencil_to_dense(cl.g, cl.fix, cl.A64, c.Dc, c.nc, c.ldc, c.st);
   gj_inverse(c.Dc, c.nc, c.ldc, c.gjwork, c.st);
 }

@@ -85,7 +85,7 @@ struct Ctx {
   OCState* h_oc = nullptr;
   PCGState* h_pcg = nullptr;
   double* h_scal = nullptr;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, tev0 = nullptr, tev1 = nullptr;
   // statistics of the last solve
   int last_iters = 0, last_vcycles = 0, last_refine = 0, last_converged = 0;
   double last_relres = 0.0;

@@ -77,6 +77,7 @@ void filter_apply_ex(const Grid& g, const FilterStencil& fs, const double* x, co
                      const double* Hs, double* y, int mode, const double* xold, double* part_sum,
                      double* part_max, cudaStream_t st) {
   const unsigned blocks = red_blocks(g.nel());
+  prof_begin(PK_FILTER, st);
 #define TG_F(ND, M) k_filter<ND, M><<<blocks, RED_THREADS, 0, st>>>(g, fs.R, fs.w, x, d, Hs, y, xold, part_sum, part_max)
   if (g.ndim == 3) {
     if (mode == 0) TG_F(3, 0); else if (mode == 1) TG_F(3, 1); else if (mode == 2) TG_F(3, 2);
@@ -86,6 +87,7 @@ void filter_apply_ex(const Grid& g, const FilterStencil& fs, const double* x, co
     else if (mode == 3) TG_F(2, 3); else TG_F(2, 4);
   }
 #undef TG_F
+  prof_end(PK_FILTER, st);
   TG_CHECK_LAUNCH();
 }
 
@@ -213,13 +215,18 @@ void oc_begin(int64_t n, const double* dc, const double* dv, double* S, OCState*
               cudaStream_t s, double l1, double l2) {
   k_oc_prep<<<(unsigned)cdiv(n, RED_THREADS), RED_THREADS, 0, s>>>(n, dc, dv, S);
   k_oc_init<<<1, 1, 0, s>>>(st, g, l1, l2);
+  count_launches(1);
   TG_CHECK_LAUNCH();
 }
 void oc_steps(int64_t n, const double* x, const double* S, const double* dv, const int8_t* flags,
               double move, double* xnew, double* part, OCState* st, int nsteps, cudaStream_t s) {
   const unsigned blocks = red_blocks(n);
-  for (int k = 0; k < nsteps; ++k)
+  for (int k = 0; k < nsteps; ++k) {
+    prof_begin(PK_OC, s);
     k_oc_step<<<blocks, RED_THREADS, 0, s>>>(n, x, S, dv, flags, move, xnew, part, st);
+    prof_end(PK_OC, s);
+  }
+  count_launches(nsteps - 1);
   TG_CHECK_LAUNCH();
 }
 

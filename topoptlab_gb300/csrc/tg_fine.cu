@@ -15,6 +15,7 @@
 // KE = H B H (Walsh-Hadamard over corner bits, B block diagonal), ~240 flops
 // per hex8 element instead of 1152: GB300's FP64 pipe is narrow, and the
 // FP64 residual is the one K.u the mixed-precision solver cannot avoid.
+#include <type_traits>
 #include "tg_ops.cuh"
 
 namespace tg {
@@ -210,7 +211,11 @@ static void launch_apply(const ApplyArgs<T, S>& a, cudaStream_t st) {
   }
   dim3 grid((unsigned)cdiv(a.g.nny, TL::Y), (unsigned)cdiv(a.g.nnx, TL::X),
             (unsigned)cdiv(a.g.nnz, TL::Z));
+  const int pk = std::is_same<T, double>::value ? PK_FINE_F64
+                 : (std::is_same<S, float>::value ? PK_FINE_F32 : PK_FINE_BF16);
+  prof_begin(pk, st);
   kern<<<grid, 256, smem, st>>>(a);
+  prof_end(pk, st);
   TG_CHECK_LAUNCH();
 }
 

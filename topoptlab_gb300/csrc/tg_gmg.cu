@@ -87,6 +87,8 @@ void stencil_apply(const Grid& g, const T* A, const T* u, T* y, const T* b, cons
                    double omega, int mode, cudaStream_t st) {
   const unsigned blocks = (unsigned)cdiv(g.nnodes(), 256);
   const int key = g.ndim * 10 + g.ndof;
+  const int pk = sizeof(T) == 8 ? PK_STENCIL_F64 : PK_STENCIL_F32;
+  prof_begin(pk, st);
 #define TG_SA(ND, NF)                                                                          \
   if (mode == AM_Y) k_stencil_apply<ND, NF, T, AM_Y><<<blocks, 256, 0, st>>>(g, A, u, y, b, dinv, (T)omega); \
   else if (mode == AM_RES) k_stencil_apply<ND, NF, T, AM_RES><<<blocks, 256, 0, st>>>(g, A, u, y, b, dinv, (T)omega); \
@@ -99,6 +101,7 @@ void stencil_apply(const Grid& g, const T* A, const T* u, T* y, const T* b, cons
     default: throw Error{EINVAL_, "unsupported (ndim, nnode_dof)"};
   }
 #undef TG_SA
+  prof_end(pk, st);
   TG_CHECK_LAUNCH();
 }
 template void stencil_apply<double>(const Grid&, const double*, const double*, double*,
@@ -244,6 +247,73 @@ void build_level1(const FineOp& op, const double* scale, const uint8_t* touch, c
     case 31: k_build_level1<3, 1><<<blocks, 256, 0, st>>>(op.g, gc, scale, touch, op.fix, Q, op.KE64, fixc, Ac); break;
     case 22: k_build_level1<2, 2><<<blocks, 256, 0, st>>>(op.g, gc, scale, touch, op.fix, Q, op.KE64, fixc, Ac); break;
     case 21: k_build_level1<2, 1><<<blocks, 256, 0, st>>>(op.g, gc, scale, touch, op.fix, Q, op.KE64, fixc, Ac); break;
+    default: throw Error{EINVAL_, "unsupported (ndim, nnode_dof)"};
+  }
+  TG_CHECK_LAUNCH();
+}
+
+// fine-level stencil assembled from the element scale factors (used when the
+// fine grid is itself the coarsest level): A[I][D] = sum_e s_e M KE M
+template <int NDIM, int NDOF>
+__global__ void __launch_bounds__(256) k_build_fine(Grid g, const double* __restrict__ scale,
+                                                    const uint8_t* __restrict__ fix,
+                                                    const double* __restrict__ KE,
+                                                    double* __restrict__ A) {
+  constexpr int NE = (1 << NDIM) * NDOF;
+  const int64_t ld = g.nnodes();
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= ld * ndir<NDIM>()) return;
+  const int64_t I = t % ld;
+  const int D = (int)(t / ld);
+  int ix, iy, iz, dx, dy, dz;
+  node_xyz(g, I, ix, iy, iz);
+  dir_xyz(D, NDIM, dx, dy, dz);
+  const int jx = ix + dx, jy = iy + dy, jz = iz + dz;
+  double acc[NDOF][NDOF];
+#pragma unroll
+  for (int a = 0; a < NDOF; ++a)
+#pragma unroll
+    for (int b = 0; b < NDOF; ++b) acc[a][b] = 0.0;
+  if (in_grid(g, jx, jy, jz)) {
+    const int64_t J = g.node(jx, jy, jz);
+    const int exl = max(max(ix, jx) - 1, 0), exh = min(min(ix, jx), g.nex - 1);
+    const int eyl = max(max(iy, jy) - 1, 0), eyh = min(min(iy, jy), g.ney - 1);
+    const int ezl = (NDIM == 3) ? max(max(iz, jz) - 1, 0) : 0;
+    const int ezh = (NDIM == 3) ? min(min(iz, jz), g.nez - 1) : 0;
+    for (int ez = ezl; ez <= ezh; ++ez)
+      for (int ex = exl; ex <= exh; ++ex)
+        for (int ey = eyl; ey <= eyh; ++ey) {
+          const int ca = (ix - ex) | ((iy - ey) << 1) | ((NDIM == 3 ? iz - ez : 0) << 2);
+          const int cb = (jx - ex) | ((jy - ey) << 1) | ((NDIM == 3 ? jz - ez : 0) << 2);
+          const double s = scale[g.elem(ex, ey, ez)];
+#pragma unroll
+          for (int ci = 0; ci < NDOF; ++ci)
+#pragma unroll
+            for (int cj = 0; cj < NDOF; ++cj)
+              acc[ci][cj] += s * KE[(ca * NDOF + ci) * NE + cb * NDOF + cj];
+        }
+    const uint8_t mi = fix[I], mj = fix[J];
+#pragma unroll
+    for (int ci = 0; ci < NDOF; ++ci)
+#pragma unroll
+      for (int cj = 0; cj < NDOF; ++cj)
+        if (((mi >> ci) & 1) || ((mj >> cj) & 1)) acc[ci][cj] = 0.0;
+  }
+#pragma unroll
+  for (int ci = 0; ci < NDOF; ++ci)
+#pragma unroll
+    for (int cj = 0; cj < NDOF; ++cj) A[((D * NDOF + ci) * NDOF + cj) * ld + I] = acc[ci][cj];
+}
+
+void build_fine_stencil(const FineOp& op, const double* scale, double* A, cudaStream_t st) {
+  const int64_t nt = op.g.nnodes() * (op.g.ndim == 3 ? 27 : 9);
+  const unsigned blocks = (unsigned)cdiv(nt, 256);
+  const int key = op.g.ndim * 10 + op.g.ndof;
+  switch (key) {
+    case 33: k_build_fine<3, 3><<<blocks, 256, 0, st>>>(op.g, scale, op.fix, op.KE64, A); break;
+    case 31: k_build_fine<3, 1><<<blocks, 256, 0, st>>>(op.g, scale, op.fix, op.KE64, A); break;
+    case 22: k_build_fine<2, 2><<<blocks, 256, 0, st>>>(op.g, scale, op.fix, op.KE64, A); break;
+    case 21: k_build_fine<2, 1><<<blocks, 256, 0, st>>>(op.g, scale, op.fix, op.KE64, A); break;
     default: throw Error{EINVAL_, "unsupported (ndim, nnode_dof)"};
   }
   TG_CHECK_LAUNCH();
@@ -514,6 +584,7 @@ void gj_inverse(double* D, int64_t n, int64_t ld, double* work, cudaStream_t st)
     k_gj_update<<<dim3(nb, nb), thr, 0, st>>>(D, ld, k, R);
     k_gj_finish<<<nb, thr, 0, st>>>(D, ld, k, P, R);
   }
+  count_launches(4 * (int64_t)nb - 1);
   TG_CHECK_LAUNCH();
 }
 

@@ -63,6 +63,8 @@ void stencil_dinv(const Grid& g, const uint8_t* fix, const T* A, T* dinv, cudaSt
 void build_level1(const FineOp& op, const double* scale, const uint8_t* elem_touch_fixed,
                   const double* Q /* [nchild][NE][NE] */, const Grid& gc,
                   const uint8_t* fixc, double* Ac, cudaStream_t st);
+// fine-level stencil from the element scale factors (fine grid = coarsest level)
+void build_fine_stencil(const FineOp& op, const double* scale, double* A, cudaStream_t st);
 // Galerkin product of an assembled stencil: Ac = M_c P^T A P M_c
 void build_galerkin(const Grid& gf, const double* Af, const Grid& gc, const uint8_t* fixc,
                     double* Ac, cudaStream_t st);

@@ -1,0 +1,98 @@
+// Launch counting and optional CUDA-event timing of one kernel family.
+//
+// The bench reports how many of the library's kernels ran in its timed
+// region (gpu_launches) and the average device time of the dominant kernel,
+// measured with events recorded on the stream that launches it.
+#include <atomic>
+#include <mutex>
+#include <vector>
+#include "tg_common.cuh"
+#include "../../include/topopt_gb300.h"
+
+namespace tg {
+
+static std::atomic<int64_t> g_launches{0};
+void count_launches(int64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+namespace {
+std::mutex g_mu;
+int g_kind = PK_NONE;
+std::vector<cudaEvent_t> g_pool;     // recorded pairs (start, stop)
+size_t g_used = 0;
+int g_open = 0;
+double g_ms = 0.0;
+int64_t g_count = 0;
+
+cudaEvent_t next_event() {
+  if (g_used == g_pool.size()) {
+    cudaEvent_t e;
+    TG_CUDA(cudaEventCreate(&e));
+    g_pool.push_back(e);
+  }
+  return g_pool[g_used++];
+}
+
+// fold finished pairs into the totals once the pool grows large
+void drain_locked() {
+  for (size_t i = 0; i + 1 < g_used; i += 2) {
+    TG_CUDA(cudaEventSynchronize(g_pool[i + 1]));
+    float ms = 0.f;
+    TG_CUDA(cudaEventElapsedTime(&ms, g_pool[i], g_pool[i + 1]));
+    g_ms += ms;
+    g_count += 1;
+  }
+  g_used = 0;
+}
+}  // namespace
+
+void prof_begin(int kind, cudaStream_t st) {
+  if (kind != g_kind || kind == PK_NONE) return;
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (g_used >= 4096 && g_open == 0) drain_locked();
+  TG_CUDA(cudaEventRecord(next_event(), st));
+  g_open = 1;
+}
+
+void prof_end(int kind, cudaStream_t st) {
+  if (kind != g_kind || kind == PK_NONE) return;
+  std::lock_guard<std::mutex> lk(g_mu);
+  TG_CUDA(cudaEventRecord(next_event(), st));
+  g_open = 0;
+}
+
+}  // namespace tg
+
+extern "C" {
+
+int32_t tg_profile_kernel(int32_t kind) {
+  try {
+    std::lock_guard<std::mutex> lk(tg::g_mu);
+    tg::drain_locked();
+    tg::g_kind = kind;
+    tg::g_ms = 0.0;
+    tg::g_count = 0;
+    return TG_OK;
+  } catch (const tg::Error& e) {
+    return e.code;
+  }
+}
+
+int32_t tg_stats(int32_t reset, int64_t* launches, double* prof_ms, int64_t* prof_launches) {
+  try {
+    std::lock_guard<std::mutex> lk(tg::g_mu);
+    tg::drain_locked();
+    if (launches) *launches = tg::g_launches.load();
+    if (prof_ms) *prof_ms = tg::g_ms;
+    if (prof_launches) *prof_launches = tg::g_count;
+    if (reset) {
+      tg::g_launches.store(0);
+      tg::g_ms = 0.0;
+      tg::g_count = 0;
+    }
+    return TG_OK;
+  } catch (const tg::Error& e) {
+    return e.code;
+  }
+}
+
+}  // extern "C"
