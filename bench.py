@@ -1,0 +1,380 @@
+#!/usr/bin/env python
+"""Design iterations per second of the SIMP compliance loop on one GB300.
+
+Workload: 3-D hex8 cantilever, 160 x 80 x 80 elements (1,024,000 elements,
+3,168,963 DOFs), E=1, nu=0.3, volfrac 0.12, penal 3, rmin 1.5, density
+filter, OC; boundary conditions of the reference's cantilever_3d callable
+(x=0 face clamped, z=0 symmetry plane, linearly varying tip line load).
+Every design iteration solves K u = f to an FP64 relative residual of 1e-8.
+
+A step is one design iteration (solve, compliance + sensitivities, filter,
+OC, density filter).  The headline arm is the mixed-precision solver (FP32
+V-cycle and K.u with BF16 densities in the smoother, FP64 residual /
+refinement / dots / compliance / coarsest solve); the plain FP64 GMG-PCG arm
+runs the same iterations for the ratio.  Inputs are synthetic (the reference
+publishes no dataset); the per-iteration working set (~1 GB) exceeds L2, so
+no L2 flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference algorithm's CPU path (the oracle port of
+assembly + SciPy SuperLU direct solve + filter + OC) on the host cores on a
+bounded sample grid and scales it to the workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "design iters/s, 3D hex8 1M elems: learned+mixed vs plain GMG-PCG at res 1e-8"
+UNIT = "design iters/s"
+SIZE = (160, 80, 80)
+VOLFRAC, RMIN, PENAL = 0.12, 1.5, 3.0
+CPU_SAMPLE = (24, 12, 12)
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return None, 0, 1, 0
+    import torch
+    import torch.distributed as dist
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    backend = "nccl" if torch.cuda.is_available() else "gloo"
+    if backend == "nccl":
+        torch.cuda.set_device(local)
+    dist.init_process_group(backend=backend)
+    return dist, rank, ws, local
+
+
+def _barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def _max_over_ranks(dist, v: float) -> float:
+    if dist is None:
+        return v
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = tempfile.mktemp(suffix=".csv")
+
+    def __enter__(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, p[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _problem(precision, device, size=SIZE):
+    from topoptlab_gb300.context import GpuProblem
+    from topoptlab_gb300.elements import lk_linear_elast_3d
+    from topoptlab_gb300.example_bc import cantilever_3d
+    nx, ny, nz = size
+    ndof = 3 * (nx + 1) * (ny + 1) * (nz + 1)
+    _, f, fixed, _, _ = cantilever_3d(nx, ny, nz, ndof)
+    return GpuProblem(nx, ny, nz, lk_linear_elast_3d(), fixed, f[:, 0], VOLFRAC, RMIN, ft=1,
+                      penal=PENAL, precision=precision, rtol=1e-8, device=device)
+
+
+def _fine_bytes(kind, size=SIZE):
+    """Algorithmic HBM bytes of one launch of a fine-grid K.u family."""
+    nx, ny, nz = size
+    nel = nx * ny * nz
+    nnodes = (nx + 1) * (ny + 1) * (nz + 1)
+    ndof = 3 * nnodes
+    if kind == 3:    # FP32 V-cycle smoother sweep, BF16 densities: u, b, dinv in, y out
+        return 4 * 4 * ndof + 2 * nel + nnodes
+    if kind == 2:    # FP32 K.u of the inner PCG: u in, y out, FP32 densities
+        return 2 * 4 * ndof + 4 * nel + nnodes
+    if kind == 1:    # FP64 residual b - K u: u, b in, y out, FP64 densities
+        return 3 * 8 * ndof + 8 * nel + nnodes
+    raise ValueError(kind)
+
+
+def run_ours(args, dist, rank, ws, local):
+    from topoptlab_gb300 import _lib
+    import ctypes as C
+    lib = _lib.load()
+    device = local
+    prof_kind = int(os.environ.get("TG_BENCH_PROF_KIND", "3"))
+
+    # ---------------- mixed precision (headline) ----------------
+    prob = _problem("mixed", device)
+    steps_info = []
+    for _ in range(args.warmup):
+        prob.step()
+    lib.tg_stats(1, None, None, None)
+    lib.tg_profile_kernel(prof_kind)
+    _barrier(dist)
+    with ClockSampler(device) as clk:
+        lib.tg_timer(prob._h, 0, None)
+        for _ in range(args.steps):
+            steps_info.append(prob.step())
+        ms = C.c_double()
+        lib.tg_timer(prob._h, 1, C.byref(ms))
+    t_mixed = ms.value / 1000.0
+    launches, pms, pcount = C.c_int64(), C.c_double(), C.c_int64()
+    lib.tg_stats(1, C.byref(launches), C.byref(pms), C.byref(pcount))
+    lib.tg_profile_kernel(0)
+    t_max = _max_over_ranks(dist, t_mixed)
+    value = args.steps * ws / t_max
+
+    # ---------------- end to end through the public API, host buffers ----------------
+    try:
+        import torch
+        xh = torch.empty(prob.nel, dtype=torch.float64, pin_memory=True).numpy()
+        xp = torch.empty(prob.nel, dtype=torch.float64, pin_memory=True).numpy()
+    except Exception:
+        xh = np.empty(prob.nel)
+        xp = np.empty(prob.nel)
+    xh[:] = prob.get(_lib.TG_FIELD_X)
+    nsteps_e2e = max(1, min(args.steps, 5))
+    _barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(nsteps_e2e):
+        prob.set(_lib.TG_FIELD_X, xh)                 # H2D: the design
+        prob.step()
+        xp[:] = prob.get(_lib.TG_FIELD_XPHYS)         # D2H: the physical densities
+        xh[:] = prob.get(_lib.TG_FIELD_X)             # D2H: the updated design
+    t_e2e = _max_over_ranks(dist, time.perf_counter() - t0)
+    e2e = {"value": nsteps_e2e * ws / t_e2e, "unit": UNIT,
+           "h2d_bytes_per_step": 8 * prob.nel, "d2h_bytes_per_step": 16 * prob.nel,
+           "api": "GpuProblem.set/step/get over the C ABI (tg_set, tg_step, tg_get)"}
+    obj_mixed = [s.obj for s in steps_info]
+    prob.close()
+    if os.environ.get("TG_BENCH_VERBOSE"):
+        for s in steps_info:
+            print("mixed", s, file=sys.stderr)
+
+    # ---------------- plain FP64 GMG-PCG, same iterations ----------------
+    plain = _problem("fp64", device)
+    for _ in range(args.warmup):
+        plain.step()
+    lib.tg_timer(plain._h, 0, None)
+    pinfo = [plain.step() for _ in range(args.steps)]
+    ms2 = C.c_double()
+    lib.tg_timer(plain._h, 1, C.byref(ms2))
+    plain.close()
+    if os.environ.get("TG_BENCH_VERBOSE"):
+        for s in pinfo:
+            print("plain", s, file=sys.stderr)
+    t_plain = _max_over_ranks(dist, ms2.value / 1000.0)
+    value_plain = args.steps * ws / t_plain
+    obj_plain = [s.obj for s in pinfo]
+    obj_diff = max(abs(a - b) / abs(b) for a, b in zip(obj_mixed, obj_plain))
+
+    # ---------------- roofline of the dominant kernel ----------------
+    peaks = {}
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        peaks = json.load(open(pk))
+    peak_hbm = peaks.get("hbm_gbs", 6800.0)
+    avg_s = (pms.value / 1000.0 / pcount.value) if pcount.value else float("nan")
+    nbytes = _fine_bytes(prof_kind)
+    achieved = nbytes / avg_s / 1e9 if pcount.value else None
+    roofline = {"kernel": {1: "k_fine_apply FP64 residual", 2: "k_fine_apply FP32 K.u",
+                           3: "k_fine_apply FP32 Jacobi sweep (BF16 densities)"}.get(prof_kind),
+                "bound": "hbm", "achieved": achieved, "peak": peak_hbm, "unit": "GB/s",
+                "frac": (achieved / peak_hbm) if achieved else None,
+                "traffic": None, "launches": pcount.value,
+                "avg_launch_us": avg_s * 1e6 if pcount.value else None,
+                "algorithmic_bytes_per_launch": nbytes,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if peaks else "fallback"}
+
+    if rank != 0:
+        return None
+    mean = lambda k, L: float(np.mean([getattr(s, k) for s in L]))
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * t_max / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64+f32+bf16", "data": "synthetic",
+        "config": {"workload": "3-D hex8 cantilever 160x80x80 (1,024,000 elements, "
+                               "3,168,963 DOFs), volfrac 0.12, rmin 1.5, ft=1, OC, "
+                               "FP64 relative residual 1e-8",
+                   "solver": "mixed-precision GMG-PCG (FP32 V-cycle, BF16 smoother densities, "
+                             "FP64 refinement), 5 levels, 2 damped-Jacobi sweeps omega 0.6",
+                   "learned_warm_start": False,
+                   "design_iterations_timed": f"{args.warmup + 1}..{args.warmup + args.steps}",
+                   "l2": "working set > L2 (126 MB); no flush",
+                   "parallelism": f"replicas x{ws}"},
+        "e2e": e2e,
+        "gpu_launches": int(launches.value),
+        "roofline": roofline,
+        "plain_fp64": {"value": value_plain, "ms_per_step": 1000.0 * t_plain / args.steps,
+                       "pcg_iters_per_step": mean("pcg_iters", pinfo),
+                       "max_rel_res": max(s.rel_res for s in pinfo)},
+        "mixed": {"pcg_iters_per_step": mean("pcg_iters", steps_info),
+                  "refinements_per_step": mean("refinements", steps_info),
+                  "max_rel_res": max(s.rel_res for s in steps_info),
+                  "solve_ms_per_step": mean("t_solve_ms", steps_info)},
+        "ratio_vs_plain_fp64": value / value_plain,
+        "compliance_max_rel_diff_vs_fp64": obj_diff,
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(steps=2, warmup=1)
+    return line
+
+
+def _cpu_step_factory(size=CPU_SAMPLE):
+    """One design iteration of the reference algorithm on the CPU (oracle port:
+    COO->CSR assembly, Dirichlet slicing, SciPy SuperLU spsolve, compliance,
+    sensitivity / density filter, OC), state carried between calls."""
+    from oracle import topopt as O
+    nx, ny, nz = size
+    KE = O.ke_elast(3)
+    fixed, f = O.bc_cantilever_3d(nx, ny, nz)
+    edof = O.edofmat(nx, ny, nz, 3)
+    H, Hs = O.filter_matrix(nx, ny, nz, RMIN)
+    ndof = f.shape[0]
+    nel = nx * ny * nz
+    free = np.setdiff1d(np.arange(ndof), fixed)
+    st = {"x": np.full(nel, VOLFRAC), "xPhys": np.full(nel, VOLFRAC), "g": 0.0}
+    dv = np.asarray(H @ (np.ones(nel) / Hs))
+
+    def step():
+        K = O.assemble(KE, edof, O.simp(st["xPhys"]), ndof)
+        u = O.solve_direct(K, f, free)
+        obj, dc, _ = O.compliance_sens(st["xPhys"], u, KE, edof)
+        dc = np.asarray(H @ (dc / Hs))
+        st["x"], st["g"], _ = O.oc_top88(st["x"], dc, dv, st["g"])
+        st["xPhys"] = np.asarray(H @ st["x"]) / Hs
+        return obj
+    return step, nel
+
+
+def cpu_baseline(steps=2, warmup=1):
+    step, nel = _cpu_step_factory()
+    for _ in range(warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    t = (time.perf_counter() - t0) / steps
+    scale = (SIZE[0] * SIZE[1] * SIZE[2]) / nel
+    return {"value": 1.0 / (t * scale), "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"3-D cantilever {CPU_SAMPLE[0]}x{CPU_SAMPLE[1]}x{CPU_SAMPLE[2]} "
+                      f"({nel} elements) with the reference algorithm (SciPy SuperLU direct "
+                      f"solve), {t:.2f} s per design iteration, scaled linearly by element "
+                      f"count x{scale:.0f} to 160x80x80 (an upper bound on CPU throughput: "
+                      f"direct-solve fill grows faster than linearly)",
+            "seconds_per_iteration_sample": t}
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return None
+    step, nel = _cpu_step_factory()
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    t = (time.perf_counter() - t0) / args.steps
+    scale = (SIZE[0] * SIZE[1] * SIZE[2]) / nel
+    value = 1.0 / (t * scale)
+    return {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * t * scale,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": "3-D hex8 cantilever 160x80x80 (1,024,000 elements), "
+                               "volfrac 0.12, rmin 1.5, ft=1, OC",
+                   "sample_grid": "x".join(map(str, CPU_SAMPLE)),
+                   "solver": "SciPy SuperLU direct solve (reference default scipy-direct)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
+                         "sample": f"each step one design iteration of the reference "
+                                   f"algorithm on the {CPU_SAMPLE[0]}x{CPU_SAMPLE[1]}x"
+                                   f"{CPU_SAMPLE[2]} cantilever ({nel} elements, {t:.2f} s), "
+                                   f"scaled linearly by element count to 160x80x80"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" else max(args.warmup, 1)
+    dist, rank, ws, local = _dist()
+    if args.impl == "reference":
+        line = run_reference(args, rank)
+    else:
+        line = run_ours(args, dist, rank, ws, local)
+    if line is not None:
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()
