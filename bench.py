@@ -129,7 +129,8 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def _problem(precision, device, size=SIZE):
+def _problem(precision, device, size=None):
+    size = size or SIZE
     from topoptlab_gb300.context import GpuProblem
     from topoptlab_gb300.elements import lk_linear_elast_3d
     from topoptlab_gb300.example_bc import cantilever_3d
@@ -140,9 +141,9 @@ def _problem(precision, device, size=SIZE):
                       penal=PENAL, precision=precision, rtol=1e-8, device=device)
 
 
-def _fine_bytes(kind, size=SIZE):
+def _fine_bytes(kind, size=None):
     """Algorithmic HBM bytes of one launch of a fine-grid K.u family."""
-    nx, ny, nz = size
+    nx, ny, nz = size or SIZE
     nel = nx * ny * nz
     nnodes = (nx + 1) * (ny + 1) * (nz + 1)
     ndof = 3 * nnodes
@@ -363,7 +364,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--size", default=None,
+                    help="override the grid, e.g. 80,40,40 (profiling runs only)")
     args = ap.parse_args()
+    if args.size:
+        global SIZE
+        SIZE = tuple(int(v) for v in args.size.split(","))
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else max(args.warmup, 1)
     dist, rank, ws, local = _dist()
     if args.impl == "reference":

@@ -131,6 +131,8 @@ int32_t tg_kmul(tg_ctx* ctx, const double* xPhys, const double* u, double* y, in
     const int64_t nel = c.g.nel(), nd = c.g.ndofs();
     h2d(c.xnew.p, xPhys, nel, c.st);
     h2d(c.r.p, u, nd, c.st);
+    // the operator expects inputs that are zero on fixed DOFs
+    tg::mask_vec_f64(c.g.nnodes(), c.g.ndof, c.op.fix, c.r, c.st);
     if (precision == TG_PREC_FP64) {
       tg::simp_scale(nel, c.xnew, c.eps, c.penal, c.s64, nullptr, nullptr, c.st);
       tg::fine_apply<double, double>(c.op, c.s64, c.r, c.q, nullptr, nullptr, 0.0, tg::AM_Y, c.st);

@@ -98,43 +98,75 @@ template <int NDIM, int NDOF, typename T, bool SECTOR>
 constexpr size_t apply_smem() {
   using TL = Tile<NDIM>;
   constexpr int HZ = (NDIM == 3) ? TL::Z + 2 : 1;
+  constexpr int EZ = (NDIM == 3) ? TL::Z + 1 : 1;
   constexpr int NE = (1 << NDIM) * NDOF;
   return sizeof(T) * ((size_t)HZ * (TL::X + 2) * (TL::Y + 2) * NDOF +
-                      (size_t)TL::Z * TL::X * TL::Y * NDOF + (SECTOR ? 0 : NE * NE));
+                      (size_t)TL::Z * TL::X * TL::Y * NDOF + (SECTOR ? 0 : NE * NE) +
+                      (size_t)EZ * (TL::X + 1) * (TL::Y + 1));
 }
 
+// asynchronous global -> shared copies (all of a thread's copies in flight at once)
+template <int BYTES> __device__ __forceinline__ void cp_async(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  if (BYTES == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
+
+// The input u must be zero on fixed DOFs (every producer in the library keeps
+// that invariant; the unit entry point masks its input explicitly), so the
+// halo is a plain copy; the output is masked in the epilogue.
 template <int NDIM, int NDOF, typename T, typename S, bool SECTOR, int MODE>
 __global__ void __launch_bounds__(256) k_fine_apply(ApplyArgs<T, S> a) {
   using TL = Tile<NDIM>;
   constexpr int TX = TL::X, TY = TL::Y, TZ = TL::Z;
   constexpr int HX = TX + 2, HY = TY + 2, HZ = (NDIM == 3) ? TZ + 2 : 1;
+  constexpr int EX = TX + 1, EY = TY + 1, EZ = (NDIM == 3) ? TZ + 1 : 1;
   constexpr int NC = 1 << NDIM;
   constexpr int NE = NC * NDOF;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* us = reinterpret_cast<T*>(smem_raw);       // [HZ][HX][HY][NDOF]
   T* ys = us + HZ * HX * HY * NDOF;              // [TZ][TX][TY][NDOF]
-  T* KEs = ys + TZ * TX * TY * NDOF;             // dense path only
+  T* rs = ys + TZ * TX * TY * NDOF;              // [EZ][EX][EY] element scale factors
+  T* KEs = rs + EZ * EX * EY;                    // dense path only
   const Grid& g = a.g;
   const int y0 = blockIdx.x * TY, x0 = blockIdx.y * TX, z0 = blockIdx.z * TZ;
   const int tid = threadIdx.x, nth = blockDim.x;
 
-  // stage u (masked) with a one-node halo
+  // stage u with a one-node halo
   for (int i = tid; i < HZ * HX * HY * NDOF; i += nth) {
     const int c = i % NDOF;
     const int hy = (i / NDOF) % HY;
     const int hx = (i / (NDOF * HY)) % HX;
     const int hz = i / (NDOF * HY * HX);
     const int gx = x0 - 1 + hx, gy = y0 - 1 + hy, gz = (NDIM == 3) ? z0 - 1 + hz : 0;
-    T v = T(0);
-    if (gx >= 0 && gx < g.nnx && gy >= 0 && gy < g.nny && gz >= 0 && gz < g.nnz) {
-      const int64_t n = g.node(gx, gy, gz);
-      if (!((a.fix[n] >> c) & 1)) v = a.u[n * NDOF + c];
+    if (gx >= 0 && gx < g.nnx && gy >= 0 && gy < g.nny && gz >= 0 && gz < g.nnz)
+      cp_async<sizeof(T)>(us + i, a.u + g.node(gx, gy, gz) * NDOF + c);
+    else
+      us[i] = T(0);
+  }
+  // stage the scale factors of the elements touching the tile
+  for (int i = tid; i < EZ * EX * EY; i += nth) {
+    const int ly = i % EY, lx = (i / EY) % EX, lz = i / (EY * EX);
+    const int ex = x0 - 1 + lx, ey = y0 - 1 + ly, ez = (NDIM == 3) ? z0 - 1 + lz : 0;
+    if (ex >= 0 && ex < g.nex && ey >= 0 && ey < g.ney && ez >= 0 && ez < g.nez) {
+      if (sizeof(S) == sizeof(T))
+        cp_async<sizeof(T)>(rs + i, a.scale + g.elem(ex, ey, ez));
+      else
+        rs[i] = load_scale<T, S>(a.scale, g.elem(ex, ey, ez));
+    } else {
+      rs[i] = T(0);
     }
-    us[i] = v;
   }
   for (int i = tid; i < TZ * TX * TY * NDOF; i += nth) ys[i] = T(0);
   if (!SECTOR)
     for (int i = tid; i < NE * NE; i += nth) KEs[i] = a.KE[i];
+  cp_async_wait_all();
   __syncthreads();
 
   // elements with local coords l in [0, T+1): global = origin - 1 + l
@@ -149,7 +181,7 @@ __global__ void __launch_bounds__(256) k_fine_apply(ApplyArgs<T, S> a) {
       const int lz = (NDIM == 3) ? cz + 2 * (t / (nyc * nxc)) : 0;
       const int ex = x0 - 1 + lx, ey = y0 - 1 + ly, ez = (NDIM == 3) ? z0 - 1 + lz : 0;
       if (ex < 0 || ex >= g.nex || ey < 0 || ey >= g.ney || ez < 0 || ez >= g.nez) continue;
-      const T rho = load_scale<T, S>(a.scale, g.elem(ex, ey, ez));
+      const T rho = rs[(lz * EX + lx) * EY + ly];
       T ue[NC][NDOF], ye[NC][NDOF];
 #pragma unroll
       for (int d = 0; d < NC; ++d) {
@@ -183,19 +215,19 @@ __global__ void __launch_bounds__(256) k_fine_apply(ApplyArgs<T, S> a) {
     if (gx >= g.nnx || gy >= g.nny || gz >= g.nnz) continue;
     const int64_t n = g.node(gx, gy, gz);
     const int64_t k = n * NDOF + c;
-    T out = T(0);
-    if (!((a.fix[n] >> c) & 1)) {
-      const T au = ys[i];
-      if (MODE == AM_Y) {
-        out = au;
-      } else if (MODE == AM_RES) {
-        out = a.b[k] - au;
-      } else {
-        const T uc = us[(((NDIM == 3 ? oz + 1 : 0) * HX + ox + 1) * HY + oy + 1) * NDOF + c];
-        out = uc + a.omega * a.dinv[k] * (a.b[k] - au);
-      }
+    // loads issued without a dependency on the fixed flag; the flag selects
+    const bool fixed = (a.fix[n] >> c) & 1;
+    const T au = ys[i];
+    T out;
+    if (MODE == AM_Y) {
+      out = au;
+    } else if (MODE == AM_RES) {
+      out = a.b[k] - au;
+    } else {
+      const T uc = us[(((NDIM == 3 ? oz + 1 : 0) * HX + ox + 1) * HY + oy + 1) * NDOF + c];
+      out = uc + a.omega * a.dinv[k] * (a.b[k] - au);
     }
-    a.y[k] = out;
+    a.y[k] = fixed ? T(0) : out;
   }
 }
 
