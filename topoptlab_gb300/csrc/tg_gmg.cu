@@ -506,19 +506,24 @@ constexpr int GJB = 32;
 
 // invert the k-th diagonal block (SPD, no pivoting) into P (GJB x GJB)
 __global__ void __launch_bounds__(GJB * GJB) k_gj_pivot(const double* D, int64_t ld, int k, double* P) {
+  // GB300's FP64 pipe is narrow: one reciprocal per step (not one divide per
+  // thread), everything else is multiply / FMA
   __shared__ double a[GJB][GJB + 1];
+  __shared__ double rpiv;
   const int i = threadIdx.y, j = threadIdx.x;
   a[i][j] = D[(int64_t)(k * GJB + i) * ld + k * GJB + j];
   __syncthreads();
   for (int p = 0; p < GJB; ++p) {
-    const double piv = a[p][p];
+    if (i == 0 && j == 0) rpiv = 1.0 / a[p][p];
+    __syncthreads();
+    const double rp = rpiv;
     const double aip = a[i][p], apj = a[p][j];
     __syncthreads();
     double v;
-    if (i == p && j == p) v = 1.0 / piv;
-    else if (i == p) v = apj / piv;
-    else if (j == p) v = -aip / piv;
-    else v = a[i][j] - aip * apj / piv;
+    if (i == p && j == p) v = rp;
+    else if (i == p) v = apj * rp;
+    else if (j == p) v = -aip * rp;
+    else v = fma(-aip, apj * rp, a[i][j]);
     a[i][j] = v;
     __syncthreads();
   }
