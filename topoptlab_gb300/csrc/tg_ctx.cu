@@ -485,15 +485,17 @@ void solve(Ctx& c, const double* b, double* u) {
     c.last_vcycles = (c.precond == TG_PRECOND_GMG) ? it : 0;
     c.last_converged = conv;
   } else {
-    // FP64 iterative refinement around the FP32 PCG
+    // FP64 iterative refinement around the FP32 PCG; every pass starts from
+    // the true FP64 residual, so the last one is the reported residual
     int total = 0;
     bool conv = false;
+    double rr = 0.0;
     for (int k = 0; k < 64 && total < c.maxiter; ++k) {
       fine_apply<double, double>(c.op, c.s64, u, c.r, b, nullptr, 0.0, AM_RES, c.st);
       pcg_reset(c.pcg_out, c.st);
       dot<double, double>(n, c.r.p, c.r.p, c.part, c.pcg_out, DOT_RR, c.st);
       read_pcg(c, c.pcg_out);
-      const double rr = c.h_pcg->rr;
+      rr = c.h_pcg->rr;
       check_finite(rr, "FP64 residual");
       if (std::sqrt(rr) < tol) {
         conv = true;
@@ -508,13 +510,16 @@ void solve(Ctx& c, const double* b, double* u) {
     c.last_iters = total;
     c.last_vcycles = (c.precond == TG_PRECOND_GMG) ? total : 0;
     c.last_converged = conv;
+    if (conv) c.last_relres = std::sqrt(rr) / bnorm;
   }
-  // true FP64 residual
-  fine_apply<double, double>(c.op, c.s64, u, c.r, b, nullptr, 0.0, AM_RES, c.st);
-  pcg_reset(c.pcg_out, c.st);
-  dot<double, double>(n, c.r.p, c.r.p, c.part, c.pcg_out, DOT_RR, c.st);
-  read_pcg(c, c.pcg_out);
-  c.last_relres = std::sqrt(c.h_pcg->rr) / bnorm;
+  if (c.precision == TG_PREC_FP64 || !c.last_converged) {
+    // true FP64 residual (the FP64 PCG's recursive residual can drift from it)
+    fine_apply<double, double>(c.op, c.s64, u, c.r, b, nullptr, 0.0, AM_RES, c.st);
+    pcg_reset(c.pcg_out, c.st);
+    dot<double, double>(n, c.r.p, c.r.p, c.part, c.pcg_out, DOT_RR, c.st);
+    read_pcg(c, c.pcg_out);
+    c.last_relres = std::sqrt(c.h_pcg->rr) / bnorm;
+  }
   if (!c.last_converged)
     throw Error{ENOTCONV, "gb300 pcg iteration did not converge (iterations: " +
                               std::to_string(c.last_iters) +

@@ -121,73 +121,105 @@ __device__ __forceinline__ void cp_async_wait_all() {
 // The input u must be zero on fixed DOFs (every producer in the library keeps
 // that invariant; the unit entry point masks its input explicitly), so the
 // halo is a plain copy; the output is masked in the epilogue.
-template <int NDIM, int NDOF, typename T, typename S, bool SECTOR, int MODE>
-__global__ void __launch_bounds__(256) k_fine_apply(ApplyArgs<T, S> a) {
+// Shared-memory layout of a node tile (halo included): component-major, and
+// each y-row split into even and odd y so that the 2-strided accesses of one
+// colour pass hit consecutive words; the half-row pitch is padded so that
+// neighbouring x-rows of a warp land on different banks.
+template <int NDIM> struct SLayout {
   using TL = Tile<NDIM>;
+  static constexpr int HX = TL::X + 2, HY = TL::Y + 2, HZ = (NDIM == 3) ? TL::Z + 2 : 1;
+  static constexpr int HH = HY / 2 + (NDIM == 3 ? 1 : 3);          // half-row pitch
+  static constexpr int ROWS = HZ * HX;
+  static constexpr int NODE_WORDS = ROWS * 2 * HH;                  // per component
+  __device__ static constexpr int at(int c, int hz, int hx, int hy) {
+    return c * NODE_WORDS + (hz * HX + hx) * 2 * HH + (hy & 1) * HH + (hy >> 1);
+  }
+  // element scale factors, same parity split along y
+  static constexpr int EX = TL::X + 1, EY = TL::Y + 1, EZ = (NDIM == 3) ? TL::Z + 1 : 1;
+  static constexpr int EH = (EY + 1) / 2 + 1;
+  static constexpr int ELEM_WORDS = EZ * EX * 2 * EH;
+  __device__ static constexpr int eat(int lz, int lx, int ly) {
+    return (lz * EX + lx) * 2 * EH + (ly & 1) * EH + (ly >> 1);
+  }
+};
+
+template <int NDIM, int NDOF, typename T, bool SECTOR>
+constexpr size_t apply_smem_v2() {
+  using L = SLayout<NDIM>;
+  constexpr int NE = (1 << NDIM) * NDOF;
+  return sizeof(T) * ((size_t)2 * NDOF * L::NODE_WORDS + L::ELEM_WORDS + (SECTOR ? 0 : NE * NE));
+}
+
+template <int NDIM, int NDOF, typename T, typename S, bool SECTOR, int MODE>
+__global__ void __launch_bounds__(256, sizeof(T) == 8 ? 2 : 4) k_fine_apply(ApplyArgs<T, S> a) {
+  using TL = Tile<NDIM>;
+  using L = SLayout<NDIM>;
   constexpr int TX = TL::X, TY = TL::Y, TZ = TL::Z;
-  constexpr int HX = TX + 2, HY = TY + 2, HZ = (NDIM == 3) ? TZ + 2 : 1;
-  constexpr int EX = TX + 1, EY = TY + 1, EZ = (NDIM == 3) ? TZ + 1 : 1;
+  constexpr int HX = L::HX, HY = L::HY, HZ = L::HZ;
+  constexpr int EX = L::EX, EY = L::EY, EZ = L::EZ;
   constexpr int NC = 1 << NDIM;
   constexpr int NE = NC * NDOF;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* us = reinterpret_cast<T*>(smem_raw);       // [HZ][HX][HY][NDOF]
-  T* ys = us + HZ * HX * HY * NDOF;              // [TZ][TX][TY][NDOF]
-  T* rs = ys + TZ * TX * TY * NDOF;              // [EZ][EX][EY] element scale factors
-  T* KEs = rs + EZ * EX * EY;                    // dense path only
+  T* us = reinterpret_cast<T*>(smem_raw);       // u tile with halo
+  T* ys = us + NDOF * L::NODE_WORDS;             // accumulator, same shape (halo discarded)
+  T* rs = ys + NDOF * L::NODE_WORDS;             // element scale factors
+  T* KEs = rs + L::ELEM_WORDS;                   // dense path only
   const Grid& g = a.g;
   const int y0 = blockIdx.x * TY, x0 = blockIdx.y * TX, z0 = blockIdx.z * TZ;
   const int tid = threadIdx.x, nth = blockDim.x;
 
-  // stage u with a one-node halo
+  // stage u with a one-node halo (global order for coalescing)
   for (int i = tid; i < HZ * HX * HY * NDOF; i += nth) {
     const int c = i % NDOF;
     const int hy = (i / NDOF) % HY;
     const int hx = (i / (NDOF * HY)) % HX;
     const int hz = i / (NDOF * HY * HX);
     const int gx = x0 - 1 + hx, gy = y0 - 1 + hy, gz = (NDIM == 3) ? z0 - 1 + hz : 0;
+    T* dst = us + L::at(c, hz, hx, hy);
     if (gx >= 0 && gx < g.nnx && gy >= 0 && gy < g.nny && gz >= 0 && gz < g.nnz)
-      cp_async<sizeof(T)>(us + i, a.u + g.node(gx, gy, gz) * NDOF + c);
+      cp_async<sizeof(T)>(dst, a.u + g.node(gx, gy, gz) * NDOF + c);
     else
-      us[i] = T(0);
+      *dst = T(0);
   }
   // stage the scale factors of the elements touching the tile
   for (int i = tid; i < EZ * EX * EY; i += nth) {
     const int ly = i % EY, lx = (i / EY) % EX, lz = i / (EY * EX);
     const int ex = x0 - 1 + lx, ey = y0 - 1 + ly, ez = (NDIM == 3) ? z0 - 1 + lz : 0;
+    T* dst = rs + L::eat(lz, lx, ly);
     if (ex >= 0 && ex < g.nex && ey >= 0 && ey < g.ney && ez >= 0 && ez < g.nez) {
       if (sizeof(S) == sizeof(T))
-        cp_async<sizeof(T)>(rs + i, a.scale + g.elem(ex, ey, ez));
+        cp_async<sizeof(T)>(dst, a.scale + g.elem(ex, ey, ez));
       else
-        rs[i] = load_scale<T, S>(a.scale, g.elem(ex, ey, ez));
+        *dst = load_scale<T, S>(a.scale, g.elem(ex, ey, ez));
     } else {
-      rs[i] = T(0);
+      *dst = T(0);
     }
   }
-  for (int i = tid; i < TZ * TX * TY * NDOF; i += nth) ys[i] = T(0);
+  for (int i = tid; i < NDOF * L::NODE_WORDS; i += nth) ys[i] = T(0);
   if (!SECTOR)
     for (int i = tid; i < NE * NE; i += nth) KEs[i] = a.KE[i];
   cp_async_wait_all();
   __syncthreads();
 
-  // elements with local coords l in [0, T+1): global = origin - 1 + l
-#pragma unroll 1
+  // elements with local coords l in [0, T+1) (global = origin - 1 + l), in
+  // 2^ndim colour passes; the accumulator covers the halo, so corners need no
+  // bounds test.  Elements outside the grid have rho = 0 and u = 0.
+#pragma unroll
   for (int col = 0; col < NC; ++col) {
     const int cx = col & 1, cy = (col >> 1) & 1, cz = (col >> 2) & 1;
-    const int nyc = (TY + 1 - cy + 1) / 2, nxc = (TX + 1 - cx + 1) / 2;
-    const int nzc = (NDIM == 3) ? (TZ + 1 - cz + 1) / 2 : 1;
+    const int nyc = (EY - cy + 1) / 2, nxc = (EX - cx + 1) / 2;
+    const int nzc = (NDIM == 3) ? (EZ - cz + 1) / 2 : 1;
     for (int t = tid; t < nyc * nxc * nzc; t += nth) {
       const int ly = cy + 2 * (t % nyc);
       const int lx = cx + 2 * ((t / nyc) % nxc);
       const int lz = (NDIM == 3) ? cz + 2 * (t / (nyc * nxc)) : 0;
-      const int ex = x0 - 1 + lx, ey = y0 - 1 + ly, ez = (NDIM == 3) ? z0 - 1 + lz : 0;
-      if (ex < 0 || ex >= g.nex || ey < 0 || ey >= g.ney || ez < 0 || ez >= g.nez) continue;
-      const T rho = rs[(lz * EX + lx) * EY + ly];
+      const T rho = rs[L::eat(lz, lx, ly)];
       T ue[NC][NDOF], ye[NC][NDOF];
 #pragma unroll
       for (int d = 0; d < NC; ++d) {
         const int hx = lx + (d & 1), hy = ly + ((d >> 1) & 1), hz = (NDIM == 3) ? lz + ((d >> 2) & 1) : 0;
 #pragma unroll
-        for (int c = 0; c < NDOF; ++c) ue[d][c] = us[((hz * HX + hx) * HY + hy) * NDOF + c];
+        for (int c = 0; c < NDOF; ++c) ue[d][c] = us[L::at(c, hz, hx, hy)];
       }
       if (SECTOR)
         elem_sector<NDIM, NDOF, T>(ue, a.B, rho, ye);
@@ -195,17 +227,15 @@ __global__ void __launch_bounds__(256) k_fine_apply(ApplyArgs<T, S> a) {
         elem_dense<NDIM, NDOF, T>(ue, KEs, rho, ye);
 #pragma unroll
       for (int d = 0; d < NC; ++d) {
-        const int ox = lx + (d & 1) - 1, oy = ly + ((d >> 1) & 1) - 1;
-        const int oz = (NDIM == 3) ? lz + ((d >> 2) & 1) - 1 : 0;
-        if (ox < 0 || ox >= TX || oy < 0 || oy >= TY || oz < 0 || oz >= TZ) continue;
+        const int hx = lx + (d & 1), hy = ly + ((d >> 1) & 1), hz = (NDIM == 3) ? lz + ((d >> 2) & 1) : 0;
 #pragma unroll
-        for (int c = 0; c < NDOF; ++c) ys[((oz * TX + ox) * TY + oy) * NDOF + c] += ye[d][c];
+        for (int c = 0; c < NDOF; ++c) ys[L::at(c, hz, hx, hy)] += ye[d][c];
       }
     }
     __syncthreads();
   }
 
-  // epilogue: owned nodes
+  // epilogue: owned nodes (interior of the halo tile)
   for (int i = tid; i < TZ * TX * TY * NDOF; i += nth) {
     const int c = i % NDOF;
     const int oy = (i / NDOF) % TY;
@@ -215,17 +245,17 @@ __global__ void __launch_bounds__(256) k_fine_apply(ApplyArgs<T, S> a) {
     if (gx >= g.nnx || gy >= g.nny || gz >= g.nnz) continue;
     const int64_t n = g.node(gx, gy, gz);
     const int64_t k = n * NDOF + c;
+    const int s = L::at(c, (NDIM == 3) ? oz + 1 : 0, ox + 1, oy + 1);
     // loads issued without a dependency on the fixed flag; the flag selects
     const bool fixed = (a.fix[n] >> c) & 1;
-    const T au = ys[i];
+    const T au = ys[s];
     T out;
     if (MODE == AM_Y) {
       out = au;
     } else if (MODE == AM_RES) {
       out = a.b[k] - au;
     } else {
-      const T uc = us[(((NDIM == 3 ? oz + 1 : 0) * HX + ox + 1) * HY + oy + 1) * NDOF + c];
-      out = uc + a.omega * a.dinv[k] * (a.b[k] - au);
+      out = us[s] + a.omega * a.dinv[k] * (a.b[k] - au);
     }
     a.y[k] = fixed ? T(0) : out;
   }
@@ -234,7 +264,7 @@ __global__ void __launch_bounds__(256) k_fine_apply(ApplyArgs<T, S> a) {
 template <int NDIM, int NDOF, typename T, typename S, bool SECTOR, int MODE>
 static void launch_apply(const ApplyArgs<T, S>& a, cudaStream_t st) {
   using TL = Tile<NDIM>;
-  constexpr size_t smem = apply_smem<NDIM, NDOF, T, SECTOR>();
+  constexpr size_t smem = apply_smem_v2<NDIM, NDOF, T, SECTOR>();
   auto kern = k_fine_apply<NDIM, NDOF, T, S, SECTOR, MODE>;
   static bool attr_set = false;   // per instantiation; attribute is per function
   if (!attr_set) {

@@ -45,19 +45,22 @@ __device__ __forceinline__ bool in_grid(const Grid& g, int x, int y, int z) {
 // ---------------------------------------------------------------------------
 // stencil mat-vec with fused residual / Jacobi epilogues
 // ---------------------------------------------------------------------------
+// one thread per (row component ci, node): coalesced coefficient loads (the
+// node index is fastest), NDOF times the parallelism of a thread per node,
+// which matters on the small coarse grids
 template <int NDIM, int NDOF, typename T, int MODE>
 __global__ void __launch_bounds__(256) k_stencil_apply(Grid g, const T* __restrict__ A,
                                                       const T* __restrict__ u, T* __restrict__ y,
                                                       const T* __restrict__ b,
                                                       const T* __restrict__ dinv, T omega) {
-  const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t ld = g.nnodes();
-  if (n >= ld) return;
+  if (t >= ld * NDOF) return;
+  const int ci = (int)(t / ld);
+  const int64_t n = t - (int64_t)ci * ld;
   int x, yy, z;
   node_xyz(g, n, x, yy, z);
-  T acc[NDOF];
-#pragma unroll
-  for (int c = 0; c < NDOF; ++c) acc[c] = T(0);
+  T acc = T(0);
 #pragma unroll
   for (int d = 0; d < ndir<NDIM>(); ++d) {
     int dx, dy, dz;
@@ -65,27 +68,21 @@ __global__ void __launch_bounds__(256) k_stencil_apply(Grid g, const T* __restri
     if (!in_grid(g, x + dx, yy + dy, z + dz)) continue;
     const int64_t m = g.node(x + dx, yy + dy, z + dz);
 #pragma unroll
-    for (int cj = 0; cj < NDOF; ++cj) {
-      const T uj = __ldg(u + m * NDOF + cj);
-#pragma unroll
-      for (int ci = 0; ci < NDOF; ++ci) acc[ci] += __ldg(A + ((d * NDOF + ci) * NDOF + cj) * ld + n) * uj;
-    }
+    for (int cj = 0; cj < NDOF; ++cj)
+      acc += __ldg(A + ((d * NDOF + ci) * NDOF + cj) * ld + n) * __ldg(u + m * NDOF + cj);
   }
-#pragma unroll
-  for (int c = 0; c < NDOF; ++c) {
-    const int64_t k = n * NDOF + c;
-    T out;
-    if (MODE == AM_Y) out = acc[c];
-    else if (MODE == AM_RES) out = b[k] - acc[c];
-    else out = u[k] + omega * dinv[k] * (b[k] - acc[c]);
-    y[k] = out;
-  }
+  const int64_t k = n * NDOF + ci;
+  T out;
+  if (MODE == AM_Y) out = acc;
+  else if (MODE == AM_RES) out = b[k] - acc;
+  else out = u[k] + omega * dinv[k] * (b[k] - acc);
+  y[k] = out;
 }
 
 template <typename T>
 void stencil_apply(const Grid& g, const T* A, const T* u, T* y, const T* b, const T* dinv,
                    double omega, int mode, cudaStream_t st) {
-  const unsigned blocks = (unsigned)cdiv(g.nnodes(), 256);
+  const unsigned blocks = (unsigned)cdiv(g.nnodes() * g.ndof, 256);
   const int key = g.ndim * 10 + g.ndof;
   const int pk = sizeof(T) == 8 ? PK_STENCIL_F64 : PK_STENCIL_F32;
   prof_begin(pk, st);
