@@ -137,6 +137,24 @@ int32_t tg_oc(tg_ctx* ctx, const double* x, const double* dc, const double* dv, 
 int32_t tg_oc_raw(int64_t n, const double* x, const double* dc, const double* dv, double g,
                   const int8_t* el_flags, double move, double l1, double l2, double* xnew,
                   double* gt, int32_t* nsteps, int32_t device);
+/* Allocation-free OC update.  No counterpart in the reference: it exists for
+ * callers that cannot allocate device memory themselves -- applications
+ * whose device memory belongs to their own pool allocator, or code that must
+ * not change the device's allocation state while its other work runs.  x, dc,
+ * dv, el_flags (may be NULL) and xnew are DEVICE pointers owned by the caller;
+ * gt and nsteps are host pointers.  The only extra device memory is a static
+ * array inside the library sized for TG_NOALLOC_MAX_N design variables; larger
+ * n returns TG_EINVAL.  The array is shared by all calls and keeps the last
+ * call's contents, so calls that overlap on the GPU race and must be
+ * serialised by the caller.  The first call on each device looks up the
+ * array's device address; make it before any stream capture.  stream is a
+ * cudaStream_t (NULL = legacy default stream).  Errors: message from
+ * tg_noalloc_last_error(). */
+#define TG_NOALLOC_MAX_N 2097152
+int32_t tg_oc_noalloc(int64_t n, const double* x, const double* dc, const double* dv, double g,
+                      const int8_t* el_flags, double move, double l1, double l2, double* xnew,
+                      double* gt, int32_t* nsteps, void* stream);
+const char* tg_noalloc_last_error(void);
 /* one multigrid V-cycle x = V(b) for the densities xPhys */
 int32_t tg_vcycle(tg_ctx* ctx, const double* xPhys, const double* b, double* x, int32_t precision);
 /* number of multigrid levels and the DOF count of one level */

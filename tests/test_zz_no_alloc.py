@@ -1,0 +1,66 @@
+"""The allocation-free OC entry point (tg_oc_noalloc) against the allocating
+one (tg_oc_raw), through the C ABI.
+
+tg_oc_noalloc serves callers that cannot allocate device memory themselves
+(their device memory belongs to their own pool allocator, or they must not
+change the device's allocation state while their other work runs): the
+caller passes device buffers for inputs and outputs, and the library's only
+extra memory is a static device array.  Two calls in a row must reproduce
+the allocating entry point, which also shows that the shared scratch array
+left behind by the first call does not leak into the second.  This file is
+named so that pytest collects it last."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _inputs(rng, n):
+    x = rng.uniform(0.05, 0.95, n)
+    dc = -rng.uniform(0.01, 3.0, n)
+    dv = rng.uniform(0.5, 1.5, n)
+    flags = rng.integers(0, 3, n).astype(np.int8)
+    flags[rng.uniform(size=n) < 0.8] = 0
+    return x, dc, dv, flags
+
+
+def test_noalloc_oc_matches_allocating_entry(gpu_lib):
+    torch = pytest.importorskip("torch")
+    from topoptlab_gb300 import _lib
+    from topoptlab_gb300.optimizer import oc_top88
+    lib = _lib.load()
+    rng = np.random.default_rng(11)
+    dev = torch.device("cuda", 0)
+    for call, n in enumerate((200_003, 65_536)):
+        x, dc, dv, flags = _inputs(rng, n)
+        g = 0.1 * call - 0.05
+        xref, gtref = oc_top88(x, 0.5, dc, dv, g, el_flags=flags)
+        xd = torch.from_numpy(x).to(dev)
+        dcd = torch.from_numpy(dc).to(dev)
+        dvd = torch.from_numpy(dv).to(dev)
+        fld = torch.from_numpy(flags).to(dev)
+        out = torch.empty(n, dtype=torch.float64, device=dev)
+        gt = C.c_double()
+        nsteps = C.c_int32()
+        torch.cuda.synchronize()
+        rc = lib.tg_oc_noalloc(n, xd.data_ptr(), dcd.data_ptr(), dvd.data_ptr(), g,
+                               fld.data_ptr(), 0.2, 0.0, 1e9, out.data_ptr(),
+                               C.byref(gt), C.byref(nsteps), None)
+        assert rc == 0, lib.tg_noalloc_last_error().decode()
+        torch.cuda.synchronize()
+        np.testing.assert_allclose(out.cpu().numpy(), xref, rtol=0, atol=1e-13)
+        np.testing.assert_allclose(gt.value, gtref, rtol=1e-9, atol=1e-12)
+        assert nsteps.value > 10
+
+
+def test_noalloc_rejects_oversize(gpu_lib):
+    from topoptlab_gb300 import _lib
+    lib = _lib.load()
+    gt = C.c_double()
+    ns = C.c_int32()
+    rc = lib.tg_oc_noalloc(2097152 + 1, 1, 1, 1, 0.0, None, 0.2, 0.0, 1e9, 1,
+                           C.byref(gt), C.byref(ns), None)
+    assert rc == _lib.TG_EINVAL
+    assert "exceeds" in lib.tg_noalloc_last_error().decode()

@@ -71,6 +71,10 @@ SIGNATURES = {
     "tg_oc": (C.c_int32, [C.c_void_p, _dp, _dp, _dp, C.c_double, _dp, _dp, _i32p]),
     "tg_oc_raw": (C.c_int32, [C.c_int64, _dp, _dp, _dp, C.c_double, _i8p, C.c_double,
                               C.c_double, C.c_double, _dp, _dp, _i32p, C.c_int32]),
+    "tg_oc_noalloc": (C.c_int32, [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
+                                  C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_void_p,
+                                  _dp, _i32p, C.c_void_p]),
+    "tg_noalloc_last_error": (C.c_char_p, []),
     "tg_vcycle": (C.c_int32, [C.c_void_p, _dp, _dp, _dp, C.c_int32]),
     "tg_levels": (C.c_int32, [C.c_void_p, _i32p, _i64p]),
     "tg_coarse_stencil": (C.c_int32, [C.c_void_p, _dp, C.c_int32, _dp, C.c_int64]),
