@@ -169,7 +169,6 @@ def run_ours(args, dist, rank, ws, local):
     for _ in range(args.warmup):
         prob.step()
     lib.tg_stats(1, None, None, None)
-    lib.tg_profile_kernel(prof_kind)
     _barrier(dist)
     with ClockSampler(device) as clk:
         lib.tg_timer(prob._h, 0, None)
@@ -178,11 +177,20 @@ def run_ours(args, dist, rank, ws, local):
         ms = C.c_double()
         lib.tg_timer(prob._h, 1, C.byref(ms))
     t_mixed = ms.value / 1000.0
-    launches, pms, pcount = C.c_int64(), C.c_double(), C.c_int64()
-    lib.tg_stats(1, C.byref(launches), C.byref(pms), C.byref(pcount))
-    lib.tg_profile_kernel(0)
+    launches = C.c_int64()
+    lib.tg_stats(1, C.byref(launches), None, None)
     t_max = _max_over_ranks(dist, t_mixed)
     value = args.steps * ws / t_max
+
+    # the roofline kernel: CUDA events around each of its launches on the
+    # library's stream, over further design iterations launched directly
+    # (CUDA-graph replay is switched off while a kernel family is timed)
+    pms, pcount = C.c_double(), C.c_int64()
+    lib.tg_profile_kernel(prof_kind)
+    for _ in range(max(1, min(args.steps, 3))):
+        steps_info.append(prob.step())
+    lib.tg_stats(1, None, C.byref(pms), C.byref(pcount))
+    lib.tg_profile_kernel(0)
 
     # ---------------- end to end through the public API, host buffers ----------------
     try:

@@ -84,6 +84,8 @@ enum ProfKind : int {
 };
 void prof_begin(int kind, cudaStream_t st);
 void prof_end(int kind, cudaStream_t st);
+int prof_kind();              // family being timed (PK_NONE when off)
+int64_t launch_count();       // kernels launched so far
 
 #define TG_REQUIRE(cond, msg)                                                \
   do {                                                                       \

@@ -14,6 +14,8 @@
 namespace tg {
 
 Ctx::~Ctx() {
+  if (g64.exec) cudaGraphExecDestroy(g64.exec);
+  if (g32.exec) cudaGraphExecDestroy(g32.exec);
   for (Level* l : lv) delete l;
   if (h_oc) cudaFreeHost(h_oc);
   if (h_pcg) cudaFreeHost(h_pcg);
@@ -72,11 +74,23 @@ static void setup_element(Ctx& c, const double* KEref) {
   c.op.sector = vec_ok && off <= 1e-12 * bmax;
   std::memset(&c.op.B64, 0, sizeof(c.op.B64));
   std::memset(&c.op.B32, 0, sizeof(c.op.B32));
-  if (c.op.sector)
+  // hex8 elasticity: does the block zero pattern match the reference element's?
+  bool hex8 = c.op.sector && nd == 3 && nf == 3;
+  if (hex8)
     for (int chi = 0; chi < NC; ++chi)
       for (int a = 0; a < nf; ++a)
         for (int b = 0; b < nf; ++b) {
           const double v = B[(sigf(chi, a) * nf + a) * NE + sigf(chi, b) * nf + b];
+          const bool nz = std::fabs(v) > 1e-12 * bmax;
+          if (nz != (((hex8_mask(chi) >> (a * 3 + b)) & 1u) != 0)) hex8 = false;
+        }
+  c.op.kind = !c.op.sector ? EK_DENSE : (hex8 ? EK_SECTOR_HEX8 : EK_SECTOR);
+  if (c.op.sector)
+    for (int chi = 0; chi < NC; ++chi)
+      for (int a = 0; a < nf; ++a)
+        for (int b = 0; b < nf; ++b) {
+          double v = B[(sigf(chi, a) * nf + a) * NE + sigf(chi, b) * nf + b];
+          if (hex8 && !((hex8_mask(chi) >> (a * 3 + b)) & 1u)) v = 0.0;   // exact zeros
           c.op.B64.b[chi][a][b] = v;
           c.op.B32.b[chi][a][b] = (float)v;
         }
@@ -247,7 +261,7 @@ void ctx_init(Ctx& c, const tg_problem& p) {
   c.part.alloc(RED_BLOCKS); c.part2.alloc(RED_BLOCKS); c.scal.alloc(8);
   c.oc.alloc(1); c.pcg.alloc(1); c.pcg_out.alloc(1);
   c.oc.zero(c.st); c.pcg.zero(c.st); c.pcg_out.zero(c.st);
-  c.r.alloc(nd); c.z.alloc(nd); c.p.alloc(nd); c.q.alloc(nd);
+  c.r.alloc(nd); c.z.alloc(nd); c.p.alloc(nd); c.q.alloc(nd); c.z2.alloc(nd);
   if (mixed) { c.r32.alloc(nd); c.z32.alloc(nd); c.p32.alloc(nd); c.q32.alloc(nd); c.d32.alloc(nd); }
   TG_CUDA(cudaMallocHost(&c.h_oc, sizeof(OCState)));
   TG_CUDA(cudaMallocHost(&c.h_pcg, sizeof(PCGState)));
@@ -409,6 +423,39 @@ static void check_finite(double v, const char* what) {
   if (!std::isfinite(v)) throw Error{ENAN, std::string("non-finite value in ") + what};
 }
 
+// Run one PCG iteration body: replayed from a CUDA graph captured on first
+// use (one launch per iteration instead of ~35), or launched directly while a
+// kernel family is being event-timed.  Ends with the PCG scalars in h_pcg.
+template <typename F>
+static void run_iteration(Ctx& c, Ctx::IterGraph& gr, F&& body) {
+  if (!c.use_graphs || prof_kind() != PK_NONE) {
+    body();
+    TG_CUDA(cudaStreamSynchronize(c.st));
+    return;
+  }
+  if (!gr.exec) {
+    const int64_t before = launch_count();
+    cudaGraph_t graph = nullptr;
+    TG_CUDA(cudaStreamBeginCapture(c.st, cudaStreamCaptureModeThreadLocal));
+    try {
+      body();
+    } catch (...) {
+      cudaStreamEndCapture(c.st, &graph);
+      if (graph) cudaGraphDestroy(graph);
+      throw;
+    }
+    TG_CUDA(cudaStreamEndCapture(c.st, &graph));
+    const cudaError_t e = cudaGraphInstantiate(&gr.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    TG_CUDA(e);
+    gr.launches = launch_count() - before;
+    count_launches(-gr.launches);      // capture recorded, did not launch
+  }
+  TG_CUDA(cudaGraphLaunch(gr.exec, c.st));
+  count_launches(gr.launches);
+  TG_CUDA(cudaStreamSynchronize(c.st));
+}
+
 // plain FP64 PCG (linear_solvers.py:114-134), x in/out
 static int pcg64(Ctx& c, const double* b, double* x, double tol_abs, int maxiter, bool& conv) {
   const int64_t n = c.g.ndofs();
@@ -420,19 +467,25 @@ static int pcg64(Ctx& c, const double* b, double* x, double tol_abs, int maxiter
   check_finite(rr, "PCG residual");
   conv = std::sqrt(rr) < tol_abs;
   int it = 0;
+  // x lives in the caller's buffer; the captured body must not depend on it
+  double* xs = c.z2.p;
+  TG_CUDA(cudaMemcpyAsync(xs, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, c.st));
   while (!conv && it < maxiter) {
-    precondition<double>(c, c.r, c.z);
-    dot<double, double>(n, c.r.p, c.z.p, c.part, c.pcg, DOT_RHO, c.st);
-    update_p<double>(n, c.z, c.p, c.pcg, c.st);
-    fine_apply<double, double>(c.op, c.s64, c.p, c.q, nullptr, nullptr, 0.0, AM_Y, c.st);
-    dot<double, double>(n, c.p.p, c.q.p, c.part, c.pcg, DOT_ALPHA, c.st);
-    update_xr<double>(n, c.p, c.q, x, c.r, c.part, c.pcg, c.st);
+    run_iteration(c, c.g64, [&] {
+      precondition<double>(c, c.r, c.z);
+      dot<double, double>(n, c.r.p, c.z.p, c.part, c.pcg, DOT_RHO, c.st);
+      update_p<double>(n, c.z, c.p, c.pcg, c.st);
+      fine_apply<double, double>(c.op, c.s64, c.p, c.q, nullptr, nullptr, 0.0, AM_Y, c.st);
+      dot<double, double>(n, c.p.p, c.q.p, c.part, c.pcg, DOT_ALPHA, c.st);
+      update_xr<double>(n, c.p, c.q, xs, c.r, c.part, c.pcg, c.st);
+      TG_CUDA(cudaMemcpyAsync(c.h_pcg, c.pcg.p, sizeof(PCGState), cudaMemcpyDeviceToHost, c.st));
+    });
     ++it;
-    read_pcg(c, c.pcg);
     rr = c.h_pcg->rr;
     check_finite(rr, "PCG residual");
     conv = std::sqrt(rr) < tol_abs;
   }
+  TG_CUDA(cudaMemcpyAsync(x, xs, sizeof(double) * n, cudaMemcpyDeviceToDevice, c.st));
   return it;
 }
 
@@ -443,14 +496,16 @@ static int pcg32(Ctx& c, double tol_abs, int maxiter) {
   pcg_reset(c.pcg, c.st);
   int it = 0;
   while (it < maxiter) {
-    precondition<float>(c, c.r32, c.z32);
-    dot<float, float>(n, c.r32.p, c.z32.p, c.part, c.pcg, DOT_RHO, c.st);
-    update_p<float>(n, c.z32, c.p32, c.pcg, c.st);
-    fine_apply<float, float>(c.op, c.s32, c.p32, c.q32, nullptr, nullptr, 0.0, AM_Y, c.st);
-    dot<float, float>(n, c.p32.p, c.q32.p, c.part, c.pcg, DOT_ALPHA, c.st);
-    update_xr<float>(n, c.p32, c.q32, c.d32, c.r32, c.part, c.pcg, c.st);
+    run_iteration(c, c.g32, [&] {
+      precondition<float>(c, c.r32, c.z32);
+      dot<float, float>(n, c.r32.p, c.z32.p, c.part, c.pcg, DOT_RHO, c.st);
+      update_p<float>(n, c.z32, c.p32, c.pcg, c.st);
+      fine_apply<float, float>(c.op, c.s32, c.p32, c.q32, nullptr, nullptr, 0.0, AM_Y, c.st);
+      dot<float, float>(n, c.p32.p, c.q32.p, c.part, c.pcg, DOT_ALPHA, c.st);
+      update_xr<float>(n, c.p32, c.q32, c.d32, c.r32, c.part, c.pcg, c.st);
+      TG_CUDA(cudaMemcpyAsync(c.h_pcg, c.pcg.p, sizeof(PCGState), cudaMemcpyDeviceToHost, c.st));
+    });
     ++it;
-    read_pcg(c, c.pcg);
     const double rr = c.h_pcg->rr;
     check_finite(rr, "inner PCG residual");
     if (std::sqrt(rr) < tol_abs) break;

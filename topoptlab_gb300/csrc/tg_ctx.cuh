@@ -72,7 +72,7 @@ struct Ctx {
   DevBuf<OCState> oc;
   DevBuf<PCGState> pcg, pcg_out;
   // PCG vectors
-  DevBuf<double> r, z, p, q;
+  DevBuf<double> r, z, p, q, z2;   // z2: FP64 PCG iterate (fixed address for the graph)
   DevBuf<float> r32, z32, p32, q32, d32;
   // hierarchy
   std::vector<Level*> lv;
@@ -86,6 +86,13 @@ struct Ctx {
   PCGState* h_pcg = nullptr;
   double* h_scal = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, tev0 = nullptr, tev1 = nullptr;
+  // one PCG iteration captured as a CUDA graph (FP64 / FP32 loop); every
+  // pointer and kernel argument it uses is fixed for the context's lifetime
+  struct IterGraph {
+    cudaGraphExec_t exec = nullptr;
+    int64_t launches = 0;        // kernels per replay
+  } g64, g32;
+  bool use_graphs = true;
   // statistics of the last solve
   int last_iters = 0, last_vcycles = 0, last_refine = 0, last_converged = 0;
   double last_relres = 0.0;

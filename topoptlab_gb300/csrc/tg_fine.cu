@@ -46,30 +46,29 @@ __device__ __forceinline__ void wht(T (&v)[1 << NDIM][NDOF]) {
       }
 }
 
-// y = rho * KE u  for one element, sector form.  u is destroyed.
-template <int NDIM, int NDOF, typename T>
-__device__ __forceinline__ void elem_sector(T (&u)[1 << NDIM][NDOF], const Sector<T>& B, T rho,
+// y = KE u for one element, sector form (u is destroyed); the density is
+// applied by the caller's fused multiply-add into the accumulator.
+template <int NDIM, int NDOF, typename T, int KIND>
+__device__ __forceinline__ void elem_sector(T (&u)[1 << NDIM][NDOF], const Sector<T>& B,
                                             T (&y)[1 << NDIM][NDOF]) {
   constexpr int NC = 1 << NDIM;
   wht<NDIM, NDOF, T>(u);
-#pragma unroll
-  for (int c = 0; c < NDOF; ++c)
-#pragma unroll
-    for (int s = 0; s < NC; ++s) u[s][c] *= rho;
 #pragma unroll
   for (int chi = 0; chi < NC; ++chi)
 #pragma unroll
     for (int c = 0; c < NDOF; ++c) {
       T acc = T(0);
 #pragma unroll
-      for (int c2 = 0; c2 < NDOF; ++c2) acc += B.b[chi][c][c2] * u[sig<NDIM, NDOF>(chi, c2)][c2];
+      for (int c2 = 0; c2 < NDOF; ++c2)
+        if (KIND != EK_SECTOR_HEX8 || ((hex8_mask(chi) >> (c * 3 + c2)) & 1u))
+          acc += B.b[chi][c][c2] * u[sig<NDIM, NDOF>(chi, c2)][c2];
       y[sig<NDIM, NDOF>(chi, c)][c] = acc;
     }
   wht<NDIM, NDOF, T>(y);
 }
 
 template <int NDIM, int NDOF, typename T>
-__device__ __forceinline__ void elem_dense(const T (&u)[1 << NDIM][NDOF], const T* KEs, T rho,
+__device__ __forceinline__ void elem_dense(const T (&u)[1 << NDIM][NDOF], const T* KEs,
                                            T (&y)[1 << NDIM][NDOF]) {
   constexpr int NE = (1 << NDIM) * NDOF;
 #pragma unroll 4
@@ -77,7 +76,7 @@ __device__ __forceinline__ void elem_dense(const T (&u)[1 << NDIM][NDOF], const 
     T acc = T(0);
 #pragma unroll
     for (int j = 0; j < NE; ++j) acc += KEs[i * NE + j] * u[j / NDOF][j % NDOF];
-    y[i / NDOF][i % NDOF] = rho * acc;
+    y[i / NDOF][i % NDOF] = acc;
   }
 }
 
@@ -143,14 +142,14 @@ template <int NDIM> struct SLayout {
   }
 };
 
-template <int NDIM, int NDOF, typename T, bool SECTOR>
+template <int NDIM, int NDOF, typename T, int KIND>
 constexpr size_t apply_smem_v2() {
   using L = SLayout<NDIM>;
   constexpr int NE = (1 << NDIM) * NDOF;
-  return sizeof(T) * ((size_t)2 * NDOF * L::NODE_WORDS + L::ELEM_WORDS + (SECTOR ? 0 : NE * NE));
+  return sizeof(T) * ((size_t)2 * NDOF * L::NODE_WORDS + L::ELEM_WORDS + (KIND != EK_DENSE ? 0 : NE * NE));
 }
 
-template <int NDIM, int NDOF, typename T, typename S, bool SECTOR, int MODE>
+template <int NDIM, int NDOF, typename T, typename S, int KIND, int MODE>
 __global__ void __launch_bounds__(256, sizeof(T) == 8 ? 2 : 4) k_fine_apply(ApplyArgs<T, S> a) {
   using TL = Tile<NDIM>;
   using L = SLayout<NDIM>;
@@ -196,7 +195,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 8 ? 2 : 4) k_fine_apply(Appl
     }
   }
   for (int i = tid; i < NDOF * L::NODE_WORDS; i += nth) ys[i] = T(0);
-  if (!SECTOR)
+  if (KIND == EK_DENSE)
     for (int i = tid; i < NE * NE; i += nth) KEs[i] = a.KE[i];
   cp_async_wait_all();
   __syncthreads();
@@ -221,15 +220,18 @@ __global__ void __launch_bounds__(256, sizeof(T) == 8 ? 2 : 4) k_fine_apply(Appl
 #pragma unroll
         for (int c = 0; c < NDOF; ++c) ue[d][c] = us[L::at(c, hz, hx, hy)];
       }
-      if (SECTOR)
-        elem_sector<NDIM, NDOF, T>(ue, a.B, rho, ye);
+      if (KIND != EK_DENSE)
+        elem_sector<NDIM, NDOF, T, KIND>(ue, a.B, ye);
       else
-        elem_dense<NDIM, NDOF, T>(ue, KEs, rho, ye);
+        elem_dense<NDIM, NDOF, T>(ue, KEs, ye);
 #pragma unroll
       for (int d = 0; d < NC; ++d) {
         const int hx = lx + (d & 1), hy = ly + ((d >> 1) & 1), hz = (NDIM == 3) ? lz + ((d >> 2) & 1) : 0;
 #pragma unroll
-        for (int c = 0; c < NDOF; ++c) ys[L::at(c, hz, hx, hy)] += ye[d][c];
+        for (int c = 0; c < NDOF; ++c) {
+          T& acc = ys[L::at(c, hz, hx, hy)];
+          acc = fma(rho, ye[d][c], acc);
+        }
       }
     }
     __syncthreads();
@@ -261,11 +263,11 @@ __global__ void __launch_bounds__(256, sizeof(T) == 8 ? 2 : 4) k_fine_apply(Appl
   }
 }
 
-template <int NDIM, int NDOF, typename T, typename S, bool SECTOR, int MODE>
+template <int NDIM, int NDOF, typename T, typename S, int KIND, int MODE>
 static void launch_apply(const ApplyArgs<T, S>& a, cudaStream_t st) {
   using TL = Tile<NDIM>;
-  constexpr size_t smem = apply_smem_v2<NDIM, NDOF, T, SECTOR>();
-  auto kern = k_fine_apply<NDIM, NDOF, T, S, SECTOR, MODE>;
+  constexpr size_t smem = apply_smem_v2<NDIM, NDOF, T, KIND>();
+  auto kern = k_fine_apply<NDIM, NDOF, T, S, KIND, MODE>;
   static bool attr_set = false;   // per instantiation; attribute is per function
   if (!attr_set) {
     TG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -281,17 +283,21 @@ static void launch_apply(const ApplyArgs<T, S>& a, cudaStream_t st) {
   TG_CHECK_LAUNCH();
 }
 
+template <int NDIM, int NDOF, typename T, typename S, int KIND>
+static void dispatch_mode(const ApplyArgs<T, S>& a, int mode, cudaStream_t st) {
+  if (mode == AM_Y) launch_apply<NDIM, NDOF, T, S, KIND, AM_Y>(a, st);
+  else if (mode == AM_RES) launch_apply<NDIM, NDOF, T, S, KIND, AM_RES>(a, st);
+  else launch_apply<NDIM, NDOF, T, S, KIND, AM_JACOBI>(a, st);
+}
+
 template <int NDIM, int NDOF, typename T, typename S>
-static void dispatch_apply(const ApplyArgs<T, S>& a, bool sector, int mode, cudaStream_t st) {
-  if (sector) {
-    if (mode == AM_Y) launch_apply<NDIM, NDOF, T, S, true, AM_Y>(a, st);
-    else if (mode == AM_RES) launch_apply<NDIM, NDOF, T, S, true, AM_RES>(a, st);
-    else launch_apply<NDIM, NDOF, T, S, true, AM_JACOBI>(a, st);
-  } else {
-    if (mode == AM_Y) launch_apply<NDIM, NDOF, T, S, false, AM_Y>(a, st);
-    else if (mode == AM_RES) launch_apply<NDIM, NDOF, T, S, false, AM_RES>(a, st);
-    else launch_apply<NDIM, NDOF, T, S, false, AM_JACOBI>(a, st);
-  }
+static void dispatch_apply(const ApplyArgs<T, S>& a, int kind, int mode, cudaStream_t st) {
+  if (kind == EK_SECTOR_HEX8 && NDIM == 3 && NDOF == 3)
+    dispatch_mode<NDIM, NDOF, T, S, EK_SECTOR_HEX8>(a, mode, st);
+  else if (kind != EK_DENSE)
+    dispatch_mode<NDIM, NDOF, T, S, EK_SECTOR>(a, mode, st);
+  else
+    dispatch_mode<NDIM, NDOF, T, S, EK_DENSE>(a, mode, st);
 }
 
 template <typename T> static const T* ke_ptr(const FineOp& op);
@@ -309,10 +315,10 @@ void fine_apply(const FineOp& op, const S* scale, const T* u, T* y, const T* b, 
   a.omega = (T)omega; a.KE = ke_ptr<T>(op); a.B = sec_ref<T>(op);
   const int key = op.g.ndim * 10 + op.g.ndof;
   switch (key) {
-    case 33: dispatch_apply<3, 3, T, S>(a, op.sector, mode, st); break;
-    case 31: dispatch_apply<3, 1, T, S>(a, op.sector, mode, st); break;
-    case 22: dispatch_apply<2, 2, T, S>(a, op.sector, mode, st); break;
-    case 21: dispatch_apply<2, 1, T, S>(a, op.sector, mode, st); break;
+    case 33: dispatch_apply<3, 3, T, S>(a, op.kind, mode, st); break;
+    case 31: dispatch_apply<3, 1, T, S>(a, op.kind, mode, st); break;
+    case 22: dispatch_apply<2, 2, T, S>(a, op.kind, mode, st); break;
+    case 21: dispatch_apply<2, 1, T, S>(a, op.kind, mode, st); break;
     default: throw Error{EINVAL_, "unsupported (ndim, nnode_dof) combination"};
   }
 }

@@ -393,65 +393,88 @@ void build_galerkin(const Grid& gf, const double* Af, const Grid& gc, const uint
 // ---------------------------------------------------------------------------
 // transfers
 // ---------------------------------------------------------------------------
-template <typename T>
-__global__ void k_restrict(Grid gf, Grid gc, const uint8_t* fixc, const T* __restrict__ rf,
-                           T* __restrict__ bc) {
-  const int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (I >= gc.nnodes()) return;
-  const int ndof = gc.ndof;
+// restriction: one thread per (component, coarse node), fully unrolled over
+// the 3^ndim fine nodes of the coarse node's support
+template <int NDIM, int NDOF, typename T>
+__global__ void __launch_bounds__(256) k_restrict(Grid gf, Grid gc, const uint8_t* fixc,
+                                                  const T* __restrict__ rf, T* __restrict__ bc) {
+  const int64_t ldc = gc.nnodes();
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= ldc * NDOF) return;
+  const int c = (int)(t / ldc);
+  const int64_t I = t - (int64_t)c * ldc;
   int ix, iy, iz;
   node_xyz(gc, I, ix, iy, iz);
-  double acc[3] = {0.0, 0.0, 0.0};
-  const int nd = (gc.ndim == 3) ? 27 : 9;
-  for (int al = 0; al < nd; ++al) {
+  T acc = T(0);
+#pragma unroll
+  for (int al = 0; al < ndir<NDIM>(); ++al) {
     int ax, ay, az;
-    dir_xyz(al, gc.ndim, ax, ay, az);
+    dir_xyz(al, NDIM, ax, ay, az);
     const int fx = 2 * ix + ax, fy = 2 * iy + ay, fz = 2 * iz + az;
     if (!in_grid(gf, fx, fy, fz)) continue;
-    const double w = (ax ? 0.5 : 1.0) * (ay ? 0.5 : 1.0) * (az ? 0.5 : 1.0);
-    const int64_t fi = gf.node(fx, fy, fz);
-    for (int c = 0; c < ndof; ++c) acc[c] += w * (double)rf[fi * ndof + c];
+    const T w = T((ax ? 0.5 : 1.0) * (ay ? 0.5 : 1.0) * (az ? 0.5 : 1.0));
+    acc += w * __ldg(rf + gf.node(fx, fy, fz) * NDOF + c);
   }
-  for (int c = 0; c < ndof; ++c) bc[I * ndof + c] = ((fixc[I] >> c) & 1) ? T(0) : (T)acc[c];
+  bc[I * NDOF + c] = ((fixc[I] >> c) & 1) ? T(0) : acc;
 }
 
 template <typename T>
 void restrict_(const Grid& gf, const Grid& gc, const uint8_t* fixc, const T* rf, T* bc,
                cudaStream_t st) {
-  k_restrict<T><<<(unsigned)cdiv(gc.nnodes(), 256), 256, 0, st>>>(gf, gc, fixc, rf, bc);
+  const unsigned blocks = (unsigned)cdiv(gc.nnodes() * gc.ndof, 256);
+  switch (gf.ndim * 10 + gf.ndof) {
+    case 33: k_restrict<3, 3, T><<<blocks, 256, 0, st>>>(gf, gc, fixc, rf, bc); break;
+    case 31: k_restrict<3, 1, T><<<blocks, 256, 0, st>>>(gf, gc, fixc, rf, bc); break;
+    case 22: k_restrict<2, 2, T><<<blocks, 256, 0, st>>>(gf, gc, fixc, rf, bc); break;
+    case 21: k_restrict<2, 1, T><<<blocks, 256, 0, st>>>(gf, gc, fixc, rf, bc); break;
+    default: throw Error{EINVAL_, "unsupported (ndim, nnode_dof)"};
+  }
   TG_CHECK_LAUNCH();
 }
 template void restrict_<double>(const Grid&, const Grid&, const uint8_t*, const double*, double*, cudaStream_t);
 template void restrict_<float>(const Grid&, const Grid&, const uint8_t*, const float*, float*, cudaStream_t);
 
-template <typename T>
-__global__ void k_prolong_add(Grid gf, Grid gc, const uint8_t* fixf, const T* __restrict__ xc,
-                              T* __restrict__ xf) {
+// prolongation: one thread per fine node, all components; the 1, 2, 4 or 8
+// coarse parents follow from the parity of the fine coordinates
+template <int NDIM, int NDOF, typename T>
+__global__ void __launch_bounds__(256) k_prolong_add(Grid gf, Grid gc, const uint8_t* fixf,
+                                                     const T* __restrict__ xc,
+                                                     T* __restrict__ xf) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= gf.nnodes()) return;
-  const int ndof = gf.ndof;
   int fx, fy, fz;
   node_xyz(gf, i, fx, fy, fz);
-  double acc[3] = {0.0, 0.0, 0.0};
-  const int nzc = (gf.ndim == 3 && (fz & 1)) ? 2 : 1;
-  const int nxc = (fx & 1) ? 2 : 1, nyc = (fy & 1) ? 2 : 1;
-  const double w = ((fx & 1) ? 0.5 : 1.0) * ((fy & 1) ? 0.5 : 1.0) *
-                   ((gf.ndim == 3 && (fz & 1)) ? 0.5 : 1.0);
-  for (int a = 0; a < nzc; ++a)
-    for (int b = 0; b < nxc; ++b)
-      for (int c2 = 0; c2 < nyc; ++c2) {
-        const int cz = (gf.ndim == 3) ? fz / 2 + a : 0, cx = fx / 2 + b, cy = fy / 2 + c2;
-        const int64_t I = gc.node(cx, cy, cz);
-        for (int c = 0; c < ndof; ++c) acc[c] += w * (double)xc[I * ndof + c];
-      }
-  for (int c = 0; c < ndof; ++c)
-    if (!((fixf[i] >> c) & 1)) xf[i * ndof + c] += (T)acc[c];
+  const int ox = fx & 1, oy = fy & 1, oz = (NDIM == 3) ? (fz & 1) : 0;
+  const int cx0 = fx >> 1, cy0 = fy >> 1, cz0 = (NDIM == 3) ? fz >> 1 : 0;
+  const T w = T((ox ? 0.5 : 1.0) * (oy ? 0.5 : 1.0) * (oz ? 0.5 : 1.0));
+  T acc[NDOF];
+#pragma unroll
+  for (int c = 0; c < NDOF; ++c) acc[c] = T(0);
+#pragma unroll
+  for (int k = 0; k < (1 << NDIM); ++k) {
+    const int a = k & 1, b = (k >> 1) & 1, d = (k >> 2) & 1;
+    if ((a && !ox) || (b && !oy) || (d && !oz)) continue;
+    const int64_t I = gc.node(cx0 + a, cy0 + b, cz0 + d);
+#pragma unroll
+    for (int c = 0; c < NDOF; ++c) acc[c] += __ldg(xc + I * NDOF + c);
+  }
+  const uint8_t m = fixf[i];
+#pragma unroll
+  for (int c = 0; c < NDOF; ++c)
+    if (!((m >> c) & 1)) xf[i * NDOF + c] += w * acc[c];
 }
 
 template <typename T>
 void prolong_add(const Grid& gf, const Grid& gc, const uint8_t* fixf, const T* xc, T* xf,
                  cudaStream_t st) {
-  k_prolong_add<T><<<(unsigned)cdiv(gf.nnodes(), 256), 256, 0, st>>>(gf, gc, fixf, xc, xf);
+  const unsigned blocks = (unsigned)cdiv(gf.nnodes(), 256);
+  switch (gf.ndim * 10 + gf.ndof) {
+    case 33: k_prolong_add<3, 3, T><<<blocks, 256, 0, st>>>(gf, gc, fixf, xc, xf); break;
+    case 31: k_prolong_add<3, 1, T><<<blocks, 256, 0, st>>>(gf, gc, fixf, xc, xf); break;
+    case 22: k_prolong_add<2, 2, T><<<blocks, 256, 0, st>>>(gf, gc, fixf, xc, xf); break;
+    case 21: k_prolong_add<2, 1, T><<<blocks, 256, 0, st>>>(gf, gc, fixf, xc, xf); break;
+    default: throw Error{EINVAL_, "unsupported (ndim, nnode_dof)"};
+  }
   TG_CHECK_LAUNCH();
 }
 template void prolong_add<double>(const Grid&, const Grid&, const uint8_t*, const double*, double*, cudaStream_t);

@@ -13,6 +13,17 @@ template <typename T> struct Sector {
   T b[8][3][3];
 };
 
+// Element-product kinds: dense KE, sector form with any block contents, and
+// sector form with the zero pattern of the reference's hex8 elasticity
+// blocks (45 of 72 entries non-zero; the host verifies the pattern).
+enum ElemKind : int { EK_DENSE = 0, EK_SECTOR = 1, EK_SECTOR_HEX8 = 2 };
+// bit (c*3 + c2) set: block chi, row c, column c2 is structurally non-zero
+__host__ __device__ constexpr unsigned hex8_mask(int chi) {
+  return chi == 0 || chi == 7 ? 0x1FFu
+         : chi == 1 ? 0x1B0u : chi == 2 ? 0x145u : chi == 3 ? 0x11Bu
+         : chi == 4 ? 0x01Bu : chi == 5 ? 0x155u : 0x1B1u;
+}
+
 // Fine-level (matrix-free) operator description.
 struct FineOp {
   Grid g;
@@ -22,6 +33,7 @@ struct FineOp {
   Sector<double> B64;
   Sector<float> B32;
   bool sector;              // use the sector path
+  int kind;                 // element product: 0 dense, 1 sector, 2 sector with the hex8 zero pattern
   double KEdiag[24];        // diagonal of KE, corner-bit order
 };
 

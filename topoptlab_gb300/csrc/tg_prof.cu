@@ -13,6 +13,7 @@ namespace tg {
 
 static std::atomic<int64_t> g_launches{0};
 void count_launches(int64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+int64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
 namespace {
 std::mutex g_mu;
@@ -44,6 +45,8 @@ void drain_locked() {
   g_used = 0;
 }
 }  // namespace
+
+int prof_kind() { return g_kind; }
 
 void prof_begin(int kind, cudaStream_t st) {
   if (kind != g_kind || kind == PK_NONE) return;
