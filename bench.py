@@ -220,11 +220,12 @@ def run_ours(args, dist, rank, ws, local):
             print("mixed", s, file=sys.stderr)
 
     # ---------------- plain FP64 GMG-PCG, same iterations ----------------
+    nplain = 0 if args.no_plain else args.steps
     plain = _problem("fp64", device)
-    for _ in range(args.warmup):
+    for _ in range(args.warmup if nplain else 0):
         plain.step()
     lib.tg_timer(plain._h, 0, None)
-    pinfo = [plain.step() for _ in range(args.steps)]
+    pinfo = [plain.step() for _ in range(nplain)] or [steps_info[0]]
     ms2 = C.c_double()
     lib.tg_timer(plain._h, 1, C.byref(ms2))
     plain.close()
@@ -232,7 +233,7 @@ def run_ours(args, dist, rank, ws, local):
         for s in pinfo:
             print("plain", s, file=sys.stderr)
     t_plain = _max_over_ranks(dist, ms2.value / 1000.0)
-    value_plain = args.steps * ws / t_plain
+    value_plain = (nplain * ws / t_plain) if nplain else float("nan")
     obj_plain = [s.obj for s in pinfo]
     obj_diff = max(abs(a - b) / abs(b) for a, b in zip(obj_mixed, obj_plain))
 
@@ -372,6 +373,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true",
+                    help="skip the plain FP64 arm (profiling runs only)")
     ap.add_argument("--size", default=None,
                     help="override the grid, e.g. 80,40,40 (profiling runs only)")
     args = ap.parse_args()
