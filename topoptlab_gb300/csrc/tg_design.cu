@@ -233,17 +233,20 @@ void oc_steps(int64_t n, const double* x, const double* S, const double* dv, con
 // ---------------------------------------------------------------------------
 // PCG vector algebra (scalars live in device memory)
 // ---------------------------------------------------------------------------
+// Arithmetic runs in the vector's own type (GB300's FP64 pipe is ~1/64 of
+// FP32, so FP64 work per element would dominate an FP32 vector kernel); each
+// thread's partial sum is widened to FP64 for the block and grid reduction.
 template <typename TA, typename TB>
 __global__ void __launch_bounds__(RED_THREADS) k_dot(int64_t n, const TA* __restrict__ a,
                                                     const TB* __restrict__ b, double* part,
                                                     PCGState* st, int op) {
   __shared__ double sh[32];
   __shared__ int last;
-  double acc = 0.0;
+  TA acc = TA(0);
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
-    acc += (double)a[i] * (double)b[i];
-  const double s = block_sum(acc, sh);
+    acc = fma(a[i], (TA)b[i], acc);
+  const double s = block_sum((double)acc, sh);
   if (threadIdx.x == 0) {
     part[blockIdx.x] = s;
     __threadfence();
@@ -263,6 +266,8 @@ __global__ void __launch_bounds__(RED_THREADS) k_dot(int64_t n, const TA* __rest
       st->alpha = st->rho / tot;
     } else if (op == DOT_RR) {
       st->rr = tot;
+      st->rnorm = sqrt(tot);
+      st->rinv = tot > 0.0 ? 1.0 / st->rnorm : 0.0;
     } else if (op == DOT_BB) {
       st->bb = tot;
     }
@@ -282,8 +287,8 @@ template <typename T>
 __global__ void k_update_p(int64_t n, const T* __restrict__ z, T* __restrict__ p, const PCGState* st) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const double beta = st->beta;
-  p[i] = (st->iter > 0) ? (T)((double)z[i] + beta * (double)p[i]) : z[i];
+  const T beta = (T)st->beta;
+  p[i] = (st->iter > 0) ? fma(beta, p[i], z[i]) : z[i];
 }
 template <typename T>
 void update_p(int64_t n, const T* z, T* p, const PCGState* st, cudaStream_t s) {
@@ -300,16 +305,16 @@ __global__ void __launch_bounds__(RED_THREADS) k_update_xr(int64_t n, const T* _
                                                           T* __restrict__ r, double* part, PCGState* st) {
   __shared__ double sh[32];
   __shared__ int last;
-  const double alpha = st->alpha;
-  double acc = 0.0;
+  const T alpha = (T)st->alpha;
+  T acc = T(0);
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
-    x[i] = (T)((double)x[i] + alpha * (double)p[i]);
-    const T ri = (T)((double)r[i] - alpha * (double)q[i]);
+    x[i] = fma(alpha, p[i], x[i]);
+    const T ri = fma(-alpha, q[i], r[i]);
     r[i] = ri;
-    acc += (double)ri * (double)ri;
+    acc = fma(ri, ri, acc);
   }
-  const double s = block_sum(acc, sh);
+  const double s = block_sum((double)acc, sh);
   if (threadIdx.x == 0) {
     part[blockIdx.x] = s;
     __threadfence();
@@ -345,19 +350,18 @@ void pcg_reset(PCGState* st, cudaStream_t s) {
   TG_CHECK_LAUNCH();
 }
 
-// r32 = r64 / sqrt(rr) ;   x64 += sqrt(rr) * d32
+// r32 = r64 / ||r64|| ;   x64 += ||r64|| * d32   (the norm comes from DOT_RR)
 __global__ void k_to_unit_f32(int64_t n, const double* __restrict__ r, const PCGState* st,
                               float* __restrict__ r32) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const double inv = 1.0 / sqrt(st->rr);
-  r32[i] = (float)(r[i] * inv);
+  r32[i] = (float)r[i] * (float)st->rinv;
 }
 __global__ void k_add_scaled_f32(int64_t n, const float* __restrict__ d, const PCGState* st,
                                  double* __restrict__ x) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
-  x[i] += sqrt(st->rr) * (double)d[i];
+  x[i] = fma(st->rnorm, (double)d[i], x[i]);
 }
 void to_unit_f32(int64_t n, const double* r, const PCGState* st, float* r32, cudaStream_t s) {
   k_to_unit_f32<<<(unsigned)cdiv(n, 256), 256, 0, s>>>(n, r, st, r32);
@@ -372,14 +376,14 @@ void add_scaled_f32(int64_t n, const float* d, const PCGState* st, double* x, cu
 // small helpers
 // ---------------------------------------------------------------------------
 template <typename T>
-__global__ void k_scale_mul(int64_t n, double a, const T* __restrict__ d, const T* __restrict__ b,
+__global__ void k_scale_mul(int64_t n, T a, const T* __restrict__ d, const T* __restrict__ b,
                             T* __restrict__ x) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i < n) x[i] = (T)(a * (double)d[i] * (double)b[i]);
+  if (i < n) x[i] = a * d[i] * b[i];
 }
 template <typename T>
 void scale_mul(int64_t n, double a, const T* d, const T* b, T* x, cudaStream_t s) {
-  k_scale_mul<T><<<(unsigned)cdiv(n, 256), 256, 0, s>>>(n, a, d, b, x);
+  k_scale_mul<T><<<(unsigned)cdiv(n, 256), 256, 0, s>>>(n, (T)a, d, b, x);
   TG_CHECK_LAUNCH();
 }
 template void scale_mul<double>(int64_t, double, const double*, const double*, double*, cudaStream_t);

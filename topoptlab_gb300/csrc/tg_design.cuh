@@ -15,7 +15,7 @@ struct OCState {
 // PCG scalars (linear_solvers.py:114-134)
 enum DotOp : int { DOT_RHO = 0, DOT_ALPHA = 1, DOT_RR = 2, DOT_BB = 3 };
 struct PCGState {
-  double rho, beta, alpha, pq, rr, bb;
+  double rho, beta, alpha, pq, rr, bb, rnorm, rinv;
   int iter;
   unsigned int ticket;
 };

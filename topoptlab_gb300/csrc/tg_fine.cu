@@ -341,20 +341,20 @@ __global__ void k_fine_dinv(Grid g, const uint8_t* fix, const S* scale, T* dinv,
   const int y = (int)(n % g.nny);
   const int x = (int)((n / g.nny) % g.nnx);
   const int z = (int)(n / ((int64_t)g.nny * g.nnx));
-  double acc[NDOF];
+  T acc[NDOF];   // in the operator's own precision (no FP64 work in the FP32 path)
 #pragma unroll
-  for (int c = 0; c < NDOF; ++c) acc[c] = 0.0;
+  for (int c = 0; c < NDOF; ++c) acc[c] = T(0);
 #pragma unroll
   for (int d = 0; d < (1 << NDIM); ++d) {
     const int ex = x - (d & 1), ey = y - ((d >> 1) & 1), ez = (NDIM == 3) ? z - ((d >> 2) & 1) : 0;
     if (ex < 0 || ex >= g.nex || ey < 0 || ey >= g.ney || ez < 0 || ez >= g.nez) continue;
-    const double s = (double)load_scale<T, S>(scale, g.elem(ex, ey, ez));
+    const T s = load_scale<T, S>(scale, g.elem(ex, ey, ez));
 #pragma unroll
-    for (int c = 0; c < NDOF; ++c) acc[c] += s * op.KEdiag[d * NDOF + c];
+    for (int c = 0; c < NDOF; ++c) acc[c] = fma(s, (T)op.KEdiag[d * NDOF + c], acc[c]);
   }
 #pragma unroll
   for (int c = 0; c < NDOF; ++c)
-    dinv[n * NDOF + c] = ((fix[n] >> c) & 1) ? T(0) : (T)(1.0 / acc[c]);
+    dinv[n * NDOF + c] = ((fix[n] >> c) & 1) ? T(0) : T(1) / acc[c];
 }
 
 template <typename T, typename S>
