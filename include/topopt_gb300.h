@@ -162,6 +162,37 @@ int32_t tg_levels(tg_ctx* ctx, int32_t* nlevels, int64_t* ndofs_per_level /* >= 
 /* assembled stencil of level >= 1 for the densities xPhys, layout
  * [(dir*ndof+ci)*ndof+cj][node], n = 3^ndim*ndof^2*nnodes(level) */
 int32_t tg_coarse_stencil(tg_ctx* ctx, const double* xPhys, int32_t level, double* out, int64_t n);
+/* Learned warm start (no counterpart in the reference: new capability of the
+ * GB300 solver).  A 3-level 3-D convolutional encoder-decoder (16/32/64
+ * channels, FP32) on the context's multigrid level-1 node grid predicts a
+ * level-1 displacement correction from the filtered density, the previous
+ * displacement and its residual; the warm start is u_prev + P(correction).
+ * tg_step keeps u_prev whenever the candidate's residual is not smaller
+ * (tg_iter_out.fallback = 1).  Training runs on the GPU with the library's
+ * own forward / backward / Adam kernels. */
+typedef struct tg_cnn tg_cnn;
+/* network for ctx (3-D elasticity, >= 2 multigrid levels); capacity = number
+ * of training samples to hold; seed = weight initialisation */
+int32_t tg_cnn_create(tg_ctx* ctx, int32_t capacity, uint64_t seed, tg_cnn** out);
+void tg_cnn_destroy(tg_cnn* cnn);
+/* use cnn for the warm starts of ctx's tg_step (NULL detaches) */
+int32_t tg_cnn_attach(tg_ctx* ctx, tg_cnn* cnn);
+/* record one training pair around a tg_step: begin (features of the current
+ * design and displacement) before the step, end (target = new - previous
+ * displacement) after it */
+int32_t tg_cnn_record_begin(tg_cnn* cnn, tg_ctx* ctx);
+int32_t tg_cnn_record_end(tg_cnn* cnn, tg_ctx* ctx);
+/* Adam (lr, beta 0.9 / 0.999) over the recorded pairs; final mean loss */
+int32_t tg_cnn_train(tg_cnn* cnn, int32_t epochs, double lr, uint64_t seed, double* final_loss);
+/* parameter count, level-1 grid (nx, ny, nz), recorded samples */
+int32_t tg_cnn_info(tg_cnn* cnn, int64_t* nparams, int32_t* grid_dims, int32_t* nsamples);
+/* copy the flat parameter vector out (set = 0) or in (set = 1) */
+int32_t tg_cnn_params(tg_cnn* cnn, int32_t set, float* host, int64_t n);
+/* forward pass on host features x0 [nodes][7] -> y [nodes][3]; with a target
+ * also the MSE loss and the parameter gradient (host buffers, y / loss /
+ * grads may be NULL) */
+int32_t tg_cnn_eval(tg_cnn* cnn, const float* x0, const float* target, float* y, double* loss,
+                    float* grads);
 /* Device time between two calls on the context's stream: op 0 records the
  * start event, op 1 records the stop event, synchronises and writes the
  * elapsed milliseconds to *ms. */

@@ -78,6 +78,16 @@ SIGNATURES = {
     "tg_vcycle": (C.c_int32, [C.c_void_p, _dp, _dp, _dp, C.c_int32]),
     "tg_levels": (C.c_int32, [C.c_void_p, _i32p, _i64p]),
     "tg_coarse_stencil": (C.c_int32, [C.c_void_p, _dp, C.c_int32, _dp, C.c_int64]),
+    "tg_cnn_create": (C.c_int32, [C.c_void_p, C.c_int32, C.c_uint64, C.POINTER(C.c_void_p)]),
+    "tg_cnn_destroy": (None, [C.c_void_p]),
+    "tg_cnn_attach": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "tg_cnn_record_begin": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "tg_cnn_record_end": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "tg_cnn_train": (C.c_int32, [C.c_void_p, C.c_int32, C.c_double, C.c_uint64, _dp]),
+    "tg_cnn_info": (C.c_int32, [C.c_void_p, _i64p, _i32p, _i32p]),
+    "tg_cnn_params": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(C.c_float), C.c_int64]),
+    "tg_cnn_eval": (C.c_int32, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                C.POINTER(C.c_float), _dp, C.POINTER(C.c_float)]),
     "tg_timer": (C.c_int32, [C.c_void_p, C.c_int32, _dp]),
     "tg_profile_kernel": (C.c_int32, [C.c_int32]),
     "tg_stats": (C.c_int32, [C.c_int32, _i64p, _dp, _i64p]),

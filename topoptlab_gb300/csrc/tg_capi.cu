@@ -4,6 +4,7 @@
 #include <cstring>
 #include <vector>
 #include "tg_ctx.cuh"
+#include "tg_cnn.cuh"
 #include "../../include/topopt_gb300.h"
 
 struct tg_ctx {
@@ -345,6 +346,119 @@ int32_t tg_edofmat(int32_t ndim, int32_t nelx, int32_t nely, int32_t nelz, int32
     d.alloc(n);
     tg::edofmat(g, d, 0);
     TG_CUDA(cudaMemcpy(out, d.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
+  });
+}
+
+// ---------------------------------------------------------------------------
+// learned warm start
+// ---------------------------------------------------------------------------
+struct tg_cnn {
+  tg_ctx* owner;
+  tg::Cnn* net;
+};
+
+int32_t tg_cnn_create(tg_ctx* ctx, int32_t capacity, uint64_t seed, tg_cnn** out) {
+  if (!ctx || !out || capacity < 0) return TG_EINVAL;
+  *out = nullptr;
+  return guarded(ctx, [&] {
+    tg_cnn* w = new tg_cnn{ctx, nullptr};
+    try {
+      w->net = new tg::Cnn(ctx->c, capacity, seed);
+    } catch (...) {
+      delete w;
+      throw;
+    }
+    *out = w;
+  });
+}
+
+void tg_cnn_destroy(tg_cnn* cnn) {
+  if (!cnn) return;
+  if (cnn->owner && cnn->owner->c.cnn == cnn->net) cnn->owner->c.cnn = nullptr;
+  cudaSetDevice(cnn->owner->c.dev);
+  cudaStreamSynchronize(cnn->owner->c.st);
+  delete cnn->net;
+  delete cnn;
+}
+
+int32_t tg_cnn_attach(tg_ctx* ctx, tg_cnn* cnn) {
+  if (!ctx) return TG_EINVAL;
+  return guarded(ctx, [&] {
+    TG_REQUIRE(!cnn || cnn->owner == ctx, "the network belongs to another context");
+    ctx->c.cnn = cnn ? cnn->net : nullptr;
+    ctx->c.learned = cnn ? 1 : 0;
+  });
+}
+
+int32_t tg_cnn_record_begin(tg_cnn* cnn, tg_ctx* ctx) {
+  if (!cnn || !ctx) return TG_EINVAL;
+  return guarded(ctx, [&] {
+    TG_REQUIRE(cnn->owner == ctx, "the network belongs to another context");
+    cnn->net->record_begin(ctx->c);
+  });
+}
+
+int32_t tg_cnn_record_end(tg_cnn* cnn, tg_ctx* ctx) {
+  if (!cnn || !ctx) return TG_EINVAL;
+  return guarded(ctx, [&] {
+    TG_REQUIRE(cnn->owner == ctx, "the network belongs to another context");
+    cnn->net->record_end(ctx->c);
+  });
+}
+
+int32_t tg_cnn_train(tg_cnn* cnn, int32_t epochs, double lr, uint64_t seed, double* final_loss) {
+  if (!cnn || epochs < 1) return TG_EINVAL;
+  return guarded(cnn->owner, [&] {
+    const double l = cnn->net->train(epochs, (float)lr, seed);
+    if (final_loss) *final_loss = l;
+  });
+}
+
+int32_t tg_cnn_info(tg_cnn* cnn, int64_t* nparams, int32_t* grid_dims, int32_t* nsamples) {
+  if (!cnn) return TG_EINVAL;
+  return guarded(cnn->owner, [&] {
+    if (nparams) *nparams = cnn->net->nparams;
+    if (grid_dims) {
+      grid_dims[0] = cnn->net->A.nx;
+      grid_dims[1] = cnn->net->A.ny;
+      grid_dims[2] = cnn->net->A.nz;
+    }
+    if (nsamples) *nsamples = cnn->net->nsamples;
+  });
+}
+
+int32_t tg_cnn_params(tg_cnn* cnn, int32_t set, float* host, int64_t n) {
+  if (!cnn || !host) return TG_EINVAL;
+  return guarded(cnn->owner, [&] {
+    TG_REQUIRE(n == cnn->net->nparams, "tg_cnn_params: wrong element count");
+    cudaStream_t st = cnn->owner->c.st;
+    if (set) {
+      h2d(cnn->net->params.p, host, n, st);
+      TG_CUDA(cudaStreamSynchronize(st));
+      cnn->net->trained = true;   // loaded weights count as a trained network
+    } else {
+      d2h(host, cnn->net->params.p, n, st);
+    }
+  });
+}
+
+int32_t tg_cnn_eval(tg_cnn* cnn, const float* x0, const float* target, float* y, double* loss,
+                    float* grads) {
+  if (!cnn || !x0) return TG_EINVAL;
+  return guarded(cnn->owner, [&] {
+    tg::Cnn& net = *cnn->net;
+    cudaStream_t st = cnn->owner->c.st;
+    const int64_t na = net.A.n();
+    h2d(net.x0.p, x0, na * 7, st);
+    net.forward(st);
+    if (y) d2h(y, net.y.p, na * 3, st);
+    if (target) {
+      h2d(net.tgt.p, target, na * 3, st);
+      const double l = net.backward(st, true);
+      if (loss) *loss = l;
+      if (grads) d2h(grads, net.grads.p, net.nparams, st);
+    }
+    TG_CUDA(cudaStreamSynchronize(st));
   });
 }
 

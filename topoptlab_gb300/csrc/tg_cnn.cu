@@ -1,0 +1,631 @@
+// Learned warm start: a small 3-D convolutional encoder-decoder trained on the
+// GPU by the library's own forward / backward / Adam kernels.
+//
+// No counterpart in the reference (new capability of the spec solver).
+//
+// Grid: the multigrid's level-1 node grid (every second fine node), tensors
+// channels-last FP32, node index ((z*nnx)+x)*nny+y like every other array.
+// Network (3 levels, 16/32/64 channels, 3x3x3 stride-1 convolutions):
+//   x0 (7 ch: filtered density, u_prev/s_u, r/s_r)
+//   e1 = relu(conv 7->16)         level A (full)
+//   e2 = relu(conv 16->32 (pool e1))      level B (half)
+//   e3 = relu(conv 32->64 (pool e2))      level C (quarter)
+//   d2 = relu(conv 64->32 (up e3) + e2)   level B
+//   d1 = relu(conv 32->16 (up d2) + e1)   level A
+//   y  = conv 16->3 (d1)                  level A, linear
+// y * s_u is a level-1 displacement correction; the warm start is
+// u_prev + P (y * s_u) with the multigrid prolongation P.
+#include <algorithm>
+#include <cmath>
+#include <random>
+#include <vector>
+#include "tg_ctx.cuh"
+#include "tg_cnn.cuh"
+
+namespace tg {
+
+// ---------------------------------------------------------------------------
+// grid helpers
+// ---------------------------------------------------------------------------
+static NG half_grid(const NG& g) { return NG{(g.nx + 1) / 2, (g.ny + 1) / 2, (g.nz + 1) / 2}; }
+
+__device__ __forceinline__ void ng_xyz(const NG& g, int64_t i, int& x, int& y, int& z) {
+  y = (int)(i % g.ny);
+  x = (int)((i / g.ny) % g.nx);
+  z = (int)(i / ((int64_t)g.ny * g.nx));
+}
+__device__ __forceinline__ int64_t ng_idx(const NG& g, int x, int y, int z) {
+  return ((int64_t)z * g.nx + x) * g.ny + y;
+}
+
+// ---------------------------------------------------------------------------
+// 3x3x3 convolution, stride 1, zero padding (forward; also the input gradient
+// with flipped / transposed weights).  One thread per output node, CC output
+// channels per CTA; weights of the chunk staged in shared memory and read as
+// broadcasts.  Epilogue: + bias, + skip, relu, * (mask > 0).
+// ---------------------------------------------------------------------------
+template <int CIN, int CC>
+__global__ void __launch_bounds__(128) k_conv3(NG g, const float* __restrict__ in,
+                                               const float* __restrict__ W, int cout,
+                                               const float* __restrict__ bias,
+                                               const float* __restrict__ skip, int relu,
+                                               const float* __restrict__ mask,
+                                               float* __restrict__ out) {
+  extern __shared__ __align__(16) float ws[];      // [27][CIN][CC]
+  const int co0 = blockIdx.y * CC;
+  for (int i = threadIdx.x; i < 27 * CIN * CC; i += blockDim.x) {
+    const int j = i % CC, ci = (i / CC) % CIN, k = i / (CC * CIN);
+    ws[i] = (co0 + j < cout) ? W[((int64_t)k * CIN + ci) * cout + co0 + j] : 0.f;
+  }
+  __syncthreads();
+  const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (n >= g.n()) return;
+  int x, y, z;
+  ng_xyz(g, n, x, y, z);
+  float acc[CC];
+#pragma unroll
+  for (int j = 0; j < CC; ++j) acc[j] = (bias && co0 + j < cout) ? bias[co0 + j] : 0.f;
+#pragma unroll 1
+  for (int k = 0; k < 27; ++k) {
+    const int dy = k % 3 - 1, dx = (k / 3) % 3 - 1, dz = k / 9 - 1;
+    const int X = x + dx, Y = y + dy, Z = z + dz;
+    if (X < 0 || X >= g.nx || Y < 0 || Y >= g.ny || Z < 0 || Z >= g.nz) continue;
+    const float* src = in + ng_idx(g, X, Y, Z) * CIN;
+    const float* wk = ws + k * CIN * CC;
+#pragma unroll 4
+    for (int ci = 0; ci < CIN; ++ci) {
+      const float v = __ldg(src + ci);
+#pragma unroll
+      for (int j = 0; j < CC; ++j) acc[j] = fmaf(v, wk[ci * CC + j], acc[j]);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < CC; ++j) {
+    const int co = co0 + j;
+    if (co >= cout) break;
+    float v = acc[j];
+    if (skip) v += skip[n * cout + co];
+    if (relu) v = fmaxf(v, 0.f);
+    if (mask && !(mask[n * cout + co] > 0.f)) v = 0.f;
+    out[n * cout + co] = v;
+  }
+}
+
+template <int CIN>
+static void conv3_launch(const NG& g, const float* in, const float* W, int cout, const float* bias,
+                         const float* skip, int relu, const float* mask, float* out,
+                         cudaStream_t st) {
+  const int cc = cout >= 16 ? 16 : 4;
+  const unsigned gx = (unsigned)cdiv(g.n(), 128);
+  if (cc == 16) {
+    const size_t smem = sizeof(float) * 27 * CIN * 16;
+    static bool set = false;
+    if (!set) {
+      TG_CUDA(cudaFuncSetAttribute(k_conv3<CIN, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)smem));
+      set = true;
+    }
+    k_conv3<CIN, 16><<<dim3(gx, (unsigned)cdiv(cout, 16)), 128, smem, st>>>(g, in, W, cout, bias,
+                                                                          skip, relu, mask, out);
+  } else {
+    const size_t smem = sizeof(float) * 27 * CIN * 4;
+    k_conv3<CIN, 4><<<dim3(gx, (unsigned)cdiv(cout, 4)), 128, smem, st>>>(g, in, W, cout, bias,
+                                                                        skip, relu, mask, out);
+  }
+  TG_CHECK_LAUNCH();
+}
+
+static void conv3(const NG& g, int cin, const float* in, const float* W, int cout,
+                  const float* bias, const float* skip, int relu, const float* mask, float* out,
+                  cudaStream_t st) {
+  switch (cin) {
+    case 3: conv3_launch<3>(g, in, W, cout, bias, skip, relu, mask, out, st); break;
+    case 7: conv3_launch<7>(g, in, W, cout, bias, skip, relu, mask, out, st); break;
+    case 16: conv3_launch<16>(g, in, W, cout, bias, skip, relu, mask, out, st); break;
+    case 32: conv3_launch<32>(g, in, W, cout, bias, skip, relu, mask, out, st); break;
+    case 64: conv3_launch<64>(g, in, W, cout, bias, skip, relu, mask, out, st); break;
+    default: throw Error{EINVAL_, "conv3: unsupported input channel count"};
+  }
+}
+
+// W'[k'][co][ci] = W[26-k'][ci][co]: the input gradient is a convolution of the
+// output gradient with these weights
+__global__ void k_flip_transpose(const float* W, int cin, int cout, float* Wt) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= (int64_t)27 * cin * cout) return;
+  const int ci = (int)(i % cin), co = (int)((i / cin) % cout), k = (int)(i / ((int64_t)cin * cout));
+  Wt[i] = W[((int64_t)(26 - k) * cin + ci) * cout + co];
+}
+
+// ---------------------------------------------------------------------------
+// weight gradient: dW[k][ci][co] = sum_n in[n+off_k][ci] g[n][co]; one CTA per
+// (k, chunk of nodes) writes a partial, a second kernel sums the partials in
+// fixed order (deterministic, no atomics)
+// ---------------------------------------------------------------------------
+constexpr int DW_CHUNK = 2048;
+constexpr int DW_BATCH = 32;
+
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(256) k_conv3_dw(NG g, const float* __restrict__ in,
+                                                  const float* __restrict__ gout,
+                                                  float* __restrict__ part) {
+  constexpr int NP = CIN * COUT;
+  constexpr int PER = (NP + 255) / 256;
+  __shared__ float sin[DW_BATCH][CIN];
+  __shared__ float sgo[DW_BATCH][COUT];
+  const int k = blockIdx.y;
+  const int dy = k % 3 - 1, dx = (k / 3) % 3 - 1, dz = k / 9 - 1;
+  const int64_t n0 = (int64_t)blockIdx.x * DW_CHUNK;
+  const int64_t n1 = (n0 + DW_CHUNK < g.n()) ? n0 + DW_CHUNK : g.n();
+  float acc[PER];
+#pragma unroll
+  for (int p = 0; p < PER; ++p) acc[p] = 0.f;
+  for (int64_t b0 = n0; b0 < n1; b0 += DW_BATCH) {
+    for (int i = threadIdx.x; i < DW_BATCH * CIN; i += blockDim.x) {
+      const int v = i / CIN, ci = i % CIN;
+      const int64_t n = b0 + v;
+      float val = 0.f;
+      if (n < n1) {
+        int x, y, z;
+        ng_xyz(g, n, x, y, z);
+        const int X = x + dx, Y = y + dy, Z = z + dz;
+        if (X >= 0 && X < g.nx && Y >= 0 && Y < g.ny && Z >= 0 && Z < g.nz)
+          val = in[ng_idx(g, X, Y, Z) * CIN + ci];
+      }
+      sin[v][ci] = val;
+    }
+    for (int i = threadIdx.x; i < DW_BATCH * COUT; i += blockDim.x) {
+      const int v = i / COUT, co = i % COUT;
+      const int64_t n = b0 + v;
+      sgo[v][co] = (n < n1) ? gout[n * COUT + co] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int p = 0; p < PER; ++p) {
+      const int pi = threadIdx.x + p * 256;
+      if (pi < NP) {
+        const int ci = pi / COUT, co = pi % COUT;
+        float a = acc[p];
+#pragma unroll 8
+        for (int v = 0; v < DW_BATCH; ++v) a = fmaf(sin[v][ci], sgo[v][co], a);
+        acc[p] = a;
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int p = 0; p < PER; ++p) {
+    const int pi = threadIdx.x + p * 256;
+    if (pi < NP) part[((int64_t)blockIdx.x * 27 + k) * NP + pi] = acc[p];
+  }
+}
+
+__global__ void k_sum_parts(const float* part, int nchunks, int64_t m, float* out) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  double s = 0.0;
+  for (int c = 0; c < nchunks; ++c) s += part[(int64_t)c * m + i];
+  out[i] = (float)s;
+}
+
+// bias gradient db[co] = sum_n g[n][co] (one block per channel, fixed order)
+__global__ void k_bias_grad(const float* gout, int64_t n, int cout, float* db) {
+  __shared__ double sh[32];
+  const int co = blockIdx.x;
+  double s = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s += gout[i * cout + co];
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) db[co] = (float)s;
+}
+
+template <int CIN, int COUT>
+static void dw_launch(const NG& g, const float* in, const float* gout, float* part, float* dW,
+                      cudaStream_t st) {
+  const int nch = (int)cdiv(g.n(), DW_CHUNK);
+  k_conv3_dw<CIN, COUT><<<dim3(nch, 27), 256, 0, st>>>(g, in, gout, part);
+  TG_CHECK_LAUNCH();
+  const int64_t m = (int64_t)27 * CIN * COUT;
+  k_sum_parts<<<(unsigned)cdiv(m, 256), 256, 0, st>>>(part, nch, m, dW);
+  TG_CHECK_LAUNCH();
+}
+
+static void conv3_dw(const NG& g, int cin, int cout, const float* in, const float* gout,
+                     float* part, float* dW, float* db, cudaStream_t st) {
+  const int key = cin * 1000 + cout;
+  switch (key) {
+    case 7016: dw_launch<7, 16>(g, in, gout, part, dW, st); break;
+    case 16032: dw_launch<16, 32>(g, in, gout, part, dW, st); break;
+    case 32064: dw_launch<32, 64>(g, in, gout, part, dW, st); break;
+    case 64032: dw_launch<64, 32>(g, in, gout, part, dW, st); break;
+    case 32016: dw_launch<32, 16>(g, in, gout, part, dW, st); break;
+    case 16003: dw_launch<16, 3>(g, in, gout, part, dW, st); break;
+    default: throw Error{EINVAL_, "conv3_dw: unsupported channel pair"};
+  }
+  k_bias_grad<<<cout, 256, 0, st>>>(gout, g.n(), cout, db);
+  TG_CHECK_LAUNCH();
+}
+
+// ---------------------------------------------------------------------------
+// pooling (average of the present children), nearest upsampling, and their
+// adjoints; elementwise helpers
+// ---------------------------------------------------------------------------
+__global__ void k_pool(NG gf, NG gc, int C, const float* in, float* out) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= gc.n() * C) return;
+  const int c = (int)(t % C);
+  const int64_t I = t / C;
+  int X, Y, Z;
+  ng_xyz(gc, I, X, Y, Z);
+  float s = 0.f;
+  int cnt = 0;
+  for (int a = 0; a < 8; ++a) {
+    const int x = 2 * X + (a & 1), y = 2 * Y + ((a >> 1) & 1), z = 2 * Z + (a >> 2);
+    if (x < gf.nx && y < gf.ny && z < gf.nz) {
+      s += in[ng_idx(gf, x, y, z) * C + c];
+      ++cnt;
+    }
+  }
+  out[t] = s / (float)cnt;
+}
+__global__ void k_pool_bwd(NG gf, NG gc, int C, const float* gout, float* gin, int accumulate) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= gf.n() * C) return;
+  const int c = (int)(t % C);
+  const int64_t i = t / C;
+  int x, y, z;
+  ng_xyz(gf, i, x, y, z);
+  const int X = x / 2, Y = y / 2, Z = z / 2;
+  int cnt = 0;
+  for (int a = 0; a < 8; ++a) {
+    const int xx = 2 * X + (a & 1), yy = 2 * Y + ((a >> 1) & 1), zz = 2 * Z + (a >> 2);
+    if (xx < gf.nx && yy < gf.ny && zz < gf.nz) ++cnt;
+  }
+  const float v = gout[ng_idx(gc, X, Y, Z) * C + c] / (float)cnt;
+  gin[t] = accumulate ? gin[t] + v : v;
+}
+__global__ void k_up(NG gf, NG gc, int C, const float* in, float* out) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= gf.n() * C) return;
+  const int c = (int)(t % C);
+  int x, y, z;
+  ng_xyz(gf, t / C, x, y, z);
+  out[t] = in[ng_idx(gc, x / 2, y / 2, z / 2) * C + c];
+}
+__global__ void k_up_bwd(NG gf, NG gc, int C, const float* gout, float* gin) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= gc.n() * C) return;
+  const int c = (int)(t % C);
+  int X, Y, Z;
+  ng_xyz(gc, t / C, X, Y, Z);
+  float s = 0.f;
+  for (int a = 0; a < 8; ++a) {
+    const int x = 2 * X + (a & 1), y = 2 * Y + ((a >> 1) & 1), z = 2 * Z + (a >> 2);
+    if (x < gf.nx && y < gf.ny && z < gf.nz) s += gout[ng_idx(gf, x, y, z) * C + c];
+  }
+  gin[t] = s;
+}
+__global__ void k_add_inplace(int64_t n, const float* a, float* b) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) b[i] += a[i];
+}
+// gradient through relu: g *= (act > 0)
+__global__ void k_relu_mask(int64_t n, const float* act, float* g) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n && !(act[i] > 0.f)) g[i] = 0.f;
+}
+// MSE: L = mean((y - t)^2), dL/dy = 2 (y - t) / N; partial loss per block
+__global__ void k_mse(int64_t n, const float* y, const float* t, float* g, double* part) {
+  __shared__ double sh[32];
+  double s = 0.0;
+  const float scale = 2.f / (float)n;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float d = y[i] - t[i];
+    g[i] = scale * d;
+    s += (double)d * (double)d;
+  }
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+// Adam (Kingma & Ba), bias-corrected
+__global__ void k_adam(int64_t n, float* w, const float* g, float* m, float* v, float lr, float b1,
+                       float b2, float eps, float c1, float c2) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float gi = g[i];
+  const float mi = b1 * m[i] + (1.f - b1) * gi;
+  const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  w[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+}
+
+static unsigned nb(int64_t n) { return (unsigned)cdiv(n, 256); }
+
+// ---------------------------------------------------------------------------
+// features and targets from the solver state
+// ---------------------------------------------------------------------------
+// x0[I] = (density at fine node 2I, u(2I)/s_u, r(2I)/s_r) with the density
+// averaged over the fine elements touching the node
+__global__ void k_features(Grid gf, NG g1, const double* __restrict__ xPhys,
+                           const double* __restrict__ u, const float* __restrict__ r,
+                           const PCGState* su, const PCGState* sr, float* __restrict__ x0) {
+  const int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (I >= g1.n()) return;
+  int X, Y, Z;
+  ng_xyz(g1, I, X, Y, Z);
+  const int fx = 2 * X, fy = 2 * Y, fz = (gf.ndim == 3) ? 2 * Z : 0;
+  double dsum = 0.0;
+  int cnt = 0;
+  for (int a = 0; a < 8; ++a) {
+    const int ex = fx - (a & 1), ey = fy - ((a >> 1) & 1), ez = fz - (a >> 2);
+    if (ex < 0 || ex >= gf.nex || ey < 0 || ey >= gf.ney || ez < 0 || ez >= gf.nez) continue;
+    dsum += xPhys[gf.elem(ex, ey, ez)];
+    ++cnt;
+  }
+  const int64_t fn = gf.node(fx, fy, fz);
+  const float iu = (float)su->rinv, ir = (float)sr->rinv;
+  float* o = x0 + I * 7;
+  o[0] = (float)(dsum / cnt);
+  for (int c = 0; c < 3; ++c) {
+    o[1 + c] = (float)u[fn * 3 + c] * iu;
+    o[4 + c] = r[fn * 3 + c] * ir;
+  }
+}
+// target t[I] = (u_new(2I) - u_prev(2I)) / s_u
+__global__ void k_target(Grid gf, NG g1, const double* __restrict__ unew,
+                         const double* __restrict__ uprev, const PCGState* su, float* __restrict__ t) {
+  const int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (I >= g1.n()) return;
+  int X, Y, Z;
+  ng_xyz(g1, I, X, Y, Z);
+  const int64_t fn = gf.node(2 * X, 2 * Y, (gf.ndim == 3) ? 2 * Z : 0);
+  const float iu = (float)su->rinv;
+  for (int c = 0; c < 3; ++c) t[I * 3 + c] = (float)(unew[fn * 3 + c] - uprev[fn * 3 + c]) * iu;
+}
+// level-1 correction in FP64: d[I] = y[I] * s_u
+__global__ void k_correction(int64_t n, const float* y, const PCGState* su, double* d) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) d[i] = (double)y[i] * su->rnorm;
+}
+
+// ---------------------------------------------------------------------------
+// the network object
+// ---------------------------------------------------------------------------
+Cnn::Cnn(Ctx& c, int capacity, uint64_t seed) : ctx(&c) {
+  TG_REQUIRE(c.g.ndim == 3 && c.g.ndof == 3, "the learned warm start is built for 3-D elasticity");
+  TG_REQUIRE(c.L >= 2, "the learned warm start needs a multigrid context (>= 2 levels)");
+  const Grid& g1 = c.lv[1]->g;
+  A = NG{g1.nnx, g1.nny, g1.nnz};
+  B = half_grid(A);
+  Cg = half_grid(B);
+  const int spec[6][2] = {{7, 16}, {16, 32}, {32, 64}, {64, 32}, {32, 16}, {16, 3}};
+  int64_t off = 0;
+  for (auto& s : spec) {
+    Layer l{s[0], s[1], off, 0};
+    off += (int64_t)27 * s[0] * s[1];
+    l.b_off = off;
+    off += s[1];
+    layers.push_back(l);
+  }
+  nparams = off;
+  params.alloc(nparams); grads.alloc(nparams); adam_m.alloc(nparams); adam_v.alloc(nparams);
+  wt.alloc((int64_t)27 * 64 * 64);
+  adam_m.zero(c.st);
+  adam_v.zero(c.st);
+  // He-normal initialisation from a seeded generator
+  std::vector<float> h(nparams, 0.f);
+  std::mt19937_64 rng(seed);
+  for (auto& l : layers) {
+    std::normal_distribution<float> nd(0.f, std::sqrt(2.f / (27.f * l.cin)));
+    for (int64_t i = 0; i < (int64_t)27 * l.cin * l.cout; ++i) h[l.w_off + i] = nd(rng);
+  }
+  TG_CUDA(cudaMemcpy(params.p, h.data(), sizeof(float) * nparams, cudaMemcpyHostToDevice));
+  const int64_t na = A.n(), nbn = B.n(), nc = Cg.n();
+  x0.alloc(na * 7); e1.alloc(na * 16); p1.alloc(nbn * 16); e2.alloc(nbn * 32); p2.alloc(nc * 32);
+  e3.alloc(nc * 64); u2.alloc(nbn * 64); d2.alloc(nbn * 32); u1.alloc(na * 32); d1.alloc(na * 16);
+  y.alloc(na * 3); tgt.alloc(na * 3);
+  g_a16.alloc(na * 16); g_a32.alloc(na * 32); g_b64.alloc(nbn * 64); g_b32.alloc(nbn * 32);
+  g_b16.alloc(nbn * 16); g_c64.alloc(nc * 64); g_c32.alloc(nc * 32); g_e1.alloc(na * 16);
+  g_e2.alloc(nbn * 32); g_y.alloc(na * 3);
+  dw_part.alloc(cdiv(na, DW_CHUNK) * 27 * 64 * 64);
+  loss_part.alloc(RED_BLOCKS);
+  loss_out.alloc(1);
+  capacity_ = capacity;
+  data_x.alloc((int64_t)capacity * na * 7);
+  data_t.alloc((int64_t)capacity * na * 3);
+  uprev.alloc(c.g.ndofs());
+  corr.alloc(g1.ndofs());
+  r32a.alloc(c.g.ndofs());
+  su.alloc(1); sr.alloc(1); su.zero(c.st); sr.zero(c.st);
+  TG_CUDA(cudaStreamSynchronize(c.st));
+}
+
+void Cnn::forward(cudaStream_t st) {
+  const float* P = params.p;
+  auto W = [&](int i) { return P + layers[i].w_off; };
+  auto b = [&](int i) { return P + layers[i].b_off; };
+  conv3(A, 7, x0, W(0), 16, b(0), nullptr, 1, nullptr, e1, st);
+  k_pool<<<nb(B.n() * 16), 256, 0, st>>>(A, B, 16, e1, p1);
+  TG_CHECK_LAUNCH();
+  conv3(B, 16, p1, W(1), 32, b(1), nullptr, 1, nullptr, e2, st);
+  k_pool<<<nb(Cg.n() * 32), 256, 0, st>>>(B, Cg, 32, e2, p2);
+  TG_CHECK_LAUNCH();
+  conv3(Cg, 32, p2, W(2), 64, b(2), nullptr, 1, nullptr, e3, st);
+  k_up<<<nb(B.n() * 64), 256, 0, st>>>(B, Cg, 64, e3, u2);
+  TG_CHECK_LAUNCH();
+  conv3(B, 64, u2, W(3), 32, b(3), e2, 1, nullptr, d2, st);
+  k_up<<<nb(A.n() * 32), 256, 0, st>>>(A, B, 32, d2, u1);
+  TG_CHECK_LAUNCH();
+  conv3(A, 32, u1, W(4), 16, b(4), e1, 1, nullptr, d1, st);
+  conv3(A, 16, d1, W(5), 3, b(5), nullptr, 0, nullptr, y, st);
+}
+
+// loss against tgt, gradients into grads (forward must have run)
+double Cnn::backward(cudaStream_t st, bool want_loss) {
+  const float* P = params.p;
+  float* G = grads.p;
+  auto gW = [&](int i) { return G + layers[i].w_off; };
+  auto gb = [&](int i) { return G + layers[i].b_off; };
+  auto flip = [&](int i) {
+    const Layer& l = layers[i];
+    k_flip_transpose<<<nb((int64_t)27 * l.cin * l.cout), 256, 0, st>>>(P + l.w_off, l.cin, l.cout, wt);
+    TG_CHECK_LAUNCH();
+  };
+  const int64_t na = A.n(), nbn = B.n(), nc = Cg.n();
+  const unsigned lb = red_blocks(na * 3);
+  k_mse<<<lb, RED_THREADS, 0, st>>>(na * 3, y, tgt, g_y, loss_part);
+  TG_CHECK_LAUNCH();
+  // head: y = conv(d1)
+  conv3_dw(A, 16, 3, d1, g_y, dw_part, gW(5), gb(5), st);
+  flip(5);
+  conv3(A, 3, g_y, wt, 16, nullptr, nullptr, 0, d1, g_a16, st);        // g(pre d1) = dx * (d1 > 0)
+  // d1 = relu(conv(u1) + e1)
+  conv3_dw(A, 32, 16, u1, g_a16, dw_part, gW(4), gb(4), st);
+  TG_CUDA(cudaMemcpyAsync(g_e1.p, g_a16.p, sizeof(float) * na * 16, cudaMemcpyDeviceToDevice, st));
+  flip(4);
+  conv3(A, 16, g_a16, wt, 32, nullptr, nullptr, 0, nullptr, g_a32, st);  // g(u1)
+  k_up_bwd<<<nb(nbn * 32), 256, 0, st>>>(A, B, 32, g_a32, g_b32);       // g(d2)
+  TG_CHECK_LAUNCH();
+  k_relu_mask<<<nb(nbn * 32), 256, 0, st>>>(nbn * 32, d2, g_b32);        // g(pre d2)
+  TG_CHECK_LAUNCH();
+  // d2 = relu(conv(u2) + e2)
+  conv3_dw(B, 64, 32, u2, g_b32, dw_part, gW(3), gb(3), st);
+  TG_CUDA(cudaMemcpyAsync(g_e2.p, g_b32.p, sizeof(float) * nbn * 32, cudaMemcpyDeviceToDevice, st));
+  flip(3);
+  conv3(B, 32, g_b32, wt, 64, nullptr, nullptr, 0, nullptr, g_b64, st);  // g(u2)
+  k_up_bwd<<<nb(nc * 64), 256, 0, st>>>(B, Cg, 64, g_b64, g_c64);        // g(e3)
+  TG_CHECK_LAUNCH();
+  k_relu_mask<<<nb(nc * 64), 256, 0, st>>>(nc * 64, e3, g_c64);
+  TG_CHECK_LAUNCH();
+  // e3 = relu(conv(p2))
+  conv3_dw(Cg, 32, 64, p2, g_c64, dw_part, gW(2), gb(2), st);
+  flip(2);
+  conv3(Cg, 64, g_c64, wt, 32, nullptr, nullptr, 0, nullptr, g_c32, st); // g(p2)
+  k_pool_bwd<<<nb(nbn * 32), 256, 0, st>>>(B, Cg, 32, g_c32, g_e2, 1);  // g(e2) += pool^T g(p2)
+  TG_CHECK_LAUNCH();
+  k_relu_mask<<<nb(nbn * 32), 256, 0, st>>>(nbn * 32, e2, g_e2);
+  TG_CHECK_LAUNCH();
+  // e2 = relu(conv(p1))
+  conv3_dw(B, 16, 32, p1, g_e2, dw_part, gW(1), gb(1), st);
+  flip(1);
+  conv3(B, 32, g_e2, wt, 16, nullptr, nullptr, 0, nullptr, g_b16, st);  // g(p1)
+  k_pool_bwd<<<nb(na * 16), 256, 0, st>>>(A, B, 16, g_b16, g_e1, 1);    // g(e1) += pool^T g(p1)
+  TG_CHECK_LAUNCH();
+  k_relu_mask<<<nb(na * 16), 256, 0, st>>>(na * 16, e1, g_e1);
+  TG_CHECK_LAUNCH();
+  // e1 = relu(conv(x0))
+  conv3_dw(A, 7, 16, x0, g_e1, dw_part, gW(0), gb(0), st);
+  if (!want_loss) return 0.0;
+  reduce_partials(loss_part, (int)lb, loss_out, false, st);
+  double l = 0.0;
+  TG_CUDA(cudaMemcpyAsync(&l, loss_out.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+  TG_CUDA(cudaStreamSynchronize(st));
+  return l / (double)(na * 3);
+}
+
+void Cnn::adam_step(cudaStream_t st) {
+  ++adam_t;
+  const float b1 = 0.9f, b2 = 0.999f;
+  const float c1 = 1.f - std::pow(b1, (float)adam_t), c2 = 1.f - std::pow(b2, (float)adam_t);
+  k_adam<<<nb(nparams), 256, 0, st>>>(nparams, params, grads, adam_m, adam_v, lr, b1, b2, 1e-8f,
+                                      c1, c2);
+  TG_CHECK_LAUNCH();
+}
+
+// ---------------------------------------------------------------------------
+// solver-state interface
+// ---------------------------------------------------------------------------
+// r32a = f - K(xPhys) u in FP32 (scale factors s32 must hold simp(xPhys))
+static void residual32(Ctx& c, const double* u, float* out) {
+  const int64_t n = c.g.ndofs();
+  d2f(n, u, c.p32, c.st);
+  d2f(n, c.f, c.q32, c.st);
+  fine_apply<float, float>(c.op, c.s32, c.p32, out, c.q32, nullptr, 0.0, AM_RES, c.st);
+}
+
+void Cnn::features(Ctx& c, const double* u_prev) {
+  const int64_t n = c.g.ndofs();
+  residual32(c, u_prev, r32a);
+  pcg_reset(su, c.st);
+  dot<double, double>(n, u_prev, u_prev, c.part, su, DOT_RR, c.st);
+  pcg_reset(sr, c.st);
+  dot<float, float>(n, r32a.p, r32a.p, c.part, sr, DOT_RR, c.st);
+  k_features<<<nb(A.n()), 256, 0, c.st>>>(c.g, A, c.xPhys, u_prev, r32a, su, sr, x0);
+  TG_CHECK_LAUNCH();
+}
+
+void Cnn::record_begin(Ctx& c) {
+  TG_REQUIRE(nsamples < capacity_, "training set is full");
+  TG_REQUIRE(c.precision == TG_PREC_MIXED, "recording needs a mixed-precision context");
+  set_density(c, c.xPhys);
+  TG_CUDA(cudaMemcpyAsync(uprev.p, c.u.p, sizeof(double) * c.g.ndofs(), cudaMemcpyDeviceToDevice, c.st));
+  features(c, uprev);
+  TG_CUDA(cudaMemcpyAsync(data_x.p + (int64_t)nsamples * A.n() * 7, x0.p, sizeof(float) * A.n() * 7,
+                          cudaMemcpyDeviceToDevice, c.st));
+}
+
+void Cnn::record_end(Ctx& c) {
+  k_target<<<nb(A.n()), 256, 0, c.st>>>(c.g, A, c.u, uprev, su,
+                                        data_t.p + (int64_t)nsamples * A.n() * 3);
+  TG_CHECK_LAUNCH();
+  ++nsamples;
+  TG_CUDA(cudaStreamSynchronize(c.st));
+}
+
+double Cnn::train(int epochs, float lr_, uint64_t seed) {
+  TG_REQUIRE(nsamples > 0, "no training samples recorded");
+  lr = lr_;
+  cudaStream_t st = ctx->st;
+  std::mt19937_64 rng(seed);
+  std::vector<int> order(nsamples);
+  double last = 0.0;
+  for (int e = 0; e < epochs; ++e) {
+    for (int i = 0; i < nsamples; ++i) order[i] = i;
+    std::shuffle(order.begin(), order.end(), rng);
+    double sum = 0.0;
+    for (int i = 0; i < nsamples; ++i) {
+      const int s = order[i];
+      TG_CUDA(cudaMemcpyAsync(x0.p, data_x.p + (int64_t)s * A.n() * 7, sizeof(float) * A.n() * 7,
+                              cudaMemcpyDeviceToDevice, st));
+      TG_CUDA(cudaMemcpyAsync(tgt.p, data_t.p + (int64_t)s * A.n() * 3, sizeof(float) * A.n() * 3,
+                              cudaMemcpyDeviceToDevice, st));
+      forward(st);
+      sum += backward(st, e == epochs - 1);
+      adam_step(st);
+    }
+    if (e == epochs - 1) last = sum / nsamples;
+  }
+  TG_CUDA(cudaStreamSynchronize(st));
+  trained = true;
+  return last;
+}
+
+// Warm start for the current design: u_prev + P (network correction); keeps
+// u_prev when the candidate's FP32 residual is not smaller.  Returns 1 on
+// fallback.
+int Cnn::warm_start(Ctx& c) {
+  const int64_t n = c.g.ndofs();
+  double* cand = c.z2.p;
+  features(c, c.u);            // also leaves r32a = f - K u_prev
+  forward(c.st);
+  k_correction<<<nb(c.lv[1]->g.ndofs()), 256, 0, c.st>>>(c.lv[1]->g.ndofs(), y, su, corr);
+  TG_CHECK_LAUNCH();
+  TG_CUDA(cudaMemcpyAsync(cand, c.u.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, c.st));
+  prolong_add<double>(c.g, c.lv[1]->g, c.op.fix, corr, cand, c.st);
+  residual32(c, cand, c.r32);
+  pcg_reset(c.pcg_out, c.st);
+  dot<float, float>(n, c.r32.p, c.r32.p, c.part, c.pcg_out, DOT_RR, c.st);
+  PCGState hs{};
+  TG_CUDA(cudaMemcpyAsync(&hs, c.pcg_out.p, sizeof(PCGState), cudaMemcpyDeviceToHost, c.st));
+  PCGState hp{};
+  TG_CUDA(cudaMemcpyAsync(&hp, sr.p, sizeof(PCGState), cudaMemcpyDeviceToHost, c.st));
+  TG_CUDA(cudaStreamSynchronize(c.st));
+  if (std::isfinite(hs.rr) && hs.rr < hp.rr) {
+    TG_CUDA(cudaMemcpyAsync(c.u.p, cand, sizeof(double) * n, cudaMemcpyDeviceToDevice, c.st));
+    return 0;
+  }
+  return 1;
+}
+
+}  // namespace tg

@@ -1,0 +1,52 @@
+// The learned warm-start network (see tg_cnn.cu).
+#pragma once
+#include <vector>
+#include "tg_ctx.cuh"
+
+namespace tg {
+
+// node grid of one network level
+struct NG {
+  int nx, ny, nz;
+  __host__ __device__ int64_t n() const { return (int64_t)nx * ny * nz; }
+};
+
+struct Layer {
+  int cin, cout;
+  int64_t w_off, b_off;    // offsets of W[27][cin][cout] and b[cout] in the parameter buffer
+};
+
+struct Cnn {
+  Ctx* ctx;
+  NG A{}, B{}, Cg{};               // full / half / quarter of the level-1 node grid
+  std::vector<Layer> layers;
+  int64_t nparams = 0;
+  DevBuf<float> params, grads, adam_m, adam_v, wt;
+  // activations (channels-last) and their gradients
+  DevBuf<float> x0, e1, p1, e2, p2, e3, u2, d2, u1, d1, y, tgt;
+  DevBuf<float> g_a16, g_a32, g_b64, g_b32, g_b16, g_c64, g_c32, g_e1, g_e2, g_y;
+  DevBuf<float> dw_part;
+  DevBuf<double> loss_part, loss_out;
+  // training set recorded from solver runs
+  int capacity_ = 0, nsamples = 0;
+  DevBuf<float> data_x, data_t;
+  // solver-state scratch
+  DevBuf<double> uprev, corr;
+  DevBuf<float> r32a;
+  DevBuf<PCGState> su, sr;       // norms of u_prev and of its residual
+  float lr = 1e-3f;
+  int adam_t = 0;
+  bool trained = false;
+
+  Cnn(Ctx& c, int capacity, uint64_t seed);
+  void forward(cudaStream_t st);
+  double backward(cudaStream_t st, bool want_loss);
+  void adam_step(cudaStream_t st);
+  void features(Ctx& c, const double* u_prev);
+  void record_begin(Ctx& c);
+  void record_end(Ctx& c);
+  double train(int epochs, float lr, uint64_t seed);
+  int warm_start(Ctx& c);
+};
+
+}  // namespace tg

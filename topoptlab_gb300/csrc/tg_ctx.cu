@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstring>
 #include "tg_ctx.cuh"
+#include "tg_cnn.cuh"
 #include "../../include/topopt_gb300.h"
 
 namespace tg {
@@ -591,6 +592,10 @@ void ctx_step(Ctx& c, tg_iter_out& out) {
   set_density(c, c.xPhys);
   TG_CUDA(cudaEventRecord(c.ev0, c.st));
   build_hierarchy(c);
+  // learned warm start (falls back to the previous displacement when its
+  // residual is not smaller); the solve below is unchanged either way
+  int fallback = 0;
+  if (c.learned && c.cnn && c.cnn->trained && c.iter > 0) fallback = c.cnn->warm_start(c);
   solve(c, c.f, c.u);
   TG_CUDA(cudaEventRecord(c.ev1, c.st));
   // compliance + raw sensitivity
@@ -634,7 +639,7 @@ void ctx_step(Ctx& c, tg_iter_out& out) {
   out.vcycles = c.last_vcycles;
   out.refinements = c.last_refine;
   out.oc_steps = c.h_oc->nsteps;
-  out.fallback = 0;
+  out.fallback = fallback;
   out.nlevels = c.L;
   out.t_solve_ms = ms;
   check_finite(out.obj, "objective");

@@ -93,6 +93,7 @@ struct Ctx {
     int64_t launches = 0;        // kernels per replay
   } g64, g32;
   bool use_graphs = true;
+  struct Cnn* cnn = nullptr;     // learned warm start (not owned)
   // statistics of the last solve
   int last_iters = 0, last_vcycles = 0, last_refine = 0, last_converged = 0;
   double last_relres = 0.0;
