@@ -438,6 +438,7 @@ Cnn::Cnn(Ctx& c, int capacity, uint64_t seed) : ctx(&c) {
   corr.alloc(g1.ndofs());
   r32a.alloc(c.g.ndofs());
   su.alloc(1); sr.alloc(1); su.zero(c.st); sr.zero(c.st);
+  gal.alloc(5); gal.zero(c.st);
   TG_CUDA(cudaStreamSynchronize(c.st));
 }
 
@@ -601,25 +602,55 @@ double Cnn::train(int epochs, float lr_, uint64_t seed) {
   return last;
 }
 
-// Warm start for the current design: u_prev + P (network correction); keeps
-// u_prev when the candidate's FP32 residual is not smaller.  Returns 1 on
-// fallback.
+__global__ void k_combine(int64_t n, double c1, const double* v1, double c2, const double* v2,
+                          double* out) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = c1 * v1[i] + c2 * v2[i];
+}
+
+// Warm start for the current design.  The network's level-1 correction is
+// prolongated to the fine grid (v2 = P d) and combined with the previous
+// displacement (v1) by the energy-optimal (Galerkin) 2x2 solve
+//   [v_i^T K v_j] c = [v_i^T f],   u0 = c1 v1 + c2 v2,
+// with the products in FP32; u0 replaces u_prev only when its FP32 residual
+// is smaller.  Returns 1 on fallback.
 int Cnn::warm_start(Ctx& c) {
   const int64_t n = c.g.ndofs();
-  double* cand = c.z2.p;
+  double* v2 = c.z2.p;
   features(c, c.u);            // also leaves r32a = f - K u_prev
   forward(c.st);
   k_correction<<<nb(c.lv[1]->g.ndofs()), 256, 0, c.st>>>(c.lv[1]->g.ndofs(), y, su, corr);
   TG_CHECK_LAUNCH();
-  TG_CUDA(cudaMemcpyAsync(cand, c.u.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, c.st));
-  prolong_add<double>(c.g, c.lv[1]->g, c.op.fix, corr, cand, c.st);
+  TG_CUDA(cudaMemsetAsync(v2, 0, sizeof(double) * n, c.st));
+  prolong_add<double>(c.g, c.lv[1]->g, c.op.fix, corr, v2, c.st);
+  // FP32 copies and products: p32 = v1, d32 = v2, q32 = K v1, r32 = K v2, z32 = f
+  d2f(n, c.u, c.p32, c.st);
+  d2f(n, v2, c.d32, c.st);
+  d2f(n, c.f, c.z32, c.st);
+  fine_apply<float, float>(c.op, c.s32, c.p32, c.q32, nullptr, nullptr, 0.0, AM_Y, c.st);
+  fine_apply<float, float>(c.op, c.s32, c.d32, c.r32, nullptr, nullptr, 0.0, AM_Y, c.st);
+  const float* a[5] = {c.p32, c.p32, c.d32, c.p32, c.d32};
+  const float* b[5] = {c.q32, c.r32, c.r32, c.z32, c.z32};
+  for (int k = 0; k < 5; ++k) {
+    pcg_reset(gal.p + k, c.st);
+    dot<float, float>(n, a[k], b[k], c.part, gal.p + k, DOT_BB, c.st);
+  }
+  PCGState hg[5], hp{};
+  TG_CUDA(cudaMemcpyAsync(hg, gal.p, sizeof(PCGState) * 5, cudaMemcpyDeviceToHost, c.st));
+  TG_CUDA(cudaMemcpyAsync(&hp, sr.p, sizeof(PCGState), cudaMemcpyDeviceToHost, c.st));
+  TG_CUDA(cudaStreamSynchronize(c.st));
+  const double g11 = hg[0].bb, g12 = hg[1].bb, g22 = hg[2].bb, f1 = hg[3].bb, f2 = hg[4].bb;
+  const double det = g11 * g22 - g12 * g12;
+  if (!(std::isfinite(det) && det > 1e-12 * std::fabs(g11 * g22) && g11 > 0 && g22 > 0)) return 1;
+  const double c1 = (f1 * g22 - f2 * g12) / det, c2 = (f2 * g11 - f1 * g12) / det;
+  double* cand = c.r.p;        // free until the solve starts
+  k_combine<<<nb(n), 256, 0, c.st>>>(n, c1, c.u, c2, v2, cand);
+  TG_CHECK_LAUNCH();
   residual32(c, cand, c.r32);
   pcg_reset(c.pcg_out, c.st);
   dot<float, float>(n, c.r32.p, c.r32.p, c.part, c.pcg_out, DOT_RR, c.st);
   PCGState hs{};
   TG_CUDA(cudaMemcpyAsync(&hs, c.pcg_out.p, sizeof(PCGState), cudaMemcpyDeviceToHost, c.st));
-  PCGState hp{};
-  TG_CUDA(cudaMemcpyAsync(&hp, sr.p, sizeof(PCGState), cudaMemcpyDeviceToHost, c.st));
   TG_CUDA(cudaStreamSynchronize(c.st));
   if (std::isfinite(hs.rr) && hs.rr < hp.rr) {
     TG_CUDA(cudaMemcpyAsync(c.u.p, cand, sizeof(double) * n, cudaMemcpyDeviceToDevice, c.st));

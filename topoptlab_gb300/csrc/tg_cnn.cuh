@@ -34,6 +34,7 @@ struct Cnn {
   DevBuf<double> uprev, corr;
   DevBuf<float> r32a;
   DevBuf<PCGState> su, sr;       // norms of u_prev and of its residual
+  DevBuf<PCGState> gal;          // the five products of the 2x2 Galerkin combination
   float lr = 1e-3f;
   int adam_t = 0;
   bool trained = false;
