@@ -156,15 +156,56 @@ def _fine_bytes(kind, size=None):
     raise ValueError(kind)
 
 
+def _train_network(device, args):
+    """Train the warm-start network on solver-generated pairs: an optimisation
+    run of the same cantilever started from seeded random densities uniform in
+    [0.05, 1] smoothed once by the rmin=1.5 filter, one (features, displacement
+    change) pair per design iteration, then Adam at lr 1e-3."""
+    from topoptlab_gb300 import _lib
+    from topoptlab_gb300.learned import LearnedWarmStart
+    if args.train_iters <= 0:
+        return None, {"trained": False}
+    gen = _problem("mixed", device)
+    rng = np.random.default_rng(0)
+    x = rng.uniform(0.05, 1.0, gen.nel)
+    xs = gen.filter(x, 0)                      # (H x) / Hs
+    gen.set(_lib.TG_FIELD_X, xs)
+    gen.set(_lib.TG_FIELD_XPHYS, gen.filter(xs, 0))
+    net = LearnedWarmStart(gen, capacity=args.train_iters, seed=0)
+    try:
+        for _ in range(args.train_iters):
+            net.record_step()
+        loss = net.train(epochs=args.train_epochs, lr=1e-3, seed=0)
+        params = net.params()
+    finally:
+        net.close()
+        gen.close()
+    return params, {"trained": True, "pairs": args.train_iters, "epochs": args.train_epochs,
+                    "final_loss": loss, "optimizer": "Adam lr 1e-3",
+                    "data": "design iterations 1..N from seeded random densities U[0.05,1] "
+                            "smoothed by the rmin=1.5 filter"}
+
+
 def run_ours(args, dist, rank, ws, local):
     from topoptlab_gb300 import _lib
     import ctypes as C
     lib = _lib.load()
     device = local
     prof_kind = int(os.environ.get("TG_BENCH_PROF_KIND", "3"))
+    from topoptlab_gb300.learned import LearnedWarmStart
 
-    # ---------------- mixed precision (headline) ----------------
+    # ---------------- learned warm start: training (set-up, not timed) ----------------
+    t_train0 = time.perf_counter()
+    net_params, train_info = _train_network(device, args)
+    train_info["seconds"] = time.perf_counter() - t_train0
+
+    # ---------------- learned + mixed precision (headline) ----------------
     prob = _problem("mixed", device)
+    net = None
+    if net_params is not None:
+        net = LearnedWarmStart(prob, capacity=0, seed=0)
+        net.set_params(net_params)
+        net.attach(prob)
     steps_info = []
     for _ in range(args.warmup):
         prob.step()
@@ -214,10 +255,24 @@ def run_ours(args, dist, rank, ws, local):
            "h2d_bytes_per_step": 8 * prob.nel, "d2h_bytes_per_step": 16 * prob.nel,
            "api": "GpuProblem.set/step/get over the C ABI (tg_set, tg_step, tg_get)"}
     obj_mixed = [s.obj for s in steps_info]
+    if net is not None:
+        net.close()
     prob.close()
     if os.environ.get("TG_BENCH_VERBOSE"):
         for s in steps_info:
-            print("mixed", s, file=sys.stderr)
+            print("learned+mixed", s, file=sys.stderr)
+
+    # ---------------- mixed precision without the network, same iterations ----------------
+    probm = _problem("mixed", device)
+    for _ in range(args.warmup):
+        probm.step()
+    lib.tg_timer(probm._h, 0, None)
+    minfo = [probm.step() for _ in range(args.steps)]
+    ms3 = C.c_double()
+    lib.tg_timer(probm._h, 1, C.byref(ms3))
+    probm.close()
+    t_nolearn = _max_over_ranks(dist, ms3.value / 1000.0)
+    value_nolearn = args.steps * ws / t_nolearn
 
     # ---------------- plain FP64 GMG-PCG, same iterations ----------------
     nplain = 0 if args.no_plain else args.steps
@@ -267,8 +322,9 @@ def run_ours(args, dist, rank, ws, local):
                                "3,168,963 DOFs), volfrac 0.12, rmin 1.5, ft=1, OC, "
                                "FP64 relative residual 1e-8",
                    "solver": "mixed-precision GMG-PCG (FP32 V-cycle, BF16 smoother densities, "
-                             "FP64 refinement), 5 levels, 2 damped-Jacobi sweeps omega 0.6",
-                   "learned_warm_start": False,
+                             "FP64 refinement), 5 levels, 2 damped-Jacobi sweeps omega 0.6, "
+                             "learned warm start (3-level 16/32/64 conv encoder-decoder, FP32)",
+                   "learned_warm_start": train_info,
                    "design_iterations_timed": f"{args.warmup + 1}..{args.warmup + args.steps}",
                    "l2": "working set > L2 (126 MB); no flush",
                    "parallelism": f"replicas x{ws}"},
@@ -278,10 +334,15 @@ def run_ours(args, dist, rank, ws, local):
         "plain_fp64": {"value": value_plain, "ms_per_step": 1000.0 * t_plain / args.steps,
                        "pcg_iters_per_step": mean("pcg_iters", pinfo),
                        "max_rel_res": max(s.rel_res for s in pinfo)},
-        "mixed": {"pcg_iters_per_step": mean("pcg_iters", steps_info),
-                  "refinements_per_step": mean("refinements", steps_info),
-                  "max_rel_res": max(s.rel_res for s in steps_info),
-                  "solve_ms_per_step": mean("t_solve_ms", steps_info)},
+        "learned_mixed": {"pcg_iters_per_step": mean("pcg_iters", steps_info[:args.steps]),
+                          "refinements_per_step": mean("refinements", steps_info[:args.steps]),
+                          "fallbacks": int(sum(s.fallback for s in steps_info[:args.steps])),
+                          "max_rel_res": max(s.rel_res for s in steps_info),
+                          "solve_ms_per_step": mean("t_solve_ms", steps_info[:args.steps])},
+        "mixed_without_network": {"value": value_nolearn,
+                                  "ms_per_step": 1000.0 * t_nolearn / args.steps,
+                                  "pcg_iters_per_step": mean("pcg_iters", minfo),
+                                  "max_rel_res": max(s.rel_res for s in minfo)},
         "ratio_vs_plain_fp64": value / value_plain,
         "compliance_max_rel_diff_vs_fp64": obj_diff,
         "clocks": clk.summary(),
@@ -373,6 +434,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--train-iters", type=int, default=200,
+                    help="design iterations recorded to train the warm-start network")
+    ap.add_argument("--train-epochs", type=int, default=10)
     ap.add_argument("--no-plain", action="store_true",
                     help="skip the plain FP64 arm (profiling runs only)")
     ap.add_argument("--size", default=None,
