@@ -123,6 +123,15 @@ int32_t tg_kmul(tg_ctx* ctx, const double* xPhys, const double* u, double* y, in
 /* K u = rhs on the free DOFs (solve_linsystem.py:20-365 slot).  u0 may be NULL. */
 int32_t tg_solve(tg_ctx* ctx, const double* xPhys, const double* rhs, const double* u0, double* u,
                  tg_solve_info* info);
+/* PCG on an assembled CSR matrix (indptr int64 [n+1], indices int32, data
+ * FP64), Jacobi-preconditioned when jacobi != 0, stopping at
+ * ||b - A x|| < max(atol, rtol ||b||): the pcg / solve_lin path for callers
+ * that pass an assembled matrix (linear_solvers.py:50-136,
+ * solve_linsystem.py:341-352).  x0 may be NULL.  Errors: tg_csr_last_error(). */
+int32_t tg_csr_pcg(int64_t n, const int64_t* indptr, const int32_t* indices, const double* data,
+                   const double* rhs, const double* x0, double* x, double rtol, double atol,
+                   int32_t maxiter, int32_t jacobi, tg_solve_info* info, int32_t device);
+const char* tg_csr_last_error(void);
 /* mode 0: (H x)/Hs   1: H(x/Hs)   2: H(x*d)/Hs/max(1e-3,x)   3: Hs
  * (filter/matrix_filter.py:101-232 + topology_optimization.py:545-558, :639) */
 int32_t tg_filter(tg_ctx* ctx, const double* x, const double* d, double* y, int32_t mode);
