@@ -308,11 +308,15 @@ int32_t tg_coarse_stencil(tg_ctx* ctx, const double* xPhys, int32_t level, doubl
     TG_REQUIRE(c.precond == TG_PRECOND_GMG, "no multigrid hierarchy");
     TG_REQUIRE(level >= 1 && level < c.L, "level out of range");
     tg::Level& v = *c.lv[level];
-    TG_REQUIRE(n == v.A64.n, "tg_coarse_stencil: wrong element count");
+    TG_REQUIRE(n == v.g.nnodes() * (v.g.ndim == 3 ? 27 : 9) * v.g.ndof * v.g.ndof,
+               "tg_coarse_stencil: wrong element count");
     h2d(c.xnew.p, xPhys, c.g.nel(), c.st);
     tg::set_density(c, c.xnew);
     tg::build_hierarchy(c);
-    d2h(out, v.A64.p, n, c.st);
+    tg::DevBuf<double> full;
+    full.alloc(n);
+    tg::stencil_expand(v.g, v.A64, full, c.st);
+    d2h(out, full.p, n, c.st);
   });
 }
 

@@ -231,7 +231,7 @@ void ctx_init(Ctx& c, const tg_problem& p) {
     const int64_t n = v.g.ndofs();
     v.fix.alloc(v.g.nnodes());
     TG_CUDA(cudaMemcpy(v.fix.p, fixl[l].data(), fixl[l].size(), cudaMemcpyHostToDevice));
-    const int64_t ns = v.g.nnodes() * (g.ndim == 3 ? 27 : 9) * g.ndof * g.ndof;
+    const int64_t ns = v.g.nnodes() * stencil_half_dirs(g.ndim) * g.ndof * g.ndof;
     const bool last = (l == c.L - 1) && c.precond == TG_PRECOND_GMG;
     if (l >= 1 || last) v.A64.alloc(ns);
     if (!last || l == 0) {

@@ -45,6 +45,21 @@ __device__ __forceinline__ bool in_grid(const Grid& g, int x, int y, int z) {
 // ---------------------------------------------------------------------------
 // stencil mat-vec with fused residual / Jacobi epilogues
 // ---------------------------------------------------------------------------
+// Coarse operators are symmetric, so only the centre block and the blocks of
+// the "upper" directions (index >= centre: dz, dx, dy lexicographically >= 0)
+// are stored: A_h[((d - C)*ndof + ci)*ndof + cj][node].  The block of a lower
+// direction d at node n is the transpose of the block of direction -d (index
+// 2C - d) stored at the neighbour m = n + d.
+template <int NDIM> __host__ __device__ constexpr int ndir_half() { return ndir<NDIM>() / 2 + 1; }
+
+template <int NDIM, int NDOF, typename T>
+__device__ __forceinline__ T coef(const T* __restrict__ A, int64_t ld, int d, int ci, int cj,
+                                  int64_t n, int64_t m) {
+  constexpr int C = ndir<NDIM>() / 2;
+  return d >= C ? __ldg(A + (((d - C) * NDOF + ci) * NDOF + cj) * ld + n)
+                : __ldg(A + (((C - d) * NDOF + cj) * NDOF + ci) * ld + m);
+}
+
 // one thread per (row component ci, node): coalesced coefficient loads (the
 // node index is fastest), NDOF times the parallelism of a thread per node,
 // which matters on the small coarse grids
@@ -69,7 +84,7 @@ __global__ void __launch_bounds__(256) k_stencil_apply(Grid g, const T* __restri
     const int64_t m = g.node(x + dx, yy + dy, z + dz);
 #pragma unroll
     for (int cj = 0; cj < NDOF; ++cj)
-      acc += __ldg(A + ((d * NDOF + ci) * NDOF + cj) * ld + n) * __ldg(u + m * NDOF + cj);
+      acc += coef<NDIM, NDOF, T>(A, ld, d, ci, cj, n, m) * __ldg(u + m * NDOF + cj);
   }
   const int64_t k = n * NDOF + ci;
   T out;
@@ -111,10 +126,9 @@ __global__ void k_stencil_dinv(Grid g, const uint8_t* fix, const T* A, T* dinv) 
   const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t ld = g.nnodes();
   if (n >= ld) return;
-  const int center = ndir<NDIM>() / 2;
 #pragma unroll
   for (int c = 0; c < NDOF; ++c) {
-    const T dg = A[((center * NDOF + c) * NDOF + c) * ld + n];
+    const T dg = A[(c * NDOF + c) * ld + n];     // centre block (half index 0)
     dinv[n * NDOF + c] = (((fix[n] >> c) & 1) || dg == T(0)) ? T(0) : T(1) / dg;
   }
 }
@@ -161,9 +175,9 @@ __global__ void __launch_bounds__(256) k_build_level1(Grid gf, Grid gc, const do
   constexpr int NE = NC * NDOF;
   const int64_t ldc = gc.nnodes();
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t >= ldc * ndir<NDIM>()) return;
+  if (t >= ldc * ndir_half<NDIM>()) return;
   const int64_t I = t % ldc;
-  const int D = (int)(t / ldc);
+  const int DH = (int)(t / ldc), D = DH + ndir<NDIM>() / 2;   // upper directions only
   int ix, iy, iz, dx, dy, dz;
   node_xyz(gc, I, ix, iy, iz);
   dir_xyz(D, NDIM, dx, dy, dz);
@@ -231,12 +245,12 @@ __global__ void __launch_bounds__(256) k_build_level1(Grid gf, Grid gc, const do
 #pragma unroll
   for (int ci = 0; ci < NDOF; ++ci)
 #pragma unroll
-    for (int cj = 0; cj < NDOF; ++cj) Ac[((D * NDOF + ci) * NDOF + cj) * ldc + I] = acc[ci][cj];
+    for (int cj = 0; cj < NDOF; ++cj) Ac[((DH * NDOF + ci) * NDOF + cj) * ldc + I] = acc[ci][cj];
 }
 
 void build_level1(const FineOp& op, const double* scale, const uint8_t* touch, const double* Q,
                   const Grid& gc, const uint8_t* fixc, double* Ac, cudaStream_t st) {
-  const int64_t nt = gc.nnodes() * (op.g.ndim == 3 ? 27 : 9);
+  const int64_t nt = gc.nnodes() * (op.g.ndim == 3 ? 14 : 5);
   const unsigned blocks = (unsigned)cdiv(nt, 256);
   const int key = op.g.ndim * 10 + op.g.ndof;
   switch (key) {
@@ -259,9 +273,9 @@ __global__ void __launch_bounds__(256) k_build_fine(Grid g, const double* __rest
   constexpr int NE = (1 << NDIM) * NDOF;
   const int64_t ld = g.nnodes();
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t >= ld * ndir<NDIM>()) return;
+  if (t >= ld * ndir_half<NDIM>()) return;
   const int64_t I = t % ld;
-  const int D = (int)(t / ld);
+  const int DH = (int)(t / ld), D = DH + ndir<NDIM>() / 2;
   int ix, iy, iz, dx, dy, dz;
   node_xyz(g, I, ix, iy, iz);
   dir_xyz(D, NDIM, dx, dy, dz);
@@ -299,11 +313,11 @@ __global__ void __launch_bounds__(256) k_build_fine(Grid g, const double* __rest
 #pragma unroll
   for (int ci = 0; ci < NDOF; ++ci)
 #pragma unroll
-    for (int cj = 0; cj < NDOF; ++cj) A[((D * NDOF + ci) * NDOF + cj) * ld + I] = acc[ci][cj];
+    for (int cj = 0; cj < NDOF; ++cj) A[((DH * NDOF + ci) * NDOF + cj) * ld + I] = acc[ci][cj];
 }
 
 void build_fine_stencil(const FineOp& op, const double* scale, double* A, cudaStream_t st) {
-  const int64_t nt = op.g.nnodes() * (op.g.ndim == 3 ? 27 : 9);
+  const int64_t nt = op.g.nnodes() * (op.g.ndim == 3 ? 14 : 5);
   const unsigned blocks = (unsigned)cdiv(nt, 256);
   const int key = op.g.ndim * 10 + op.g.ndof;
   switch (key) {
@@ -325,9 +339,9 @@ __global__ void __launch_bounds__(256) k_galerkin(Grid gf, const double* __restr
                                                   double* __restrict__ Ac) {
   const int64_t ldc = gc.nnodes(), ldf = gf.nnodes();
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t >= ldc * ndir<NDIM>()) return;
+  if (t >= ldc * ndir_half<NDIM>()) return;
   const int64_t I = t % ldc;
-  const int D = (int)(t / ldc);
+  const int DH = (int)(t / ldc), D = DH + ndir<NDIM>() / 2;
   int ix, iy, iz, dx, dy, dz;
   node_xyz(gc, I, ix, iy, iz);
   dir_xyz(D, NDIM, dx, dy, dz);
@@ -355,11 +369,12 @@ __global__ void __launch_bounds__(256) k_galerkin(Grid gf, const double* __restr
         if (!in_grid(gf, gx, gy, gz)) continue;
         const double w = wi * (bx ? 0.5 : 1.0) * (by ? 0.5 : 1.0) * (bz ? 0.5 : 1.0);
         const int dd = dir_index(rx, ry, rz, NDIM);
+        const int64_t gi = gf.node(gx, gy, gz);
 #pragma unroll
         for (int ci = 0; ci < NDOF; ++ci)
 #pragma unroll
           for (int cj = 0; cj < NDOF; ++cj)
-            acc[ci][cj] += w * __ldg(Af + ((dd * NDOF + ci) * NDOF + cj) * ldf + fi);
+            acc[ci][cj] += w * coef<NDIM, NDOF, double>(Af, ldf, dd, ci, cj, fi, gi);
       }
     }
     const uint8_t mi = fixc[I], mj = fixc[J];
@@ -372,12 +387,12 @@ __global__ void __launch_bounds__(256) k_galerkin(Grid gf, const double* __restr
 #pragma unroll
   for (int ci = 0; ci < NDOF; ++ci)
 #pragma unroll
-    for (int cj = 0; cj < NDOF; ++cj) Ac[((D * NDOF + ci) * NDOF + cj) * ldc + I] = acc[ci][cj];
+    for (int cj = 0; cj < NDOF; ++cj) Ac[((DH * NDOF + ci) * NDOF + cj) * ldc + I] = acc[ci][cj];
 }
 
 void build_galerkin(const Grid& gf, const double* Af, const Grid& gc, const uint8_t* fixc,
                     double* Ac, cudaStream_t st) {
-  const int64_t nt = gc.nnodes() * (gf.ndim == 3 ? 27 : 9);
+  const int64_t nt = gc.nnodes() * (gf.ndim == 3 ? 14 : 5);
   const unsigned blocks = (unsigned)cdiv(nt, 256);
   const int key = gf.ndim * 10 + gf.ndof;
   switch (key) {
@@ -385,6 +400,34 @@ void build_galerkin(const Grid& gf, const double* Af, const Grid& gc, const uint
     case 31: k_galerkin<3, 1><<<blocks, 256, 0, st>>>(gf, Af, gc, fixc, Ac); break;
     case 22: k_galerkin<2, 2><<<blocks, 256, 0, st>>>(gf, Af, gc, fixc, Ac); break;
     case 21: k_galerkin<2, 1><<<blocks, 256, 0, st>>>(gf, Af, gc, fixc, Ac); break;
+    default: throw Error{EINVAL_, "unsupported (ndim, nnode_dof)"};
+  }
+  TG_CHECK_LAUNCH();
+}
+
+template <int NDIM, int NDOF>
+__global__ void k_stencil_expand(Grid g, const double* __restrict__ Ah, double* __restrict__ Af) {
+  const int64_t ld = g.nnodes();
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= ld * ndir<NDIM>() * NDOF * NDOF) return;
+  const int64_t n = t % ld;
+  const int k = (int)(t / ld);
+  const int cj = k % NDOF, ci = (k / NDOF) % NDOF, d = k / (NDOF * NDOF);
+  int x, y, z, dx, dy, dz;
+  node_xyz(g, n, x, y, z);
+  dir_xyz(d, NDIM, dx, dy, dz);
+  Af[t] = in_grid(g, x + dx, y + dy, z + dz)
+              ? coef<NDIM, NDOF, double>(Ah, ld, d, ci, cj, n, g.node(x + dx, y + dy, z + dz))
+              : 0.0;
+}
+
+void stencil_expand(const Grid& g, const double* Ah, double* Af, cudaStream_t st) {
+  const unsigned blocks = (unsigned)cdiv(g.nnodes() * (g.ndim == 3 ? 27 : 9) * g.ndof * g.ndof, 256);
+  switch (g.ndim * 10 + g.ndof) {
+    case 33: k_stencil_expand<3, 3><<<blocks, 256, 0, st>>>(g, Ah, Af); break;
+    case 31: k_stencil_expand<3, 1><<<blocks, 256, 0, st>>>(g, Ah, Af); break;
+    case 22: k_stencil_expand<2, 2><<<blocks, 256, 0, st>>>(g, Ah, Af); break;
+    case 21: k_stencil_expand<2, 1><<<blocks, 256, 0, st>>>(g, Ah, Af); break;
     default: throw Error{EINVAL_, "unsupported (ndim, nnode_dof)"};
   }
   TG_CHECK_LAUNCH();
@@ -486,19 +529,22 @@ template void prolong_add<float>(const Grid&, const Grid&, const uint8_t*, const
 __global__ void k_stencil_to_dense(Grid g, const uint8_t* fix, const double* __restrict__ A,
                                    double* D, int64_t n, int64_t ld) {
   const int64_t ldA = g.nnodes();
-  const int nd = g.ndim == 3 ? 27 : 9;
+  const int C = g.ndim == 3 ? 13 : 4;
+  const int nh = C + 1;
   const int ndof = g.ndof;
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t >= ldA * nd * ndof * ndof) return;
+  if (t >= ldA * nh * ndof * ndof) return;
   const int64_t I = t % ldA;
-  const int k = (int)(t / ldA);          // (dir*ndof+ci)*ndof+cj
-  const int cj = k % ndof, ci = (k / ndof) % ndof, d = k / (ndof * ndof);
+  const int k = (int)(t / ldA);          // (dh*ndof+ci)*ndof+cj
+  const int cj = k % ndof, ci = (k / ndof) % ndof, dh = k / (ndof * ndof);
   int ix, iy, iz, dx, dy, dz;
   node_xyz(g, I, ix, iy, iz);
-  dir_xyz(d, g.ndim, dx, dy, dz);
+  dir_xyz(C + dh, g.ndim, dx, dy, dz);
   if (!in_grid(g, ix + dx, iy + dy, iz + dz)) return;
   const int64_t J = g.node(ix + dx, iy + dy, iz + dz);
-  D[(I * ndof + ci) * ld + J * ndof + cj] = A[(int64_t)k * ldA + I];
+  const double v = A[(int64_t)k * ldA + I];
+  D[(I * ndof + ci) * ld + J * ndof + cj] = v;
+  if (dh > 0) D[(J * ndof + cj) * ld + I * ndof + ci] = v;   // mirrored lower block
 }
 __global__ void k_dense_fix_diag(Grid g, const uint8_t* fix, double* D, int64_t n, int64_t ld) {
   const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -515,7 +561,7 @@ __global__ void k_dense_fix_diag(Grid g, const uint8_t* fix, double* D, int64_t 
 void stencil_to_dense(const Grid& g, const uint8_t* fix, const double* A, double* D, int64_t n,
                       int64_t ld, cudaStream_t st) {
   TG_CUDA(cudaMemsetAsync(D, 0, sizeof(double) * ld * ld, st));
-  const int64_t nt = g.nnodes() * (g.ndim == 3 ? 27 : 9) * g.ndof * g.ndof;
+  const int64_t nt = g.nnodes() * (g.ndim == 3 ? 14 : 5) * g.ndof * g.ndof;
   k_stencil_to_dense<<<(unsigned)cdiv(nt, 256), 256, 0, st>>>(g, fix, A, D, n, ld);
   TG_CHECK_LAUNCH();
   k_dense_fix_diag<<<(unsigned)cdiv(ld, 256), 256, 0, st>>>(g, fix, D, n, ld);

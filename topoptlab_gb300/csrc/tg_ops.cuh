@@ -58,13 +58,9 @@ void fine_compliance(const FineOp& op, const double* xPhys, const double* u, dou
 // assembled 3^ndim-point block stencils (coarse levels)
 // layout: A[(dir * ndof + ci) * ndof + cj][node]   (structure of arrays)
 // ---------------------------------------------------------------------------
-struct Stencil {
-  Grid g;
-  const uint8_t* fix;
-  void* A;             // double* or float*
-  int64_t ld;          // leading dimension = nnodes
-};
-
+// Stencils are symmetric and stored half: the centre block and the 3^ndim/2
+// upper direction blocks per node, [(dh*ndof+ci)*ndof+cj][node]
+inline int stencil_half_dirs(int ndim) { return ndim == 3 ? 14 : 5; }
 template <typename T>
 void stencil_apply(const Grid& g, const T* A, const T* u, T* y, const T* b, const T* dinv,
                    double omega, int mode, cudaStream_t st);
@@ -80,6 +76,10 @@ void build_fine_stencil(const FineOp& op, const double* scale, double* A, cudaSt
 // Galerkin product of an assembled stencil: Ac = M_c P^T A P M_c
 void build_galerkin(const Grid& gf, const double* Af, const Grid& gc, const uint8_t* fixc,
                     double* Ac, cudaStream_t st);
+
+// full 3^ndim-direction layout [(d*ndof+ci)*ndof+cj][node] of a half-stored
+// stencil (diagnostic export)
+void stencil_expand(const Grid& g, const double* Ah, double* Afull, cudaStream_t st);
 
 // transfers (masked): bc = Mc P^T rf ;  xf += Mf P xc
 template <typename T>
