@@ -88,6 +88,30 @@ def test_kmul_fp32(gpu_lib, nelx, nely, nelz, kind):
     np.testing.assert_allclose(y, yref, rtol=0, atol=1e-5 * np.abs(yref).max())
 
 
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-13), ("mixed", 1e-5)])
+@pytest.mark.parametrize("nelx,nely,nelz,kind", [(31, 17, 9, "elast"), (17, 32, 5, "poisson"),
+                                                 (60, 60, 30, "elast")])
+def test_kmul_3d_multi_tile(gpu_lib, precision, tol, nelx, nely, nelz, kind):
+    """3-D grids spanning several node columns in x and y and several z chunks
+    (the largest one gives every CTA more than one node plane); the oracle
+    product is the element-by-element sum y = sum_e s_e KE u_e."""
+    rng = np.random.default_rng(3)
+    prob, KE, fixed, f, x, ndof = _setup(nelx, nely, nelz, kind, rng, precision=precision,
+                                         precond="gb300-jacobi")
+    try:
+        u = rng.standard_normal(ndof)
+        y = prob.kmul(x, u, precision=precision)
+    finally:
+        prob.close()
+    nnd = KE.shape[0] // 8
+    edof = O.edofmat(nelx, nely, nelz, nnd)
+    m = np.ones(ndof)
+    m[fixed] = 0.0
+    ye = ((m * u)[edof] @ KE.T) * O.simp(x)[:, None]
+    yref = m * np.bincount(edof.ravel(), ye.ravel(), minlength=ndof)
+    np.testing.assert_allclose(y, yref, rtol=0, atol=tol * np.abs(yref).max())
+
+
 @pytest.mark.parametrize("nelx,nely,nelz,rmin", [(7, 5, None, 2.4), (9, 6, None, 1.5),
                                                  (6, 5, 4, 1.5), (5, 4, 3, 2.4), (60, 20, None, 2.4)])
 def test_filter_modes(gpu_lib, nelx, nely, nelz, rmin):

@@ -15,6 +15,7 @@
 // KE = H B H (Walsh-Hadamard over corner bits, B block diagonal), ~240 flops
 // per hex8 element instead of 1152: GB300's FP64 pipe is narrow, and the
 // FP64 residual is the one K.u the mixed-precision solver cannot avoid.
+#include <algorithm>
 #include <type_traits>
 #include "tg_ops.cuh"
 
@@ -263,8 +264,228 @@ __global__ void __launch_bounds__(256, sizeof(T) == 8 ? 2 : 4) k_fine_apply(Appl
   }
 }
 
+// ---------------------------------------------------------------------------
+// 3-D: z-streaming variant.  A CTA owns a 15 x 15 column of nodes (x, y) over
+// a chunk of node planes and marches up in z: per element layer each of its
+// 256 threads evaluates one of the 16 x 16 elements touching the column
+// (every element once per layer, no colour passes), writes rho * KE u_e to a
+// shared element-output buffer, and after one barrier each owned node sums
+// the four element outputs below and above it in a fixed order (bit-
+// reproducible, no atomics).  Node planes stream through a 3-slot shared ring
+// filled by cp.async one layer ahead; densities, b and dinv are loaded into
+// registers one layer ahead.  Recomputed elements: (16*16)/(15*15) in x-y and
+// one extra layer per z chunk, against (9*17*9)/(8*16*8) for the brick kernel.
+// ---------------------------------------------------------------------------
+namespace zs {
+constexpr int EXT = 16, EYT = 16;          // element tile = threads (x, y)
+constexpr int OX = EXT - 1, OY = EYT - 1;  // owned nodes per tile
+constexpr int PX = EXT + 1, PY = EYT + 1;  // node plane incl. halo
+constexpr int PITCH = 48;                  // row pitch in words: the two x-rows of a warp
+                                           // (16 lanes each) fall on disjoint banks
+constexpr int PLANE = PX * PITCH;          // words per component plane
+constexpr int NT = EXT * EYT;
+template <int NDOF> __host__ __device__ constexpr int ncopy() { return (NDOF * PX * PY + NT - 1) / NT; }
+template <int NDOF, typename T, int KIND> constexpr size_t smem() {
+  constexpr int NE = 8 * NDOF;
+  return sizeof(T) * ((size_t)3 * NDOF * PLANE + (size_t)NE * NT + (KIND == EK_DENSE ? NE * NE : 0));
+}
+}  // namespace zs
+
+template <int NDOF, typename T, typename S, int KIND, int MODE>
+__global__ void __launch_bounds__(zs::NT, sizeof(T) == 8 ? 2 : 4) k_fine_zstream(ApplyArgs<T, S> a,
+                                                                                int zc) {
+  using namespace zs;
+  constexpr int NC = 8;
+  constexpr int NE = NC * NDOF;
+  constexpr int SLOT = NDOF * PLANE;
+  constexpr int NCP = ncopy<NDOF>();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* us = reinterpret_cast<T*>(smem_raw);        // 3 node-plane slots [c][x][PITCH]
+  T* yo = us + 3 * SLOT;                          // element outputs [corner*NDOF+c][NT]
+  T* KEs = yo + NE * NT;                          // dense path only
+  const Grid& g = a.g;
+  const int tid = threadIdx.x;
+  const int y0 = blockIdx.x * OY, x0 = blockIdx.y * OX;
+  const int zbeg = blockIdx.z * zc, zend = min(zbeg + zc, g.nnz);
+  const int64_t pstride = (int64_t)g.nnx * g.nny * NDOF;   // words per global node plane
+  const int64_t lstride = (int64_t)g.nex * g.ney;           // elements per layer
+
+  // per-thread plane-copy descriptors (same (x, y) pattern for every plane)
+  int goff[NCP], soff[NCP];
+#pragma unroll
+  for (int k = 0; k < NCP; ++k) {
+    const int i = tid + k * NT;
+    soff[k] = -1;
+    goff[k] = 0;
+    if (i < NDOF * PX * PY) {
+      const int hx = i / (PY * NDOF), j = i % (PY * NDOF);
+      const int hy = j / NDOF, c = j % NDOF;
+      const int gx = x0 - 1 + hx, gy = y0 - 1 + hy;
+      if (gx >= 0 && gx < g.nnx && gy >= 0 && gy < g.nny) {
+        soff[k] = c * PLANE + hx * PITCH + hy;
+        goff[k] = (gx * g.nny + gy) * NDOF + c;
+      }
+    }
+  }
+  // slots never written by a copy (outside the grid in x or y) stay zero
+  for (int i = tid; i < 3 * SLOT; i += NT) us[i] = T(0);
+  if (KIND == EK_DENSE)
+    for (int i = tid; i < NE * NE; i += NT) KEs[i] = a.KE[i];
+  __syncthreads();
+  auto load_plane = [&](int p, int slot) {
+    if (p < 0 || p >= g.nnz) return;
+    const T* src = a.u + p * pstride;
+    T* dst = us + slot * SLOT;
+#pragma unroll
+    for (int k = 0; k < NCP; ++k)
+      if (soff[k] >= 0) cp_async<sizeof(T)>(dst + soff[k], src + goff[k]);
+  };
+
+  // element handled by this thread
+  const int exl = tid / EYT, eyl = tid % EYT;
+  const int ex = x0 - 1 + exl, ey = y0 - 1 + eyl;
+  const bool evalid = ex >= 0 && ex < g.nex && ey >= 0 && ey < g.ney;
+  const int64_t eoff = (int64_t)ex * g.ney + ey;
+  auto load_rho = [&](int ez) -> T {
+    return (evalid && ez >= 0 && ez < g.nez) ? load_scale<T, S>(a.scale, ez * lstride + eoff) : T(0);
+  };
+  const int ubase = exl * PITCH + eyl;
+  // node owned by this thread (tid < OX*OY)
+  const int ox = tid / OY, oy = tid % OY;
+  const int nx = x0 + ox, ny = y0 + oy;
+  const bool nvalid = tid < OX * OY && nx < g.nnx && ny < g.nny;
+  const int obase = (ox + 1) * EYT + (oy + 1);     // element (ox+1, oy+1) has this node as corner 0
+  const int nubase = (ox + 1) * PITCH + (oy + 1);
+
+  int s0 = 0, s1 = 1, s2 = 2;     // slots of planes ez, ez+1, ez+2
+  load_plane(zbeg - 1, s0);
+  load_plane(zbeg, s1);
+  cp_async_wait_all();
+  __syncthreads();
+  T rho = load_rho(zbeg - 1);
+  T acc[NDOF];
+#pragma unroll
+  for (int c = 0; c < NDOF; ++c) acc[c] = T(0);
+
+  for (int ez = zbeg - 1; ez < zend; ++ez) {
+    if (ez + 1 < zend) load_plane(ez + 2, s2);
+    const T rho_next = load_rho(ez + 1);
+    // epilogue inputs of plane ez (issued early, used after the barrier)
+    const bool owned = nvalid && ez >= zbeg;
+    const int64_t nid = ((int64_t)ez * g.nnx + nx) * g.nny + ny;
+    T bv[NDOF], dv[NDOF];
+    uint8_t fx = 0;
+    if (owned) {
+      fx = a.fix[nid];
+#pragma unroll
+      for (int c = 0; c < NDOF; ++c) {
+        bv[c] = (MODE != AM_Y) ? a.b[nid * NDOF + c] : T(0);
+        dv[c] = (MODE == AM_JACOBI) ? a.dinv[nid * NDOF + c] : T(0);
+      }
+    }
+    const bool lvalid = ez >= 0 && ez < g.nez;   // uniform over the CTA
+    if (lvalid) {
+      const T* p0 = us + s0 * SLOT + ubase;
+      const T* p1 = us + s1 * SLOT + ubase;
+      T ue[NC][NDOF], ye[NC][NDOF];
+#pragma unroll
+      for (int d = 0; d < NC; ++d)
+#pragma unroll
+        for (int c = 0; c < NDOF; ++c)
+          ue[d][c] = ((d >> 2) ? p1 : p0)[c * PLANE + (d & 1) * PITCH + ((d >> 1) & 1)];
+      if (KIND != EK_DENSE)
+        elem_sector<3, NDOF, T, KIND>(ue, a.B, ye);
+      else
+        elem_dense<3, NDOF, T>(ue, KEs, ye);
+#pragma unroll
+      for (int d = 0; d < NC; ++d)
+#pragma unroll
+        for (int c = 0; c < NDOF; ++c) yo[(d * NDOF + c) * NT + tid] = rho * ye[d][c];
+    }
+    __syncthreads();
+    if (nvalid) {
+      T hi[NDOF];
+#pragma unroll
+      for (int c = 0; c < NDOF; ++c) hi[c] = T(0);
+      if (lvalid) {
+        // element (ox+1-dx, oy+1-dy) of this layer has the node as corner (dx, dy, dz)
+#pragma unroll
+        for (int d = 0; d < NC; ++d) {
+          const int e = obase - (d & 1) * EYT - ((d >> 1) & 1);
+#pragma unroll
+          for (int c = 0; c < NDOF; ++c) {
+            const T v = yo[(d * NDOF + c) * NT + e];
+            if (d >> 2) hi[c] += v;
+            else acc[c] += v;
+          }
+        }
+      }
+      if (owned) {
+        const T* pu = us + s0 * SLOT + nubase;
+#pragma unroll
+        for (int c = 0; c < NDOF; ++c) {
+          T out;
+          if (MODE == AM_Y) out = acc[c];
+          else if (MODE == AM_RES) out = bv[c] - acc[c];
+          else out = pu[c * PLANE] + a.omega * dv[c] * (bv[c] - acc[c]);
+          a.y[nid * NDOF + c] = ((fx >> c) & 1) ? T(0) : out;
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < NDOF; ++c) acc[c] = hi[c];
+    }
+    rho = rho_next;
+    cp_async_wait_all();
+    __syncthreads();
+    const int t = s0;
+    s0 = s1; s1 = s2; s2 = t;
+  }
+}
+
+static int sm_count() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    TG_CUDA(cudaGetDevice(&dev));
+    TG_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+  }
+  return n;
+}
+
+template <int NDOF, typename T, typename S, int KIND, int MODE>
+static void launch_zstream(const ApplyArgs<T, S>& a, cudaStream_t st) {
+  constexpr size_t smem = zs::smem<NDOF, T, KIND>();
+  auto kern = k_fine_zstream<NDOF, T, S, KIND, MODE>;
+  static bool attr_set = false;
+  if (!attr_set) {
+    TG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr_set = true;
+  }
+  const int gy = (int)cdiv(a.g.nny, zs::OY), gx = (int)cdiv(a.g.nnx, zs::OX);
+  // z chunks: as many as fit in one wave of resident CTAs (4 per SM in FP32,
+  // 2 in FP64), so that no second partial wave doubles the kernel time
+  const int target = sm_count() * (sizeof(T) == 8 ? 2 : 4);
+  const int cols = gx * gy;
+  int chunks = std::max(1, std::min(a.g.nnz, target / cols));
+  const int zc = (int)cdiv(a.g.nnz, chunks);
+  chunks = (int)cdiv(a.g.nnz, zc);
+  const int pk = std::is_same<T, double>::value ? PK_FINE_F64
+                 : (std::is_same<S, float>::value ? PK_FINE_F32 : PK_FINE_BF16);
+  prof_begin(pk, st);
+  kern<<<dim3((unsigned)gy, (unsigned)gx, (unsigned)chunks), zs::NT, smem, st>>>(a, zc);
+  prof_end(pk, st);
+  TG_CHECK_LAUNCH();
+}
+
 template <int NDIM, int NDOF, typename T, typename S, int KIND, int MODE>
 static void launch_apply(const ApplyArgs<T, S>& a, cudaStream_t st) {
+  // the z-streaming kernel keeps 32-bit in-plane offsets
+  if constexpr (NDIM == 3) {
+    if ((int64_t)a.g.nnx * a.g.nny * NDOF < (int64_t(1) << 31)) {
+      launch_zstream<NDOF, T, S, KIND, MODE>(a, st);
+      return;
+    }
+  }
   using TL = Tile<NDIM>;
   constexpr size_t smem = apply_smem_v2<NDIM, NDOF, T, KIND>();
   auto kern = k_fine_apply<NDIM, NDOF, T, S, KIND, MODE>;

@@ -62,7 +62,10 @@ __device__ __forceinline__ T coef(const T* __restrict__ A, int64_t ld, int d, in
 
 // one thread per (row component ci, node): coalesced coefficient loads (the
 // node index is fastest), NDOF times the parallelism of a thread per node,
-// which matters on the small coarse grids
+// which matters on the small coarse grids.  No branches around the loads: a
+// neighbour outside the grid is replaced by the node itself and its u is
+// selected to zero, so all 2*27*NDOF loads of a thread can be in flight at
+// once (the small levels are latency-bound).
 template <int NDIM, int NDOF, typename T, int MODE>
 __global__ void __launch_bounds__(256) k_stencil_apply(Grid g, const T* __restrict__ A,
                                                       const T* __restrict__ u, T* __restrict__ y,
@@ -75,16 +78,22 @@ __global__ void __launch_bounds__(256) k_stencil_apply(Grid g, const T* __restri
   const int64_t n = t - (int64_t)ci * ld;
   int x, yy, z;
   node_xyz(g, n, x, yy, z);
+  const bool ok[3][3] = {{x > 0, true, x + 1 < g.nnx},
+                         {yy > 0, true, yy + 1 < g.nny},
+                         {z > 0, true, z + 1 < g.nnz}};
+  const int64_t sx = g.nny, sz = (int64_t)g.nny * g.nnx;
   T acc = T(0);
 #pragma unroll
   for (int d = 0; d < ndir<NDIM>(); ++d) {
     int dx, dy, dz;
     dir_xyz(d, NDIM, dx, dy, dz);
-    if (!in_grid(g, x + dx, yy + dy, z + dz)) continue;
-    const int64_t m = g.node(x + dx, yy + dy, z + dz);
+    const bool v = ok[0][dx + 1] && ok[1][dy + 1] && ok[2][dz + 1];
+    const int64_t m = v ? n + dz * sz + dx * sx + dy : n;
 #pragma unroll
-    for (int cj = 0; cj < NDOF; ++cj)
-      acc += coef<NDIM, NDOF, T>(A, ld, d, ci, cj, n, m) * __ldg(u + m * NDOF + cj);
+    for (int cj = 0; cj < NDOF; ++cj) {
+      const T uu = __ldg(u + m * NDOF + cj);
+      acc = fma(coef<NDIM, NDOF, T>(A, ld, d, ci, cj, n, m), v ? uu : T(0), acc);
+    }
   }
   const int64_t k = n * NDOF + ci;
   T out;
@@ -595,52 +604,80 @@ __global__ void __launch_bounds__(GJB * GJB) k_gj_pivot(const double* D, int64_t
   }
   P[i * GJB + j] = a[i][j];
 }
-// R[:, jb] = P * D[k-block, jb]
-__global__ void __launch_bounds__(GJB * GJB) k_gj_rowpanel(const double* D, int64_t ld, int k,
+// The coarsest matrix is SPD, so it is inverted with the block sweep operator,
+// which keeps the matrix symmetric at every step (pivot block K, P = A_KK^-1):
+//   A_KK <- -P,  A_KJ <- P A_KJ,  A_IK <- A_IK P,  A_IJ <- A_IJ - A_IK P A_KJ,
+// ending with -A^-1.  Only blocks (ib <= jb) are kept up to date, which halves
+// the rank-32 update flops of a plain Gauss-Jordan inverse and removes its
+// column-panel product (A_IK P is the transpose of the row panel P A_KI).
+// Block (k, j) of the upper-stored matrix, as a 32 x 32 tile X[m][c]:
+__device__ __forceinline__ double sw_panel(const double* D, int64_t ld, int k, int jb, int m, int c) {
+  return k <= jb ? D[(int64_t)(k * GJB + m) * ld + jb * GJB + c]
+                 : D[(int64_t)(jb * GJB + c) * ld + k * GJB + m];
+}
+// R[:, jb] = P * A_K,jb
+__global__ void __launch_bounds__(GJB * GJB) k_sw_rowpanel(const double* D, int64_t ld, int k,
                                                           const double* P, double* R) {
-  __shared__ double ps[GJB][GJB + 1], ds[GJB][GJB + 1];
-  const int i = threadIdx.y, j = threadIdx.x, jb = blockIdx.x;
+  __shared__ double ps[GJB][GJB + 1], xs[GJB][GJB + 1];
+  const int jb = blockIdx.x;
+  if (jb == k) return;
+  const int i = threadIdx.y, j = threadIdx.x;
   ps[i][j] = P[i * GJB + j];
-  ds[i][j] = D[(int64_t)(k * GJB + i) * ld + jb * GJB + j];
+  if (k < jb) xs[i][j] = D[(int64_t)(k * GJB + i) * ld + jb * GJB + j];
+  else xs[j][i] = D[(int64_t)(jb * GJB + i) * ld + k * GJB + j];   // coalesced, transposed in smem
   __syncthreads();
   double acc = 0.0;
 #pragma unroll 8
-  for (int m = 0; m < GJB; ++m) acc += ps[i][m] * ds[m][j];
+  for (int m = 0; m < GJB; ++m) acc = fma(ps[i][m], xs[m][j], acc);
   R[(int64_t)i * ld + jb * GJB + j] = acc;
 }
-// D[ib, jb] -= D[ib, k] R[:, jb]   for ib != k, jb != k
-__global__ void __launch_bounds__(GJB * GJB) k_gj_update(double* D, int64_t ld, int k,
+// A_IJ -= X_I^T R_J  for ib <= jb, ib != k != jb  (X_I = A_KI before this step)
+__global__ void __launch_bounds__(GJB * GJB) k_sw_update(double* D, int64_t ld, int k,
                                                         const double* R) {
   const int ib = blockIdx.y, jb = blockIdx.x;
-  if (ib == k || jb == k) return;
-  __shared__ double cs[GJB][GJB + 1], rs[GJB][GJB + 1];
+  if (ib > jb || ib == k || jb == k) return;
+  __shared__ double xs[GJB][GJB + 1], rs[GJB][GJB + 1];
   const int i = threadIdx.y, j = threadIdx.x;
-  cs[i][j] = D[(int64_t)(ib * GJB + i) * ld + k * GJB + j];
+  if (k < ib) xs[i][j] = D[(int64_t)(k * GJB + i) * ld + ib * GJB + j];
+  else xs[j][i] = D[(int64_t)(ib * GJB + i) * ld + k * GJB + j];
   rs[i][j] = R[(int64_t)i * ld + jb * GJB + j];
   __syncthreads();
   double acc = 0.0;
 #pragma unroll 8
-  for (int m = 0; m < GJB; ++m) acc += cs[i][m] * rs[m][j];
+  for (int m = 0; m < GJB; ++m) acc = fma(xs[m][i], rs[m][j], acc);
   D[(int64_t)(ib * GJB + i) * ld + jb * GJB + j] -= acc;
 }
-// column k <- -D[:,k] P ; row k <- R ; pivot block <- P
-__global__ void __launch_bounds__(GJB * GJB) k_gj_finish(double* D, int64_t ld, int k,
+// panel K <- R (stored in the upper orientation), pivot block <- -P
+__global__ void __launch_bounds__(GJB * GJB) k_sw_finish(double* D, int64_t ld, int k,
                                                         const double* P, const double* R) {
   const int b = blockIdx.x;
   const int i = threadIdx.y, j = threadIdx.x;
   if (b == k) {
-    D[(int64_t)(k * GJB + i) * ld + k * GJB + j] = P[i * GJB + j];
-    return;
+    D[(int64_t)(k * GJB + i) * ld + k * GJB + j] = -P[i * GJB + j];
+  } else if (k < b) {
+    D[(int64_t)(k * GJB + i) * ld + b * GJB + j] = R[(int64_t)i * ld + b * GJB + j];
+  } else {
+    __shared__ double rs[GJB][GJB + 1];
+    rs[i][j] = R[(int64_t)i * ld + b * GJB + j];
+    __syncthreads();
+    D[(int64_t)(b * GJB + i) * ld + k * GJB + j] = rs[j][i];
   }
-  __shared__ double cs[GJB][GJB + 1], ps[GJB][GJB + 1];
-  cs[i][j] = D[(int64_t)(b * GJB + i) * ld + k * GJB + j];
-  ps[i][j] = P[i * GJB + j];
+}
+// D <- -D on the upper blocks, mirrored into the lower ones: the full A^-1
+__global__ void __launch_bounds__(GJB * GJB) k_sw_mirror(double* D, int64_t ld) {
+  const int ib = blockIdx.y, jb = blockIdx.x;
+  if (ib > jb) return;
+  __shared__ double ts[GJB][GJB + 1];
+  const int i = threadIdx.y, j = threadIdx.x;
+  const double v = -D[(int64_t)(ib * GJB + i) * ld + jb * GJB + j];
+  ts[i][j] = v;
   __syncthreads();
-  double acc = 0.0;
-#pragma unroll 8
-  for (int m = 0; m < GJB; ++m) acc += cs[i][m] * ps[m][j];
-  D[(int64_t)(b * GJB + i) * ld + k * GJB + j] = -acc;
-  D[(int64_t)(k * GJB + i) * ld + b * GJB + j] = R[(int64_t)i * ld + b * GJB + j];
+  if (ib == jb) {
+    D[(int64_t)(ib * GJB + i) * ld + jb * GJB + j] = 0.5 * (v + ts[j][i]);   // exact symmetry
+  } else {
+    D[(int64_t)(ib * GJB + i) * ld + jb * GJB + j] = v;
+    D[(int64_t)(jb * GJB + i) * ld + ib * GJB + j] = ts[j][i];
+  }
 }
 
 void gj_inverse(double* D, int64_t n, int64_t ld, double* work, cudaStream_t st) {
@@ -651,11 +688,12 @@ void gj_inverse(double* D, int64_t n, int64_t ld, double* work, cudaStream_t st)
   const dim3 thr(GJB, GJB);
   for (int k = 0; k < nb; ++k) {
     k_gj_pivot<<<1, thr, 0, st>>>(D, ld, k, P);
-    k_gj_rowpanel<<<nb, thr, 0, st>>>(D, ld, k, P, R);
-    k_gj_update<<<dim3(nb, nb), thr, 0, st>>>(D, ld, k, R);
-    k_gj_finish<<<nb, thr, 0, st>>>(D, ld, k, P, R);
+    k_sw_rowpanel<<<nb, thr, 0, st>>>(D, ld, k, P, R);
+    k_sw_update<<<dim3(nb, nb), thr, 0, st>>>(D, ld, k, R);
+    k_sw_finish<<<nb, thr, 0, st>>>(D, ld, k, P, R);
   }
-  count_launches(4 * (int64_t)nb - 1);
+  k_sw_mirror<<<dim3(nb, nb), thr, 0, st>>>(D, ld);
+  count_launches(4 * (int64_t)nb);
   TG_CHECK_LAUNCH();
 }
 
