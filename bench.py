@@ -141,9 +141,25 @@ def _problem(precision, device, size=None):
                       penal=PENAL, precision=precision, rtol=1e-8, device=device)
 
 
+# kernel families timed one at a time with CUDA events (library profiling kinds)
+FAMILIES = [(1, "fine_f64_residual"), (2, "fine_f32_kmul"), (3, "fine_bf16_jacobi"),
+            (8, "stencil_level1_f32"), (4, "stencil_levels2plus_f32"), (5, "stencil_f64"),
+            (6, "filter"), (7, "oc"), (9, "coarse_build"), (10, "coarse_inverse"),
+            (11, "vector"), (12, "transfer"), (13, "compliance"), (14, "learned_warm_start")]
+ROOFLINE_KERNEL = {1: "k_fine_zstream FP64 residual b - K u",
+                   2: "k_fine_zstream FP32 K.u (inner PCG)",
+                   3: "k_fine_zstream FP32 damped-Jacobi sweep (BF16 densities)",
+                   8: "k_stencil_apply FP32 level 1 (3 Jacobi sweeps + 1 residual per V-cycle)"}
+
+
 def _fine_bytes(kind, size=None):
-    """Algorithmic HBM bytes of one launch of a fine-grid K.u family."""
+    """Algorithmic HBM bytes of one launch of a kernel family."""
     nx, ny, nz = size or SIZE
+    if kind == 8:    # level-1 stencil: 14 stored 3x3 FP32 blocks per node + vectors
+        nn1 = (nx // 2 + 1) * (ny // 2 + 1) * (nz // 2 + 1)
+        jac = 14 * 9 * 4 * nn1 + 4 * 4 * 3 * nn1     # A, u, b, dinv in; x out
+        res = 14 * 9 * 4 * nn1 + 3 * 4 * 3 * nn1     # A, u, b in; r out
+        return (3 * jac + res) // 4
     nel = nx * ny * nz
     nnodes = (nx + 1) * (ny + 1) * (nz + 1)
     ndof = 3 * nnodes
@@ -233,6 +249,27 @@ def run_ours(args, dist, rank, ws, local):
     lib.tg_stats(1, None, C.byref(pms), C.byref(pcount))
     lib.tg_profile_kernel(0)
 
+    # device time per kernel family, one further design iteration per family
+    families = {}
+    tms = C.c_double()
+    step_ms = []
+    for kind, name in FAMILIES:
+        fms, fcount = C.c_double(), C.c_int64()
+        lib.tg_profile_kernel(kind)
+        lib.tg_timer(prob._h, 0, None)
+        steps_info.append(prob.step())
+        lib.tg_timer(prob._h, 1, C.byref(tms))
+        lib.tg_stats(1, None, C.byref(fms), C.byref(fcount))
+        lib.tg_profile_kernel(0)
+        step_ms.append(tms.value)
+        families[name] = {"ms": round(fms.value, 4), "launches": int(fcount.value)}
+    breakdown = {"method": "CUDA events around each family's launches on the library stream "
+                           "(event nodes inside the captured PCG-iteration graphs), one design "
+                           "iteration per family; learned_warm_start includes its own FP32 K.u "
+                           "launches (also in fine_f32_kmul)",
+                 "step_ms_profiled": round(float(np.mean(step_ms)), 3),
+                 "families": families}
+
     # ---------------- end to end through the public API, host buffers ----------------
     try:
         import torch
@@ -301,8 +338,7 @@ def run_ours(args, dist, rank, ws, local):
     avg_s = (pms.value / 1000.0 / pcount.value) if pcount.value else float("nan")
     nbytes = _fine_bytes(prof_kind)
     achieved = nbytes / avg_s / 1e9 if pcount.value else None
-    roofline = {"kernel": {1: "k_fine_apply FP64 residual", 2: "k_fine_apply FP32 K.u",
-                           3: "k_fine_apply FP32 Jacobi sweep (BF16 densities)"}.get(prof_kind),
+    roofline = {"kernel": ROOFLINE_KERNEL.get(prof_kind),
                 "bound": "hbm", "achieved": achieved, "peak": peak_hbm, "unit": "GB/s",
                 "frac": (achieved / peak_hbm) if achieved else None,
                 "traffic": None, "launches": pcount.value,
@@ -346,6 +382,7 @@ def run_ours(args, dist, rank, ws, local):
         "ratio_vs_plain_fp64": value / value_plain,
         "compliance_max_rel_diff_vs_fp64": obj_diff,
         "clocks": clk.summary(),
+        "time_breakdown": breakdown,
     }
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(steps=2, warmup=1)

@@ -221,13 +221,15 @@ int32_t tg_oc(tg_ctx* ctx, const double* x, const double* dc, const double* dv, 
     h2d(xd.p, x, nel, c.st);
     h2d(dcd.p, dc, nel, c.st);
     h2d(dvd.p, dv, nel, c.st);
-    tg::oc_begin(nel, dcd, dvd, c.S, c.oc, g, c.st);
+    const tg::OCScratch ocs{c.S.p, c.S.p + nel, c.S.p + 2 * nel};
+    tg::oc_begin(nel, xd, dcd, dvd, c.flags.p, c.move, ocs, c.oc, g, c.st);
     for (int k = 0; k < 16; ++k) {
-      tg::oc_steps(nel, xd, c.S, dvd, c.flags.p, c.move, xn, c.part2, c.oc, 16, c.st);
+      tg::oc_steps(nel, xd, ocs, dvd, c.flags.p, c.move, c.part2, c.oc, 16, c.st);
       d2h(c.h_oc, c.oc.p, 1, c.st);
       if (c.h_oc->done) break;
     }
     if (!c.h_oc->done) throw tg::Error{TG_ENOTCONV, "OC bisection did not terminate"};
+    tg::oc_finish(nel, xd, ocs, c.flags.p, c.move, xn, c.oc, c.st);
     d2h(xnew, xn.p, nel, c.st);
     if (gt) *gt = c.h_oc->gt;
     if (nsteps) *nsteps = c.h_oc->nsteps;
@@ -244,7 +246,7 @@ int32_t tg_oc_raw(int64_t n, const double* x, const double* dc, const double* dv
     tg::DevBuf<double> xd, dcd, dvd, xn, S, part;
     tg::DevBuf<int8_t> fl;
     tg::DevBuf<tg::OCState> oc;
-    xd.alloc(n); dcd.alloc(n); dvd.alloc(n); xn.alloc(n); S.alloc(n); part.alloc(tg::RED_BLOCKS);
+    xd.alloc(n); dcd.alloc(n); dvd.alloc(n); xn.alloc(n); S.alloc(3 * n); part.alloc(tg::RED_BLOCKS);
     oc.alloc(1);
     h2d(xd.p, x, n, st);
     h2d(dcd.p, dc, n, st);
@@ -254,13 +256,15 @@ int32_t tg_oc_raw(int64_t n, const double* x, const double* dc, const double* dv
       h2d(fl.p, el_flags, n, st);
     }
     tg::OCState h;
-    tg::oc_begin(n, dcd, dvd, S, oc, g, st, l1, l2);
+    const tg::OCScratch ocs{S.p, S.p + n, S.p + 2 * n};
+    tg::oc_begin(n, xd, dcd, dvd, fl.p, move, ocs, oc, g, st, l1, l2);
     for (int k = 0; k < 16; ++k) {
-      tg::oc_steps(n, xd, S, dvd, fl.p, move, xn, part, oc, 16, st);
+      tg::oc_steps(n, xd, ocs, dvd, fl.p, move, part, oc, 16, st);
       d2h(&h, oc.p, 1, st);
       if (h.done) break;
     }
     if (!h.done) throw tg::Error{TG_ENOTCONV, "OC bisection did not terminate"};
+    tg::oc_finish(n, xd, ocs, fl.p, move, xn, oc, st);
     d2h(xnew, xn.p, n, st);
     if (gt) *gt = h.gt;
     if (nsteps) *nsteps = h.nsteps;

@@ -14,6 +14,8 @@
 // fixed DOFs.
 #pragma once
 #include <cuda_runtime.h>
+#include <utility>
+#include <vector>
 #include <cuda_bf16.h>
 #include <stdint.h>
 #include <string>
@@ -78,13 +80,51 @@ void count_launches(int64_t n);
 
 // Optional event timing of one kernel family (see tg_profile_kernel):
 // prof_begin/prof_end bracket the launches of family `kind` on stream st.
+// Families are disjoint; a composite region (e.g. the coarsest inverse) is
+// timed as a whole.
 enum ProfKind : int {
-  PK_NONE = 0, PK_FINE_F64 = 1, PK_FINE_F32 = 2, PK_FINE_BF16 = 3, PK_STENCIL_F32 = 4,
-  PK_STENCIL_F64 = 5, PK_FILTER = 6, PK_OC = 7
+  PK_NONE = 0, PK_FINE_F64 = 1, PK_FINE_F32 = 2, PK_FINE_BF16 = 3,
+  PK_STENCIL_F32 = 4,     // coarse stencil sweeps, FP32, levels >= 2
+  PK_STENCIL_F64 = 5, PK_FILTER = 6, PK_OC = 7,
+  PK_STENCIL1_F32 = 8,    // coarse stencil sweeps, FP32, level 1
+  PK_COARSE_BUILD = 9,    // level operators, diagonals, dense coarsest matrix
+  PK_COARSE_INV = 10,     // coarsest dense inverse
+  PK_VECTOR = 11,         // PCG / refinement vector kernels and reductions
+  PK_TRANSFER = 12,       // restriction, prolongation, coarsest dense apply
+  PK_COMPLIANCE = 13,     // compliance and sensitivities
+  PK_LEARNED = 14,        // learned warm start inference
+  PK_NKINDS = 15
 };
 void prof_begin(int kind, cudaStream_t st);
 void prof_end(int kind, cudaStream_t st);
 int prof_kind();              // family being timed (PK_NONE when off)
+// brackets the enclosed launches of family k (no nesting of one family)
+struct ProfScope {
+  int k;
+  cudaStream_t s;
+  ProfScope(int k_, cudaStream_t s_) : k(k_), s(s_) { prof_begin(k, s); }
+  ~ProfScope() {
+    try {
+      prof_end(k, s);
+    } catch (...) {
+    }
+  }
+  ProfScope(const ProfScope&) = delete;
+  ProfScope& operator=(const ProfScope&) = delete;
+};
+// Event pairs recorded while a CUDA graph is captured: they become event
+// nodes of the graph and are read after every replay (device time of the
+// family inside the graph, without the host launch gaps of direct launches).
+struct ProfCapture {
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pairs;
+  cudaEvent_t open = nullptr;
+  int kind = 0;
+  void release();
+  ~ProfCapture() { release(); }
+};
+void prof_capture_begin(ProfCapture* pc);   // prof_begin/end now record into pc
+void prof_capture_end();
+void prof_collect(const ProfCapture& pc);   // after a replay has completed
 int64_t launch_count();       // kernels launched so far
 
 #define TG_REQUIRE(cond, msg)                                                \

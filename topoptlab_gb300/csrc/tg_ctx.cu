@@ -256,7 +256,7 @@ void ctx_init(Ctx& c, const tg_problem& p) {
   // vectors
   c.f.alloc(nd); c.u.alloc(nd);
   c.x.alloc(nel); c.xPhys.alloc(nel); c.xold.alloc(nel); c.xnew.alloc(nel);
-  c.dc.alloc(nel); c.dcf.alloc(nel); c.dv.alloc(nel); c.Hs.alloc(nel); c.S.alloc(nel);
+  c.dc.alloc(nel); c.dcf.alloc(nel); c.dv.alloc(nel); c.Hs.alloc(nel); c.S.alloc(3 * nel);
   c.s64.alloc(nel);
   if (mixed) { c.s32.alloc(nel); c.s16.alloc(nel); }
   c.part.alloc(RED_BLOCKS); c.part2.alloc(RED_BLOCKS); c.scal.alloc(8);
@@ -291,6 +291,7 @@ void ctx_init(Ctx& c, const tg_problem& p) {
   c.fw.alloc(nw);
   TG_CUDA(cudaMemcpy(c.fw.p, w.data(), sizeof(double) * nw, cudaMemcpyHostToDevice));
   c.fs.R = R; c.fs.nw = nw; c.fs.w = c.fw.p;
+  c.fs.tmp = c.S.p + nel;   // OC scratch, idle while a filter runs
   filter_apply(g, c.fs, nullptr, nullptr, nullptr, c.Hs, 3, c.st);
   // dv: ones, filtered once for the density filter (topology_optimization.py:520, :558)
   std::vector<double> ones(nel, 1.0);
@@ -309,12 +310,15 @@ void ctx_init(Ctx& c, const tg_problem& p) {
 // hierarchy
 // ---------------------------------------------------------------------------
 void set_density(Ctx& c, const double* xPhys) {
+  ProfScope ps(PK_COARSE_BUILD, c.st);
   simp_scale(c.g.nel(), xPhys, c.eps, c.penal, c.s64, c.s32.p, c.s16.p, c.st);
 }
 
 void build_hierarchy(Ctx& c) {
   const bool mixed = c.precision == TG_PREC_MIXED;
   Level& f = *c.lv[0];
+  {
+  ProfScope ps(PK_COARSE_BUILD, c.st);
   fine_dinv<double, double>(c.op, c.s64, f.dinv64, c.st);
   if (mixed) fine_dinv<float, __nv_bfloat16>(c.op, c.s16, f.dinv32, c.st);
   if (c.precond != TG_PRECOND_GMG) return;
@@ -333,6 +337,8 @@ void build_hierarchy(Ctx& c) {
   Level& cl = *c.lv[c.L - 1];
   if (c.L == 1) build_fine_stencil(c.op, c.s64, cl.A64, c.st);
   stencil_to_dense(cl.g, cl.fix, cl.A64, c.Dc, c.nc, c.ldc, c.st);
+  }
+  ProfScope ps(PK_COARSE_INV, c.st);
   gj_inverse(c.Dc, c.nc, c.ldc, c.gjwork, c.st);
 }
 
@@ -369,6 +375,7 @@ static void level_apply(Ctx& c, int l, const T* in, T* out, const T* b, int mode
                                        (const float*)b, (const float*)LvBufs<T>::dinv(v), c.omega,
                                        mode, c.st);
   } else {
+    ProfScope ps(sizeof(T) == 8 ? PK_STENCIL_F64 : (l == 1 ? PK_STENCIL1_F32 : PK_STENCIL_F32), c.st);
     stencil_apply<T>(v.g, LvBufs<T>::A(v), in, out, b, LvBufs<T>::dinv(v), c.omega, mode, c.st);
   }
 }
@@ -377,12 +384,16 @@ template <typename T> void vcycle(Ctx& c, int l, const T* b, T* x) {
   Level& v = *c.lv[l];
   const int64_t n = v.g.ndofs();
   if (l == c.L - 1) {
-    dense_apply<T>(c.Dc, c.nc, c.ldc, b, x, c.st);
+    ProfScope ps(PK_TRANSFER, c.st);
+    dense_apply<T>(c.Dc, c.nc, c.ldc, b, x, c.gjwork, c.st);   // GJ scratch is idle here
     return;
   }
   T* bufs[2] = {x, LvBufs<T>::t(v)};
   int cur = 0;
-  scale_mul<T>(n, c.omega, LvBufs<T>::dinv(v), b, bufs[cur], c.st);
+  {
+    ProfScope ps(PK_VECTOR, c.st);
+    scale_mul<T>(n, c.omega, LvBufs<T>::dinv(v), b, bufs[cur], c.st);
+  }
   for (int s = 1; s < c.nsmooth; ++s) {
     level_apply<T>(c, l, bufs[cur], bufs[1 - cur], b, AM_JACOBI);
     cur = 1 - cur;
@@ -390,15 +401,23 @@ template <typename T> void vcycle(Ctx& c, int l, const T* b, T* x) {
   T* r = LvBufs<T>::r(v);
   level_apply<T>(c, l, bufs[cur], r, b, AM_RES);
   Level& w = *c.lv[l + 1];
-  restrict_<T>(v.g, w.g, w.fix, r, LvBufs<T>::b(w), c.st);
+  {
+    ProfScope ps(PK_TRANSFER, c.st);
+    restrict_<T>(v.g, w.g, w.fix, r, LvBufs<T>::b(w), c.st);
+  }
   vcycle<T>(c, l + 1, LvBufs<T>::b(w), LvBufs<T>::x(w));
-  prolong_add<T>(v.g, w.g, v.fix, LvBufs<T>::x(w), bufs[cur], c.st);
+  {
+    ProfScope ps(PK_TRANSFER, c.st);
+    prolong_add<T>(v.g, w.g, v.fix, LvBufs<T>::x(w), bufs[cur], c.st);
+  }
   for (int s = 0; s < c.nsmooth; ++s) {
     level_apply<T>(c, l, bufs[cur], bufs[1 - cur], b, AM_JACOBI);
     cur = 1 - cur;
   }
-  if (bufs[cur] != x)
+  if (bufs[cur] != x) {
+    ProfScope ps(PK_VECTOR, c.st);
     TG_CUDA(cudaMemcpyAsync(x, bufs[cur], sizeof(T) * n, cudaMemcpyDeviceToDevice, c.st));
+  }
 }
 template void vcycle<double>(Ctx&, int, const double*, double*);
 template void vcycle<float>(Ctx&, int, const float*, float*);
@@ -408,6 +427,7 @@ static void precondition(Ctx& c, const T* r, T* z) {
   if (c.precond == TG_PRECOND_GMG) {
     vcycle<T>(c, 0, r, z);
   } else {
+    ProfScope ps(PK_VECTOR, c.st);
     scale_mul<T>(c.g.ndofs(), 1.0, LvBufs<T>::dinv(*c.lv[0]), r, z, c.st);
   }
 }
@@ -425,26 +445,37 @@ static void check_finite(double v, const char* what) {
 }
 
 // Run one PCG iteration body: replayed from a CUDA graph captured on first
-// use (one launch per iteration instead of ~35), or launched directly while a
-// kernel family is being event-timed.  Ends with the PCG scalars in h_pcg.
+// use (one launch per iteration instead of ~35).  While a kernel family is
+// event-timed the graph is captured again with the family's event pairs as
+// graph nodes, read after each replay.  Ends with the PCG scalars in h_pcg.
 template <typename F>
 static void run_iteration(Ctx& c, Ctx::IterGraph& gr, F&& body) {
-  if (!c.use_graphs || prof_kind() != PK_NONE) {
+  if (!c.use_graphs) {
     body();
     TG_CUDA(cudaStreamSynchronize(c.st));
     return;
+  }
+  const int kind = prof_kind();
+  if (gr.exec && gr.kind != kind) {
+    cudaGraphExecDestroy(gr.exec);
+    gr.exec = nullptr;
+    gr.prof.release();
   }
   if (!gr.exec) {
     const int64_t before = launch_count();
     cudaGraph_t graph = nullptr;
     TG_CUDA(cudaStreamBeginCapture(c.st, cudaStreamCaptureModeThreadLocal));
+    if (kind != PK_NONE) prof_capture_begin(&gr.prof);
     try {
       body();
     } catch (...) {
+      prof_capture_end();
       cudaStreamEndCapture(c.st, &graph);
       if (graph) cudaGraphDestroy(graph);
       throw;
     }
+    prof_capture_end();
+    gr.kind = kind;
     TG_CUDA(cudaStreamEndCapture(c.st, &graph));
     const cudaError_t e = cudaGraphInstantiate(&gr.exec, graph, 0);
     cudaGraphDestroy(graph);
@@ -455,6 +486,7 @@ static void run_iteration(Ctx& c, Ctx::IterGraph& gr, F&& body) {
   TG_CUDA(cudaGraphLaunch(gr.exec, c.st));
   count_launches(gr.launches);
   TG_CUDA(cudaStreamSynchronize(c.st));
+  if (kind != PK_NONE) prof_collect(gr.prof);
 }
 
 // plain FP64 PCG (linear_solvers.py:114-134), x in/out
@@ -474,9 +506,13 @@ static int pcg64(Ctx& c, const double* b, double* x, double tol_abs, int maxiter
   while (!conv && it < maxiter) {
     run_iteration(c, c.g64, [&] {
       precondition<double>(c, c.r, c.z);
-      dot<double, double>(n, c.r.p, c.z.p, c.part, c.pcg, DOT_RHO, c.st);
-      update_p<double>(n, c.z, c.p, c.pcg, c.st);
+      {
+        ProfScope ps(PK_VECTOR, c.st);
+        dot<double, double>(n, c.r.p, c.z.p, c.part, c.pcg, DOT_RHO, c.st);
+        update_p<double>(n, c.z, c.p, c.pcg, c.st);
+      }
       fine_apply<double, double>(c.op, c.s64, c.p, c.q, nullptr, nullptr, 0.0, AM_Y, c.st);
+      ProfScope ps(PK_VECTOR, c.st);
       dot<double, double>(n, c.p.p, c.q.p, c.part, c.pcg, DOT_ALPHA, c.st);
       update_xr<double>(n, c.p, c.q, xs, c.r, c.part, c.pcg, c.st);
       TG_CUDA(cudaMemcpyAsync(c.h_pcg, c.pcg.p, sizeof(PCGState), cudaMemcpyDeviceToHost, c.st));
@@ -499,9 +535,13 @@ static int pcg32(Ctx& c, double tol_abs, int maxiter) {
   while (it < maxiter) {
     run_iteration(c, c.g32, [&] {
       precondition<float>(c, c.r32, c.z32);
-      dot<float, float>(n, c.r32.p, c.z32.p, c.part, c.pcg, DOT_RHO, c.st);
-      update_p<float>(n, c.z32, c.p32, c.pcg, c.st);
+      {
+        ProfScope ps(PK_VECTOR, c.st);
+        dot<float, float>(n, c.r32.p, c.z32.p, c.part, c.pcg, DOT_RHO, c.st);
+        update_p<float>(n, c.z32, c.p32, c.pcg, c.st);
+      }
       fine_apply<float, float>(c.op, c.s32, c.p32, c.q32, nullptr, nullptr, 0.0, AM_Y, c.st);
+      ProfScope ps(PK_VECTOR, c.st);
       dot<float, float>(n, c.p32.p, c.q32.p, c.part, c.pcg, DOT_ALPHA, c.st);
       update_xr<float>(n, c.p32, c.q32, c.d32, c.r32, c.part, c.pcg, c.st);
       TG_CUDA(cudaMemcpyAsync(c.h_pcg, c.pcg.p, sizeof(PCGState), cudaMemcpyDeviceToHost, c.st));
@@ -548,8 +588,11 @@ void solve(Ctx& c, const double* b, double* u) {
     double rr = 0.0;
     for (int k = 0; k < 64 && total < c.maxiter; ++k) {
       fine_apply<double, double>(c.op, c.s64, u, c.r, b, nullptr, 0.0, AM_RES, c.st);
-      pcg_reset(c.pcg_out, c.st);
-      dot<double, double>(n, c.r.p, c.r.p, c.part, c.pcg_out, DOT_RR, c.st);
+      {
+        ProfScope ps(PK_VECTOR, c.st);
+        pcg_reset(c.pcg_out, c.st);
+        dot<double, double>(n, c.r.p, c.r.p, c.part, c.pcg_out, DOT_RR, c.st);
+      }
       read_pcg(c, c.pcg_out);
       rr = c.h_pcg->rr;
       check_finite(rr, "FP64 residual");
@@ -557,9 +600,13 @@ void solve(Ctx& c, const double* b, double* u) {
         conv = true;
         break;
       }
-      to_unit_f32(n, c.r, c.pcg_out, c.r32, c.st);
+      {
+        ProfScope ps(PK_VECTOR, c.st);
+        to_unit_f32(n, c.r, c.pcg_out, c.r32, c.st);
+      }
       const double inner = std::max(c.inner_rtol, 0.5 * tol / std::sqrt(rr));
       total += pcg32(c, inner, c.maxiter - total);
+      ProfScope ps(PK_VECTOR, c.st);
       add_scaled_f32(n, c.d32, c.pcg_out, u, c.st);
       c.last_refine = k + 1;
     }
@@ -595,27 +642,35 @@ void ctx_step(Ctx& c, tg_iter_out& out) {
   // learned warm start (falls back to the previous displacement when its
   // residual is not smaller); the solve below is unchanged either way
   int fallback = 0;
-  if (c.learned && c.cnn && c.cnn->trained && c.iter > 0) fallback = c.cnn->warm_start(c);
+  if (c.learned && c.cnn && c.cnn->trained && c.iter > 0) {
+    ProfScope ps(PK_LEARNED, c.st);
+    fallback = c.cnn->warm_start(c);
+  }
   solve(c, c.f, c.u);
   TG_CUDA(cudaEventRecord(c.ev1, c.st));
   // compliance + raw sensitivity
-  fine_compliance(c.op, c.xPhys, c.u, c.eps, c.penal, c.dc, c.part, c.st);
   const int nbe = (int)red_blocks(nel);
-  reduce_partials(c.part, nbe, c.scal.p + 0, false, c.st);
+  {
+    ProfScope ps(PK_COMPLIANCE, c.st);
+    fine_compliance(c.op, c.xPhys, c.u, c.eps, c.penal, c.dc, c.part, c.st);
+    reduce_partials(c.part, nbe, c.scal.p + 0, false, c.st);
+  }
   // sensitivity filter
   if (c.ft == 1) filter_apply(g, c.fs, c.dc, nullptr, c.Hs, c.dcf, 1, c.st);
   else if (c.ft == 0) filter_apply(g, c.fs, c.x, c.dc, c.Hs, c.dcf, 2, c.st);
   else TG_CUDA(cudaMemcpyAsync(c.dcf.p, c.dc.p, sizeof(double) * nel, cudaMemcpyDeviceToDevice, c.st));
   // OC
-  oc_begin(nel, c.dcf, c.dv, c.S, c.oc, c.g_oc, c.st);
+  const OCScratch ocs{c.S.p, c.S.p + nel, c.S.p + 2 * nel};
+  oc_begin(nel, c.x, c.dcf, c.dv, c.flags.p, c.move, ocs, c.oc, c.g_oc, c.st);
   int guard = 0;
   for (;;) {
-    oc_steps(nel, c.x, c.S, c.dv, c.flags.p, c.move, c.xnew, c.part2, c.oc, 16, c.st);
+    oc_steps(nel, c.x, ocs, c.dv, c.flags.p, c.move, c.part2, c.oc, 16, c.st);
     TG_CUDA(cudaMemcpyAsync(c.h_oc, c.oc.p, sizeof(OCState), cudaMemcpyDeviceToHost, c.st));
     TG_CUDA(cudaStreamSynchronize(c.st));
     if (c.h_oc->done) break;
     if (++guard > 16) throw Error{ENOTCONV, "OC bisection did not terminate within 256 steps"};
   }
+  oc_finish(nel, c.x, ocs, c.flags.p, c.move, c.xnew, c.oc, c.st);
   c.g_oc = c.h_oc->gt;
   // x_old <- x ; x <- x_new
   std::swap(c.xold.p, c.x.p);

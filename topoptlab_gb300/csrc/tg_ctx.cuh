@@ -91,6 +91,8 @@ struct Ctx {
   struct IterGraph {
     cudaGraphExec_t exec = nullptr;
     int64_t launches = 0;        // kernels per replay
+    int kind = 0;                // profiled family the graph was captured for
+    ProfCapture prof;            // its event pairs
   } g64, g32;
   bool use_graphs = true;
   struct Cnn* cnn = nullptr;     // learned warm start (not owned)

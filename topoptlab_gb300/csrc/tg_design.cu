@@ -45,8 +45,9 @@ __global__ void __launch_bounds__(RED_THREADS) k_filter(Grid g, int R, const dou
           const int ny = ey + oy;
           if (ny < 0 || ny >= g.ney) continue;
           const double wt = w[((NDIM == 3 ? (oz + R) * W : 0) + (ox + R)) * W + (oy + R)];
+          if (wt == 0.0) continue;          // uniform over the block: taps beyond rmin
           const int64_t nb = g.elem(nx, ny, nz);
-          if (MODE == 0) acc += wt * x[nb];
+          if (MODE == 0 || MODE == 5) acc += wt * x[nb];
           else if (MODE == 1) acc += wt * (x[nb] / Hs[nb]);
           else if (MODE == 2) acc += wt * (x[nb] * d[nb]);
           else acc += wt;
@@ -57,7 +58,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_filter(Grid g, int R, const dou
     if (MODE == 0) out = acc / Hs[e];
     else if (MODE == 1) out = acc;
     else if (MODE == 2) out = acc / Hs[e] / fmax(0.001, x[e]);
-    else if (MODE == 3) out = acc;
+    else if (MODE == 3 || MODE == 5) out = acc;
     else out = x[e];
     y[e] = out;
     if (part_sum) psum += out;
@@ -73,18 +74,32 @@ __global__ void __launch_bounds__(RED_THREADS) k_filter(Grid g, int R, const dou
   }
 }
 
+__global__ void k_div(int64_t n, const double* __restrict__ a, const double* __restrict__ b,
+                      double* __restrict__ q) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) q[i] = a[i] / b[i];
+}
+
 void filter_apply_ex(const Grid& g, const FilterStencil& fs, const double* x, const double* d,
                      const double* Hs, double* y, int mode, const double* xold, double* part_sum,
                      double* part_max, cudaStream_t st) {
   const unsigned blocks = red_blocks(g.nel());
   prof_begin(PK_FILTER, st);
+  if (mode == 1 && fs.tmp) {
+    // H (x / Hs): the quotient once per element (GB300's FP64 divide is a
+    // multi-instruction sequence on the narrow FP64 pipe), then a plain sum
+    k_div<<<(unsigned)cdiv(g.nel(), 256), 256, 0, st>>>(g.nel(), x, Hs, fs.tmp);
+    TG_CHECK_LAUNCH();
+    x = fs.tmp;
+    mode = 5;
+  }
 #define TG_F(ND, M) k_filter<ND, M><<<blocks, RED_THREADS, 0, st>>>(g, fs.R, fs.w, x, d, Hs, y, xold, part_sum, part_max)
   if (g.ndim == 3) {
     if (mode == 0) TG_F(3, 0); else if (mode == 1) TG_F(3, 1); else if (mode == 2) TG_F(3, 2);
-    else if (mode == 3) TG_F(3, 3); else TG_F(3, 4);
+    else if (mode == 3) TG_F(3, 3); else if (mode == 5) TG_F(3, 5); else TG_F(3, 4);
   } else {
     if (mode == 0) TG_F(2, 0); else if (mode == 1) TG_F(2, 1); else if (mode == 2) TG_F(2, 2);
-    else if (mode == 3) TG_F(2, 3); else TG_F(2, 4);
+    else if (mode == 3) TG_F(2, 3); else if (mode == 5) TG_F(2, 5); else TG_F(2, 4);
   }
 #undef TG_F
   prof_end(PK_FILTER, st);
@@ -154,42 +169,68 @@ __global__ void k_oc_init(OCState* s, double g, double l1, double l2) {
   s->nsteps = 0;
   s->done = ((l2 - l1) / (l1 + l2) > 1e-3) ? 0 : 1;
   s->lmid = 0.5 * (l2 + l1);
+  s->sc = 1.0 / sqrt(s->lmid);
+  s->sc_last = s->sc;
   s->ticket = 0;
 }
 
-__global__ void __launch_bounds__(RED_THREADS) k_oc_prep(int64_t n, const double* __restrict__ dc,
-                                                        const double* __restrict__ dv,
-                                                        double* __restrict__ S) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i < n) S[i] = sqrt(-dc[i] / dv[i]);
-}
-
-__global__ void __launch_bounds__(RED_THREADS) k_oc_step(int64_t n, const double* __restrict__ x,
-                                                        const double* __restrict__ S,
+// Per design iteration: P = x * sqrt(-dc/dv) and, when stored, the bounds
+// lo = max(0, x - move), hi = min(1, x + move) (flags: lo = hi = 0 or 1).
+// The step value max(lo, min(hi, P / sqrt(lmid))) equals the reference's
+// max(0, max(x - move, min(1, min(x + move, x sqrt(-dc/dv/lmid))))) with the
+// square root of the quotient split as sqrt(-dc/dv) / sqrt(lmid).
+__global__ void __launch_bounds__(RED_THREADS) k_oc_prep(int64_t n, const double* __restrict__ x,
+                                                        const double* __restrict__ dc,
                                                         const double* __restrict__ dv,
                                                         const int8_t* __restrict__ flags,
-                                                        double move, double* __restrict__ xnew,
-                                                        double* part, OCState* st) {
+                                                        double move, OCScratch sc) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double xi = x[i];
+  sc.P[i] = xi * sqrt(-dc[i] / dv[i]);
+  if (sc.lo) {
+    double lo = fmax(0.0, xi - move), hi = fmin(1.0, xi + move);
+    if (flags) {
+      if (flags[i] == 1) lo = hi = 0.0;
+      else if (flags[i] == 2) lo = hi = 1.0;
+    }
+    sc.lo[i] = lo;
+    sc.hi[i] = hi;
+  }
+}
+
+template <bool BOUNDS>
+__device__ __forceinline__ double oc_value(int64_t i, double xi, const OCScratch& sc,
+                                           const int8_t* __restrict__ flags, double move,
+                                           double s) {
+  const double b = sc.P[i] * s;
+  if (BOUNDS) return fmax(sc.lo[i], fmin(sc.hi[i], b));
+  double xn = fmax(0.0, fmax(xi - move, fmin(1.0, fmin(xi + move, b))));
+  if (flags) {
+    if (flags[i] == 1) xn = 0.0;
+    else if (flags[i] == 2) xn = 1.0;
+  }
+  return xn;
+}
+
+template <bool BOUNDS>
+__global__ void __launch_bounds__(RED_THREADS) k_oc_step(int64_t n, const double* __restrict__ x,
+                                                        OCScratch sc, const double* __restrict__ dv,
+                                                        const int8_t* __restrict__ flags,
+                                                        double move, double* part, OCState* st) {
   __shared__ double sh[32];
   __shared__ int last;
   if (st->done) return;   // uniform: written by a previous launch
-  const double lmid = st->lmid;
-  const double sc = 1.0 / sqrt(lmid);
+  const double s = st->sc;
   double acc = 0.0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     const double xi = x[i];
-    double xn = fmax(0.0, fmax(xi - move, fmin(1.0, fmin(xi + move, xi * S[i] * sc))));
-    if (flags) {
-      if (flags[i] == 1) xn = 0.0;
-      else if (flags[i] == 2) xn = 1.0;
-    }
-    xnew[i] = xn;
-    acc += dv[i] * (xn - xi);
+    acc += dv[i] * (oc_value<BOUNDS>(i, xi, sc, flags, move, s) - xi);
   }
-  const double s = block_sum(acc, sh);
+  const double bs = block_sum(acc, sh);
   if (threadIdx.x == 0) {
-    part[blockIdx.x] = s;
+    part[blockIdx.x] = bs;
     __threadfence();
     const unsigned t = atomicAdd(&st->ticket, 1u);
     last = (t == gridDim.x - 1);
@@ -201,32 +242,60 @@ __global__ void __launch_bounds__(RED_THREADS) k_oc_step(int64_t n, const double
   if (threadIdx.x == 0) {
     const double gt = st->g + tot;
     st->gt = gt;
-    if (gt > 0) st->l1 = lmid;
-    else st->l2 = lmid;
+    st->sc_last = s;
+    if (gt > 0) st->l1 = st->lmid;
+    else st->l2 = st->lmid;
     st->nsteps += 1;
     const double l1 = st->l1, l2 = st->l2;
-    if ((l2 - l1) / (l1 + l2) > 1e-3) st->lmid = 0.5 * (l2 + l1);
-    else st->done = 1;
+    if ((l2 - l1) / (l1 + l2) > 1e-3) {
+      st->lmid = 0.5 * (l2 + l1);
+      st->sc = 1.0 / sqrt(st->lmid);
+    } else {
+      st->done = 1;
+    }
     st->ticket = 0;
   }
 }
 
-void oc_begin(int64_t n, const double* dc, const double* dv, double* S, OCState* st, double g,
-              cudaStream_t s, double l1, double l2) {
-  k_oc_prep<<<(unsigned)cdiv(n, RED_THREADS), RED_THREADS, 0, s>>>(n, dc, dv, S);
+template <bool BOUNDS>
+__global__ void __launch_bounds__(RED_THREADS) k_oc_finish(int64_t n, const double* __restrict__ x,
+                                                          OCScratch sc,
+                                                          const int8_t* __restrict__ flags,
+                                                          double move, double* __restrict__ xnew,
+                                                          const OCState* st) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) xnew[i] = oc_value<BOUNDS>(i, x[i], sc, flags, move, st->sc_last);
+}
+
+void oc_begin(int64_t n, const double* x, const double* dc, const double* dv, const int8_t* flags,
+              double move, OCScratch sc, OCState* st, double g, cudaStream_t s, double l1,
+              double l2) {
+  prof_begin(PK_OC, s);
+  k_oc_prep<<<(unsigned)cdiv(n, RED_THREADS), RED_THREADS, 0, s>>>(n, x, dc, dv, flags, move, sc);
   k_oc_init<<<1, 1, 0, s>>>(st, g, l1, l2);
+  prof_end(PK_OC, s);
   count_launches(1);
   TG_CHECK_LAUNCH();
 }
-void oc_steps(int64_t n, const double* x, const double* S, const double* dv, const int8_t* flags,
-              double move, double* xnew, double* part, OCState* st, int nsteps, cudaStream_t s) {
+void oc_steps(int64_t n, const double* x, OCScratch sc, const double* dv, const int8_t* flags,
+              double move, double* part, OCState* st, int nsteps, cudaStream_t s) {
   const unsigned blocks = red_blocks(n);
+  prof_begin(PK_OC, s);
   for (int k = 0; k < nsteps; ++k) {
-    prof_begin(PK_OC, s);
-    k_oc_step<<<blocks, RED_THREADS, 0, s>>>(n, x, S, dv, flags, move, xnew, part, st);
-    prof_end(PK_OC, s);
+    if (sc.lo) k_oc_step<true><<<blocks, RED_THREADS, 0, s>>>(n, x, sc, dv, flags, move, part, st);
+    else k_oc_step<false><<<blocks, RED_THREADS, 0, s>>>(n, x, sc, dv, flags, move, part, st);
   }
+  prof_end(PK_OC, s);
   count_launches(nsteps - 1);
+  TG_CHECK_LAUNCH();
+}
+void oc_finish(int64_t n, const double* x, OCScratch sc, const int8_t* flags, double move,
+               double* xnew, const OCState* st, cudaStream_t s) {
+  const unsigned blocks = (unsigned)cdiv(n, RED_THREADS);
+  prof_begin(PK_OC, s);
+  if (sc.lo) k_oc_finish<true><<<blocks, RED_THREADS, 0, s>>>(n, x, sc, flags, move, xnew, st);
+  else k_oc_finish<false><<<blocks, RED_THREADS, 0, s>>>(n, x, sc, flags, move, xnew, st);
+  prof_end(PK_OC, s);
   TG_CHECK_LAUNCH();
 }
 
@@ -243,6 +312,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_dot(int64_t n, const TA* __rest
   __shared__ double sh[32];
   __shared__ int last;
   TA acc = TA(0);
+#pragma unroll 4
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
     acc = fma(a[i], (TA)b[i], acc);
@@ -307,6 +377,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_update_xr(int64_t n, const T* _
   __shared__ int last;
   const T alpha = (T)st->alpha;
   T acc = T(0);
+#pragma unroll 4
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     x[i] = fma(alpha, p[i], x[i]);

@@ -8,8 +8,17 @@ namespace tg {
 // OC bisection state (optimizer/optimality_criterion.py:59-77)
 struct OCState {
   double l1, l2, lmid, g, gt;
+  double sc;         // 1/sqrt(lmid) of the next step (computed once per step)
+  double sc_last;    // 1/sqrt(lmid) of the last evaluated step
   int done, nsteps;
   unsigned int ticket;
+};
+// per-call scratch: P = x*sqrt(-dc/dv); lo/hi = the move-limit bounds with the
+// passive/active flags folded in (both null: recomputed from x every step)
+struct OCScratch {
+  double* P;
+  double* lo;
+  double* hi;
 };
 
 // PCG scalars (linear_solvers.py:114-134)
@@ -25,10 +34,15 @@ void filter_apply_ex(const Grid& g, const FilterStencil& fs, const double* x, co
                      double* part_max, cudaStream_t st);
 void reduce_partials(const double* part, int nb, double* out, bool is_max, cudaStream_t st);
 
-void oc_begin(int64_t n, const double* dc, const double* dv, double* S, OCState* st, double g,
-              cudaStream_t s, double l1 = 0.0, double l2 = 1e9);
-void oc_steps(int64_t n, const double* x, const double* S, const double* dv, const int8_t* flags,
-              double move, double* xnew, double* part, OCState* st, int nsteps, cudaStream_t s);
+void oc_begin(int64_t n, const double* x, const double* dc, const double* dv, const int8_t* flags,
+              double move, OCScratch sc, OCState* st, double g, cudaStream_t s, double l1 = 0.0,
+              double l2 = 1e9);
+// nsteps bisection steps (launches after `done` return at once)
+void oc_steps(int64_t n, const double* x, OCScratch sc, const double* dv, const int8_t* flags,
+              double move, double* part, OCState* st, int nsteps, cudaStream_t s);
+// xnew at the last evaluated lmid (call once `done` is set)
+void oc_finish(int64_t n, const double* x, OCScratch sc, const int8_t* flags, double move,
+               double* xnew, const OCState* st, cudaStream_t s);
 
 template <typename TA, typename TB>
 void dot(int64_t n, const TA* a, const TB* b, double* part, PCGState* st, int op, cudaStream_t s);

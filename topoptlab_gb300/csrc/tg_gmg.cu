@@ -18,6 +18,7 @@
 //  * the coarsest level (a few hundred to ~2000 DOFs) is inverted once per
 //    design iteration by a blocked Gauss-Jordan in FP64 and applied as one
 //    dense mat-vec per V-cycle.
+#include <algorithm>
 #include "tg_ops.cuh"
 
 namespace tg {
@@ -60,60 +61,87 @@ __device__ __forceinline__ T coef(const T* __restrict__ A, int64_t ld, int d, in
                 : __ldg(A + (((C - d) * NDOF + cj) * NDOF + ci) * ld + m);
 }
 
-// one thread per (row component ci, node): coalesced coefficient loads (the
-// node index is fastest), NDOF times the parallelism of a thread per node,
-// which matters on the small coarse grids.  No branches around the loads: a
-// neighbour outside the grid is replaced by the node itself and its u is
-// selected to zero, so all 2*27*NDOF loads of a thread can be in flight at
-// once (the small levels are latency-bound).
+// One thread per node (all NDOF rows), one CTA per (TY x TX) patch of a node
+// plane.  TY spans whole y-rows where the grid allows, so consecutive threads
+// own consecutive nodes and every coefficient load of a warp is contiguous.
+// The u values of the patch and its one-node halo in the planes z-1, z, z+1
+// are staged in shared memory, component-major (stride-1 reads across a
+// warp), with zeros outside the grid.  A lower-direction block is read at the
+// neighbour; outside the grid the node's own (finite) block is read instead
+// and meets a zero u, so the loads need no branches.
 template <int NDIM, int NDOF, typename T, int MODE>
-__global__ void __launch_bounds__(256) k_stencil_apply(Grid g, const T* __restrict__ A,
+__global__ void __launch_bounds__(256) k_stencil_apply(Grid g, int TY, int TX,
+                                                      const T* __restrict__ A,
                                                       const T* __restrict__ u, T* __restrict__ y,
                                                       const T* __restrict__ b,
                                                       const T* __restrict__ dinv, T omega) {
-  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  constexpr int NP = (NDIM == 3) ? 3 : 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* us = reinterpret_cast<T*>(smem_raw);
+  const int RY = TY + 2, PL = (TX + 2) * RY;
+  const int y0 = blockIdx.x * TY, x0 = blockIdx.y * TX, z = blockIdx.z;
   const int64_t ld = g.nnodes();
-  if (t >= ld * NDOF) return;
-  const int ci = (int)(t / ld);
-  const int64_t n = t - (int64_t)ci * ld;
-  int x, yy, z;
-  node_xyz(g, n, x, yy, z);
-  const bool ok[3][3] = {{x > 0, true, x + 1 < g.nnx},
+  const int tid = threadIdx.x;
+  // stage u (global order: component fastest)
+  for (int i = tid; i < NDOF * NP * PL; i += blockDim.x) {
+    const int c = i % NDOF, hy = (i / NDOF) % RY, hx = (i / (NDOF * RY)) % (TX + 2);
+    const int pz = i / (NDOF * PL);
+    const int gx = x0 - 1 + hx, gy = y0 - 1 + hy, gz = (NDIM == 3) ? z - 1 + pz : 0;
+    T v = T(0);
+    if (in_grid(g, gx, gy, gz)) v = __ldg(u + g.node(gx, gy, gz) * NDOF + c);
+    us[(c * NP + pz) * PL + hx * RY + hy] = v;
+  }
+  __syncthreads();
+  const int ty = tid % TY, tx = tid / TY;
+  const int xx = x0 + tx, yy = y0 + ty;
+  if (tx >= TX || xx >= g.nnx || yy >= g.nny) return;
+  const int64_t n = g.node(xx, yy, z);
+  const bool ok[3][3] = {{xx > 0, true, xx + 1 < g.nnx},
                          {yy > 0, true, yy + 1 < g.nny},
                          {z > 0, true, z + 1 < g.nnz}};
   const int64_t sx = g.nny, sz = (int64_t)g.nny * g.nnx;
-  T acc = T(0);
+  const T* uc = us + ((NDIM == 3) ? PL : 0) + (tx + 1) * RY + (ty + 1);   // centre, plane z
+  T acc[NDOF];
+#pragma unroll
+  for (int ci = 0; ci < NDOF; ++ci) acc[ci] = T(0);
 #pragma unroll
   for (int d = 0; d < ndir<NDIM>(); ++d) {
     int dx, dy, dz;
     dir_xyz(d, NDIM, dx, dy, dz);
     const bool v = ok[0][dx + 1] && ok[1][dy + 1] && ok[2][dz + 1];
     const int64_t m = v ? n + dz * sz + dx * sx + dy : n;
+    const int so = dz * PL + dx * RY + dy;
 #pragma unroll
     for (int cj = 0; cj < NDOF; ++cj) {
-      const T uu = __ldg(u + m * NDOF + cj);
-      acc = fma(coef<NDIM, NDOF, T>(A, ld, d, ci, cj, n, m), v ? uu : T(0), acc);
+      const T uu = uc[cj * NP * PL + so];
+#pragma unroll
+      for (int ci = 0; ci < NDOF; ++ci)
+        acc[ci] = fma(coef<NDIM, NDOF, T>(A, ld, d, ci, cj, n, m), uu, acc[ci]);
     }
   }
-  const int64_t k = n * NDOF + ci;
-  T out;
-  if (MODE == AM_Y) out = acc;
-  else if (MODE == AM_RES) out = b[k] - acc;
-  else out = u[k] + omega * dinv[k] * (b[k] - acc);
-  y[k] = out;
+#pragma unroll
+  for (int ci = 0; ci < NDOF; ++ci) {
+    const int64_t k = n * NDOF + ci;
+    T out;
+    if (MODE == AM_Y) out = acc[ci];
+    else if (MODE == AM_RES) out = b[k] - acc[ci];
+    else out = uc[ci * NP * PL] + omega * dinv[k] * (b[k] - acc[ci]);
+    y[k] = out;
+  }
 }
 
 template <typename T>
 void stencil_apply(const Grid& g, const T* A, const T* u, T* y, const T* b, const T* dinv,
                    double omega, int mode, cudaStream_t st) {
-  const unsigned blocks = (unsigned)cdiv(g.nnodes() * g.ndof, 256);
+  const int TY = std::min(g.nny, 256);
+  const int TX = std::max(1, std::min(g.nnx, 256 / TY));
+  const dim3 grid((unsigned)cdiv(g.nny, TY), (unsigned)cdiv(g.nnx, TX), (unsigned)g.nnz);
+  const size_t smem = sizeof(T) * g.ndof * (g.ndim == 3 ? 3 : 1) * (TX + 2) * (TY + 2);
   const int key = g.ndim * 10 + g.ndof;
-  const int pk = sizeof(T) == 8 ? PK_STENCIL_F64 : PK_STENCIL_F32;
-  prof_begin(pk, st);
 #define TG_SA(ND, NF)                                                                          \
-  if (mode == AM_Y) k_stencil_apply<ND, NF, T, AM_Y><<<blocks, 256, 0, st>>>(g, A, u, y, b, dinv, (T)omega); \
-  else if (mode == AM_RES) k_stencil_apply<ND, NF, T, AM_RES><<<blocks, 256, 0, st>>>(g, A, u, y, b, dinv, (T)omega); \
-  else k_stencil_apply<ND, NF, T, AM_JACOBI><<<blocks, 256, 0, st>>>(g, A, u, y, b, dinv, (T)omega);
+  if (mode == AM_Y) k_stencil_apply<ND, NF, T, AM_Y><<<grid, 256, smem, st>>>(g, TY, TX, A, u, y, b, dinv, (T)omega); \
+  else if (mode == AM_RES) k_stencil_apply<ND, NF, T, AM_RES><<<grid, 256, smem, st>>>(g, TY, TX, A, u, y, b, dinv, (T)omega); \
+  else k_stencil_apply<ND, NF, T, AM_JACOBI><<<grid, 256, smem, st>>>(g, TY, TX, A, u, y, b, dinv, (T)omega);
   switch (key) {
     case 33: TG_SA(3, 3) break;
     case 31: TG_SA(3, 1) break;
@@ -122,7 +150,6 @@ void stencil_apply(const Grid& g, const T* A, const T* u, T* y, const T* b, cons
     default: throw Error{EINVAL_, "unsupported (ndim, nnode_dof)"};
   }
 #undef TG_SA
-  prof_end(pk, st);
   TG_CHECK_LAUNCH();
 }
 template void stencil_apply<double>(const Grid&, const double*, const double*, double*,
@@ -697,25 +724,45 @@ void gj_inverse(double* D, int64_t n, int64_t ld, double* work, cudaStream_t st)
   TG_CHECK_LAUNCH();
 }
 
-// x = Dinv b (warp per row), fixed rows of Dinv hold identity and b is 0 there
+// x = Dinv b: a warp per (row, column chunk) writes a partial sum, a second
+// kernel adds the DA_CHUNKS partials of a row in fixed order (deterministic;
+// 8x the parallelism of a warp per row on the ~1200-row coarsest matrix).
+// Fixed rows of Dinv hold the identity and b is 0 there.
+constexpr int DA_CHUNKS = 8;
 template <typename T>
-__global__ void k_dense_apply(const double* __restrict__ Dinv, int64_t n, int64_t ld,
-                              const T* __restrict__ b, T* __restrict__ x) {
-  const int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+__global__ void __launch_bounds__(256) k_dense_partial(const double* __restrict__ Dinv, int64_t n,
+                                                      int64_t ld, const T* __restrict__ b,
+                                                      double* __restrict__ part) {
+  const int64_t row = blockIdx.x * 8 + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (row >= n) return;
+  const int64_t w = (n + DA_CHUNKS - 1) / DA_CHUNKS;
+  const int64_t j0 = blockIdx.y * w, j1 = min(n, j0 + w);
   double acc = 0.0;
-  for (int64_t j = lane; j < n; j += 32) acc += Dinv[row * ld + j] * (double)b[j];
+#pragma unroll 4
+  for (int64_t j = j0 + lane; j < j1; j += 32) acc = fma(Dinv[row * ld + j], (double)b[j], acc);
   acc = warp_sum(acc);
-  if (lane == 0) x[row] = (T)acc;
+  if (lane == 0) part[blockIdx.y * n + row] = acc;
+}
+template <typename T>
+__global__ void k_dense_sum(const double* __restrict__ part, int64_t n, T* __restrict__ x) {
+  const int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (row >= n) return;
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < DA_CHUNKS; ++k) s += part[k * n + row];
+  x[row] = (T)s;
 }
 
 template <typename T>
-void dense_apply(const double* Dinv, int64_t n, int64_t ld, const T* b, T* x, cudaStream_t st) {
-  k_dense_apply<T><<<(unsigned)cdiv(n * 32, 256), 256, 0, st>>>(Dinv, n, ld, b, x);
+void dense_apply(const double* Dinv, int64_t n, int64_t ld, const T* b, T* x, double* work,
+                 cudaStream_t st) {
+  k_dense_partial<T><<<dim3((unsigned)cdiv(n, 8), DA_CHUNKS), 256, 0, st>>>(Dinv, n, ld, b, work);
+  TG_CHECK_LAUNCH();
+  k_dense_sum<T><<<(unsigned)cdiv(n, 256), 256, 0, st>>>(work, n, x);
   TG_CHECK_LAUNCH();
 }
-template void dense_apply<double>(const double*, int64_t, int64_t, const double*, double*, cudaStream_t);
-template void dense_apply<float>(const double*, int64_t, int64_t, const float*, float*, cudaStream_t);
+template void dense_apply<double>(const double*, int64_t, int64_t, const double*, double*, double*, cudaStream_t);
+template void dense_apply<float>(const double*, int64_t, int64_t, const float*, float*, double*, cudaStream_t);
 
 }  // namespace tg

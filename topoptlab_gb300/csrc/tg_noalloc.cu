@@ -29,7 +29,7 @@ namespace {
 constexpr int64_t kMaxN = TG_NOALLOC_MAX_N;
 
 struct NoAllocScratch {
-  double S[kMaxN];                 // sqrt(-dc/dv) per design variable
+  double S[kMaxN];                 // x*sqrt(-dc/dv) per design variable
   double part[tg::RED_BLOCKS];     // per-block partial sums
   tg::OCState state;               // bisection interval, carry, step count
 };
@@ -80,14 +80,18 @@ int32_t tg_oc_noalloc(int64_t n, const double* x, const double* dc, const double
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   try {
     tg::OCState h{};
-    tg::oc_begin(n, dc, dv, s->S, &s->state, g, st, l1, l2);
+    // one scratch array: the move-limit bounds are recomputed from x each step
+    const tg::OCScratch ocs{s->S, nullptr, nullptr};
+    tg::oc_begin(n, x, dc, dv, el_flags, move, ocs, &s->state, g, st, l1, l2);
     for (int k = 0; k < 16; ++k) {
-      tg::oc_steps(n, x, s->S, dv, el_flags, move, xnew, s->part, &s->state, 16, st);
+      tg::oc_steps(n, x, ocs, dv, el_flags, move, s->part, &s->state, 16, st);
       TG_CUDA(cudaMemcpyAsync(&h, &s->state, sizeof(tg::OCState), cudaMemcpyDeviceToHost, st));
       TG_CUDA(cudaStreamSynchronize(st));
       if (h.done) break;
     }
     if (!h.done) return fail(TG_ENOTCONV, "tg_oc_noalloc: OC bisection did not terminate");
+    tg::oc_finish(n, x, ocs, el_flags, move, xnew, &s->state, st);
+    TG_CUDA(cudaStreamSynchronize(st));
     if (gt) *gt = h.gt;
     if (nsteps) *nsteps = h.nsteps;
     return TG_OK;

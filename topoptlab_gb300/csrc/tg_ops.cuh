@@ -94,7 +94,8 @@ void stencil_to_dense(const Grid& g, const uint8_t* fix, const double* A, double
                       int64_t ld, cudaStream_t st);
 void gj_inverse(double* D, int64_t n, int64_t ld, double* work, cudaStream_t st);
 template <typename T>
-void dense_apply(const double* Dinv, int64_t n, int64_t ld, const T* b, T* x, cudaStream_t st);
+void dense_apply(const double* Dinv, int64_t n, int64_t ld, const T* b, T* x,
+                 double* work /* >= 8*n */, cudaStream_t st);
 
 // ---------------------------------------------------------------------------
 // design-variable kernels
@@ -103,6 +104,7 @@ struct FilterStencil {
   int R;                 // half width
   int nw;                // (2R+1)^ndim
   const double* w;       // [nw] weights, dz slowest, dx, dy fastest
+  double* tmp;           // nel scratch for mode 1 (null: divide inside the stencil loop)
 };
 // mode 0: y = (H x) / Hs ; mode 1: y = H (x / Hs) ; mode 2: y = H(x*d)/Hs/max(1e-3, x)
 // mode 3: Hs = H 1 (x unused) ; mode 4: y = x (copy, used with the fused reductions)

@@ -48,8 +48,47 @@ void drain_locked() {
 
 int prof_kind() { return g_kind; }
 
+namespace {
+thread_local ProfCapture* g_cap = nullptr;
+}
+
+void ProfCapture::release() {
+  for (auto& pr : pairs) {
+    cudaEventDestroy(pr.first);
+    cudaEventDestroy(pr.second);
+  }
+  pairs.clear();
+  if (open) cudaEventDestroy(open);
+  open = nullptr;
+}
+
+void prof_capture_begin(ProfCapture* pc) {
+  pc->release();
+  pc->kind = g_kind;
+  g_cap = pc;
+}
+void prof_capture_end() { g_cap = nullptr; }
+
+void prof_collect(const ProfCapture& pc) {
+  if (pc.kind != g_kind || pc.kind == PK_NONE) return;
+  std::lock_guard<std::mutex> lk(g_mu);
+  for (const auto& pr : pc.pairs) {
+    float ms = 0.f;
+    TG_CUDA(cudaEventElapsedTime(&ms, pr.first, pr.second));
+    g_ms += ms;
+    g_count += 1;
+  }
+}
+
 void prof_begin(int kind, cudaStream_t st) {
   if (kind != g_kind || kind == PK_NONE) return;
+  if (g_cap) {
+    // external record: becomes an event node of the graph (a plain record
+    // during capture only expresses a dependency)
+    TG_CUDA(cudaEventCreate(&g_cap->open));
+    TG_CUDA(cudaEventRecordWithFlags(g_cap->open, st, cudaEventRecordExternal));
+    return;
+  }
   std::lock_guard<std::mutex> lk(g_mu);
   if (g_used >= 4096 && g_open == 0) drain_locked();
   TG_CUDA(cudaEventRecord(next_event(), st));
@@ -58,6 +97,14 @@ void prof_begin(int kind, cudaStream_t st) {
 
 void prof_end(int kind, cudaStream_t st) {
   if (kind != g_kind || kind == PK_NONE) return;
+  if (g_cap) {
+    cudaEvent_t e;
+    TG_CUDA(cudaEventCreate(&e));
+    TG_CUDA(cudaEventRecordWithFlags(e, st, cudaEventRecordExternal));
+    g_cap->pairs.emplace_back(g_cap->open, e);
+    g_cap->open = nullptr;
+    return;
+  }
   std::lock_guard<std::mutex> lk(g_mu);
   TG_CUDA(cudaEventRecord(next_event(), st));
   g_open = 0;
