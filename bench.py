@@ -253,7 +253,7 @@ def run_ours(args, dist, rank, ws, local):
     families = {}
     tms = C.c_double()
     step_ms = []
-    for kind, name in FAMILIES:
+    for kind, name in ([] if args.no_breakdown else FAMILIES):
         fms, fcount = C.c_double(), C.c_int64()
         lib.tg_profile_kernel(kind)
         lib.tg_timer(prob._h, 0, None)
@@ -267,7 +267,7 @@ def run_ours(args, dist, rank, ws, local):
                            "(event nodes inside the captured PCG-iteration graphs), one design "
                            "iteration per family; learned_warm_start includes its own FP32 K.u "
                            "launches (also in fine_f32_kmul)",
-                 "step_ms_profiled": round(float(np.mean(step_ms)), 3),
+                 "step_ms_profiled": round(float(np.mean(step_ms)), 3) if step_ms else None,
                  "families": families}
 
     # ---------------- end to end through the public API, host buffers ----------------
@@ -476,6 +476,8 @@ def main():
     ap.add_argument("--train-epochs", type=int, default=10)
     ap.add_argument("--no-plain", action="store_true",
                     help="skip the plain FP64 arm (profiling runs only)")
+    ap.add_argument("--no-breakdown", action="store_true",
+                    help="skip the per-family time breakdown (profiling runs only)")
     ap.add_argument("--size", default=None,
                     help="override the grid, e.g. 80,40,40 (profiling runs only)")
     args = ap.parse_args()

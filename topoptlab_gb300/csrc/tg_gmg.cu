@@ -61,20 +61,25 @@ __device__ __forceinline__ T coef(const T* __restrict__ A, int64_t ld, int d, in
                 : __ldg(A + (((C - d) * NDOF + cj) * NDOF + ci) * ld + m);
 }
 
-// One thread per node (all NDOF rows), one CTA per (TY x TX) patch of a node
-// plane.  TY spans whole y-rows where the grid allows, so consecutive threads
-// own consecutive nodes and every coefficient load of a warp is contiguous.
-// The u values of the patch and its one-node halo in the planes z-1, z, z+1
-// are staged in shared memory, component-major (stride-1 reads across a
-// warp), with zeros outside the grid.  A lower-direction block is read at the
-// neighbour; outside the grid the node's own (finite) block is read instead
-// and meets a zero u, so the loads need no branches.
+// One CTA per (TY x TX) patch of a node plane, NDOF x 256 threads: thread
+// (ci, node) computes row ci of its node (81 coefficient loads in 3-D
+// elasticity), so there are NDOF times more warps in flight than with a
+// thread per node and fewer registers each -- the level-1 sweep is bound by
+// the latency of its coefficient loads, not by their bandwidth.  TY spans
+// whole y-rows where the grid allows, so consecutive threads own consecutive
+// nodes and every coefficient load of a warp is contiguous.  The u values of
+// the patch and its one-node halo in the planes z-1, z, z+1 are staged in
+// shared memory, component-major (stride-1 reads across a warp), with zeros
+// outside the grid.  A lower-direction block is read at the neighbour;
+// outside the grid the node's own (finite) block is read instead and meets a
+// zero u, so the loads need no branches.
 template <int NDIM, int NDOF, typename T, int MODE>
-__global__ void __launch_bounds__(256) k_stencil_apply(Grid g, int TY, int TX,
-                                                      const T* __restrict__ A,
-                                                      const T* __restrict__ u, T* __restrict__ y,
-                                                      const T* __restrict__ b,
-                                                      const T* __restrict__ dinv, T omega) {
+__global__ void __launch_bounds__(NDOF * 256) k_stencil_apply(Grid g, int TY, int TX,
+                                                             const T* __restrict__ A,
+                                                             const T* __restrict__ u,
+                                                             T* __restrict__ y,
+                                                             const T* __restrict__ b,
+                                                             const T* __restrict__ dinv, T omega) {
   constexpr int NP = (NDIM == 3) ? 3 : 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* us = reinterpret_cast<T*>(smem_raw);
@@ -92,7 +97,8 @@ __global__ void __launch_bounds__(256) k_stencil_apply(Grid g, int TY, int TX,
     us[(c * NP + pz) * PL + hx * RY + hy] = v;
   }
   __syncthreads();
-  const int ty = tid % TY, tx = tid / TY;
+  const int ci = tid >> 8, tn = tid & 255;      // row (warp-uniform), node of the patch
+  const int ty = tn % TY, tx = tn / TY;
   const int xx = x0 + tx, yy = y0 + ty;
   if (tx >= TX || xx >= g.nnx || yy >= g.nny) return;
   const int64_t n = g.node(xx, yy, z);
@@ -101,9 +107,7 @@ __global__ void __launch_bounds__(256) k_stencil_apply(Grid g, int TY, int TX,
                          {z > 0, true, z + 1 < g.nnz}};
   const int64_t sx = g.nny, sz = (int64_t)g.nny * g.nnx;
   const T* uc = us + ((NDIM == 3) ? PL : 0) + (tx + 1) * RY + (ty + 1);   // centre, plane z
-  T acc[NDOF];
-#pragma unroll
-  for (int ci = 0; ci < NDOF; ++ci) acc[ci] = T(0);
+  T acc = T(0);
 #pragma unroll
   for (int d = 0; d < ndir<NDIM>(); ++d) {
     int dx, dy, dz;
@@ -112,22 +116,15 @@ __global__ void __launch_bounds__(256) k_stencil_apply(Grid g, int TY, int TX,
     const int64_t m = v ? n + dz * sz + dx * sx + dy : n;
     const int so = dz * PL + dx * RY + dy;
 #pragma unroll
-    for (int cj = 0; cj < NDOF; ++cj) {
-      const T uu = uc[cj * NP * PL + so];
-#pragma unroll
-      for (int ci = 0; ci < NDOF; ++ci)
-        acc[ci] = fma(coef<NDIM, NDOF, T>(A, ld, d, ci, cj, n, m), uu, acc[ci]);
-    }
+    for (int cj = 0; cj < NDOF; ++cj)
+      acc = fma(coef<NDIM, NDOF, T>(A, ld, d, ci, cj, n, m), uc[cj * NP * PL + so], acc);
   }
-#pragma unroll
-  for (int ci = 0; ci < NDOF; ++ci) {
-    const int64_t k = n * NDOF + ci;
-    T out;
-    if (MODE == AM_Y) out = acc[ci];
-    else if (MODE == AM_RES) out = b[k] - acc[ci];
-    else out = uc[ci * NP * PL] + omega * dinv[k] * (b[k] - acc[ci]);
-    y[k] = out;
-  }
+  const int64_t k = n * NDOF + ci;
+  T out;
+  if (MODE == AM_Y) out = acc;
+  else if (MODE == AM_RES) out = b[k] - acc;
+  else out = uc[ci * NP * PL] + omega * dinv[k] * (b[k] - acc);
+  y[k] = out;
 }
 
 template <typename T>
@@ -137,11 +134,12 @@ void stencil_apply(const Grid& g, const T* A, const T* u, T* y, const T* b, cons
   const int TX = std::max(1, std::min(g.nnx, 256 / TY));
   const dim3 grid((unsigned)cdiv(g.nny, TY), (unsigned)cdiv(g.nnx, TX), (unsigned)g.nnz);
   const size_t smem = sizeof(T) * g.ndof * (g.ndim == 3 ? 3 : 1) * (TX + 2) * (TY + 2);
+  const unsigned nt = 256u * (unsigned)g.ndof;
   const int key = g.ndim * 10 + g.ndof;
 #define TG_SA(ND, NF)                                                                          \
-  if (mode == AM_Y) k_stencil_apply<ND, NF, T, AM_Y><<<grid, 256, smem, st>>>(g, TY, TX, A, u, y, b, dinv, (T)omega); \
-  else if (mode == AM_RES) k_stencil_apply<ND, NF, T, AM_RES><<<grid, 256, smem, st>>>(g, TY, TX, A, u, y, b, dinv, (T)omega); \
-  else k_stencil_apply<ND, NF, T, AM_JACOBI><<<grid, 256, smem, st>>>(g, TY, TX, A, u, y, b, dinv, (T)omega);
+  if (mode == AM_Y) k_stencil_apply<ND, NF, T, AM_Y><<<grid, nt, smem, st>>>(g, TY, TX, A, u, y, b, dinv, (T)omega); \
+  else if (mode == AM_RES) k_stencil_apply<ND, NF, T, AM_RES><<<grid, nt, smem, st>>>(g, TY, TX, A, u, y, b, dinv, (T)omega); \
+  else k_stencil_apply<ND, NF, T, AM_JACOBI><<<grid, nt, smem, st>>>(g, TY, TX, A, u, y, b, dinv, (T)omega);
   switch (key) {
     case 33: TG_SA(3, 3) break;
     case 31: TG_SA(3, 1) break;
