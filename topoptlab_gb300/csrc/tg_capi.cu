@@ -45,16 +45,46 @@ void d2h(T* dst, const T* src, int64_t n, cudaStream_t st) {
   TG_CUDA(cudaStreamSynchronize(st));
 }
 
-double* field_ptr(tg::Ctx& c, int32_t field, int64_t& n) {
+// device array of a field; n = its length in the caller's numbering
+double* field_ptr(tg::Ctx& c, int32_t field, int64_t& n, bool& nodes) {
+  nodes = field == TG_FIELD_U || field == TG_FIELD_F;
+  n = nodes ? c.rg.ndofs() : c.rg.nel();
   switch (field) {
-    case TG_FIELD_X: n = c.g.nel(); return c.x;
-    case TG_FIELD_XPHYS: n = c.g.nel(); return c.xPhys;
-    case TG_FIELD_U: n = c.g.ndofs(); return c.u;
-    case TG_FIELD_DC: n = c.g.nel(); return c.dcf;
-    case TG_FIELD_DV: n = c.g.nel(); return c.dv;
-    case TG_FIELD_F: n = c.g.ndofs(); return c.f;
+    case TG_FIELD_X: return c.x;
+    case TG_FIELD_XPHYS: return c.xPhys;
+    case TG_FIELD_U: return c.u;
+    case TG_FIELD_DC: return c.dcf;
+    case TG_FIELD_DV: return c.dv;
+    case TG_FIELD_F: return c.f;
     default: throw tg::Error{TG_EINVAL, "unknown field"};
   }
+}
+
+// host (caller numbering) -> device array (device numbering), and back; on a
+// padded grid through the staging buffer and the embedding kernel (the
+// padding entries of dst keep their values)
+void put_field(tg::Ctx& c, double* dev, const double* host, bool nodes) {
+  const int64_t n = nodes ? c.rg.ndofs() : c.rg.nel();
+  if (!c.padded) {
+    h2d(dev, host, n, c.st);
+    return;
+  }
+  h2d(c.emb.p, host, n, c.st);
+  tg::embed_copy(c.rg, c.g, nodes, c.emb, dev, true, c.st);
+}
+void get_field(tg::Ctx& c, double* host, const double* dev, bool nodes) {
+  const int64_t n = nodes ? c.rg.ndofs() : c.rg.nel();
+  if (!c.padded) {
+    d2h(host, dev, n, c.st);
+    return;
+  }
+  tg::embed_copy(c.rg, c.g, nodes, dev, c.emb, false, c.st);
+  d2h(host, c.emb.p, n, c.st);
+}
+void require_unpadded(const tg::Ctx& c, const char* what) {
+  if (c.padded)
+    throw tg::Error{TG_EINVAL, std::string(what) + ": not available for a grid embedded in a "
+                               "padded device grid (its element counts do not coarsen)"};
 }
 }  // namespace
 
@@ -105,9 +135,10 @@ int32_t tg_get(tg_ctx* ctx, int32_t field, double* host, int64_t n) {
   if (!ctx || !host) return TG_EINVAL;
   return guarded(ctx, [&] {
     int64_t m = 0;
-    double* p = field_ptr(ctx->c, field, m);
+    bool nodes = false;
+    double* p = field_ptr(ctx->c, field, m, nodes);
     TG_REQUIRE(n == m, "tg_get: wrong element count");
-    d2h(host, p, n, ctx->c.st);
+    get_field(ctx->c, host, p, nodes);
   });
 }
 
@@ -116,9 +147,10 @@ int32_t tg_set(tg_ctx* ctx, int32_t field, const double* host, int64_t n) {
   return guarded(ctx, [&] {
     tg::Ctx& c = ctx->c;
     int64_t m = 0;
-    double* p = field_ptr(c, field, m);
+    bool nodes = false;
+    double* p = field_ptr(c, field, m, nodes);
     TG_REQUIRE(n == m, "tg_set: wrong element count");
-    h2d(p, host, n, c.st);
+    put_field(c, p, host, nodes);
     if (field == TG_FIELD_F || field == TG_FIELD_U)
       tg::mask_vec_f64(c.g.nnodes(), c.g.ndof, c.op.fix, p, c.st);
     TG_CUDA(cudaStreamSynchronize(c.st));
@@ -129,6 +161,7 @@ int32_t tg_kmul(tg_ctx* ctx, const double* xPhys, const double* u, double* y, in
   if (!ctx || !xPhys || !u || !y) return TG_EINVAL;
   return guarded(ctx, [&] {
     tg::Ctx& c = ctx->c;
+    require_unpadded(c, "tg_kmul");
     const int64_t nel = c.g.nel(), nd = c.g.ndofs();
     h2d(c.xnew.p, xPhys, nel, c.st);
     h2d(c.r.p, u, nd, c.st);
@@ -155,14 +188,16 @@ int32_t tg_solve(tg_ctx* ctx, const double* xPhys, const double* rhs, const doub
   if (!ctx || !xPhys || !rhs || !u) return TG_EINVAL;
   tg::Ctx& c = ctx->c;
   const int32_t rc = guarded(ctx, [&] {
-    const int64_t nel = c.g.nel(), nd = c.g.ndofs();
-    h2d(c.xnew.p, xPhys, nel, c.st);
+    const int64_t nd = c.g.ndofs();
+    TG_CUDA(cudaMemsetAsync(c.xnew.p, 0, sizeof(double) * c.g.nel(), c.st));
+    TG_CUDA(cudaMemsetAsync(c.z.p, 0, sizeof(double) * nd, c.st));
+    TG_CUDA(cudaMemsetAsync(c.p.p, 0, sizeof(double) * nd, c.st));
+    put_field(c, c.xnew.p, xPhys, false);
     tg::set_density(c, c.xnew);
     tg::build_hierarchy(c);
-    h2d(c.z.p, rhs, nd, c.st);
+    put_field(c, c.z.p, rhs, true);
     tg::mask_vec_f64(c.g.nnodes(), c.g.ndof, c.op.fix, c.z, c.st);
-    if (u0) h2d(c.p.p, u0, nd, c.st);
-    else TG_CUDA(cudaMemsetAsync(c.p.p, 0, sizeof(double) * nd, c.st));
+    if (u0) put_field(c, c.p.p, u0, true);
     // solve() uses r, q and the level buffers; rhs lives in z, the iterate in a
     // dedicated copy so the PCG vectors stay free
     std::vector<double> host(nd);
@@ -172,7 +207,7 @@ int32_t tg_solve(tg_ctx* ctx, const double* xPhys, const double* rhs, const doub
     TG_CUDA(cudaMemcpyAsync(b.p, c.z.p, sizeof(double) * nd, cudaMemcpyDeviceToDevice, c.st));
     TG_CUDA(cudaMemcpyAsync(x.p, c.p.p, sizeof(double) * nd, cudaMemcpyDeviceToDevice, c.st));
     tg::solve(c, b, x);
-    d2h(u, x.p, nd, c.st);
+    get_field(c, u, x.p, true);
   });
   if (info) {
     info->iters = c.last_iters;
@@ -188,6 +223,7 @@ int32_t tg_filter(tg_ctx* ctx, const double* x, const double* d, double* y, int3
   if (!ctx || !y || mode < 0 || mode > 3 || (mode != 3 && !x) || (mode == 2 && !d)) return TG_EINVAL;
   return guarded(ctx, [&] {
     tg::Ctx& c = ctx->c;
+    require_unpadded(c, "tg_filter");
     const int64_t nel = c.g.nel();
     if (x) h2d(c.xnew.p, x, nel, c.st);
     if (d) h2d(c.S.p, d, nel, c.st);
@@ -200,6 +236,7 @@ int32_t tg_compliance(tg_ctx* ctx, const double* xPhys, const double* u, double*
   if (!ctx || !xPhys || !u || !obj) return TG_EINVAL;
   return guarded(ctx, [&] {
     tg::Ctx& c = ctx->c;
+    require_unpadded(c, "tg_compliance");
     const int64_t nel = c.g.nel(), nd = c.g.ndofs();
     h2d(c.xnew.p, xPhys, nel, c.st);
     h2d(c.r.p, u, nd, c.st);
@@ -215,6 +252,7 @@ int32_t tg_oc(tg_ctx* ctx, const double* x, const double* dc, const double* dv, 
   if (!ctx || !x || !dc || !dv || !xnew) return TG_EINVAL;
   return guarded(ctx, [&] {
     tg::Ctx& c = ctx->c;
+    require_unpadded(c, "tg_oc");
     const int64_t nel = c.g.nel();
     tg::DevBuf<double> xd, dcd, dvd, xn;
     xd.alloc(nel); dcd.alloc(nel); dvd.alloc(nel); xn.alloc(nel);
@@ -276,6 +314,7 @@ int32_t tg_vcycle(tg_ctx* ctx, const double* xPhys, const double* b, double* x, 
   return guarded(ctx, [&] {
     tg::Ctx& c = ctx->c;
     TG_REQUIRE(c.precond == TG_PRECOND_GMG, "tg_vcycle needs a multigrid context");
+    require_unpadded(c, "tg_vcycle");
     const int64_t nel = c.g.nel(), nd = c.g.ndofs();
     h2d(c.xnew.p, xPhys, nel, c.st);
     tg::set_density(c, c.xnew);
@@ -310,6 +349,7 @@ int32_t tg_coarse_stencil(tg_ctx* ctx, const double* xPhys, int32_t level, doubl
   return guarded(ctx, [&] {
     tg::Ctx& c = ctx->c;
     TG_REQUIRE(c.precond == TG_PRECOND_GMG, "no multigrid hierarchy");
+    require_unpadded(c, "tg_coarse_stencil");
     TG_REQUIRE(level >= 1 && level < c.L, "level out of range");
     tg::Level& v = *c.lv[level];
     TG_REQUIRE(n == v.g.nnodes() * (v.g.ndim == 3 ? 27 : 9) * v.g.ndof * v.g.ndof,

@@ -136,6 +136,36 @@ static void setup_element(Ctx& c, const double* KEref) {
   c.op.KE32 = c.KE32.p;
 }
 
+static int choose_levels(const Grid& g, int requested);
+static int choose_levels_nat(const Grid& g) { return choose_levels(g, 0); }
+
+static Grid coarsest_of(const Grid& g, int L) {
+  Grid c = g;
+  for (int l = 1; l < L; ++l) c = coarsen(c);
+  return c;
+}
+
+// Grids whose element counts do not halve down to a small coarsest level
+// (odd counts, e.g. a 65x65 heat plate) are embedded in the smallest grid
+// with counts that are multiples of 2^k whose k-times coarsened grid has at
+// most 1200 DOFs.  The padding layers sit at the high end of each axis:
+// padding elements have zero stiffness (flag EL_OUTSIDE) and padding nodes
+// are fixed, so the caller's nodes see exactly the caller's operator; the
+// filter, volume, compliance and OC skip padding elements.
+static Grid embedding_grid(const Grid& rg, int requested_levels) {
+  if (requested_levels > 0) return rg;
+  if (coarsest_of(rg, choose_levels_nat(rg)).ndofs() <= 1200) return rg;
+  for (int k = 1; k <= 12; ++k) {
+    const int m = 1 << k;
+    auto up = [m](int v) { return ((v + m - 1) / m) * m; };
+    const Grid gp = make_grid(rg.ndim, rg.ndof, up(rg.nex), up(rg.ney), rg.ndim == 3 ? up(rg.nez) : 1);
+    Grid c = gp;
+    for (int l = 0; l < k; ++l) c = coarsen(c);
+    if (c.ndofs() <= 1200) return gp;
+  }
+  return rg;
+}
+
 static int choose_levels(const Grid& g, int requested) {
   int L = 1;
   Grid cur = g;
@@ -166,7 +196,9 @@ void ctx_init(Ctx& c, const tg_problem& p) {
   TG_CUDA(cudaEventCreate(&c.ev1));
   TG_CUDA(cudaEventCreate(&c.tev0));
   TG_CUDA(cudaEventCreate(&c.tev1));
-  c.g = make_grid(p.ndim, p.nnode_dof, p.nelx, p.nely, p.nelz);
+  c.rg = make_grid(p.ndim, p.nnode_dof, p.nelx, p.nely, p.nelz);
+  c.g = (p.precond == TG_PRECOND_GMG) ? embedding_grid(c.rg, p.nlevels) : c.rg;
+  c.padded = c.g.nex != c.rg.nex || c.g.ney != c.rg.ney || c.g.nez != c.rg.nez;
   c.volfrac = p.volfrac; c.rmin = p.rmin; c.eps = p.eps; c.penal = p.penal;
   c.move = p.move > 0 ? p.move : 0.2;
   c.ft = p.ft; c.precond = p.precond; c.precision = p.precision;
@@ -181,12 +213,27 @@ void ctx_init(Ctx& c, const tg_problem& p) {
   c.op.g = g;
   setup_element(c, p.KE);
 
-  // fixed-DOF bits per node, and per element "touches a fixed DOF"
+  // fixed-DOF bits per node (caller's DOF numbers mapped to the device grid;
+  // padding nodes fully fixed), and per element "touches a fixed DOF"
+  const Grid& rg = c.rg;
+  const int64_t rnd = rg.ndofs(), rnel = rg.nel();
+  auto dev_node = [&](int64_t rn) {
+    const int y = (int)(rn % rg.nny), x = (int)((rn / rg.nny) % rg.nnx);
+    const int z = (int)(rn / ((int64_t)rg.nny * rg.nnx));
+    return g.node(x, y, z);
+  };
   std::vector<uint8_t> fix(nn, 0);
+  if (c.padded) {
+    const uint8_t all = (uint8_t)((1u << g.ndof) - 1u);
+    for (int z = 0; z < g.nnz; ++z)
+      for (int x = 0; x < g.nnx; ++x)
+        for (int y = 0; y < g.nny; ++y)
+          if (x >= rg.nnx || y >= rg.nny || z >= rg.nnz) fix[g.node(x, y, z)] = all;
+  }
   for (int64_t i = 0; i < p.nfixed; ++i) {
     const int64_t d = p.fixed[i];
-    TG_REQUIRE(d >= 0 && d < nd, "fixed DOF index out of range");
-    fix[d / g.ndof] |= (uint8_t)(1u << (d % g.ndof));
+    TG_REQUIRE(d >= 0 && d < rnd, "fixed DOF index out of range");
+    fix[dev_node(d / g.ndof)] |= (uint8_t)(1u << (d % g.ndof));
   }
   std::vector<uint8_t> touch(nel, 0);
   for (int ez = 0; ez < g.nez; ++ez)
@@ -249,10 +296,16 @@ void ctx_init(Ctx& c, const tg_problem& p) {
   c.op.fix = c.lv[0]->fix.p;
   c.touch.alloc(nel);
   TG_CUDA(cudaMemcpy(c.touch.p, touch.data(), nel, cudaMemcpyHostToDevice));
-  if (p.el_flags) {
+  if (p.el_flags || c.padded) {
+    std::vector<int8_t> fl(nel, EL_OUTSIDE);
+    for (int ez = 0; ez < rg.nez; ++ez)
+      for (int ex = 0; ex < rg.nex; ++ex)
+        for (int ey = 0; ey < rg.ney; ++ey)
+          fl[g.elem(ex, ey, ez)] = p.el_flags ? p.el_flags[rg.elem(ex, ey, ez)] : 0;
     c.flags.alloc(nel);
-    TG_CUDA(cudaMemcpy(c.flags.p, p.el_flags, nel, cudaMemcpyHostToDevice));
+    TG_CUDA(cudaMemcpy(c.flags.p, fl.data(), nel, cudaMemcpyHostToDevice));
   }
+  if (c.padded) c.emb.alloc(std::max(rnd, rnel));
   // vectors
   c.f.alloc(nd); c.u.alloc(nd);
   c.x.alloc(nel); c.xPhys.alloc(nel); c.xold.alloc(nel); c.xnew.alloc(nel);
@@ -269,7 +322,8 @@ void ctx_init(Ctx& c, const tg_problem& p) {
   TG_CUDA(cudaMallocHost(&c.h_scal, 8 * sizeof(double)));
 
   // load (masked to the free DOFs) and its norm
-  std::vector<double> fh(p.f, p.f + nd);
+  std::vector<double> fh(nd, 0.0);
+  for (int64_t i = 0; i < rnd; ++i) fh[dev_node(i / g.ndof) * g.ndof + i % g.ndof] = p.f[i];
   double bb = 0.0;
   for (int64_t i = 0; i < nd; ++i) {
     if ((fix[i / g.ndof] >> (i % g.ndof)) & 1) fh[i] = 0.0;
@@ -291,15 +345,22 @@ void ctx_init(Ctx& c, const tg_problem& p) {
   c.fw.alloc(nw);
   TG_CUDA(cudaMemcpy(c.fw.p, w.data(), sizeof(double) * nw, cudaMemcpyHostToDevice));
   c.fs.R = R; c.fs.nw = nw; c.fs.w = c.fw.p;
+  c.fs.rex = rg.nex; c.fs.rey = rg.ney; c.fs.rez = rg.nez;
   c.fs.tmp = c.S.p + nel;   // OC scratch, idle while a filter runs
   filter_apply(g, c.fs, nullptr, nullptr, nullptr, c.Hs, 3, c.st);
   // dv: ones, filtered once for the density filter (topology_optimization.py:520, :558)
-  std::vector<double> ones(nel, 1.0);
+  std::vector<double> ones(nel, 0.0);
+  for (int ez = 0; ez < rg.nez; ++ez)
+    for (int ex = 0; ex < rg.nex; ++ex)
+      for (int ey = 0; ey < rg.ney; ++ey) ones[g.elem(ex, ey, ez)] = 1.0;
   TG_CUDA(cudaMemcpy(c.xnew.p, ones.data(), sizeof(double) * nel, cudaMemcpyHostToDevice));
   if (c.ft == 1) filter_apply(g, c.fs, c.xnew, nullptr, c.Hs, c.dv, 1, c.st);
   else TG_CUDA(cudaMemcpyAsync(c.dv.p, c.xnew.p, sizeof(double) * nel, cudaMemcpyDeviceToDevice, c.st));
   // initial design x = xPhys = volfrac (topology_optimization.py:216-219)
-  std::vector<double> x0(nel, c.volfrac);
+  std::vector<double> x0(nel, 0.0);
+  for (int ez = 0; ez < rg.nez; ++ez)
+    for (int ex = 0; ex < rg.nex; ++ex)
+      for (int ey = 0; ey < rg.ney; ++ey) x0[g.elem(ex, ey, ez)] = c.volfrac;
   TG_CUDA(cudaMemcpy(c.x.p, x0.data(), sizeof(double) * nel, cudaMemcpyHostToDevice));
   TG_CUDA(cudaMemcpy(c.xPhys.p, x0.data(), sizeof(double) * nel, cudaMemcpyHostToDevice));
   c.g_oc = 0.0;
@@ -311,7 +372,7 @@ void ctx_init(Ctx& c, const tg_problem& p) {
 // ---------------------------------------------------------------------------
 void set_density(Ctx& c, const double* xPhys) {
   ProfScope ps(PK_COARSE_BUILD, c.st);
-  simp_scale(c.g.nel(), xPhys, c.eps, c.penal, c.s64, c.s32.p, c.s16.p, c.st);
+  simp_scale(c.g.nel(), xPhys, c.eps, c.penal, c.s64, c.s32.p, c.s16.p, c.st, c.flags.p);
 }
 
 void build_hierarchy(Ctx& c) {
@@ -652,7 +713,7 @@ void ctx_step(Ctx& c, tg_iter_out& out) {
   const int nbe = (int)red_blocks(nel);
   {
     ProfScope ps(PK_COMPLIANCE, c.st);
-    fine_compliance(c.op, c.xPhys, c.u, c.eps, c.penal, c.dc, c.part, c.st);
+    fine_compliance(c.op, c.xPhys, c.u, c.eps, c.penal, c.dc, c.part, c.st, c.flags.p);
     reduce_partials(c.part, nbe, c.scal.p + 0, false, c.st);
   }
   // sensitivity filter
@@ -686,7 +747,7 @@ void ctx_step(Ctx& c, tg_iter_out& out) {
   float ms = 0.f;
   TG_CUDA(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
   out.obj = c.h_scal[0];
-  out.vol = vol_sum / (double)nel;
+  out.vol = vol_sum / (double)c.rg.nel();   // padding elements hold 0
   out.change = c.h_scal[2];
   out.g = c.g_oc;
   out.rel_res = c.last_relres;

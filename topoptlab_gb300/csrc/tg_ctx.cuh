@@ -48,7 +48,10 @@ struct Ctx {
   cudaStream_t st = nullptr;
   std::string err;
   // problem
-  Grid g;                       // fine grid (element counts in nex/ney/nez)
+  Grid g;                       // fine grid on the device (element counts in nex/ney/nez)
+  Grid rg;                      // the caller's grid; g == rg unless padded
+  bool padded = false;          // g has padding layers at the high end of each axis
+  DevBuf<double> emb;           // caller-numbered staging buffer (padded grids)
   int ne = 0;                   // element matrix dim
   double volfrac = 0.5, rmin = 1.5, eps = 1e-9, penal = 3.0, move = 0.2;
   int ft = 1;

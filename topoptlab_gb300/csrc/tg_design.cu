@@ -17,7 +17,8 @@ namespace tg {
 // filter: weights max(0, rmin - |d|) over |d_i| <= R; H is never formed
 // ---------------------------------------------------------------------------
 template <int NDIM, int MODE>
-__global__ void __launch_bounds__(RED_THREADS) k_filter(Grid g, int R, const double* __restrict__ w,
+__global__ void __launch_bounds__(RED_THREADS) k_filter(Grid g, int R, int rex, int rey, int rez,
+                                                       const double* __restrict__ w,
                                                        const double* __restrict__ x,
                                                        const double* __restrict__ d,
                                                        const double* __restrict__ Hs,
@@ -33,17 +34,21 @@ __global__ void __launch_bounds__(RED_THREADS) k_filter(Grid g, int R, const dou
     const int ey = (int)(e % g.ney);
     const int ex = (int)((e / g.ney) % g.nex);
     const int ez = (int)(e / ((int64_t)g.ney * g.nex));
+    if (ex >= rex || ey >= rey || ez >= rez) {   // padding element
+      y[e] = 0.0;
+      continue;
+    }
     double acc = 0.0;
     const int zlo = (NDIM == 3) ? -R : 0, zhi = (NDIM == 3) ? R : 0;
     for (int oz = zlo; oz <= zhi && MODE != 4; ++oz) {
       const int nz = ez + oz;
-      if (nz < 0 || nz >= g.nez) continue;
+      if (nz < 0 || nz >= rez) continue;
       for (int ox = -R; ox <= R; ++ox) {
         const int nx = ex + ox;
-        if (nx < 0 || nx >= g.nex) continue;
+        if (nx < 0 || nx >= rex) continue;
         for (int oy = -R; oy <= R; ++oy) {
           const int ny = ey + oy;
-          if (ny < 0 || ny >= g.ney) continue;
+          if (ny < 0 || ny >= rey) continue;
           const double wt = w[((NDIM == 3 ? (oz + R) * W : 0) + (ox + R)) * W + (oy + R)];
           if (wt == 0.0) continue;          // uniform over the block: taps beyond rmin
           const int64_t nb = g.elem(nx, ny, nz);
@@ -93,7 +98,7 @@ void filter_apply_ex(const Grid& g, const FilterStencil& fs, const double* x, co
     x = fs.tmp;
     mode = 5;
   }
-#define TG_F(ND, M) k_filter<ND, M><<<blocks, RED_THREADS, 0, st>>>(g, fs.R, fs.w, x, d, Hs, y, xold, part_sum, part_max)
+#define TG_F(ND, M) k_filter<ND, M><<<blocks, RED_THREADS, 0, st>>>(g, fs.R, fs.rex, fs.rey, fs.rez, fs.w, x, d, Hs, y, xold, part_sum, part_max)
   if (g.ndim == 3) {
     if (mode == 0) TG_F(3, 0); else if (mode == 1) TG_F(3, 1); else if (mode == 2) TG_F(3, 2);
     else if (mode == 3) TG_F(3, 3); else if (mode == 5) TG_F(3, 5); else TG_F(3, 4);
@@ -115,20 +120,21 @@ void filter_apply(const Grid& g, const FilterStencil& fs, const double* x, const
 // SIMP scale factors eps + (1-eps) x^p in FP64 / FP32 / BF16
 // ---------------------------------------------------------------------------
 __global__ void k_simp(int64_t n, const double* __restrict__ x, double eps, double penal,
-                       double* s64, float* s32, __nv_bfloat16* s16) {
+                       double* s64, float* s32, __nv_bfloat16* s16, const int8_t* flags) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double xv = x[i];
   const double xp = (penal == 3.0) ? xv * xv * xv : pow(xv, penal);
-  const double s = eps + (1.0 - eps) * xp;
+  double s = eps + (1.0 - eps) * xp;
+  if (flags && flags[i] == EL_OUTSIDE) s = 0.0;
   if (s64) s64[i] = s;
   if (s32) s32[i] = (float)s;
   if (s16) s16[i] = __double2bfloat16(s);
 }
 
 void simp_scale(int64_t n, const double* x, double eps, double penal, double* s64, float* s32,
-                __nv_bfloat16* s16, cudaStream_t st) {
-  k_simp<<<(unsigned)cdiv(n, 256), 256, 0, st>>>(n, x, eps, penal, s64, s32, s16);
+                __nv_bfloat16* s16, cudaStream_t st, const int8_t* flags) {
+  k_simp<<<(unsigned)cdiv(n, 256), 256, 0, st>>>(n, x, eps, penal, s64, s32, s16, flags);
   TG_CHECK_LAUNCH();
 }
 
@@ -187,11 +193,12 @@ __global__ void __launch_bounds__(RED_THREADS) k_oc_prep(int64_t n, const double
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double xi = x[i];
-  sc.P[i] = xi * sqrt(-dc[i] / dv[i]);
+  const bool outside = flags && flags[i] == EL_OUTSIDE;
+  sc.P[i] = outside ? 0.0 : xi * sqrt(-dc[i] / dv[i]);
   if (sc.lo) {
     double lo = fmax(0.0, xi - move), hi = fmin(1.0, xi + move);
     if (flags) {
-      if (flags[i] == 1) lo = hi = 0.0;
+      if (flags[i] == 1 || outside) lo = hi = 0.0;
       else if (flags[i] == 2) lo = hi = 1.0;
     }
     sc.lo[i] = lo;
@@ -207,7 +214,7 @@ __device__ __forceinline__ double oc_value(int64_t i, double xi, const OCScratch
   if (BOUNDS) return fmax(sc.lo[i], fmin(sc.hi[i], b));
   double xn = fmax(0.0, fmax(xi - move, fmin(1.0, fmin(xi + move, b))));
   if (flags) {
-    if (flags[i] == 1) xn = 0.0;
+    if (flags[i] == 1 || flags[i] == EL_OUTSIDE) xn = 0.0;
     else if (flags[i] == 2) xn = 1.0;
   }
   return xn;
@@ -487,6 +494,31 @@ __global__ void k_mask(int64_t nnodes, int ndof, const uint8_t* fix, double* v) 
   if (i >= nnodes * ndof) return;
   if ((fix[i / ndof] >> (i % ndof)) & 1) v[i] = 0.0;
 }
+// user's grid numbering <-> device grid numbering (same coordinates; the
+// device grid has extra element / node layers at the high end of each axis)
+__global__ void k_embed(Grid rg, Grid g, int nodes, const double* __restrict__ src,
+                        double* __restrict__ dst, int to_dev) {
+  const int per = nodes ? g.ndof : 1;
+  const int64_t nr = nodes ? rg.nnodes() : rg.nel();
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= nr * per) return;
+  const int64_t i = t / per;
+  const int c = (int)(t - i * per);
+  const int ny = nodes ? rg.nny : rg.ney, nx = nodes ? rg.nnx : rg.nex;
+  const int y = (int)(i % ny), x = (int)((i / ny) % nx), z = (int)(i / ((int64_t)ny * nx));
+  const int64_t j = (nodes ? g.node(x, y, z) : g.elem(x, y, z)) * per + c;
+  if (to_dev) dst[j] = src[t];
+  else dst[t] = src[j];
+}
+
+void embed_copy(const Grid& rg, const Grid& g, bool nodes, const double* src, double* dst,
+                bool to_device_grid, cudaStream_t st) {
+  const int64_t n = (nodes ? rg.nnodes() * g.ndof : rg.nel());
+  k_embed<<<(unsigned)cdiv(n, 256), 256, 0, st>>>(rg, g, nodes ? 1 : 0, src, dst,
+                                                  to_device_grid ? 1 : 0);
+  TG_CHECK_LAUNCH();
+}
+
 void mask_vec_f64(int64_t nnodes, int ndof, const uint8_t* fix, double* v, cudaStream_t st) {
   k_mask<<<(unsigned)cdiv(nnodes * ndof, 256), 256, 0, st>>>(nnodes, ndof, fix, v);
   TG_CHECK_LAUNCH();

@@ -606,7 +606,8 @@ __global__ void __launch_bounds__(RED_THREADS) k_compliance(Grid g, const double
                                                            const double* __restrict__ KE,
                                                            Sector<double> B, double eps,
                                                            double penal, double* dc,
-                                                           double* partial) {
+                                                           double* partial,
+                                                           const int8_t* __restrict__ flags) {
   constexpr int NC = 1 << NDIM;
   constexpr int NE = NC * NDOF;
   __shared__ double sh[32];
@@ -617,6 +618,10 @@ __global__ void __launch_bounds__(RED_THREADS) k_compliance(Grid g, const double
     const int ey = (int)(e % g.ney);
     const int ex = (int)((e / g.ney) % g.nex);
     const int ez = (int)(e / ((int64_t)g.ney * g.nex));
+    if (flags && flags[e] == EL_OUTSIDE) {
+      dc[e] = 0.0;
+      continue;
+    }
     double ue[NC][NDOF];
 #pragma unroll
     for (int d = 0; d < NC; ++d) {
@@ -662,17 +667,18 @@ __global__ void __launch_bounds__(RED_THREADS) k_compliance(Grid g, const double
 }
 
 void fine_compliance(const FineOp& op, const double* xPhys, const double* u, double eps,
-                     double penal, double* dc, double* partial, cudaStream_t st) {
+                     double penal, double* dc, double* partial, cudaStream_t st,
+                     const int8_t* flags) {
   const int64_t nel = op.g.nel();
   const unsigned blocks = red_blocks(nel);
   const int key = op.g.ndim * 10 + op.g.ndof;
 #define TG_COMP(ND, NF)                                                                     \
   if (op.sector)                                                                            \
     k_compliance<ND, NF, true><<<blocks, RED_THREADS, 0, st>>>(op.g, xPhys, u, op.KE64,      \
-                                                              op.B64, eps, penal, dc, partial); \
+                                                              op.B64, eps, penal, dc, partial, flags); \
   else                                                                                      \
     k_compliance<ND, NF, false><<<blocks, RED_THREADS, 0, st>>>(op.g, xPhys, u, op.KE64,     \
-                                                               op.B64, eps, penal, dc, partial);
+                                                               op.B64, eps, penal, dc, partial, flags);
   switch (key) {
     case 33: TG_COMP(3, 3) break;
     case 31: TG_COMP(3, 1) break;

@@ -49,10 +49,16 @@ void fine_apply(const FineOp& op, const S* scale, const T* u, T* y, const T* b, 
 template <typename T, typename S>
 void fine_dinv(const FineOp& op, const S* scale, T* dinv, cudaStream_t st);
 
+// Element flag of padding elements (outside the user's grid, see ctx_init):
+// zero stiffness, excluded from filter, volume, compliance and OC.
+constexpr int8_t EL_OUTSIDE = 3;
+
 // ce_e = u_e^T KE u_e ;  dc_e = -penal (1-eps) x^(penal-1) ce_e ;
-// partial[b] = sum over the block's elements of simp(x_e) ce_e
+// partial[b] = sum over the block's elements of simp(x_e) ce_e (padding
+// elements, flag EL_OUTSIDE, contribute nothing and get dc = 0)
 void fine_compliance(const FineOp& op, const double* xPhys, const double* u, double eps,
-                     double penal, double* dc, double* partial, cudaStream_t st);
+                     double penal, double* dc, double* partial, cudaStream_t st,
+                     const int8_t* flags = nullptr);
 
 // ---------------------------------------------------------------------------
 // assembled 3^ndim-point block stencils (coarse levels)
@@ -105,6 +111,8 @@ struct FilterStencil {
   int nw;                // (2R+1)^ndim
   const double* w;       // [nw] weights, dz slowest, dx, dy fastest
   double* tmp;           // nel scratch for mode 1 (null: divide inside the stencil loop)
+  int rex, rey, rez;     // element extents of the user's grid (smaller than the
+                         // device grid when it is padded); taps beyond are skipped
 };
 // mode 0: y = (H x) / Hs ; mode 1: y = H (x / Hs) ; mode 2: y = H(x*d)/Hs/max(1e-3, x)
 // mode 3: Hs = H 1 (x unused) ; mode 4: y = x (copy, used with the fused reductions)
@@ -112,7 +120,11 @@ void filter_apply(const Grid& ge, const FilterStencil& fs, const double* x, cons
                   const double* Hs, double* y, int mode, cudaStream_t st);
 
 void simp_scale(int64_t n, const double* x, double eps, double penal, double* s64, float* s32,
-                __nv_bfloat16* s16, cudaStream_t st);
+                __nv_bfloat16* s16, cudaStream_t st, const int8_t* flags = nullptr);
+// copy between the user's grid numbering (rg) and the device grid (g, padded
+// at the high end of each axis): per = values per node (nodes) or 1 (elements)
+void embed_copy(const Grid& rg, const Grid& g, bool nodes, const double* src, double* dst,
+                bool to_device_grid, cudaStream_t st);
 
 // vector helpers
 template <typename T>
