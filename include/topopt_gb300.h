@@ -111,6 +111,15 @@ void tg_destroy(tg_ctx* ctx);
 /* One design iteration (topology_optimization.py:411-673, OC branch). */
 int32_t tg_step(tg_ctx* ctx, tg_iter_out* out);
 
+/* One design iteration of each of n independent contexts (a batch of
+ * designs, e.g. heat plates of different sizes), run concurrently by
+ * nthreads host threads (<= 0: min(n, 16)), each context on its own CUDA
+ * stream.  Each context's result equals its own tg_step.  rcs[i] receives
+ * the status of ctxs[i]; the return value is the first non-OK status (or OK).
+ * No reference counterpart: the reference runs one design per process. */
+int32_t tg_step_many(tg_ctx* const* ctxs, int32_t n, tg_iter_out* outs, int32_t* rcs,
+                     int32_t nthreads);
+
 /* Host <-> device copies of a field (TG_FIELD_*), n = number of doubles. */
 int32_t tg_get(tg_ctx* ctx, int32_t field, double* host, int64_t n);
 int32_t tg_set(tg_ctx* ctx, int32_t field, const double* host, int64_t n);

@@ -62,6 +62,8 @@ SIGNATURES = {
     "tg_create": (C.c_int32, [C.POINTER(TgProblem), C.POINTER(C.c_void_p)]),
     "tg_destroy": (None, [C.c_void_p]),
     "tg_step": (C.c_int32, [C.c_void_p, C.POINTER(TgIterOut)]),
+    "tg_step_many": (C.c_int32, [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(TgIterOut),
+                                 C.POINTER(C.c_int32), C.c_int32]),
     "tg_get": (C.c_int32, [C.c_void_p, C.c_int32, _dp, C.c_int64]),
     "tg_set": (C.c_int32, [C.c_void_p, C.c_int32, _dp, C.c_int64]),
     "tg_kmul": (C.c_int32, [C.c_void_p, _dp, _dp, _dp, C.c_int32]),

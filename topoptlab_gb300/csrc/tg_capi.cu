@@ -1,7 +1,10 @@
 // extern "C" entry points (include/topopt_gb300.h).  Every call catches the
 // library's exceptions and turns them into a status code plus a message;
 // nothing aborts and no device code traps.
+#include <algorithm>
+#include <atomic>
 #include <cstring>
+#include <thread>
 #include <vector>
 #include "tg_ctx.cuh"
 #include "tg_cnn.cuh"
@@ -129,6 +132,31 @@ void tg_destroy(tg_ctx* ctx) {
 int32_t tg_step(tg_ctx* ctx, tg_iter_out* out) {
   if (!ctx || !out) return TG_EINVAL;
   return guarded(ctx, [&] { tg::ctx_step(ctx->c, *out); });
+}
+
+int32_t tg_step_many(tg_ctx* const* ctxs, int32_t n, tg_iter_out* outs, int32_t* rcs,
+                     int32_t nthreads) {
+  if (!ctxs || !outs || !rcs || n < 0) return TG_EINVAL;
+  for (int32_t i = 0; i < n; ++i)
+    if (!ctxs[i]) return TG_EINVAL;
+  const int nt = (int)std::max<int32_t>(1, std::min<int32_t>(n, nthreads > 0 ? nthreads : 16));
+  std::atomic<int32_t> next{0};
+  auto worker = [&] {
+    for (int32_t i = next.fetch_add(1); i < n; i = next.fetch_add(1)) {
+      tg_ctx* ctx = ctxs[i];
+      rcs[i] = guarded(ctx, [&] {
+        TG_CUDA(cudaSetDevice(ctx->c.dev));
+        tg::ctx_step(ctx->c, outs[i]);
+      });
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int t = 1; t < nt; ++t) pool.emplace_back(worker);
+  worker();
+  for (auto& th : pool) th.join();
+  for (int32_t i = 0; i < n; ++i)
+    if (rcs[i] != TG_OK) return rcs[i];
+  return TG_OK;
 }
 
 int32_t tg_get(tg_ctx* ctx, int32_t field, double* host, int64_t n) {

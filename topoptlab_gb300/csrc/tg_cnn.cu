@@ -99,12 +99,12 @@ static void conv3_launch(const NG& g, const float* in, const float* W, int cout,
   const unsigned gx = (unsigned)cdiv(g.n(), 128);
   if (cc == 16) {
     const size_t smem = sizeof(float) * 27 * CIN * 16;
-    static bool set = false;
-    if (!set) {
+    static const bool set = [&] {   // once per instantiation, thread-safe
       TG_CUDA(cudaFuncSetAttribute(k_conv3<CIN, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)smem));
-      set = true;
-    }
+      return true;
+    }();
+    (void)set;
     k_conv3<CIN, 16><<<dim3(gx, (unsigned)cdiv(cout, 16)), 128, smem, st>>>(g, in, W, cout, bias,
                                                                           skip, relu, mask, out);
   } else {

@@ -443,12 +443,12 @@ __global__ void __launch_bounds__(zs::NT, sizeof(T) == 8 ? 2 : 4) k_fine_zstream
 }
 
 static int sm_count() {
-  static int n = 0;
-  if (!n) {
-    int dev = 0;
+  static const int n = [] {     // thread-safe one-time initialisation
+    int dev = 0, v = 0;
     TG_CUDA(cudaGetDevice(&dev));
-    TG_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
-  }
+    TG_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev));
+    return v;
+  }();
   return n;
 }
 
@@ -456,11 +456,11 @@ template <int NDOF, typename T, typename S, int KIND, int MODE>
 static void launch_zstream(const ApplyArgs<T, S>& a, cudaStream_t st) {
   constexpr size_t smem = zs::smem<NDOF, T, KIND>();
   auto kern = k_fine_zstream<NDOF, T, S, KIND, MODE>;
-  static bool attr_set = false;
-  if (!attr_set) {
+  static const bool attr_set = [&] {   // once per instantiation, thread-safe
     TG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr_set = true;
-  }
+    return true;
+  }();
+  (void)attr_set;
   const int gy = (int)cdiv(a.g.nny, zs::OY), gx = (int)cdiv(a.g.nnx, zs::OX);
   // z chunks: as many as fit in one wave of resident CTAs (4 per SM in FP32,
   // 2 in FP64), so that no second partial wave doubles the kernel time
@@ -489,11 +489,11 @@ static void launch_apply(const ApplyArgs<T, S>& a, cudaStream_t st) {
   using TL = Tile<NDIM>;
   constexpr size_t smem = apply_smem_v2<NDIM, NDOF, T, KIND>();
   auto kern = k_fine_apply<NDIM, NDOF, T, S, KIND, MODE>;
-  static bool attr_set = false;   // per instantiation; attribute is per function
-  if (!attr_set) {
+  static const bool attr_set = [&] {   // once per instantiation, thread-safe
     TG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr_set = true;
-  }
+    return true;
+  }();
+  (void)attr_set;
   dim3 grid((unsigned)cdiv(a.g.nny, TL::Y), (unsigned)cdiv(a.g.nnx, TL::X),
             (unsigned)cdiv(a.g.nnz, TL::Z));
   const int pk = std::is_same<T, double>::value ? PK_FINE_F64

@@ -52,3 +52,17 @@ def heatplate_2d(nelx, nely, ndof, **kwargs):
     u = np.zeros((ndof, 1))
     fixed = np.arange(int(nely / 2 - nely / 20), int(nely / 2 + 1 + nely / 20))
     return u, f, fixed, np.setdiff1d(np.arange(ndof), fixed), None
+
+
+def heatplate_2d_element_source(nelx, nely, ndof, source=0.01, **kwargs):
+    """heatplate_2d with a uniform volumetric source of `source` per element
+    (each element's source split equally over its 4 nodes) instead of the
+    reference's 0.01 per node; same T = 0 sink on the middle of the x = 0 edge."""
+    u, _, fixed, free, springs = heatplate_2d(nelx, nely, ndof)
+    cnt = np.zeros((nelx + 1, nely + 1))
+    cnt[:-1, :-1] += 1
+    cnt[1:, :-1] += 1
+    cnt[:-1, 1:] += 1
+    cnt[1:, 1:] += 1
+    f = (0.25 * source * cnt).reshape(-1, 1)     # node (x, y) -> x*(nely+1) + y
+    return u, f, fixed, free, springs
