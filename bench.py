@@ -206,6 +206,43 @@ def _train_network(device, args):
                             "smoothed by the rmin=1.5 filter"}
 
 
+def _run_c5(device, steps=3, warmup=2):
+    """C5: 64 heat plates, nelx = nely uniform in [64, 512] (seed 0), stepped
+    concurrently (tg_step_many), mixed precision and plain FP64, each to an
+    FP64 relative residual of 1e-8; wall time of whole batch iterations."""
+    from topoptlab_gb300.batch import heat_plate_batch, heat_plate_sizes
+    sizes = heat_plate_sizes(64, seed=0, nmin=64, nmax=512)
+    out = {"workload": "64 heat plates, nelx=nely ~ U{64..512} (seed 0), kmin 1e-3, penal 3, "
+                       "volfrac 0.4, rmin 1.5, ft=1, source 0.01 per element, T=0 sink on the "
+                       "middle 10% of the left edge, FP64 relative residual 1e-8",
+           "elements": int(sum(n * n for n in sizes)), "sizes_min_max": [min(sizes), max(sizes)],
+           "odd_sizes_padded": int(sum(n % 2 for n in sizes)), "steps": steps, "warmup": warmup,
+           "execution": "one context per design on its own CUDA stream, stepped concurrently "
+                        "by a host thread pool (tg_step_many); no learned warm start (the network "
+                        "is built for 3-D elasticity)"}
+    objs = {}
+    for prec in ("mixed", "fp64"):
+        batch = heat_plate_batch(sizes, precision=prec, device=device)
+        try:
+            for _ in range(warmup):
+                batch.step()
+            t0 = time.perf_counter()
+            res = [batch.step() for _ in range(steps)]
+            t = time.perf_counter() - t0
+        finally:
+            batch.close()
+        objs[prec] = [[r.obj for r in it] for it in res]
+        out[prec] = {"design_iters_per_s": len(sizes) * steps / t,
+                     "batch_iteration_ms": 1000.0 * t / steps,
+                     "max_rel_res": max(r.rel_res for it in res for r in it),
+                     "pcg_iters_mean": float(np.mean([r.pcg_iters for it in res for r in it]))}
+    out["ratio_mixed_vs_fp64"] = (out["mixed"]["design_iters_per_s"] /
+                                  out["fp64"]["design_iters_per_s"])
+    out["compliance_max_rel_diff_vs_fp64"] = max(
+        abs(a - b) / abs(b) for ia, ib in zip(objs["mixed"], objs["fp64"]) for a, b in zip(ia, ib))
+    return out
+
+
 def run_ours(args, dist, rank, ws, local):
     from topoptlab_gb300 import _lib
     import ctypes as C
@@ -353,6 +390,8 @@ def run_ours(args, dist, rank, ws, local):
                 "algorithmic_bytes_per_launch": nbytes,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if peaks else "fallback"}
 
+    c5 = None if args.no_c5 else _run_c5(device)
+
     if rank != 0:
         return None
     mean = lambda k, L: float(np.mean([getattr(s, k) for s in L]))
@@ -391,6 +430,8 @@ def run_ours(args, dist, rank, ws, local):
         "clocks": clk.summary(),
         "time_breakdown": breakdown,
     }
+    if c5 is not None:
+        line["c5_batch"] = c5
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(steps=2, warmup=1)
     return line
@@ -483,6 +524,8 @@ def main():
     ap.add_argument("--train-epochs", type=int, default=10)
     ap.add_argument("--no-plain", action="store_true",
                     help="skip the plain FP64 arm (profiling runs only)")
+    ap.add_argument("--no-c5", action="store_true",
+                    help="skip the batched heat-plate measurement")
     ap.add_argument("--no-breakdown", action="store_true",
                     help="skip the per-family time breakdown (profiling runs only)")
     ap.add_argument("--size", default=None,
