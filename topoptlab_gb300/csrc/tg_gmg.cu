@@ -193,27 +193,25 @@ void stencil_pack_f32(const Grid& g, const double* A, float* B, cudaStream_t st)
   }
   TG_CHECK_LAUNCH();
 }
-// + 4 floats: the streaming sweep reads whole 16-byte units
 int64_t stencil_blk_floats(const Grid& g) {
-  return g.nnodes() * (g.ndim == 3 ? 14 : 5) * g.ndof * (g.ndof == 3 ? 4 : g.ndof) + 4;
+  return g.nnodes() * (g.ndim == 3 ? 14 : 5) * g.ndof * (g.ndof == 3 ? 4 : g.ndof);
 }
 
-// The nodes of a CTA (a TY x TX patch with TY = nny, or TX = 1) form one
-// contiguous node range [n0, n0 + TY*TX), so direction d's blocks for all of
-// them -- stored at the nodes (upper directions) or at the neighbours
-// n + off(d) (lower directions, transposed) -- are one contiguous chunk of
-// the blocked array.  The chunks stream through a ring of STAGES shared
-// buffers with 16-byte cp.async (no registers held while in flight); thread
-// t of the CTA finds its block at entry t of every chunk.
-constexpr int SB_STAGES = 4;
-
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N> __device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+// row ci of a block as NDOF floats
+template <int NDOF>
+__device__ __forceinline__ void load_rows(const float* __restrict__ p, float (&r)[NDOF][NDOF]) {
+  if constexpr (NDOF == 3) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const float4 v = __ldg(reinterpret_cast<const float4*>(p) + i);
+      r[i][0] = v.x; r[i][1] = v.y; r[i][2] = v.z;
+    }
+  } else if constexpr (NDOF == 2) {
+    const float4 v = __ldg(reinterpret_cast<const float4*>(p));
+    r[0][0] = v.x; r[0][1] = v.y; r[1][0] = v.z; r[1][1] = v.w;
+  } else {
+    r[0][0] = __ldg(p);
+  }
 }
 
 template <int NDIM, int NDOF, int MODE>
@@ -225,54 +223,13 @@ __global__ void __launch_bounds__(256) k_stencil_blk(Grid g, int TY, int TX,
                                                     const float* __restrict__ dinv, float omega) {
   constexpr int NP = (NDIM == 3) ? 3 : 1;
   constexpr int C = ndir<NDIM>() / 2;
-  constexpr int ND = ndir<NDIM>();
   constexpr int BS = NDOF * blk_rw<NDOF>();        // floats per block
-  constexpr int BV = (BS + 3) / 4;                 // 16-byte units per block (NDOF = 1: 1 unit / 4 nodes)
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  float* us = reinterpret_cast<float*>(smem_raw);
   const int RY = TY + 2, PL = (TX + 2) * RY;
-  const int nn = TY * TX;                           // nodes of the CTA (<= 256)
-  const int64_t ld = g.nnodes();
-  // chunk of one direction in 16-byte units (NDOF = 1: 4 nodes per unit)
-  const int CU = (NDOF == 1) ? (nn + 3) / 4 + 1 : nn * BV;
-  float4* cb = reinterpret_cast<float4*>(smem_raw);                 // [STAGES][CU]
-  float* us = reinterpret_cast<float*>(cb + SB_STAGES * CU);        // u planes
   const int y0 = blockIdx.x * TY, x0 = blockIdx.y * TX, z = blockIdx.z;
+  const int64_t ld = g.nnodes();
   const int tid = threadIdx.x;
-  const int64_t n0 = g.node(x0, y0, z);
-  const int64_t sx = g.nny, sz = (int64_t)g.nny * g.nnx;
-  const int64_t nunits = (NDOF == 1) ? (ld * (ND / 2 + 1) + 3) / 4 : ld * (ND / 2 + 1) * BV;
-  const float4* A4 = reinterpret_cast<const float4*>(A);
-  // first unit of direction d's chunk (NDOF = 1: the unit holding the first
-  // float; e0 = offset of that float inside the chunk's first unit)
-  auto chunk_start = [&](int d, int& e0) -> int64_t {
-    int dx, dy, dz;
-    dir_xyz(d, NDIM, dx, dy, dz);
-    const int64_t node = (d >= C) ? n0 : n0 + dz * sz + dx * sx + dy;
-    const int dh = (d >= C) ? d - C : C - d;
-    const int64_t f = ((int64_t)dh * ld + node) * BS;                  // first float
-    if (NDOF == 1) {
-      const int64_t fu = (f >= 0) ? f / 4 : -((-f + 3) / 4);
-      e0 = (int)(f - fu * 4);
-      return fu;
-    }
-    e0 = 0;
-    return f / 4;
-  };
-  auto issue = [&](int d) {
-    if (d < ND) {
-      int e0;
-      const int64_t u0 = chunk_start(d, e0);
-      float4* dst = cb + (d % SB_STAGES) * CU;
-      for (int i = tid; i < CU; i += blockDim.x) {
-        const int64_t src = u0 + i;
-        if (src >= 0 && src < nunits) cp_async16(dst + i, A4 + src);
-      }
-    }
-    cp_async_commit();
-  };
-#pragma unroll
-  for (int d = 0; d < SB_STAGES - 1; ++d) issue(d);
-  // stage u (global order: component fastest) while the first chunks fly
   for (int i = tid; i < NDOF * NP * PL; i += blockDim.x) {
     const int c = i % NDOF, hy = (i / NDOF) % RY, hx = (i / (NDOF * RY)) % (TX + 2);
     const int pz = i / (NDOF * PL);
@@ -281,67 +238,44 @@ __global__ void __launch_bounds__(256) k_stencil_blk(Grid g, int TY, int TX,
     if (in_grid(g, gx, gy, gz)) v = __ldg(u + g.node(gx, gy, gz) * NDOF + c);
     us[(c * NP + pz) * PL + hx * RY + hy] = v;
   }
+  __syncthreads();
   const int ty = tid % TY, tx = tid / TY;
   const int xx = x0 + tx, yy = y0 + ty;
-  const bool active = tid < nn && xx < g.nnx && yy < g.nny;
-  // neighbour-in-grid bits: bit (axis*2 + 0) low side exists, +1 high side
-  const unsigned okb = (xx > 0 ? 1u : 0u) | (xx + 1 < g.nnx ? 2u : 0u) | (yy > 0 ? 4u : 0u) |
-                       (yy + 1 < g.nny ? 8u : 0u) | (z > 0 ? 16u : 0u) | (z + 1 < g.nnz ? 32u : 0u);
-  auto side_ok = [okb](int dd, int axis) {
-    return dd == 0 || ((okb >> (axis * 2 + (dd > 0 ? 1 : 0))) & 1u);
-  };
+  if (tx >= TX || xx >= g.nnx || yy >= g.nny) return;
+  const int64_t n = g.node(xx, yy, z);
+  const bool ok[3][3] = {{xx > 0, true, xx + 1 < g.nnx},
+                         {yy > 0, true, yy + 1 < g.nny},
+                         {z > 0, true, z + 1 < g.nnz}};
+  const int64_t sx = g.nny, sz = (int64_t)g.nny * g.nnx;
   const float* uc = us + ((NDIM == 3) ? PL : 0) + (tx + 1) * RY + (ty + 1);
   float acc[NDOF];
 #pragma unroll
   for (int ci = 0; ci < NDOF; ++ci) acc[ci] = 0.f;
-#pragma unroll 1
-  for (int d = 0; d < ND; ++d) {
-    issue(d + SB_STAGES - 1);
-    cp_async_wait<SB_STAGES - 1>();
-    __syncthreads();
-    if (active) {
-      int dx, dy, dz;
-      dir_xyz(d, NDIM, dx, dy, dz);
-      const bool v = side_ok(dx, 0) && side_ok(dy, 1) && side_ok(dz, 2);
-      if (v) {
-        const int so = dz * PL + dx * RY + dy;
-        float uu[NDOF];
 #pragma unroll
-        for (int cj = 0; cj < NDOF; ++cj) uu[cj] = uc[cj * NP * PL + so];
-        const float4* blk = cb + (d % SB_STAGES) * CU;
-        float r[NDOF][NDOF];
-        if constexpr (NDOF == 1) {
-          int e0;
-          (void)chunk_start(d, e0);
-          r[0][0] = reinterpret_cast<const float*>(blk)[e0 + tid];
-        } else if constexpr (NDOF == 2) {
-          const float4 q = blk[tid];
-          r[0][0] = q.x; r[0][1] = q.y; r[1][0] = q.z; r[1][1] = q.w;
-        } else {
+  for (int d = 0; d < ndir<NDIM>(); ++d) {
+    int dx, dy, dz;
+    dir_xyz(d, NDIM, dx, dy, dz);
+    const bool v = ok[0][dx + 1] && ok[1][dy + 1] && ok[2][dz + 1];
+    const int64_t m = v ? n + dz * sz + dx * sx + dy : n;
+    const int so = dz * PL + dx * RY + dy;
+    float uu[NDOF];
 #pragma unroll
-          for (int i = 0; i < NDOF; ++i) {
-            const float4 q = blk[tid * BV + i];
-            r[i][0] = q.x; r[i][1] = q.y; r[i][2] = q.z;
-          }
-        }
-        if (d >= C) {
+    for (int cj = 0; cj < NDOF; ++cj) uu[cj] = uc[cj * NP * PL + so];
+    float r[NDOF][NDOF];
+    if (d >= C) {
+      load_rows<NDOF>(A + ((int64_t)(d - C) * ld + n) * BS, r);
 #pragma unroll
-          for (int ci = 0; ci < NDOF; ++ci)
+      for (int ci = 0; ci < NDOF; ++ci)
 #pragma unroll
-            for (int cj = 0; cj < NDOF; ++cj) acc[ci] = fmaf(r[ci][cj], uu[cj], acc[ci]);
-        } else {
+        for (int cj = 0; cj < NDOF; ++cj) acc[ci] = fmaf(r[ci][cj], uu[cj], acc[ci]);
+    } else {
+      load_rows<NDOF>(A + ((int64_t)(C - d) * ld + m) * BS, r);     // transpose at the neighbour
 #pragma unroll
-          for (int ci = 0; ci < NDOF; ++ci)
+      for (int ci = 0; ci < NDOF; ++ci)
 #pragma unroll
-            for (int cj = 0; cj < NDOF; ++cj) acc[ci] = fmaf(r[cj][ci], uu[cj], acc[ci]);
-        }
-      }
+        for (int cj = 0; cj < NDOF; ++cj) acc[ci] = fmaf(r[cj][ci], uu[cj], acc[ci]);
     }
-    __syncthreads();     // stage d % STAGES is refilled by the next iteration's issue
   }
-  cp_async_wait<0>();
-  if (!active) return;
-  const int64_t n = n0 + tid;
 #pragma unroll
   for (int ci = 0; ci < NDOF; ++ci) {
     const int64_t k = n * NDOF + ci;
@@ -353,37 +287,17 @@ __global__ void __launch_bounds__(256) k_stencil_blk(Grid g, int TY, int TX,
   }
 }
 
-// the largest request: 4 stages x 256 nodes x 3 units + u planes of a 256 x 1 patch
-constexpr int SB_SMEM_MAX = 16 * SB_STAGES * 768 + 4 * 9 * 3 * 258;
-
-template <int NDIM, int NDOF, int MODE>
-static void launch_blk(dim3 grid, size_t smem, cudaStream_t st, const Grid& g, int TY, int TX,
-                       const float* A, const float* u, float* y, const float* b,
-                       const float* dinv, float om) {
-  static const bool attr = [] {   // once per instantiation, thread-safe
-    TG_CUDA(cudaFuncSetAttribute(k_stencil_blk<NDIM, NDOF, MODE>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, SB_SMEM_MAX));
-    return true;
-  }();
-  (void)attr;
-  k_stencil_blk<NDIM, NDOF, MODE><<<grid, 256, smem, st>>>(g, TY, TX, A, u, y, b, dinv, om);
-}
-
 void stencil_apply_blk(const Grid& g, const float* A, const float* u, float* y, const float* b,
                        const float* dinv, double omega, int mode, cudaStream_t st) {
   const int TY = std::min(g.nny, 256);
   const int TX = std::max(1, std::min(g.nnx, 256 / TY));
   const dim3 grid((unsigned)cdiv(g.nny, TY), (unsigned)cdiv(g.nnx, TX), (unsigned)g.nnz);
-  const int nn = TY * TX;
-  const int bv = (g.ndof * (g.ndof == 3 ? 4 : g.ndof) + 3) / 4;
-  const int cu = g.ndof == 1 ? (nn + 3) / 4 + 1 : nn * bv;
-  const size_t smem = 16 * (size_t)SB_STAGES * cu +
-                      sizeof(float) * g.ndof * (g.ndim == 3 ? 3 : 1) * (TX + 2) * (TY + 2);
+  const size_t smem = sizeof(float) * g.ndof * (g.ndim == 3 ? 3 : 1) * (TX + 2) * (TY + 2);
   const float om = (float)omega;
 #define TG_SB(ND, NF)                                                                          \
-  if (mode == AM_Y) launch_blk<ND, NF, AM_Y>(grid, smem, st, g, TY, TX, A, u, y, b, dinv, om); \
-  else if (mode == AM_RES) launch_blk<ND, NF, AM_RES>(grid, smem, st, g, TY, TX, A, u, y, b, dinv, om); \
-  else launch_blk<ND, NF, AM_JACOBI>(grid, smem, st, g, TY, TX, A, u, y, b, dinv, om);
+  if (mode == AM_Y) k_stencil_blk<ND, NF, AM_Y><<<grid, 256, smem, st>>>(g, TY, TX, A, u, y, b, dinv, om); \
+  else if (mode == AM_RES) k_stencil_blk<ND, NF, AM_RES><<<grid, 256, smem, st>>>(g, TY, TX, A, u, y, b, dinv, om); \
+  else k_stencil_blk<ND, NF, AM_JACOBI><<<grid, 256, smem, st>>>(g, TY, TX, A, u, y, b, dinv, om);
   switch (g.ndim * 10 + g.ndof) {
     case 33: TG_SB(3, 3) break;
     case 31: TG_SB(3, 1) break;
