@@ -285,7 +285,7 @@ void ctx_init(Ctx& c, const tg_problem& p) {
       v.dinv64.alloc(n); v.t64.alloc(n); v.r64.alloc(n);
       if (mixed) {
         v.dinv32.alloc(n); v.t32.alloc(n); v.r32.alloc(n);
-        if (l >= 1) v.A32.alloc(stencil_blk_floats(v.g));   // blocked FP32 layout
+        if (l >= 1) v.A32.alloc(ns);
       }
     }
     if (l >= 1) {
@@ -390,8 +390,8 @@ void build_hierarchy(Ctx& c) {
     if (l < c.L - 1) {
       stencil_dinv<double>(v.g, v.fix, v.A64, v.dinv64, c.st);
       if (mixed) {
-        stencil_pack_f32(v.g, v.A64, v.A32, c.st);
-        d2f(v.g.ndofs(), v.dinv64, v.dinv32, c.st);
+        d2f(v.A64.n, v.A64, v.A32, c.st);
+        stencil_dinv<float>(v.g, v.fix, v.A32, v.dinv32, c.st);
       }
     }
   }
@@ -437,10 +437,7 @@ static void level_apply(Ctx& c, int l, const T* in, T* out, const T* b, int mode
                                        mode, c.st);
   } else {
     ProfScope ps(sizeof(T) == 8 ? PK_STENCIL_F64 : (l == 1 ? PK_STENCIL1_F32 : PK_STENCIL_F32), c.st);
-    if constexpr (std::is_same<T, float>::value)
-      stencil_apply_blk(v.g, v.A32, in, out, b, v.dinv32, c.omega, mode, c.st);
-    else
-      stencil_apply<T>(v.g, LvBufs<T>::A(v), in, out, b, LvBufs<T>::dinv(v), c.omega, mode, c.st);
+    stencil_apply<T>(v.g, LvBufs<T>::A(v), in, out, b, LvBufs<T>::dinv(v), c.omega, mode, c.st);
   }
 }
 

@@ -38,7 +38,7 @@ struct Level {
   Grid g;
   DevBuf<uint8_t> fix;
   DevBuf<double> A64;       // stencil (levels >= 1)
-  DevBuf<float> A32;        // FP32 V-cycle copy, blocked layout (stencil_pack_f32)
+  DevBuf<float> A32;
   DevBuf<double> dinv64, b64, x64, t64, r64;
   DevBuf<float> dinv32, b32, x32, t32, r32;
 };

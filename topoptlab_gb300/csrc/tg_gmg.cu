@@ -155,160 +155,6 @@ template void stencil_apply<double>(const Grid&, const double*, const double*, d
 template void stencil_apply<float>(const Grid&, const float*, const float*, float*, const float*,
                                    const float*, double, int, cudaStream_t);
 
-// ---------------------------------------------------------------------------
-// FP32 V-cycle stencils in blocked layout: the half-stored blocks of a node
-// are contiguous rows [dh][node][ci][RW] (RW = 4 for 3x3 blocks, one float4
-// per row with a zero pad; 2 for 2x2, the block is one float4; 1 for
-// scalars).  A thread per node reads a whole block with NDOF vector loads
-// (81 LDG.128 per node in 3-D elasticity instead of 243 scalar loads), so
-// the latency-bound sweep has a third of the load instructions in flight for
-// 4/3 of the bytes.
-// ---------------------------------------------------------------------------
-template <int NDOF> __host__ __device__ constexpr int blk_rw() { return NDOF == 3 ? 4 : NDOF; }
-
-template <int NDIM, int NDOF>
-__global__ void k_stencil_pack(Grid g, const double* __restrict__ A, float* __restrict__ B) {
-  constexpr int RW = blk_rw<NDOF>();
-  const int64_t ld = g.nnodes();
-  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t >= ld * ndir_half<NDIM>() * NDOF * RW) return;
-  const int k = (int)(t % (NDOF * RW));
-  const int64_t bn = t / (NDOF * RW);               // dh * ld + node
-  const int dh = (int)(bn / ld);
-  const int64_t n = bn - (int64_t)dh * ld;
-  const int ci = k / RW, cj = k % RW;
-  B[t] = cj < NDOF ? (float)A[((dh * NDOF + ci) * NDOF + cj) * ld + n] : 0.f;
-}
-
-void stencil_pack_f32(const Grid& g, const double* A, float* B, cudaStream_t st) {
-  const int rw = g.ndof == 3 ? 4 : g.ndof;
-  const int64_t n = g.nnodes() * (g.ndim == 3 ? 14 : 5) * g.ndof * rw;
-  const unsigned blocks = (unsigned)cdiv(n, 256);
-  switch (g.ndim * 10 + g.ndof) {
-    case 33: k_stencil_pack<3, 3><<<blocks, 256, 0, st>>>(g, A, B); break;
-    case 31: k_stencil_pack<3, 1><<<blocks, 256, 0, st>>>(g, A, B); break;
-    case 22: k_stencil_pack<2, 2><<<blocks, 256, 0, st>>>(g, A, B); break;
-    case 21: k_stencil_pack<2, 1><<<blocks, 256, 0, st>>>(g, A, B); break;
-    default: throw Error{EINVAL_, "unsupported (ndim, nnode_dof)"};
-  }
-  TG_CHECK_LAUNCH();
-}
-int64_t stencil_blk_floats(const Grid& g) {
-  return g.nnodes() * (g.ndim == 3 ? 14 : 5) * g.ndof * (g.ndof == 3 ? 4 : g.ndof);
-}
-
-// row ci of a block as NDOF floats
-template <int NDOF>
-__device__ __forceinline__ void load_rows(const float* __restrict__ p, float (&r)[NDOF][NDOF]) {
-  if constexpr (NDOF == 3) {
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-      const float4 v = __ldg(reinterpret_cast<const float4*>(p) + i);
-      r[i][0] = v.x; r[i][1] = v.y; r[i][2] = v.z;
-    }
-  } else if constexpr (NDOF == 2) {
-    const float4 v = __ldg(reinterpret_cast<const float4*>(p));
-    r[0][0] = v.x; r[0][1] = v.y; r[1][0] = v.z; r[1][1] = v.w;
-  } else {
-    r[0][0] = __ldg(p);
-  }
-}
-
-template <int NDIM, int NDOF, int MODE>
-__global__ void __launch_bounds__(256) k_stencil_blk(Grid g, int TY, int TX,
-                                                    const float* __restrict__ A,
-                                                    const float* __restrict__ u,
-                                                    float* __restrict__ y,
-                                                    const float* __restrict__ b,
-                                                    const float* __restrict__ dinv, float omega) {
-  constexpr int NP = (NDIM == 3) ? 3 : 1;
-  constexpr int C = ndir<NDIM>() / 2;
-  constexpr int BS = NDOF * blk_rw<NDOF>();        // floats per block
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  float* us = reinterpret_cast<float*>(smem_raw);
-  const int RY = TY + 2, PL = (TX + 2) * RY;
-  const int y0 = blockIdx.x * TY, x0 = blockIdx.y * TX, z = blockIdx.z;
-  const int64_t ld = g.nnodes();
-  const int tid = threadIdx.x;
-  for (int i = tid; i < NDOF * NP * PL; i += blockDim.x) {
-    const int c = i % NDOF, hy = (i / NDOF) % RY, hx = (i / (NDOF * RY)) % (TX + 2);
-    const int pz = i / (NDOF * PL);
-    const int gx = x0 - 1 + hx, gy = y0 - 1 + hy, gz = (NDIM == 3) ? z - 1 + pz : 0;
-    float v = 0.f;
-    if (in_grid(g, gx, gy, gz)) v = __ldg(u + g.node(gx, gy, gz) * NDOF + c);
-    us[(c * NP + pz) * PL + hx * RY + hy] = v;
-  }
-  __syncthreads();
-  const int ty = tid % TY, tx = tid / TY;
-  const int xx = x0 + tx, yy = y0 + ty;
-  if (tx >= TX || xx >= g.nnx || yy >= g.nny) return;
-  const int64_t n = g.node(xx, yy, z);
-  const bool ok[3][3] = {{xx > 0, true, xx + 1 < g.nnx},
-                         {yy > 0, true, yy + 1 < g.nny},
-                         {z > 0, true, z + 1 < g.nnz}};
-  const int64_t sx = g.nny, sz = (int64_t)g.nny * g.nnx;
-  const float* uc = us + ((NDIM == 3) ? PL : 0) + (tx + 1) * RY + (ty + 1);
-  float acc[NDOF];
-#pragma unroll
-  for (int ci = 0; ci < NDOF; ++ci) acc[ci] = 0.f;
-#pragma unroll
-  for (int d = 0; d < ndir<NDIM>(); ++d) {
-    int dx, dy, dz;
-    dir_xyz(d, NDIM, dx, dy, dz);
-    const bool v = ok[0][dx + 1] && ok[1][dy + 1] && ok[2][dz + 1];
-    const int64_t m = v ? n + dz * sz + dx * sx + dy : n;
-    const int so = dz * PL + dx * RY + dy;
-    float uu[NDOF];
-#pragma unroll
-    for (int cj = 0; cj < NDOF; ++cj) uu[cj] = uc[cj * NP * PL + so];
-    float r[NDOF][NDOF];
-    if (d >= C) {
-      load_rows<NDOF>(A + ((int64_t)(d - C) * ld + n) * BS, r);
-#pragma unroll
-      for (int ci = 0; ci < NDOF; ++ci)
-#pragma unroll
-        for (int cj = 0; cj < NDOF; ++cj) acc[ci] = fmaf(r[ci][cj], uu[cj], acc[ci]);
-    } else {
-      load_rows<NDOF>(A + ((int64_t)(C - d) * ld + m) * BS, r);     // transpose at the neighbour
-#pragma unroll
-      for (int ci = 0; ci < NDOF; ++ci)
-#pragma unroll
-        for (int cj = 0; cj < NDOF; ++cj) acc[ci] = fmaf(r[cj][ci], uu[cj], acc[ci]);
-    }
-  }
-#pragma unroll
-  for (int ci = 0; ci < NDOF; ++ci) {
-    const int64_t k = n * NDOF + ci;
-    float out;
-    if (MODE == AM_Y) out = acc[ci];
-    else if (MODE == AM_RES) out = b[k] - acc[ci];
-    else out = uc[ci * NP * PL] + omega * dinv[k] * (b[k] - acc[ci]);
-    y[k] = out;
-  }
-}
-
-void stencil_apply_blk(const Grid& g, const float* A, const float* u, float* y, const float* b,
-                       const float* dinv, double omega, int mode, cudaStream_t st) {
-  const int TY = std::min(g.nny, 256);
-  const int TX = std::max(1, std::min(g.nnx, 256 / TY));
-  const dim3 grid((unsigned)cdiv(g.nny, TY), (unsigned)cdiv(g.nnx, TX), (unsigned)g.nnz);
-  const size_t smem = sizeof(float) * g.ndof * (g.ndim == 3 ? 3 : 1) * (TX + 2) * (TY + 2);
-  const float om = (float)omega;
-#define TG_SB(ND, NF)                                                                          \
-  if (mode == AM_Y) k_stencil_blk<ND, NF, AM_Y><<<grid, 256, smem, st>>>(g, TY, TX, A, u, y, b, dinv, om); \
-  else if (mode == AM_RES) k_stencil_blk<ND, NF, AM_RES><<<grid, 256, smem, st>>>(g, TY, TX, A, u, y, b, dinv, om); \
-  else k_stencil_blk<ND, NF, AM_JACOBI><<<grid, 256, smem, st>>>(g, TY, TX, A, u, y, b, dinv, om);
-  switch (g.ndim * 10 + g.ndof) {
-    case 33: TG_SB(3, 3) break;
-    case 31: TG_SB(3, 1) break;
-    case 22: TG_SB(2, 2) break;
-    case 21: TG_SB(2, 1) break;
-    default: throw Error{EINVAL_, "unsupported (ndim, nnode_dof)"};
-  }
-#undef TG_SB
-  TG_CHECK_LAUNCH();
-}
-
 template <int NDIM, int NDOF, typename T>
 __global__ void k_stencil_dinv(Grid g, const uint8_t* fix, const T* A, T* dinv) {
   const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;

@@ -72,12 +72,6 @@ void stencil_apply(const Grid& g, const T* A, const T* u, T* y, const T* b, cons
                    double omega, int mode, cudaStream_t st);
 template <typename T>
 void stencil_dinv(const Grid& g, const uint8_t* fix, const T* A, T* dinv, cudaStream_t st);
-// FP32 blocked copy of a half-stored FP64 stencil (the V-cycle layout):
-// [dh][node][ci][RW], RW = 4 (3x3 blocks), 2 (2x2) or 1; and its sweep
-int64_t stencil_blk_floats(const Grid& g);
-void stencil_pack_f32(const Grid& g, const double* A, float* B, cudaStream_t st);
-void stencil_apply_blk(const Grid& g, const float* A, const float* u, float* y, const float* b,
-                       const float* dinv, double omega, int mode, cudaStream_t st);
 
 // level-1 stencil straight from element scale factors (exact masked Galerkin)
 void build_level1(const FineOp& op, const double* scale, const uint8_t* elem_touch_fixed,
