@@ -604,15 +604,11 @@ void stencil_to_dense(const Grid& g, const uint8_t* fix, const double* A, double
 
 constexpr int GJB = 32;
 
-// invert the k-th diagonal block (SPD, no pivoting) into P (GJB x GJB)
-__global__ void __launch_bounds__(GJB * GJB) k_gj_pivot(const double* D, int64_t ld, int k, double* P) {
-  // GB300's FP64 pipe is narrow: one reciprocal per step (not one divide per
-  // thread), everything else is multiply / FMA
-  __shared__ double a[GJB][GJB + 1];
-  __shared__ double rpiv;
-  const int i = threadIdx.y, j = threadIdx.x;
-  a[i][j] = D[(int64_t)(k * GJB + i) * ld + k * GJB + j];
-  __syncthreads();
+// invert a GJB x GJB SPD tile in shared memory (Gauss-Jordan without pivoting;
+// GB300's FP64 pipe is narrow: one reciprocal per step, not one divide per
+// thread, everything else multiply / FMA); 1024 threads, (i, j) = (y, x)
+__device__ __forceinline__ void gj_tile_inverse(double (&a)[GJB][GJB + 1], double& rpiv, int i,
+                                                int j) {
   for (int p = 0; p < GJB; ++p) {
     if (i == 0 && j == 0) rpiv = 1.0 / a[p][p];
     __syncthreads();
@@ -627,66 +623,75 @@ __global__ void __launch_bounds__(GJB * GJB) k_gj_pivot(const double* D, int64_t
     a[i][j] = v;
     __syncthreads();
   }
-  P[i * GJB + j] = a[i][j];
 }
+
 // The coarsest matrix is SPD, so it is inverted with the block sweep operator,
 // which keeps the matrix symmetric at every step (pivot block K, P = A_KK^-1):
 //   A_KK <- -P,  A_KJ <- P A_KJ,  A_IK <- A_IK P,  A_IJ <- A_IJ - A_IK P A_KJ,
 // ending with -A^-1.  Only blocks (ib <= jb) are kept up to date, which halves
 // the rank-32 update flops of a plain Gauss-Jordan inverse and removes its
 // column-panel product (A_IK P is the transpose of the row panel P A_KI).
-// Block (k, j) of the upper-stored matrix, as a 32 x 32 tile X[m][c]:
-__device__ __forceinline__ double sw_panel(const double* D, int64_t ld, int k, int jb, int m, int c) {
-  return k <= jb ? D[(int64_t)(k * GJB + m) * ld + jb * GJB + c]
-                 : D[(int64_t)(jb * GJB + c) * ld + k * GJB + m];
-}
-// R[:, jb] = P * A_K,jb
-__global__ void __launch_bounds__(GJB * GJB) k_sw_rowpanel(const double* D, int64_t ld, int k,
-                                                          const double* P, double* R) {
-  __shared__ double ps[GJB][GJB + 1], xs[GJB][GJB + 1];
+// Two launches per pivot step:
+//  (1) panel: every CTA jb inverts the pivot tile itself (no serial pivot
+//      launch; the redundant tile inversions are ~1 % of the step's FP64
+//      work), saves the original panel tile X_J = A_KJ to Xb and writes
+//      R_J = P X_J; CTA K writes P;
+//  (2) update: D_IJ -= X_I^T R_J for ib <= jb off the pivot row/column, and
+//      the panel row/column and the pivot tile are overwritten with R and -P
+//      in the same launch (the update reads X from Xb, so no tile is read
+//      and written by different CTAs of one launch).
+__global__ void __launch_bounds__(GJB * GJB) k_sw_panel(const double* D, int64_t ld, int k,
+                                                       double* P, double* R, double* Xb) {
+  __shared__ double a[GJB][GJB + 1], xs[GJB][GJB + 1];
+  __shared__ double rpiv;
   const int jb = blockIdx.x;
-  if (jb == k) return;
   const int i = threadIdx.y, j = threadIdx.x;
-  ps[i][j] = P[i * GJB + j];
-  if (k < jb) xs[i][j] = D[(int64_t)(k * GJB + i) * ld + jb * GJB + j];
-  else xs[j][i] = D[(int64_t)(jb * GJB + i) * ld + k * GJB + j];   // coalesced, transposed in smem
+  a[i][j] = D[(int64_t)(k * GJB + i) * ld + k * GJB + j];
+  if (jb != k) {
+    if (k < jb) xs[i][j] = D[(int64_t)(k * GJB + i) * ld + jb * GJB + j];
+    else xs[j][i] = D[(int64_t)(jb * GJB + i) * ld + k * GJB + j];   // coalesced, transposed in smem
+  }
   __syncthreads();
+  gj_tile_inverse(a, rpiv, i, j);
+  if (jb == k) {
+    P[i * GJB + j] = a[i][j];
+    return;
+  }
   double acc = 0.0;
 #pragma unroll 8
-  for (int m = 0; m < GJB; ++m) acc = fma(ps[i][m], xs[m][j], acc);
+  for (int m = 0; m < GJB; ++m) acc = fma(a[i][m], xs[m][j], acc);
   R[(int64_t)i * ld + jb * GJB + j] = acc;
+  Xb[(int64_t)i * ld + jb * GJB + j] = xs[i][j];
 }
-// A_IJ -= X_I^T R_J  for ib <= jb, ib != k != jb  (X_I = A_KI before this step)
+
 __global__ void __launch_bounds__(GJB * GJB) k_sw_update(double* D, int64_t ld, int k,
-                                                        const double* R) {
+                                                        const double* P, const double* R,
+                                                        const double* Xb) {
   const int ib = blockIdx.y, jb = blockIdx.x;
-  if (ib > jb || ib == k || jb == k) return;
-  __shared__ double xs[GJB][GJB + 1], rs[GJB][GJB + 1];
+  if (ib > jb) return;
   const int i = threadIdx.y, j = threadIdx.x;
-  if (k < ib) xs[i][j] = D[(int64_t)(k * GJB + i) * ld + ib * GJB + j];
-  else xs[j][i] = D[(int64_t)(ib * GJB + i) * ld + k * GJB + j];
+  if (ib == k && jb == k) {                       // pivot tile <- -P
+    D[(int64_t)(k * GJB + i) * ld + k * GJB + j] = -P[i * GJB + j];
+    return;
+  }
+  if (ib == k) {                                  // panel row (upper orientation) <- R_J
+    D[(int64_t)(k * GJB + i) * ld + jb * GJB + j] = R[(int64_t)i * ld + jb * GJB + j];
+    return;
+  }
+  __shared__ double xs[GJB][GJB + 1], rs[GJB][GJB + 1];
+  if (jb == k) {                                  // panel column (ib < k) <- R_I^T
+    rs[i][j] = R[(int64_t)i * ld + ib * GJB + j];
+    __syncthreads();
+    D[(int64_t)(ib * GJB + i) * ld + k * GJB + j] = rs[j][i];
+    return;
+  }
+  xs[i][j] = Xb[(int64_t)i * ld + ib * GJB + j];  // X_I[m = i][c = j]
   rs[i][j] = R[(int64_t)i * ld + jb * GJB + j];
   __syncthreads();
   double acc = 0.0;
 #pragma unroll 8
   for (int m = 0; m < GJB; ++m) acc = fma(xs[m][i], rs[m][j], acc);
   D[(int64_t)(ib * GJB + i) * ld + jb * GJB + j] -= acc;
-}
-// panel K <- R (stored in the upper orientation), pivot block <- -P
-__global__ void __launch_bounds__(GJB * GJB) k_sw_finish(double* D, int64_t ld, int k,
-                                                        const double* P, const double* R) {
-  const int b = blockIdx.x;
-  const int i = threadIdx.y, j = threadIdx.x;
-  if (b == k) {
-    D[(int64_t)(k * GJB + i) * ld + k * GJB + j] = -P[i * GJB + j];
-  } else if (k < b) {
-    D[(int64_t)(k * GJB + i) * ld + b * GJB + j] = R[(int64_t)i * ld + b * GJB + j];
-  } else {
-    __shared__ double rs[GJB][GJB + 1];
-    rs[i][j] = R[(int64_t)i * ld + b * GJB + j];
-    __syncthreads();
-    D[(int64_t)(b * GJB + i) * ld + k * GJB + j] = rs[j][i];
-  }
 }
 // D <- -D on the upper blocks, mirrored into the lower ones: the full A^-1
 __global__ void __launch_bounds__(GJB * GJB) k_sw_mirror(double* D, int64_t ld) {
@@ -708,17 +713,16 @@ __global__ void __launch_bounds__(GJB * GJB) k_sw_mirror(double* D, int64_t ld) 
 void gj_inverse(double* D, int64_t n, int64_t ld, double* work, cudaStream_t st) {
   TG_REQUIRE(ld % GJB == 0, "dense leading dimension must be a multiple of 32");
   const int nb = (int)(ld / GJB);
-  double* P = work;                 // GJB*GJB
-  double* R = work + GJB * GJB;     // GJB*ld
+  double* P = work;                  // GJB*GJB
+  double* R = work + GJB * GJB;      // GJB*ld
+  double* Xb = R + GJB * ld;         // GJB*ld
   const dim3 thr(GJB, GJB);
   for (int k = 0; k < nb; ++k) {
-    k_gj_pivot<<<1, thr, 0, st>>>(D, ld, k, P);
-    k_sw_rowpanel<<<nb, thr, 0, st>>>(D, ld, k, P, R);
-    k_sw_update<<<dim3(nb, nb), thr, 0, st>>>(D, ld, k, R);
-    k_sw_finish<<<nb, thr, 0, st>>>(D, ld, k, P, R);
+    k_sw_panel<<<nb, thr, 0, st>>>(D, ld, k, P, R, Xb);
+    k_sw_update<<<dim3(nb, nb), thr, 0, st>>>(D, ld, k, P, R, Xb);
   }
   k_sw_mirror<<<dim3(nb, nb), thr, 0, st>>>(D, ld);
-  count_launches(4 * (int64_t)nb);
+  count_launches(2 * (int64_t)nb);
   TG_CHECK_LAUNCH();
 }
 
