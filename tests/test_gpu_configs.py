@@ -36,7 +36,7 @@ def test_cantilever_128x64x64_plain_fp64_4_levels(gpu_lib):
             a, b = plain.step(), mixed.step()
             assert a.rel_res <= 1e-8 and b.rel_res <= 1e-8
             np.testing.assert_allclose(b.obj, a.obj, rtol=1e-7)
-            np.testing.assert_allclose(b.vol, a.vol, rtol=1e-9)
+            np.testing.assert_allclose(b.vol, a.vol, rtol=1e-6)   # OC bisection tolerance
         np.testing.assert_allclose(mixed.get(0), plain.get(0), atol=1e-6)
     finally:
         plain.close()
