@@ -35,7 +35,9 @@ def test_cantilever_128x64x64_plain_fp64_4_levels(gpu_lib):
         for _ in range(3):
             a, b = plain.step(), mixed.step()
             assert a.rel_res <= 1e-8 and b.rel_res <= 1e-8
-            np.testing.assert_allclose(b.obj, a.obj, rtol=1e-7)
+            # two solutions with residuals <= 1e-8 ||f|| differ in compliance by
+            # at most ||u|| ||r1 - r2||, a few 1e-8 ||f|| ||u|| -- not 1e-8 f.u
+            np.testing.assert_allclose(b.obj, a.obj, rtol=1e-6)
             np.testing.assert_allclose(b.vol, a.vol, rtol=1e-6)   # OC bisection tolerance
         np.testing.assert_allclose(mixed.get(0), plain.get(0), atol=1e-6)
     finally:
