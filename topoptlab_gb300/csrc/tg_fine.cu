@@ -285,57 +285,24 @@ constexpr int PITCH = 48;                  // row pitch in words: the two x-rows
 constexpr int PLANE = PX * PITCH;          // words per component plane
 constexpr int NT = EXT * EYT;
 template <int NDOF> __host__ __device__ constexpr int ncopy() { return (NDOF * PX * PY + NT - 1) / NT; }
-// FP32 3-D elasticity runs the element product on the tensor cores (below)
-template <int NDOF, typename T> __host__ __device__ constexpr bool use_tc() {
-  return NDOF == 3 && sizeof(T) == 4;
-}
-// element-output row stride: NT, or NT + 4 for the tensor-core path so that the
-// 4 column pairs of an MMA accumulator fragment land on different banks
-template <int NDOF, typename T> __host__ __device__ constexpr int ystride() {
-  return use_tc<NDOF, T>() ? NT + 4 : NT;
-}
 template <int NDOF, typename T, int KIND> constexpr size_t smem() {
   constexpr int NE = 8 * NDOF;
-  return sizeof(T) * ((size_t)3 * NDOF * PLANE + (size_t)NE * ystride<NDOF, T>() +
-                      (KIND == EK_DENSE ? NE * NE : 0));
+  return sizeof(T) * ((size_t)3 * NDOF * PLANE + (size_t)NE * NT + (KIND == EK_DENSE ? NE * NE : 0));
 }
 }  // namespace zs
 
-// 3xTF32 tensor-core product (hi*hi + hi*lo + lo*hi, FP32 accumulation):
-// error ~2^-21 relative, FP32-level, with mma.sync m16n8k8 on operands held
-// in registers.  x = hi + lo with hi, lo rounded to TF32.
-__device__ __forceinline__ uint32_t tf32_bits(float x) {
-  uint32_t r;
-  asm("cvt.rna.tf32.f32 %0, %1;\n" : "=r"(r) : "f"(x));
-  return r;
-}
-__device__ __forceinline__ void tf32_split(float x, uint32_t& hi, uint32_t& lo) {
-  hi = tf32_bits(x);
-  lo = tf32_bits(x - __uint_as_float(hi));
-}
-__device__ __forceinline__ void mma_tf32(float (&c)[4], const uint32_t (&a)[4], uint32_t b0,
-                                         uint32_t b1) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
-      "{%8,%9}, {%0,%1,%2,%3};\n"
-      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
-
 template <int NDOF, typename T, typename S, int KIND, int MODE>
-__global__ void __launch_bounds__(zs::NT, sizeof(T) == 8 || zs::use_tc<NDOF, T>() ? 2 : 4)
-    k_fine_zstream(ApplyArgs<T, S> a, int zc) {
+__global__ void __launch_bounds__(zs::NT, sizeof(T) == 8 ? 2 : 4) k_fine_zstream(ApplyArgs<T, S> a,
+                                                                                int zc) {
   using namespace zs;
   constexpr int NC = 8;
   constexpr int NE = NC * NDOF;
   constexpr int SLOT = NDOF * PLANE;
   constexpr int NCP = ncopy<NDOF>();
-  constexpr bool TC = use_tc<NDOF, T>();
-  constexpr int YS = ystride<NDOF, T>();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* us = reinterpret_cast<T*>(smem_raw);        // 3 node-plane slots [c][x][PITCH]
-  T* yo = us + 3 * SLOT;                          // element outputs [corner*NDOF+c][YS]
-  T* KEs = yo + NE * YS;                          // dense path only
+  T* yo = us + 3 * SLOT;                          // element outputs [corner*NDOF+c][NT]
+  T* KEs = yo + NE * NT;                          // dense path only
   const Grid& g = a.g;
   const int tid = threadIdx.x;
   const int y0 = blockIdx.x * OY, x0 = blockIdx.y * OX;
@@ -383,35 +350,6 @@ __global__ void __launch_bounds__(zs::NT, sizeof(T) == 8 || zs::use_tc<NDOF, T>(
     return (evalid && ez >= 0 && ez < g.nez) ? load_scale<T, S>(a.scale, ez * lstride + eoff) : T(0);
   };
   const int ubase = exl * PITCH + eyl;
-  // tensor-core path: warp w computes the 32 elements 32w..32w+31 as the rows
-  // of Y = U KE^T (m16n8k8: rows gid, gid+8 of two row tiles; k / n columns
-  // from tig); the B fragments (KE^T, split in hi / lo) stay in registers
-  const int lane = tid & 31, gid = lane >> 2, tig = lane & 3, wbase = tid & ~31;
-  int ubr[4] = {0, 0, 0, 0}, koff[3][2] = {}, kpl[3][2] = {};
-  uint32_t bhi[3][3][2] = {}, blo[3][3][2] = {};
-  if constexpr (TC) {
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int er = wbase + (q >> 1) * 16 + gid + (q & 1) * 8;
-      ubr[q] = (er / EYT) * PITCH + (er % EYT);
-    }
-#pragma unroll
-    for (int kt = 0; kt < 3; ++kt)
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int k = kt * 8 + tig + 4 * h, d = k / 3, c = k % 3;
-        koff[kt][h] = c * PLANE + (d & 1) * PITCH + ((d >> 1) & 1);
-        kpl[kt][h] = d >> 2;
-      }
-#pragma unroll
-    for (int nt = 0; nt < 3; ++nt)
-#pragma unroll
-      for (int kt = 0; kt < 3; ++kt)
-#pragma unroll
-        for (int h = 0; h < 2; ++h)
-          tf32_split((float)a.KE[(nt * 8 + gid) * NE + kt * 8 + tig + 4 * h], bhi[nt][kt][h],
-                     blo[nt][kt][h]);
-  }
   // node owned by this thread (tid < OX*OY)
   const int ox = tid / OY, oy = tid % OY;
   const int nx = x0 + ox, ny = y0 + oy;
@@ -446,43 +384,7 @@ __global__ void __launch_bounds__(zs::NT, sizeof(T) == 8 || zs::use_tc<NDOF, T>(
       }
     }
     const bool lvalid = ez >= 0 && ez < g.nez;   // uniform over the CTA
-    if (TC && lvalid) {
-      const float* P0 = reinterpret_cast<const float*>(us + s0 * SLOT);
-      const float* P1 = reinterpret_cast<const float*>(us + s1 * SLOT);
-#pragma unroll
-      for (int rt = 0; rt < 2; ++rt) {
-        float c[3][4] = {};
-#pragma unroll
-        for (int kt = 0; kt < 3; ++kt) {
-          uint32_t ah[4], al[4];
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {     // a0: (row gid, k0) a1: (gid+8, k0) a2: (gid, k1) a3: (gid+8, k1)
-            const int h = q >> 1, row = rt * 2 + (q & 1);
-            const float* P = kpl[kt][h] ? P1 : P0;
-            tf32_split(P[ubr[row] + koff[kt][h]], ah[q], al[q]);
-          }
-#pragma unroll
-          for (int nt = 0; nt < 3; ++nt) {
-            mma_tf32(c[nt], al, bhi[nt][kt][0], bhi[nt][kt][1]);
-            mma_tf32(c[nt], ah, blo[nt][kt][0], blo[nt][kt][1]);
-            mma_tf32(c[nt], ah, bhi[nt][kt][0], bhi[nt][kt][1]);
-          }
-        }
-        // accumulator (row gid / gid+8, columns 2 tig, 2 tig + 1) times the row's density
-        const float r0 = __shfl_sync(0xffffffffu, (float)rho, rt * 16 + gid);
-        const float r1 = __shfl_sync(0xffffffffu, (float)rho, rt * 16 + gid + 8);
-        const int e0 = wbase + rt * 16 + gid, e1 = e0 + 8;
-        float* yf = reinterpret_cast<float*>(yo);
-#pragma unroll
-        for (int nt = 0; nt < 3; ++nt) {
-          const int col = nt * 8 + 2 * tig;
-          yf[col * YS + e0] = r0 * c[nt][0];
-          yf[(col + 1) * YS + e0] = r0 * c[nt][1];
-          yf[col * YS + e1] = r1 * c[nt][2];
-          yf[(col + 1) * YS + e1] = r1 * c[nt][3];
-        }
-      }
-    } else if (lvalid) {
+    if (lvalid) {
       const T* p0 = us + s0 * SLOT + ubase;
       const T* p1 = us + s1 * SLOT + ubase;
       T ue[NC][NDOF], ye[NC][NDOF];
@@ -498,7 +400,7 @@ __global__ void __launch_bounds__(zs::NT, sizeof(T) == 8 || zs::use_tc<NDOF, T>(
 #pragma unroll
       for (int d = 0; d < NC; ++d)
 #pragma unroll
-        for (int c = 0; c < NDOF; ++c) yo[(d * NDOF + c) * YS + tid] = rho * ye[d][c];
+        for (int c = 0; c < NDOF; ++c) yo[(d * NDOF + c) * NT + tid] = rho * ye[d][c];
     }
     __syncthreads();
     if (nvalid) {
@@ -512,7 +414,7 @@ __global__ void __launch_bounds__(zs::NT, sizeof(T) == 8 || zs::use_tc<NDOF, T>(
           const int e = obase - (d & 1) * EYT - ((d >> 1) & 1);
 #pragma unroll
           for (int c = 0; c < NDOF; ++c) {
-            const T v = yo[(d * NDOF + c) * YS + e];
+            const T v = yo[(d * NDOF + c) * NT + e];
             if (d >> 2) hi[c] += v;
             else acc[c] += v;
           }
@@ -562,7 +464,7 @@ static void launch_zstream(const ApplyArgs<T, S>& a, cudaStream_t st) {
   const int gy = (int)cdiv(a.g.nny, zs::OY), gx = (int)cdiv(a.g.nnx, zs::OX);
   // z chunks: as many as fit in one wave of resident CTAs (4 per SM in FP32,
   // 2 in FP64), so that no second partial wave doubles the kernel time
-  const int target = sm_count() * (sizeof(T) == 8 || zs::use_tc<NDOF, T>() ? 2 : 4);
+  const int target = sm_count() * (sizeof(T) == 8 ? 2 : 4);
   const int cols = gx * gy;
   int chunks = std::max(1, std::min(a.g.nnz, target / cols));
   const int zc = (int)cdiv(a.g.nnz, chunks);
