@@ -17,6 +17,10 @@ namespace tg {
 Ctx::~Ctx() {
   if (g64.exec) cudaGraphExecDestroy(g64.exec);
   if (g32.exec) cudaGraphExecDestroy(g32.exec);
+  for (LoopGraph* l : {&l64, &l32}) {
+    if (l->exec) cudaGraphExecDestroy(l->exec);
+    if (l->graph) cudaGraphDestroy(l->graph);
+  }
   for (Level* l : lv) delete l;
   if (h_oc) cudaFreeHost(h_oc);
   if (h_pcg) cudaFreeHost(h_pcg);
@@ -550,6 +554,83 @@ static void run_iteration(Ctx& c, Ctx::IterGraph& gr, F&& body) {
   if (kind != PK_NONE) prof_collect(gr.prof);
 }
 
+__global__ void k_loop_ctl(PCGState* s, double tol, int maxit) {
+  s->tol = tol;
+  s->maxit = maxit;
+}
+__global__ void k_loop_continue(cudaGraphConditionalHandle h, const PCGState* s) {
+  const double rr = s->rr;
+  const bool cont = isfinite(rr) && sqrt(rr) >= s->tol && s->iter < s->maxit;
+  cudaGraphSetConditional(h, cont ? 1u : 0u);
+}
+
+// Run PCG iterations (body = one iteration, no host read inside) until
+// sqrt(rr) < tol, maxit iterations (counted by the PCG state's iter since
+// its reset) or a non-finite rr: as one WHILE-node graph replay, captured on
+// first use; while a kernel family is event-timed or graphs are off, one
+// iteration at a time from the host.  Leaves the PCG state in h_pcg and
+// returns the number of iterations run.
+template <typename F>
+static int run_loop(Ctx& c, Ctx::IterGraph& gr, Ctx::LoopGraph& lg, double tol, int maxit,
+                    F&& body) {
+  if (maxit <= 0) {
+    read_pcg(c, c.pcg);
+    return 0;
+  }
+  if (!c.use_graphs || prof_kind() != PK_NONE) {
+    int it = 0;
+    while (it < maxit) {
+      run_iteration(c, gr, [&] {
+        body();
+        TG_CUDA(cudaMemcpyAsync(c.h_pcg, c.pcg.p, sizeof(PCGState), cudaMemcpyDeviceToHost, c.st));
+      });
+      ++it;
+      const double rr = c.h_pcg->rr;
+      if (!std::isfinite(rr) || std::sqrt(rr) < tol) break;
+    }
+    return it;
+  }
+  if (!lg.exec) {
+    TG_CUDA(cudaGraphCreate(&lg.graph, 0));
+    TG_CUDA(cudaGraphConditionalHandleCreate(&lg.h, lg.graph, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = lg.h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    TG_CUDA(cudaGraphAddNode(&node, lg.graph, nullptr, nullptr, 0, &np));
+    cudaGraph_t bodyg = np.conditional.phGraph_out[0];
+    const int64_t before = launch_count();
+    TG_CUDA(cudaStreamBeginCaptureToGraph(c.st, bodyg, nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeThreadLocal));
+    try {
+      body();
+      k_loop_continue<<<1, 1, 0, c.st>>>(lg.h, c.pcg);
+      TG_CHECK_LAUNCH();
+    } catch (...) {
+      cudaGraph_t g2 = nullptr;
+      cudaStreamEndCapture(c.st, &g2);
+      cudaGraphDestroy(lg.graph);
+      lg.graph = nullptr;
+      throw;
+    }
+    cudaGraph_t g2 = nullptr;
+    TG_CUDA(cudaStreamEndCapture(c.st, &g2));
+    TG_CUDA(cudaGraphInstantiate(&lg.exec, lg.graph, 0));
+    lg.body_launches = launch_count() - before;
+    count_launches(-lg.body_launches);    // captured, not launched
+  }
+  // the PCG state was reset (iter = 0) by the caller just before the loop
+  k_loop_ctl<<<1, 1, 0, c.st>>>(c.pcg, tol, maxit);
+  TG_CHECK_LAUNCH();
+  TG_CUDA(cudaGraphLaunch(lg.exec, c.st));
+  read_pcg(c, c.pcg);
+  const int it = c.h_pcg->iter;
+  count_launches(lg.body_launches * it);
+  return it;
+}
+
 // plain FP64 PCG (linear_solvers.py:114-134), x in/out
 static int pcg64(Ctx& c, const double* b, double* x, double tol_abs, int maxiter, bool& conv) {
   const int64_t n = c.g.ndofs();
@@ -564,8 +645,8 @@ static int pcg64(Ctx& c, const double* b, double* x, double tol_abs, int maxiter
   // x lives in the caller's buffer; the captured body must not depend on it
   double* xs = c.z2.p;
   TG_CUDA(cudaMemcpyAsync(xs, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, c.st));
-  while (!conv && it < maxiter) {
-    run_iteration(c, c.g64, [&] {
+  if (!conv) {
+    it = run_loop(c, c.g64, c.l64, tol_abs, maxiter, [&] {
       precondition<double>(c, c.r, c.z);
       {
         ProfScope ps(PK_VECTOR, c.st);
@@ -576,9 +657,7 @@ static int pcg64(Ctx& c, const double* b, double* x, double tol_abs, int maxiter
       ProfScope ps(PK_VECTOR, c.st);
       dot<double, double>(n, c.p.p, c.q.p, c.part, c.pcg, DOT_ALPHA, c.st);
       update_xr<double>(n, c.p, c.q, xs, c.r, c.part, c.pcg, c.st);
-      TG_CUDA(cudaMemcpyAsync(c.h_pcg, c.pcg.p, sizeof(PCGState), cudaMemcpyDeviceToHost, c.st));
     });
-    ++it;
     rr = c.h_pcg->rr;
     check_finite(rr, "PCG residual");
     conv = std::sqrt(rr) < tol_abs;
@@ -592,26 +671,19 @@ static int pcg32(Ctx& c, double tol_abs, int maxiter) {
   const int64_t n = c.g.ndofs();
   TG_CUDA(cudaMemsetAsync(c.d32.p, 0, sizeof(float) * n, c.st));
   pcg_reset(c.pcg, c.st);
-  int it = 0;
-  while (it < maxiter) {
-    run_iteration(c, c.g32, [&] {
-      precondition<float>(c, c.r32, c.z32);
-      {
-        ProfScope ps(PK_VECTOR, c.st);
-        dot<float, float>(n, c.r32.p, c.z32.p, c.part, c.pcg, DOT_RHO, c.st);
-        update_p<float>(n, c.z32, c.p32, c.pcg, c.st);
-      }
-      fine_apply<float, float>(c.op, c.s32, c.p32, c.q32, nullptr, nullptr, 0.0, AM_Y, c.st);
+  const int it = run_loop(c, c.g32, c.l32, tol_abs, maxiter, [&] {
+    precondition<float>(c, c.r32, c.z32);
+    {
       ProfScope ps(PK_VECTOR, c.st);
-      dot<float, float>(n, c.p32.p, c.q32.p, c.part, c.pcg, DOT_ALPHA, c.st);
-      update_xr<float>(n, c.p32, c.q32, c.d32, c.r32, c.part, c.pcg, c.st);
-      TG_CUDA(cudaMemcpyAsync(c.h_pcg, c.pcg.p, sizeof(PCGState), cudaMemcpyDeviceToHost, c.st));
-    });
-    ++it;
-    const double rr = c.h_pcg->rr;
-    check_finite(rr, "inner PCG residual");
-    if (std::sqrt(rr) < tol_abs) break;
-  }
+      dot<float, float>(n, c.r32.p, c.z32.p, c.part, c.pcg, DOT_RHO, c.st);
+      update_p<float>(n, c.z32, c.p32, c.pcg, c.st);
+    }
+    fine_apply<float, float>(c.op, c.s32, c.p32, c.q32, nullptr, nullptr, 0.0, AM_Y, c.st);
+    ProfScope ps(PK_VECTOR, c.st);
+    dot<float, float>(n, c.p32.p, c.q32.p, c.part, c.pcg, DOT_ALPHA, c.st);
+    update_xr<float>(n, c.p32, c.q32, c.d32, c.r32, c.part, c.pcg, c.st);
+  });
+  check_finite(c.h_pcg->rr, "inner PCG residual");
   return it;
 }
 

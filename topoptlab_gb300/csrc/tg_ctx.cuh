@@ -97,6 +97,15 @@ struct Ctx {
     int kind = 0;                // profiled family the graph was captured for
     ProfCapture prof;            // its event pairs
   } g64, g32;
+  // the whole PCG loop as one graph: a WHILE conditional node whose body is
+  // one iteration plus a one-thread kernel that sets the condition from the
+  // PCG state on the device (no host round trip per iteration)
+  struct LoopGraph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaGraphConditionalHandle h = 0;
+    int64_t body_launches = 0;   // kernels per iteration
+  } l64, l32;
   bool use_graphs = true;
   struct Cnn* cnn = nullptr;     // learned warm start (not owned)
   // statistics of the last solve

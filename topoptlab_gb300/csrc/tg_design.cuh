@@ -27,6 +27,8 @@ struct PCGState {
   double rho, beta, alpha, pq, rr, bb, rnorm, rinv;
   int iter;
   unsigned int ticket;
+  double tol;        // device-side PCG loop: continue while sqrt(rr) >= tol
+  int maxit;         //   and iter < maxit (and rr finite)
 };
 
 void filter_apply_ex(const Grid& g, const FilterStencil& fs, const double* x, const double* d,
