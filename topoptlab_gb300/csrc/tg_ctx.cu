@@ -453,8 +453,10 @@ template <typename T> void vcycle(Ctx& c, int l, const T* b, T* x) {
     dense_apply<T>(c.Dc, c.nc, c.ldc, b, x, c.gjwork, c.st);   // GJ scratch is idle here
     return;
   }
+  // 2*nsmooth - 1 sweeps swap the buffers an odd number of times: starting in
+  // the scratch buffer ends in x (no copy at the end of the level)
   T* bufs[2] = {x, LvBufs<T>::t(v)};
-  int cur = 0;
+  int cur = 1;
   {
     ProfScope ps(PK_VECTOR, c.st);
     scale_mul<T>(n, c.omega, LvBufs<T>::dinv(v), b, bufs[cur], c.st);

@@ -319,10 +319,26 @@ __global__ void __launch_bounds__(RED_THREADS) k_dot(int64_t n, const TA* __rest
   __shared__ double sh[32];
   __shared__ int last;
   TA acc = TA(0);
+  const int64_t t0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t ts = (int64_t)gridDim.x * blockDim.x;
+  if constexpr (sizeof(TA) == 4 && sizeof(TB) == 4) {
+    // FP32: 16-byte loads (the vectors start at allocation boundaries), scalar tail
+    const int64_t n4 = n / 4;
+    const float4* a4 = reinterpret_cast<const float4*>(a);
+    const float4* b4 = reinterpret_cast<const float4*>(b);
+#pragma unroll 2
+    for (int64_t i = t0; i < n4; i += ts) {
+      const float4 x = a4[i], y = b4[i];
+      acc = fmaf(x.x, y.x, acc);
+      acc = fmaf(x.y, y.y, acc);
+      acc = fmaf(x.z, y.z, acc);
+      acc = fmaf(x.w, y.w, acc);
+    }
+    for (int64_t i = 4 * n4 + t0; i < n; i += ts) acc = fmaf(a[i], b[i], acc);
+  } else {
 #pragma unroll 4
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
-    acc = fma(a[i], (TA)b[i], acc);
+    for (int64_t i = t0; i < n; i += ts) acc = fma(a[i], (TA)b[i], acc);
+  }
   const double s = block_sum((double)acc, sh);
   if (threadIdx.x == 0) {
     part[blockIdx.x] = s;
@@ -363,13 +379,31 @@ template void dot<float, float>(int64_t, const float*, const float*, double*, PC
 template <typename T>
 __global__ void k_update_p(int64_t n, const T* __restrict__ z, T* __restrict__ p, const PCGState* st) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= n) return;
   const T beta = (T)st->beta;
-  p[i] = (st->iter > 0) ? fma(beta, p[i], z[i]) : z[i];
+  const bool first = st->iter == 0;
+  if constexpr (sizeof(T) == 4) {         // thread per 4 values, 16-byte accesses
+    const int64_t n4 = n / 4;
+    if (i < n4) {
+      const float4 zv = reinterpret_cast<const float4*>(z)[i];
+      float4 pv = first ? zv : reinterpret_cast<const float4*>(p)[i];
+      if (!first) {
+        pv.x = fmaf(beta, pv.x, zv.x); pv.y = fmaf(beta, pv.y, zv.y);
+        pv.z = fmaf(beta, pv.z, zv.z); pv.w = fmaf(beta, pv.w, zv.w);
+      }
+      reinterpret_cast<float4*>(p)[i] = pv;
+    } else if (i < n4 + (n - 4 * n4)) {
+      const int64_t j = 4 * n4 + (i - n4);
+      p[j] = first ? z[j] : fma(beta, p[j], z[j]);
+    }
+  } else {
+    if (i >= n) return;
+    p[i] = first ? z[i] : fma(beta, p[i], z[i]);
+  }
 }
 template <typename T>
 void update_p(int64_t n, const T* z, T* p, const PCGState* st, cudaStream_t s) {
-  k_update_p<T><<<(unsigned)cdiv(n, 256), 256, 0, s>>>(n, z, p, st);
+  const int64_t nt = sizeof(T) == 4 ? n / 4 + (n % 4) : n;
+  k_update_p<T><<<(unsigned)cdiv(nt, 256), 256, 0, s>>>(n, z, p, st);
   TG_CHECK_LAUNCH();
 }
 template void update_p<double>(int64_t, const double*, double*, const PCGState*, cudaStream_t);
@@ -384,9 +418,31 @@ __global__ void __launch_bounds__(RED_THREADS) k_update_xr(int64_t n, const T* _
   __shared__ int last;
   const T alpha = (T)st->alpha;
   T acc = T(0);
+  const int64_t t0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t ts = (int64_t)gridDim.x * blockDim.x;
+  int64_t i0 = 0;
+  if constexpr (sizeof(T) == 4) {
+    const int64_t n4 = n / 4;
+    const float4* p4 = reinterpret_cast<const float4*>(p);
+    const float4* q4 = reinterpret_cast<const float4*>(q);
+    float4* x4 = reinterpret_cast<float4*>(x);
+    float4* r4 = reinterpret_cast<float4*>(r);
+    for (int64_t i = t0; i < n4; i += ts) {
+      const float4 pv = p4[i], qv = q4[i];
+      float4 xv = x4[i], rv = r4[i];
+      xv.x = fmaf(alpha, pv.x, xv.x); xv.y = fmaf(alpha, pv.y, xv.y);
+      xv.z = fmaf(alpha, pv.z, xv.z); xv.w = fmaf(alpha, pv.w, xv.w);
+      rv.x = fmaf(-alpha, qv.x, rv.x); rv.y = fmaf(-alpha, qv.y, rv.y);
+      rv.z = fmaf(-alpha, qv.z, rv.z); rv.w = fmaf(-alpha, qv.w, rv.w);
+      x4[i] = xv;
+      r4[i] = rv;
+      acc = fmaf(rv.x, rv.x, acc); acc = fmaf(rv.y, rv.y, acc);
+      acc = fmaf(rv.z, rv.z, acc); acc = fmaf(rv.w, rv.w, acc);
+    }
+    i0 = 4 * n4;
+  }
 #pragma unroll 4
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t i = i0 + t0; i < n; i += ts) {
     x[i] = fma(alpha, p[i], x[i]);
     const T ri = fma(-alpha, q[i], r[i]);
     r[i] = ri;
@@ -457,11 +513,25 @@ template <typename T>
 __global__ void k_scale_mul(int64_t n, T a, const T* __restrict__ d, const T* __restrict__ b,
                             T* __restrict__ x) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i < n) x[i] = a * d[i] * b[i];
+  if constexpr (sizeof(T) == 4) {         // thread per 4 values, 16-byte accesses
+    const int64_t n4 = n / 4;
+    if (i < n4) {
+      const float4 dv = reinterpret_cast<const float4*>(d)[i];
+      const float4 bv = reinterpret_cast<const float4*>(b)[i];
+      reinterpret_cast<float4*>(x)[i] = make_float4(a * dv.x * bv.x, a * dv.y * bv.y,
+                                                    a * dv.z * bv.z, a * dv.w * bv.w);
+    } else if (i < n4 + (n - 4 * n4)) {
+      const int64_t j = 4 * n4 + (i - n4);
+      x[j] = a * d[j] * b[j];
+    }
+  } else {
+    if (i < n) x[i] = a * d[i] * b[i];
+  }
 }
 template <typename T>
 void scale_mul(int64_t n, double a, const T* d, const T* b, T* x, cudaStream_t s) {
-  k_scale_mul<T><<<(unsigned)cdiv(n, 256), 256, 0, s>>>(n, (T)a, d, b, x);
+  const int64_t nt = sizeof(T) == 4 ? n / 4 + (n % 4) : n;
+  k_scale_mul<T><<<(unsigned)cdiv(nt, 256), 256, 0, s>>>(n, (T)a, d, b, x);
   TG_CHECK_LAUNCH();
 }
 template void scale_mul<double>(int64_t, double, const double*, const double*, double*, cudaStream_t);
