@@ -350,6 +350,8 @@ int32_t tg_vcycle(tg_ctx* ctx, const double* xPhys, const double* b, double* x, 
     h2d(c.r.p, b, nd, c.st);
     tg::mask_vec_f64(c.g.nnodes(), c.g.ndof, c.op.fix, c.r, c.st);
     if (precision == TG_PREC_FP64) {
+      TG_REQUIRE(c.precision == TG_PREC_FP64 || c.L == 1,
+                 "an FP64 V-cycle needs an fp64 context (mixed contexts build FP32 levels)");
       tg::vcycle<double>(c, 0, c.r, c.z);
       d2h(x, c.z.p, nd, c.st);
     } else {
@@ -387,7 +389,8 @@ int32_t tg_coarse_stencil(tg_ctx* ctx, const double* xPhys, int32_t level, doubl
     tg::build_hierarchy(c);
     tg::DevBuf<double> full;
     full.alloc(n);
-    tg::stencil_expand(v.g, v.A64, full, c.st);
+    if (c.precision == TG_PREC_MIXED) tg::stencil_expand<float>(v.g, v.A32, full, c.st);
+    else tg::stencil_expand<double>(v.g, v.A64, full, c.st);
     d2h(out, full.p, n, c.st);
   });
 }

@@ -136,6 +136,9 @@ static void setup_element(Ctx& c, const double* KEref) {
   TG_CUDA(cudaMemcpy(c.KE64.p, c.KEh.data(), sizeof(double) * NE * NE, cudaMemcpyHostToDevice));
   TG_CUDA(cudaMemcpy(c.KE32.p, k32.data(), sizeof(float) * NE * NE, cudaMemcpyHostToDevice));
   TG_CUDA(cudaMemcpy(c.Q.p, Qh.data(), sizeof(double) * Qh.size(), cudaMemcpyHostToDevice));
+  std::vector<float> q32(Qh.begin(), Qh.end());
+  c.Q32.alloc((int64_t)q32.size());
+  TG_CUDA(cudaMemcpy(c.Q32.p, q32.data(), sizeof(float) * q32.size(), cudaMemcpyHostToDevice));
   c.op.KE64 = c.KE64.p;
   c.op.KE32 = c.KE32.p;
 }
@@ -283,18 +286,20 @@ void ctx_init(Ctx& c, const tg_problem& p) {
     v.fix.alloc(v.g.nnodes());
     TG_CUDA(cudaMemcpy(v.fix.p, fixl[l].data(), fixl[l].size(), cudaMemcpyHostToDevice));
     const int64_t ns = v.g.nnodes() * stencil_half_dirs(g.ndim) * g.ndof * g.ndof;
+    // mixed precision: the coarse operators (levels >= 1) exist in FP32 only,
+    // built in FP32 for the FP32 V-cycle; the fine level keeps its FP64 data
     const bool last = (l == c.L - 1) && c.precond == TG_PRECOND_GMG;
-    if (l >= 1 || last) v.A64.alloc(ns);
+    if (l >= 1 || last) {
+      if (mixed && l >= 1) v.A32.alloc(ns);
+      else v.A64.alloc(ns);
+    }
     if (!last || l == 0) {
-      v.dinv64.alloc(n); v.t64.alloc(n); v.r64.alloc(n);
-      if (mixed) {
-        v.dinv32.alloc(n); v.t32.alloc(n); v.r32.alloc(n);
-        if (l >= 1) v.A32.alloc(ns);
-      }
+      if (!mixed || l == 0) { v.dinv64.alloc(n); v.t64.alloc(n); v.r64.alloc(n); }
+      if (mixed) { v.dinv32.alloc(n); v.t32.alloc(n); v.r32.alloc(n); }
     }
     if (l >= 1) {
-      v.b64.alloc(n); v.x64.alloc(n);
       if (mixed) { v.b32.alloc(n); v.x32.alloc(n); }
+      else { v.b64.alloc(n); v.x64.alloc(n); }
     }
   }
   c.op.fix = c.lv[0]->fix.p;
@@ -387,21 +392,29 @@ void build_hierarchy(Ctx& c) {
   fine_dinv<double, double>(c.op, c.s64, f.dinv64, c.st);
   if (mixed) fine_dinv<float, __nv_bfloat16>(c.op, c.s16, f.dinv32, c.st);
   if (c.precond != TG_PRECOND_GMG) return;
+  // mixed: level operators in FP32 (they only serve the FP32 V-cycle, which
+  // would round FP64 ones to FP32 anyway); the coarsest matrix is inverted in FP64
   for (int l = 1; l < c.L; ++l) {
     Level& v = *c.lv[l];
-    if (l == 1) build_level1(c.op, c.s64, c.touch, c.Q, v.g, v.fix, v.A64, c.st);
-    else build_galerkin(c.lv[l - 1]->g, c.lv[l - 1]->A64, v.g, v.fix, v.A64, c.st);
-    if (l < c.L - 1) {
-      stencil_dinv<double>(v.g, v.fix, v.A64, v.dinv64, c.st);
-      if (mixed) {
-        d2f(v.A64.n, v.A64, v.A32, c.st);
-        stencil_dinv<float>(v.g, v.fix, v.A32, v.dinv32, c.st);
-      }
+    if (mixed) {
+      if (l == 1) build_level1<float>(c.op, c.s32, c.touch, c.Q32, c.KE32, v.g, v.fix, v.A32, c.st);
+      else build_galerkin<float>(c.lv[l - 1]->g, c.lv[l - 1]->A32, v.g, v.fix, v.A32, c.st);
+      if (l < c.L - 1) stencil_dinv<float>(v.g, v.fix, v.A32, v.dinv32, c.st);
+    } else {
+      if (l == 1) build_level1<double>(c.op, c.s64, c.touch, c.Q, c.KE64, v.g, v.fix, v.A64, c.st);
+      else build_galerkin<double>(c.lv[l - 1]->g, c.lv[l - 1]->A64, v.g, v.fix, v.A64, c.st);
+      if (l < c.L - 1) stencil_dinv<double>(v.g, v.fix, v.A64, v.dinv64, c.st);
     }
   }
   Level& cl = *c.lv[c.L - 1];
-  if (c.L == 1) build_fine_stencil(c.op, c.s64, cl.A64, c.st);
-  stencil_to_dense(cl.g, cl.fix, cl.A64, c.Dc, c.nc, c.ldc, c.st);
+  if (c.L == 1) {
+    build_fine_stencil(c.op, c.s64, cl.A64, c.st);
+    stencil_to_dense<double>(cl.g, cl.fix, cl.A64, c.Dc, c.nc, c.ldc, c.st);
+  } else if (mixed) {
+    stencil_to_dense<float>(cl.g, cl.fix, cl.A32, c.Dc, c.nc, c.ldc, c.st);
+  } else {
+    stencil_to_dense<double>(cl.g, cl.fix, cl.A64, c.Dc, c.nc, c.ldc, c.st);
+  }
   }
   ProfScope ps(PK_COARSE_INV, c.st);
   gj_inverse(c.Dc, c.nc, c.ldc, c.gjwork, c.st);

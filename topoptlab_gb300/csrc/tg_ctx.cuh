@@ -64,6 +64,7 @@ struct Ctx {
   DevBuf<uint8_t> touch;
   DevBuf<int8_t> flags;
   DevBuf<double> KE64, Q;
+  DevBuf<float> Q32;            // Q in FP32 (mixed: coarse operators built in FP32)
   DevBuf<float> KE32;
   DevBuf<double> f, u, x, xPhys, xold, xnew, dc, dcf, dv, Hs, S, s64;
   DevBuf<float> s32;

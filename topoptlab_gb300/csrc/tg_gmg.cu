@@ -197,14 +197,14 @@ __device__ __forceinline__ double pweight(int o, int p, int a, int ndim) {
   return w;
 }
 
-template <int NDIM, int NDOF>
-__global__ void __launch_bounds__(256) k_build_level1(Grid gf, Grid gc, const double* __restrict__ scale,
+template <int NDIM, int NDOF, typename T>
+__global__ void __launch_bounds__(256) k_build_level1(Grid gf, Grid gc, const T* __restrict__ scale,
                                                       const uint8_t* __restrict__ touch,
                                                       const uint8_t* __restrict__ fixf,
-                                                      const double* __restrict__ Q,
-                                                      const double* __restrict__ KE,
+                                                      const T* __restrict__ Q,
+                                                      const T* __restrict__ KE,
                                                       const uint8_t* __restrict__ fixc,
-                                                      double* __restrict__ Ac) {
+                                                      T* __restrict__ Ac) {
   constexpr int NC = 1 << NDIM;
   constexpr int NE = NC * NDOF;
   const int64_t ldc = gc.nnodes();
@@ -216,11 +216,11 @@ __global__ void __launch_bounds__(256) k_build_level1(Grid gf, Grid gc, const do
   node_xyz(gc, I, ix, iy, iz);
   dir_xyz(D, NDIM, dx, dy, dz);
   const int jx = ix + dx, jy = iy + dy, jz = iz + dz;
-  double acc[NDOF][NDOF];
+  T acc[NDOF][NDOF];
 #pragma unroll
   for (int a = 0; a < NDOF; ++a)
 #pragma unroll
-    for (int b = 0; b < NDOF; ++b) acc[a][b] = 0.0;
+    for (int b = 0; b < NDOF; ++b) acc[a][b] = T(0);
   if (in_grid(gc, jx, jy, jz)) {
     const int64_t J = gc.node(jx, jy, jz);
     const int exl = max(max(ix, jx) - 1, 0), exh = min(min(ix, jx), gc.nex - 1);
@@ -237,9 +237,9 @@ __global__ void __launch_bounds__(256) k_build_level1(Grid gf, Grid gc, const do
             const int fx = 2 * ex + (o & 1), fy = 2 * ey + ((o >> 1) & 1);
             const int fz = (NDIM == 3) ? 2 * ez + ((o >> 2) & 1) : 0;
             const int64_t fe = gf.elem(fx, fy, fz);
-            const double rho = scale[fe];
+            const T rho = scale[fe];
             if (!touch[fe]) {
-              const double* Qo = Q + (int64_t)o * NE * NE;
+              const T* Qo = Q + (int64_t)o * NE * NE;
 #pragma unroll
               for (int ci = 0; ci < NDOF; ++ci)
 #pragma unroll
@@ -248,13 +248,13 @@ __global__ void __launch_bounds__(256) k_build_level1(Grid gf, Grid gc, const do
             } else {
               // exact: sum_{p,q} P[p,a] P[q,b] m(p,ci) m(q,cj) KE[(p,ci),(q,cj)]
               for (int p = 0; p < NC; ++p) {
-                const double wp = pweight(o, p, ca, NDIM);
-                if (wp == 0.0) continue;
+                const T wp = (T)pweight(o, p, ca, NDIM);
+                if (wp == T(0)) continue;
                 const uint8_t mp = fixf[gf.node(fx + (p & 1), fy + ((p >> 1) & 1),
                                                  (NDIM == 3) ? fz + ((p >> 2) & 1) : 0)];
                 for (int q = 0; q < NC; ++q) {
-                  const double wq = pweight(o, q, cb, NDIM);
-                  if (wq == 0.0) continue;
+                  const T wq = (T)pweight(o, q, cb, NDIM);
+                  if (wq == T(0)) continue;
                   const uint8_t mq = fixf[gf.node(fx + (q & 1), fy + ((q >> 1) & 1),
                                                    (NDIM == 3) ? fz + ((q >> 2) & 1) : 0)];
                   for (int ci = 0; ci < NDOF; ++ci) {
@@ -274,7 +274,7 @@ __global__ void __launch_bounds__(256) k_build_level1(Grid gf, Grid gc, const do
     for (int ci = 0; ci < NDOF; ++ci)
 #pragma unroll
       for (int cj = 0; cj < NDOF; ++cj)
-        if (((mi >> ci) & 1) || ((mj >> cj) & 1)) acc[ci][cj] = 0.0;
+        if (((mi >> ci) & 1) || ((mj >> cj) & 1)) acc[ci][cj] = T(0);
   }
 #pragma unroll
   for (int ci = 0; ci < NDOF; ++ci)
@@ -282,20 +282,25 @@ __global__ void __launch_bounds__(256) k_build_level1(Grid gf, Grid gc, const do
     for (int cj = 0; cj < NDOF; ++cj) Ac[((DH * NDOF + ci) * NDOF + cj) * ldc + I] = acc[ci][cj];
 }
 
-void build_level1(const FineOp& op, const double* scale, const uint8_t* touch, const double* Q,
-                  const Grid& gc, const uint8_t* fixc, double* Ac, cudaStream_t st) {
+template <typename T>
+void build_level1(const FineOp& op, const T* scale, const uint8_t* touch, const T* Q, const T* KE,
+                  const Grid& gc, const uint8_t* fixc, T* Ac, cudaStream_t st) {
   const int64_t nt = gc.nnodes() * (op.g.ndim == 3 ? 14 : 5);
   const unsigned blocks = (unsigned)cdiv(nt, 256);
   const int key = op.g.ndim * 10 + op.g.ndof;
   switch (key) {
-    case 33: k_build_level1<3, 3><<<blocks, 256, 0, st>>>(op.g, gc, scale, touch, op.fix, Q, op.KE64, fixc, Ac); break;
-    case 31: k_build_level1<3, 1><<<blocks, 256, 0, st>>>(op.g, gc, scale, touch, op.fix, Q, op.KE64, fixc, Ac); break;
-    case 22: k_build_level1<2, 2><<<blocks, 256, 0, st>>>(op.g, gc, scale, touch, op.fix, Q, op.KE64, fixc, Ac); break;
-    case 21: k_build_level1<2, 1><<<blocks, 256, 0, st>>>(op.g, gc, scale, touch, op.fix, Q, op.KE64, fixc, Ac); break;
+    case 33: k_build_level1<3, 3, T><<<blocks, 256, 0, st>>>(op.g, gc, scale, touch, op.fix, Q, KE, fixc, Ac); break;
+    case 31: k_build_level1<3, 1, T><<<blocks, 256, 0, st>>>(op.g, gc, scale, touch, op.fix, Q, KE, fixc, Ac); break;
+    case 22: k_build_level1<2, 2, T><<<blocks, 256, 0, st>>>(op.g, gc, scale, touch, op.fix, Q, KE, fixc, Ac); break;
+    case 21: k_build_level1<2, 1, T><<<blocks, 256, 0, st>>>(op.g, gc, scale, touch, op.fix, Q, KE, fixc, Ac); break;
     default: throw Error{EINVAL_, "unsupported (ndim, nnode_dof)"};
   }
   TG_CHECK_LAUNCH();
 }
+template void build_level1<double>(const FineOp&, const double*, const uint8_t*, const double*,
+                                   const double*, const Grid&, const uint8_t*, double*, cudaStream_t);
+template void build_level1<float>(const FineOp&, const float*, const uint8_t*, const float*,
+                                  const float*, const Grid&, const uint8_t*, float*, cudaStream_t);
 
 // fine-level stencil assembled from the element scale factors (used when the
 // fine grid is itself the coarsest level): A[I][D] = sum_e s_e M KE M
@@ -367,10 +372,10 @@ void build_fine_stencil(const FineOp& op, const double* scale, double* A, cudaSt
 // ---------------------------------------------------------------------------
 // Galerkin product of an assembled stencil
 // ---------------------------------------------------------------------------
-template <int NDIM, int NDOF>
-__global__ void __launch_bounds__(256) k_galerkin(Grid gf, const double* __restrict__ Af, Grid gc,
+template <int NDIM, int NDOF, typename T>
+__global__ void __launch_bounds__(256) k_galerkin(Grid gf, const T* __restrict__ Af, Grid gc,
                                                   const uint8_t* __restrict__ fixc,
-                                                  double* __restrict__ Ac) {
+                                                  T* __restrict__ Ac) {
   const int64_t ldc = gc.nnodes(), ldf = gf.nnodes();
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= ldc * ndir_half<NDIM>()) return;
@@ -380,11 +385,11 @@ __global__ void __launch_bounds__(256) k_galerkin(Grid gf, const double* __restr
   node_xyz(gc, I, ix, iy, iz);
   dir_xyz(D, NDIM, dx, dy, dz);
   const int jx = ix + dx, jy = iy + dy, jz = iz + dz;
-  double acc[NDOF][NDOF];
+  T acc[NDOF][NDOF];
 #pragma unroll
   for (int a = 0; a < NDOF; ++a)
 #pragma unroll
-    for (int b = 0; b < NDOF; ++b) acc[a][b] = 0.0;
+    for (int b = 0; b < NDOF; ++b) acc[a][b] = T(0);
   if (in_grid(gc, jx, jy, jz)) {
     const int64_t J = gc.node(jx, jy, jz);
     for (int al = 0; al < ndir<NDIM>(); ++al) {
@@ -392,7 +397,7 @@ __global__ void __launch_bounds__(256) k_galerkin(Grid gf, const double* __restr
       dir_xyz(al, NDIM, ax, ay, az);
       const int fx = 2 * ix + ax, fy = 2 * iy + ay, fz = 2 * iz + az;
       if (!in_grid(gf, fx, fy, fz)) continue;
-      const double wi = (ax ? 0.5 : 1.0) * (ay ? 0.5 : 1.0) * (az ? 0.5 : 1.0);
+      const T wi = T((ax ? 0.5 : 1.0) * (ay ? 0.5 : 1.0) * (az ? 0.5 : 1.0));
       const int64_t fi = gf.node(fx, fy, fz);
       for (int be = 0; be < ndir<NDIM>(); ++be) {
         int bx, by, bz;
@@ -401,14 +406,14 @@ __global__ void __launch_bounds__(256) k_galerkin(Grid gf, const double* __restr
         const int rx = gx - fx, ry = gy - fy, rz = gz - fz;
         if (rx < -1 || rx > 1 || ry < -1 || ry > 1 || rz < -1 || rz > 1) continue;
         if (!in_grid(gf, gx, gy, gz)) continue;
-        const double w = wi * (bx ? 0.5 : 1.0) * (by ? 0.5 : 1.0) * (bz ? 0.5 : 1.0);
+        const T w = wi * T((bx ? 0.5 : 1.0) * (by ? 0.5 : 1.0) * (bz ? 0.5 : 1.0));
         const int dd = dir_index(rx, ry, rz, NDIM);
         const int64_t gi = gf.node(gx, gy, gz);
 #pragma unroll
         for (int ci = 0; ci < NDOF; ++ci)
 #pragma unroll
           for (int cj = 0; cj < NDOF; ++cj)
-            acc[ci][cj] += w * coef<NDIM, NDOF, double>(Af, ldf, dd, ci, cj, fi, gi);
+            acc[ci][cj] += w * coef<NDIM, NDOF, T>(Af, ldf, dd, ci, cj, fi, gi);
       }
     }
     const uint8_t mi = fixc[I], mj = fixc[J];
@@ -416,7 +421,7 @@ __global__ void __launch_bounds__(256) k_galerkin(Grid gf, const double* __restr
     for (int ci = 0; ci < NDOF; ++ci)
 #pragma unroll
       for (int cj = 0; cj < NDOF; ++cj)
-        if (((mi >> ci) & 1) || ((mj >> cj) & 1)) acc[ci][cj] = 0.0;
+        if (((mi >> ci) & 1) || ((mj >> cj) & 1)) acc[ci][cj] = T(0);
   }
 #pragma unroll
   for (int ci = 0; ci < NDOF; ++ci)
@@ -424,23 +429,28 @@ __global__ void __launch_bounds__(256) k_galerkin(Grid gf, const double* __restr
     for (int cj = 0; cj < NDOF; ++cj) Ac[((DH * NDOF + ci) * NDOF + cj) * ldc + I] = acc[ci][cj];
 }
 
-void build_galerkin(const Grid& gf, const double* Af, const Grid& gc, const uint8_t* fixc,
-                    double* Ac, cudaStream_t st) {
+template <typename T>
+void build_galerkin(const Grid& gf, const T* Af, const Grid& gc, const uint8_t* fixc, T* Ac,
+                    cudaStream_t st) {
   const int64_t nt = gc.nnodes() * (gf.ndim == 3 ? 14 : 5);
   const unsigned blocks = (unsigned)cdiv(nt, 256);
   const int key = gf.ndim * 10 + gf.ndof;
   switch (key) {
-    case 33: k_galerkin<3, 3><<<blocks, 256, 0, st>>>(gf, Af, gc, fixc, Ac); break;
-    case 31: k_galerkin<3, 1><<<blocks, 256, 0, st>>>(gf, Af, gc, fixc, Ac); break;
-    case 22: k_galerkin<2, 2><<<blocks, 256, 0, st>>>(gf, Af, gc, fixc, Ac); break;
-    case 21: k_galerkin<2, 1><<<blocks, 256, 0, st>>>(gf, Af, gc, fixc, Ac); break;
+    case 33: k_galerkin<3, 3, T><<<blocks, 256, 0, st>>>(gf, Af, gc, fixc, Ac); break;
+    case 31: k_galerkin<3, 1, T><<<blocks, 256, 0, st>>>(gf, Af, gc, fixc, Ac); break;
+    case 22: k_galerkin<2, 2, T><<<blocks, 256, 0, st>>>(gf, Af, gc, fixc, Ac); break;
+    case 21: k_galerkin<2, 1, T><<<blocks, 256, 0, st>>>(gf, Af, gc, fixc, Ac); break;
     default: throw Error{EINVAL_, "unsupported (ndim, nnode_dof)"};
   }
   TG_CHECK_LAUNCH();
 }
+template void build_galerkin<double>(const Grid&, const double*, const Grid&, const uint8_t*,
+                                     double*, cudaStream_t);
+template void build_galerkin<float>(const Grid&, const float*, const Grid&, const uint8_t*,
+                                    float*, cudaStream_t);
 
-template <int NDIM, int NDOF>
-__global__ void k_stencil_expand(Grid g, const double* __restrict__ Ah, double* __restrict__ Af) {
+template <int NDIM, int NDOF, typename T>
+__global__ void k_stencil_expand(Grid g, const T* __restrict__ Ah, double* __restrict__ Af) {
   const int64_t ld = g.nnodes();
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= ld * ndir<NDIM>() * NDOF * NDOF) return;
@@ -451,21 +461,24 @@ __global__ void k_stencil_expand(Grid g, const double* __restrict__ Ah, double* 
   node_xyz(g, n, x, y, z);
   dir_xyz(d, NDIM, dx, dy, dz);
   Af[t] = in_grid(g, x + dx, y + dy, z + dz)
-              ? coef<NDIM, NDOF, double>(Ah, ld, d, ci, cj, n, g.node(x + dx, y + dy, z + dz))
+              ? (double)coef<NDIM, NDOF, T>(Ah, ld, d, ci, cj, n, g.node(x + dx, y + dy, z + dz))
               : 0.0;
 }
 
-void stencil_expand(const Grid& g, const double* Ah, double* Af, cudaStream_t st) {
+template <typename T>
+void stencil_expand(const Grid& g, const T* Ah, double* Af, cudaStream_t st) {
   const unsigned blocks = (unsigned)cdiv(g.nnodes() * (g.ndim == 3 ? 27 : 9) * g.ndof * g.ndof, 256);
   switch (g.ndim * 10 + g.ndof) {
-    case 33: k_stencil_expand<3, 3><<<blocks, 256, 0, st>>>(g, Ah, Af); break;
-    case 31: k_stencil_expand<3, 1><<<blocks, 256, 0, st>>>(g, Ah, Af); break;
-    case 22: k_stencil_expand<2, 2><<<blocks, 256, 0, st>>>(g, Ah, Af); break;
-    case 21: k_stencil_expand<2, 1><<<blocks, 256, 0, st>>>(g, Ah, Af); break;
+    case 33: k_stencil_expand<3, 3, T><<<blocks, 256, 0, st>>>(g, Ah, Af); break;
+    case 31: k_stencil_expand<3, 1, T><<<blocks, 256, 0, st>>>(g, Ah, Af); break;
+    case 22: k_stencil_expand<2, 2, T><<<blocks, 256, 0, st>>>(g, Ah, Af); break;
+    case 21: k_stencil_expand<2, 1, T><<<blocks, 256, 0, st>>>(g, Ah, Af); break;
     default: throw Error{EINVAL_, "unsupported (ndim, nnode_dof)"};
   }
   TG_CHECK_LAUNCH();
 }
+template void stencil_expand<double>(const Grid&, const double*, double*, cudaStream_t);
+template void stencil_expand<float>(const Grid&, const float*, double*, cudaStream_t);
 
 // ---------------------------------------------------------------------------
 // transfers
@@ -560,7 +573,8 @@ template void prolong_add<float>(const Grid&, const Grid&, const uint8_t*, const
 // ---------------------------------------------------------------------------
 // coarsest level: dense matrix and blocked Gauss-Jordan inverse (FP64)
 // ---------------------------------------------------------------------------
-__global__ void k_stencil_to_dense(Grid g, const uint8_t* fix, const double* __restrict__ A,
+template <typename T>
+__global__ void k_stencil_to_dense(Grid g, const uint8_t* fix, const T* __restrict__ A,
                                    double* D, int64_t n, int64_t ld) {
   const int64_t ldA = g.nnodes();
   const int C = g.ndim == 3 ? 13 : 4;
@@ -576,7 +590,7 @@ __global__ void k_stencil_to_dense(Grid g, const uint8_t* fix, const double* __r
   dir_xyz(C + dh, g.ndim, dx, dy, dz);
   if (!in_grid(g, ix + dx, iy + dy, iz + dz)) return;
   const int64_t J = g.node(ix + dx, iy + dy, iz + dz);
-  const double v = A[(int64_t)k * ldA + I];
+  const double v = (double)A[(int64_t)k * ldA + I];
   D[(I * ndof + ci) * ld + J * ndof + cj] = v;
   if (dh > 0) D[(J * ndof + cj) * ld + I * ndof + ci] = v;   // mirrored lower block
 }
@@ -592,15 +606,20 @@ __global__ void k_dense_fix_diag(Grid g, const uint8_t* fix, double* D, int64_t 
   if ((fix[node] >> c) & 1) D[r * ld + r] = 1.0;
 }
 
-void stencil_to_dense(const Grid& g, const uint8_t* fix, const double* A, double* D, int64_t n,
+template <typename T>
+void stencil_to_dense(const Grid& g, const uint8_t* fix, const T* A, double* D, int64_t n,
                       int64_t ld, cudaStream_t st) {
   TG_CUDA(cudaMemsetAsync(D, 0, sizeof(double) * ld * ld, st));
   const int64_t nt = g.nnodes() * (g.ndim == 3 ? 14 : 5) * g.ndof * g.ndof;
-  k_stencil_to_dense<<<(unsigned)cdiv(nt, 256), 256, 0, st>>>(g, fix, A, D, n, ld);
+  k_stencil_to_dense<T><<<(unsigned)cdiv(nt, 256), 256, 0, st>>>(g, fix, A, D, n, ld);
   TG_CHECK_LAUNCH();
   k_dense_fix_diag<<<(unsigned)cdiv(ld, 256), 256, 0, st>>>(g, fix, D, n, ld);
   TG_CHECK_LAUNCH();
 }
+template void stencil_to_dense<double>(const Grid&, const uint8_t*, const double*, double*,
+                                       int64_t, int64_t, cudaStream_t);
+template void stencil_to_dense<float>(const Grid&, const uint8_t*, const float*, double*, int64_t,
+                                      int64_t, cudaStream_t);
 
 constexpr int GJB = 32;
 

@@ -74,18 +74,21 @@ template <typename T>
 void stencil_dinv(const Grid& g, const uint8_t* fix, const T* A, T* dinv, cudaStream_t st);
 
 // level-1 stencil straight from element scale factors (exact masked Galerkin)
-void build_level1(const FineOp& op, const double* scale, const uint8_t* elem_touch_fixed,
-                  const double* Q /* [nchild][NE][NE] */, const Grid& gc,
-                  const uint8_t* fixc, double* Ac, cudaStream_t st);
+template <typename T>
+void build_level1(const FineOp& op, const T* scale, const uint8_t* elem_touch_fixed,
+                  const T* Q /* [nchild][NE][NE] */, const T* KE, const Grid& gc,
+                  const uint8_t* fixc, T* Ac, cudaStream_t st);
 // fine-level stencil from the element scale factors (fine grid = coarsest level)
 void build_fine_stencil(const FineOp& op, const double* scale, double* A, cudaStream_t st);
 // Galerkin product of an assembled stencil: Ac = M_c P^T A P M_c
-void build_galerkin(const Grid& gf, const double* Af, const Grid& gc, const uint8_t* fixc,
-                    double* Ac, cudaStream_t st);
+template <typename T>
+void build_galerkin(const Grid& gf, const T* Af, const Grid& gc, const uint8_t* fixc, T* Ac,
+                    cudaStream_t st);
 
 // full 3^ndim-direction layout [(d*ndof+ci)*ndof+cj][node] of a half-stored
 // stencil (diagnostic export)
-void stencil_expand(const Grid& g, const double* Ah, double* Afull, cudaStream_t st);
+template <typename T>
+void stencil_expand(const Grid& g, const T* Ah, double* Afull, cudaStream_t st);
 
 // transfers (masked): bc = Mc P^T rf ;  xf += Mf P xc
 template <typename T>
@@ -96,7 +99,8 @@ void prolong_add(const Grid& gf, const Grid& gc, const uint8_t* fixf, const T* x
                  cudaStream_t st);
 
 // coarsest level: dense matrix (fixed DOFs -> identity) and its inverse
-void stencil_to_dense(const Grid& g, const uint8_t* fix, const double* A, double* D, int64_t n,
+template <typename T>
+void stencil_to_dense(const Grid& g, const uint8_t* fix, const T* A, double* D, int64_t n,
                       int64_t ld, cudaStream_t st);
 void gj_inverse(double* D, int64_t n, int64_t ld, double* work, cudaStream_t st);
 template <typename T>
