@@ -127,9 +127,81 @@ __global__ void __launch_bounds__(NDOF * 256) k_stencil_apply(Grid g, int TY, in
   y[k] = out;
 }
 
+// Small levels (too few (row, node) pairs to hide the coefficient-load
+// latency): three threads per pair, each summing the 9 directions of one
+// neighbour plane (dz = -1, 0, +1; in 2-D three columns dx), the partial sums
+// added in fixed order through shared memory.
+constexpr int SMALL_PAIRS = 128;
+template <int NDIM, int NDOF, typename T, int MODE>
+__global__ void __launch_bounds__(3 * SMALL_PAIRS) k_stencil_small(Grid g, const T* __restrict__ A,
+                                                                  const T* __restrict__ u,
+                                                                  T* __restrict__ y,
+                                                                  const T* __restrict__ b,
+                                                                  const T* __restrict__ dinv,
+                                                                  T omega) {
+  __shared__ T part[3][SMALL_PAIRS];
+  const int slot = threadIdx.x % SMALL_PAIRS, pz = threadIdx.x / SMALL_PAIRS;
+  const int64_t ld = g.nnodes();
+  const int64_t t = blockIdx.x * (int64_t)SMALL_PAIRS + slot;
+  const bool active = t < ld * NDOF;
+  T acc = T(0);
+  int ci = 0;
+  int64_t n = 0;
+  if (active) {
+    ci = (int)(t / ld);
+    n = t - (int64_t)ci * ld;
+    int x, yy, z;
+    node_xyz(g, n, x, yy, z);
+    const int64_t sx = g.nny, sz = (int64_t)g.nny * g.nnx;
+#pragma unroll
+    for (int e = 0; e < 9; ++e) {
+      // 3-D: directions pz*9 + e (dz = pz - 1); 2-D: directions pz*3 + e (dx = pz - 1)
+      if (NDIM == 2 && e >= 3) break;
+      const int d = (NDIM == 3) ? pz * 9 + e : pz * 3 + e;
+      int dx, dy, dz;
+      dir_xyz(d, NDIM, dx, dy, dz);
+      const bool v = in_grid(g, x + dx, yy + dy, z + dz);
+      const int64_t m = v ? n + dz * sz + dx * sx + dy : n;
+#pragma unroll
+      for (int cj = 0; cj < NDOF; ++cj) {
+        const T uu = __ldg(u + m * NDOF + cj);
+        acc = fma(coef<NDIM, NDOF, T>(A, ld, d, ci, cj, n, m), v ? uu : T(0), acc);
+      }
+    }
+  }
+  part[pz][slot] = acc;
+  __syncthreads();
+  if (pz != 0 || !active) return;
+  const T s = (part[0][slot] + part[1][slot]) + part[2][slot];
+  const int64_t k = n * NDOF + ci;
+  T out;
+  if (MODE == AM_Y) out = s;
+  else if (MODE == AM_RES) out = b[k] - s;
+  else out = u[k] + omega * dinv[k] * (b[k] - s);
+  y[k] = out;
+}
+
 template <typename T>
 void stencil_apply(const Grid& g, const T* A, const T* u, T* y, const T* b, const T* dinv,
                    double omega, int mode, cudaStream_t st) {
+  const int64_t pairs = g.nnodes() * g.ndof;
+  if (pairs < 150000) {
+    const unsigned blocks = (unsigned)cdiv(pairs, SMALL_PAIRS);
+#define TG_SS(ND, NF)                                                                          \
+  if (mode == AM_Y) k_stencil_small<ND, NF, T, AM_Y><<<blocks, 3 * SMALL_PAIRS, 0, st>>>(g, A, u, y, b, dinv, (T)omega); \
+  else if (mode == AM_RES) k_stencil_small<ND, NF, T, AM_RES><<<blocks, 3 * SMALL_PAIRS, 0, st>>>(g, A, u, y, b, dinv, (T)omega); \
+  else k_stencil_small<ND, NF, T, AM_JACOBI><<<blocks, 3 * SMALL_PAIRS, 0, st>>>(g, A, u, y, b, dinv, (T)omega);
+    switch (g.ndim * 10 + g.ndof) {
+      case 33: TG_SS(3, 3) break;
+      case 31: TG_SS(3, 1) break;
+      case 22: TG_SS(2, 2) break;
+      case 21: TG_SS(2, 1) break;
+      default: throw Error{EINVAL_, "unsupported (ndim, nnode_dof)"};
+    }
+#undef TG_SS
+    TG_CHECK_LAUNCH();
+    return;
+  }
   const int TY = std::min(g.nny, 256);
   const int TX = std::max(1, std::min(g.nnx, 256 / TY));
   const dim3 grid((unsigned)cdiv(g.nny, TY), (unsigned)cdiv(g.nnx, TX), (unsigned)g.nnz);
