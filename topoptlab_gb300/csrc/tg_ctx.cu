@@ -458,7 +458,7 @@ static void level_apply(Ctx& c, int l, const T* in, T* out, const T* b, int mode
   }
 }
 
-template <typename T> void vcycle(Ctx& c, int l, const T* b, T* x) {
+template <typename T> void vcycle(Ctx& c, int l, const T* b, T* x, bool prescaled) {
   Level& v = *c.lv[l];
   const int64_t n = v.g.ndofs();
   if (l == c.L - 1) {
@@ -470,7 +470,7 @@ template <typename T> void vcycle(Ctx& c, int l, const T* b, T* x) {
   // the scratch buffer ends in x (no copy at the end of the level)
   T* bufs[2] = {x, LvBufs<T>::t(v)};
   int cur = 1;
-  {
+  if (!prescaled) {
     ProfScope ps(PK_VECTOR, c.st);
     scale_mul<T>(n, c.omega, LvBufs<T>::dinv(v), b, bufs[cur], c.st);
   }
@@ -481,11 +481,16 @@ template <typename T> void vcycle(Ctx& c, int l, const T* b, T* x) {
   T* r = LvBufs<T>::r(v);
   level_apply<T>(c, l, bufs[cur], r, b, AM_RES);
   Level& w = *c.lv[l + 1];
+  const bool fuse = l + 1 < c.L - 1;       // the coarsest level has no smoother
   {
     ProfScope ps(PK_TRANSFER, c.st);
-    restrict_<T>(v.g, w.g, w.fix, r, LvBufs<T>::b(w), c.st);
+    if (fuse)
+      restrict_<T>(v.g, w.g, w.fix, r, LvBufs<T>::b(w), c.st, LvBufs<T>::dinv(w), LvBufs<T>::t(w),
+                   c.omega);
+    else
+      restrict_<T>(v.g, w.g, w.fix, r, LvBufs<T>::b(w), c.st);
   }
-  vcycle<T>(c, l + 1, LvBufs<T>::b(w), LvBufs<T>::x(w));
+  vcycle<T>(c, l + 1, LvBufs<T>::b(w), LvBufs<T>::x(w), fuse);
   {
     ProfScope ps(PK_TRANSFER, c.st);
     prolong_add<T>(v.g, w.g, v.fix, LvBufs<T>::x(w), bufs[cur], c.st);
@@ -499,8 +504,8 @@ template <typename T> void vcycle(Ctx& c, int l, const T* b, T* x) {
     TG_CUDA(cudaMemcpyAsync(x, bufs[cur], sizeof(T) * n, cudaMemcpyDeviceToDevice, c.st));
   }
 }
-template void vcycle<double>(Ctx&, int, const double*, double*);
-template void vcycle<float>(Ctx&, int, const float*, float*);
+template void vcycle<double>(Ctx&, int, const double*, double*, bool);
+template void vcycle<float>(Ctx&, int, const float*, float*, bool);
 
 template <typename T>
 static void precondition(Ctx& c, const T* r, T* z) {

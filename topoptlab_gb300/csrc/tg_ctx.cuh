@@ -122,6 +122,8 @@ void build_hierarchy(Ctx& c);     // uses c.s64 / c.s32 / c.s16 of the current x
 void set_density(Ctx& c, const double* xPhys_dev);   // scale factors for xPhys
 // solve K u = b (b, u device FP64, u holds the warm start)
 void solve(Ctx& c, const double* b, double* u);
-template <typename T> void vcycle(Ctx& c, int l, const T* b, T* x);
+// prescaled: the level's scratch buffer already holds omega D^-1 b (fused
+// into the restriction that produced b)
+template <typename T> void vcycle(Ctx& c, int l, const T* b, T* x, bool prescaled = false);
 
 }  // namespace tg

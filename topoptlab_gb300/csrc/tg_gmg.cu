@@ -557,9 +557,13 @@ template void stencil_expand<float>(const Grid&, const float*, double*, cudaStre
 // ---------------------------------------------------------------------------
 // restriction: one thread per (component, coarse node), fully unrolled over
 // the 3^ndim fine nodes of the coarse node's support
+// (optionally fused with the coarse level's first smoothing step from a zero
+// guess, xc = omega * dinvc * bc)
 template <int NDIM, int NDOF, typename T>
 __global__ void __launch_bounds__(256) k_restrict(Grid gf, Grid gc, const uint8_t* fixc,
-                                                  const T* __restrict__ rf, T* __restrict__ bc) {
+                                                  const T* __restrict__ rf, T* __restrict__ bc,
+                                                  const T* __restrict__ dinvc, T* __restrict__ xc,
+                                                  T omega) {
   const int64_t ldc = gc.nnodes();
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= ldc * NDOF) return;
@@ -577,24 +581,28 @@ __global__ void __launch_bounds__(256) k_restrict(Grid gf, Grid gc, const uint8_
     const T w = T((ax ? 0.5 : 1.0) * (ay ? 0.5 : 1.0) * (az ? 0.5 : 1.0));
     acc += w * __ldg(rf + gf.node(fx, fy, fz) * NDOF + c);
   }
-  bc[I * NDOF + c] = ((fixc[I] >> c) & 1) ? T(0) : acc;
+  const T bv = ((fixc[I] >> c) & 1) ? T(0) : acc;
+  bc[I * NDOF + c] = bv;
+  if (xc) xc[I * NDOF + c] = omega * dinvc[I * NDOF + c] * bv;
 }
 
 template <typename T>
 void restrict_(const Grid& gf, const Grid& gc, const uint8_t* fixc, const T* rf, T* bc,
-               cudaStream_t st) {
+               cudaStream_t st, const T* dinvc, T* xc, double omega) {
   const unsigned blocks = (unsigned)cdiv(gc.nnodes() * gc.ndof, 256);
   switch (gf.ndim * 10 + gf.ndof) {
-    case 33: k_restrict<3, 3, T><<<blocks, 256, 0, st>>>(gf, gc, fixc, rf, bc); break;
-    case 31: k_restrict<3, 1, T><<<blocks, 256, 0, st>>>(gf, gc, fixc, rf, bc); break;
-    case 22: k_restrict<2, 2, T><<<blocks, 256, 0, st>>>(gf, gc, fixc, rf, bc); break;
-    case 21: k_restrict<2, 1, T><<<blocks, 256, 0, st>>>(gf, gc, fixc, rf, bc); break;
+    case 33: k_restrict<3, 3, T><<<blocks, 256, 0, st>>>(gf, gc, fixc, rf, bc, dinvc, xc, (T)omega); break;
+    case 31: k_restrict<3, 1, T><<<blocks, 256, 0, st>>>(gf, gc, fixc, rf, bc, dinvc, xc, (T)omega); break;
+    case 22: k_restrict<2, 2, T><<<blocks, 256, 0, st>>>(gf, gc, fixc, rf, bc, dinvc, xc, (T)omega); break;
+    case 21: k_restrict<2, 1, T><<<blocks, 256, 0, st>>>(gf, gc, fixc, rf, bc, dinvc, xc, (T)omega); break;
     default: throw Error{EINVAL_, "unsupported (ndim, nnode_dof)"};
   }
   TG_CHECK_LAUNCH();
 }
-template void restrict_<double>(const Grid&, const Grid&, const uint8_t*, const double*, double*, cudaStream_t);
-template void restrict_<float>(const Grid&, const Grid&, const uint8_t*, const float*, float*, cudaStream_t);
+template void restrict_<double>(const Grid&, const Grid&, const uint8_t*, const double*, double*, cudaStream_t,
+                                const double*, double*, double);
+template void restrict_<float>(const Grid&, const Grid&, const uint8_t*, const float*, float*, cudaStream_t,
+                               const float*, float*, double);
 
 // prolongation: one thread per fine node, all components; the 1, 2, 4 or 8
 // coarse parents follow from the parity of the fine coordinates

@@ -93,7 +93,7 @@ void stencil_expand(const Grid& g, const T* Ah, double* Afull, cudaStream_t st);
 // transfers (masked): bc = Mc P^T rf ;  xf += Mf P xc
 template <typename T>
 void restrict_(const Grid& gf, const Grid& gc, const uint8_t* fixc, const T* rf, T* bc,
-               cudaStream_t st);
+               cudaStream_t st, const T* dinvc = nullptr, T* xc = nullptr, double omega = 0.0);
 template <typename T>
 void prolong_add(const Grid& gf, const Grid& gc, const uint8_t* fixf, const T* xc, T* xf,
                  cudaStream_t st);
