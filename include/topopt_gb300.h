@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define TG_ABI_VERSION 1
+#define TG_ABI_VERSION 2
 
 enum {
   TG_OK = 0,
@@ -72,6 +72,9 @@ typedef struct tg_problem {
   double inner_rtol;     /* mixed precision: FP32 inner solve target (1e-4) */
   int32_t learned;       /* 1: learned warm start (requires tg_cnn_* setup) */
   int32_t device;        /* CUDA device ordinal */
+  int32_t nload;         /* load cases (columns of bcs()'s f, topology_optimization.py:
+                            463-500): f holds nload vectors of ndof one after another;
+                            0 or 1 = one load case */
 } tg_problem;
 
 typedef struct tg_iter_out {

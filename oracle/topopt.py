@@ -268,10 +268,19 @@ def run(nelx, nely, nelz, volfrac, rmin, ft, KE, fixed, f, eps=1e-9, penal=3.0,
     u = np.zeros(ndof)
     out = {"obj": [], "vol": [], "change": [], "g": [], "oc_steps": [], "rec": {}}
     solve = solve or (lambda K, f, free, u0: solve_direct(K, f, free))
+    # several load cases (f with columns): one solve each, compliance and
+    # sensitivities summed over the cases (topology_optimization.py:446-500)
+    fcols = f[:, None] if f.ndim == 1 else f
+    ucols = np.zeros(fcols.shape)
     for loop in range(nouteriter):
         K = assemble(KE, edof, simp(xPhys, eps, penal), ndof)
-        u = solve(K, f, free, u)
-        obj, dc, ce = compliance_sens(xPhys, u, KE, edof, eps, penal)
+        obj, dc = 0.0, np.zeros(nel)
+        for i in range(fcols.shape[1]):
+            ucols[:, i] = solve(K, fcols[:, i], free, ucols[:, i])
+            o_i, dc_i, ce = compliance_sens(xPhys, ucols[:, i], KE, edof, eps, penal)
+            obj += o_i
+            dc += dc_i
+        u = ucols[:, 0] if f.ndim == 1 else ucols.copy()
         dv = np.ones(nel)
         if ft == 0:
             dc = np.asarray(H @ (x * dc)) / Hs / np.maximum(0.001, x)
@@ -308,6 +317,18 @@ def bc_mbb_2d(nelx, nely):
     fixed = np.union1d(np.arange(0, 2 * (nely + 1), 2), [ndof - 1])
     f = np.zeros(ndof)
     f[1] = -1.0
+    return fixed, f
+
+
+def bc_cantilever_2d_twoloads(nelx, nely):
+    """example_bc/lin_elast.py:141-182: left wall clamped; case 0 downward unit
+    load on the last DOF, case 1 upward unit load on the y-DOF of node
+    nelx*(nely+1)."""
+    ndof = 2 * (nelx + 1) * (nely + 1)
+    fixed = np.arange(0, 2 * (nely + 1))
+    f = np.zeros((ndof, 2))
+    f[-1, 0] = -1.0
+    f[2 * nelx * (nely + 1) + 1, 1] = 1.0
     return fixed, f
 
 

@@ -86,4 +86,4 @@ def test_library_loads_and_exports_every_symbol():
     lib = ctypes.CDLL(path)
     for name in _declared_symbols():
         assert hasattr(lib, name), name
-    assert _lib.load().tg_abi_version() == 1
+    assert _lib.load().tg_abi_version() == 2

@@ -36,7 +36,7 @@ class TgProblem(C.Structure):
         ("precond", C.c_int32), ("precision", C.c_int32), ("nlevels", C.c_int32),
         ("nsmooth", C.c_int32), ("omega", C.c_double), ("rtol", C.c_double),
         ("maxiter", C.c_int32), ("inner_rtol", C.c_double), ("learned", C.c_int32),
-        ("device", C.c_int32),
+        ("device", C.c_int32), ("nload", C.c_int32),
     ]
 
 

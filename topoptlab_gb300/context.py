@@ -50,9 +50,15 @@ class GpuProblem:
         self.nnode_dof = ne // 2 ** self.ndim
         nn = (nelx + 1) * (nely + 1) * ((nelz + 1) if self.ndim == 3 else 1)
         self.ndof = nn * self.nnode_dof
-        f = _lib.f64(f).reshape(-1)
-        if f.shape[0] != self.ndof:
-            raise ValueError(f"load vector has {f.shape[0]} entries, expected {self.ndof}")
+        # f: (ndof,) or (ndof, nload) -- one column per load case, passed to
+        # the library as nload vectors one after another
+        f = np.asarray(f, dtype=np.float64)
+        if f.ndim == 1:
+            f = f[:, None]
+        if f.ndim != 2 or f.shape[0] != self.ndof:
+            raise ValueError(f"load vector has shape {f.shape}, expected ({self.ndof}, nload)")
+        self.nload = f.shape[1]
+        f = np.ascontiguousarray(f.T).reshape(-1)
         fixed = np.ascontiguousarray(np.asarray(fixed, dtype=np.int64).reshape(-1))
         if precision not in PRECISIONS:
             raise ValueError(f"Unknown precision: {precision}")
@@ -80,6 +86,7 @@ class GpuProblem:
         p.rtol, p.maxiter, p.inner_rtol = rtol, maxiter, inner_rtol
         p.learned = int(bool(learned))
         p.device = device
+        p.nload = self.nload
         h = C.c_void_p()
         rc = self._lib.tg_create(C.byref(p), C.byref(h))
         _lib.check(rc, None, "tg_create")
@@ -106,13 +113,21 @@ class GpuProblem:
         return IterResult(*(getattr(out, k) for k, _ in _lib.TgIterOut._fields_))
 
     def get(self, field: int) -> np.ndarray:
-        n = self.ndof if field in (_lib.TG_FIELD_U, _lib.TG_FIELD_F) else self.nel
+        """Element fields: (nel,); u and f: (ndof,) for one load case, else
+        (ndof, nload)."""
+        nodes = field in (_lib.TG_FIELD_U, _lib.TG_FIELD_F)
+        n = self.ndof * self.nload if nodes else self.nel
         a = np.empty(n)
         self._check(self._lib.tg_get(self._h, field, _lib.dptr(a), n), "tg_get")
+        if nodes and self.nload > 1:
+            return np.ascontiguousarray(a.reshape(self.nload, self.ndof).T)
         return a
 
     def set(self, field: int, values) -> None:
-        a = _lib.f64(values).reshape(-1)
+        a = np.asarray(values, dtype=np.float64)
+        if a.ndim == 2 and field in (_lib.TG_FIELD_U, _lib.TG_FIELD_F):
+            a = a.T                                     # (ndof, nload) -> load cases first
+        a = np.ascontiguousarray(a).reshape(-1)
         self._check(self._lib.tg_set(self._h, field, _lib.dptr(a), a.shape[0]), "tg_set")
 
     # unit entry points -------------------------------------------------

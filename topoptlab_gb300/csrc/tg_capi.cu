@@ -48,10 +48,11 @@ void d2h(T* dst, const T* src, int64_t n, cudaStream_t st) {
   TG_CUDA(cudaStreamSynchronize(st));
 }
 
-// device array of a field; n = its length in the caller's numbering
+// device array of a field; n = its length in the caller's numbering (u and f:
+// all load cases, one vector after another)
 double* field_ptr(tg::Ctx& c, int32_t field, int64_t& n, bool& nodes) {
   nodes = field == TG_FIELD_U || field == TG_FIELD_F;
-  n = nodes ? c.rg.ndofs() : c.rg.nel();
+  n = nodes ? c.rg.ndofs() * c.nload : c.rg.nel();
   switch (field) {
     case TG_FIELD_X: return c.x;
     case TG_FIELD_XPHYS: return c.xPhys;
@@ -166,7 +167,9 @@ int32_t tg_get(tg_ctx* ctx, int32_t field, double* host, int64_t n) {
     bool nodes = false;
     double* p = field_ptr(ctx->c, field, m, nodes);
     TG_REQUIRE(n == m, "tg_get: wrong element count");
-    get_field(ctx->c, host, p, nodes);
+    const int nv = nodes ? ctx->c.nload : 1;
+    for (int k = 0; k < nv; ++k)
+      get_field(ctx->c, host + k * (m / nv), p + k * ctx->c.g.ndofs(), nodes);
   });
 }
 
@@ -178,9 +181,11 @@ int32_t tg_set(tg_ctx* ctx, int32_t field, const double* host, int64_t n) {
     bool nodes = false;
     double* p = field_ptr(c, field, m, nodes);
     TG_REQUIRE(n == m, "tg_set: wrong element count");
-    put_field(c, p, host, nodes);
+    const int nv = nodes ? c.nload : 1;
+    for (int k = 0; k < nv; ++k) put_field(c, p + k * c.g.ndofs(), host + k * (m / nv), nodes);
     if (field == TG_FIELD_F || field == TG_FIELD_U)
-      tg::mask_vec_f64(c.g.nnodes(), c.g.ndof, c.op.fix, p, c.st);
+      for (int k = 0; k < c.nload; ++k)
+        tg::mask_vec_f64(c.g.nnodes(), c.g.ndof, c.op.fix, p + k * c.g.ndofs(), c.st);
     TG_CUDA(cudaStreamSynchronize(c.st));
   });
 }

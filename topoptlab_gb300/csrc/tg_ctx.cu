@@ -215,6 +215,7 @@ void ctx_init(Ctx& c, const tg_problem& p) {
   c.maxiter = p.maxiter > 0 ? p.maxiter : 2000;
   c.inner_rtol = p.inner_rtol > 0 ? p.inner_rtol : 1e-4;
   c.learned = p.learned;
+  c.nload = p.nload > 1 ? p.nload : 1;
   const Grid& g = c.g;
   const int64_t nn = g.nnodes(), nd = g.ndofs(), nel = g.nel();
   c.op.g = g;
@@ -316,7 +317,7 @@ void ctx_init(Ctx& c, const tg_problem& p) {
   }
   if (c.padded) c.emb.alloc(std::max(rnd, rnel));
   // vectors
-  c.f.alloc(nd); c.u.alloc(nd);
+  c.f.alloc(nd * c.nload); c.u.alloc(nd * c.nload);
   c.x.alloc(nel); c.xPhys.alloc(nel); c.xold.alloc(nel); c.xnew.alloc(nel);
   c.dc.alloc(nel); c.dcf.alloc(nel); c.dv.alloc(nel); c.Hs.alloc(nel); c.S.alloc(3 * nel);
   c.s64.alloc(nel);
@@ -330,16 +331,20 @@ void ctx_init(Ctx& c, const tg_problem& p) {
   TG_CUDA(cudaMallocHost(&c.h_pcg, sizeof(PCGState)));
   TG_CUDA(cudaMallocHost(&c.h_scal, 8 * sizeof(double)));
 
-  // load (masked to the free DOFs) and its norm
-  std::vector<double> fh(nd, 0.0);
-  for (int64_t i = 0; i < rnd; ++i) fh[dev_node(i / g.ndof) * g.ndof + i % g.ndof] = p.f[i];
-  double bb = 0.0;
-  for (int64_t i = 0; i < nd; ++i) {
-    if ((fix[i / g.ndof] >> (i % g.ndof)) & 1) fh[i] = 0.0;
-    bb += fh[i] * fh[i];
+  // loads (masked to the free DOFs), one device vector per load case
+  for (int lc = 0; lc < c.nload; ++lc) {
+    std::vector<double> fh(nd, 0.0);
+    const double* fsrc = p.f + (int64_t)lc * rnd;
+    for (int64_t i = 0; i < rnd; ++i) fh[dev_node(i / g.ndof) * g.ndof + i % g.ndof] = fsrc[i];
+    double bb = 0.0;
+    for (int64_t i = 0; i < nd; ++i) {
+      if ((fix[i / g.ndof] >> (i % g.ndof)) & 1) fh[i] = 0.0;
+      bb += fh[i] * fh[i];
+    }
+    if (lc == 0) c.bnorm = std::sqrt(bb);
+    TG_CUDA(cudaMemcpy(c.f.p + (int64_t)lc * nd, fh.data(), sizeof(double) * nd,
+                       cudaMemcpyHostToDevice));
   }
-  c.bnorm = std::sqrt(bb);
-  TG_CUDA(cudaMemcpy(c.f.p, fh.data(), sizeof(double) * nd, cudaMemcpyHostToDevice));
   c.u.zero(c.st);
 
   // filter stencil weights and the normaliser Hs (filter/matrix_filter.py:185-231)
@@ -795,17 +800,31 @@ void ctx_step(Ctx& c, tg_iter_out& out) {
   // learned warm start (falls back to the previous displacement when its
   // residual is not smaller); the solve below is unchanged either way
   int fallback = 0;
-  if (c.learned && c.cnn && c.cnn->trained && c.iter > 0) {
+  if (c.learned && c.cnn && c.cnn->trained && c.iter > 0 && c.nload == 1) {
     ProfScope ps(PK_LEARNED, c.st);
     fallback = c.cnn->warm_start(c);
   }
-  solve(c, c.f, c.u);
+  // one solve per load case with the same hierarchy (topology_optimization.py:446-459)
+  const int64_t nd = g.ndofs();
+  int iters = 0, vcycles = 0, refine = 0;
+  double relres = 0.0;
+  for (int lc = 0; lc < c.nload; ++lc) {
+    solve(c, c.f.p + lc * nd, c.u.p + lc * nd);
+    iters += c.last_iters;
+    vcycles += c.last_vcycles;
+    refine += c.last_refine;
+    relres = std::max(relres, c.last_relres);
+  }
   TG_CUDA(cudaEventRecord(c.ev1, c.st));
   // compliance + raw sensitivity
   const int nbe = (int)red_blocks(nel);
   {
     ProfScope ps(PK_COMPLIANCE, c.st);
-    fine_compliance(c.op, c.xPhys, c.u, c.eps, c.penal, c.dc, c.part, c.st, c.flags.p);
+    // compliance and sensitivities summed over the load cases in fixed order
+    // (topology_optimization.py:463-500; compliance is self-adjoint)
+    for (int lc = 0; lc < c.nload; ++lc)
+      fine_compliance(c.op, c.xPhys, c.u.p + lc * nd, c.eps, c.penal, c.dc, c.part, c.st,
+                      c.flags.p, lc > 0);
     reduce_partials(c.part, nbe, c.scal.p + 0, false, c.st);
   }
   // sensitivity filter
@@ -842,10 +861,10 @@ void ctx_step(Ctx& c, tg_iter_out& out) {
   out.vol = vol_sum / (double)c.rg.nel();   // padding elements hold 0
   out.change = c.h_scal[2];
   out.g = c.g_oc;
-  out.rel_res = c.last_relres;
-  out.pcg_iters = c.last_iters;
-  out.vcycles = c.last_vcycles;
-  out.refinements = c.last_refine;
+  out.rel_res = relres;
+  out.pcg_iters = iters;
+  out.vcycles = vcycles;
+  out.refinements = refine;
   out.oc_steps = c.h_oc->nsteps;
   out.fallback = fallback;
   out.nlevels = c.L;

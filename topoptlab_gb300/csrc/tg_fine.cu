@@ -607,7 +607,8 @@ __global__ void __launch_bounds__(RED_THREADS) k_compliance(Grid g, const double
                                                            Sector<double> B, double eps,
                                                            double penal, double* dc,
                                                            double* partial,
-                                                           const int8_t* __restrict__ flags) {
+                                                           const int8_t* __restrict__ flags,
+                                                           int accumulate) {
   constexpr int NC = 1 << NDIM;
   constexpr int NE = NC * NDOF;
   __shared__ double sh[32];
@@ -619,7 +620,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_compliance(Grid g, const double
     const int ex = (int)((e / g.ney) % g.nex);
     const int ez = (int)(e / ((int64_t)g.ney * g.nex));
     if (flags && flags[e] == EL_OUTSIDE) {
-      dc[e] = 0.0;
+      if (!accumulate) dc[e] = 0.0;
       continue;
     }
     double ue[NC][NDOF];
@@ -660,25 +661,26 @@ __global__ void __launch_bounds__(RED_THREADS) k_compliance(Grid g, const double
       xpm1 = pow(xv, penal - 1.0);
     }
     objp += (eps + (1.0 - eps) * xp) * ce;
-    dc[e] = -(penal * (1.0 - eps) * xpm1) * ce;
+    const double dce = -(penal * (1.0 - eps) * xpm1) * ce;
+    dc[e] = accumulate ? dc[e] + dce : dce;
   }
   const double s = block_sum(objp, sh);
-  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+  if (threadIdx.x == 0) partial[blockIdx.x] = accumulate ? partial[blockIdx.x] + s : s;
 }
 
 void fine_compliance(const FineOp& op, const double* xPhys, const double* u, double eps,
                      double penal, double* dc, double* partial, cudaStream_t st,
-                     const int8_t* flags) {
+                     const int8_t* flags, bool accumulate) {
   const int64_t nel = op.g.nel();
   const unsigned blocks = red_blocks(nel);
   const int key = op.g.ndim * 10 + op.g.ndof;
 #define TG_COMP(ND, NF)                                                                     \
   if (op.sector)                                                                            \
     k_compliance<ND, NF, true><<<blocks, RED_THREADS, 0, st>>>(op.g, xPhys, u, op.KE64,      \
-                                                              op.B64, eps, penal, dc, partial, flags); \
+                                                              op.B64, eps, penal, dc, partial, flags, accumulate ? 1 : 0); \
   else                                                                                      \
     k_compliance<ND, NF, false><<<blocks, RED_THREADS, 0, st>>>(op.g, xPhys, u, op.KE64,     \
-                                                               op.B64, eps, penal, dc, partial, flags);
+                                                               op.B64, eps, penal, dc, partial, flags, accumulate ? 1 : 0);
   switch (key) {
     case 33: TG_COMP(3, 3) break;
     case 31: TG_COMP(3, 1) break;

@@ -56,9 +56,10 @@ constexpr int8_t EL_OUTSIDE = 3;
 // ce_e = u_e^T KE u_e ;  dc_e = -penal (1-eps) x^(penal-1) ce_e ;
 // partial[b] = sum over the block's elements of simp(x_e) ce_e (padding
 // elements, flag EL_OUTSIDE, contribute nothing and get dc = 0)
+// (accumulate: dc and partial are added to, for a further load case)
 void fine_compliance(const FineOp& op, const double* xPhys, const double* u, double eps,
                      double penal, double* dc, double* partial, cudaStream_t st,
-                     const int8_t* flags = nullptr);
+                     const int8_t* flags = nullptr, bool accumulate = false);
 
 // ---------------------------------------------------------------------------
 // assembled 3^ndim-point block stencils (coarse levels)

@@ -4,9 +4,11 @@
 The driver also accepts the reference's own callables unchanged; these are
 the ones a GPU machine without the reference package uses.
 
-  mbb_2d         example_bc/lin_elast.py:6-46
-  cantilever_3d  example_bc/lin_elast.py:274-338
-  heatplate_2d   example_bc/heat_conduction.py:5-49
+  mbb_2d                  example_bc/lin_elast.py:6-46
+  cantilever_2d           example_bc/lin_elast.py:100-139
+  cantilever_2d_twoloads  example_bc/lin_elast.py:141-182 (two load cases)
+  cantilever_3d           example_bc/lin_elast.py:274-338
+  heatplate_2d            example_bc/heat_conduction.py:5-49
 """
 from __future__ import annotations
 
@@ -20,6 +22,27 @@ def mbb_2d(nelx, nely, ndof, **kwargs):
     u = np.zeros((ndof, 1))
     fixed = np.union1d(np.arange(0, 2 * (nely + 1), 2), np.array([ndof - 1]))
     f[1, 0] = -1.0
+    return u, f, fixed, np.setdiff1d(np.arange(ndof), fixed), None
+
+
+def cantilever_2d(nelx, nely, ndof, **kwargs):
+    """All DOFs of the left wall fixed; unit downward load on the last DOF
+    (the y-DOF of the bottom-right node)."""
+    f = np.zeros((ndof, 1))
+    u = np.zeros((ndof, 1))
+    fixed = np.arange(0, 2 * (nely + 1))
+    f[-1, 0] = -1.0
+    return u, f, fixed, np.setdiff1d(np.arange(ndof), fixed), None
+
+
+def cantilever_2d_twoloads(nelx, nely, ndof, **kwargs):
+    """Left wall fixed; two load cases: downward unit load at the bottom-right
+    node, upward unit load at the top-right node (y-DOF of node nelx*(nely+1))."""
+    f = np.zeros((ndof, 2))
+    u = np.zeros((ndof, 2))
+    fixed = np.arange(0, 2 * (nely + 1))
+    f[-1, 0] = -1.0
+    f[2 * nelx * (nely + 1) + 1, 1] = 1.0
     return u, f, fixed, np.setdiff1d(np.arange(ndof), fixed), None
 
 

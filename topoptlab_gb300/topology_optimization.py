@@ -8,7 +8,7 @@ compliance of the last solved design), same per-iteration log line
 
 Supported: quad4 / hex8 structured grids, ``lk`` callables returning the
 element matrix (elasticity or Poisson), ``bcs`` callables of the reference
-example_bc signature with one load case and no springs, ``ft`` in {-1, 0, 1}
+example_bc signature (any number of load cases, no springs), ``ft`` in {-1, 0, 1}
 with ``filter_mode`` "matrix" or "convolution" (identical operators),
 ``optimizer="oc"``, SIMP (``matinterpol_kw`` eps / penal), ``el_flags``.
 Anything else raises ValueError, as the reference does for unknown options
@@ -167,9 +167,11 @@ def main(nelx: int, nely: int,
     if springs is not None:
         raise ValueError("springs are not supported by the GPU path")
     f = np.asarray(f, dtype=np.float64)
-    if f.ndim == 2 and f.shape[1] != 1:
-        raise ValueError("the GPU path solves one load case (f must have one column)")
-    prob = GpuProblem(nelx, nely, nelz, KE, fixed, f.reshape(-1), volfrac, rmin, ft=int(ft),
+    if f.ndim == 1:
+        f = f[:, None]
+    # several columns = several load cases: one solve each, compliance and
+    # sensitivities summed (topology_optimization.py:446-500)
+    prob = GpuProblem(nelx, nely, nelz, KE, fixed, f, volfrac, rmin, ft=int(ft),
                       eps=eps, penal=penal, el_flags=el_flags, device=device, **opts)
     obj = 0.0
     try:
