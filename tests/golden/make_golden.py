@@ -17,6 +17,9 @@ Outputs (small .npz files, committed):
   heat2d_40x40.npz heat plate 40x40, ft=0, OC (Poisson KE)
   mbb2d_60x20_ft0.npz  MBB beam 60x20 with the sensitivity filter
   cant3d_12x6x6.npz    3-D cantilever (reference callable), ft=1, 12 iterations
+  vtk.npz          what the reference's export_vtk hands to meshio (points,
+                   cells, point and cell data) for a 2-D and a 3-D grid, seeded
+                   fields, recorded through a stand-in for meshio.Mesh
 """
 import os
 import sys
@@ -71,6 +74,7 @@ from topoptlab.example_bc.lin_elast import mbb_2d, cantilever_3d  # noqa: E402
 from topoptlab.example_bc.heat_conduction import heatplate_2d  # noqa: E402
 from topoptlab.objectives import compliance  # noqa: E402
 from topoptlab.optimizer.optimality_criterion import oc_top88  # noqa: E402
+import topoptlab.output_designs as OD  # noqa: E402
 
 OUT_KW = {"file": None, "display": False, "export": False, "write_log": False,
           "profile": False, "debug": 0}
@@ -167,7 +171,48 @@ def run_traced(name, snap_its, **kw):
     return x, obj, it["k"]
 
 
+class _MeshRecorder:
+    """Stand-in for meshio.Mesh: keeps what export_vtk passes to it."""
+    last = None
+
+    def __init__(self, points, cells, point_data=None, cell_data=None):
+        _MeshRecorder.last = dict(points=np.asarray(points), cells=cells,
+                                  point_data=point_data or {}, cell_data=cell_data or {})
+
+    def write(self, filename):
+        _MeshRecorder.last["filename"] = filename
+
+
+def gen_vtk():
+    OD.Mesh = _MeshRecorder
+    rng = np.random.default_rng(7)
+    d = {}
+    for tag, (nx, ny, nz, nd) in {"2d": (4, 3, None, 2), "3d": (3, 2, 2, 3)}.items():
+        nel = nx * ny * (nz or 1)
+        nnodes = (nx + 1) * (ny + 1) * ((nz or 0) + 1)
+        xPhys = rng.uniform(0, 1, (nel, 1))
+        x = rng.uniform(0, 1, (nel, 1))
+        u = rng.standard_normal((nnodes * nd, 2))
+        f = rng.standard_normal((nnodes * nd, 2))
+        OD.export_vtk(filename="out", nelx=nx, nely=ny, nelz=nz, xPhys=xPhys, x=x, u=u, f=f,
+                      volfrac=0.4)
+        m = _MeshRecorder.last
+        d[f"{tag}_points"] = m["points"]
+        d[f"{tag}_cells"] = np.asarray(m["cells"][0][1])
+        d[f"{tag}_celltype"] = np.array(m["cells"][0][0])
+        for k, v in m["point_data"].items():
+            d[f"{tag}_pd_{k}"] = np.asarray(v)
+        for k, v in m["cell_data"].items():
+            d[f"{tag}_cd_{k}"] = np.asarray(v[0])
+        d[f"{tag}_in_xPhys"], d[f"{tag}_in_x"], d[f"{tag}_in_u"], d[f"{tag}_in_f"] = xPhys, x, u, f
+    np.savez_compressed(os.path.join(HERE, "vtk.npz"), **d)
+
+
 def main():
+    if len(sys.argv) > 2 and sys.argv[2] == "vtk":
+        gen_vtk()
+        return
+    gen_vtk()
     gen_elements()
     gen_filters()
     r = run_traced("mbb2d_60x20.npz", {0, 1, 2, 24, 143},

@@ -141,3 +141,21 @@ def test_nan_density_raises(gpu_lib):
             prob.step()
     finally:
         prob.close()
+
+
+def test_main_exports_vtk(gpu_lib, tmp_path):
+    """output_kw export / output_movie write the reference's VTK files: one per
+    design iteration, named file_<iteration>, and the final design as file.vtk,
+    whose xPhys cell data is the returned design's filtered density."""
+    from topoptlab_gb300 import main
+    from topoptlab_gb300.example_bc import mbb_2d
+    name = str(tmp_path / "mbb")
+    out = dict(OUT, file=name, export=True, output_movie=True)
+    x, _ = main(nelx=12, nely=4, volfrac=0.5, rmin=1.5, ft=1, optimizer="oc", bcs=mbb_2d,
+                nouteriter=5, output_kw=out)
+    assert (tmp_path / "mbb.vtk").exists()
+    assert sorted(p.name for p in tmp_path.glob("mbb_*.vtk")) == [f"mbb_{i}.vtk" for i in range(5)]
+    txt = (tmp_path / "mbb.vtk").read_text()
+    assert "CELLS 48 240" in txt and "POINTS 65 double" in txt
+    for field in ("u0", "f0", "xPhys", "x", "xThresh"):
+        assert f" {field} " in txt

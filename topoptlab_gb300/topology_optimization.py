@@ -38,6 +38,7 @@ from .example_bc import mbb_2d
 from .log_utils import EmptyLogger, SimpleLogger
 from .material_interpolation import simp, simp_dx
 from .objectives import compliance
+from .output_designs import export_vtk
 from .utils import default_outputkw, check_output_kw, check_simulation_params
 
 _DIRECT = {"scipy-direct", "scipy-lu", "cvxopt-cholmod"}
@@ -174,19 +175,28 @@ def main(nelx: int, nely: int,
     prob = GpuProblem(nelx, nely, nelz, KE, fixed, f, volfrac, rmin, ft=int(ft),
                       eps=eps, penal=penal, el_flags=el_flags, device=device, **opts)
     obj = 0.0
+
+    def export(name):
+        # output_designs.export_vtk with the fields the reference exports (:663-680)
+        export_vtk(filename=name, nelx=nelx, nely=nely, nelz=nelz,
+                   xPhys=prob.get(_lib.TG_FIELD_XPHYS), x=prob.get(_lib.TG_FIELD_X),
+                   u=prob.get(_lib.TG_FIELD_U).reshape(ndof, -1), f=f, volfrac=volfrac)
+
     try:
         for loop in range(nouteriter):
             it = prob.step()
             obj = it.obj
             log.perf(f"PCGit. {it.pcg_iters} rel.res. {it.rel_res:.3e} "
                      f"vcycles {it.vcycles} refinements {it.refinements}")
+            if output_kw.get("output_movie"):
+                export("_".join([output_kw["file"], str(loop).zfill(len(str(nouteriter)))]))
             log.info("it.: {0} obj.: {1:.10f} vol.: {2:.10f} ch.: {3:.10f}".format(
                 loop + 1, obj, it.vol, it.change))
             if it.change < 0.01:
                 break
         x = prob.get(_lib.TG_FIELD_X)
+        if output_kw["export"]:
+            export(output_kw["file"])
     finally:
         prob.close()
-    if output_kw["export"]:
-        warnings.warn("VTK export is not implemented on the GPU path; skipped")
     return x.reshape(-1, 1), obj
