@@ -100,6 +100,31 @@ def ke_poisson(ndim, k=1.0, l=None):
     return k * _integrate(corners, l, lambda dN: dN @ dN.T)
 
 
+def _shape(corners, xi):
+    """N_k(xi) for multilinear shape functions on [-1,1]^d."""
+    return np.array([np.prod([0.5 * (1 + (2 * ci - 1) * xi[a]) for a, ci in enumerate(c)])
+                     for c in corners])
+
+
+def ke_mass(ndim, rho=1.0, l=None):
+    """Consistent scalar mass matrix rho * int N N^T (elements/mass_scalar_2d.py:68-110,
+    mass_scalar_3d.py), 3-point Gauss rule per axis (exact for the product)."""
+    l = np.ones(ndim) if l is None else np.asarray(l, float)
+    corners = _phys_corners(ndim)
+    acc = np.zeros((len(corners), len(corners)))
+    for idx in np.ndindex(*(3,) * ndim):
+        xi = np.array([_GP[i] for i in idx])
+        w = np.prod([_GW[i] for i in idx])
+        N = _shape(corners, xi)
+        acc += np.outer(N, N) * w * np.prod(l / 2.0)
+    return rho * acc
+
+
+def ke_screened_poisson(ndim, k=1.0, l=None):
+    """k * Laplacian + mass (elements/screenedpoisson_2d.py:8-37, screenedpoisson_3d.py:9-40)."""
+    return ke_poisson(ndim, k, l) + ke_mass(ndim, 1.0, l)
+
+
 def _elastic_D(ndim, E, nu):
     if ndim == 2:   # plane stress
         return E / (1 - nu ** 2) * np.array([[1, nu, 0], [nu, 1, 0], [0, 0, (1 - nu) / 2]])
@@ -199,6 +224,32 @@ def filter_matrix(nelx, nely, nelz, rmin):
 # --------------------------------------------------------------------------
 # objective + sensitivity (objectives.py:51-55, topology_optimization.py:491-500)
 # --------------------------------------------------------------------------
+# --------------------------------------------------------------------------
+# Helmholtz PDE filter (filter/helmholtz_filter.py:133-200; applied as in
+# topology_optimization.py:554-555, 568-570, 646-647)
+# --------------------------------------------------------------------------
+def helmholtz_operators(nelx, nely, nelz, rmin, l=None):
+    """KF (screened Poisson matrix, k = (rmin / (2 sqrt 3))^2, no boundary
+    conditions) and TF (element -> node averaging, 1/2^d per element node).
+    Returns (solve, TF) with solve a factorised KF."""
+    ndim = 2 if nelz is None else 3
+    KE = ke_screened_poisson(ndim, (rmin / (2 * np.sqrt(3))) ** 2, l)
+    edof = edofmat(nelx, nely, nelz, 1)
+    nel = edof.shape[0]
+    nnodes = int(np.prod(np.array([nelx, nely] + ([nelz] if ndim == 3 else [])) + 1))
+    KF = assemble(KE, edof, np.ones(nel), nnodes).tocsc()
+    nper = edof.shape[1]
+    TF = sp.coo_matrix((np.full(nel * nper, 1.0 / nper),
+                        (edof.ravel(), np.repeat(np.arange(nel), nper))),
+                       shape=(nnodes, nel)).tocsr()
+    return spla.factorized(KF), TF
+
+
+def helmholtz_apply(solve, TF, x):
+    """x_filtered = TF^T KF^-1 TF x."""
+    return TF.T @ solve(TF @ x)
+
+
 def compliance_sens(xPhys, u, KE, edof, eps=1e-9, penal=3.0):
     ue = u[edof]
     ce = np.einsum("ei,ij,ej->e", ue, KE, ue)
@@ -249,10 +300,11 @@ def solve_direct(K, f, free):
 # the design loop (topology_optimization.py:411-673; OC, ft in {0, 1})
 # --------------------------------------------------------------------------
 def run(nelx, nely, nelz, volfrac, rmin, ft, KE, fixed, f, eps=1e-9, penal=3.0,
-        nouteriter=2000, solve=None, record=()):
+        nouteriter=2000, solve=None, record=(), filter_mode="matrix"):
     """Return dict with obj/vol/change per iteration, final x, xPhys, u.
 
-    ``solve(K, f, free, u_prev) -> u`` defaults to the direct solve."""
+    ``solve(K, f, free, u_prev) -> u`` defaults to the direct solve.
+    ``filter_mode`` "helmholtz" replaces the distance filter by the PDE filter."""
     ndim = 2 if nelz is None else 3
     dims = (nelx, nely) if ndim == 2 else (nelx, nely, nelz)
     nel = int(np.prod(dims))
@@ -260,6 +312,9 @@ def run(nelx, nely, nelz, volfrac, rmin, ft, KE, fixed, f, eps=1e-9, penal=3.0,
     ndof = nnode_dof * int(np.prod(np.array(dims) + 1))
     edof = edofmat(nelx, nely, nelz, nnode_dof)
     H, Hs = filter_matrix(nelx, nely, nelz, rmin)
+    if filter_mode == "helmholtz":
+        hsolve, TF = helmholtz_operators(nelx, nely, nelz, rmin)
+        pde = lambda v: helmholtz_apply(hsolve, TF, v)   # noqa: E731
     free = np.setdiff1d(np.arange(ndof), fixed)
     x = volfrac * np.ones(nel)
     xPhys = x.copy()
@@ -282,7 +337,12 @@ def run(nelx, nely, nelz, volfrac, rmin, ft, KE, fixed, f, eps=1e-9, penal=3.0,
             dc += dc_i
         u = ucols[:, 0] if f.ndim == 1 else ucols.copy()
         dv = np.ones(nel)
-        if ft == 0:
+        if filter_mode == "helmholtz" and ft == 0:
+            dc = pde(dc * xPhys) / np.maximum(0.001, x)
+        elif filter_mode == "helmholtz" and ft == 1:
+            dc = pde(dc)
+            dv = pde(dv)
+        elif ft == 0:
             dc = np.asarray(H @ (x * dc)) / Hs / np.maximum(0.001, x)
         elif ft == 1:
             dc = np.asarray(H @ (dc / Hs))
@@ -292,7 +352,9 @@ def run(nelx, nely, nelz, volfrac, rmin, ft, KE, fixed, f, eps=1e-9, penal=3.0,
                                     dv=dv.copy(), x=x.copy(), g=g)
         xold = x.copy()
         x, g, nsteps = oc_top88(x, dc, dv, g)
-        if ft == 1:
+        if ft == 1 and filter_mode == "helmholtz":
+            xPhys = pde(x)
+        elif ft == 1:
             xPhys = np.asarray(H @ x) / Hs
         else:
             xPhys = x.copy()

@@ -75,6 +75,10 @@ from topoptlab.example_bc.heat_conduction import heatplate_2d  # noqa: E402
 from topoptlab.objectives import compliance  # noqa: E402
 from topoptlab.optimizer.optimality_criterion import oc_top88  # noqa: E402
 import topoptlab.output_designs as OD  # noqa: E402
+from topoptlab.elements.screenedpoisson_2d import lk_screened_poisson_2d  # noqa: E402
+from topoptlab.elements.screenedpoisson_3d import lk_screened_poisson_3d  # noqa: E402
+from topoptlab.filter.helmholtz_filter import assemble_helmholtz_filter  # noqa: E402
+from scipy.sparse.linalg import factorized  # noqa: E402
 
 OUT_KW = {"file": None, "display": False, "export": False, "write_log": False,
           "profile": False, "debug": 0}
@@ -208,11 +212,47 @@ def gen_vtk():
     np.savez_compressed(os.path.join(HERE, "vtk.npz"), **d)
 
 
+def gen_helmholtz():
+    """Screened Poisson element matrices, the Helmholtz filter applied to seeded
+    fields (filter/helmholtz_filter.py), and the reference design loop with
+    filter_mode="helmholtz" on the 60x20 MBB beam (tests/test_compliance.py:11-12)."""
+    rng = np.random.default_rng(11)
+    d = {}
+    for rmin in (2.4, 1.5):
+        k = (rmin / (2 * np.sqrt(3))) ** 2
+        d[f"KF2d_{rmin}"] = lk_screened_poisson_2d(k=k, l=np.array([1., 1.]))
+        d[f"KF3d_{rmin}"] = lk_screened_poisson_3d(k=k, l=np.array([1., 1., 1.]))
+    d["KF2d_rect"] = lk_screened_poisson_2d(k=0.3, l=np.array([2., 0.5]))
+    for (nx, ny, rmin) in [(7, 5, 2.4), (12, 8, 1.5)]:
+        # the operators main() uses (topology_optimization.py:360-365, 569, 647);
+        # the HelmholtzFilter class itself is abstract (no vol_conserv)
+        KF, TF = assemble_helmholtz_filter(nelx=nx, nely=ny, rmin=rmin)
+        lu_solve = factorized(KF)
+        x = rng.uniform(0.0, 1.0, (nx * ny, 1))
+        dx = rng.standard_normal((nx * ny, 1))
+        key = f"{nx}_{ny}_{rmin}"
+        d["x_" + key], d["dx_" + key] = x[:, 0], dx[:, 0]
+        d["y_" + key] = (TF.T @ lu_solve(TF @ x))[:, 0]
+        d["dy_" + key] = (TF.T @ lu_solve(TF @ (dx * x)) / np.maximum(0.001, x))[:, 0]
+    np.savez_compressed(os.path.join(HERE, "helmholtz.npz"), **d)
+    for ft in (1, 0):
+        r = run_traced(f"mbb2d_60x20_helmholtz_ft{ft}.npz", {0, 1, 2},
+                       nelx=60, nely=20, volfrac=0.5, rmin=2.4, ft=ft, bcs=mbb_2d,
+                       filter_mode="helmholtz")
+        print(f"mbb helmholtz ft{ft}", r[1], r[2])
+
+
+GENERATORS = {"vtk": lambda: gen_vtk(), "helmholtz": lambda: gen_helmholtz()}
+
+
 def main():
-    if len(sys.argv) > 2 and sys.argv[2] == "vtk":
-        gen_vtk()
+    # optional names after the reference path regenerate only those fixtures
+    if len(sys.argv) > 2:
+        for name in sys.argv[2:]:
+            GENERATORS[name]()
         return
     gen_vtk()
+    gen_helmholtz()
     gen_elements()
     gen_filters()
     r = run_traced("mbb2d_60x20.npz", {0, 1, 2, 24, 143},

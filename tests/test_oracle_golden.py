@@ -124,3 +124,36 @@ def test_gmg_pcg_matches_direct():
     assert it > 0
     ud = O.solve_direct(K, f, np.setdiff1d(np.arange(K.shape[0]), fixed))
     np.testing.assert_allclose(u, ud, atol=1e-8 * np.abs(ud).max())
+
+
+def test_helmholtz_element_and_filter(golden):
+    """Screened Poisson element matrices (k = (rmin/(2 sqrt 3))^2) and the PDE
+    filter TF^T KF^-1 TF on seeded fields, density and ft=0 sensitivity forms
+    (filter/helmholtz_filter.py:133-200, topology_optimization.py:555, :647)."""
+    g = golden("helmholtz.npz")
+    for rmin in (2.4, 1.5):
+        k = (rmin / (2 * np.sqrt(3))) ** 2
+        np.testing.assert_allclose(O.ke_screened_poisson(2, k), g[f"KF2d_{rmin}"], atol=1e-15)
+        np.testing.assert_allclose(O.ke_screened_poisson(3, k), g[f"KF3d_{rmin}"], atol=1e-15)
+    np.testing.assert_allclose(O.ke_screened_poisson(2, 0.3, [2.0, 0.5]), g["KF2d_rect"],
+                               atol=1e-15)
+    for (nx, ny, rmin) in [(7, 5, 2.4), (12, 8, 1.5)]:
+        solve, TF = O.helmholtz_operators(nx, ny, None, rmin)
+        key = f"{nx}_{ny}_{rmin}"
+        x, dx = g["x_" + key], g["dx_" + key]
+        np.testing.assert_allclose(O.helmholtz_apply(solve, TF, x), g["y_" + key], atol=1e-14)
+        np.testing.assert_allclose(O.helmholtz_apply(solve, TF, dx * x) / np.maximum(0.001, x),
+                                   g["dy_" + key], atol=1e-13)
+
+
+@pytest.mark.parametrize("ft,golden_obj", [(1, 237.59964), (0, 218.79281)])
+def test_mbb_helmholtz_trajectory(golden, ft, golden_obj):
+    """tests/test_compliance.py:11-12 (decimal=5) and the reference's whole
+    trajectory with filter_mode="helmholtz"."""
+    g = golden(f"mbb2d_60x20_helmholtz_ft{ft}.npz")
+    fixed, f = O.bc_mbb_2d(60, 20)
+    r = O.run(60, 20, None, 0.5, 2.4, ft, O.ke_elast(2), fixed, f, filter_mode="helmholtz")
+    assert len(r["obj"]) == int(g["n_iter"])
+    np.testing.assert_allclose(r["obj"], g["obj"], rtol=1e-9)
+    np.testing.assert_almost_equal(r["final_obj"], golden_obj, decimal=5)
+    np.testing.assert_allclose(r["x"], g["final_x"], atol=1e-8)
