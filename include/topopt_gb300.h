@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define TG_ABI_VERSION 2
+#define TG_ABI_VERSION 3
 
 enum {
   TG_OK = 0,
@@ -75,6 +75,12 @@ typedef struct tg_problem {
   int32_t nload;         /* load cases (columns of bcs()'s f, topology_optimization.py:
                             463-500): f holds nload vectors of ndof one after another;
                             0 or 1 = one load case */
+  int32_t filter_pde;    /* 1: Helmholtz PDE filter for ft 0/1 instead of the distance
+                            filter (topology_optimization.py:360-365, 554-555, 568-570,
+                            646-647; filter/helmholtz_filter.py:133-200) */
+  const double* KF;      /* filter_pde: screened Poisson element matrix, (2^ndim)^2 row
+                            major, reference local node order (lk_screened_poisson_2d/_3d
+                            with k = (rmin / (2 sqrt 3))^2, elements/screenedpoisson_2d.py:8) */
 } tg_problem;
 
 typedef struct tg_iter_out {
@@ -145,7 +151,9 @@ int32_t tg_csr_pcg(int64_t n, const int64_t* indptr, const int32_t* indices, con
                    int32_t maxiter, int32_t jacobi, tg_solve_info* info, int32_t device);
 const char* tg_csr_last_error(void);
 /* mode 0: (H x)/Hs   1: H(x/Hs)   2: H(x*d)/Hs/max(1e-3,x)   3: Hs
- * (filter/matrix_filter.py:101-232 + topology_optimization.py:545-558, :639) */
+ * (filter/matrix_filter.py:101-232 + topology_optimization.py:545-558, :639)
+ * contexts with filter_pde:  6: TF^T KF^-1 TF x   7: TF^T KF^-1 TF (x*d) / max(1e-3,x)
+ * (topology_optimization.py:555, :569, :647) */
 int32_t tg_filter(tg_ctx* ctx, const double* x, const double* d, double* y, int32_t mode);
 /* obj = sum simp(xPhys) u_e^T KE u_e, dc = -simp_dx(xPhys) u_e^T KE u_e
  * (objectives.py:51-55, topology_optimization.py:491-500) */

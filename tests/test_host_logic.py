@@ -57,7 +57,8 @@ def test_solver_options_mapping():
 
 
 @pytest.mark.parametrize("kw", [dict(optimizer="mma"), dict(optimizer="oc", ft=5),
-                                dict(optimizer="oc", filter_mode="helmholtz"),
+                                dict(optimizer="oc", filter_mode="helmholtz", ft=-1),
+                                dict(optimizer="oc", filter_mode="no-such-filter"),
                                 dict(optimizer="oc", body_forces_kw={"density_coupled": 1}),
                                 dict(optimizer="oc", mix=0.5)])
 def test_main_rejects_unsupported_options(kw):
@@ -66,6 +67,14 @@ def test_main_rejects_unsupported_options(kw):
     with pytest.raises(ValueError):
         main(nelx=4, nely=2, volfrac=0.5, rmin=1.5,
              output_kw={"file": None, "display": False, "export": False, "write_log": False}, **kw)
+
+
+def test_main_helmholtz_3d_not_implemented():
+    """assemble_helmholtz_filter raises NotImplementedError for 3-D grids
+    (filter/helmholtz_filter.py:180); the drop-in does the same."""
+    with pytest.raises(NotImplementedError):
+        main(nelx=4, nely=2, nelz=2, volfrac=0.5, rmin=1.5, ft=1, filter_mode="helmholtz", optimizer="oc",
+             output_kw={"file": None, "display": False, "export": False, "write_log": False})
 
 
 def _declared_symbols():
@@ -86,4 +95,4 @@ def test_library_loads_and_exports_every_symbol():
     lib = ctypes.CDLL(path)
     for name in _declared_symbols():
         assert hasattr(lib, name), name
-    assert _lib.load().tg_abi_version() == 2
+    assert _lib.load().tg_abi_version() == 3

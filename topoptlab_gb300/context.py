@@ -38,7 +38,7 @@ class GpuProblem:
     def __init__(self, nelx, nely, nelz, KE, fixed, f, volfrac, rmin, ft=1, eps=1e-9,
                  penal=3.0, move=0.2, el_flags=None, precond="gb300-gmg", precision="fp64",
                  nlevels=0, nsmooth=2, omega=0.6, rtol=1e-8, maxiter=2000, inner_rtol=1e-4,
-                 learned=False, device=0):
+                 learned=False, device=0, filter_mode="matrix", filter_l=None):
         self._lib = _lib.load()
         self.ndim = 2 if nelz is None else 3
         self.nelx, self.nely, self.nelz = nelx, nely, nelz
@@ -87,6 +87,16 @@ class GpuProblem:
         p.learned = int(bool(learned))
         p.device = device
         p.nload = self.nload
+        if filter_mode == "helmholtz":
+            # screened Poisson element of the PDE filter (filter/helmholtz_filter.py:188-193)
+            from .elements import lk_screened_poisson_2d, lk_screened_poisson_3d
+            lkf = lk_screened_poisson_2d if self.ndim == 2 else lk_screened_poisson_3d
+            l = np.ones(self.ndim) if filter_l is None else np.asarray(filter_l, dtype=float)
+            KF = _lib.f64(lkf(k=(rmin / (2 * np.sqrt(3))) ** 2, l=l))
+            self._keep.append(KF)
+            p.filter_pde, p.KF = 1, _lib.dptr(KF)
+        elif filter_mode not in ("matrix", "convolution"):
+            raise ValueError(f"Unknown filter. ft: {ft} filter_mode {filter_mode}")
         h = C.c_void_p()
         rc = self._lib.tg_create(C.byref(p), C.byref(h))
         _lib.check(rc, None, "tg_create")

@@ -253,14 +253,20 @@ int32_t tg_solve(tg_ctx* ctx, const double* xPhys, const double* rhs, const doub
 }
 
 int32_t tg_filter(tg_ctx* ctx, const double* x, const double* d, double* y, int32_t mode) {
-  if (!ctx || !y || mode < 0 || mode > 3 || (mode != 3 && !x) || (mode == 2 && !d)) return TG_EINVAL;
+  const bool pde = mode == 6 || mode == 7;
+  if (!ctx || !y || mode < 0 || (mode > 3 && !pde) || (mode != 3 && !x) ||
+      ((mode == 2 || mode == 7) && !d))
+    return TG_EINVAL;
+  if (pde && !ctx->c.hf) return TG_EINVAL;
   return guarded(ctx, [&] {
     tg::Ctx& c = ctx->c;
     require_unpadded(c, "tg_filter");
     const int64_t nel = c.g.nel();
     if (x) h2d(c.xnew.p, x, nel, c.st);
     if (d) h2d(c.S.p, d, nel, c.st);
-    tg::filter_apply(c.g, c.fs, c.xnew, c.S, c.Hs, c.dc, mode, c.st);
+    if (mode == 6) tg::helmholtz_apply(c, c.xnew, nullptr, nullptr, c.dc);
+    else if (mode == 7) tg::helmholtz_apply(c, c.S, c.xnew, c.xnew, c.dc);
+    else tg::filter_apply(c.g, c.fs, c.xnew, c.S, c.Hs, c.dc, mode, c.st);
     d2h(y, c.dc.p, nel, c.st);
   });
 }

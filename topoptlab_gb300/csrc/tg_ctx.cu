@@ -22,6 +22,9 @@ Ctx::~Ctx() {
     if (l->graph) cudaGraphDestroy(l->graph);
   }
   for (Level* l : lv) delete l;
+  delete hf;
+  if (hev0) cudaEventDestroy(hev0);
+  if (hev1) cudaEventDestroy(hev1);
   if (h_oc) cudaFreeHost(h_oc);
   if (h_pcg) cudaFreeHost(h_pcg);
   if (h_scal) cudaFreeHost(h_scal);
@@ -368,8 +371,16 @@ void ctx_init(Ctx& c, const tg_problem& p) {
     for (int ex = 0; ex < rg.nex; ++ex)
       for (int ey = 0; ey < rg.ney; ++ey) ones[g.elem(ex, ey, ez)] = 1.0;
   TG_CUDA(cudaMemcpy(c.xnew.p, ones.data(), sizeof(double) * nel, cudaMemcpyHostToDevice));
-  if (c.ft == 1) filter_apply(g, c.fs, c.xnew, nullptr, c.Hs, c.dv, 1, c.st);
-  else TG_CUDA(cudaMemcpyAsync(c.dv.p, c.xnew.p, sizeof(double) * nel, cudaMemcpyDeviceToDevice, c.st));
+  if (p.filter_pde) {
+    // dv = TF^T KF^-1 TF 1 for the density form (topology_optimization.py:570)
+    helmholtz_init(c, p.KF);
+    if (c.ft == 1) helmholtz_apply(c, c.xnew, nullptr, nullptr, c.dv);
+    else TG_CUDA(cudaMemcpyAsync(c.dv.p, c.xnew.p, sizeof(double) * nel, cudaMemcpyDeviceToDevice, c.st));
+  } else if (c.ft == 1) {
+    filter_apply(g, c.fs, c.xnew, nullptr, c.Hs, c.dv, 1, c.st);
+  } else {
+    TG_CUDA(cudaMemcpyAsync(c.dv.p, c.xnew.p, sizeof(double) * nel, cudaMemcpyDeviceToDevice, c.st));
+  }
   // initial design x = xPhys = volfrac (topology_optimization.py:216-219)
   std::vector<double> x0(nel, 0.0);
   for (int ez = 0; ez < rg.nez; ++ez)
@@ -828,7 +839,9 @@ void ctx_step(Ctx& c, tg_iter_out& out) {
     reduce_partials(c.part, nbe, c.scal.p + 0, false, c.st);
   }
   // sensitivity filter
-  if (c.ft == 1) filter_apply(g, c.fs, c.dc, nullptr, c.Hs, c.dcf, 1, c.st);
+  if (c.hf && c.ft == 1) helmholtz_apply(c, c.dc, nullptr, nullptr, c.dcf);
+  else if (c.hf && c.ft == 0) helmholtz_apply(c, c.dc, c.xPhys, c.x, c.dcf);
+  else if (c.ft == 1) filter_apply(g, c.fs, c.dc, nullptr, c.Hs, c.dcf, 1, c.st);
   else if (c.ft == 0) filter_apply(g, c.fs, c.x, c.dc, c.Hs, c.dcf, 2, c.st);
   else TG_CUDA(cudaMemcpyAsync(c.dcf.p, c.dc.p, sizeof(double) * nel, cudaMemcpyDeviceToDevice, c.st));
   // OC
@@ -848,8 +861,11 @@ void ctx_step(Ctx& c, tg_iter_out& out) {
   std::swap(c.xold.p, c.x.p);
   std::swap(c.x.p, c.xnew.p);
   // density filter (or copy) fused with the volume sum and max |x - x_old|
-  filter_apply_ex(g, c.fs, c.x, nullptr, c.Hs, c.xPhys, c.ft == 1 ? 0 : 4, c.xold, c.part,
-                  c.part2, c.st);
+  if (c.hf && c.ft == 1)
+    helmholtz_apply(c, c.x, nullptr, nullptr, c.xPhys, c.x, c.xold, c.part, c.part2);
+  else
+    filter_apply_ex(g, c.fs, c.x, nullptr, c.Hs, c.xPhys, c.ft == 1 ? 0 : 4, c.xold, c.part,
+                    c.part2, c.st);
   reduce_partials(c.part, nbe, c.scal.p + 1, false, c.st);
   reduce_partials(c.part2, nbe, c.scal.p + 2, true, c.st);
   TG_CUDA(cudaMemcpyAsync(c.h_scal, c.scal.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, c.st));

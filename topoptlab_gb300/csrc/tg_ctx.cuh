@@ -110,6 +110,12 @@ struct Ctx {
   } l64, l32;
   bool use_graphs = true;
   struct Cnn* cnn = nullptr;     // learned warm start (not owned)
+  // Helmholtz PDE filter: the screened Poisson problem on the same device
+  // grid, one scalar DOF per node, as its own context (owned); events order
+  // its stream after this context's and back
+  Ctx* hf = nullptr;
+  cudaEvent_t hev0 = nullptr, hev1 = nullptr;
+  int64_t filter_iters = 0;      // PCG iterations of all filter solves so far
   // statistics of the last solve
   int last_iters = 0, last_vcycles = 0, last_refine = 0, last_converged = 0;
   double last_relres = 0.0;
@@ -126,5 +132,13 @@ void solve(Ctx& c, const double* b, double* u);
 // prescaled: the level's scratch buffer already holds omega D^-1 b (fused
 // into the restriction that produced b)
 template <typename T> void vcycle(Ctx& c, int l, const T* b, T* x, bool prescaled = false);
+// Helmholtz PDE filter: set-up (KF: screened Poisson element matrix, host)
+// and y = TF^T KF^-1 TF (v * mul) [/ max(1e-3, xdiv)]; mul and xdiv may be
+// null; with part_sum / part_max also the sums of the density filter
+// (sum y per block, max |x - xold| per block)
+void helmholtz_init(Ctx& c, const double* KF);
+void helmholtz_apply(Ctx& c, const double* v, const double* mul, const double* xdiv, double* y,
+                     const double* x = nullptr, const double* xold = nullptr,
+                     double* part_sum = nullptr, double* part_max = nullptr);
 
 }  // namespace tg

@@ -10,6 +10,8 @@ Mirrors:
   lk_linear_elast_2d   elements/linear_elasticity_2d.py:69 (plane stress)
   lk_linear_elast_3d   elements/linear_elasticity_3d.py:65
   lk_poisson_2d / 3d   elements/poisson_2d.py:68, elements/poisson_3d.py:62
+  lk_screened_poisson_2d / 3d   elements/screenedpoisson_2d.py:8,
+                   elements/screenedpoisson_3d.py:9 (Laplacian + consistent mass)
 """
 from __future__ import annotations
 
@@ -121,3 +123,26 @@ def lk_poisson_2d(k: float = 1.0, l=np.array([1.0, 1.0]), t: float = 1.0, **kwar
 
 def lk_poisson_3d(k: float = 1.0, l=np.array([1.0, 1.0, 1.0]), **kwargs) -> np.ndarray:
     return k * _element_matrix(3, l, lambda dN: dN @ dN.T)
+
+
+def _mass_matrix(ndim, l):
+    """Consistent scalar mass matrix int N N^T (2-point Gauss, exact here)."""
+    local = _LOCAL_2D if ndim == 2 else _LOCAL_3D
+    phys = [np.array((c[0], 1 - c[1]) + tuple(c[2:])) for c in local]
+    l = np.broadcast_to(np.asarray(l, dtype=float), (ndim,))
+    gp = np.array([-1.0, 1.0]) / np.sqrt(3.0)
+    M = np.zeros((len(phys), len(phys)))
+    for xi in itertools.product(gp, repeat=ndim):
+        N = np.array([np.prod(0.5 * (1 + (2 * c - 1) * np.asarray(xi))) for c in phys])
+        M += np.outer(N, N) * np.prod(l / 2.0)
+    return M
+
+
+def lk_screened_poisson_2d(k: float = 1.0, l=np.array([1.0, 1.0]), t: float = 1.0,
+                           **kwargs) -> np.ndarray:
+    """k * Laplacian + mass; the Helmholtz filter uses k = (rmin / (2 sqrt 3))^2."""
+    return t * (k * _element_matrix(2, l, lambda dN: dN @ dN.T) + _mass_matrix(2, l))
+
+
+def lk_screened_poisson_3d(k: float = 1.0, l=np.array([1.0, 1.0, 1.0]), **kwargs) -> np.ndarray:
+    return k * _element_matrix(3, l, lambda dN: dN @ dN.T) + _mass_matrix(3, l)

@@ -9,7 +9,9 @@ compliance of the last solved design), same per-iteration log line
 Supported: quad4 / hex8 structured grids, ``lk`` callables returning the
 element matrix (elasticity or Poisson), ``bcs`` callables of the reference
 example_bc signature (any number of load cases, no springs), ``ft`` in {-1, 0, 1}
-with ``filter_mode`` "matrix" or "convolution" (identical operators),
+with ``filter_mode`` "matrix" or "convolution" (identical operators), or
+"helmholtz" (the PDE filter, ft in {0, 1}, 2-D like the reference's
+filter/helmholtz_filter.py:177-180),
 ``optimizer="oc"``, SIMP (``matinterpol_kw`` eps / penal), ``el_flags``.
 Anything else raises ValueError, as the reference does for unknown options
 (:262, :367).  There is no CPU path.
@@ -126,8 +128,12 @@ def main(nelx: int, nely: int,
                          "(the GPU path implements the optimality criteria method 'oc')")
     if not isinstance(ft, (int, np.integer)) or ft not in (-1, 0, 1):
         raise ValueError(f"Unknown filter. ft: {ft} filter_mode {filter_mode}")
-    if filter_mode not in ("matrix", "convolution"):
+    if filter_mode not in ("matrix", "convolution") and not (filter_mode == "helmholtz"
+                                                            and ft in (0, 1)):
         raise ValueError(f"Unknown filter. ft: {ft} filter_mode {filter_mode}")
+    if filter_mode == "helmholtz" and ndim == 3:
+        # assemble_helmholtz_filter raises this for 3-D (filter/helmholtz_filter.py:180)
+        raise NotImplementedError("3D not yet completely implemented.")
     if len(body_forces_kw) > 0:
         raise ValueError("body forces are not supported by the GPU path")
     if mix is not None or (accelerator_kw is not None and accelerator_kw.get("accelerator") is not None):
@@ -173,7 +179,8 @@ def main(nelx: int, nely: int,
     # several columns = several load cases: one solve each, compliance and
     # sensitivities summed (topology_optimization.py:446-500)
     prob = GpuProblem(nelx, nely, nelz, KE, fixed, f, volfrac, rmin, ft=int(ft),
-                      eps=eps, penal=penal, el_flags=el_flags, device=device, **opts)
+                      eps=eps, penal=penal, el_flags=el_flags, device=device,
+                      filter_mode=filter_mode, filter_l=l, **opts)
     obj = 0.0
 
     def export(name):
