@@ -281,7 +281,7 @@ void ctx_init(Ctx& c, const tg_problem& p) {
                              "preconditioner gb300-jacobi)");
     c.ldc = cdiv(c.nc, 32) * 32;
     c.Dc.alloc(c.ldc * c.ldc);
-    c.gjwork.alloc(2 * (32 * 32 + 2 * 32 * c.ldc));   // pivot tile, row panel R, saved panel X; x2
+    c.gjwork.alloc(32 * 32 + 2 * 32 * c.ldc);   // pivot tile, row panel R, saved panel X
   }
   const bool mixed = c.precision == TG_PREC_MIXED;
   for (int l = 0; l < c.L; ++l) {

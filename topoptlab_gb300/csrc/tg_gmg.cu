@@ -701,14 +701,16 @@ template void stencil_to_dense<double>(const Grid&, const uint8_t*, const double
 template void stencil_to_dense<float>(const Grid&, const uint8_t*, const float*, double*, int64_t,
                                       int64_t, cudaStream_t);
 
-constexpr int GJB = 32;
+constexpr int GJB = 32;   // tile of the final mirror / negate pass
+constexpr int SWB = 16;   // pivot block of the sweep operator
 
-// invert a GJB x GJB SPD tile in shared memory (Gauss-Jordan without pivoting;
+// invert a TB x TB SPD tile in shared memory (Gauss-Jordan without pivoting;
 // GB300's FP64 pipe is narrow: one reciprocal per step, not one divide per
-// thread, everything else multiply / FMA); 1024 threads, (i, j) = (y, x)
-__device__ __forceinline__ void gj_tile_inverse(double (&a)[GJB][GJB + 1], double& rpiv, int i,
+// thread, everything else multiply / FMA); TB*TB threads, (i, j) = (y, x)
+template <int TB>
+__device__ __forceinline__ void gj_tile_inverse(double (&a)[TB][TB + 1], double& rpiv, int i,
                                                 int j) {
-  for (int p = 0; p < GJB; ++p) {
+  for (int p = 0; p < TB; ++p) {
     if (i == 0 && j == 0) rpiv = 1.0 / a[p][p];
     __syncthreads();
     const double rp = rpiv;
@@ -724,165 +726,88 @@ __device__ __forceinline__ void gj_tile_inverse(double (&a)[GJB][GJB + 1], doubl
   }
 }
 
-// Warp version of gj_tile_inverse (the same operations in the same order, so
-// the same bits): lane j owns column j; every pivot step reads tile a and
-// writes tile b (two shared buffers, no hazard inside a step); after the 32
-// steps (an even number) the inverse is back in a.
-__device__ __forceinline__ void gj_tile_inverse_warp(double (&a)[GJB][GJB + 1],
-                                                     double (&b)[GJB][GJB + 1], int lane) {
-  for (int p = 0; p < GJB; p += 2) {
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      double (&src)[GJB][GJB + 1] = h ? b : a;
-      double (&dst)[GJB][GJB + 1] = h ? a : b;
-      const int q = p + h;
-      const double rp = 1.0 / src[q][q];
-      const double s = src[q][lane] * rp;
-#pragma unroll 2
-      for (int i = 0; i < GJB; ++i) {
-        const double aiq = src[i][q];
-        double v;
-        if (i == q) v = (lane == q) ? rp : s;
-        else v = (lane == q) ? -aiq * rp : fma(-aiq, s, src[i][lane]);
-        dst[i][lane] = v;
-      }
-      __syncwarp();
-    }
-  }
-}
-
 // The coarsest matrix is SPD, so it is inverted with the block sweep operator,
 // which keeps the matrix symmetric at every step (pivot block K, P = A_KK^-1):
 //   A_KK <- -P,  A_KJ <- P A_KJ,  A_IK <- A_IK P,  A_IJ <- A_IJ - A_IK P A_KJ,
 // ending with -A^-1.  Only blocks (ib <= jb) are kept up to date, which halves
-// the rank-32 update flops of a plain Gauss-Jordan inverse and removes its
+// the rank-TB update flops of a plain Gauss-Jordan inverse and removes its
 // column-panel product (A_IK P is the transpose of the row panel P A_KI).
-// Per pivot step K the panel quantities are P, the saved panel X_J = A_KJ
-// and R_J = P X_J; the update is D_IJ -= X_I^T R_J for ib <= jb off the pivot
-// row / column, which become R and -P.
-//
-// One launch per step with look-ahead: launch k applies the update of step k
-// and also produces the panel of step k+1.  The tiles of row / column k+1 are
-// the next step's X; their CTAs (launched first) compute their updated tile,
-// each also computes the updated pivot tile k+1 and inverts it with one warp,
-// and they write X, R and P of step k+1 into the other half of double
-// buffers instead of writing D (the next launch overwrites those tiles with
-// R and -P, so their intermediate values are never read from D).  k_sw_panel
-// produces the panel of step 0.  Every tile product is the same FMA chain as
-// a separate panel / update pair, so the result is bit-identical to it.
-__global__ void __launch_bounds__(GJB * GJB) k_sw_panel(const double* D, int64_t ld, int k,
-                                                       double* P, double* R, double* Xb) {
-  __shared__ double a[GJB][GJB + 1], xs[GJB][GJB + 1];
+// Two launches per pivot step:
+//  (1) panel: every CTA jb inverts the pivot tile itself (no serial pivot
+//      launch), saves the original panel tile X_J = A_KJ to Xb and writes
+//      R_J = P X_J; CTA K writes P;
+//  (2) update: D_IJ -= X_I^T R_J for ib <= jb off the pivot row/column, and
+//      the panel row/column and the pivot tile are overwritten with R and -P
+//      in the same launch (the update reads X from Xb, so no tile is read
+//      and written by different CTAs of one launch); one CTA per tile of the
+//      upper triangle.
+// Pivot block 16, not 32: the step's critical path (pivot-tile inverse and
+// panel product, TB^3 FP64 FMAs each on one SM) shrinks 8x while the update
+// work per matrix stays n^3 / 2; on GB300's narrow FP64 pipe the 32-wide
+// panel cost more than the update it precedes.
+template <int TB>
+__global__ void __launch_bounds__(TB * TB) k_sw_panel(const double* D, int64_t ld, int k,
+                                                     double* P, double* R, double* Xb) {
+  __shared__ double a[TB][TB + 1], xs[TB][TB + 1];
   __shared__ double rpiv;
   const int jb = blockIdx.x;
   const int i = threadIdx.y, j = threadIdx.x;
-  a[i][j] = D[(int64_t)(k * GJB + i) * ld + k * GJB + j];
+  a[i][j] = D[(int64_t)(k * TB + i) * ld + k * TB + j];
   if (jb != k) {
-    if (k < jb) xs[i][j] = D[(int64_t)(k * GJB + i) * ld + jb * GJB + j];
-    else xs[j][i] = D[(int64_t)(jb * GJB + i) * ld + k * GJB + j];   // coalesced, transposed in smem
+    if (k < jb) xs[i][j] = D[(int64_t)(k * TB + i) * ld + jb * TB + j];
+    else xs[j][i] = D[(int64_t)(jb * TB + i) * ld + k * TB + j];   // coalesced, transposed in smem
   }
   __syncthreads();
-  gj_tile_inverse(a, rpiv, i, j);
+  gj_tile_inverse<TB>(a, rpiv, i, j);
   if (jb == k) {
-    P[i * GJB + j] = a[i][j];
+    P[i * TB + j] = a[i][j];
     return;
   }
   double acc = 0.0;
-#pragma unroll 8
-  for (int m = 0; m < GJB; ++m) acc = fma(a[i][m], xs[m][j], acc);
-  R[(int64_t)i * ld + jb * GJB + j] = acc;
-  Xb[(int64_t)i * ld + jb * GJB + j] = xs[i][j];
+#pragma unroll
+  for (int m = 0; m < TB; ++m) acc = fma(a[i][m], xs[m][j], acc);
+  R[(int64_t)i * ld + jb * TB + j] = acc;
+  Xb[(int64_t)i * ld + jb * TB + j] = xs[i][j];
 }
 
-// one thread's element of X_I^T R_J (tiles staged in xs, rs)
-__device__ __forceinline__ double sw_xtr(const double (&xs)[GJB][GJB + 1],
-                                         const double (&rs)[GJB][GJB + 1], int i, int j) {
-  double acc = 0.0;
-#pragma unroll 8
-  for (int m = 0; m < GJB; ++m) acc = fma(xs[m][i], rs[m][j], acc);
-  return acc;
+// upper-triangle tile of linear index t, column by column: (ib, jb), ib <= jb
+__device__ __forceinline__ void tri_tile(int t, int& ib, int& jb) {
+  int c = (int)((sqrt(8.0 * t + 1.0) - 1.0) * 0.5);
+  while (c * (c + 1) / 2 > t) --c;
+  while ((c + 1) * (c + 2) / 2 <= t) ++c;
+  jb = c;
+  ib = t - c * (c + 1) / 2;
 }
 
-__global__ void __launch_bounds__(GJB * GJB, 2) k_sw_step(double* D, int64_t ld, int nb, int k,
-                                                      const double* Pc, const double* Rc,
-                                                      const double* Xc, double* Pn, double* Rn,
-                                                      double* Xn) {
-  __shared__ double xs[GJB][GJB + 1], rs[GJB][GJB + 1], ta[GJB][GJB + 1], tb[GJB][GJB + 1];
-  const int i = threadIdx.y, j = threadIdx.x;
-  const int K1 = k + 1;
-  const bool ahead = K1 < nb;                 // a next step exists
-  const int nset = ahead ? nb : 0;            // blocks [0, nset): row / column K1
+template <int TB>
+__global__ void __launch_bounds__(TB * TB) k_sw_update(double* D, int64_t ld, int k,
+                                                      const double* P, const double* R,
+                                                      const double* Xb) {
   int ib, jb;
-  const int b = blockIdx.x;
-  if (b < nset) {
-    ib = b < K1 ? b : K1;
-    jb = b < K1 ? K1 : b;
-  } else {
-    const int m = ahead ? nb - 1 : nb;        // the other tiles: index K1 removed
-    const int r = b - nset, ii = r / m, jj = r % m;
-    if (ii > jj) return;
-    ib = (ahead && ii >= K1) ? ii + 1 : ii;
-    jb = (ahead && jj >= K1) ? jj + 1 : jj;
-  }
-  const int64_t tile = (int64_t)(ib * GJB + i) * ld + jb * GJB + j;
-  if (b >= nset) {
-    // ---- update of step k -------------------------------------------------
-    if (ib == k && jb == k) {                       // pivot tile <- -P
-      D[tile] = -Pc[i * GJB + j];
-    } else if (ib == k) {                           // panel row (upper orientation) <- R_J
-      D[tile] = Rc[(int64_t)i * ld + jb * GJB + j];
-    } else if (jb == k) {                           // panel column (ib < k) <- R_I^T
-      rs[i][j] = Rc[(int64_t)i * ld + ib * GJB + j];
-      __syncthreads();
-      D[tile] = rs[j][i];
-    } else {
-      xs[i][j] = Xc[(int64_t)i * ld + ib * GJB + j];  // X_I[m = i][c = j]
-      rs[i][j] = Rc[(int64_t)i * ld + jb * GJB + j];
-      __syncthreads();
-      D[tile] -= sw_xtr(xs, rs, i, j);
-    }
+  tri_tile(blockIdx.x, ib, jb);
+  const int i = threadIdx.y, j = threadIdx.x;
+  if (ib == k && jb == k) {                       // pivot tile <- -P
+    D[(int64_t)(k * TB + i) * ld + k * TB + j] = -P[i * TB + j];
     return;
   }
-  // ---- row / column K1: updated tile -> panel of step K1 -------------------
-  // the updated pivot tile (K1 != k, so the plain update), inverted by warp 0
-  xs[i][j] = Xc[(int64_t)i * ld + K1 * GJB + j];
-  rs[i][j] = Rc[(int64_t)i * ld + K1 * GJB + j];
-  const double dpiv = D[(int64_t)(K1 * GJB + i) * ld + K1 * GJB + j];
-  __syncthreads();
-  ta[i][j] = dpiv - sw_xtr(xs, rs, i, j);
-  __syncthreads();
-  // this block's own updated tile T (upper orientation)
-  double t;
-  if (ib == K1 && jb == K1) {
-    t = ta[i][j];
-  } else if (ib == k) {                             // (k, K1): the panel row of step k, R_K1
-    t = rs[i][j];
-  } else {
-    const double dv = D[tile];
-    const double xv = Xc[(int64_t)i * ld + ib * GJB + j];
-    const double rv = Rc[(int64_t)i * ld + jb * GJB + j];
-    __syncthreads();                                // everyone is done with xs, rs of the pivot
-    xs[i][j] = xv;
-    rs[i][j] = rv;
+  if (ib == k) {                                  // panel row (upper orientation) <- R_J
+    D[(int64_t)(k * TB + i) * ld + jb * TB + j] = R[(int64_t)i * ld + jb * TB + j];
+    return;
+  }
+  __shared__ double xs[TB][TB + 1], rs[TB][TB + 1];
+  if (jb == k) {                                  // panel column (ib < k) <- R_I^T
+    rs[i][j] = R[(int64_t)i * ld + ib * TB + j];
     __syncthreads();
-    t = dv - sw_xtr(xs, rs, i, j);
-  }
-  if (i == 0) gj_tile_inverse_warp(ta, tb, j);     // warp 0: ta <- P of step K1
-  __syncthreads();
-  if (ib == K1 && jb == K1) {
-    Pn[i * GJB + j] = ta[i][j];
+    D[(int64_t)(ib * TB + i) * ld + k * TB + j] = rs[j][i];
     return;
   }
-  // X_J = A_K1,J in the orientation of row K1: T itself on row K1, T^T on column K1
-  const int other = (ib == K1) ? jb : ib;
-  if (ib == K1) tb[i][j] = t;
-  else tb[j][i] = t;
+  xs[i][j] = Xb[(int64_t)i * ld + ib * TB + j];   // X_I[m = i][c = j]
+  rs[i][j] = R[(int64_t)i * ld + jb * TB + j];
   __syncthreads();
   double acc = 0.0;
-#pragma unroll 8
-  for (int m = 0; m < GJB; ++m) acc = fma(ta[i][m], tb[m][j], acc);
-  Rn[(int64_t)i * ld + other * GJB + j] = acc;
-  Xn[(int64_t)i * ld + other * GJB + j] = tb[i][j];
+#pragma unroll
+  for (int m = 0; m < TB; ++m) acc = fma(xs[m][i], rs[m][j], acc);
+  D[(int64_t)(ib * TB + i) * ld + jb * TB + j] -= acc;
 }
 // D <- -D on the upper blocks, mirrored into the lower ones: the full A^-1
 __global__ void __launch_bounds__(GJB * GJB) k_sw_mirror(double* D, int64_t ld) {
@@ -903,21 +828,19 @@ __global__ void __launch_bounds__(GJB * GJB) k_sw_mirror(double* D, int64_t ld) 
 
 void gj_inverse(double* D, int64_t n, int64_t ld, double* work, cudaStream_t st) {
   TG_REQUIRE(ld % GJB == 0, "dense leading dimension must be a multiple of 32");
-  const int nb = (int)(ld / GJB);
-  // double buffers of the panel quantities: P (GJB*GJB), R and X (GJB*ld)
-  double* P[2] = {work, work + GJB * GJB};
-  double* R[2] = {work + 2 * GJB * GJB, work + 2 * GJB * GJB + GJB * ld};
-  double* X[2] = {R[1] + GJB * ld, R[1] + 2 * GJB * ld};
-  const dim3 thr(GJB, GJB);
-  k_sw_panel<<<nb, thr, 0, st>>>(D, ld, 0, P[0], R[0], X[0]);
+  const int nb = (int)(ld / SWB);
+  double* P = work;                  // SWB*SWB
+  double* R = work + SWB * SWB;      // SWB*ld
+  double* Xb = R + SWB * ld;         // SWB*ld
+  const dim3 thr(SWB, SWB);
+  const unsigned tiles = (unsigned)(nb * (nb + 1) / 2);
   for (int k = 0; k < nb; ++k) {
-    const int c = k & 1;
-    const int m = (k + 1 < nb) ? nb - 1 : nb;
-    const unsigned blocks = (unsigned)((k + 1 < nb ? nb : 0) + m * m);
-    k_sw_step<<<blocks, thr, 0, st>>>(D, ld, nb, k, P[c], R[c], X[c], P[c ^ 1], R[c ^ 1], X[c ^ 1]);
+    k_sw_panel<SWB><<<nb, thr, 0, st>>>(D, ld, k, P, R, Xb);
+    k_sw_update<SWB><<<tiles, thr, 0, st>>>(D, ld, k, P, R, Xb);
   }
-  k_sw_mirror<<<dim3(nb, nb), thr, 0, st>>>(D, ld);
-  count_launches((int64_t)nb + 2);
+  const int nm = (int)(ld / GJB);
+  k_sw_mirror<<<dim3(nm, nm), dim3(GJB, GJB), 0, st>>>(D, ld);
+  count_launches(2 * (int64_t)nb + 1);
   TG_CHECK_LAUNCH();
 }
 

@@ -103,7 +103,7 @@ void prolong_add(const Grid& gf, const Grid& gc, const uint8_t* fixf, const T* x
 template <typename T>
 void stencil_to_dense(const Grid& g, const uint8_t* fix, const T* A, double* D, int64_t n,
                       int64_t ld, cudaStream_t st);
-// work: 2 * (32 * 32 + 2 * 32 * ld) doubles
+// work: 32 * 32 + 2 * 32 * ld doubles (enough for pivot blocks up to 32)
 void gj_inverse(double* D, int64_t n, int64_t ld, double* work, cudaStream_t st);
 template <typename T>
 void dense_apply(const double* Dinv, int64_t n, int64_t ld, const T* b, T* x,
