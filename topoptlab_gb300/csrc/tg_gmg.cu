@@ -810,6 +810,7 @@ __global__ void __launch_bounds__(TB * TB) k_sw_update(double* D, int64_t ld, in
   D[(int64_t)(ib * TB + i) * ld + jb * TB + j] -= acc;
 }
 // D <- -D on the upper blocks, mirrored into the lower ones: the full A^-1
+// (GJB is a multiple of SWB)
 __global__ void __launch_bounds__(GJB * GJB) k_sw_mirror(double* D, int64_t ld) {
   const int ib = blockIdx.y, jb = blockIdx.x;
   if (ib > jb) return;
@@ -819,7 +820,11 @@ __global__ void __launch_bounds__(GJB * GJB) k_sw_mirror(double* D, int64_t ld) 
   ts[i][j] = v;
   __syncthreads();
   if (ib == jb) {
-    D[(int64_t)(ib * GJB + i) * ld + jb * GJB + j] = 0.5 * (v + ts[j][i]);   // exact symmetry
+    // the sweep keeps only pivot-block tiles with row block <= column block up
+    // to date: below them take the transpose, on them enforce exact symmetry
+    const int ri = i / SWB, cj = j / SWB;
+    const double w = ri > cj ? ts[j][i] : (ri < cj ? v : 0.5 * (v + ts[j][i]));
+    D[(int64_t)(ib * GJB + i) * ld + jb * GJB + j] = w;
   } else {
     D[(int64_t)(ib * GJB + i) * ld + jb * GJB + j] = v;
     D[(int64_t)(jb * GJB + i) * ld + ib * GJB + j] = ts[j][i];
