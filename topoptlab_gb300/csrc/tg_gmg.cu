@@ -771,8 +771,11 @@ __global__ void __launch_bounds__(TB * TB) k_sw_panel(const double* D, int64_t l
 }
 
 // upper-triangle tile of linear index t, column by column: (ib, jb), ib <= jb
+// (FP32 estimate, corrected exactly in integers: an FP64 sqrt per thread would
+// cost more on GB300's narrow FP64 pipe than the tile's own FMAs)
 __device__ __forceinline__ void tri_tile(int t, int& ib, int& jb) {
-  int c = (int)((sqrt(8.0 * t + 1.0) - 1.0) * 0.5);
+  int c = (int)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
+  c = max(c, 0);
   while (c * (c + 1) / 2 > t) --c;
   while ((c + 1) * (c + 2) / 2 <= t) ++c;
   jb = c;
