@@ -704,25 +704,33 @@ template void stencil_to_dense<float>(const Grid&, const uint8_t*, const float*,
 constexpr int GJB = 32;   // tile of the final mirror / negate pass
 constexpr int SWB = 16;   // pivot block of the sweep operator
 
-// invert a TB x TB SPD tile in shared memory (Gauss-Jordan without pivoting;
-// GB300's FP64 pipe is narrow: one reciprocal per step, not one divide per
-// thread, everything else multiply / FMA); TB*TB threads, (i, j) = (y, x)
+// Invert a TB x TB SPD tile in shared memory (Gauss-Jordan without pivoting)
+// with the first TB lanes of one warp: lane j owns column j; every pivot step
+// reads tile a and writes tile b (two shared buffers, no hazard inside a
+// step, one __syncwarp per step); TB is even, so the inverse ends in a.  Each
+// lane issues one FP64 operation per row (GB300's FP64 pipe is narrow): the
+// pivot column's -a_iq / a_qq is fma(-a_iq, 1 / a_qq, 0), the other columns
+// get fma(-a_iq, a_qj / a_qq, a_ij).
 template <int TB>
-__device__ __forceinline__ void gj_tile_inverse(double (&a)[TB][TB + 1], double& rpiv, int i,
-                                                int j) {
-  for (int p = 0; p < TB; ++p) {
-    if (i == 0 && j == 0) rpiv = 1.0 / a[p][p];
-    __syncthreads();
-    const double rp = rpiv;
-    const double aip = a[i][p], apj = a[p][j];
-    __syncthreads();
-    double v;
-    if (i == p && j == p) v = rp;
-    else if (i == p) v = apj * rp;
-    else if (j == p) v = -aip * rp;
-    else v = fma(-aip, apj * rp, a[i][j]);
-    a[i][j] = v;
-    __syncthreads();
+__device__ __forceinline__ void gj_tile_inverse_warp(double (&a)[TB][TB + 1],
+                                                     double (&b)[TB][TB + 1], int lane) {
+  constexpr unsigned mask = TB == 32 ? 0xffffffffu : ((1u << TB) - 1u);
+  for (int p = 0; p < TB; p += 2) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      double (&src)[TB][TB + 1] = h ? b : a;
+      double (&dst)[TB][TB + 1] = h ? a : b;
+      const int q = p + h;
+      const double rp = 1.0 / src[q][q];
+      const bool piv = lane == q;
+      const double sq = piv ? rp : src[q][lane] * rp;
+#pragma unroll 4
+      for (int i = 0; i < TB; ++i) {
+        const double base = piv ? 0.0 : src[i][lane];
+        dst[i][lane] = (i == q) ? sq : fma(-src[i][q], sq, base);
+      }
+      __syncwarp(mask);
+    }
   }
 }
 
@@ -733,8 +741,8 @@ __device__ __forceinline__ void gj_tile_inverse(double (&a)[TB][TB + 1], double&
 // the rank-TB update flops of a plain Gauss-Jordan inverse and removes its
 // column-panel product (A_IK P is the transpose of the row panel P A_KI).
 // Two launches per pivot step:
-//  (1) panel: every CTA jb inverts the pivot tile itself (no serial pivot
-//      launch), saves the original panel tile X_J = A_KJ to Xb and writes
+//  (1) panel: every CTA jb inverts the pivot tile itself with one warp (no
+//      serial pivot launch), saves the original panel tile X_J = A_KJ to Xb and writes
 //      R_J = P X_J; CTA K writes P;
 //  (2) update: D_IJ -= X_I^T R_J for ib <= jb off the pivot row/column, and
 //      the panel row/column and the pivot tile are overwritten with R and -P
@@ -748,8 +756,7 @@ __device__ __forceinline__ void gj_tile_inverse(double (&a)[TB][TB + 1], double&
 template <int TB>
 __global__ void __launch_bounds__(TB * TB) k_sw_panel(const double* D, int64_t ld, int k,
                                                      double* P, double* R, double* Xb) {
-  __shared__ double a[TB][TB + 1], xs[TB][TB + 1];
-  __shared__ double rpiv;
+  __shared__ double a[TB][TB + 1], xs[TB][TB + 1], tb[TB][TB + 1];
   const int jb = blockIdx.x;
   const int i = threadIdx.y, j = threadIdx.x;
   a[i][j] = D[(int64_t)(k * TB + i) * ld + k * TB + j];
@@ -758,7 +765,8 @@ __global__ void __launch_bounds__(TB * TB) k_sw_panel(const double* D, int64_t l
     else xs[j][i] = D[(int64_t)(jb * TB + i) * ld + k * TB + j];   // coalesced, transposed in smem
   }
   __syncthreads();
-  gj_tile_inverse<TB>(a, rpiv, i, j);
+  if (i == 0) gj_tile_inverse_warp<TB>(a, tb, j);   // lanes 0..TB-1 of warp 0
+  __syncthreads();
   if (jb == k) {
     P[i * TB + j] = a[i][j];
     return;
