@@ -705,31 +705,35 @@ constexpr int GJB = 32;   // tile of the final mirror / negate pass
 constexpr int SWB = 16;   // pivot block of the sweep operator
 
 // Invert a TB x TB SPD tile in shared memory (Gauss-Jordan without pivoting)
-// with the first TB lanes of one warp: lane j owns column j; every pivot step
-// reads tile a and writes tile b (two shared buffers, no hazard inside a
-// step, one __syncwarp per step); TB is even, so the inverse ends in a.  Each
-// lane issues one FP64 operation per row (GB300's FP64 pipe is narrow): the
-// pivot column's -a_iq / a_qq is fma(-a_iq, 1 / a_qq, 0), the other columns
-// get fma(-a_iq, a_qj / a_qq, a_ij).
+// with TB*TB threads, (i, j) = (y, x).  Every pivot step reads tile a and
+// writes tile b (two shared buffers: no hazard inside a step) and costs one
+// barrier: the thread that computes the next pivot element also computes its
+// reciprocal in the same step (GB300's FP64 pipe is narrow and a divide is a
+// long dependent sequence, so there is one per step, off the other threads'
+// path); all other elements take one multiply or FMA.  A single warp would
+// use only its own sub-partition's share of the FP64 pipe.  TB is even, so
+// the inverse ends in a.
 template <int TB>
-__device__ __forceinline__ void gj_tile_inverse_warp(double (&a)[TB][TB + 1],
-                                                     double (&b)[TB][TB + 1], int lane) {
-  constexpr unsigned mask = TB == 32 ? 0xffffffffu : ((1u << TB) - 1u);
+__device__ __forceinline__ void gj_tile_inverse(double (&a)[TB][TB + 1], double (&b)[TB][TB + 1],
+                                                double (&rpiv)[2], int i, int j) {
+  if (i == 0 && j == 0) rpiv[0] = 1.0 / a[0][0];
+  __syncthreads();
   for (int p = 0; p < TB; p += 2) {
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       double (&src)[TB][TB + 1] = h ? b : a;
       double (&dst)[TB][TB + 1] = h ? a : b;
       const int q = p + h;
-      const double rp = 1.0 / src[q][q];
-      const bool piv = lane == q;
-      const double sq = piv ? rp : src[q][lane] * rp;
-#pragma unroll 4
-      for (int i = 0; i < TB; ++i) {
-        const double base = piv ? 0.0 : src[i][lane];
-        dst[i][lane] = (i == q) ? sq : fma(-src[i][q], sq, base);
-      }
-      __syncwarp(mask);
+      const double rp = rpiv[h];
+      const double aiq = src[i][q], aqj = src[q][j];
+      double v;
+      if (i == q && j == q) v = rp;
+      else if (i == q) v = aqj * rp;
+      else if (j == q) v = -aiq * rp;
+      else v = fma(-aiq, aqj * rp, src[i][j]);
+      dst[i][j] = v;
+      if (i == q + 1 && j == q + 1) rpiv[h ^ 1] = 1.0 / v;   // next pivot (q + 1 < TB here)
+      __syncthreads();
     }
   }
 }
@@ -741,8 +745,8 @@ __device__ __forceinline__ void gj_tile_inverse_warp(double (&a)[TB][TB + 1],
 // the rank-TB update flops of a plain Gauss-Jordan inverse and removes its
 // column-panel product (A_IK P is the transpose of the row panel P A_KI).
 // Two launches per pivot step:
-//  (1) panel: every CTA jb inverts the pivot tile itself with one warp (no
-//      serial pivot launch), saves the original panel tile X_J = A_KJ to Xb and writes
+//  (1) panel: every CTA jb inverts the pivot tile itself (no serial pivot
+//      launch), saves the original panel tile X_J = A_KJ to Xb and writes
 //      R_J = P X_J; CTA K writes P;
 //  (2) update: D_IJ -= X_I^T R_J for ib <= jb off the pivot row/column, and
 //      the panel row/column and the pivot tile are overwritten with R and -P
@@ -757,6 +761,7 @@ template <int TB>
 __global__ void __launch_bounds__(TB * TB) k_sw_panel(const double* D, int64_t ld, int k,
                                                      double* P, double* R, double* Xb) {
   __shared__ double a[TB][TB + 1], xs[TB][TB + 1], tb[TB][TB + 1];
+  __shared__ double rpiv[2];
   const int jb = blockIdx.x;
   const int i = threadIdx.y, j = threadIdx.x;
   a[i][j] = D[(int64_t)(k * TB + i) * ld + k * TB + j];
@@ -765,8 +770,7 @@ __global__ void __launch_bounds__(TB * TB) k_sw_panel(const double* D, int64_t l
     else xs[j][i] = D[(int64_t)(jb * TB + i) * ld + k * TB + j];   // coalesced, transposed in smem
   }
   __syncthreads();
-  if (i == 0) gj_tile_inverse_warp<TB>(a, tb, j);   // lanes 0..TB-1 of warp 0
-  __syncthreads();
+  gj_tile_inverse<TB>(a, tb, rpiv, i, j);
   if (jb == k) {
     P[i * TB + j] = a[i][j];
     return;
