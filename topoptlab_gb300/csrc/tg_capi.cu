@@ -300,11 +300,9 @@ int32_t tg_oc(tg_ctx* ctx, const double* x, const double* dc, const double* dv, 
     h2d(dvd.p, dv, nel, c.st);
     const tg::OCScratch ocs{c.S.p, c.S.p + nel, c.S.p + 2 * nel};
     tg::oc_begin(nel, xd, dcd, dvd, c.flags.p, c.move, ocs, c.oc, g, c.st);
-    for (int k = 0; k < 16; ++k) {
-      tg::oc_steps(nel, xd, ocs, dvd, c.flags.p, c.move, c.part2, c.oc, 16, c.st);
-      d2h(c.h_oc, c.oc.p, 1, c.st);
-      if (c.h_oc->done) break;
-    }
+    tg::oc_steps(nel, xd, ocs, dvd, c.flags.p, c.move, c.part2, c.oc, 256, c.st);
+    d2h(c.h_oc, c.oc.p, 1, c.st);
+    if (c.h_oc->bar.err) throw tg::Error{TG_ETIMEOUT, "OC bisection: a grid barrier wait timed out"};
     if (!c.h_oc->done) throw tg::Error{TG_ENOTCONV, "OC bisection did not terminate"};
     tg::oc_finish(nel, xd, ocs, c.flags.p, c.move, xn, c.oc, c.st);
     d2h(xnew, xn.p, nel, c.st);
@@ -335,11 +333,9 @@ int32_t tg_oc_raw(int64_t n, const double* x, const double* dc, const double* dv
     tg::OCState h;
     const tg::OCScratch ocs{S.p, S.p + n, S.p + 2 * n};
     tg::oc_begin(n, xd, dcd, dvd, fl.p, move, ocs, oc, g, st, l1, l2);
-    for (int k = 0; k < 16; ++k) {
-      tg::oc_steps(n, xd, ocs, dvd, fl.p, move, part, oc, 16, st);
-      d2h(&h, oc.p, 1, st);
-      if (h.done) break;
-    }
+    tg::oc_steps(n, xd, ocs, dvd, fl.p, move, part, oc, 256, st);
+    d2h(&h, oc.p, 1, st);
+    if (h.bar.err) throw tg::Error{TG_ETIMEOUT, "OC bisection: a grid barrier wait timed out"};
     if (!h.done) throw tg::Error{TG_ENOTCONV, "OC bisection did not terminate"};
     tg::oc_finish(n, xd, ocs, fl.p, move, xn, oc, st);
     d2h(xnew, xn.p, n, st);

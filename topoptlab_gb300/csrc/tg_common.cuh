@@ -191,6 +191,45 @@ __device__ inline double block_max(double v, double* sh) {
   return v;
 }
 
+// Grid-wide barrier of a cooperative launch (all blocks co-resident):
+// arrival count plus a generation number.  Every wait is bounded: a block that
+// polls about 2^22 times (a fraction of a second) without the generation
+// moving, or that sees another block's error, records the error flag and
+// returns false; callers then leave the kernel and the host reports
+// TG_ETIMEOUT.  count and err start at zero.
+struct GridBar {
+  unsigned int count, gen;
+  int err;
+};
+__device__ __forceinline__ bool grid_sync(GridBar* b) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ok = 1;
+    const unsigned int nb = gridDim.x * gridDim.y * gridDim.z;
+    const unsigned int g = *(volatile unsigned int*)&b->gen;
+    __threadfence();
+    if (atomicAdd(&b->count, 1u) == nb - 1) {
+      atomicExch(&b->count, 0u);
+      __threadfence();
+      atomicAdd(&b->gen, 1u);
+    } else {
+      unsigned int polls = 0;
+      while (*(volatile unsigned int*)&b->gen == g) {
+        if (*(volatile int*)&b->err != 0 || ++polls > (1u << 22)) {
+          atomicExch(&b->err, 1);
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
 // Number of partial-sum slots used by every grid-wide reduction.  Grids that
 // reduce are launched with at most this many blocks (grid-stride loops), so
 // the summation order depends only on the problem size, never on timing.

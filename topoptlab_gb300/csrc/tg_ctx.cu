@@ -846,17 +846,12 @@ void ctx_step(Ctx& c, tg_iter_out& out) {
   else TG_CUDA(cudaMemcpyAsync(c.dcf.p, c.dc.p, sizeof(double) * nel, cudaMemcpyDeviceToDevice, c.st));
   // OC
   const OCScratch ocs{c.S.p, c.S.p + nel, c.S.p + 2 * nel};
+  // the whole bisection in one launch; its state is read back with the
+  // iteration's scalars at the end (no host round trip in between)
   oc_begin(nel, c.x, c.dcf, c.dv, c.flags.p, c.move, ocs, c.oc, c.g_oc, c.st);
-  int guard = 0;
-  for (;;) {
-    oc_steps(nel, c.x, ocs, c.dv, c.flags.p, c.move, c.part2, c.oc, 16, c.st);
-    TG_CUDA(cudaMemcpyAsync(c.h_oc, c.oc.p, sizeof(OCState), cudaMemcpyDeviceToHost, c.st));
-    TG_CUDA(cudaStreamSynchronize(c.st));
-    if (c.h_oc->done) break;
-    if (++guard > 16) throw Error{ENOTCONV, "OC bisection did not terminate within 256 steps"};
-  }
+  oc_steps(nel, c.x, ocs, c.dv, c.flags.p, c.move, c.part2, c.oc, 256, c.st);
   oc_finish(nel, c.x, ocs, c.flags.p, c.move, c.xnew, c.oc, c.st);
-  c.g_oc = c.h_oc->gt;
+  TG_CUDA(cudaMemcpyAsync(c.h_oc, c.oc.p, sizeof(OCState), cudaMemcpyDeviceToHost, c.st));
   // x_old <- x ; x <- x_new
   std::swap(c.xold.p, c.x.p);
   std::swap(c.x.p, c.xnew.p);
@@ -870,6 +865,9 @@ void ctx_step(Ctx& c, tg_iter_out& out) {
   reduce_partials(c.part2, nbe, c.scal.p + 2, true, c.st);
   TG_CUDA(cudaMemcpyAsync(c.h_scal, c.scal.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, c.st));
   TG_CUDA(cudaStreamSynchronize(c.st));
+  if (c.h_oc->bar.err) throw Error{ETIMEOUT, "OC bisection: a grid barrier wait timed out"};
+  if (!c.h_oc->done) throw Error{ENOTCONV, "OC bisection did not terminate within 256 steps"};
+  c.g_oc = c.h_oc->gt;
   const double vol_sum = c.h_scal[1];
   float ms = 0.f;
   TG_CUDA(cudaEventElapsedTime(&ms, c.ev0, c.ev1));

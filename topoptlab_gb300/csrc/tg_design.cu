@@ -8,6 +8,7 @@
 // (optimizer/optimality_criterion.py:9-79), the change/volume reductions
 // (topology_optimization.py:516, :654, :670) and the PCG vector algebra
 // (linear_solvers.py:114-134).
+#include <algorithm>
 #include "tg_ops.cuh"
 #include "tg_design.cuh"
 
@@ -164,8 +165,7 @@ void reduce_partials(const double* part, int nb, double* out, bool is_max, cudaS
 }
 
 // ---------------------------------------------------------------------------
-// OC bisection: each launch is one bisection step; the last block to finish
-// sums the partials in fixed order and advances (l1, l2, lmid) or sets done.
+// OC bisection (optimizer/optimality_criterion.py:59-79)
 // ---------------------------------------------------------------------------
 __global__ void k_oc_init(OCState* s, double g, double l1, double l2) {
   s->l1 = l1;
@@ -178,6 +178,8 @@ __global__ void k_oc_init(OCState* s, double g, double l1, double l2) {
   s->sc = 1.0 / sqrt(s->lmid);
   s->sc_last = s->sc;
   s->ticket = 0;
+  s->bar.count = 0;
+  s->bar.err = 0;
 }
 
 // Per design iteration: P = x * sqrt(-dc/dv) and, when stored, the bounds
@@ -220,47 +222,64 @@ __device__ __forceinline__ double oc_value(int64_t i, double xi, const OCScratch
   return xn;
 }
 
+// The whole bisection in one cooperative launch (all blocks co-resident):
+// per step every block sums its elements' dv * (xnew - x) in a fixed
+// grid-stride order, writes the block sum to the partials of the step's
+// parity, meets the others at a grid barrier and then sums all partials in
+// the same fixed order, so every block takes the same decision on (l1, l2)
+// without another launch or a host round trip.  Double-buffered partials need
+// one barrier per step: a block writes step k+1's partials only after every
+// block has passed step k's barrier, i.e. finished reading step k-1's.
+// Block 0 writes the final state.  Runs at most max_steps steps.
 template <bool BOUNDS>
-__global__ void __launch_bounds__(RED_THREADS) k_oc_step(int64_t n, const double* __restrict__ x,
-                                                        OCScratch sc, const double* __restrict__ dv,
-                                                        const int8_t* __restrict__ flags,
-                                                        double move, double* part, OCState* st) {
+__global__ void __launch_bounds__(RED_THREADS) k_oc_bisect(int64_t n, const double* __restrict__ x,
+                                                          OCScratch sc,
+                                                          const double* __restrict__ dv,
+                                                          const int8_t* __restrict__ flags,
+                                                          double move, double* part, OCState* st,
+                                                          int max_steps) {
   __shared__ double sh[32];
-  __shared__ int last;
-  if (st->done) return;   // uniform: written by a previous launch
-  const double s = st->sc;
-  double acc = 0.0;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const double xi = x[i];
-    acc += dv[i] * (oc_value<BOUNDS>(i, xi, sc, flags, move, s) - xi);
-  }
-  const double bs = block_sum(acc, sh);
-  if (threadIdx.x == 0) {
-    part[blockIdx.x] = bs;
-    __threadfence();
-    const unsigned t = atomicAdd(&st->ticket, 1u);
-    last = (t == gridDim.x - 1);
-  }
-  __syncthreads();
-  if (!last) return;
-  __threadfence();
-  const double tot = sum_partials(part, gridDim.x, sh);
-  if (threadIdx.x == 0) {
-    const double gt = st->g + tot;
-    st->gt = gt;
-    st->sc_last = s;
-    if (gt > 0) st->l1 = st->lmid;
-    else st->l2 = st->lmid;
-    st->nsteps += 1;
-    const double l1 = st->l1, l2 = st->l2;
-    if ((l2 - l1) / (l1 + l2) > 1e-3) {
-      st->lmid = 0.5 * (l2 + l1);
-      st->sc = 1.0 / sqrt(st->lmid);
-    } else {
-      st->done = 1;
+  __shared__ double tot_s;
+  double l1 = st->l1, l2 = st->l2, lmid = st->lmid, s = st->sc, s_last = st->sc_last;
+  double gt = st->gt;
+  const double g = st->g;
+  int done = st->done, steps = 0;
+  const unsigned int nb = gridDim.x;
+  while (!done && steps < max_steps) {
+    double acc = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+      const double xi = x[i];
+      acc += dv[i] * (oc_value<BOUNDS>(i, xi, sc, flags, move, s) - xi);
     }
-    st->ticket = 0;
+    double* pp = part + (steps & 1) * nb;
+    const double bs = block_sum(acc, sh);
+    if (threadIdx.x == 0) pp[blockIdx.x] = bs;
+    if (!grid_sync(&st->bar)) return;
+    const double t0 = sum_partials(pp, (int)nb, sh);
+    if (threadIdx.x == 0) tot_s = t0;
+    __syncthreads();
+    gt = g + tot_s;
+    s_last = s;
+    if (gt > 0) l1 = lmid;
+    else l2 = lmid;
+    ++steps;
+    if ((l2 - l1) / (l1 + l2) > 1e-3) {
+      lmid = 0.5 * (l2 + l1);
+      s = 1.0 / sqrt(lmid);
+    } else {
+      done = 1;
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    st->l1 = l1;
+    st->l2 = l2;
+    st->lmid = lmid;
+    st->sc = s;
+    st->sc_last = s_last;
+    st->gt = gt;
+    st->done = done;
+    st->nsteps += steps;
   }
 }
 
@@ -286,14 +305,21 @@ void oc_begin(int64_t n, const double* x, const double* dc, const double* dv, co
 }
 void oc_steps(int64_t n, const double* x, OCScratch sc, const double* dv, const int8_t* flags,
               double move, double* part, OCState* st, int nsteps, cudaStream_t s) {
-  const unsigned blocks = red_blocks(n);
+  // co-resident grid: at most half the partial slots (double-buffered), what
+  // the device holds at once, and at least 8 elements per thread (small
+  // designs stepped concurrently take few SMs each)
+  int dev = 0, nsm = 0, per_sm = 0;
+  TG_CUDA(cudaGetDevice(&dev));
+  TG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const void* fn = sc.lo ? (const void*)k_oc_bisect<true> : (const void*)k_oc_bisect<false>;
+  TG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, RED_THREADS, 0));
+  const int64_t cap = std::min<int64_t>(RED_BLOCKS / 2, (int64_t)nsm * std::max(per_sm, 1));
+  const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(cdiv(n, 8 * RED_THREADS), cap));
+  void* args[] = {(void*)&n, (void*)&x, (void*)&sc, (void*)&dv, (void*)&flags, (void*)&move,
+                  (void*)&part, (void*)&st, (void*)&nsteps};
   prof_begin(PK_OC, s);
-  for (int k = 0; k < nsteps; ++k) {
-    if (sc.lo) k_oc_step<true><<<blocks, RED_THREADS, 0, s>>>(n, x, sc, dv, flags, move, part, st);
-    else k_oc_step<false><<<blocks, RED_THREADS, 0, s>>>(n, x, sc, dv, flags, move, part, st);
-  }
+  TG_CUDA(cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(RED_THREADS), args, 0, s));
   prof_end(PK_OC, s);
-  count_launches(nsteps - 1);
   TG_CHECK_LAUNCH();
 }
 void oc_finish(int64_t n, const double* x, OCScratch sc, const int8_t* flags, double move,

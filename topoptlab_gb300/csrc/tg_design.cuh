@@ -12,6 +12,7 @@ struct OCState {
   double sc_last;    // 1/sqrt(lmid) of the last evaluated step
   int done, nsteps;
   unsigned int ticket;
+  GridBar bar;       // barrier of the one-launch bisection (bar.err: a wait timed out)
 };
 // per-call scratch: P = x*sqrt(-dc/dv); lo/hi = the move-limit bounds with the
 // passive/active flags folded in (both null: recomputed from x every step)
@@ -39,7 +40,8 @@ void reduce_partials(const double* part, int nb, double* out, bool is_max, cudaS
 void oc_begin(int64_t n, const double* x, const double* dc, const double* dv, const int8_t* flags,
               double move, OCScratch sc, OCState* st, double g, cudaStream_t s, double l1 = 0.0,
               double l2 = 1e9);
-// nsteps bisection steps (launches after `done` return at once)
+// up to nsteps bisection steps in one cooperative launch (none once `done`);
+// st->bar.err set: a grid barrier timed out
 void oc_steps(int64_t n, const double* x, OCScratch sc, const double* dv, const int8_t* flags,
               double move, double* part, OCState* st, int nsteps, cudaStream_t s);
 // xnew at the last evaluated lmid (call once `done` is set)

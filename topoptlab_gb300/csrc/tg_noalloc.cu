@@ -83,12 +83,10 @@ int32_t tg_oc_noalloc(int64_t n, const double* x, const double* dc, const double
     // one scratch array: the move-limit bounds are recomputed from x each step
     const tg::OCScratch ocs{s->S, nullptr, nullptr};
     tg::oc_begin(n, x, dc, dv, el_flags, move, ocs, &s->state, g, st, l1, l2);
-    for (int k = 0; k < 16; ++k) {
-      tg::oc_steps(n, x, ocs, dv, el_flags, move, s->part, &s->state, 16, st);
-      TG_CUDA(cudaMemcpyAsync(&h, &s->state, sizeof(tg::OCState), cudaMemcpyDeviceToHost, st));
-      TG_CUDA(cudaStreamSynchronize(st));
-      if (h.done) break;
-    }
+    tg::oc_steps(n, x, ocs, dv, el_flags, move, s->part, &s->state, 256, st);
+    TG_CUDA(cudaMemcpyAsync(&h, &s->state, sizeof(tg::OCState), cudaMemcpyDeviceToHost, st));
+    TG_CUDA(cudaStreamSynchronize(st));
+    if (h.bar.err) return fail(TG_ETIMEOUT, "tg_oc_noalloc: a grid barrier wait timed out");
     if (!h.done) return fail(TG_ENOTCONV, "tg_oc_noalloc: OC bisection did not terminate");
     tg::oc_finish(n, x, ocs, el_flags, move, xnew, &s->state, st);
     TG_CUDA(cudaStreamSynchronize(st));
