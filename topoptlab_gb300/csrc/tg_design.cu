@@ -305,16 +305,16 @@ void oc_begin(int64_t n, const double* x, const double* dc, const double* dv, co
 }
 void oc_steps(int64_t n, const double* x, OCScratch sc, const double* dv, const int8_t* flags,
               double move, double* part, OCState* st, int nsteps, cudaStream_t s) {
-  // co-resident grid: at most half the partial slots (double-buffered), what
-  // the device holds at once, and at least 8 elements per thread (small
-  // designs stepped concurrently take few SMs each)
+  // co-resident grid: at most half the partial slots (double-buffered) and
+  // what the device holds at once (the per-element FP64 work of a step needs
+  // all the warps it can get on GB300's narrow FP64 pipe)
   int dev = 0, nsm = 0, per_sm = 0;
   TG_CUDA(cudaGetDevice(&dev));
   TG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   const void* fn = sc.lo ? (const void*)k_oc_bisect<true> : (const void*)k_oc_bisect<false>;
   TG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, RED_THREADS, 0));
   const int64_t cap = std::min<int64_t>(RED_BLOCKS / 2, (int64_t)nsm * std::max(per_sm, 1));
-  const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(cdiv(n, 8 * RED_THREADS), cap));
+  const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(cdiv(n, RED_THREADS), cap));
   void* args[] = {(void*)&n, (void*)&x, (void*)&sc, (void*)&dv, (void*)&flags, (void*)&move,
                   (void*)&part, (void*)&st, (void*)&nsteps};
   prof_begin(PK_OC, s);
