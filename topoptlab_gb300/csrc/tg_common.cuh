@@ -191,6 +191,14 @@ __device__ inline double block_max(double v, double* sh) {
   return v;
 }
 
+// sum of nb per-block partials in fixed order (bypassing L1: other blocks
+// wrote them); result valid in thread 0
+__device__ inline double sum_partials(const double* part, int nb, double* sh) {
+  double v = 0.0;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) v += __ldcg(part + i);
+  return block_sum(v, sh);
+}
+
 // Grid-wide barrier of a cooperative launch (all blocks co-resident):
 // arrival count plus a generation number.  Every wait is bounded: a block that
 // polls about 2^22 times (a fraction of a second) without the generation

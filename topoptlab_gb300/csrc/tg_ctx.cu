@@ -474,12 +474,18 @@ static void level_apply(Ctx& c, int l, const T* in, T* out, const T* b, int mode
   }
 }
 
-template <typename T> void vcycle(Ctx& c, int l, const T* b, T* x, bool prescaled) {
+template <typename T> void vcycle(Ctx& c, int l, const T* b, T* x, bool prescaled, int dot_op) {
   Level& v = *c.lv[l];
   const int64_t n = v.g.ndofs();
   if (l == c.L - 1) {
-    ProfScope ps(PK_TRANSFER, c.st);
-    dense_apply<T>(c.Dc, c.nc, c.ldc, b, x, c.gjwork, c.st);   // GJ scratch is idle here
+    {
+      ProfScope ps(PK_TRANSFER, c.st);
+      dense_apply<T>(c.Dc, c.nc, c.ldc, b, x, c.gjwork, c.st);   // GJ scratch is idle here
+    }
+    if (dot_op >= 0) {
+      ProfScope ps(PK_VECTOR, c.st);
+      dot<T, T>(n, b, x, c.part, c.pcg, dot_op, c.st);
+    }
     return;
   }
   // 2*nsmooth - 1 sweeps swap the buffers an odd number of times: starting in
@@ -511,17 +517,29 @@ template <typename T> void vcycle(Ctx& c, int l, const T* b, T* x, bool prescale
     ProfScope ps(PK_TRANSFER, c.st);
     prolong_add<T>(v.g, w.g, v.fix, LvBufs<T>::x(w), bufs[cur], c.st);
   }
+  // the fine level's last sweep of the FP32 cycle also forms the PCG dot b . x
+  const bool fused_dot = dot_op >= 0 && l == 0 && std::is_same<T, float>::value;
   for (int s = 0; s < c.nsmooth; ++s) {
-    level_apply<T>(c, l, bufs[cur], bufs[1 - cur], b, AM_JACOBI);
+    if (fused_dot && s == c.nsmooth - 1)
+      fine_apply_dot<float, __nv_bfloat16>(c.op, c.s16, (const float*)bufs[cur],
+                                           (float*)bufs[1 - cur], (const float*)b,
+                                           (const float*)LvBufs<T>::dinv(v), c.omega, AM_JACOBI,
+                                           c.part, c.pcg, dot_op, c.st);
+    else
+      level_apply<T>(c, l, bufs[cur], bufs[1 - cur], b, AM_JACOBI);
     cur = 1 - cur;
+  }
+  if (dot_op >= 0 && !fused_dot) {
+    ProfScope ps(PK_VECTOR, c.st);
+    dot<T, T>(n, b, bufs[cur], c.part, c.pcg, dot_op, c.st);
   }
   if (bufs[cur] != x) {
     ProfScope ps(PK_VECTOR, c.st);
     TG_CUDA(cudaMemcpyAsync(x, bufs[cur], sizeof(T) * n, cudaMemcpyDeviceToDevice, c.st));
   }
 }
-template void vcycle<double>(Ctx&, int, const double*, double*, bool);
-template void vcycle<float>(Ctx&, int, const float*, float*, bool);
+template void vcycle<double>(Ctx&, int, const double*, double*, bool, int);
+template void vcycle<float>(Ctx&, int, const float*, float*, bool, int);
 
 template <typename T>
 static void precondition(Ctx& c, const T* r, T* z) {
@@ -708,15 +726,22 @@ static int pcg32(Ctx& c, double tol_abs, int maxiter) {
   TG_CUDA(cudaMemsetAsync(c.d32.p, 0, sizeof(float) * n, c.st));
   pcg_reset(c.pcg, c.st);
   const int it = run_loop(c, c.g32, c.l32, tol_abs, maxiter, [&] {
-    precondition<float>(c, c.r32, c.z32);
-    {
+    // z = M r with rho = r . z fused into the cycle's last fine sweep; q = A p
+    // with p . q (alpha) fused into the product
+    if (c.precond == TG_PRECOND_GMG) {
+      vcycle<float>(c, 0, c.r32, c.z32, false, DOT_RHO);
+    } else {
+      precondition<float>(c, c.r32, c.z32);
       ProfScope ps(PK_VECTOR, c.st);
       dot<float, float>(n, c.r32.p, c.z32.p, c.part, c.pcg, DOT_RHO, c.st);
+    }
+    {
+      ProfScope ps(PK_VECTOR, c.st);
       update_p<float>(n, c.z32, c.p32, c.pcg, c.st);
     }
-    fine_apply<float, float>(c.op, c.s32, c.p32, c.q32, nullptr, nullptr, 0.0, AM_Y, c.st);
+    fine_apply_dot<float, float>(c.op, c.s32, c.p32, c.q32, nullptr, nullptr, 0.0, AM_Y, c.part,
+                                 c.pcg, DOT_ALPHA, c.st);
     ProfScope ps(PK_VECTOR, c.st);
-    dot<float, float>(n, c.p32.p, c.q32.p, c.part, c.pcg, DOT_ALPHA, c.st);
     update_xr<float>(n, c.p32, c.q32, c.d32, c.r32, c.part, c.pcg, c.st);
   });
   check_finite(c.h_pcg->rr, "inner PCG residual");

@@ -130,8 +130,10 @@ void set_density(Ctx& c, const double* xPhys_dev);   // scale factors for xPhys
 // solve K u = b (b, u device FP64, u holds the warm start)
 void solve(Ctx& c, const double* b, double* u);
 // prescaled: the level's scratch buffer already holds omega D^-1 b (fused
-// into the restriction that produced b)
-template <typename T> void vcycle(Ctx& c, int l, const T* b, T* x, bool prescaled = false);
+// into the restriction that produced b); dot_op >= 0: also the PCG dot b . x
+// of the result into c.pcg (DOT_RHO), fused into the last fine sweep
+template <typename T>
+void vcycle(Ctx& c, int l, const T* b, T* x, bool prescaled = false, int dot_op = -1);
 // Helmholtz PDE filter: set-up (KF: screened Poisson element matrix, host)
 // and y = TF^T KF^-1 TF (v * mul) [/ max(1e-3, xdiv)]; mul and xdiv may be
 // null; with part_sum / part_max also the sums of the density filter

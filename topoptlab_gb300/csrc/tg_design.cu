@@ -142,11 +142,6 @@ void simp_scale(int64_t n, const double* x, double eps, double penal, double* s6
 // ---------------------------------------------------------------------------
 // deterministic finalisation of block partials (single block, fixed order)
 // ---------------------------------------------------------------------------
-__device__ double sum_partials(const double* part, int nb, double* sh) {
-  double v = 0.0;
-  for (int i = threadIdx.x; i < nb; i += blockDim.x) v += __ldcg(part + i);
-  return block_sum(v, sh);
-}
 __device__ double max_partials(const double* part, int nb, double* sh) {
   double v = 0.0;
   for (int i = threadIdx.x; i < nb; i += blockDim.x) v = fmax(v, __ldcg(part + i));
@@ -377,19 +372,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_dot(int64_t n, const TA* __rest
   __threadfence();
   const double tot = sum_partials(part, gridDim.x, sh);
   if (threadIdx.x == 0) {
-    if (op == DOT_RHO) {
-      st->beta = (st->iter > 0) ? tot / st->rho : 0.0;
-      st->rho = tot;
-    } else if (op == DOT_ALPHA) {
-      st->pq = tot;
-      st->alpha = st->rho / tot;
-    } else if (op == DOT_RR) {
-      st->rr = tot;
-      st->rnorm = sqrt(tot);
-      st->rinv = tot > 0.0 ? 1.0 / st->rnorm : 0.0;
-    } else if (op == DOT_BB) {
-      st->bb = tot;
-    }
+    pcg_dot_finish(st, op, tot);
     st->ticket = 0;
   }
 }

@@ -32,6 +32,30 @@ struct PCGState {
   int maxit;         //   and iter < maxit (and rr finite)
 };
 
+// PCG scalars from a finished dot product (the last block of a reduction)
+__device__ inline void pcg_dot_finish(PCGState* st, int op, double tot) {
+  if (op == DOT_RHO) {
+    st->beta = (st->iter > 0) ? tot / st->rho : 0.0;
+    st->rho = tot;
+  } else if (op == DOT_ALPHA) {
+    st->pq = tot;
+    st->alpha = st->rho / tot;
+  } else if (op == DOT_RR) {
+    st->rr = tot;
+    st->rnorm = sqrt(tot);
+    st->rinv = tot > 0.0 ? 1.0 / st->rnorm : 0.0;
+  } else if (op == DOT_BB) {
+    st->bb = tot;
+  }
+}
+
+// fine_apply that also forms a PCG dot of its output, finalised into the PCG
+// state like dot(): DOT_ALPHA = u . y (mode AM_Y), DOT_RHO = b . y (AM_JACOBI)
+template <typename T, typename S>
+void fine_apply_dot(const FineOp& op, const S* scale, const T* u, T* y, const T* b, const T* dinv,
+                    double omega, int mode, double* part, PCGState* pst, int dot_op,
+                    cudaStream_t st);
+
 void filter_apply_ex(const Grid& g, const FilterStencil& fs, const double* x, const double* d,
                      const double* Hs, double* y, int mode, const double* xold, double* part_sum,
                      double* part_max, cudaStream_t st);

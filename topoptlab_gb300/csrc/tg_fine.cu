@@ -18,6 +18,7 @@
 #include <algorithm>
 #include <type_traits>
 #include "tg_ops.cuh"
+#include "tg_design.cuh"
 
 namespace tg {
 
@@ -92,6 +93,8 @@ template <typename T, typename S> struct ApplyArgs {
   T omega;
   const T* KE;      // dense path
   Sector<T> B;
+  double* part;     // fused PCG dot: per-CTA partial sums
+  PCGState* pst;    //   and the state it finalises
 };
 
 template <int NDIM, int NDOF, typename T, bool SECTOR>
@@ -291,7 +294,10 @@ template <int NDOF, typename T, int KIND> constexpr size_t smem() {
 }
 }  // namespace zs
 
-template <int NDOF, typename T, typename S, int KIND, int MODE>
+// DOTK >= 0: also the PCG dot DOTK of the output with the input (AM_Y: u . y)
+// or with b (AM_JACOBI: b . y) over the owned nodes, one FP64 partial per CTA,
+// summed in fixed order by the last CTA to finish.
+template <int NDOF, typename T, typename S, int KIND, int MODE, int DOTK = -1>
 __global__ void __launch_bounds__(zs::NT, sizeof(T) == 8 ? 2 : 4) k_fine_zstream(ApplyArgs<T, S> a,
                                                                                 int zc) {
   using namespace zs;
@@ -363,6 +369,7 @@ __global__ void __launch_bounds__(zs::NT, sizeof(T) == 8 ? 2 : 4) k_fine_zstream
   cp_async_wait_all();
   __syncthreads();
   T rho = load_rho(zbeg - 1);
+  T dacc = T(0);
   T acc[NDOF];
 #pragma unroll
   for (int c = 0; c < NDOF; ++c) acc[c] = T(0);
@@ -428,7 +435,10 @@ __global__ void __launch_bounds__(zs::NT, sizeof(T) == 8 ? 2 : 4) k_fine_zstream
           if (MODE == AM_Y) out = acc[c];
           else if (MODE == AM_RES) out = bv[c] - acc[c];
           else out = pu[c * PLANE] + a.omega * dv[c] * (bv[c] - acc[c]);
-          a.y[nid * NDOF + c] = ((fx >> c) & 1) ? T(0) : out;
+          out = ((fx >> c) & 1) ? T(0) : out;
+          a.y[nid * NDOF + c] = out;
+          if (DOTK == DOT_ALPHA) dacc = fma(pu[c * PLANE], out, dacc);
+          else if (DOTK == DOT_RHO) dacc = fma(bv[c], out, dacc);
         }
       }
 #pragma unroll
@@ -439,6 +449,27 @@ __global__ void __launch_bounds__(zs::NT, sizeof(T) == 8 ? 2 : 4) k_fine_zstream
     __syncthreads();
     const int t = s0;
     s0 = s1; s1 = s2; s2 = t;
+  }
+  if constexpr (DOTK >= 0) {
+    __shared__ double sh[32];
+    __shared__ int last;
+    const double bs = block_sum((double)dacc, sh);
+    const unsigned nblk = gridDim.x * gridDim.y * gridDim.z;
+    const unsigned bid = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+    if (tid == 0) {
+      a.part[bid] = bs;
+      __threadfence();
+      last = (atomicAdd(&a.pst->ticket, 1u) == nblk - 1);
+    }
+    __syncthreads();
+    if (last) {
+      __threadfence();
+      const double tot = sum_partials(a.part, (int)nblk, sh);
+      if (tid == 0) {
+        pcg_dot_finish(a.pst, DOTK, tot);
+        a.pst->ticket = 0;
+      }
+    }
   }
 }
 
@@ -452,23 +483,38 @@ static int sm_count() {
   return n;
 }
 
-template <int NDOF, typename T, typename S, int KIND, int MODE>
+// z-streaming launch shape: (y columns, x columns, z chunks) and the chunk
+// length; as many z chunks as fit in one wave of resident CTAs (4 per SM in
+// FP32, 2 in FP64), so that no second partial wave doubles the kernel time
+struct ZsShape {
+  int gy, gx, chunks, zc;
+  int64_t ctas() const { return (int64_t)gy * gx * chunks; }
+};
+static ZsShape zstream_shape(const Grid& g, bool fp64) {
+  ZsShape s;
+  s.gy = (int)cdiv(g.nny, zs::OY);
+  s.gx = (int)cdiv(g.nnx, zs::OX);
+  const int target = sm_count() * (fp64 ? 2 : 4);
+  const int cols = s.gx * s.gy;
+  const int chunks = std::max(1, std::min(g.nnz, target / cols));
+  s.zc = (int)cdiv(g.nnz, chunks);
+  s.chunks = (int)cdiv(g.nnz, s.zc);
+  return s;
+}
+
+template <int NDOF, typename T, typename S, int KIND, int MODE, int DOTK = -1>
 static void launch_zstream(const ApplyArgs<T, S>& a, cudaStream_t st) {
   constexpr size_t smem = zs::smem<NDOF, T, KIND>();
-  auto kern = k_fine_zstream<NDOF, T, S, KIND, MODE>;
+  auto kern = k_fine_zstream<NDOF, T, S, KIND, MODE, DOTK>;
   static const bool attr_set = [&] {   // once per instantiation, thread-safe
     TG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     return true;
   }();
   (void)attr_set;
-  const int gy = (int)cdiv(a.g.nny, zs::OY), gx = (int)cdiv(a.g.nnx, zs::OX);
-  // z chunks: as many as fit in one wave of resident CTAs (4 per SM in FP32,
-  // 2 in FP64), so that no second partial wave doubles the kernel time
-  const int target = sm_count() * (sizeof(T) == 8 ? 2 : 4);
-  const int cols = gx * gy;
-  int chunks = std::max(1, std::min(a.g.nnz, target / cols));
-  const int zc = (int)cdiv(a.g.nnz, chunks);
-  chunks = (int)cdiv(a.g.nnz, zc);
+  const ZsShape sh = zstream_shape(a.g, sizeof(T) == 8);
+  const int gy = sh.gy, gx = sh.gx, chunks = sh.chunks, zc = sh.zc;
+  if (DOTK >= 0 && sh.ctas() > RED_BLOCKS)
+    throw Error{EINVAL_, "fused dot: more CTAs than partial-sum slots"};
   const int pk = std::is_same<T, double>::value ? PK_FINE_F64
                  : (std::is_same<S, float>::value ? PK_FINE_F32 : PK_FINE_BF16);
   prof_begin(pk, st);
@@ -534,6 +580,7 @@ void fine_apply(const FineOp& op, const S* scale, const T* u, T* y, const T* b, 
   ApplyArgs<T, S> a;
   a.g = op.g; a.fix = op.fix; a.scale = scale; a.u = u; a.y = y; a.b = b; a.dinv = dinv;
   a.omega = (T)omega; a.KE = ke_ptr<T>(op); a.B = sec_ref<T>(op);
+  a.part = nullptr; a.pst = nullptr;
   const int key = op.g.ndim * 10 + op.g.ndof;
   switch (key) {
     case 33: dispatch_apply<3, 3, T, S>(a, op.kind, mode, st); break;
@@ -543,6 +590,35 @@ void fine_apply(const FineOp& op, const S* scale, const T* u, T* y, const T* b, 
     default: throw Error{EINVAL_, "unsupported (ndim, nnode_dof) combination"};
   }
 }
+
+template <typename T, typename S>
+void fine_apply_dot(const FineOp& op, const S* scale, const T* u, T* y, const T* b, const T* dinv,
+                    double omega, int mode, double* part, PCGState* pst, int dot_op,
+                    cudaStream_t st) {
+  TG_REQUIRE((dot_op == DOT_ALPHA && mode == AM_Y) || (dot_op == DOT_RHO && mode == AM_JACOBI),
+             "fused dot: DOT_ALPHA with AM_Y or DOT_RHO with AM_JACOBI");
+  const bool zstream = op.g.ndim == 3 && op.g.ndof == 3 && op.kind == EK_SECTOR_HEX8 &&
+                       (int64_t)op.g.nnx * op.g.nny * 3 < (int64_t(1) << 31) &&
+                       zstream_shape(op.g, sizeof(T) == 8).ctas() <= RED_BLOCKS;
+  if (!zstream) {   // other kernels (or more CTAs than partial slots): product, then dot
+    fine_apply<T, S>(op, scale, u, y, b, dinv, omega, mode, st);
+    dot<T, T>(op.g.ndofs(), dot_op == DOT_ALPHA ? u : b, y, part, pst, dot_op, st);
+    return;
+  }
+  ApplyArgs<T, S> a;
+  a.g = op.g; a.fix = op.fix; a.scale = scale; a.u = u; a.y = y; a.b = b; a.dinv = dinv;
+  a.omega = (T)omega; a.KE = ke_ptr<T>(op); a.B = sec_ref<T>(op);
+  a.part = part; a.pst = pst;
+  if (dot_op == DOT_ALPHA) launch_zstream<3, T, S, EK_SECTOR_HEX8, AM_Y, DOT_ALPHA>(a, st);
+  else launch_zstream<3, T, S, EK_SECTOR_HEX8, AM_JACOBI, DOT_RHO>(a, st);
+}
+template void fine_apply_dot<float, float>(const FineOp&, const float*, const float*, float*,
+                                           const float*, const float*, double, int, double*,
+                                           PCGState*, int, cudaStream_t);
+template void fine_apply_dot<float, __nv_bfloat16>(const FineOp&, const __nv_bfloat16*,
+                                                   const float*, float*, const float*,
+                                                   const float*, double, int, double*, PCGState*,
+                                                   int, cudaStream_t);
 
 template void fine_apply<double, double>(const FineOp&, const double*, const double*, double*,
                                          const double*, const double*, double, int, cudaStream_t);
