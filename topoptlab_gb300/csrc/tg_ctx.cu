@@ -612,10 +612,12 @@ __global__ void k_loop_ctl(PCGState* s, double tol, int maxit) {
   s->tol = tol;
   s->maxit = maxit;
 }
+// continue while not converged (finite rr) and under the iteration cap
+__device__ __host__ inline bool pcg_continue(const PCGState& s) {
+  return isfinite(s.rr) && sqrt(s.rr) >= s.tol && s.iter < s.maxit;
+}
 __global__ void k_loop_continue(cudaGraphConditionalHandle h, const PCGState* s) {
-  const double rr = s->rr;
-  const bool cont = isfinite(rr) && sqrt(rr) >= s->tol && s->iter < s->maxit;
-  cudaGraphSetConditional(h, cont ? 1u : 0u);
+  cudaGraphSetConditional(h, pcg_continue(*s) ? 1u : 0u);
 }
 
 // Run PCG iterations (body = one iteration, no host read inside) until
@@ -639,8 +641,10 @@ static int run_loop(Ctx& c, Ctx::IterGraph& gr, Ctx::LoopGraph& lg, double tol, 
         TG_CUDA(cudaMemcpyAsync(c.h_pcg, c.pcg.p, sizeof(PCGState), cudaMemcpyDeviceToHost, c.st));
       });
       ++it;
-      const double rr = c.h_pcg->rr;
-      if (!std::isfinite(rr) || std::sqrt(rr) < tol) break;
+      PCGState s = *c.h_pcg;
+      s.tol = tol;
+      s.maxit = maxit;
+      if (!pcg_continue(s)) break;
     }
     return it;
   }
@@ -799,7 +803,12 @@ void solve(Ctx& c, const double* b, double* u) {
         to_unit_f32(n, c.r, c.pcg_out, c.r32, c.st);
       }
       const double inner = std::max(c.inner_rtol, 0.5 * tol / std::sqrt(rr));
-      total += pcg32(c, inner, c.maxiter - total);
+      // with multigrid at most 200 iterations per pass (a pass normally takes
+      // 20-60): an FP32 recurrence that stalls -- seen on one design of a
+      // 200-iteration run from random densities -- is restarted from the true
+      // FP64 residual by the next pass
+      const int cap = c.precond == TG_PRECOND_GMG ? 200 : c.maxiter;
+      total += pcg32(c, inner, std::min(c.maxiter - total, cap));
       ProfScope ps(PK_VECTOR, c.st);
       add_scaled_f32(n, c.d32, c.pcg_out, u, c.st);
       c.last_refine = k + 1;
