@@ -132,17 +132,17 @@ __global__ void __launch_bounds__(NDOF * 256) k_stencil_apply(Grid g, int TY, in
 // neighbour plane (dz = -1, 0, +1; in 2-D three columns dx), the partial sums
 // added in fixed order through shared memory.
 constexpr int SMALL_PAIRS = 128;
+// one block's work: pairs [vb * SMALL_PAIRS, (vb + 1) * SMALL_PAIRS) with
+// 3 * SMALL_PAIRS threads; ends with a barrier, so part can be reused
 template <int NDIM, int NDOF, typename T, int MODE>
-__global__ void __launch_bounds__(3 * SMALL_PAIRS) k_stencil_small(Grid g, const T* __restrict__ A,
-                                                                  const T* __restrict__ u,
-                                                                  T* __restrict__ y,
-                                                                  const T* __restrict__ b,
-                                                                  const T* __restrict__ dinv,
-                                                                  T omega) {
-  __shared__ T part[3][SMALL_PAIRS];
+__device__ __forceinline__ void stencil_small_vb(const Grid& g, const T* __restrict__ A,
+                                                 const T* __restrict__ u, T* __restrict__ y,
+                                                 const T* __restrict__ b,
+                                                 const T* __restrict__ dinv, T omega, int64_t vb,
+                                                 T (&part)[3][SMALL_PAIRS]) {
   const int slot = threadIdx.x % SMALL_PAIRS, pz = threadIdx.x / SMALL_PAIRS;
   const int64_t ld = g.nnodes();
-  const int64_t t = blockIdx.x * (int64_t)SMALL_PAIRS + slot;
+  const int64_t t = vb * SMALL_PAIRS + slot;
   const bool active = t < ld * NDOF;
   T acc = T(0);
   int ci = 0;
@@ -171,14 +171,26 @@ __global__ void __launch_bounds__(3 * SMALL_PAIRS) k_stencil_small(Grid g, const
   }
   part[pz][slot] = acc;
   __syncthreads();
-  if (pz != 0 || !active) return;
-  const T s = (part[0][slot] + part[1][slot]) + part[2][slot];
-  const int64_t k = n * NDOF + ci;
-  T out;
-  if (MODE == AM_Y) out = s;
-  else if (MODE == AM_RES) out = b[k] - s;
-  else out = u[k] + omega * dinv[k] * (b[k] - s);
-  y[k] = out;
+  if (pz == 0 && active) {
+    const T s = (part[0][slot] + part[1][slot]) + part[2][slot];
+    const int64_t k = n * NDOF + ci;
+    T out;
+    if (MODE == AM_Y) out = s;
+    else if (MODE == AM_RES) out = b[k] - s;
+    else out = u[k] + omega * dinv[k] * (b[k] - s);
+    y[k] = out;
+  }
+  __syncthreads();
+}
+template <int NDIM, int NDOF, typename T, int MODE>
+__global__ void __launch_bounds__(3 * SMALL_PAIRS) k_stencil_small(Grid g, const T* __restrict__ A,
+                                                                  const T* __restrict__ u,
+                                                                  T* __restrict__ y,
+                                                                  const T* __restrict__ b,
+                                                                  const T* __restrict__ dinv,
+                                                                  T omega) {
+  __shared__ T part[3][SMALL_PAIRS];
+  stencil_small_vb<NDIM, NDOF, T, MODE>(g, A, u, y, b, dinv, omega, blockIdx.x, part);
 }
 
 template <typename T>
@@ -560,13 +572,11 @@ template void stencil_expand<float>(const Grid&, const float*, double*, cudaStre
 // (optionally fused with the coarse level's first smoothing step from a zero
 // guess, xc = omega * dinvc * bc)
 template <int NDIM, int NDOF, typename T>
-__global__ void __launch_bounds__(256) k_restrict(Grid gf, Grid gc, const uint8_t* fixc,
-                                                  const T* __restrict__ rf, T* __restrict__ bc,
-                                                  const T* __restrict__ dinvc, T* __restrict__ xc,
-                                                  T omega) {
+__device__ __forceinline__ void restrict_one(const Grid& gf, const Grid& gc, const uint8_t* fixc,
+                                             const T* __restrict__ rf, T* __restrict__ bc,
+                                             const T* __restrict__ dinvc, T* __restrict__ xc,
+                                             T omega, int64_t t) {
   const int64_t ldc = gc.nnodes();
-  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t >= ldc * NDOF) return;
   const int c = (int)(t / ldc);
   const int64_t I = t - (int64_t)c * ldc;
   int ix, iy, iz;
@@ -584,6 +594,14 @@ __global__ void __launch_bounds__(256) k_restrict(Grid gf, Grid gc, const uint8_
   const T bv = ((fixc[I] >> c) & 1) ? T(0) : acc;
   bc[I * NDOF + c] = bv;
   if (xc) xc[I * NDOF + c] = omega * dinvc[I * NDOF + c] * bv;
+}
+template <int NDIM, int NDOF, typename T>
+__global__ void __launch_bounds__(256) k_restrict(Grid gf, Grid gc, const uint8_t* fixc,
+                                                  const T* __restrict__ rf, T* __restrict__ bc,
+                                                  const T* __restrict__ dinvc, T* __restrict__ xc,
+                                                  T omega) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t < gc.nnodes() * NDOF) restrict_one<NDIM, NDOF, T>(gf, gc, fixc, rf, bc, dinvc, xc, omega, t);
 }
 
 template <typename T>
@@ -607,11 +625,9 @@ template void restrict_<float>(const Grid&, const Grid&, const uint8_t*, const f
 // prolongation: one thread per fine node, all components; the 1, 2, 4 or 8
 // coarse parents follow from the parity of the fine coordinates
 template <int NDIM, int NDOF, typename T>
-__global__ void __launch_bounds__(256) k_prolong_add(Grid gf, Grid gc, const uint8_t* fixf,
-                                                     const T* __restrict__ xc,
-                                                     T* __restrict__ xf) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= gf.nnodes()) return;
+__device__ __forceinline__ void prolong_one(const Grid& gf, const Grid& gc, const uint8_t* fixf,
+                                            const T* __restrict__ xc, T* __restrict__ xf,
+                                            int64_t i) {
   int fx, fy, fz;
   node_xyz(gf, i, fx, fy, fz);
   const int ox = fx & 1, oy = fy & 1, oz = (NDIM == 3) ? (fz & 1) : 0;
@@ -632,6 +648,13 @@ __global__ void __launch_bounds__(256) k_prolong_add(Grid gf, Grid gc, const uin
 #pragma unroll
   for (int c = 0; c < NDOF; ++c)
     if (!((m >> c) & 1)) xf[i * NDOF + c] += w * acc[c];
+}
+template <int NDIM, int NDOF, typename T>
+__global__ void __launch_bounds__(256) k_prolong_add(Grid gf, Grid gc, const uint8_t* fixf,
+                                                     const T* __restrict__ xc,
+                                                     T* __restrict__ xf) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < gf.nnodes()) prolong_one<NDIM, NDOF, T>(gf, gc, fixf, xc, xf, i);
 }
 
 template <typename T>
@@ -869,29 +892,39 @@ void gj_inverse(double* D, int64_t n, int64_t ld, double* work, cudaStream_t st)
 // 8x the parallelism of a warp per row on the ~1200-row coarsest matrix).
 // Fixed rows of Dinv hold the identity and b is 0 there.
 constexpr int DA_CHUNKS = 8;
+// one warp: the partial sum of row `row` over column chunk `chunk`
+template <typename T>
+__device__ __forceinline__ void dense_partial_one(const double* __restrict__ Dinv, int64_t n,
+                                                  int64_t ld, const T* __restrict__ b,
+                                                  double* __restrict__ part, int64_t row,
+                                                  int chunk, int lane) {
+  const int64_t w = (n + DA_CHUNKS - 1) / DA_CHUNKS;
+  const int64_t j0 = chunk * w, j1 = min(n, j0 + w);
+  double acc = 0.0;
+#pragma unroll 4
+  for (int64_t j = j0 + lane; j < j1; j += 32) acc = fma(Dinv[row * ld + j], (double)b[j], acc);
+  acc = warp_sum(acc);
+  if (lane == 0) part[chunk * n + row] = acc;
+}
+template <typename T>
+__device__ __forceinline__ void dense_sum_one(const double* __restrict__ part, int64_t n,
+                                              T* __restrict__ x, int64_t row) {
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < DA_CHUNKS; ++k) s += part[k * n + row];
+  x[row] = (T)s;
+}
 template <typename T>
 __global__ void __launch_bounds__(256) k_dense_partial(const double* __restrict__ Dinv, int64_t n,
                                                       int64_t ld, const T* __restrict__ b,
                                                       double* __restrict__ part) {
   const int64_t row = blockIdx.x * 8 + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
-  if (row >= n) return;
-  const int64_t w = (n + DA_CHUNKS - 1) / DA_CHUNKS;
-  const int64_t j0 = blockIdx.y * w, j1 = min(n, j0 + w);
-  double acc = 0.0;
-#pragma unroll 4
-  for (int64_t j = j0 + lane; j < j1; j += 32) acc = fma(Dinv[row * ld + j], (double)b[j], acc);
-  acc = warp_sum(acc);
-  if (lane == 0) part[blockIdx.y * n + row] = acc;
+  if (row < n) dense_partial_one<T>(Dinv, n, ld, b, part, row, blockIdx.y, threadIdx.x & 31);
 }
 template <typename T>
 __global__ void k_dense_sum(const double* __restrict__ part, int64_t n, T* __restrict__ x) {
   const int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (row >= n) return;
-  double s = 0.0;
-#pragma unroll
-  for (int k = 0; k < DA_CHUNKS; ++k) s += part[k * n + row];
-  x[row] = (T)s;
+  if (row < n) dense_sum_one<T>(part, n, x, row);
 }
 
 template <typename T>
