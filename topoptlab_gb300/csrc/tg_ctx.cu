@@ -389,7 +389,6 @@ void ctx_init(Ctx& c, const tg_problem& p) {
   TG_CUDA(cudaMemcpy(c.x.p, x0.data(), sizeof(double) * nel, cudaMemcpyHostToDevice));
   TG_CUDA(cudaMemcpy(c.xPhys.p, x0.data(), sizeof(double) * nel, cudaMemcpyHostToDevice));
   c.g_oc = 0.0;
-  build_coarse_program(c);
   TG_CUDA(cudaStreamSynchronize(c.st));
 }
 
@@ -475,89 +474,6 @@ static void level_apply(Ctx& c, int l, const T* in, T* out, const T* b, int mode
   }
 }
 
-// Record the ops of vcycle<float>(c, l, b, x, prescaled) for the levels below
-// the large ones (small-level stencils, transfers, the dense coarsest solve),
-// mirroring vcycle's buffer use exactly.
-static void record_cycle(Ctx& c, int l, const float* b, float* x, bool prescaled,
-                         std::vector<CyOp>& ops) {
-  Level& v = *c.lv[l];
-  CyOp op{};
-  if (l == c.L - 1) {
-    op.type = CY_DENSE_PARTIAL; op.in = b; ops.push_back(op);
-    op = CyOp{}; op.type = CY_DENSE_SUM; op.out = x; ops.push_back(op);
-    return;
-  }
-  TG_REQUIRE(prescaled, "coarse cycle program: level entered without the fused first sweep");
-  float* bufs[2] = {x, v.t32};
-  int cur = 1;
-  auto sweep = [&](const float* in, float* out, int mode) {
-    CyOp s{};
-    s.type = CY_STENCIL; s.mode = mode; s.gf = v.g; s.A = v.A32; s.in = in; s.out = out; s.b = b;
-    s.dinv = v.dinv32; s.omega = (float)c.omega;
-    ops.push_back(s);
-  };
-  for (int s = 1; s < c.nsmooth; ++s) {
-    sweep(bufs[cur], bufs[1 - cur], AM_JACOBI);
-    cur = 1 - cur;
-  }
-  sweep(bufs[cur], v.r32, AM_RES);
-  Level& w = *c.lv[l + 1];
-  const bool fuse = l + 1 < c.L - 1;
-  op = CyOp{};
-  op.type = CY_RESTRICT; op.gf = v.g; op.gc = w.g; op.fix = w.fix; op.in = v.r32; op.out = w.b32;
-  op.dinv = fuse ? w.dinv32.p : nullptr; op.x2 = fuse ? w.t32.p : nullptr; op.omega = (float)c.omega;
-  ops.push_back(op);
-  record_cycle(c, l + 1, w.b32, w.x32, fuse, ops);
-  op = CyOp{};
-  op.type = CY_PROLONG; op.gf = v.g; op.gc = w.g; op.fix = v.fix; op.in = w.x32; op.out = bufs[cur];
-  ops.push_back(op);
-  for (int s = 0; s < c.nsmooth; ++s) {
-    sweep(bufs[cur], bufs[1 - cur], AM_JACOBI);
-    cur = 1 - cur;
-  }
-  TG_REQUIRE(bufs[cur] == x, "coarse cycle program: the sweeps must end in x");
-}
-
-// The program run from level le (the last level with the large stencil or
-// matrix-free kernels): restrict le's residual, the cycle of the small levels
-// below, prolong into le's current buffer.  le's current buffer after its
-// pre-smoothing: vcycle starts a level in its scratch buffer and each of the
-// nsmooth - 1 pre-sweeps swaps, so it is x (fine level: the PCG's z) or the
-// scratch buffer.
-void build_coarse_program(Ctx& c) {
-  c.cy_n = 0;
-  if (c.precision != TG_PREC_MIXED || c.precond != TG_PRECOND_GMG || c.L < 2) return;
-  int ls = c.L - 1;
-  for (int l = 1; l < c.L - 1; ++l)
-    if (c.lv[l]->g.ndofs() < 150000) { ls = l; break; }   // stencil_apply's small-level switch
-  const int le = ls - 1;
-  Level& v = *c.lv[le];
-  Level& w = *c.lv[ls];
-  float* xle = le == 0 ? c.z32.p : v.x32.p;
-  float* bufs[2] = {xle, v.t32};
-  const int cur = ((c.nsmooth - 1) % 2 == 0) ? 1 : 0;
-  std::vector<CyOp> ops;
-  const bool fuse = ls < c.L - 1;
-  CyOp op{};
-  op.type = CY_RESTRICT; op.gf = v.g; op.gc = w.g; op.fix = w.fix; op.in = v.r32; op.out = w.b32;
-  op.dinv = fuse ? w.dinv32.p : nullptr; op.x2 = fuse ? w.t32.p : nullptr; op.omega = (float)c.omega;
-  ops.push_back(op);
-  record_cycle(c, ls, w.b32, w.x32, fuse, ops);
-  op = CyOp{};
-  op.type = CY_PROLONG; op.gf = v.g; op.gc = w.g; op.fix = v.fix; op.in = w.x32; op.out = bufs[cur];
-  ops.push_back(op);
-  int64_t units = 1;
-  for (const CyOp& o : ops) units = std::max(units, coarse_op_blocks(o, c.nc));
-  c.cy_grid = coarse_cycle_grid(c.g.ndim, c.g.ndof, units);
-  if (c.cy_grid < 1) return;
-  c.cy_ops.alloc((int64_t)ops.size());
-  TG_CUDA(cudaMemcpy(c.cy_ops.p, ops.data(), sizeof(CyOp) * ops.size(), cudaMemcpyHostToDevice));
-  c.cy_n = (int)ops.size();
-  c.cy_level = le;
-  c.cy_r = v.r32;
-  c.cy_x = bufs[cur];
-}
-
 template <typename T> void vcycle(Ctx& c, int l, const T* b, T* x, bool prescaled, int dot_op) {
   Level& v = *c.lv[l];
   const int64_t n = v.g.ndofs();
@@ -588,13 +504,6 @@ template <typename T> void vcycle(Ctx& c, int l, const T* b, T* x, bool prescale
   level_apply<T>(c, l, bufs[cur], r, b, AM_RES);
   Level& w = *c.lv[l + 1];
   const bool fuse = l + 1 < c.L - 1;       // the coarsest level has no smoother
-  if (std::is_same<T, float>::value && c.cy_n > 0 && l == c.cy_level &&
-      (const void*)r == (const void*)c.cy_r && (void*)bufs[cur] == (void*)c.cy_x) {
-    // restrict, the cycle of the small levels and prolong: one launch
-    ProfScope ps(PK_STENCIL_F32, c.st);
-    coarse_cycle(c.g.ndim, c.g.ndof, c.cy_ops, c.cy_n, c.Dc, c.nc, c.ldc, c.gjwork, &c.pcg.p->bar,
-                 c.cy_grid, c.st);
-  } else {
   {
     ProfScope ps(PK_TRANSFER, c.st);
     if (fuse)
@@ -607,7 +516,6 @@ template <typename T> void vcycle(Ctx& c, int l, const T* b, T* x, bool prescale
   {
     ProfScope ps(PK_TRANSFER, c.st);
     prolong_add<T>(v.g, w.g, v.fix, LvBufs<T>::x(w), bufs[cur], c.st);
-  }
   }
   // the fine level's last sweep of the FP32 cycle also forms the PCG dot b . x
   const bool fused_dot = dot_op >= 0 && l == 0 && std::is_same<T, float>::value;
@@ -901,8 +809,6 @@ void solve(Ctx& c, const double* b, double* u) {
       // FP64 residual by the next pass
       const int cap = c.precond == TG_PRECOND_GMG ? 200 : c.maxiter;
       total += pcg32(c, inner, std::min(c.maxiter - total, cap));
-      if (c.h_pcg->bar.err)
-        throw Error{ETIMEOUT, "coarse multigrid cycle: a grid barrier wait timed out"};
       ProfScope ps(PK_VECTOR, c.st);
       add_scaled_f32(n, c.d32, c.pcg_out, u, c.st);
       c.last_refine = k + 1;

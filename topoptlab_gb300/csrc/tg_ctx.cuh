@@ -115,13 +115,6 @@ struct Ctx {
   // its stream after this context's and back
   Ctx* hf = nullptr;
   cudaEvent_t hev0 = nullptr, hev1 = nullptr;
-  // coarse part of the FP32 V-cycle as one cooperative launch (mixed
-  // precision with multigrid): recorded once; replaces restrict / cycle /
-  // prolong below level cy_level when that level's pointers match
-  DevBuf<CyOp> cy_ops;
-  int cy_n = 0, cy_level = -1, cy_grid = 0;
-  const float* cy_r = nullptr;  // residual buffer of cy_level the program restricts
-  float* cy_x = nullptr;        // buffer of cy_level the program prolongs into
   int64_t filter_iters = 0;      // PCG iterations of all filter solves so far
   // statistics of the last solve
   int last_iters = 0, last_vcycles = 0, last_refine = 0, last_converged = 0;
@@ -133,7 +126,6 @@ struct Ctx {
 void ctx_init(Ctx& c, const ::tg_problem& p);
 void ctx_step(Ctx& c, ::tg_iter_out& out);
 void build_hierarchy(Ctx& c);     // uses c.s64 / c.s32 / c.s16 of the current xPhys
-void build_coarse_program(Ctx& c);  // records the one-launch coarse cycle (end of ctx_init)
 void set_density(Ctx& c, const double* xPhys_dev);   // scale factors for xPhys
 // solve K u = b (b, u device FP64, u holds the warm start)
 void solve(Ctx& c, const double* b, double* u);

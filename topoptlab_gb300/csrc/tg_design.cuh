@@ -30,7 +30,6 @@ struct PCGState {
   unsigned int ticket;
   double tol;        // device-side PCG loop: continue while sqrt(rr) >= tol
   int maxit;         //   and iter < maxit (and rr finite)
-  GridBar bar;       // barrier of the one-launch coarse cycle (bar.err: a wait timed out)
 };
 
 // PCG scalars from a finished dot product (the last block of a reduction)

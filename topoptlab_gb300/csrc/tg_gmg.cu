@@ -938,98 +938,4 @@ void dense_apply(const double* Dinv, int64_t n, int64_t ld, const T* b, T* x, do
 template void dense_apply<double>(const double*, int64_t, int64_t, const double*, double*, double*, cudaStream_t);
 template void dense_apply<float>(const double*, int64_t, int64_t, const float*, float*, double*, cudaStream_t);
 
-// ---------------------------------------------------------------------------
-// coarse part of the FP32 V-cycle in one cooperative launch
-// ---------------------------------------------------------------------------
-// Each op is spread over the whole grid (stencil: a block per SMALL_PAIRS
-// pairs, transfers and the dense sum: a thread per node or row, the dense
-// partials: a warp per (row, chunk)) with exactly the arithmetic of the
-// standalone kernels, so results are bit-identical to launching them one by
-// one; a grid barrier separates consecutive ops.  On a timed-out barrier
-// wait the blocks leave (bar->err set).
-template <int NDIM, int NDOF>
-__global__ void __launch_bounds__(CY_THREADS, 2) k_coarse_cycle(const CyOp* __restrict__ ops, int nops,
-                                                            const double* __restrict__ Dinv,
-                                                            int64_t n, int64_t ld, double* work,
-                                                            GridBar* bar) {
-  __shared__ float part[3][SMALL_PAIRS];
-  const int64_t gtid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int64_t gstride = (int64_t)gridDim.x * blockDim.x;
-  for (int o = 0; o < nops; ++o) {
-    const CyOp& op = ops[o];
-    const int type = op.type;
-    if (type == CY_STENCIL) {
-      const int64_t nvb = cdiv(op.gf.nnodes() * NDOF, SMALL_PAIRS);
-      for (int64_t vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
-        if (op.mode == AM_RES)
-          stencil_small_vb<NDIM, NDOF, float, AM_RES>(op.gf, op.A, op.in, op.out, op.b, op.dinv,
-                                                      op.omega, vb, part);
-        else
-          stencil_small_vb<NDIM, NDOF, float, AM_JACOBI>(op.gf, op.A, op.in, op.out, op.b,
-                                                         op.dinv, op.omega, vb, part);
-      }
-    } else if (type == CY_RESTRICT) {
-      const int64_t nt = op.gc.nnodes() * NDOF;
-      for (int64_t t = gtid; t < nt; t += gstride)
-        restrict_one<NDIM, NDOF, float>(op.gf, op.gc, op.fix, op.in, op.out, op.dinv, op.x2,
-                                        op.omega, t);
-    } else if (type == CY_PROLONG) {
-      const int64_t nt = op.gf.nnodes();
-      for (int64_t i = gtid; i < nt; i += gstride)
-        prolong_one<NDIM, NDOF, float>(op.gf, op.gc, op.fix, op.in, op.out, i);
-    } else if (type == CY_DENSE_PARTIAL) {
-      const int64_t nw = n * DA_CHUNKS;
-      for (int64_t w = gtid >> 5; w < nw; w += gstride >> 5)
-        dense_partial_one<float>(Dinv, n, ld, op.in, work, w % n, (int)(w / n), threadIdx.x & 31);
-    } else if (type == CY_DENSE_SUM) {
-      for (int64_t row = gtid; row < n; row += gstride) dense_sum_one<float>(work, n, op.out, row);
-    }
-    if (o + 1 < nops && !grid_sync(bar)) return;
-  }
-}
-
-template <int NDIM, int NDOF> static const void* cy_kernel() {
-  return (const void*)k_coarse_cycle<NDIM, NDOF>;
-}
-static const void* cy_kernel_for(int ndim, int ndof) {
-  switch (ndim * 10 + ndof) {
-    case 33: return cy_kernel<3, 3>();
-    case 31: return cy_kernel<3, 1>();
-    case 22: return cy_kernel<2, 2>();
-    case 21: return cy_kernel<2, 1>();
-    default: throw Error{EINVAL_, "unsupported (ndim, nnode_dof)"};
-  }
-}
-
-int64_t coarse_op_blocks(const CyOp& op, int64_t ndense) {
-  switch (op.type) {
-    case CY_STENCIL: return cdiv(op.gf.nnodes() * op.gf.ndof, SMALL_PAIRS);
-    case CY_RESTRICT: return cdiv(op.gc.nnodes() * op.gc.ndof, CY_THREADS);
-    case CY_PROLONG: return cdiv(op.gf.nnodes(), CY_THREADS);
-    case CY_DENSE_PARTIAL: return cdiv(ndense * DA_CHUNKS, CY_THREADS / 32);
-    default: return cdiv(ndense, CY_THREADS);
-  }
-}
-
-// at most two blocks per SM (a barrier over fewer blocks is cheaper; the
-// largest small level needs a few hundred blocks) and what is co-resident
-int coarse_cycle_grid(int ndim, int ndof, int64_t units) {
-  int dev = 0, nsm = 0, per_sm = 0;
-  TG_CUDA(cudaGetDevice(&dev));
-  TG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  TG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cy_kernel_for(ndim, ndof),
-                                                        CY_THREADS, 0));
-  const int64_t cap = (int64_t)nsm * std::min(std::max(per_sm, 0), 2);
-  return (int)std::max<int64_t>(0, std::min<int64_t>(units, cap));
-}
-
-void coarse_cycle(int ndim, int ndof, const CyOp* ops, int nops, const double* Dinv, int64_t n,
-                  int64_t ld, double* work, GridBar* bar, int grid, cudaStream_t st) {
-  void* args[] = {(void*)&ops, (void*)&nops, (void*)&Dinv, (void*)&n, (void*)&ld, (void*)&work,
-                  (void*)&bar};
-  TG_CUDA(cudaLaunchCooperativeKernel(cy_kernel_for(ndim, ndof), dim3((unsigned)grid),
-                                      dim3(CY_THREADS), args, 0, st));
-  count_launches(1);
-}
-
 }  // namespace tg

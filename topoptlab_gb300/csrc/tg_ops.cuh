@@ -105,30 +105,6 @@ void stencil_to_dense(const Grid& g, const uint8_t* fix, const T* A, double* D, 
                       int64_t ld, cudaStream_t st);
 // work: 32 * 32 + 2 * 32 * ld doubles (enough for pivot blocks up to 32)
 void gj_inverse(double* D, int64_t n, int64_t ld, double* work, cudaStream_t st);
-// The coarse part of the FP32 V-cycle as one cooperative launch: the ops
-// below run in order, separated by grid barriers (bar: bounded waits).
-enum CyType : int { CY_STENCIL = 0, CY_RESTRICT = 1, CY_PROLONG = 2, CY_DENSE_PARTIAL = 3,
-                    CY_DENSE_SUM = 4 };
-struct CyOp {
-  int type, mode;        // mode: AM_RES / AM_JACOBI for CY_STENCIL
-  Grid gf, gc;           // stencil: gf; transfers: fine and coarse grid
-  const float* A;        // stencil coefficients
-  const float* in;       // stencil u / restrict r_f / prolong x_c / dense b
-  float* out;            // stencil y / restrict b_c / prolong x_f (added to) / dense x
-  const float* b;        // stencil right-hand side
-  const float* dinv;     // stencil D^-1 / restrict: coarse D^-1 of the fused sweep
-  float* x2;             // restrict: fused omega D^-1 b_c (null: none)
-  const uint8_t* fix;    // restrict: coarse / prolong: fine fixed bits
-  float omega;
-};
-struct GridBar;
-constexpr int CY_THREADS = 384;
-// co-resident grid for a program whose largest op needs `units` blocks
-int coarse_cycle_grid(int ndim, int ndof, int64_t units);
-int64_t coarse_op_blocks(const CyOp& op, int64_t ndense);
-void coarse_cycle(int ndim, int ndof, const CyOp* ops, int nops, const double* Dinv, int64_t n,
-                  int64_t ld, double* work, GridBar* bar, int grid, cudaStream_t st);
-
 template <typename T>
 void dense_apply(const double* Dinv, int64_t n, int64_t ld, const T* b, T* x,
                  double* work /* >= 8*n */, cudaStream_t st);
