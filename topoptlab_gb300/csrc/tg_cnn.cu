@@ -91,10 +91,144 @@ __global__ void __launch_bounds__(128) k_conv3(NG g, const float* __restrict__ i
   }
 }
 
+// The same convolution on the tensor cores (input channel counts that are
+// multiples of 8): an implicit GEMM out[n][co] = sum_{k, ci} in[nbr(n, k)][ci]
+// W[k][ci][co] with warp-level mma.sync m16n8k8 TF32 and FP32 accumulation.
+// Each FP32 operand is split as hi = tf32(v), lo = tf32(v - hi) and the
+// product taken as hi*hi + hi*lo + lo*hi (three MMAs), which keeps FP32-level
+// accuracy (the network is trained and checked in FP32).  A CTA of 4 warps
+// computes 128 consecutive nodes (a warp: two 16-row tiles) times 8*NT output
+// channels (blockIdx.y selects the chunk); A fragments are gathered from the
+// channels-last input (zero outside the grid), B fragments read through the
+// read-only cache.  Fragment layouts of m16n8k8 (PTX ISA): with g = lane / 4,
+// t = lane % 4, A holds (g, t), (g + 8, t), (g, t + 4), (g + 8, t + 4); B
+// holds (t, g), (t + 4, g); C holds (g, 2t), (g, 2t + 1), (g + 8, 2t),
+// (g + 8, 2t + 1).
+__device__ __forceinline__ uint32_t f2tf32(float v) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(v));
+  return r;
+}
+__device__ __forceinline__ void mma_tf32(float (&d)[4], const uint32_t (&a)[4],
+                                         const uint32_t (&b)[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+      "{%8,%9}, {%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+template <int CIN, int NT>
+__global__ void __launch_bounds__(128) k_conv3_mma(NG g, const float* __restrict__ in,
+                                                   const float* __restrict__ W, int cout,
+                                                   const float* __restrict__ bias,
+                                                   const float* __restrict__ skip, int relu,
+                                                   const float* __restrict__ mask,
+                                                   float* __restrict__ out) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int gq = lane >> 2, tq = lane & 3;
+  const int co0 = blockIdx.y * 8 * NT;
+  const int64_t nbase = blockIdx.x * (int64_t)128 + warp * 32;
+  const int64_t nn = g.n();
+  // the four A rows this thread gathers: tile m (0, 1), row gq or gq + 8
+  int rx[4], ry[4], rz[4];
+  bool rv[4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int64_t node = nbase + (r >> 1) * 16 + (r & 1) * 8 + gq;
+    rv[r] = node < nn;
+    int x = 0, y = 0, z = 0;
+    if (rv[r]) ng_xyz(g, node, x, y, z);
+    rx[r] = x; ry[r] = y; rz[r] = z;
+  }
+  float acc[2][NT][4];
+#pragma unroll
+  for (int m = 0; m < 2; ++m)
+#pragma unroll
+    for (int j = 0; j < NT; ++j)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc[m][j][q] = 0.f;
+#pragma unroll 1
+  for (int k = 0; k < 27; ++k) {
+    const int dy = k % 3 - 1, dx = (k / 3) % 3 - 1, dz = k / 9 - 1;
+    const float* src[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int X = rx[r] + dx, Y = ry[r] + dy, Z = rz[r] + dz;
+      const bool ok = rv[r] && X >= 0 && X < g.nx && Y >= 0 && Y < g.ny && Z >= 0 && Z < g.nz;
+      src[r] = ok ? in + ng_idx(g, X, Y, Z) * CIN : nullptr;
+    }
+    const float* wk = W + (int64_t)k * CIN * cout;
+#pragma unroll 2
+    for (int c0 = 0; c0 < CIN; c0 += 8) {
+      uint32_t ahi[2][4], alo[2][4];
+#pragma unroll
+      for (int m = 0; m < 2; ++m) {
+        // a0 (g, t), a1 (g + 8, t), a2 (g, t + 4), a3 (g + 8, t + 4)
+        const float* s0 = src[2 * m];
+        const float* s1 = src[2 * m + 1];
+        const float v[4] = {s0 ? __ldg(s0 + c0 + tq) : 0.f, s1 ? __ldg(s1 + c0 + tq) : 0.f,
+                            s0 ? __ldg(s0 + c0 + tq + 4) : 0.f,
+                            s1 ? __ldg(s1 + c0 + tq + 4) : 0.f};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          ahi[m][q] = f2tf32(v[q]);
+          alo[m][q] = f2tf32(v[q] - __uint_as_float(ahi[m][q]));
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < NT; ++j) {
+        const int co = co0 + j * 8 + gq;
+        const float w0 = co < cout ? __ldg(wk + (int64_t)(c0 + tq) * cout + co) : 0.f;
+        const float w1 = co < cout ? __ldg(wk + (int64_t)(c0 + tq + 4) * cout + co) : 0.f;
+        uint32_t bhi[2], blo[2];
+        bhi[0] = f2tf32(w0);
+        bhi[1] = f2tf32(w1);
+        blo[0] = f2tf32(w0 - __uint_as_float(bhi[0]));
+        blo[1] = f2tf32(w1 - __uint_as_float(bhi[1]));
+#pragma unroll
+        for (int m = 0; m < 2; ++m) {
+          mma_tf32(acc[m][j], alo[m], bhi);
+          mma_tf32(acc[m][j], ahi[m], blo);
+          mma_tf32(acc[m][j], ahi[m], bhi);
+        }
+      }
+    }
+  }
+  // epilogue: c0 (g, 2t), c1 (g, 2t + 1), c2 (g + 8, 2t), c3 (g + 8, 2t + 1)
+#pragma unroll
+  for (int m = 0; m < 2; ++m)
+#pragma unroll
+    for (int j = 0; j < NT; ++j)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int64_t node = nbase + m * 16 + (q >> 1) * 8 + gq;
+        const int co = co0 + j * 8 + 2 * tq + (q & 1);
+        if (node >= nn || co >= cout) continue;
+        float v = acc[m][j][q] + (bias ? bias[co] : 0.f);
+        if (skip) v += skip[node * cout + co];
+        if (relu) v = fmaxf(v, 0.f);
+        if (mask && !(mask[node * cout + co] > 0.f)) v = 0.f;
+        out[node * cout + co] = v;
+      }
+}
+
 template <int CIN>
 static void conv3_launch(const NG& g, const float* in, const float* W, int cout, const float* bias,
                          const float* skip, int relu, const float* mask, float* out,
                          cudaStream_t st) {
+  if constexpr (CIN % 8 == 0) {
+    const unsigned gx = (unsigned)cdiv(g.n(), 128);
+    if (cout <= 8)
+      k_conv3_mma<CIN, 1><<<dim3(gx, 1), 128, 0, st>>>(g, in, W, cout, bias, skip, relu, mask, out);
+    else if (cout <= 16)
+      k_conv3_mma<CIN, 2><<<dim3(gx, 1), 128, 0, st>>>(g, in, W, cout, bias, skip, relu, mask, out);
+    else
+      k_conv3_mma<CIN, 4><<<dim3(gx, (unsigned)cdiv(cout, 32)), 128, 0, st>>>(
+          g, in, W, cout, bias, skip, relu, mask, out);
+    TG_CHECK_LAUNCH();
+    return;
+  }
   const int cc = cout >= 16 ? 16 : 4;
   const unsigned gx = (unsigned)cdiv(g.n(), 128);
   if (cc == 16) {
