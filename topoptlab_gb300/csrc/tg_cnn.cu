@@ -40,67 +40,20 @@ __device__ __forceinline__ int64_t ng_idx(const NG& g, int x, int y, int z) {
 
 // ---------------------------------------------------------------------------
 // 3x3x3 convolution, stride 1, zero padding (forward; also the input gradient
-// with flipped / transposed weights).  One thread per output node, CC output
-// channels per CTA; weights of the chunk staged in shared memory and read as
-// broadcasts.  Epilogue: + bias, + skip, relu, * (mask > 0).
+// with flipped / transposed weights).  Epilogue: + bias, + skip, relu,
+// * (mask > 0).
 // ---------------------------------------------------------------------------
-template <int CIN, int CC>
-__global__ void __launch_bounds__(128) k_conv3(NG g, const float* __restrict__ in,
-                                               const float* __restrict__ W, int cout,
-                                               const float* __restrict__ bias,
-                                               const float* __restrict__ skip, int relu,
-                                               const float* __restrict__ mask,
-                                               float* __restrict__ out) {
-  extern __shared__ __align__(16) float ws[];      // [27][CIN][CC]
-  const int co0 = blockIdx.y * CC;
-  for (int i = threadIdx.x; i < 27 * CIN * CC; i += blockDim.x) {
-    const int j = i % CC, ci = (i / CC) % CIN, k = i / (CC * CIN);
-    ws[i] = (co0 + j < cout) ? W[((int64_t)k * CIN + ci) * cout + co0 + j] : 0.f;
-  }
-  __syncthreads();
-  const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (n >= g.n()) return;
-  int x, y, z;
-  ng_xyz(g, n, x, y, z);
-  float acc[CC];
-#pragma unroll
-  for (int j = 0; j < CC; ++j) acc[j] = (bias && co0 + j < cout) ? bias[co0 + j] : 0.f;
-#pragma unroll 1
-  for (int k = 0; k < 27; ++k) {
-    const int dy = k % 3 - 1, dx = (k / 3) % 3 - 1, dz = k / 9 - 1;
-    const int X = x + dx, Y = y + dy, Z = z + dz;
-    if (X < 0 || X >= g.nx || Y < 0 || Y >= g.ny || Z < 0 || Z >= g.nz) continue;
-    const float* src = in + ng_idx(g, X, Y, Z) * CIN;
-    const float* wk = ws + k * CIN * CC;
-#pragma unroll 4
-    for (int ci = 0; ci < CIN; ++ci) {
-      const float v = __ldg(src + ci);
-#pragma unroll
-      for (int j = 0; j < CC; ++j) acc[j] = fmaf(v, wk[ci * CC + j], acc[j]);
-    }
-  }
-#pragma unroll
-  for (int j = 0; j < CC; ++j) {
-    const int co = co0 + j;
-    if (co >= cout) break;
-    float v = acc[j];
-    if (skip) v += skip[n * cout + co];
-    if (relu) v = fmaxf(v, 0.f);
-    if (mask && !(mask[n * cout + co] > 0.f)) v = 0.f;
-    out[n * cout + co] = v;
-  }
-}
-
-// The same convolution on the tensor cores (input channel counts that are
-// multiples of 8): an implicit GEMM out[n][co] = sum_{k, ci} in[nbr(n, k)][ci]
-// W[k][ci][co] with warp-level mma.sync m16n8k8 TF32 and FP32 accumulation.
+// The convolution runs on the tensor cores as an implicit GEMM
+// out[n][co] = sum_{k, ci} in[nbr(n, k)][ci] W[k][ci][co] with warp-level
+// mma.sync m16n8k8 TF32 and FP32 accumulation.
 // Each FP32 operand is split as hi = tf32(v), lo = tf32(v - hi) and the
 // product taken as hi*hi + hi*lo + lo*hi (three MMAs), which keeps FP32-level
 // accuracy (the network is trained and checked in FP32).  A CTA of 4 warps
 // computes 128 consecutive nodes (a warp: two 16-row tiles) times 8*NT output
 // channels (blockIdx.y selects the chunk); A fragments are gathered from the
 // channels-last input (zero outside the grid), B fragments read through the
-// read-only cache.  Fragment layouts of m16n8k8 (PTX ISA): with g = lane / 4,
+// read-only cache; input channels past CIN (CIN not a multiple of 8) read as
+// zero.  Fragment layouts of m16n8k8 (PTX ISA): with g = lane / 4,
 // t = lane % 4, A holds (g, t), (g + 8, t), (g, t + 4), (g + 8, t + 4); B
 // holds (t, g), (t + 4, g); C holds (g, 2t), (g, 2t + 1), (g + 8, 2t),
 // (g + 8, 2t + 1).
@@ -167,9 +120,10 @@ __global__ void __launch_bounds__(128) k_conv3_mma(NG g, const float* __restrict
         // a0 (g, t), a1 (g + 8, t), a2 (g, t + 4), a3 (g + 8, t + 4)
         const float* s0 = src[2 * m];
         const float* s1 = src[2 * m + 1];
-        const float v[4] = {s0 ? __ldg(s0 + c0 + tq) : 0.f, s1 ? __ldg(s1 + c0 + tq) : 0.f,
-                            s0 ? __ldg(s0 + c0 + tq + 4) : 0.f,
-                            s1 ? __ldg(s1 + c0 + tq + 4) : 0.f};
+        const bool k0 = c0 + tq < CIN, k1 = c0 + tq + 4 < CIN;   // compile-time true for CIN % 8 == 0
+        const float v[4] = {s0 && k0 ? __ldg(s0 + c0 + tq) : 0.f, s1 && k0 ? __ldg(s1 + c0 + tq) : 0.f,
+                            s0 && k1 ? __ldg(s0 + c0 + tq + 4) : 0.f,
+                            s1 && k1 ? __ldg(s1 + c0 + tq + 4) : 0.f};
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           ahi[m][q] = f2tf32(v[q]);
@@ -179,8 +133,9 @@ __global__ void __launch_bounds__(128) k_conv3_mma(NG g, const float* __restrict
 #pragma unroll
       for (int j = 0; j < NT; ++j) {
         const int co = co0 + j * 8 + gq;
-        const float w0 = co < cout ? __ldg(wk + (int64_t)(c0 + tq) * cout + co) : 0.f;
-        const float w1 = co < cout ? __ldg(wk + (int64_t)(c0 + tq + 4) * cout + co) : 0.f;
+        const bool k0 = c0 + tq < CIN, k1 = c0 + tq + 4 < CIN;
+        const float w0 = co < cout && k0 ? __ldg(wk + (int64_t)(c0 + tq) * cout + co) : 0.f;
+        const float w1 = co < cout && k1 ? __ldg(wk + (int64_t)(c0 + tq + 4) * cout + co) : 0.f;
         uint32_t bhi[2], blo[2];
         bhi[0] = f2tf32(w0);
         bhi[1] = f2tf32(w1);
@@ -217,35 +172,14 @@ template <int CIN>
 static void conv3_launch(const NG& g, const float* in, const float* W, int cout, const float* bias,
                          const float* skip, int relu, const float* mask, float* out,
                          cudaStream_t st) {
-  if constexpr (CIN % 8 == 0) {
-    const unsigned gx = (unsigned)cdiv(g.n(), 128);
-    if (cout <= 8)
-      k_conv3_mma<CIN, 1><<<dim3(gx, 1), 128, 0, st>>>(g, in, W, cout, bias, skip, relu, mask, out);
-    else if (cout <= 16)
-      k_conv3_mma<CIN, 2><<<dim3(gx, 1), 128, 0, st>>>(g, in, W, cout, bias, skip, relu, mask, out);
-    else
-      k_conv3_mma<CIN, 4><<<dim3(gx, (unsigned)cdiv(cout, 32)), 128, 0, st>>>(
-          g, in, W, cout, bias, skip, relu, mask, out);
-    TG_CHECK_LAUNCH();
-    return;
-  }
-  const int cc = cout >= 16 ? 16 : 4;
   const unsigned gx = (unsigned)cdiv(g.n(), 128);
-  if (cc == 16) {
-    const size_t smem = sizeof(float) * 27 * CIN * 16;
-    static const bool set = [&] {   // once per instantiation, thread-safe
-      TG_CUDA(cudaFuncSetAttribute(k_conv3<CIN, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)smem));
-      return true;
-    }();
-    (void)set;
-    k_conv3<CIN, 16><<<dim3(gx, (unsigned)cdiv(cout, 16)), 128, smem, st>>>(g, in, W, cout, bias,
-                                                                          skip, relu, mask, out);
-  } else {
-    const size_t smem = sizeof(float) * 27 * CIN * 4;
-    k_conv3<CIN, 4><<<dim3(gx, (unsigned)cdiv(cout, 4)), 128, smem, st>>>(g, in, W, cout, bias,
-                                                                        skip, relu, mask, out);
-  }
+  if (cout <= 8)
+    k_conv3_mma<CIN, 1><<<dim3(gx, 1), 128, 0, st>>>(g, in, W, cout, bias, skip, relu, mask, out);
+  else if (cout <= 16)
+    k_conv3_mma<CIN, 2><<<dim3(gx, 1), 128, 0, st>>>(g, in, W, cout, bias, skip, relu, mask, out);
+  else
+    k_conv3_mma<CIN, 4><<<dim3(gx, (unsigned)cdiv(cout, 32)), 128, 0, st>>>(g, in, W, cout, bias,
+                                                                           skip, relu, mask, out);
   TG_CHECK_LAUNCH();
 }
 
@@ -736,6 +670,67 @@ double Cnn::train(int epochs, float lr_, uint64_t seed) {
   return last;
 }
 
+// The five products of the 2x2 Galerkin combination in one pass over the
+// vectors: v1.Kv1, v1.Kv2, v2.Kv2, v1.f, v2.f (FP32 products, each thread's
+// sums widened to FP64 for the block and grid sums, finished in fixed order
+// by the last block into out[k].bb)
+constexpr int DOT5_BLOCKS = RED_BLOCKS / 5;
+__global__ void __launch_bounds__(RED_THREADS) k_dot5(int64_t n, const float* __restrict__ v1,
+                                                     const float* __restrict__ v2,
+                                                     const float* __restrict__ k1,
+                                                     const float* __restrict__ k2,
+                                                     const float* __restrict__ f, double* part,
+                                                     PCGState* out) {
+  __shared__ double sh[32];
+  __shared__ int last;
+  float a[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  const int64_t t0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t ts = (int64_t)gridDim.x * blockDim.x;
+  const int64_t n4 = n / 4;
+  for (int64_t i = t0; i < n4; i += ts) {
+    const float4 x1 = reinterpret_cast<const float4*>(v1)[i];
+    const float4 x2 = reinterpret_cast<const float4*>(v2)[i];
+    const float4 y1 = reinterpret_cast<const float4*>(k1)[i];
+    const float4 y2 = reinterpret_cast<const float4*>(k2)[i];
+    const float4 ff = reinterpret_cast<const float4*>(f)[i];
+    const float xs1[4] = {x1.x, x1.y, x1.z, x1.w}, xs2[4] = {x2.x, x2.y, x2.z, x2.w};
+    const float ys1[4] = {y1.x, y1.y, y1.z, y1.w}, ys2[4] = {y2.x, y2.y, y2.z, y2.w};
+    const float fs[4] = {ff.x, ff.y, ff.z, ff.w};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      a[0] = fmaf(xs1[q], ys1[q], a[0]);
+      a[1] = fmaf(xs1[q], ys2[q], a[1]);
+      a[2] = fmaf(xs2[q], ys2[q], a[2]);
+      a[3] = fmaf(xs1[q], fs[q], a[3]);
+      a[4] = fmaf(xs2[q], fs[q], a[4]);
+    }
+  }
+  for (int64_t i = 4 * n4 + t0; i < n; i += ts) {
+    a[0] = fmaf(v1[i], k1[i], a[0]);
+    a[1] = fmaf(v1[i], k2[i], a[1]);
+    a[2] = fmaf(v2[i], k2[i], a[2]);
+    a[3] = fmaf(v1[i], f[i], a[3]);
+    a[4] = fmaf(v2[i], f[i], a[4]);
+  }
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    const double bs = block_sum((double)a[k], sh);
+    if (threadIdx.x == 0) part[k * gridDim.x + blockIdx.x] = bs;
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = (atomicAdd(&out[0].ticket, 1u) == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  for (int k = 0; k < 5; ++k) {
+    const double tot = sum_partials(part + k * gridDim.x, (int)gridDim.x, sh);
+    if (threadIdx.x == 0) out[k].bb = tot;
+  }
+  if (threadIdx.x == 0) out[0].ticket = 0;
+}
+
 __global__ void k_combine(int64_t n, double c1, const double* v1, double c2, const double* v2,
                           double* out) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -763,12 +758,9 @@ int Cnn::warm_start(Ctx& c) {
   d2f(n, c.f, c.z32, c.st);
   fine_apply<float, float>(c.op, c.s32, c.p32, c.q32, nullptr, nullptr, 0.0, AM_Y, c.st);
   fine_apply<float, float>(c.op, c.s32, c.d32, c.r32, nullptr, nullptr, 0.0, AM_Y, c.st);
-  const float* a[5] = {c.p32, c.p32, c.d32, c.p32, c.d32};
-  const float* b[5] = {c.q32, c.r32, c.r32, c.z32, c.z32};
-  for (int k = 0; k < 5; ++k) {
-    pcg_reset(gal.p + k, c.st);
-    dot<float, float>(n, a[k], b[k], c.part, gal.p + k, DOT_BB, c.st);
-  }
+  const unsigned b5 = std::min<unsigned>(red_blocks(n), (unsigned)DOT5_BLOCKS);
+  k_dot5<<<b5, RED_THREADS, 0, c.st>>>(n, c.p32, c.d32, c.q32, c.r32, c.z32, c.part, gal.p);
+  TG_CHECK_LAUNCH();
   PCGState hg[5], hp{};
   TG_CUDA(cudaMemcpyAsync(hg, gal.p, sizeof(PCGState) * 5, cudaMemcpyDeviceToHost, c.st));
   TG_CUDA(cudaMemcpyAsync(&hp, sr.p, sizeof(PCGState), cudaMemcpyDeviceToHost, c.st));
