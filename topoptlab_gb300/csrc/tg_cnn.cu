@@ -16,6 +16,7 @@
 // y * s_u is a level-1 displacement correction; the warm start is
 // u_prev + P (y * s_u) with the multigrid prolongation P.
 #include <algorithm>
+#include <type_traits>
 #include <cmath>
 #include <random>
 #include <vector>
@@ -72,27 +73,41 @@ __device__ __forceinline__ void mma_tf32(float (&d)[4], const uint32_t (&a)[4],
 }
 
 template <int CIN, int NT>
+struct ConvTile {
+  static constexpr int CP = (CIN + 7) / 8 * 8;   // input channels padded to the MMA k
+  static constexpr int AS = CP + 4;              // A row stride (words): conflict-free fragments
+  static constexpr int NC = 8 * NT;              // output channels of a CTA
+  static constexpr int BS = NC + 8;              // B row stride (words): conflict-free fragments
+  static constexpr size_t smem() {
+    return sizeof(float) * 128 * AS + 2 * sizeof(uint32_t) * CP * BS + 4 * sizeof(int) * 128;
+  }
+};
+
+template <int CIN, int NT>
 __global__ void __launch_bounds__(128) k_conv3_mma(NG g, const float* __restrict__ in,
                                                    const float* __restrict__ W, int cout,
                                                    const float* __restrict__ bias,
                                                    const float* __restrict__ skip, int relu,
                                                    const float* __restrict__ mask,
                                                    float* __restrict__ out) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  using TT = ConvTile<CIN, NT>;
+  constexpr int CP = TT::CP, AS = TT::AS, NC = TT::NC, BS = TT::BS;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float* As = reinterpret_cast<float*>(smem_raw);                      // [128][AS]
+  uint32_t* Bh = reinterpret_cast<uint32_t*>(As + 128 * AS);          // [CP][BS] tf32 hi
+  uint32_t* Bl = Bh + CP * BS;                                         // [CP][BS] tf32 lo
+  int* rxyz = reinterpret_cast<int*>(Bl + CP * BS);                    // [128][4]: x, y, z, valid
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int gq = lane >> 2, tq = lane & 3;
-  const int co0 = blockIdx.y * 8 * NT;
-  const int64_t nbase = blockIdx.x * (int64_t)128 + warp * 32;
+  const int co0 = blockIdx.y * NC;
+  const int64_t n0 = blockIdx.x * (int64_t)128;
   const int64_t nn = g.n();
-  // the four A rows this thread gathers: tile m (0, 1), row gq or gq + 8
-  int rx[4], ry[4], rz[4];
-  bool rv[4];
-#pragma unroll
-  for (int r = 0; r < 4; ++r) {
-    const int64_t node = nbase + (r >> 1) * 16 + (r & 1) * 8 + gq;
-    rv[r] = node < nn;
+  {
+    const int64_t node = n0 + tid;
     int x = 0, y = 0, z = 0;
-    if (rv[r]) ng_xyz(g, node, x, y, z);
-    rx[r] = x; ry[r] = y; rz[r] = z;
+    if (node < nn) ng_xyz(g, node, x, y, z);
+    rxyz[4 * tid] = x; rxyz[4 * tid + 1] = y; rxyz[4 * tid + 2] = z;
+    rxyz[4 * tid + 3] = node < nn;
   }
   float acc[2][NT][4];
 #pragma unroll
@@ -104,26 +119,46 @@ __global__ void __launch_bounds__(128) k_conv3_mma(NG g, const float* __restrict
 #pragma unroll 1
   for (int k = 0; k < 27; ++k) {
     const int dy = k % 3 - 1, dx = (k / 3) % 3 - 1, dz = k / 9 - 1;
-    const float* src[4];
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      const int X = rx[r] + dx, Y = ry[r] + dy, Z = rz[r] + dz;
-      const bool ok = rv[r] && X >= 0 && X < g.nx && Y >= 0 && Y < g.ny && Z >= 0 && Z < g.nz;
-      src[r] = ok ? in + ng_idx(g, X, Y, Z) * CIN : nullptr;
+    const int64_t off = ((int64_t)dz * g.nx + dx) * g.ny + dy;
+    __syncthreads();                 // previous tap's fragments consumed (and rxyz written)
+    // A: rows n0+r+off of the input (contiguous), zero where the neighbour is outside
+    if constexpr (CIN % 4 == 0) {
+      constexpr int V = CIN / 4;
+      for (int i = tid; i < 128 * V; i += 128) {
+        const int r = i / V, v = i % V;
+        const int X = rxyz[4 * r] + dx, Y = rxyz[4 * r + 1] + dy, Z = rxyz[4 * r + 2] + dz;
+        const bool ok = rxyz[4 * r + 3] && X >= 0 && X < g.nx && Y >= 0 && Y < g.ny && Z >= 0 &&
+                        Z < g.nz;
+        float4 val = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (ok) val = __ldg(reinterpret_cast<const float4*>(in + (n0 + r + off) * CIN) + v);
+        *reinterpret_cast<float4*>(As + r * AS + 4 * v) = val;
+      }
+    } else {
+      for (int i = tid; i < 128 * CP; i += 128) {
+        const int r = i / CP, c = i % CP;
+        const int X = rxyz[4 * r] + dx, Y = rxyz[4 * r + 1] + dy, Z = rxyz[4 * r + 2] + dz;
+        const bool ok = c < CIN && rxyz[4 * r + 3] && X >= 0 && X < g.nx && Y >= 0 &&
+                        Y < g.ny && Z >= 0 && Z < g.nz;
+        As[r * AS + c] = ok ? __ldg(in + (n0 + r + off) * CIN + c) : 0.f;
+      }
     }
+    // B: this tap's weights of the CTA's output channels, split into tf32 hi / lo
     const float* wk = W + (int64_t)k * CIN * cout;
-#pragma unroll 2
-    for (int c0 = 0; c0 < CIN; c0 += 8) {
+    for (int i = tid; i < CP * NC; i += 128) {
+      const int c = i / NC, j = i % NC;
+      const float w = (c < CIN && co0 + j < cout) ? __ldg(wk + (int64_t)c * cout + co0 + j) : 0.f;
+      const uint32_t h = f2tf32(w);
+      Bh[c * BS + j] = h;
+      Bl[c * BS + j] = f2tf32(w - __uint_as_float(h));
+    }
+    __syncthreads();
+#pragma unroll
+    for (int c0 = 0; c0 < CP; c0 += 8) {
       uint32_t ahi[2][4], alo[2][4];
 #pragma unroll
       for (int m = 0; m < 2; ++m) {
-        // a0 (g, t), a1 (g + 8, t), a2 (g, t + 4), a3 (g + 8, t + 4)
-        const float* s0 = src[2 * m];
-        const float* s1 = src[2 * m + 1];
-        const bool k0 = c0 + tq < CIN, k1 = c0 + tq + 4 < CIN;   // compile-time true for CIN % 8 == 0
-        const float v[4] = {s0 && k0 ? __ldg(s0 + c0 + tq) : 0.f, s1 && k0 ? __ldg(s1 + c0 + tq) : 0.f,
-                            s0 && k1 ? __ldg(s0 + c0 + tq + 4) : 0.f,
-                            s1 && k1 ? __ldg(s1 + c0 + tq + 4) : 0.f};
+        const float* a0 = As + (warp * 32 + m * 16 + gq) * AS + c0 + tq;
+        const float v[4] = {a0[0], a0[8 * AS], a0[4], a0[8 * AS + 4]};
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           ahi[m][q] = f2tf32(v[q]);
@@ -132,15 +167,9 @@ __global__ void __launch_bounds__(128) k_conv3_mma(NG g, const float* __restrict
       }
 #pragma unroll
       for (int j = 0; j < NT; ++j) {
-        const int co = co0 + j * 8 + gq;
-        const bool k0 = c0 + tq < CIN, k1 = c0 + tq + 4 < CIN;
-        const float w0 = co < cout && k0 ? __ldg(wk + (int64_t)(c0 + tq) * cout + co) : 0.f;
-        const float w1 = co < cout && k1 ? __ldg(wk + (int64_t)(c0 + tq + 4) * cout + co) : 0.f;
-        uint32_t bhi[2], blo[2];
-        bhi[0] = f2tf32(w0);
-        bhi[1] = f2tf32(w1);
-        blo[0] = f2tf32(w0 - __uint_as_float(bhi[0]));
-        blo[1] = f2tf32(w1 - __uint_as_float(bhi[1]));
+        const int bi = (c0 + tq) * BS + j * 8 + gq;
+        const uint32_t bhi[2] = {Bh[bi], Bh[bi + 4 * BS]};
+        const uint32_t blo[2] = {Bl[bi], Bl[bi + 4 * BS]};
 #pragma unroll
         for (int m = 0; m < 2; ++m) {
           mma_tf32(acc[m][j], alo[m], bhi);
@@ -157,7 +186,7 @@ __global__ void __launch_bounds__(128) k_conv3_mma(NG g, const float* __restrict
     for (int j = 0; j < NT; ++j)
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
-        const int64_t node = nbase + m * 16 + (q >> 1) * 8 + gq;
+        const int64_t node = n0 + warp * 32 + m * 16 + (q >> 1) * 8 + gq;
         const int co = co0 + j * 8 + 2 * tq + (q & 1);
         if (node >= nn || co >= cout) continue;
         float v = acc[m][j][q] + (bias ? bias[co] : 0.f);
@@ -173,13 +202,21 @@ static void conv3_launch(const NG& g, const float* in, const float* W, int cout,
                          const float* skip, int relu, const float* mask, float* out,
                          cudaStream_t st) {
   const unsigned gx = (unsigned)cdiv(g.n(), 128);
-  if (cout <= 8)
-    k_conv3_mma<CIN, 1><<<dim3(gx, 1), 128, 0, st>>>(g, in, W, cout, bias, skip, relu, mask, out);
-  else if (cout <= 16)
-    k_conv3_mma<CIN, 2><<<dim3(gx, 1), 128, 0, st>>>(g, in, W, cout, bias, skip, relu, mask, out);
-  else
-    k_conv3_mma<CIN, 4><<<dim3(gx, (unsigned)cdiv(cout, 32)), 128, 0, st>>>(g, in, W, cout, bias,
-                                                                           skip, relu, mask, out);
+  auto go = [&](auto nt_tag, unsigned gy) {
+    constexpr int NT = decltype(nt_tag)::value;
+    constexpr size_t smem = ConvTile<CIN, NT>::smem();
+    static const bool set = [] {   // once per instantiation, thread-safe
+      TG_CUDA(cudaFuncSetAttribute(k_conv3_mma<CIN, NT>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      return true;
+    }();
+    (void)set;
+    k_conv3_mma<CIN, NT><<<dim3(gx, gy), 128, smem, st>>>(g, in, W, cout, bias, skip, relu, mask,
+                                                          out);
+  };
+  if (cout <= 8) go(std::integral_constant<int, 1>{}, 1);
+  else if (cout <= 16) go(std::integral_constant<int, 2>{}, 1);
+  else go(std::integral_constant<int, 4>{}, (unsigned)cdiv(cout, 32));
   TG_CHECK_LAUNCH();
 }
 
