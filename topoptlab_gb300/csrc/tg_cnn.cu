@@ -72,15 +72,18 @@ __device__ __forceinline__ void mma_tf32(float (&d)[4], const uint32_t (&a)[4],
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
+// CTA tile: a block of 8 (y) x 4 (x) x 4 (z) output nodes; its input block
+// with a one-node halo (10 x 6 x 6 node rows, zero outside the grid) is
+// staged in shared memory once, and all 27 taps read their A fragments from
+// it (no barrier inside the tap loop).  Warp w computes z-layer w: two
+// 16-row tiles of 8 y x 2 x nodes.
 template <int CIN, int NT>
 struct ConvTile {
+  static constexpr int TY = 8, TX = 4, TZ = 4;
+  static constexpr int HY = TY + 2, HX = TX + 2, HZ = TZ + 2;
   static constexpr int CP = (CIN + 7) / 8 * 8;   // input channels padded to the MMA k
-  static constexpr int AS = CP + 4;              // A row stride (words): conflict-free fragments
-  static constexpr int NC = 8 * NT;              // output channels of a CTA
-  static constexpr int BS = NC + 8;              // B row stride (words): conflict-free fragments
-  static constexpr size_t smem() {
-    return sizeof(float) * 128 * AS + 2 * sizeof(uint32_t) * CP * BS + 4 * sizeof(int) * 128;
-  }
+  static constexpr int AS = CP + 4;              // row stride (words): conflict-free fragments
+  static constexpr size_t smem() { return sizeof(float) * HZ * HX * HY * AS; }
 };
 
 template <int CIN, int NT>
@@ -91,24 +94,22 @@ __global__ void __launch_bounds__(128) k_conv3_mma(NG g, const float* __restrict
                                                    const float* __restrict__ mask,
                                                    float* __restrict__ out) {
   using TT = ConvTile<CIN, NT>;
-  constexpr int CP = TT::CP, AS = TT::AS, NC = TT::NC, BS = TT::BS;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  float* As = reinterpret_cast<float*>(smem_raw);                      // [128][AS]
-  uint32_t* Bh = reinterpret_cast<uint32_t*>(As + 128 * AS);          // [CP][BS] tf32 hi
-  uint32_t* Bl = Bh + CP * BS;                                         // [CP][BS] tf32 lo
-  int* rxyz = reinterpret_cast<int*>(Bl + CP * BS);                    // [128][4]: x, y, z, valid
+  constexpr int CP = TT::CP, AS = TT::AS, HY = TT::HY, HX = TT::HX, HZ = TT::HZ;
+  extern __shared__ __align__(16) float hs[];       // [HZ][HX][HY][AS]
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int gq = lane >> 2, tq = lane & 3;
-  const int co0 = blockIdx.y * NC;
-  const int64_t n0 = blockIdx.x * (int64_t)128;
-  const int64_t nn = g.n();
-  {
-    const int64_t node = n0 + tid;
-    int x = 0, y = 0, z = 0;
-    if (node < nn) ng_xyz(g, node, x, y, z);
-    rxyz[4 * tid] = x; rxyz[4 * tid + 1] = y; rxyz[4 * tid + 2] = z;
-    rxyz[4 * tid + 3] = node < nn;
+  const int y0 = blockIdx.x * TT::TY, x0 = blockIdx.y * TT::TX;
+  const int zb = gridDim.z / ((cout + 8 * NT - 1) / (8 * NT));   // z blocks per channel chunk
+  const int z0 = (blockIdx.z % zb) * TT::TZ;
+  const int co0 = (blockIdx.z / zb) * 8 * NT;
+  // stage the halo block: one (z, x) row of HY nodes at a time
+  for (int i = tid; i < HZ * HX * HY * CP; i += 128) {
+    const int c = i % CP, hy = (i / CP) % HY, hx = (i / (CP * HY)) % HX, hz = i / (CP * HY * HX);
+    const int X = x0 - 1 + hx, Y = y0 - 1 + hy, Z = z0 - 1 + hz;
+    const bool ok = c < CIN && X >= 0 && X < g.nx && Y >= 0 && Y < g.ny && Z >= 0 && Z < g.nz;
+    hs[((hz * HX + hx) * HY + hy) * AS + c] = ok ? __ldg(in + ng_idx(g, X, Y, Z) * CIN + c) : 0.f;
   }
+  __syncthreads();
   float acc[2][NT][4];
 #pragma unroll
   for (int m = 0; m < 2; ++m)
@@ -119,46 +120,17 @@ __global__ void __launch_bounds__(128) k_conv3_mma(NG g, const float* __restrict
 #pragma unroll 1
   for (int k = 0; k < 27; ++k) {
     const int dy = k % 3 - 1, dx = (k / 3) % 3 - 1, dz = k / 9 - 1;
-    const int64_t off = ((int64_t)dz * g.nx + dx) * g.ny + dy;
-    __syncthreads();                 // previous tap's fragments consumed (and rxyz written)
-    // A: rows n0+r+off of the input (contiguous), zero where the neighbour is outside
-    if constexpr (CIN % 4 == 0) {
-      constexpr int V = CIN / 4;
-      for (int i = tid; i < 128 * V; i += 128) {
-        const int r = i / V, v = i % V;
-        const int X = rxyz[4 * r] + dx, Y = rxyz[4 * r + 1] + dy, Z = rxyz[4 * r + 2] + dz;
-        const bool ok = rxyz[4 * r + 3] && X >= 0 && X < g.nx && Y >= 0 && Y < g.ny && Z >= 0 &&
-                        Z < g.nz;
-        float4 val = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (ok) val = __ldg(reinterpret_cast<const float4*>(in + (n0 + r + off) * CIN) + v);
-        *reinterpret_cast<float4*>(As + r * AS + 4 * v) = val;
-      }
-    } else {
-      for (int i = tid; i < 128 * CP; i += 128) {
-        const int r = i / CP, c = i % CP;
-        const int X = rxyz[4 * r] + dx, Y = rxyz[4 * r + 1] + dy, Z = rxyz[4 * r + 2] + dz;
-        const bool ok = c < CIN && rxyz[4 * r + 3] && X >= 0 && X < g.nx && Y >= 0 &&
-                        Y < g.ny && Z >= 0 && Z < g.nz;
-        As[r * AS + c] = ok ? __ldg(in + (n0 + r + off) * CIN + c) : 0.f;
-      }
-    }
-    // B: this tap's weights of the CTA's output channels, split into tf32 hi / lo
+    // halo row of node (ly, lx, lz) shifted by the tap: lz = warp, lx = 2m (+1 for rows 8..15)
+    const float* base = hs + (((warp + 1 + dz) * HX + (1 + dx)) * HY + (1 + dy + gq)) * AS + tq;
     const float* wk = W + (int64_t)k * CIN * cout;
-    for (int i = tid; i < CP * NC; i += 128) {
-      const int c = i / NC, j = i % NC;
-      const float w = (c < CIN && co0 + j < cout) ? __ldg(wk + (int64_t)c * cout + co0 + j) : 0.f;
-      const uint32_t h = f2tf32(w);
-      Bh[c * BS + j] = h;
-      Bl[c * BS + j] = f2tf32(w - __uint_as_float(h));
-    }
-    __syncthreads();
 #pragma unroll
     for (int c0 = 0; c0 < CP; c0 += 8) {
       uint32_t ahi[2][4], alo[2][4];
 #pragma unroll
       for (int m = 0; m < 2; ++m) {
-        const float* a0 = As + (warp * 32 + m * 16 + gq) * AS + c0 + tq;
-        const float v[4] = {a0[0], a0[8 * AS], a0[4], a0[8 * AS + 4]};
+        const float* r0 = base + (2 * m) * HY * AS + c0;       // x = 2m,     y = gq
+        const float* r1 = base + (2 * m + 1) * HY * AS + c0;   // x = 2m + 1, y = gq
+        const float v[4] = {r0[0], r1[0], r0[4], r1[4]};
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           ahi[m][q] = f2tf32(v[q]);
@@ -167,9 +139,15 @@ __global__ void __launch_bounds__(128) k_conv3_mma(NG g, const float* __restrict
       }
 #pragma unroll
       for (int j = 0; j < NT; ++j) {
-        const int bi = (c0 + tq) * BS + j * 8 + gq;
-        const uint32_t bhi[2] = {Bh[bi], Bh[bi + 4 * BS]};
-        const uint32_t blo[2] = {Bl[bi], Bl[bi + 4 * BS]};
+        const int co = co0 + j * 8 + gq;
+        const bool k0 = c0 + tq < CIN, k1 = c0 + tq + 4 < CIN;
+        const float w0 = co < cout && k0 ? __ldg(wk + (int64_t)(c0 + tq) * cout + co) : 0.f;
+        const float w1 = co < cout && k1 ? __ldg(wk + (int64_t)(c0 + tq + 4) * cout + co) : 0.f;
+        uint32_t bhi[2], blo[2];
+        bhi[0] = f2tf32(w0);
+        bhi[1] = f2tf32(w1);
+        blo[0] = f2tf32(w0 - __uint_as_float(bhi[0]));
+        blo[1] = f2tf32(w1 - __uint_as_float(bhi[1]));
 #pragma unroll
         for (int m = 0; m < 2; ++m) {
           mma_tf32(acc[m][j], alo[m], bhi);
@@ -179,40 +157,46 @@ __global__ void __launch_bounds__(128) k_conv3_mma(NG g, const float* __restrict
       }
     }
   }
-  // epilogue: c0 (g, 2t), c1 (g, 2t + 1), c2 (g + 8, 2t), c3 (g + 8, 2t + 1)
+  // epilogue: c0 (g, 2t), c1 (g, 2t + 1), c2 (g + 8, 2t), c3 (g + 8, 2t + 1); tile row
+  // r < 8 is node (y = r, x = 2m), r >= 8 node (y = r - 8, x = 2m + 1)
+  const int Z = z0 + warp;
 #pragma unroll
   for (int m = 0; m < 2; ++m)
 #pragma unroll
-    for (int j = 0; j < NT; ++j)
+    for (int q = 0; q < 4; ++q) {
+      const int X = x0 + 2 * m + (q >> 1), Y = y0 + gq;
+      if (X >= g.nx || Y >= g.ny || Z >= g.nz) continue;
+      const int64_t node = ng_idx(g, X, Y, Z);
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int64_t node = n0 + warp * 32 + m * 16 + (q >> 1) * 8 + gq;
+      for (int j = 0; j < NT; ++j) {
         const int co = co0 + j * 8 + 2 * tq + (q & 1);
-        if (node >= nn || co >= cout) continue;
+        if (co >= cout) continue;
         float v = acc[m][j][q] + (bias ? bias[co] : 0.f);
         if (skip) v += skip[node * cout + co];
         if (relu) v = fmaxf(v, 0.f);
         if (mask && !(mask[node * cout + co] > 0.f)) v = 0.f;
         out[node * cout + co] = v;
       }
+    }
 }
 
 template <int CIN>
 static void conv3_launch(const NG& g, const float* in, const float* W, int cout, const float* bias,
                          const float* skip, int relu, const float* mask, float* out,
                          cudaStream_t st) {
-  const unsigned gx = (unsigned)cdiv(g.n(), 128);
-  auto go = [&](auto nt_tag, unsigned gy) {
+  auto go = [&](auto nt_tag, unsigned chunks) {
     constexpr int NT = decltype(nt_tag)::value;
-    constexpr size_t smem = ConvTile<CIN, NT>::smem();
+    using TT = ConvTile<CIN, NT>;
+    constexpr size_t smem = TT::smem();
+    const dim3 grid((unsigned)cdiv(g.ny, TT::TY), (unsigned)cdiv(g.nx, TT::TX),
+                    (unsigned)cdiv(g.nz, TT::TZ) * chunks);
     static const bool set = [] {   // once per instantiation, thread-safe
       TG_CUDA(cudaFuncSetAttribute(k_conv3_mma<CIN, NT>,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       return true;
     }();
     (void)set;
-    k_conv3_mma<CIN, NT><<<dim3(gx, gy), 128, smem, st>>>(g, in, W, cout, bias, skip, relu, mask,
-                                                          out);
+    k_conv3_mma<CIN, NT><<<grid, 128, smem, st>>>(g, in, W, cout, bias, skip, relu, mask, out);
   };
   if (cout <= 8) go(std::integral_constant<int, 1>{}, 1);
   else if (cout <= 16) go(std::integral_constant<int, 2>{}, 1);
