@@ -222,6 +222,9 @@ int32_t tg_cnn_params(tg_cnn* cnn, int32_t set, float* host, int64_t n);
  * grads may be NULL) */
 int32_t tg_cnn_eval(tg_cnn* cnn, const float* x0, const float* target, float* y, double* loss,
                     float* grads);
+/* the forward pass as the warm start runs it (single TF32 products instead of
+ * the split FP32-level ones of tg_cnn_eval): host x0 [nodes][7] -> y [nodes][3] */
+int32_t tg_cnn_infer(tg_cnn* cnn, const float* x0, float* y);
 /* Device time between two calls on the context's stream: op 0 records the
  * start event, op 1 records the stop event, synchronises and writes the
  * elapsed milliseconds to *ms. */

@@ -55,6 +55,36 @@ def test_forward_and_gradient_match_oracle(gpu_lib):
     np.testing.assert_allclose(g, g_ref, rtol=0, atol=2e-3 * np.abs(g_ref).max())
 
 
+def test_tf32_inference_matches_oracle(gpu_lib):
+    """The warm start's forward pass uses single TF32 products (10-bit operand
+    mantissas, FP32 accumulation) instead of the split FP32-level ones: its
+    output stays within 1e-2 of the largest output of the FP32 oracle, while
+    the split pass (tg_cnn_eval) is within 1e-4."""
+    pytest.importorskip("torch")
+    from topoptlab_gb300.learned import LearnedWarmStart
+    from oracle import cnn as N
+    prob = _problem(16, 8, 8)
+    net = LearnedWarmStart(prob, capacity=1, seed=3)
+    try:
+        info = net.info()
+        grid = info["grid"]
+        nn = grid[0] * grid[1] * grid[2]
+        rng = np.random.default_rng(7)
+        p = (rng.standard_normal(info["nparams"]) * 0.05).astype(np.float32)
+        net.set_params(p)
+        x0 = rng.standard_normal((nn, 7)).astype(np.float32)
+        t = rng.standard_normal((nn, 3)).astype(np.float32)
+        y_tf32 = net.infer(x0)
+        y_split = net.eval(x0)
+    finally:
+        net.close()
+        prob.close()
+    _, _, y_ref = N.loss_and_grad(p.astype(np.float64), x0, t, grid)
+    scale = np.abs(y_ref).max()
+    np.testing.assert_allclose(y_split, y_ref, rtol=0, atol=1e-4 * scale)
+    np.testing.assert_allclose(y_tf32, y_ref, rtol=0, atol=1e-2 * scale)
+
+
 def test_training_fallback_and_gain(gpu_lib):
     """Train on pairs from optimisation runs started at seeded random
     densities, then run the same design iterations with and without the

@@ -548,4 +548,17 @@ int32_t tg_cnn_eval(tg_cnn* cnn, const float* x0, const float* target, float* y,
   });
 }
 
+int32_t tg_cnn_infer(tg_cnn* cnn, const float* x0, float* y) {
+  if (!cnn || !x0 || !y) return TG_EINVAL;
+  return guarded(cnn->owner, [&] {
+    tg::Cnn& net = *cnn->net;
+    cudaStream_t st = cnn->owner->c.st;
+    const int64_t na = net.A.n();
+    h2d(net.x0.p, x0, na * 7, st);
+    net.forward(st, false);
+    d2h(y, net.y.p, na * 3, st);
+    TG_CUDA(cudaStreamSynchronize(st));
+  });
+}
+
 }  // extern "C"

@@ -47,9 +47,12 @@ __device__ __forceinline__ int64_t ng_idx(const NG& g, int x, int y, int z) {
 // The convolution runs on the tensor cores as an implicit GEMM
 // out[n][co] = sum_{k, ci} in[nbr(n, k)][ci] W[k][ci][co] with warp-level
 // mma.sync m16n8k8 TF32 and FP32 accumulation.
-// Each FP32 operand is split as hi = tf32(v), lo = tf32(v - hi) and the
-// product taken as hi*hi + hi*lo + lo*hi (three MMAs), which keeps FP32-level
-// accuracy (the network is trained and checked in FP32).  A CTA of 4 warps
+// SPLIT: each FP32 operand is split as hi = tf32(v), lo = tf32(v - hi) and
+// the product taken as hi*hi + hi*lo + lo*hi (three MMAs), which keeps
+// FP32-level accuracy (training, and every check against the FP32 oracle);
+// without SPLIT one TF32 MMA (the warm-start inference: its output is a
+// correction whose use the fallback rule guards, so TF32 rounding of the
+// operands is immaterial).  A CTA of 4 warps
 // computes 128 consecutive nodes (a warp: two 16-row tiles) times 8*NT output
 // channels (blockIdx.y selects the chunk); A fragments are gathered from the
 // channels-last input (zero outside the grid), B fragments read through the
@@ -86,7 +89,7 @@ struct ConvTile {
   static constexpr size_t smem() { return sizeof(float) * HZ * HX * HY * AS; }
 };
 
-template <int CIN, int NT>
+template <int CIN, int NT, bool SPLIT>
 __global__ void __launch_bounds__(128) k_conv3_mma(NG g, const float* __restrict__ in,
                                                    const float* __restrict__ W, int cout,
                                                    const float* __restrict__ bias,
@@ -134,7 +137,7 @@ __global__ void __launch_bounds__(128) k_conv3_mma(NG g, const float* __restrict
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           ahi[m][q] = f2tf32(v[q]);
-          alo[m][q] = f2tf32(v[q] - __uint_as_float(ahi[m][q]));
+          if (SPLIT) alo[m][q] = f2tf32(v[q] - __uint_as_float(ahi[m][q]));
         }
       }
 #pragma unroll
@@ -146,12 +149,16 @@ __global__ void __launch_bounds__(128) k_conv3_mma(NG g, const float* __restrict
         uint32_t bhi[2], blo[2];
         bhi[0] = f2tf32(w0);
         bhi[1] = f2tf32(w1);
-        blo[0] = f2tf32(w0 - __uint_as_float(bhi[0]));
-        blo[1] = f2tf32(w1 - __uint_as_float(bhi[1]));
+        if (SPLIT) {
+          blo[0] = f2tf32(w0 - __uint_as_float(bhi[0]));
+          blo[1] = f2tf32(w1 - __uint_as_float(bhi[1]));
+        }
 #pragma unroll
         for (int m = 0; m < 2; ++m) {
-          mma_tf32(acc[m][j], alo[m], bhi);
-          mma_tf32(acc[m][j], ahi[m], blo);
+          if (SPLIT) {
+            mma_tf32(acc[m][j], alo[m], bhi);
+            mma_tf32(acc[m][j], ahi[m], blo);
+          }
           mma_tf32(acc[m][j], ahi[m], bhi);
         }
       }
@@ -180,7 +187,7 @@ __global__ void __launch_bounds__(128) k_conv3_mma(NG g, const float* __restrict
     }
 }
 
-template <int CIN>
+template <int CIN, bool SPLIT>
 static void conv3_launch(const NG& g, const float* in, const float* W, int cout, const float* bias,
                          const float* skip, int relu, const float* mask, float* out,
                          cudaStream_t st) {
@@ -191,12 +198,13 @@ static void conv3_launch(const NG& g, const float* in, const float* W, int cout,
     const dim3 grid((unsigned)cdiv(g.ny, TT::TY), (unsigned)cdiv(g.nx, TT::TX),
                     (unsigned)cdiv(g.nz, TT::TZ) * chunks);
     static const bool set = [] {   // once per instantiation, thread-safe
-      TG_CUDA(cudaFuncSetAttribute(k_conv3_mma<CIN, NT>,
+      TG_CUDA(cudaFuncSetAttribute(k_conv3_mma<CIN, NT, SPLIT>,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       return true;
     }();
     (void)set;
-    k_conv3_mma<CIN, NT><<<grid, 128, smem, st>>>(g, in, W, cout, bias, skip, relu, mask, out);
+    k_conv3_mma<CIN, NT, SPLIT><<<grid, 128, smem, st>>>(g, in, W, cout, bias, skip, relu, mask,
+                                                         out);
   };
   if (cout <= 8) go(std::integral_constant<int, 1>{}, 1);
   else if (cout <= 16) go(std::integral_constant<int, 2>{}, 1);
@@ -206,15 +214,20 @@ static void conv3_launch(const NG& g, const float* in, const float* W, int cout,
 
 static void conv3(const NG& g, int cin, const float* in, const float* W, int cout,
                   const float* bias, const float* skip, int relu, const float* mask, float* out,
-                  cudaStream_t st) {
+                  cudaStream_t st, bool split = true) {
+#define TG_C3(CI)                                                                                \
+  if (split) conv3_launch<CI, true>(g, in, W, cout, bias, skip, relu, mask, out, st);            \
+  else conv3_launch<CI, false>(g, in, W, cout, bias, skip, relu, mask, out, st);
   switch (cin) {
-    case 3: conv3_launch<3>(g, in, W, cout, bias, skip, relu, mask, out, st); break;
-    case 7: conv3_launch<7>(g, in, W, cout, bias, skip, relu, mask, out, st); break;
-    case 16: conv3_launch<16>(g, in, W, cout, bias, skip, relu, mask, out, st); break;
-    case 32: conv3_launch<32>(g, in, W, cout, bias, skip, relu, mask, out, st); break;
-    case 64: conv3_launch<64>(g, in, W, cout, bias, skip, relu, mask, out, st); break;
+    case 3: TG_C3(3) break;
+    case 7: TG_C3(7) break;
+    case 16: TG_C3(16) break;
+    case 32: TG_C3(32) break;
+    case 64: TG_C3(64) break;
     default: throw Error{EINVAL_, "conv3: unsupported input channel count"};
   }
+#undef TG_C3
+}
 }
 
 // W'[k'][co][ci] = W[26-k'][ci][co]: the input gradient is a convolution of the
@@ -531,24 +544,24 @@ Cnn::Cnn(Ctx& c, int capacity, uint64_t seed) : ctx(&c) {
   TG_CUDA(cudaStreamSynchronize(c.st));
 }
 
-void Cnn::forward(cudaStream_t st) {
+void Cnn::forward(cudaStream_t st, bool split) {
   const float* P = params.p;
   auto W = [&](int i) { return P + layers[i].w_off; };
   auto b = [&](int i) { return P + layers[i].b_off; };
-  conv3(A, 7, x0, W(0), 16, b(0), nullptr, 1, nullptr, e1, st);
+  conv3(A, 7, x0, W(0), 16, b(0), nullptr, 1, nullptr, e1, st, split);
   k_pool<<<nb(B.n() * 16), 256, 0, st>>>(A, B, 16, e1, p1);
   TG_CHECK_LAUNCH();
-  conv3(B, 16, p1, W(1), 32, b(1), nullptr, 1, nullptr, e2, st);
+  conv3(B, 16, p1, W(1), 32, b(1), nullptr, 1, nullptr, e2, st, split);
   k_pool<<<nb(Cg.n() * 32), 256, 0, st>>>(B, Cg, 32, e2, p2);
   TG_CHECK_LAUNCH();
-  conv3(Cg, 32, p2, W(2), 64, b(2), nullptr, 1, nullptr, e3, st);
+  conv3(Cg, 32, p2, W(2), 64, b(2), nullptr, 1, nullptr, e3, st, split);
   k_up<<<nb(B.n() * 64), 256, 0, st>>>(B, Cg, 64, e3, u2);
   TG_CHECK_LAUNCH();
-  conv3(B, 64, u2, W(3), 32, b(3), e2, 1, nullptr, d2, st);
+  conv3(B, 64, u2, W(3), 32, b(3), e2, 1, nullptr, d2, st, split);
   k_up<<<nb(A.n() * 32), 256, 0, st>>>(A, B, 32, d2, u1);
   TG_CHECK_LAUNCH();
-  conv3(A, 32, u1, W(4), 16, b(4), e1, 1, nullptr, d1, st);
-  conv3(A, 16, d1, W(5), 3, b(5), nullptr, 0, nullptr, y, st);
+  conv3(A, 32, u1, W(4), 16, b(4), e1, 1, nullptr, d1, st, split);
+  conv3(A, 16, d1, W(5), 3, b(5), nullptr, 0, nullptr, y, st, split);
 }
 
 // loss against tgt, gradients into grads (forward must have run)
@@ -768,7 +781,7 @@ int Cnn::warm_start(Ctx& c) {
   const int64_t n = c.g.ndofs();
   double* v2 = c.z2.p;
   features(c, c.u);            // also leaves r32a = f - K u_prev
-  forward(c.st);
+  forward(c.st, false);        // TF32 inference
   k_correction<<<nb(c.lv[1]->g.ndofs()), 256, 0, c.st>>>(c.lv[1]->g.ndofs(), y, su, corr);
   TG_CHECK_LAUNCH();
   TG_CUDA(cudaMemsetAsync(v2, 0, sizeof(double) * n, c.st));

@@ -40,7 +40,8 @@ struct Cnn {
   bool trained = false;
 
   Cnn(Ctx& c, int capacity, uint64_t seed);
-  void forward(cudaStream_t st);
+  // split: FP32-level split-TF32 products (training, checks); otherwise TF32
+  void forward(cudaStream_t st, bool split = true);
   double backward(cudaStream_t st, bool want_loss);
   void adam_step(cudaStream_t st);
   void features(Ctx& c, const double* u_prev);

@@ -99,6 +99,16 @@ class LearnedWarmStart:
                     "tg_cnn_eval")
         return (y, loss.value, grads) if target is not None else y
 
+    def infer(self, x0):
+        """Forward pass as the warm start runs it (single TF32 products)."""
+        g = self.info()["grid"]
+        nn = g[0] * g[1] * g[2]
+        x = np.ascontiguousarray(np.asarray(x0, dtype=np.float32).reshape(nn, 7))
+        y = np.empty((nn, 3), dtype=np.float32)
+        self._check(self._lib.tg_cnn_infer(self._h, x.ctypes.data_as(_fp), y.ctypes.data_as(_fp)),
+                    "tg_cnn_infer")
+        return y
+
 
 def layer_spec():
     """(cin, cout) of the six convolutions, in parameter order; each layer's
