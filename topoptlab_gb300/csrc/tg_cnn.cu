@@ -228,7 +228,6 @@ static void conv3(const NG& g, int cin, const float* in, const float* W, int cou
   }
 #undef TG_C3
 }
-}
 
 // W'[k'][co][ci] = W[26-k'][ci][co]: the input gradient is a convolution of the
 // output gradient with these weights
