@@ -539,7 +539,8 @@ Cnn::Cnn(Ctx& c, int capacity, uint64_t seed) : ctx(&c) {
   corr.alloc(g1.ndofs());
   r32a.alloc(c.g.ndofs());
   su.alloc(1); sr.alloc(1); su.zero(c.st); sr.zero(c.st);
-  gal.alloc(5); gal.zero(c.st);
+  gal.alloc(6); gal.zero(c.st);
+  wsb.alloc(4); wsb.zero(c.st);
   TG_CUDA(cudaStreamSynchronize(c.st));
 }
 
@@ -639,11 +640,12 @@ void Cnn::adam_step(cudaStream_t st) {
 // solver-state interface
 // ---------------------------------------------------------------------------
 // r32a = f - K(xPhys) u in FP32 (scale factors s32 must hold simp(xPhys))
+// out = f - K u in FP32; leaves p32 = u and z32 = f (FP32 copies)
 static void residual32(Ctx& c, const double* u, float* out) {
   const int64_t n = c.g.ndofs();
   d2f(n, u, c.p32, c.st);
-  d2f(n, c.f, c.q32, c.st);
-  fine_apply<float, float>(c.op, c.s32, c.p32, out, c.q32, nullptr, 0.0, AM_RES, c.st);
+  d2f(n, c.f, c.z32, c.st);
+  fine_apply<float, float>(c.op, c.s32, c.p32, out, c.z32, nullptr, 0.0, AM_RES, c.st);
 }
 
 void Cnn::features(Ctx& c, const double* u_prev) {
@@ -764,11 +766,6 @@ __global__ void __launch_bounds__(RED_THREADS) k_dot5(int64_t n, const float* __
   if (threadIdx.x == 0) out[0].ticket = 0;
 }
 
-__global__ void k_combine(int64_t n, double c1, const double* v1, double c2, const double* v2,
-                          double* out) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i < n) out[i] = c1 * v1[i] + c2 * v2[i];
-}
 
 // Warm start for the current design.  The network's level-1 correction is
 // prolongated to the fine grid (v2 = P d) and combined with the previous
@@ -776,46 +773,88 @@ __global__ void k_combine(int64_t n, double c1, const double* v1, double c2, con
 //   [v_i^T K v_j] c = [v_i^T f],   u0 = c1 v1 + c2 v2,
 // with the products in FP32; u0 replaces u_prev only when its FP32 residual
 // is smaller.  Returns 1 on fallback.
-int Cnn::warm_start(Ctx& c) {
+// The 2x2 Galerkin solve on the device: ws = {c1, c2, valid, accepted}
+__global__ void k_ws_solve(const PCGState* gal, double* ws) {
+  const double g11 = gal[0].bb, g12 = gal[1].bb, g22 = gal[2].bb, f1 = gal[3].bb, f2 = gal[4].bb;
+  const double det = g11 * g22 - g12 * g12;
+  const bool ok = isfinite(det) && det > 1e-12 * fabs(g11 * g22) && g11 > 0 && g22 > 0;
+  ws[0] = ok ? (f1 * g22 - f2 * g12) / det : 0.0;
+  ws[1] = ok ? (f2 * g11 - f1 * g12) / det : 0.0;
+  ws[2] = ok ? 1.0 : 0.0;
+  ws[3] = 0.0;
+}
+// ||f - c1 K v1 - c2 K v2||^2 from the products already formed (FP32 vectors,
+// FP64 block and grid sums); the last block accepts the candidate when the
+// solve was valid and this residual is below the previous displacement's
+// (sr.rr), writing the decision to ws[3] and to *accepted
+__global__ void __launch_bounds__(RED_THREADS) k_ws_check(int64_t n, const float* __restrict__ f,
+                                                         const float* __restrict__ kv1,
+                                                         const float* __restrict__ kv2,
+                                                         double* ws, const PCGState* sr,
+                                                         double* part, PCGState* tk,
+                                                         double* accepted) {
+  __shared__ double sh[32];
+  __shared__ int last;
+  const float c1 = (float)ws[0], c2 = (float)ws[1];
+  float acc = 0.f;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float r = f[i] - c1 * kv1[i] - c2 * kv2[i];
+    acc = fmaf(r, r, acc);
+  }
+  const double bs = block_sum((double)acc, sh);
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = bs;
+    __threadfence();
+    last = (atomicAdd(&tk->ticket, 1u) == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  const double tot = sum_partials(part, (int)gridDim.x, sh);
+  if (threadIdx.x == 0) {
+    const double acc_ok = (ws[2] != 0.0 && isfinite(tot) && tot < sr->rr) ? 1.0 : 0.0;
+    ws[3] = acc_ok;
+    *accepted = acc_ok;
+    tk->ticket = 0;
+  }
+}
+// u <- c1 u + c2 v2 when accepted
+__global__ void k_ws_apply(int64_t n, const double* ws, double* u, const double* v2) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n && ws[3] != 0.0) u[i] = ws[0] * u[i] + ws[1] * v2[i];
+}
+
+// Warm start for the current design.  The network's level-1 correction is
+// prolongated to the fine grid (v2 = P d) and combined with the previous
+// displacement (v1) by the energy-optimal (Galerkin) 2x2 solve
+//   [v_i^T K v_j] c = [v_i^T f],   u0 = c1 v1 + c2 v2,
+// with the products in FP32; u0 replaces u_prev only when its FP32 residual
+// f - c1 K v1 - c2 K v2 is smaller than u_prev's (the fallback rule).  All on
+// the device: the decision (1 = accepted) lands in *accepted.
+void Cnn::warm_start(Ctx& c, double* accepted) {
   const int64_t n = c.g.ndofs();
   double* v2 = c.z2.p;
-  features(c, c.u);            // also leaves r32a = f - K u_prev
+  features(c, c.u);            // p32 = u_prev, z32 = f, r32a = f - K u_prev
   forward(c.st, false);        // TF32 inference
   k_correction<<<nb(c.lv[1]->g.ndofs()), 256, 0, c.st>>>(c.lv[1]->g.ndofs(), y, su, corr);
   TG_CHECK_LAUNCH();
   TG_CUDA(cudaMemsetAsync(v2, 0, sizeof(double) * n, c.st));
   prolong_add<double>(c.g, c.lv[1]->g, c.op.fix, corr, v2, c.st);
-  // FP32 copies and products: p32 = v1, d32 = v2, q32 = K v1, r32 = K v2, z32 = f
-  d2f(n, c.u, c.p32, c.st);
+  // d32 = v2, q32 = K v1, r32 = K v2
   d2f(n, v2, c.d32, c.st);
-  d2f(n, c.f, c.z32, c.st);
   fine_apply<float, float>(c.op, c.s32, c.p32, c.q32, nullptr, nullptr, 0.0, AM_Y, c.st);
   fine_apply<float, float>(c.op, c.s32, c.d32, c.r32, nullptr, nullptr, 0.0, AM_Y, c.st);
   const unsigned b5 = std::min<unsigned>(red_blocks(n), (unsigned)DOT5_BLOCKS);
   k_dot5<<<b5, RED_THREADS, 0, c.st>>>(n, c.p32, c.d32, c.q32, c.r32, c.z32, c.part, gal.p);
   TG_CHECK_LAUNCH();
-  PCGState hg[5], hp{};
-  TG_CUDA(cudaMemcpyAsync(hg, gal.p, sizeof(PCGState) * 5, cudaMemcpyDeviceToHost, c.st));
-  TG_CUDA(cudaMemcpyAsync(&hp, sr.p, sizeof(PCGState), cudaMemcpyDeviceToHost, c.st));
-  TG_CUDA(cudaStreamSynchronize(c.st));
-  const double g11 = hg[0].bb, g12 = hg[1].bb, g22 = hg[2].bb, f1 = hg[3].bb, f2 = hg[4].bb;
-  const double det = g11 * g22 - g12 * g12;
-  if (!(std::isfinite(det) && det > 1e-12 * std::fabs(g11 * g22) && g11 > 0 && g22 > 0)) return 1;
-  const double c1 = (f1 * g22 - f2 * g12) / det, c2 = (f2 * g11 - f1 * g12) / det;
-  double* cand = c.r.p;        // free until the solve starts
-  k_combine<<<nb(n), 256, 0, c.st>>>(n, c1, c.u, c2, v2, cand);
+  k_ws_solve<<<1, 1, 0, c.st>>>(gal.p, wsb.p);
   TG_CHECK_LAUNCH();
-  residual32(c, cand, c.r32);
-  pcg_reset(c.pcg_out, c.st);
-  dot<float, float>(n, c.r32.p, c.r32.p, c.part, c.pcg_out, DOT_RR, c.st);
-  PCGState hs{};
-  TG_CUDA(cudaMemcpyAsync(&hs, c.pcg_out.p, sizeof(PCGState), cudaMemcpyDeviceToHost, c.st));
-  TG_CUDA(cudaStreamSynchronize(c.st));
-  if (std::isfinite(hs.rr) && hs.rr < hp.rr) {
-    TG_CUDA(cudaMemcpyAsync(c.u.p, cand, sizeof(double) * n, cudaMemcpyDeviceToDevice, c.st));
-    return 0;
-  }
-  return 1;
+  k_ws_check<<<red_blocks(n), RED_THREADS, 0, c.st>>>(n, c.z32, c.q32, c.r32, wsb.p, sr.p, c.part,
+                                                      gal.p + 5, accepted);
+  TG_CHECK_LAUNCH();
+  k_ws_apply<<<nb(n), 256, 0, c.st>>>(n, wsb.p, c.u.p, v2);
+  TG_CHECK_LAUNCH();
 }
 
 }  // namespace tg

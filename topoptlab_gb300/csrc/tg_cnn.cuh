@@ -34,7 +34,8 @@ struct Cnn {
   DevBuf<double> uprev, corr;
   DevBuf<float> r32a;
   DevBuf<PCGState> su, sr;       // norms of u_prev and of its residual
-  DevBuf<PCGState> gal;          // the five products of the 2x2 Galerkin combination
+  DevBuf<PCGState> gal;          // the five products of the 2x2 Galerkin combination (+ a ticket)
+  DevBuf<double> wsb;            // c1, c2, valid, accepted of the last warm start
   float lr = 1e-3f;
   int adam_t = 0;
   bool trained = false;
@@ -48,7 +49,7 @@ struct Cnn {
   void record_begin(Ctx& c);
   void record_end(Ctx& c);
   double train(int epochs, float lr, uint64_t seed);
-  int warm_start(Ctx& c);
+  void warm_start(Ctx& c, double* accepted);   // accepted: device flag (1 = used)
 };
 
 }  // namespace tg

@@ -844,10 +844,10 @@ void ctx_step(Ctx& c, tg_iter_out& out) {
   build_hierarchy(c);
   // learned warm start (falls back to the previous displacement when its
   // residual is not smaller); the solve below is unchanged either way
-  int fallback = 0;
-  if (c.learned && c.cnn && c.cnn->trained && c.iter > 0 && c.nload == 1) {
+  const bool warm = c.learned && c.cnn && c.cnn->trained && c.iter > 0 && c.nload == 1;
+  if (warm) {
     ProfScope ps(PK_LEARNED, c.st);
-    fallback = c.cnn->warm_start(c);
+    c.cnn->warm_start(c, c.scal.p + 3);   // decision read back with the scalars below
   }
   // one solve per load case with the same hierarchy (topology_optimization.py:446-459)
   const int64_t nd = g.ndofs();
@@ -897,11 +897,12 @@ void ctx_step(Ctx& c, tg_iter_out& out) {
                     c.part2, c.st);
   reduce_partials(c.part, nbe, c.scal.p + 1, false, c.st);
   reduce_partials(c.part2, nbe, c.scal.p + 2, true, c.st);
-  TG_CUDA(cudaMemcpyAsync(c.h_scal, c.scal.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, c.st));
+  TG_CUDA(cudaMemcpyAsync(c.h_scal, c.scal.p, 4 * sizeof(double), cudaMemcpyDeviceToHost, c.st));
   TG_CUDA(cudaStreamSynchronize(c.st));
   if (c.h_oc->bar.err) throw Error{ETIMEOUT, "OC bisection: a grid barrier wait timed out"};
   if (!c.h_oc->done) throw Error{ENOTCONV, "OC bisection did not terminate within 256 steps"};
   c.g_oc = c.h_oc->gt;
+  const int fallback = (warm && c.h_scal[3] == 0.0) ? 1 : 0;
   const double vol_sum = c.h_scal[1];
   float ms = 0.f;
   TG_CUDA(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
