@@ -105,13 +105,26 @@ __global__ void __launch_bounds__(128) k_conv3_mma(NG g, const float* __restrict
   const int zb = gridDim.z / ((cout + 8 * NT - 1) / (8 * NT));   // z blocks per channel chunk
   const int z0 = (blockIdx.z % zb) * TT::TZ;
   const int co0 = (blockIdx.z / zb) * 8 * NT;
-  // stage the halo block: one (z, x) row of HY nodes at a time
-  for (int i = tid; i < HZ * HX * HY * CP; i += 128) {
-    const int c = i % CP, hy = (i / CP) % HY, hx = (i / (CP * HY)) % HX, hz = i / (CP * HY * HX);
+  // stage the halo block (zero outside the grid): 16-byte pieces of a node's
+  // channels when CIN is a multiple of 8 (a node's channels are contiguous, AS
+  // is a multiple of 4 and there are no padding columns), single values
+  // (padding columns zero) otherwise
+  constexpr int VW = (CIN % 8 == 0) ? 4 : 1;     // CIN % 8 == 0: no padding columns
+  constexpr int NV = (CIN % 8 == 0) ? CIN / 4 : CP;
+  for (int i = tid; i < HZ * HX * HY * NV; i += 128) {
+    const int v = i % NV, hy = (i / NV) % HY, hx = (i / (NV * HY)) % HX, hz = i / (NV * HY * HX);
     const int X = x0 - 1 + hx, Y = y0 - 1 + hy, Z = z0 - 1 + hz;
-    const bool ok = c < CIN && X >= 0 && X < g.nx && Y >= 0 && Y < g.ny && Z >= 0 && Z < g.nz;
-    hs[((hz * HX + hx) * HY + hy) * AS + c] = ok ? __ldg(in + ng_idx(g, X, Y, Z) * CIN + c) : 0.f;
+    const bool in_grid = X >= 0 && X < g.nx && Y >= 0 && Y < g.ny && Z >= 0 && Z < g.nz;
+    float* dst = hs + ((hz * HX + hx) * HY + hy) * AS + v * VW;
+    if constexpr (VW == 4) {
+      float4 val = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (in_grid) val = __ldg(reinterpret_cast<const float4*>(in + ng_idx(g, X, Y, Z) * CIN) + v);
+      *reinterpret_cast<float4*>(dst) = val;
+    } else {
+      *dst = (in_grid && v < CIN) ? __ldg(in + ng_idx(g, X, Y, Z) * CIN + v) : 0.f;
+    }
   }
+
   __syncthreads();
   float acc[2][NT][4];
 #pragma unroll
