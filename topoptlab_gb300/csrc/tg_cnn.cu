@@ -219,7 +219,9 @@ static void conv3_launch(const NG& g, const float* in, const float* W, int cout,
     k_conv3_mma<CIN, NT, SPLIT><<<grid, 128, smem, st>>>(g, in, W, cout, bias, skip, relu, mask,
                                                          out);
   };
-  if (cout <= 8) go(std::integral_constant<int, 1>{}, 1);
+  // coarse network levels have few nodes: 8 output channels per CTA there, so
+  // that enough warps run (each CTA stages its small halo block again)
+  if (cout <= 8 || g.n() < 65536) go(std::integral_constant<int, 1>{}, (unsigned)cdiv(cout, 8));
   else if (cout <= 16) go(std::integral_constant<int, 2>{}, 1);
   else go(std::integral_constant<int, 4>{}, (unsigned)cdiv(cout, 32));
   TG_CHECK_LAUNCH();
