@@ -133,12 +133,37 @@ __global__ void __launch_bounds__(128) k_conv3_mma(NG g, const float* __restrict
     for (int j = 0; j < NT; ++j)
 #pragma unroll
       for (int q = 0; q < 4; ++q) acc[m][j][q] = 0.f;
+  // this thread's B values of a tap (rows c0 + t and c0 + t + 4, column 8 j + g),
+  // loaded one tap ahead so that the read-only-cache latency overlaps the
+  // current tap's MMAs
+  constexpr int NCH = CP / 8;
+  float wn[NCH][NT][2];
+  auto load_w = [&](int k, float (&w)[NCH][NT][2]) {
+    const float* wk = W + (int64_t)k * CIN * cout;
+#pragma unroll
+    for (int ch = 0; ch < NCH; ++ch)
+#pragma unroll
+      for (int j = 0; j < NT; ++j) {
+        const int co = co0 + j * 8 + gq, c = ch * 8 + tq;
+        w[ch][j][0] = co < cout && c < CIN ? __ldg(wk + (int64_t)c * cout + co) : 0.f;
+        w[ch][j][1] = co < cout && c + 4 < CIN ? __ldg(wk + (int64_t)(c + 4) * cout + co) : 0.f;
+      }
+  };
+  load_w(0, wn);
 #pragma unroll 1
   for (int k = 0; k < 27; ++k) {
     const int dy = k % 3 - 1, dx = (k / 3) % 3 - 1, dz = k / 9 - 1;
     // halo row of node (ly, lx, lz) shifted by the tap: lz = warp, lx = 2m (+1 for rows 8..15)
     const float* base = hs + (((warp + 1 + dz) * HX + (1 + dx)) * HY + (1 + dy + gq)) * AS + tq;
-    const float* wk = W + (int64_t)k * CIN * cout;
+    float wc[NCH][NT][2];
+#pragma unroll
+    for (int ch = 0; ch < NCH; ++ch)
+#pragma unroll
+      for (int j = 0; j < NT; ++j) {
+        wc[ch][j][0] = wn[ch][j][0];
+        wc[ch][j][1] = wn[ch][j][1];
+      }
+    if (k + 1 < 27) load_w(k + 1, wn);
 #pragma unroll
     for (int c0 = 0; c0 < CP; c0 += 8) {
       uint32_t ahi[2][4], alo[2][4];
@@ -155,10 +180,7 @@ __global__ void __launch_bounds__(128) k_conv3_mma(NG g, const float* __restrict
       }
 #pragma unroll
       for (int j = 0; j < NT; ++j) {
-        const int co = co0 + j * 8 + gq;
-        const bool k0 = c0 + tq < CIN, k1 = c0 + tq + 4 < CIN;
-        const float w0 = co < cout && k0 ? __ldg(wk + (int64_t)(c0 + tq) * cout + co) : 0.f;
-        const float w1 = co < cout && k1 ? __ldg(wk + (int64_t)(c0 + tq + 4) * cout + co) : 0.f;
+        const float w0 = wc[c0 / 8][j][0], w1 = wc[c0 / 8][j][1];
         uint32_t bhi[2], blo[2];
         bhi[0] = f2tf32(w0);
         bhi[1] = f2tf32(w1);
