@@ -6,15 +6,22 @@
 // fem.py:141-237, linear_solvers.py:130) and the compliance / sensitivity
 // gathers (objectives.py:51-55, topology_optimization.py:491-500).
 //
-// Design (GB300): one CTA owns a brick of nodes (16 y x 8 x x 8 z in 3-D,
-// 32 x 32 in 2-D), stages the u halo in shared memory, evaluates every
-// element touching the brick and accumulates into a shared output tile in
-// 2^ndim colour passes (elements of one colour share no node), so the sum
-// order at each node is fixed: results are bit-reproducible and need no
-// atomics.  The element product uses the reflection-sector form
-// KE = H B H (Walsh-Hadamard over corner bits, B block diagonal), ~240 flops
-// per hex8 element instead of 1152: GB300's FP64 pipe is narrow, and the
-// FP64 residual is the one K.u the mixed-precision solver cannot avoid.
+// Design (GB300).  3-D: k_fine_zstream -- a CTA owns a 15 x 15 column of
+// nodes and a chunk of z planes (as many chunks as make one wave of resident
+// CTAs); its 256 threads are the 16 x 16 elements touching the column; node
+// planes stream through a 3-plane shared-memory ring (cp.async, one plane
+// ahead), each layer's element outputs go to shared memory and every owned
+// node gathers its 8 contributions in a fixed order, so results are
+// bit-reproducible without atomics.  Optional fused epilogues form a PCG dot
+// product of the output (one FP64 partial per CTA, finished by the last CTA).
+// 2-D: k_fine_apply -- a CTA owns a 32 x 32 brick of nodes and accumulates
+// element outputs in 4 colour passes (elements of one colour share no node).
+// The element product uses the reflection-sector form KE = H B H
+// (Walsh-Hadamard over corner bits, B block diagonal), ~240 flops per hex8
+// element instead of 1152: GB300's FP64 pipe is narrow, and the FP64
+// residual is the one K.u the mixed-precision solver cannot avoid; the
+// differences are taken exactly first, which keeps the FP32 product accurate
+// for smooth fields.
 #include <algorithm>
 #include <type_traits>
 #include "tg_ops.cuh"

@@ -13,11 +13,14 @@
 //    rho_c * Q_c with Q_c = P_c^T KE P_c precomputed once per problem, a
 //    child touching a fixed DOF contributes the exact masked product;
 //  * deeper levels are Galerkin products of the assembled stencils;
-//  * stencils are stored structure-of-arrays, A[(dir*ndof+ci)*ndof+cj][node],
-//    so one thread per node reads coalesced coefficients;
-//  * the coarsest level (a few hundred to ~2000 DOFs) is inverted once per
-//    design iteration by a blocked Gauss-Jordan in FP64 and applied as one
-//    dense mat-vec per V-cycle.
+//  * stencils are symmetric and half-stored (the centre and the 13 upper
+//    directions in 3-D, 4 in 2-D), structure-of-arrays
+//    A[(dir*ndof+ci)*ndof+cj][node], so consecutive threads read coalesced
+//    coefficients; a lower direction reads the neighbour's upper block
+//    transposed;
+//  * the coarsest level (a few hundred to ~8000 DOFs) is inverted once per
+//    design iteration by the block sweep operator in FP64 (16-wide pivots)
+//    and applied as one dense mat-vec per V-cycle.
 #include <algorithm>
 #include "tg_ops.cuh"
 
