@@ -206,8 +206,8 @@ def _train_network(device, args):
                             "smoothed by the rmin=1.5 filter"}
 
 
-def _run_c5(device, steps=3, warmup=2):
-    """C5: 64 heat plates, nelx = nely uniform in [64, 512] (seed 0), stepped
+def _run_heat_batch(device, steps=3, warmup=2):
+    """Heat-plate batch: 64 heat plates, nelx = nely uniform in [64, 512] (seed 0), stepped
     concurrently (tg_step_many), mixed precision and plain FP64, each to an
     FP64 relative residual of 1e-8; wall time of whole batch iterations."""
     from topoptlab_gb300.batch import heat_plate_batch, heat_plate_sizes
@@ -390,7 +390,7 @@ def run_ours(args, dist, rank, ws, local):
                 "algorithmic_bytes_per_launch": nbytes,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if peaks else "fallback"}
 
-    c5 = None if args.no_c5 else _run_c5(device)
+    heat = None if args.no_heat_batch else _run_heat_batch(device)
 
     if rank != 0:
         return None
@@ -430,8 +430,8 @@ def run_ours(args, dist, rank, ws, local):
         "clocks": clk.summary(),
         "time_breakdown": breakdown,
     }
-    if c5 is not None:
-        line["c5_batch"] = c5
+    if heat is not None:
+        line["heat_plate_batch"] = heat
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(steps=2, warmup=1)
     return line
@@ -524,7 +524,7 @@ def main():
     ap.add_argument("--train-epochs", type=int, default=10)
     ap.add_argument("--no-plain", action="store_true",
                     help="skip the plain FP64 arm (profiling runs only)")
-    ap.add_argument("--no-c5", action="store_true",
+    ap.add_argument("--no-heat-batch", action="store_true",
                     help="skip the batched heat-plate measurement")
     ap.add_argument("--no-breakdown", action="store_true",
                     help="skip the per-family time breakdown (profiling runs only)")

@@ -6,7 +6,7 @@ through ``tg_step_many``, which steps them concurrently from a pool of host
 threads, so small designs overlap on the GPU instead of running one after
 another.  A design's results are those of stepping it alone.
 
-``heat_plate_batch`` builds the survey's C5 workload: stationary heat-plate
+``heat_plate_batch`` builds the 64-plate heat batch workload: stationary heat-plate
 cooling on nelx = nely drawn uniformly from [nmin, nmax] by seed, conductivity
 kmin = 1e-3 .. kmax = 1 (SIMP eps = kmin), penal 3, volfrac 0.4, rmin 1.5,
 uniform source 0.01 per element, T = 0 sink on the middle 10 % of the left

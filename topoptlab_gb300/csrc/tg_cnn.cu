@@ -1,7 +1,7 @@
 // Learned warm start: a small 3-D convolutional encoder-decoder trained on the
 // GPU by the library's own forward / backward / Adam kernels.
 //
-// No counterpart in the reference (new capability of the spec solver).
+// No counterpart in the reference (a new capability of this solver).
 //
 // Grid: the multigrid's level-1 node grid (every second fine node), tensors
 // channels-last FP32, node index ((z*nnx)+x)*nny+y like every other array.
