@@ -91,3 +91,34 @@ def test_padded_grid_trajectory(gpu_lib, precision):
         np.testing.assert_allclose(prob.get(0), ref["x"], atol=1e-8)
     finally:
         prob.close()
+
+
+def test_filter_objects(gpu_lib, golden):
+    """MatrixFilter / HelmholtzFilter objects (filter/matrix_filter.py:9-99,
+    filter/helmholtz_filter.py:16-131): H (x / Hs) for both directions of the
+    matrix filter, TF^T KF^-1 TF v for the PDE filter, volume conserved."""
+    from topoptlab_gb300.filter import HelmholtzFilter, MatrixFilter
+    rng = np.random.default_rng(9)
+    for (nx, ny, nz, rmin) in [(9, 6, None, 1.5), (6, 5, 4, 1.5)]:
+        H, Hs = O.filter_matrix(nx, ny, nz, rmin)
+        x = rng.uniform(0.0, 1.0, (nx * ny * (nz or 1), 1))
+        with MatrixFilter(nelx=nx, nely=ny, nelz=nz, rmin=rmin) as f:
+            assert f.vol_conserv
+            y = f.apply_filter(x)
+            assert y.shape == x.shape
+            ref = np.asarray(H @ (x[:, 0] / Hs))
+            np.testing.assert_allclose(y[:, 0], ref, rtol=0, atol=1e-13)
+            np.testing.assert_allclose(f.apply_filter_dx(x)[:, 0], ref, rtol=0, atol=1e-13)
+            np.testing.assert_allclose(y.sum(), x.sum(), rtol=1e-12)
+    g = golden("helmholtz.npz")
+    for (nx, ny, rmin) in [(7, 5, 2.4), (12, 8, 1.5)]:
+        key = f"{nx}_{ny}_{rmin}"
+        x, dx = g["x_" + key], g["dx_" + key]
+        solve, TF = O.helmholtz_operators(nx, ny, None, rmin)
+        with HelmholtzFilter(nelx=nx, nely=ny, rmin=rmin) as f:
+            assert f.vol_conserv
+            y = f.apply_filter(x)
+            np.testing.assert_allclose(y, g["y_" + key], rtol=0, atol=1e-11)
+            np.testing.assert_allclose(f.apply_filter_dx(y, dx), O.helmholtz_apply(solve, TF, dx),
+                                       rtol=0, atol=1e-11)
+            np.testing.assert_allclose(y.sum(), x.sum(), rtol=1e-10)

@@ -8,5 +8,6 @@ topoptlab.topology_optimization.main.
 """
 from .topology_optimization import main
 from .context import GpuProblem
+from .filter import HelmholtzFilter, MatrixFilter, TOFilter
 
-__all__ = ["main", "GpuProblem"]
+__all__ = ["main", "GpuProblem", "MatrixFilter", "HelmholtzFilter", "TOFilter"]
