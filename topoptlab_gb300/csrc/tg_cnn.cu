@@ -232,12 +232,7 @@ static void conv3_launch(const NG& g, const float* in, const float* W, int cout,
     constexpr size_t smem = TT::smem();
     const dim3 grid((unsigned)cdiv(g.ny, TT::TY), (unsigned)cdiv(g.nx, TT::TX),
                     (unsigned)cdiv(g.nz, TT::TZ) * chunks);
-    static const bool set = [] {   // once per instantiation, thread-safe
-      TG_CUDA(cudaFuncSetAttribute(k_conv3_mma<CIN, NT, SPLIT>,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      return true;
-    }();
-    (void)set;
+    set_smem_limit((const void*)k_conv3_mma<CIN, NT, SPLIT>, (int)smem);
     k_conv3_mma<CIN, NT, SPLIT><<<grid, 128, smem, st>>>(g, in, W, cout, bias, skip, relu, mask,
                                                          out);
   };

@@ -72,6 +72,10 @@ struct Error {
 // count_launches for loops), which also counts launches for the bench's
 // gpu_launches figure.
 void count_launches(int64_t n);
+// Raise a kernel's dynamic shared-memory limit to `bytes` on the current
+// device, once per (kernel, device): the attribute belongs to the device that
+// is current when it is set, and contexts may live on different devices.
+void set_smem_limit(const void* func, int bytes);
 #define TG_CHECK_LAUNCH()                 \
   do {                                    \
     ::tg::count_launches(1);              \

@@ -513,11 +513,7 @@ template <int NDOF, typename T, typename S, int KIND, int MODE, int DOTK = -1>
 static void launch_zstream(const ApplyArgs<T, S>& a, cudaStream_t st) {
   constexpr size_t smem = zs::smem<NDOF, T, KIND>();
   auto kern = k_fine_zstream<NDOF, T, S, KIND, MODE, DOTK>;
-  static const bool attr_set = [&] {   // once per instantiation, thread-safe
-    TG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    return true;
-  }();
-  (void)attr_set;
+  set_smem_limit((const void*)kern, (int)smem);
   const ZsShape sh = zstream_shape(a.g, sizeof(T) == 8);
   const int gy = sh.gy, gx = sh.gx, chunks = sh.chunks, zc = sh.zc;
   if (DOTK >= 0 && sh.ctas() > RED_BLOCKS)
@@ -542,11 +538,7 @@ static void launch_apply(const ApplyArgs<T, S>& a, cudaStream_t st) {
   using TL = Tile<NDIM>;
   constexpr size_t smem = apply_smem_v2<NDIM, NDOF, T, KIND>();
   auto kern = k_fine_apply<NDIM, NDOF, T, S, KIND, MODE>;
-  static const bool attr_set = [&] {   // once per instantiation, thread-safe
-    TG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    return true;
-  }();
-  (void)attr_set;
+  set_smem_limit((const void*)kern, (int)smem);
   dim3 grid((unsigned)cdiv(a.g.nny, TL::Y), (unsigned)cdiv(a.g.nnx, TL::X),
             (unsigned)cdiv(a.g.nnz, TL::Z));
   const int pk = std::is_same<T, double>::value ? PK_FINE_F64

@@ -5,6 +5,8 @@
 // measured with events recorded on the stream that launches it.
 #include <atomic>
 #include <mutex>
+#include <set>
+#include <utility>
 #include <vector>
 #include "tg_common.cuh"
 #include "../../include/topopt_gb300.h"
@@ -13,6 +15,17 @@ namespace tg {
 
 static std::atomic<int64_t> g_launches{0};
 void count_launches(int64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+void set_smem_limit(const void* func, int bytes) {
+  static std::mutex mu;
+  static std::set<std::pair<const void*, int>> done;
+  int dev = 0;
+  TG_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(mu);
+  if (done.count({func, dev})) return;
+  TG_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  done.insert({func, dev});
+}
 int64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
 namespace {
