@@ -19,7 +19,8 @@ Outputs (small .npz files, committed):
   cant3d_12x6x6.npz    3-D cantilever (reference callable), ft=1, 12 iterations
   vtk.npz          what the reference's export_vtk hands to meshio (points,
                    cells, point and cell data) for a 2-D and a 3-D grid, seeded
-                   fields, recorded through a stand-in for meshio.Mesh
+                   fields, and what export_stl hands it for the 2-D grid,
+                   recorded through a stand-in for meshio.Mesh
 """
 import os
 import sys
@@ -209,6 +210,20 @@ def gen_vtk():
         for k, v in m["cell_data"].items():
             d[f"{tag}_cd_{k}"] = np.asarray(v[0])
         d[f"{tag}_in_xPhys"], d[f"{tag}_in_x"], d[f"{tag}_in_u"], d[f"{tag}_in_f"] = xPhys, x, u, f
+        if nz is None:      # export_stl is 2-D (output_designs.py:181-230)
+            # As written it indexes the (nel, 4) cell array with threshold()'s
+            # (nel, 1) mask, which NumPy rejects; recorded with the mask
+            # flattened, its evident intent.
+            orig = OD.threshold
+            OD.threshold = lambda xp, vf: orig(xp, vf)[:, 0]
+            try:
+                OD.export_stl(filename="out", nelx=nx, nely=ny, xPhys=xPhys, volfrac=0.4)
+            finally:
+                OD.threshold = orig
+            m = _MeshRecorder.last
+            d["stl_points"] = m["points"]
+            d["stl_celltype"] = np.array(m["cells"][0][0])
+            d["stl_tris"] = np.asarray(m["cells"][0][1])
     np.savez_compressed(os.path.join(HERE, "vtk.npz"), **d)
 
 

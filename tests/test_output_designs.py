@@ -7,7 +7,7 @@ import os
 import numpy as np
 import pytest
 
-from topoptlab_gb300.output_designs import export_vtk, threshold
+from topoptlab_gb300.output_designs import export_stl, export_vtk, threshold
 
 GOLD = os.path.join(os.path.dirname(__file__), "golden", "vtk.npz")
 
@@ -89,3 +89,21 @@ def test_export_vtk_element_size(tmp_path):
                       xPhys=np.ones((2, 1)), elem_size=np.array([0.5, 2.0]))
     m = _read_legacy_vtk(path)
     assert m["points"][:, 0].max() == 1.0 and m["points"][:, 1].max() == 2.0
+
+
+def test_export_stl_matches_reference_triangles(tmp_path):
+    """The triangles export_stl hands to meshio (output_designs.py:181-230),
+    recorded with the mask flattened, facet by facet and in order."""
+    g = np.load(GOLD)
+    path = export_stl(str(tmp_path / "design"), nelx=4, nely=3, xPhys=g["2d_in_xPhys"],
+                      volfrac=0.4)
+    lines = [ln.split() for ln in open(path)]
+    verts = np.array([[float(v) for v in ln[1:]] for ln in lines if ln and ln[0] == "vertex"])
+    normals = np.array([[float(v) for v in ln[2:]] for ln in lines if ln and ln[0] == "facet"])
+    ref = g["stl_points"][g["stl_tris"]].reshape(-1, 2)
+    assert str(g["stl_celltype"]) == "triangle"
+    assert verts.shape == (ref.shape[0], 3)
+    np.testing.assert_array_equal(verts[:, :2], ref)
+    np.testing.assert_array_equal(verts[:, 2], 0.0)
+    np.testing.assert_allclose(np.abs(normals[:, 2]), 1.0)
+    assert lines[0][0] == "solid" and lines[-1][0] == "endsolid"

@@ -1,6 +1,6 @@
 """Design export for visualisation (e.g. ParaView): legacy-format VTK files of
 the structured quad4 / hex8 grid with the element densities and the nodal
-fields, written without meshio.
+fields, and STL files of the thresholded 2-D design, written without meshio.
 
 Mirrors topoptlab.output_designs (output_designs.py:7-178): the same point
 coordinates (x = ex, y = nely - ey, z = ez; y counted downwards like the
@@ -113,4 +113,31 @@ def export_vtk(filename: str, nelx: int, nely: int, xPhys: np.ndarray,
                 continue
             fh.write(f"SCALARS {name} double 1\nLOOKUP_TABLE default\n")
             np.savetxt(fh, np.asarray(v, dtype=np.float64).reshape(-1), fmt="%.17g")
+    return path
+
+
+def export_stl(filename: str, nelx: int, nely: int, xPhys: np.ndarray, volfrac: float) -> str:
+    """Write ``filename + ".stl"`` (ASCII STL, z = 0): the thresholded 2-D
+    design as two triangles per solid element, (n1+1, n2+1, n2) for every
+    solid element and then (n1+1, n2, n1) for every solid element, over the
+    points of export_vtk (output_designs.py:181-230).  The reference indexes
+    the cells with threshold()'s (nel, 1) mask, which NumPy rejects; the mask
+    is used flattened here.  Facet normals follow the vertex winding."""
+    mask = threshold(xPhys, volfrac)[:, 0] == 1
+    pts = _points(nelx, nely, None)
+    cells = _cells(nelx, nely, None)[mask]
+    tris = np.vstack((cells[:, [0, 1, 2]], cells[:, [0, 2, 3]]))
+    path = filename + ".stl"
+    with open(path, "w") as fh:
+        fh.write("solid topoptlab_gb300\n")
+        for t in tris:
+            v = pts[t]
+            nrm = np.cross(v[1] - v[0], v[2] - v[0])
+            ln = np.linalg.norm(nrm)
+            nrm = nrm / ln if ln > 0 else nrm
+            fh.write("  facet normal {:.9g} {:.9g} {:.9g}\n    outer loop\n".format(*nrm))
+            for p in v:
+                fh.write("      vertex {:.17g} {:.17g} {:.17g}\n".format(*p))
+            fh.write("    endloop\n  endfacet\n")
+        fh.write("endsolid topoptlab_gb300\n")
     return path
