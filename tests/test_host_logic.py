@@ -96,3 +96,24 @@ def test_library_loads_and_exports_every_symbol():
     for name in _declared_symbols():
         assert hasattr(lib, name), name
     assert _lib.load().tg_abi_version() == 3
+
+
+@pytest.mark.parametrize("case", ["nelx0", "ke_shape", "fixed_range", "f_length", "ft", "precision",
+                                  "filter_mode"])
+def test_problem_arguments_rejected_before_device_work(case):
+    """Invalid problem descriptions raise ValueError (TG_EINVAL) before any
+    device is touched (so this runs without a GPU)."""
+    from topoptlab_gb300.context import GpuProblem
+    from topoptlab_gb300.elements import lk_linear_elast_2d
+    KE = lk_linear_elast_2d()
+    f = np.zeros(50)
+    args = {"nelx0": ((0, 4, None, KE, [0], np.zeros(10)), {}),
+            "ke_shape": ((4, 4, None, np.eye(7), [0], f), {}),
+            "fixed_range": ((4, 4, None, KE, [10 ** 6], f), {}),
+            "f_length": ((4, 4, None, KE, [0], np.zeros(7)), {}),
+            "ft": ((4, 4, None, KE, [0], f), {"ft": 5}),
+            "precision": ((4, 4, None, KE, [0], f), {"precision": "fp16"}),
+            "filter_mode": ((4, 4, None, KE, [0], f), {"filter_mode": "no-such-filter"})}[case]
+    pos, kw = args
+    with pytest.raises(ValueError):
+        GpuProblem(*pos, 0.5, 1.5, **kw)

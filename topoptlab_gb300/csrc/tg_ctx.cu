@@ -199,6 +199,12 @@ void ctx_init(Ctx& c, const tg_problem& p) {
   TG_REQUIRE(p.ft >= -1 && p.ft <= 1, "ft must be -1, 0 or 1");
   TG_REQUIRE(p.precision == TG_PREC_FP64 || p.precision == TG_PREC_MIXED, "unknown precision");
   TG_REQUIRE(p.precond == TG_PRECOND_GMG || p.precond == TG_PRECOND_JACOBI, "unknown preconditioner");
+  {   // argument checks that need no device: fixed DOF indices
+    const Grid rg0 = make_grid(p.ndim, p.nnode_dof, p.nelx, p.nely, p.nelz);
+    TG_REQUIRE(p.nfixed >= 0 && (p.nfixed == 0 || p.fixed != nullptr), "fixed DOF list missing");
+    for (int64_t i = 0; i < p.nfixed; ++i)
+      TG_REQUIRE(p.fixed[i] >= 0 && p.fixed[i] < rg0.ndofs(), "fixed DOF index out of range");
+  }
   c.dev = p.device;
   TG_CUDA(cudaSetDevice(c.dev));
   TG_CUDA(cudaStreamCreateWithFlags(&c.st, cudaStreamNonBlocking));
