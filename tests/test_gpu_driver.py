@@ -159,3 +159,32 @@ def test_main_exports_vtk(gpu_lib, tmp_path):
     assert "CELLS 48 240" in txt and "POINTS 65 double" in txt
     for field in ("u0", "f0", "xPhys", "x", "xThresh"):
         assert f" {field} " in txt
+
+
+
+def test_solver_independence(gpu_lib):
+    """tests/test_solver.py:8-59 of the reference: the 10x3 MBB beam gives the
+    scipy-direct compliance (decimal 3) whatever solver and preconditioner
+    names are passed (they all run the GPU multigrid PCG here, to the
+    caller's rtol)."""
+    from topoptlab_gb300 import main
+    from topoptlab_gb300.example_bc import mbb_2d
+    cases_all = [("scipy-direct", None), ("scipy-cg", None), ("scipy-bicg", None),
+                 ("scipy-cgs", "scipy-ilu"), ("scipy-minres", None), ("scipy-lgmres", None),
+                 ("scipy-gmres", "scipy-ilu"), ("scipy-gcrotmk", None), ("scipy-cg", "scipy-ilu"),
+                 ("cvxopt-cholmod", None), ("scipy-cg", "pyamg-adaptive_sa"),
+                 ("scipy-cg", "pyamg-rootnode_solver"), ("scipy-cg", "pyamg-pairwise_solver"),
+                 ("scipy-cg", "pyamg-smoothed_aggregation"), ("topoptlab-cg", None),
+                 ("topoptlab-pcg", "scipy-ilu")]
+    out = dict(OUT)
+    for ft in (0, 1):
+        _, obj_ref = main(nelx=10, nely=3, volfrac=0.5, rmin=2.4, ft=ft, filter_mode="matrix",
+                          optimizer="oc", bcs=mbb_2d, lin_solver_kw={"name": "scipy-direct"},
+                          output_kw=dict(out))
+        cases = cases_all[:1] if ft == 0 else cases_all[1:]
+        for solver, precond in cases:
+            _, obj = main(nelx=10, nely=3, volfrac=0.5, rmin=2.4, ft=ft, filter_mode="matrix",
+                          optimizer="oc", bcs=mbb_2d,
+                          lin_solver_kw={"name": solver, "rtol": 1e-10, "maxiter": 10000},
+                          preconditioner_kw={"name": precond}, output_kw=dict(out))
+            np.testing.assert_almost_equal(obj, obj_ref, decimal=3)

@@ -117,3 +117,23 @@ def test_problem_arguments_rejected_before_device_work(case):
     pos, kw = args
     with pytest.raises(ValueError):
         GpuProblem(*pos, 0.5, 1.5, **kw)
+
+
+# the (solver, preconditioner) pairs of the reference's tests/test_solver.py:8-24
+REFERENCE_SOLVER_CASES = [("scipy-direct", None), ("scipy-cg", None), ("scipy-bicg", None),
+                          ("scipy-cgs", "scipy-ilu"), ("scipy-minres", None),
+                          ("scipy-lgmres", None), ("scipy-gmres", "scipy-ilu"),
+                          ("scipy-gcrotmk", None), ("scipy-cg", "scipy-ilu"),
+                          ("cvxopt-cholmod", None), ("scipy-cg", "pyamg-adaptive_sa"),
+                          ("scipy-cg", "pyamg-rootnode_solver"),
+                          ("scipy-cg", "pyamg-pairwise_solver"),
+                          ("scipy-cg", "pyamg-smoothed_aggregation"), ("topoptlab-cg", None),
+                          ("topoptlab-pcg", "scipy-ilu")]
+
+
+@pytest.mark.parametrize("solver,precond", REFERENCE_SOLVER_CASES)
+def test_reference_solver_names_map(solver, precond):
+    """Every solver / preconditioner name the reference's solver test uses is
+    accepted and runs the GPU multigrid PCG with the caller's tolerance."""
+    o = solver_options({"name": solver, "rtol": 1e-10, "maxiter": 10000}, {"name": precond})
+    assert o["precond"] == "gb300-gmg" and o["rtol"] == 1e-10 and o["maxiter"] == 10000
