@@ -261,7 +261,9 @@ def compliance_sens(xPhys, u, KE, edof, eps=1e-9, penal=3.0):
 # --------------------------------------------------------------------------
 # OC update (optimizer/optimality_criterion.py:9-79)
 # --------------------------------------------------------------------------
-def oc_top88(x, dc, dv, g, move=0.2, l1=0.0, l2=1e9):
+def oc_top88(x, dc, dv, g, move=0.2, l1=0.0, l2=1e9, el_flags=None):
+    """optimizer/optimality_criterion.py:59-79: passive elements (flag 1)
+    set to 0 and active ones (flag 2) to 1 before each volume sum."""
     xnew = np.zeros_like(x)
     gt = g
     nsteps = 0
@@ -269,6 +271,9 @@ def oc_top88(x, dc, dv, g, move=0.2, l1=0.0, l2=1e9):
         lmid = 0.5 * (l2 + l1)
         xnew[:] = np.maximum(0.0, np.maximum(
             x - move, np.minimum(1.0, np.minimum(x + move, x * np.sqrt(-dc / dv / lmid)))))
+        if el_flags is not None:
+            xnew[el_flags == 1] = 0.0
+            xnew[el_flags == 2] = 1.0
         gt = g + np.sum(dv * (xnew - x))
         if gt > 0:
             l1 = lmid
@@ -300,7 +305,7 @@ def solve_direct(K, f, free):
 # the design loop (topology_optimization.py:411-673; OC, ft in {0, 1})
 # --------------------------------------------------------------------------
 def run(nelx, nely, nelz, volfrac, rmin, ft, KE, fixed, f, eps=1e-9, penal=3.0,
-        nouteriter=2000, solve=None, record=(), filter_mode="matrix"):
+        nouteriter=2000, solve=None, record=(), filter_mode="matrix", el_flags=None):
     """Return dict with obj/vol/change per iteration, final x, xPhys, u.
 
     ``solve(K, f, free, u_prev) -> u`` defaults to the direct solve.
@@ -351,7 +356,7 @@ def run(nelx, nely, nelz, volfrac, rmin, ft, KE, fixed, f, eps=1e-9, penal=3.0,
             out["rec"][loop] = dict(xPhys=xPhys.copy(), u=u.copy(), dc=dc.copy(),
                                     dv=dv.copy(), x=x.copy(), g=g)
         xold = x.copy()
-        x, g, nsteps = oc_top88(x, dc, dv, g)
+        x, g, nsteps = oc_top88(x, dc, dv, g, el_flags=el_flags)
         if ft == 1 and filter_mode == "helmholtz":
             xPhys = pde(x)
         elif ft == 1:
@@ -379,6 +384,16 @@ def bc_mbb_2d(nelx, nely):
     fixed = np.union1d(np.arange(0, 2 * (nely + 1), 2), [ndof - 1])
     f = np.zeros(ndof)
     f[1] = -1.0
+    return fixed, f
+
+
+def bc_cantilever_2d(nelx, nely):
+    """example_bc/lin_elast.py:100-139: left wall clamped, downward unit load
+    on the last DOF (the y-DOF of the bottom-right node)."""
+    ndof = 2 * (nelx + 1) * (nely + 1)
+    fixed = np.arange(0, 2 * (nely + 1))
+    f = np.zeros(ndof)
+    f[-1] = -1.0
     return fixed, f
 
 

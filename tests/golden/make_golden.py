@@ -79,6 +79,8 @@ import topoptlab.output_designs as OD  # noqa: E402
 from topoptlab.elements.screenedpoisson_2d import lk_screened_poisson_2d  # noqa: E402
 from topoptlab.elements.screenedpoisson_3d import lk_screened_poisson_3d  # noqa: E402
 from topoptlab.filter.helmholtz_filter import assemble_helmholtz_filter  # noqa: E402
+from topoptlab.geometries import sphere, ellipse  # noqa: E402
+from topoptlab.example_bc.lin_elast import cantilever_2d  # noqa: E402
 from scipy.sparse.linalg import factorized  # noqa: E402
 
 OUT_KW = {"file": None, "display": False, "export": False, "write_log": False,
@@ -257,7 +259,25 @@ def gen_helmholtz():
         print(f"mbb helmholtz ft{ft}", r[1], r[2])
 
 
-GENERATORS = {"vtk": lambda: gen_vtk(), "helmholtz": lambda: gen_helmholtz()}
+def gen_passive():
+    """tests/test_passive.py:8-34 of the reference: the 60x20 cantilever with
+    a passive disc from geometries.sphere, ft=0, OC (golden 221.9720563724),
+    plus the flags of sphere and ellipse for a few shapes."""
+    d = {}
+    for (nx, ny, c, r) in [(60, 20, (60 / 3 - 1, 20 / 2 - 1), 20 / 3), (9, 7, (4.0, 3.0), 2.5)]:
+        d[f"sphere_{nx}_{ny}"] = sphere(nelx=nx, nely=ny, center=c, radius=r)
+    d["ellipse_12_8"] = ellipse(nelx=12, nely=8, center=(5.0, 3.5), ax_half_lengths=(4.0, 2.0),
+                                fill_value=2)
+    np.savez_compressed(os.path.join(HERE, "geometries.npz"), **d)
+    flags = sphere(nelx=60, nely=20, center=(60 / 3 - 1, 20 / 2 - 1), radius=20 / 3)
+    r = run_traced("cant2d_60x20_passive.npz", {0, 1},
+                   nelx=60, nely=20, volfrac=0.5, rmin=2.4, ft=0, bcs=cantilever_2d,
+                   el_flags=flags, filter_mode="matrix")
+    print("cant2d passive", r[1], r[2])
+
+
+GENERATORS = {"vtk": lambda: gen_vtk(), "helmholtz": lambda: gen_helmholtz(),
+              "passive": lambda: gen_passive()}
 
 
 def main():
@@ -268,6 +288,7 @@ def main():
         return
     gen_vtk()
     gen_helmholtz()
+    gen_passive()
     gen_elements()
     gen_filters()
     r = run_traced("mbb2d_60x20.npz", {0, 1, 2, 24, 143},

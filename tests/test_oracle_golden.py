@@ -157,3 +157,29 @@ def test_mbb_helmholtz_trajectory(golden, ft, golden_obj):
     np.testing.assert_allclose(r["obj"], g["obj"], rtol=1e-9)
     np.testing.assert_almost_equal(r["final_obj"], golden_obj, decimal=5)
     np.testing.assert_allclose(r["x"], g["final_x"], atol=1e-8)
+
+
+def test_geometries_match_reference(golden):
+    """geometries.py:6-72: element flags of spheres (discs) and ellipses."""
+    from topoptlab_gb300.geometries import ellipse, sphere
+    g = golden("geometries.npz")
+    np.testing.assert_array_equal(sphere(60, 20, (60 / 3 - 1, 20 / 2 - 1), 20 / 3),
+                                  g["sphere_60_20"])
+    np.testing.assert_array_equal(sphere(9, 7, (4.0, 3.0), 2.5), g["sphere_9_7"])
+    np.testing.assert_array_equal(ellipse(12, 8, (5.0, 3.5), (4.0, 2.0), fill_value=2),
+                                  g["ellipse_12_8"])
+
+
+def test_passive_elements_trajectory(golden):
+    """tests/test_passive.py:8-34 (221.9720563724 at decimal 2): the 60x20
+    cantilever with a passive disc, ft=0 -- the whole reference trajectory."""
+    from topoptlab_gb300.geometries import sphere
+    g = golden("cant2d_60x20_passive.npz")
+    flags = sphere(60, 20, (60 / 3 - 1, 20 / 2 - 1), 20 / 3)
+    fixed, f = O.bc_cantilever_2d(60, 20)
+    r = O.run(60, 20, None, 0.5, 2.4, 0, O.ke_elast(2), fixed, f, el_flags=flags)
+    assert len(r["obj"]) == int(g["n_iter"])
+    np.testing.assert_allclose(r["obj"], g["obj"], rtol=1e-9)
+    np.testing.assert_allclose(r["x"], g["final_x"], atol=1e-8)
+    np.testing.assert_almost_equal(r["final_obj"], 221.9720563724, decimal=2)
+    assert np.all(r["x"][flags == 1] == 0.0)
