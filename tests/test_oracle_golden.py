@@ -183,3 +183,15 @@ def test_passive_elements_trajectory(golden):
     np.testing.assert_allclose(r["x"], g["final_x"], atol=1e-8)
     np.testing.assert_almost_equal(r["final_obj"], 221.9720563724, decimal=2)
     assert np.all(r["x"][flags == 1] == 0.0)
+
+
+def test_wrong_cantilever_bcs_match_reference(golden):
+    """example_bc/lin_elast.py:184-272: the cantilever variants whose left
+    wall leaves the y-DOF of its bottom node free."""
+    from topoptlab_gb300.example_bc import cantilever_2d_twoloads_wrong, cantilever_2d_wrong
+    g = golden("geometries.npz")
+    for name, fn in (("wrong", cantilever_2d_wrong), ("twoloads_wrong", cantilever_2d_twoloads_wrong)):
+        _, f, fixed, free, springs = fn(12, 5, 2 * 13 * 6)
+        np.testing.assert_array_equal(fixed, g[f"bc_cant2d_{name}_fixed"])
+        np.testing.assert_array_equal(f, g[f"bc_cant2d_{name}_f"])
+        assert springs is None and len(free) + len(fixed) == 2 * 13 * 6

@@ -46,6 +46,27 @@ def cantilever_2d_twoloads(nelx, nely, ndof, **kwargs):
     return u, f, fixed, np.setdiff1d(np.arange(ndof), fixed), None
 
 
+def cantilever_2d_wrong(nelx, nely, ndof, **kwargs):
+    """cantilever_2d with the left wall's last DOF (the y-DOF of its bottom
+    node) left free: fixed = 0 .. 2 nely (example_bc/lin_elast.py:230-272)."""
+    f = np.zeros((ndof, 1))
+    u = np.zeros((ndof, 1))
+    fixed = np.arange(0, 2 * nely + 1)
+    f[-1, 0] = -1.0
+    return u, f, fixed, np.setdiff1d(np.arange(ndof), fixed), None
+
+
+def cantilever_2d_twoloads_wrong(nelx, nely, ndof, **kwargs):
+    """cantilever_2d_twoloads with fixed = 0 .. 2 nely
+    (example_bc/lin_elast.py:184-228)."""
+    f = np.zeros((ndof, 2))
+    u = np.zeros((ndof, 2))
+    fixed = np.arange(0, 2 * nely + 1)
+    f[-1, 0] = -1.0
+    f[2 * nelx * (nely + 1) + 1, 1] = 1.0
+    return u, f, fixed, np.setdiff1d(np.arange(ndof), fixed), None
+
+
 def cantilever_3d(nelx, nely, nelz, ndof, force_mode="linear", **kwargs):
     """All DOFs of the x=0 face and the z-DOFs of the z=0 plane fixed; a
     downward y-load on the bottom edge of the x=nelx face, one node per
