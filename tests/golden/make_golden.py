@@ -280,8 +280,27 @@ def gen_passive():
     print("cant2d passive", r[1], r[2])
 
 
+def gen_slow_cantilevers():
+    """The reference's slow compliance cases (tests/test_compliance.py:38-59):
+    cantilever_2d_wrong 160x100 (61.4282510690) and
+    cantilever_2d_twoloads_wrong 150x150 (69.2037375459), ft=0, rmin 6."""
+    r = run_traced("cant2d_wrong_160x100.npz", {0},
+                   nelx=160, nely=100, volfrac=0.4, rmin=6.0, ft=0, bcs=cantilever_2d_wrong,
+                   filter_mode="matrix")
+    print("cant2d wrong", r[1], r[2])
+    r = run_traced("cant2d_twoloads_wrong_150x150.npz", {0},
+                   nelx=150, nely=150, volfrac=0.4, rmin=6.0, ft=0,
+                   bcs=cantilever_2d_twoloads_wrong, filter_mode="matrix")
+    print("cant2d twoloads wrong", r[1], r[2])
+    for name in ("cant2d_wrong_160x100.npz", "cant2d_twoloads_wrong_150x150.npz"):
+        path = os.path.join(HERE, name)
+        d = dict(np.load(path))
+        np.savez_compressed(path, **{k: d[k] for k in ("obj", "g", "final_obj", "final_x",
+                                                        "n_iter")})
+
+
 GENERATORS = {"vtk": lambda: gen_vtk(), "helmholtz": lambda: gen_helmholtz(),
-              "passive": lambda: gen_passive()}
+              "passive": lambda: gen_passive(), "slow": lambda: gen_slow_cantilevers()}
 
 
 def main():
