@@ -299,7 +299,37 @@ def gen_slow_cantilevers():
                                                         "n_iter")})
 
 
+def gen_convolution():
+    """The reference's convolution-mode filter (filter/convolution_filter.py
+    with scipy.ndimage.convolve, as tests/test_filters.py runs it) on seeded
+    fields: the outputs the matrix filter must reproduce."""
+    from functools import partial
+    from scipy.ndimage import convolve
+    from topoptlab.filter.convolution_filter import assemble_convolution_filter
+    from topoptlab.utils import map_eltoimg, map_imgtoel, map_eltovoxel, map_voxeltoel
+    rng = np.random.default_rng(2)
+    d = {}
+    for (nx, ny, nz, rmin) in [(10, 10, None, 2.4), (20, 10, None, 2.4), (10, 20, None, 2.4),
+                               (10, 10, 10, 2.4), (20, 10, 10, 2.4), (10, 20, 10, 2.4),
+                               (9, 6, 5, 1.5)]:
+        ndim = 2 if nz is None else 3
+        if ndim == 2:
+            mp, imp = partial(map_eltoimg, nelx=nx, nely=ny), partial(map_imgtoel, nelx=nx, nely=ny)
+        else:
+            mp = partial(map_eltovoxel, nelx=nx, nely=ny, nelz=nz)
+            imp = partial(map_voxeltoel, nelx=nx, nely=ny, nelz=nz)
+        h, hs = assemble_convolution_filter(nelx=nx, nely=ny, nelz=nz, rmin=rmin, mapping=mp,
+                                            invmapping=imp)
+        n = nx * ny * (nz or 1)
+        x = rng.uniform(0.0, 1.0, (n, 1))
+        y = imp(convolve(mp(x), h, mode="constant", axes=(0, 1, 2)[:ndim], cval=0)) / hs
+        key = f"{nx}_{ny}_{nz}_{rmin}"
+        d["x_" + key], d["y_" + key] = x[:, 0], np.asarray(y).reshape(-1)
+    np.savez_compressed(os.path.join(HERE, "convolution.npz"), **d)
+
+
 GENERATORS = {"vtk": lambda: gen_vtk(), "helmholtz": lambda: gen_helmholtz(),
+              "convolution": lambda: gen_convolution(),
               "passive": lambda: gen_passive(), "slow": lambda: gen_slow_cantilevers()}
 
 
@@ -312,6 +342,7 @@ def main():
     gen_vtk()
     gen_helmholtz()
     gen_passive()
+    gen_convolution()
     gen_elements()
     gen_filters()
     r = run_traced("mbb2d_60x20.npz", {0, 1, 2, 24, 143},
