@@ -328,7 +328,27 @@ def gen_convolution():
     np.savez_compressed(os.path.join(HERE, "convolution.npz"), **d)
 
 
+def gen_stiffness():
+    """The reference's recorded SIMP systems (examples/linsolvers:
+    K[free][:, free] of design iteration 25 and its xPhys, MBB 60x20 and heat
+    plate 40x40): the densities, the matrix diagonal and its product with a
+    seeded vector, enough to pin an assembly of K from the densities."""
+    import scipy.sparse as sp
+    base = os.path.join(REF, "examples", "linsolvers")
+    rng = np.random.default_rng(4)
+    d = {}
+    for tag in ("mbb2d_60x20-2.4-0.5-0_25", "heatplate2d_40x40-1.2-0.4-0_25"):
+        K = sp.load_npz(os.path.join(base, f"stiffness-matrix_{tag}.npz")).tocsr()
+        x = np.loadtxt(os.path.join(base, f"xPhys_{tag}.csv"), delimiter=",").reshape(-1)
+        v = rng.standard_normal(K.shape[0])
+        key = tag.split("-")[0]
+        d[key + "_xPhys"], d[key + "_v"] = x, v
+        d[key + "_Kv"], d[key + "_diag"] = K @ v, K.diagonal()
+    np.savez_compressed(os.path.join(HERE, "stiffness.npz"), **d)
+
+
 GENERATORS = {"vtk": lambda: gen_vtk(), "helmholtz": lambda: gen_helmholtz(),
+              "stiffness": lambda: gen_stiffness(),
               "convolution": lambda: gen_convolution(),
               "passive": lambda: gen_passive(), "slow": lambda: gen_slow_cantilevers()}
 
@@ -343,6 +363,7 @@ def main():
     gen_helmholtz()
     gen_passive()
     gen_convolution()
+    gen_stiffness()
     gen_elements()
     gen_filters()
     r = run_traced("mbb2d_60x20.npz", {0, 1, 2, 24, 143},
