@@ -79,7 +79,7 @@ import topoptlab.output_designs as OD  # noqa: E402
 from topoptlab.elements.screenedpoisson_2d import lk_screened_poisson_2d  # noqa: E402
 from topoptlab.elements.screenedpoisson_3d import lk_screened_poisson_3d  # noqa: E402
 from topoptlab.filter.helmholtz_filter import assemble_helmholtz_filter  # noqa: E402
-from topoptlab.geometries import sphere, ellipse  # noqa: E402
+from topoptlab.geometries import sphere, ellipse, ball, ellipsoid  # noqa: E402
 from topoptlab.example_bc.lin_elast import (cantilever_2d, cantilever_2d_wrong,  # noqa: E402
                                              cantilever_2d_twoloads_wrong)
 from scipy.sparse.linalg import factorized  # noqa: E402
@@ -269,6 +269,9 @@ def gen_passive():
         d[f"sphere_{nx}_{ny}"] = sphere(nelx=nx, nely=ny, center=c, radius=r)
     d["ellipse_12_8"] = ellipse(nelx=12, nely=8, center=(5.0, 3.5), ax_half_lengths=(4.0, 2.0),
                                 fill_value=2)
+    d["ball_8_6_5"] = ball(nelx=8, nely=6, nelz=5, center=(3.5, 2.0, 2.5), radius=2.2)
+    d["ellipsoid_8_6_5"] = ellipsoid(nelx=8, nely=6, nelz=5, center=(3.0, 2.5, 2.0),
+                                     ax_half_lengths=(3.0, 1.5), fill_value=2)
     for name, fn in (("wrong", cantilever_2d_wrong), ("twoloads_wrong", cantilever_2d_twoloads_wrong)):
         u, f, fixed, free, _ = fn(nelx=12, nely=5, ndof=2 * 13 * 6)
         d[f"bc_cant2d_{name}_fixed"], d[f"bc_cant2d_{name}_f"] = fixed, f

@@ -168,6 +168,12 @@ def test_geometries_match_reference(golden):
     np.testing.assert_array_equal(sphere(9, 7, (4.0, 3.0), 2.5), g["sphere_9_7"])
     np.testing.assert_array_equal(ellipse(12, 8, (5.0, 3.5), (4.0, 2.0), fill_value=2),
                                   g["ellipse_12_8"])
+    from topoptlab_gb300.geometries import ball, ellipsoid
+    np.testing.assert_array_equal(ball(8, 6, 5, (3.5, 2.0, 2.5), 2.2), g["ball_8_6_5"])
+    np.testing.assert_array_equal(ellipsoid(8, 6, 5, (3.0, 2.5, 2.0), (3.0, 1.5), fill_value=2),
+                                  g["ellipsoid_8_6_5"])
+    with pytest.raises(ValueError):      # two semi-axes, like the reference
+        ellipsoid(8, 6, 5, (3.0, 2.5, 2.0), (3.0, 1.5, 1.0))
 
 
 def test_passive_elements_trajectory(golden):
