@@ -29,6 +29,7 @@ Solver selection (``lin_solver_kw["name"]``):
 from __future__ import annotations
 
 import warnings
+from cProfile import Profile
 from typing import Callable, Dict, List, Tuple, Union
 
 import numpy as np
@@ -121,6 +122,11 @@ def main(nelx: int, nely: int,
     """Topology optimisation with SIMP and OC on the GPU; see the module doc."""
     check_output_kw(output_kw)
     check_simulation_params(simulation_kw)
+    # host-side profile of the run, as topology_optimization.py:163-165 / 681-683
+    profiler = None
+    if output_kw.get("profile"):
+        profiler = Profile()
+        profiler.enable()
     ndim = 2 if nelz is None else 3
     # ---- options the GPU path implements (everything else: ValueError) ----
     if optimizer != "oc":
@@ -206,4 +212,7 @@ def main(nelx: int, nely: int,
             export(output_kw["file"])
     finally:
         prob.close()
+    if profiler is not None:
+        profiler.disable()
+        profiler.dump_stats(output_kw["file"] + ".prof")
     return x.reshape(-1, 1), obj
