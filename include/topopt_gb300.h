@@ -175,10 +175,11 @@ int32_t tg_oc_raw(int64_t n, const double* x, const double* dc, const double* dv
  * array inside the library sized for TG_NOALLOC_MAX_N design variables; larger
  * n returns TG_EINVAL.  The array is shared by all calls and keeps the last
  * call's contents, so calls that overlap on the GPU race and must be
- * serialised by the caller.  The first call on each device looks up the
- * array's device address; make it before any stream capture.  stream is a
- * cudaStream_t (NULL = legacy default stream).  Errors: message from
- * tg_noalloc_last_error(). */
+ * serialised by the caller.  Every call looks up the array's device address
+ * on the current device and synchronises stream before it returns, so it
+ * must never be called while stream is being captured into a CUDA graph
+ * (refused with TG_EINVAL).  stream is a cudaStream_t (NULL = legacy default
+ * stream).  Errors: message from tg_noalloc_last_error(). */
 #define TG_NOALLOC_MAX_N 2097152
 int32_t tg_oc_noalloc(int64_t n, const double* x, const double* dc, const double* dv, double g,
                       const int8_t* el_flags, double move, double l1, double l2, double* xnew,
@@ -236,6 +237,17 @@ int32_t tg_profile_kernel(int32_t kind);
 /* Kernel launches made by the library (all contexts) and the accumulated
  * device time / launch count of the profiled family; reset != 0 zeroes them. */
 int32_t tg_stats(int32_t reset, int64_t* launches, double* prof_ms, int64_t* prof_launches);
+/* Library-wide switches for tests and tuning (no counterpart in the
+ * reference).  TG_TUNE_STENCIL_SMALL_PAIRS: coarse levels with fewer
+ * (node, DOF) rows than value run the small-grid stencil kernel, the others
+ * the row-plane kernel (default 150000; 0 runs the row-plane kernel on every
+ * level, so tests can compare it with the oracle on small grids).
+ * TG_TUNE_OC_BARRIER_TIMEOUT: value != 0 makes the next OC bisection's grid
+ * barrier wait for one block more than its grid holds, so every block's
+ * bounded wait runs out (seconds) and the call returns TG_ETIMEOUT;
+ * the switch clears itself.  Unknown keys or bad values return TG_EINVAL. */
+enum { TG_TUNE_STENCIL_SMALL_PAIRS = 1, TG_TUNE_OC_BARRIER_TIMEOUT = 2 };
+int32_t tg_tune(int32_t key, int64_t value);
 /* edofMat (elements/bilinear_quadrilateral.py:7-48, trilinear_hexahedron.py:7-58)
  * generated on the device; out has nel*(2^ndim*nnode_dof) int32 entries */
 int32_t tg_edofmat(int32_t ndim, int32_t nelx, int32_t nely, int32_t nelz, int32_t nnode_dof,

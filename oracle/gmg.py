@@ -17,6 +17,12 @@ statement of the multigrid the GPU library builds in their place:
 * V-cycle with zero initial guess on every level, nu damped-Jacobi sweeps
   before and after the coarse correction, exact coarsest solve;
 * PCG exactly as linear_solvers.py:114-134 with ||r||_2 < rtol*||b||_2.
+
+The mixed-precision cycle of the GPU library (FP32 arithmetic, BF16 element
+scale factors in the fine-level smoother, coarse levels built from FP32 scale
+factors, coarsest inverse in FP64) is stated here with exact FP64 arithmetic
+on the same rounded inputs (round_bf16 / round_f32 of simp(x), K_build):
+what remains between the two is the FP32 rounding of the arithmetic.
 """
 from __future__ import annotations
 
@@ -58,8 +64,26 @@ def coarse_fixed_mask(fixed_mask, dims, ndof):
     return m[::2, ::2, :].ravel().copy()
 
 
+def round_bf16(a):
+    """Round FP64 values to the nearest BF16 value (8 significant bits,
+    ties to even), the rounding of a direct FP64 -> BF16 conversion."""
+    a = np.asarray(a, dtype=np.float64)
+    m, e = np.frexp(a)
+    return np.ldexp(np.rint(m * 256.0) / 256.0, e)
+
+
+def round_f32(a):
+    return np.asarray(a, dtype=np.float32).astype(np.float64)
+
+
 class Hierarchy:
-    def __init__(self, K, fixed_mask, dims, ndof, nlevels, omega=0.6, nsmooth=2):
+    """K: the fine-level operator of the smoother and residual.  K_build (if
+    given): the fine operator from which the level-1 Galerkin product is
+    formed instead of K -- the mixed-precision cycle smooths with BF16
+    densities on the fine level but builds the coarse levels from FP32
+    densities."""
+
+    def __init__(self, K, fixed_mask, dims, ndof, nlevels, omega=0.6, nsmooth=2, K_build=None):
         self.omega, self.nsmooth = omega, nsmooth
         free = (~fixed_mask).astype(float)
         M = sp.diags(free)
@@ -68,13 +92,15 @@ class Hierarchy:
         self.P = []
         self.dims = [tuple(dims)]
         d = tuple(dims)
+        Ab = self.A[0] if K_build is None else (M @ K_build @ M).tocsr()
         for _ in range(nlevels - 1):
             P = prolongation(d, ndof)
             cmask = coarse_fixed_mask(self.mask[-1], d, ndof)
             Pt = sp.diags((~self.mask[-1]).astype(float)) @ P @ sp.diags((~cmask).astype(float))
             Pt = Pt.tocsr()
             self.P.append(Pt)
-            self.A.append((Pt.T @ self.A[-1] @ Pt).tocsr())
+            self.A.append((Pt.T @ Ab @ Pt).tocsr())
+            Ab = self.A[-1]
             self.mask.append(cmask)
             d = tuple(x // 2 for x in d)
             self.dims.append(d)

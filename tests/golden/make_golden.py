@@ -6,7 +6,8 @@ level (matplotlib, cvxopt, pyamg, mmapy, meshio) that are not needed on the
 paths used here (scipy-direct solve, OC optimiser, no display, no export), so
 they are replaced by inert stub modules before the import.
 
-Run:  python tests/golden/make_golden.py [/path/to/reference]
+Run:  python tests/golden/make_golden.py /path/to/reference [generator ...]
+      (or set TOPOPTLAB_REFERENCE to the reference checkout and pass no path)
 
 Outputs (small .npz files, committed):
   elements.npz     edofMat (2-D / 3-D, several nnode_dof), KE matrices,
@@ -17,6 +18,10 @@ Outputs (small .npz files, committed):
   heat2d_40x40.npz heat plate 40x40, ft=0, OC (Poisson KE)
   mbb2d_60x20_ft0.npz  MBB beam 60x20 with the sensitivity filter
   cant3d_12x6x6.npz    3-D cantilever (reference callable), ft=1, 12 iterations
+  cant3d_16x8x8.npz, cant3d_32x16x16.npz, cant3d_48x24x24.npz
+                       the 3-D cantilever ladder (20 / 10 / 2 iterations): the
+                       grids on which the multigrid hierarchy is deep; also the
+                       reference's seconds per design iteration on this host
   vtk.npz          what the reference's export_vtk hands to meshio (points,
                    cells, point and cell data) for a 2-D and a 3-D grid, seeded
                    fields, and what export_stl hands it for the 2-D grid,
@@ -29,7 +34,13 @@ import types
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) > 1:
+    REF = sys.argv[1]
+elif os.environ.get("TOPOPTLAB_REFERENCE"):
+    REF = os.environ["TOPOPTLAB_REFERENCE"]
+else:
+    sys.exit("usage: make_golden.py /path/to/reference [generator ...] "
+             "(or set TOPOPTLAB_REFERENCE)")
 
 
 class _Inert:
@@ -350,8 +361,36 @@ def gen_stiffness():
     np.savez_compressed(os.path.join(HERE, "stiffness.npz"), **d)
 
 
-GENERATORS = {"vtk": lambda: gen_vtk(), "helmholtz": lambda: gen_helmholtz(),
-              "stiffness": lambda: gen_stiffness(),
+def gen_ladder():
+    """The 3-D cantilever (reference cantilever_3d callable, volfrac 0.3,
+    rmin 1.5, ft=1, OC, scipy-direct) on the grids 16x8x8 (20 iterations),
+    32x16x16 (10) and 48x24x24 (2): compliance per iteration, the final
+    design, the last iteration's xPhys and filtered dc (up to 32x16x16) and
+    u (16x8x8), plus the reference's wall time per design iteration."""
+    import time
+    for (nx, ny, nz, nit) in [(16, 8, 8, 20), (32, 16, 16, 10), (48, 24, 24, 2)]:
+        name = f"cant3d_{nx}x{ny}x{nz}.npz"
+        t0 = time.perf_counter()
+        r = run_traced(name, {nit - 1}, nelx=nx, nely=ny, nelz=nz, volfrac=0.3, rmin=1.5,
+                       ft=1, bcs=cantilever_3d, nouteriter=nit)
+        sec = (time.perf_counter() - t0) / nit
+        path = os.path.join(HERE, name)
+        d = dict(np.load(path))
+        keep = {k: d[k] for k in ("obj", "g", "final_x", "final_obj", "n_iter")}
+        last = nit - 1
+        # the last iteration's fields where they keep the fixture small
+        if nx <= 32:
+            keep["xPhys_last"] = d[f"xPhys_{last}"]
+            keep["dc_last"] = d[f"dc_{last}"]
+        if nx <= 16:
+            keep["u_last"] = d[f"u_{last}"]
+        keep["seconds_per_iteration"] = np.array(sec)
+        np.savez_compressed(path, **keep)
+        print("ladder", nx, ny, nz, r[1], f"{sec:.2f} s/iteration")
+
+
+GENERATORS = {"ladder": lambda: gen_ladder(), "vtk": lambda: gen_vtk(),
+              "helmholtz": lambda: gen_helmholtz(), "stiffness": lambda: gen_stiffness(),
               "convolution": lambda: gen_convolution(),
               "passive": lambda: gen_passive(), "slow": lambda: gen_slow_cantilevers()}
 
@@ -383,6 +422,7 @@ def main():
                    nelx=12, nely=6, nelz=6, volfrac=0.3, rmin=1.5, ft=1,
                    bcs=cantilever_3d, nouteriter=12)
     print("cant3d", r[1], r[2])
+    gen_ladder()
 
 
 if __name__ == "__main__":

@@ -184,6 +184,33 @@ def test_oc_passive_active_flags(gpu_lib):
     np.testing.assert_allclose(xnew, xr, atol=1e-13)
 
 
+def test_oc_barrier_wait_runs_out(gpu_lib):
+    """The one in-kernel wait of the library (the grid barrier of the
+    one-launch OC bisection) is bounded.  tg_tune makes the next bisection's
+    barrier wait for one block more than the grid holds -- an arrival that
+    never comes -- so every block polls until its limit (about a second),
+    records the error flag and leaves; the call returns TG_ETIMEOUT
+    (RuntimeError).  The next call on the same device runs normally."""
+    import time
+    from topoptlab_gb300 import _lib
+    from topoptlab_gb300.optimizer import oc_top88
+    lib = _lib.load()
+    rng = np.random.default_rng(9)
+    n = 5000
+    x = rng.uniform(0.1, 0.9, n)
+    dc = -rng.uniform(0.1, 2.0, n)
+    dv = np.ones(n)
+    assert lib.tg_tune(_lib.TG_TUNE_OC_BARRIER_TIMEOUT, 1) == _lib.TG_OK
+    t0 = time.perf_counter()
+    with pytest.raises(RuntimeError, match="timed out"):
+        oc_top88(x, 0.5, dc, dv, 0.0)
+    assert time.perf_counter() - t0 < 60.0
+    xnew, gt = oc_top88(x, 0.5, dc, dv, 0.0)
+    xo, gto, _ = O.oc_top88(x, dc, dv, 0.0)
+    np.testing.assert_allclose(xnew, xo, atol=1e-13)
+    assert lib.tg_tune(99, 0) == _lib.TG_EINVAL
+
+
 @pytest.mark.parametrize("nelx,nely,nelz,kind", [(12, 8, None, "elast"), (16, 8, None, "poisson"),
                                                  (8, 4, 4, "elast"), (16, 8, 8, "elast")])
 def test_coarse_operators_are_galerkin(gpu_lib, nelx, nely, nelz, kind):

@@ -101,6 +101,16 @@ def test_cantilever_3d_trajectory(golden):
     np.testing.assert_allclose(r["x"], g["final_x"], atol=1e-8)
 
 
+def test_cantilever_3d_ladder_16x8x8(golden):
+    """The first rung of the 3-D ladder (20 iterations of the reference run):
+    the oracle's trajectory and final design within 1e-9 / 1e-8."""
+    g = golden("cant3d_16x8x8.npz")
+    fixed, f = O.bc_cantilever_3d(16, 8, 8)
+    r = O.run(16, 8, 8, 0.3, 1.5, 1, O.ke_elast(3), fixed, f, nouteriter=20)
+    np.testing.assert_allclose(r["obj"], g["obj"], rtol=1e-9)
+    np.testing.assert_allclose(r["x"], g["final_x"], atol=1e-8)
+
+
 def test_oc_step_golden(golden):
     g = golden("mbb2d_60x20.npz")
     for k in (0, 1, 24):
@@ -271,3 +281,18 @@ def test_assembly_matches_reference_stiffness(golden, case):
     np.testing.assert_allclose(Kff.diagonal(), g[case + "_diag"], rtol=0, atol=1e-14 * scale)
     np.testing.assert_allclose(Kff @ g[case + "_v"], g[case + "_Kv"], rtol=0,
                                atol=1e-13 * np.abs(g[case + "_Kv"]).max())
+
+
+def test_oracle_bf16_rounding_is_round_to_nearest_even():
+    """oracle.gmg.round_bf16 (the rounding of the mixed-precision cycle's
+    BF16 scale factors) against torch's BF16 conversion on FP32-exact values,
+    including exact ties, which must go to the even neighbour."""
+    torch = pytest.importorskip("torch")
+    from oracle import gmg as G
+    rng = np.random.default_rng(3)
+    v = rng.uniform(1e-9, 1.0, 20000).astype(np.float32).astype(np.float64)
+    ties = (1.0 + (2 * np.arange(0, 64) + 1) * 2.0 ** -8) * 0.25   # halfway between BF16 values
+    ties = ties.astype(np.float32).astype(np.float64)
+    for a in (v, ties, np.array([0.0, 1e-9, 1.0, 0.12 ** 3])):
+        ref = torch.from_numpy(a.astype(np.float32)).to(torch.bfloat16).double().numpy()
+        np.testing.assert_array_equal(G.round_bf16(a), ref)

@@ -18,6 +18,7 @@ TG_OK, TG_EINVAL, TG_ENOTCONV, TG_ETIMEOUT, TG_ENAN, TG_ECUDA, TG_ENOMEM = range
 TG_PREC_FP64, TG_PREC_MIXED = 0, 1
 TG_PRECOND_GMG, TG_PRECOND_JACOBI = 0, 1
 (TG_FIELD_X, TG_FIELD_XPHYS, TG_FIELD_U, TG_FIELD_DC, TG_FIELD_DV, TG_FIELD_F) = range(6)
+TG_TUNE_STENCIL_SMALL_PAIRS, TG_TUNE_OC_BARRIER_TIMEOUT = 1, 2
 
 _dp = C.POINTER(C.c_double)
 _i64p = C.POINTER(C.c_int64)
@@ -99,6 +100,7 @@ SIGNATURES = {
     "tg_timer": (C.c_int32, [C.c_void_p, C.c_int32, _dp]),
     "tg_profile_kernel": (C.c_int32, [C.c_int32]),
     "tg_stats": (C.c_int32, [C.c_int32, _i64p, _dp, _i64p]),
+    "tg_tune": (C.c_int32, [C.c_int32, C.c_int64]),
     "tg_edofmat": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _i32p,
                                C.c_int32]),
 }

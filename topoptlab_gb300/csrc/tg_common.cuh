@@ -130,6 +130,12 @@ void prof_capture_begin(ProfCapture* pc);   // prof_begin/end now record into pc
 void prof_capture_end();
 void prof_collect(const ProfCapture& pc);   // after a replay has completed
 int64_t launch_count();       // kernels launched so far
+// Library-wide switches set through tg_tune (include/topopt_gb300.h):
+// the (row, node) pair count below which coarse stencils use the small-grid
+// kernel, and a one-shot request that the next OC bisection's grid barrier
+// wait for one block more than its grid holds (its bounded wait runs out).
+int64_t tune_stencil_small_pairs();
+bool tune_take_oc_barrier_timeout();
 
 #define TG_REQUIRE(cond, msg)                                                \
   do {                                                                       \

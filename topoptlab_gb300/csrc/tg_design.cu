@@ -162,7 +162,9 @@ void reduce_partials(const double* part, int nb, double* out, bool is_max, cudaS
 // ---------------------------------------------------------------------------
 // OC bisection (optimizer/optimality_criterion.py:59-79)
 // ---------------------------------------------------------------------------
-__global__ void k_oc_init(OCState* s, double g, double l1, double l2) {
+// bar_count0 = 0; a value no arrival sequence of the grid reaches (a test of
+// the bounded barrier wait) keeps every block waiting until its limit
+__global__ void k_oc_init(OCState* s, double g, double l1, double l2, unsigned int bar_count0) {
   s->l1 = l1;
   s->l2 = l2;
   s->g = g;
@@ -173,7 +175,7 @@ __global__ void k_oc_init(OCState* s, double g, double l1, double l2) {
   s->sc = 1.0 / sqrt(s->lmid);
   s->sc_last = s->sc;
   s->ticket = 0;
-  s->bar.count = 0;
+  s->bar.count = bar_count0;
   s->bar.err = 0;
 }
 
@@ -293,7 +295,7 @@ void oc_begin(int64_t n, const double* x, const double* dc, const double* dv, co
               double l2) {
   prof_begin(PK_OC, s);
   k_oc_prep<<<(unsigned)cdiv(n, RED_THREADS), RED_THREADS, 0, s>>>(n, x, dc, dv, flags, move, sc);
-  k_oc_init<<<1, 1, 0, s>>>(st, g, l1, l2);
+  k_oc_init<<<1, 1, 0, s>>>(st, g, l1, l2, tune_take_oc_barrier_timeout() ? 0x40000000u : 0u);
   prof_end(PK_OC, s);
   count_launches(1);
   TG_CHECK_LAUNCH();

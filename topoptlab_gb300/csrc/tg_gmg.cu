@@ -200,7 +200,7 @@ template <typename T>
 void stencil_apply(const Grid& g, const T* A, const T* u, T* y, const T* b, const T* dinv,
                    double omega, int mode, cudaStream_t st) {
   const int64_t pairs = g.nnodes() * g.ndof;
-  if (pairs < 150000) {
+  if (pairs < tune_stencil_small_pairs()) {
     const unsigned blocks = (unsigned)cdiv(pairs, SMALL_PAIRS);
 #define TG_SS(ND, NF)                                                                          \
   if (mode == AM_Y) k_stencil_small<ND, NF, T, AM_Y><<<blocks, 3 * SMALL_PAIRS, 0, st>>>(g, A, u, y, b, dinv, (T)omega); \

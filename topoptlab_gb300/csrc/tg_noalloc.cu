@@ -17,10 +17,13 @@
 //    everything that must start at zero (the reduction ticket) is cleared by
 //    each call, but calls that overlap on the GPU (two streams, two host
 //    threads) race on the array and must be serialised by the caller;
-//  * the device address of the array is looked up with cudaGetSymbolAddress on
-//    the first call on each device (with that device current); make that first
-//    call before any stream capture.
-#include <mutex>
+//  * every call looks up the array's device address with cudaGetSymbolAddress
+//    on the current device (cheap once the module is loaded, and never stale
+//    after a device reset);
+//  * every call copies the bisection state back and synchronises the stream,
+//    so it must not be called while that stream is being captured into a CUDA
+//    graph: such a call is refused with TG_EINVAL before any work.
+#include <string>
 #include "tg_design.cuh"
 #include "../../include/topopt_gb300.h"
 
@@ -36,9 +39,6 @@ struct NoAllocScratch {
 
 static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
 
-constexpr int kMaxDevices = 256;
-std::mutex g_mu;
-NoAllocScratch* g_dev_addr[kMaxDevices] = {};
 thread_local std::string g_err;
 
 int32_t fail(int32_t code, const std::string& msg) {
@@ -61,23 +61,21 @@ int32_t tg_oc_noalloc(int64_t n, const double* x, const double* dc, const double
     return fail(TG_EINVAL, "tg_oc_noalloc: n = " + std::to_string(n) +
                                " exceeds the static scratch limit of " + std::to_string(kMaxN) +
                                " design variables");
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return fail(TG_ECUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
-  if (dev < 0 || dev >= kMaxDevices) return fail(TG_EINVAL, "tg_oc_noalloc: device ordinal out of range");
-  NoAllocScratch* s = nullptr;
-  {
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_dev_addr[dev]) {
-      void* p = nullptr;
-      e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-      if (e != cudaSuccess || !p)
-        return fail(TG_ECUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-      g_dev_addr[dev] = static_cast<NoAllocScratch*>(p);
-    }
-    s = g_dev_addr[dev];
-  }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  cudaError_t e = cudaStreamIsCapturing(st, &cap);
+  if (e != cudaSuccess)
+    return fail(TG_ECUDA, std::string("cudaStreamIsCapturing: ") + cudaGetErrorString(e));
+  if (cap != cudaStreamCaptureStatusNone)
+    return fail(TG_EINVAL, "tg_oc_noalloc: the stream is being captured; this call synchronises "
+                           "the stream and cannot be part of a CUDA graph");
+  // the host-side name of the array is not its device address: look the
+  // address up on the current device
+  void* p = nullptr;
+  e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p)
+    return fail(TG_ECUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+  NoAllocScratch* s = static_cast<NoAllocScratch*>(p);
   try {
     tg::OCState h{};
     // one scratch array: the move-limit bounds are recomputed from x each step

@@ -62,6 +62,13 @@ void drain_locked() {
 int prof_kind() { return g_kind; }
 
 namespace {
+std::atomic<int64_t> g_small_pairs{150000};
+std::atomic<int> g_oc_timeout{0};
+}  // namespace
+int64_t tune_stencil_small_pairs() { return g_small_pairs.load(std::memory_order_relaxed); }
+bool tune_take_oc_barrier_timeout() { return g_oc_timeout.exchange(0) != 0; }
+
+namespace {
 thread_local ProfCapture* g_cap = nullptr;
 }
 
@@ -159,3 +166,17 @@ int32_t tg_stats(int32_t reset, int64_t* launches, double* prof_ms, int64_t* pro
 }
 
 }  // extern "C"
+
+extern "C" int32_t tg_tune(int32_t key, int64_t value) {
+  switch (key) {
+    case TG_TUNE_STENCIL_SMALL_PAIRS:
+      if (value < 0) return TG_EINVAL;
+      tg::g_small_pairs.store(value);
+      return TG_OK;
+    case TG_TUNE_OC_BARRIER_TIMEOUT:
+      tg::g_oc_timeout.store(value != 0 ? 1 : 0);
+      return TG_OK;
+    default:
+      return TG_EINVAL;
+  }
+}
