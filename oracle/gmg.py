@@ -81,9 +81,11 @@ class Hierarchy:
     given): the fine operator from which the level-1 Galerkin product is
     formed instead of K -- the mixed-precision cycle smooths with BF16
     densities on the fine level but builds the coarse levels from FP32
-    densities."""
+    densities.  coarse_ops (if given): the operators of levels 1, 2, ...
+    themselves, used in place of the Galerkin products."""
 
-    def __init__(self, K, fixed_mask, dims, ndof, nlevels, omega=0.6, nsmooth=2, K_build=None):
+    def __init__(self, K, fixed_mask, dims, ndof, nlevels, omega=0.6, nsmooth=2, K_build=None,
+                 coarse_ops=None):
         self.omega, self.nsmooth = omega, nsmooth
         free = (~fixed_mask).astype(float)
         M = sp.diags(free)
@@ -104,6 +106,11 @@ class Hierarchy:
             self.mask.append(cmask)
             d = tuple(x // 2 for x in d)
             self.dims.append(d)
+        if coarse_ops is not None:
+            # given operators of levels 1.. (e.g. ones built elsewhere in lower
+            # precision) replace the Galerkin products
+            for lvl, A in enumerate(coarse_ops, start=1):
+                self.A[lvl] = sp.csr_matrix(A)
         self.Dinv = []
         for A, m in zip(self.A, self.mask):
             dg = A.diagonal().copy()
@@ -151,3 +158,36 @@ def pcg(A, b, precond, x0=None, rtol=1e-8, maxiter=10000):
         r -= alpha * q
         rho_prev = rho
     return x, -1
+
+
+def stencil_matrix(S, dims, ndof):
+    """Sparse matrix of an assembled 27-point (9-point in 2-D) block stencil in
+    the GPU library's expanded layout S[dir][ci][cj][node] (dir: dy fastest,
+    then dx, then dz, each in {-1, 0, 1}), on the node grid of a level with
+    element counts dims."""
+    ndim = len(dims)
+    nn = [d + 1 for d in dims]
+    nnodes = int(np.prod(nn))
+    nd = 27 if ndim == 3 else 9
+    S = np.asarray(S).reshape(nd, ndof, ndof, nnodes)
+    n = np.arange(nnodes)
+    Y = n % nn[1]
+    X = (n // nn[1]) % nn[0]
+    Z = n // (nn[0] * nn[1]) if ndim == 3 else np.zeros_like(n)
+    rows, cols, vals = [], [], []
+    for d in range(nd):
+        dy, dx = d % 3 - 1, (d // 3) % 3 - 1
+        dz = d // 9 - 1 if ndim == 3 else 0
+        ok = (X + dx >= 0) & (X + dx < nn[0]) & (Y + dy >= 0) & (Y + dy < nn[1])
+        if ndim == 3:
+            ok &= (Z + dz >= 0) & (Z + dz < nn[2])
+        src = n[ok]
+        m = ((Z[ok] + dz) * nn[0] + X[ok] + dx) * nn[1] + Y[ok] + dy
+        for ci in range(ndof):
+            for cj in range(ndof):
+                rows.append(src * ndof + ci)
+                cols.append(m * ndof + cj)
+                vals.append(S[d, ci, cj, ok])
+    rows, cols, vals = np.concatenate(rows), np.concatenate(cols), np.concatenate(vals)
+    keep = vals != 0.0
+    return sp.csr_matrix((vals[keep], (rows[keep], cols[keep])), shape=(nnodes * ndof,) * 2)

@@ -8,11 +8,20 @@ grids the oracle handles in seconds, with deep hierarchies (4 levels at
 32x16x16).
 
 The mixed-precision V-cycle (FP32 arithmetic, BF16 scale factors in the
-fine-level smoother, coarse levels built from FP32 scale factors, FP64
-coarsest inverse) is compared with the oracle cycle evaluated exactly on
-the same rounded scale factors (oracle.gmg.round_bf16 / round_f32): what
-separates them is the FP32 rounding of the arithmetic, bounded by the
-tolerance 2e-4 of the largest entry (FP64 cycles: 1e-10)."""
+fine-level smoother, coarse levels built in FP32 from FP32 scale factors,
+FP64 coarsest inverse) is checked in two parts:
+  * every FP32 coarse stencil against the exact Galerkin operator of the
+    FP32-rounded scale factors (oracle.gmg.round_f32), within 1e-5 of the
+    largest coefficient (FP32 summation of the products);
+  * the cycle against the oracle cycle evaluated exactly on the GPU's own
+    coarse stencils and the BF16-rounded fine operator
+    (oracle.gmg.round_bf16), within 1e-5 of the largest entry: what remains
+    is the FP32 rounding of the sweeps and transfers.
+The cycle against the fully exact oracle is looser than either part on
+ill-conditioned coarse problems: on the 64x32 MBB beam (coarsest condition
+number ~4e3) the FP32 construction error of the coarse operators moves the
+coarse correction by ~4e-4 of the largest entry, on the 3-D cantilevers by
+~1e-6.  FP64 cycles match the exact oracle within 1e-10."""
 import numpy as np
 import pytest
 
@@ -62,14 +71,14 @@ def _case(nelx, nely, nelz, kind, nlevels, precision, seed):
     return prob, KE, edof, x, b, mask, dims, nnd, ndof
 
 
-def _oracle_cycle(KE, edof, x, mask, dims, nnd, ndof, nlevels, mixed):
+def _oracle_cycle(KE, edof, x, mask, dims, nnd, ndof, nlevels, mixed, coarse_ops=None):
     s = O.simp(x)
     if not mixed:
         K = O.assemble(KE, edof, s, ndof)
         return G.Hierarchy(K, mask, dims, nnd, nlevels)
     K16 = O.assemble(KE, edof, G.round_bf16(s), ndof)
     K32 = O.assemble(KE, edof, G.round_f32(s), ndof)
-    return G.Hierarchy(K16, mask, dims, nnd, nlevels, K_build=K32)
+    return G.Hierarchy(K16, mask, dims, nnd, nlevels, K_build=K32, coarse_ops=coarse_ops)
 
 
 def _run(grid, precision, seed):
@@ -79,10 +88,21 @@ def _run(grid, precision, seed):
     try:
         assert prob.levels()[0] == nlevels
         z = prob.vcycle(x, b, precision=precision)
+        ops = None
+        if precision == "mixed":
+            ops = [G.stencil_matrix(prob.coarse_stencil(x, lvl), [d // 2 ** lvl for d in dims], nnd)
+                   for lvl in range(1, nlevels)]
     finally:
         prob.close()
     h = _oracle_cycle(KE, edof, x, mask, dims, nnd, ndof, nlevels, precision == "mixed")
-    return z, h.vcycle(b)
+    if ops is None:
+        return z, h.vcycle(b)
+    for lvl, A in enumerate(ops, start=1):
+        Ar = h.A[lvl]
+        err = abs(A - Ar).max()
+        assert err <= 1e-5 * abs(Ar).max(), (lvl, err / abs(Ar).max())
+    hg = _oracle_cycle(KE, edof, x, mask, dims, nnd, ndof, nlevels, True, coarse_ops=ops)
+    return z, hg.vcycle(b)
 
 
 @pytest.mark.parametrize("grid", GRIDS)
@@ -94,10 +114,10 @@ def test_row_plane_stencil_vcycle_fp64(row_plane_kernel, grid):
 @pytest.mark.parametrize("grid", GRIDS)
 def test_row_plane_stencil_vcycle_mixed(row_plane_kernel, grid):
     z, zr = _run(grid, "mixed", 22)
-    np.testing.assert_allclose(z, zr, rtol=0, atol=2e-4 * np.abs(zr).max())
+    np.testing.assert_allclose(z, zr, rtol=0, atol=1e-5 * np.abs(zr).max())
 
 
 @pytest.mark.parametrize("grid", GRIDS)
 def test_small_grid_stencil_vcycle_mixed(gpu_lib, grid):
     z, zr = _run(grid, "mixed", 23)
-    np.testing.assert_allclose(z, zr, rtol=0, atol=2e-4 * np.abs(zr).max())
+    np.testing.assert_allclose(z, zr, rtol=0, atol=1e-5 * np.abs(zr).max())

@@ -296,3 +296,28 @@ def test_oracle_bf16_rounding_is_round_to_nearest_even():
     for a in (v, ties, np.array([0.0, 1e-9, 1.0, 0.12 ** 3])):
         ref = torch.from_numpy(a.astype(np.float32)).to(torch.bfloat16).double().numpy()
         np.testing.assert_array_equal(G.round_bf16(a), ref)
+
+
+def test_oracle_stencil_matrix_layout():
+    """oracle.gmg.stencil_matrix (the oracle's reading of the GPU library's
+    expanded stencil layout) against a direct loop over nodes and directions."""
+    rng = np.random.default_rng(0)
+    for dims, nnd in [((4, 2, 2), 3), ((6, 4), 2), ((4, 4), 1)]:
+        nn = [d + 1 for d in dims]
+        nnodes = int(np.prod(nn))
+        nd = 27 if len(dims) == 3 else 9
+        S = rng.standard_normal((nd, nnd, nnd, nnodes))
+        A = G.stencil_matrix(S, dims, nnd).toarray()
+        Ar = np.zeros_like(A)
+        for n in range(nnodes):
+            Y, X = n % nn[1], (n // nn[1]) % nn[0]
+            Z = n // (nn[0] * nn[1]) if len(dims) == 3 else 0
+            for d in range(nd):
+                dy, dx = d % 3 - 1, (d // 3) % 3 - 1
+                dz = d // 9 - 1 if len(dims) == 3 else 0
+                if not (0 <= X + dx < nn[0] and 0 <= Y + dy < nn[1]
+                        and (len(dims) == 2 or 0 <= Z + dz < nn[2])):
+                    continue
+                m = ((Z + dz) * nn[0] + X + dx) * nn[1] + Y + dy
+                Ar[n * nnd:(n + 1) * nnd, m * nnd:(m + 1) * nnd] = S[d, :, :, n]
+        np.testing.assert_array_equal(A, Ar)
