@@ -145,7 +145,7 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def _problem(precision, device, size=None):
+def _problem(precision, device, size=None, volfrac=None):
     size = size or SIZE
     from topoptlab_gb300.context import GpuProblem
     from topoptlab_gb300.elements import lk_linear_elast_3d
@@ -153,7 +153,7 @@ def _problem(precision, device, size=None):
     nx, ny, nz = size
     ndof = 3 * (nx + 1) * (ny + 1) * (nz + 1)
     _, f, fixed, _, _ = cantilever_3d(nx, ny, nz, ndof)
-    return GpuProblem(nx, ny, nz, lk_linear_elast_3d(), fixed, f[:, 0], VOLFRAC, RMIN, ft=1,
+    return GpuProblem(nx, ny, nz, lk_linear_elast_3d(), fixed, f[:, 0], volfrac or VOLFRAC, RMIN, ft=1,
                       penal=PENAL, precision=precision, rtol=1e-8, device=device)
 
 
@@ -192,34 +192,52 @@ def _fine_bytes(kind, size=None):
     raise ValueError(kind)
 
 
+# uniform-start runs of the same cantilever at other volume fractions than
+# the timed one: training data of the benchmark family that never contains
+# the timed trajectory itself
+TRAIN_VOLFRACS = (0.10, 0.14)
+
+
 def _train_network(device, args):
     """Train the warm-start network on solver-generated pairs: an optimisation
     run of the same cantilever started from seeded random densities uniform in
-    [0.05, 1] smoothed once by the rmin=1.5 filter, one (features, displacement
-    change) pair per design iteration, then Adam at lr 1e-3."""
+    [0.05, 1] smoothed once by the rmin=1.5 filter (--train-iters design
+    iterations), plus uniform-start runs at volume fractions 0.10 and 0.14
+    (--train-uniform iterations each); one (features, displacement change)
+    pair per design iteration, then Adam at lr 1e-3."""
     from topoptlab_gb300 import _lib
     from topoptlab_gb300.learned import LearnedWarmStart
     if args.train_iters <= 0:
         return None, {"trained": False}
-    gen = _problem("mixed", device)
-    rng = np.random.default_rng(0)
-    x = rng.uniform(0.05, 1.0, gen.nel)
-    xs = gen.filter(x, 0)                      # (H x) / Hs
-    gen.set(_lib.TG_FIELD_X, xs)
-    gen.set(_lib.TG_FIELD_XPHYS, gen.filter(xs, 0))
-    net = LearnedWarmStart(gen, capacity=args.train_iters, seed=0)
+    owner = _problem("mixed", device)
+    npairs = args.train_iters + len(TRAIN_VOLFRACS) * max(args.train_uniform, 0)
+    net = LearnedWarmStart(owner, capacity=npairs, seed=0)
     try:
+        gen = _problem("mixed", device)
+        rng = np.random.default_rng(0)
+        x = rng.uniform(0.05, 1.0, gen.nel)
+        xs = gen.filter(x, 0)                      # (H x) / Hs
+        gen.set(_lib.TG_FIELD_X, xs)
+        gen.set(_lib.TG_FIELD_XPHYS, gen.filter(xs, 0))
         for _ in range(args.train_iters):
-            net.record_step()
+            net.record_step(gen)
+        gen.close()
+        for vf in TRAIN_VOLFRACS if args.train_uniform > 0 else ():
+            gen = _problem("mixed", device, volfrac=vf)
+            for _ in range(args.train_uniform):
+                net.record_step(gen)
+            gen.close()
         loss = net.train(epochs=args.train_epochs, lr=1e-3, seed=0)
         params = net.params()
     finally:
         net.close()
-        gen.close()
-    return params, {"trained": True, "pairs": args.train_iters, "epochs": args.train_epochs,
+        owner.close()
+    return params, {"trained": True, "pairs": npairs, "epochs": args.train_epochs,
                     "final_loss": loss, "optimizer": "Adam lr 1e-3",
-                    "data": "design iterations 1..N from seeded random densities U[0.05,1] "
-                            "smoothed by the rmin=1.5 filter"}
+                    "data": f"{args.train_iters} design iterations from seeded random densities "
+                            f"U[0.05,1] smoothed by the rmin=1.5 filter, and {args.train_uniform} "
+                            f"from uniform starts at each volume fraction {TRAIN_VOLFRACS} "
+                            f"(the timed trajectory, volume fraction {VOLFRAC}, is not in it)"}
 
 
 def _run_heat_batch(device, steps=3, warmup=2):
@@ -453,7 +471,8 @@ def run_ours(args, dist, rank, ws, local):
                                "FP64 relative residual 1e-8",
                    "solver": "mixed-precision GMG-PCG (FP32 V-cycle, BF16 smoother densities, "
                              "FP64 refinement), 5 levels, 2 damped-Jacobi sweeps omega 0.6, "
-                             "learned warm start (3-level 16/32/64 conv encoder-decoder, FP32)",
+                             "learned warm start (3-level 16/32/64 conv encoder-decoder, FP32, "
+                             "on its own stream beside the hierarchy build)",
                    "learned_warm_start": train_info,
                    "design_iterations_timed": f"{args.warmup + 1}..{args.warmup + args.steps}",
                    "l2": "working set > L2 (126 MB); no flush",
@@ -468,6 +487,8 @@ def run_ours(args, dist, rank, ws, local):
         "learned_mixed": {"pcg_iters_per_step": mean("pcg_iters", steps_info[:args.steps]),
                           "refinements_per_step": mean("refinements", steps_info[:args.steps]),
                           "fallbacks": int(sum(s.fallback for s in steps_info[:args.steps])),
+                          "warm_start_residual_ratio_mean": mean("warm_ratio",
+                                                                 steps_info[:args.steps]),
                           "max_rel_res": max(s.rel_res for s in steps_info),
                           "solve_ms_per_step": mean("t_solve_ms", steps_info[:args.steps])},
         "mixed_without_network": {"value": value_nolearn,
@@ -603,6 +624,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--train-iters", type=int, default=200,
                     help="design iterations recorded to train the warm-start network")
+    ap.add_argument("--train-uniform", type=int, default=40,
+                    help="design iterations recorded from each uniform-start training run")
     ap.add_argument("--train-epochs", type=int, default=10)
     ap.add_argument("--no-plain", action="store_true",
                     help="skip the plain FP64 arm (profiling runs only)")

@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define TG_ABI_VERSION 3
+#define TG_ABI_VERSION 4
 
 enum {
   TG_OK = 0,
@@ -38,6 +38,7 @@ enum {
 };
 
 enum { TG_PREC_FP64 = 0, TG_PREC_MIXED = 1 };
+enum { TG_LEARNED_WARM_START = 1, TG_LEARNED_COARSE_CORRECTION = 2 };
 enum { TG_PRECOND_GMG = 0, TG_PRECOND_JACOBI = 1 };
 enum {
   TG_FIELD_X = 0,      /* design variables x            (nel)  */
@@ -70,7 +71,12 @@ typedef struct tg_problem {
   double rtol;           /* FP64 relative residual target (default 1e-8) */
   int32_t maxiter;       /* PCG iteration cap (default 2000) */
   double inner_rtol;     /* mixed precision: FP32 inner solve target (1e-4) */
-  int32_t learned;       /* 1: learned warm start (requires tg_cnn_* setup) */
+  int32_t learned;       /* bit mask, used once a trained network is attached
+                            (tg_cnn_attach): TG_LEARNED_WARM_START = the
+                            network's warm start, TG_LEARNED_COARSE_CORRECTION
+                            = its vector as the deflation vector of the mixed
+                            solver's FP32 PCG; 0 = the warm start alone once a
+                            network is attached */
   int32_t device;        /* CUDA device ordinal */
   int32_t nload;         /* load cases (columns of bcs()'s f, topology_optimization.py:
                             463-500): f holds nload vectors of ndof one after another;
@@ -97,6 +103,8 @@ typedef struct tg_iter_out {
   int32_t nlevels;       /* multigrid levels used */
   double t_solve_ms;     /* device time of the linear solve */
   double t_step_ms;      /* host wall time of the whole step */
+  double warm_ratio;     /* learned warm start: FP64 residual norm of the learned
+                            start over the plain start's (u_prev); 0 without one */
 } tg_iter_out;
 
 typedef struct tg_solve_info {
@@ -195,25 +203,41 @@ int32_t tg_coarse_stencil(tg_ctx* ctx, const double* xPhys, int32_t level, doubl
 /* Learned warm start (no counterpart in the reference: new capability of the
  * GB300 solver).  A 3-level 3-D convolutional encoder-decoder (16/32/64
  * channels, FP32) on the context's multigrid level-1 node grid predicts a
- * level-1 displacement correction from the filtered density, the previous
- * displacement and its residual; the warm start is u_prev + P(correction).
- * tg_step keeps u_prev whenever the candidate's residual is not smaller
- * (tg_iter_out.fallback = 1).  Training runs on the GPU with the library's
- * own forward / backward / Adam kernels. */
+ * level-1 displacement correction y from the filtered density, the previous
+ * displacement and the residual of the previous displacement restricted to
+ * the level-1 grid.  w = P y (prolongated to the fine grid) gives the warm
+ * start, the energy-optimal combination c1 u_prev + c2 w, and optionally
+ * (TG_LEARNED_COARSE_CORRECTION) the deflation vector of the mixed solver's
+ * FP32 PCG, a coarse-grid correction by one extra basis vector.  After the
+ * first cycle of the solve, tg_step compares the residual with the plain
+ * warm start's (u_prev); when it is not below, the step falls back to plain
+ * PCG from u_prev (tg_iter_out.fallback = 1).  The network runs on its own
+ * CUDA stream, overlapping the build of the multigrid hierarchy.  Training
+ * runs on the GPU with the library's own forward / backward / Adam kernels. */
 typedef struct tg_cnn tg_cnn;
 /* network for ctx (3-D elasticity, >= 2 multigrid levels); capacity = number
  * of training samples to hold; seed = weight initialisation */
 int32_t tg_cnn_create(tg_ctx* ctx, int32_t capacity, uint64_t seed, tg_cnn** out);
 void tg_cnn_destroy(tg_cnn* cnn);
-/* use cnn for the warm starts of ctx's tg_step (NULL detaches) */
+/* use cnn for the warm starts (and coarse-grid corrections) of ctx's tg_step
+ * (NULL detaches); the parts used are tg_problem.learned's bits, the warm
+ * start alone when it was 0 */
 int32_t tg_cnn_attach(tg_ctx* ctx, tg_cnn* cnn);
-/* record one training pair around a tg_step: begin (features of the current
- * design and displacement) before the step, end (target = new - previous
- * displacement) after it */
+/* record one training pair around a tg_step of ctx: begin (features of the
+ * current design and displacement) before the step, end (target = new -
+ * previous displacement) after it; ctx is the network's own context or any
+ * mixed-precision context on the same device with the same grids (runs of
+ * other volume fractions or start designs) */
 int32_t tg_cnn_record_begin(tg_cnn* cnn, tg_ctx* ctx);
 int32_t tg_cnn_record_end(tg_cnn* cnn, tg_ctx* ctx);
 /* Adam (lr, beta 0.9 / 0.999) over the recorded pairs; final mean loss */
 int32_t tg_cnn_train(tg_cnn* cnn, int32_t epochs, double lr, uint64_t seed, double* final_loss);
+/* Adam (lr, beta 0.9 / 0.999, continuing the network's optimiser state) over
+ * n caller-provided pairs: host features x0s [n][nodes][7] and targets
+ * [n][nodes][3], one step per pair, pairs in a seeded shuffled order per
+ * epoch; final mean loss */
+int32_t tg_cnn_fit(tg_cnn* cnn, int32_t n, const float* x0s, const float* targets, int32_t epochs,
+                   double lr, uint64_t seed, double* final_loss);
 /* parameter count, level-1 grid (nx, ny, nz), recorded samples */
 int32_t tg_cnn_info(tg_cnn* cnn, int64_t* nparams, int32_t* grid_dims, int32_t* nsamples);
 /* copy the flat parameter vector out (set = 0) or in (set = 1) */

@@ -81,3 +81,21 @@ def loss_and_grad(params, x0, target, grid):
     loss = ((y - t) ** 2).mean()
     loss.backward()
     return float(loss), p.grad.numpy().copy(), from_torch(y)
+
+
+def adam_steps(params, grads, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8):
+    """Parameters after len(grads) Adam steps from params with zero moments
+    (Kingma & Ba, bias-corrected), in FP32 like the network's optimiser:
+    m = b1 m + (1-b1) g, v = b2 v + (1-b2) g^2,
+    w -= lr (m / (1-b1^t)) / (sqrt(v / (1-b2^t)) + eps)."""
+    f = np.float32
+    w = np.asarray(params, dtype=f).copy()
+    m = np.zeros_like(w)
+    v = np.zeros_like(w)
+    for t, g in enumerate(grads, start=1):
+        g = np.asarray(g, dtype=f)
+        m = f(b1) * m + f(1 - b1) * g
+        v = f(b2) * v + f(1 - b2) * g * g
+        c1, c2 = f(1 - b1 ** t), f(1 - b2 ** t)
+        w = w - f(lr) * (m / c1) / (np.sqrt(v / c2) + f(eps))
+    return w

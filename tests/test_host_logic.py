@@ -69,6 +69,32 @@ def test_main_rejects_unsupported_options(kw):
              output_kw={"file": None, "display": False, "export": False, "write_log": False}, **kw)
 
 
+def test_learned_options_parse_and_refuse_without_parameters(tmp_path):
+    """preconditioner_kw["learned"]: parameters (array, .npy path or a dict
+    with a mode) pass through; True without parameters, or a network on a
+    problem it does not serve, raises ValueError before any device work."""
+    from topoptlab_gb300.topology_optimization import learned_network
+    from topoptlab_gb300.context import learned_mask
+    assert learned_network(False) == (None, 0)
+    p, mode = learned_network(np.arange(5.0))
+    assert p.dtype == np.float32 and p.size == 5 and mode == "warm_start"
+    np.save(tmp_path / "w.npy", np.ones(7, dtype=np.float32))
+    p, mode = learned_network({"params": str(tmp_path / "w.npy"), "mode": "both"})
+    assert p.size == 7 and mode == "both"
+    assert [learned_mask(v) for v in (False, True, "warm_start", "coarse_correction", 3)] == \
+        [0, 3, 1, 2, 3]
+    with pytest.raises(ValueError):
+        learned_mask("no-such-mode")
+    out = {"file": None, "display": False, "export": False, "write_log": False}
+    with pytest.raises(ValueError, match="trained network parameters"):
+        main(nelx=4, nely=2, nelz=2, volfrac=0.5, rmin=1.5, optimizer="oc", output_kw=out,
+             preconditioner_kw={"name": "gb300-gmg", "precision": "mixed", "learned": True})
+    with pytest.raises(ValueError, match="3-D problem"):
+        main(nelx=4, nely=2, volfrac=0.5, rmin=1.5, optimizer="oc", output_kw=out,
+             preconditioner_kw={"name": "gb300-gmg", "precision": "mixed",
+                                "learned": np.ones(3)})
+
+
 def test_main_helmholtz_3d_not_implemented():
     """assemble_helmholtz_filter raises NotImplementedError for 3-D grids
     (filter/helmholtz_filter.py:180); the drop-in does the same."""
@@ -95,7 +121,7 @@ def test_library_loads_and_exports_every_symbol():
     lib = ctypes.CDLL(path)
     for name in _declared_symbols():
         assert hasattr(lib, name), name
-    assert _lib.load().tg_abi_version() == 3
+    assert _lib.load().tg_abi_version() == 4
 
 
 @pytest.mark.parametrize("case", ["nelx0", "ke_shape", "fixed_range", "f_length", "ft", "precision",

@@ -48,7 +48,7 @@ class TgIterOut(C.Structure):
         ("rel_res", C.c_double),
         ("pcg_iters", C.c_int32), ("vcycles", C.c_int32), ("refinements", C.c_int32),
         ("oc_steps", C.c_int32), ("fallback", C.c_int32), ("nlevels", C.c_int32),
-        ("t_solve_ms", C.c_double), ("t_step_ms", C.c_double),
+        ("t_solve_ms", C.c_double), ("t_step_ms", C.c_double), ("warm_ratio", C.c_double),
     ]
 
 
@@ -88,6 +88,8 @@ SIGNATURES = {
     "tg_cnn_record_begin": (C.c_int32, [C.c_void_p, C.c_void_p]),
     "tg_cnn_record_end": (C.c_int32, [C.c_void_p, C.c_void_p]),
     "tg_cnn_train": (C.c_int32, [C.c_void_p, C.c_int32, C.c_double, C.c_uint64, _dp]),
+    "tg_cnn_fit": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float),
+                               C.c_int32, C.c_double, C.c_uint64, _dp]),
     "tg_cnn_info": (C.c_int32, [C.c_void_p, _i64p, _i32p, _i32p]),
     "tg_cnn_params": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(C.c_float), C.c_int64]),
     "tg_cnn_eval": (C.c_int32, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float),

@@ -27,6 +27,28 @@ class IterResult:
     nlevels: int
     t_solve_ms: float
     t_step_ms: float
+    warm_ratio: float
+
+
+# parts of a learned network a problem uses once one is attached
+# (tg_problem.learned bits: 1 warm start, 2 coarse-grid correction)
+LEARNED_MODES = {"warm_start": 1, "coarse_correction": 2, "both": 3}
+
+
+def learned_mask(learned) -> int:
+    """False / 0: none chosen (attaching a network then enables the warm
+    start); True or "both": 3; "warm_start": 1; "coarse_correction": 2; or
+    the bits themselves."""
+    if isinstance(learned, str):
+        if learned not in LEARNED_MODES:
+            raise ValueError(f"Unknown learned mode: {learned}")
+        return LEARNED_MODES[learned]
+    if isinstance(learned, (bool, np.bool_)):
+        return 3 if learned else 0
+    v = int(learned)
+    if v < 0 or v > 3:
+        raise ValueError(f"Unknown learned mode: {learned}")
+    return v
 
 
 class GpuProblem:
@@ -84,7 +106,7 @@ class GpuProblem:
         p.precision = PRECISIONS[precision]
         p.nlevels, p.nsmooth, p.omega = nlevels, nsmooth, omega
         p.rtol, p.maxiter, p.inner_rtol = rtol, maxiter, inner_rtol
-        p.learned = int(bool(learned))
+        p.learned = learned_mask(learned)
         p.device = device
         p.nload = self.nload
         if filter_mode == "helmholtz":

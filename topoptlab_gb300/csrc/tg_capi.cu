@@ -472,14 +472,26 @@ int32_t tg_cnn_attach(tg_ctx* ctx, tg_cnn* cnn) {
   return guarded(ctx, [&] {
     TG_REQUIRE(!cnn || cnn->owner == ctx, "the network belongs to another context");
     ctx->c.cnn = cnn ? cnn->net : nullptr;
-    ctx->c.learned = cnn ? 1 : 0;
+    if (cnn && (ctx->c.learned & (TG_LEARNED_WARM_START | TG_LEARNED_COARSE_CORRECTION)) == 0)
+      ctx->c.learned = TG_LEARNED_WARM_START;
   });
+}
+
+// training pairs may come from any context on the same device with the
+// network's grids (e.g. runs of other volume fractions or start designs)
+static void require_same_grids(const tg_cnn* cnn, const tg_ctx* ctx) {
+  const tg::Ctx& a = cnn->owner->c;
+  const tg::Ctx& b = ctx->c;
+  TG_REQUIRE(a.dev == b.dev && a.g.nex == b.g.nex && a.g.ney == b.g.ney && a.g.nez == b.g.nez &&
+                 a.g.ndof == b.g.ndof && b.L >= 2 && b.lv[1]->g.nnx == a.lv[1]->g.nnx &&
+                 b.lv[1]->g.nny == a.lv[1]->g.nny && b.lv[1]->g.nnz == a.lv[1]->g.nnz,
+             "the context's grids differ from the network's");
 }
 
 int32_t tg_cnn_record_begin(tg_cnn* cnn, tg_ctx* ctx) {
   if (!cnn || !ctx) return TG_EINVAL;
   return guarded(ctx, [&] {
-    TG_REQUIRE(cnn->owner == ctx, "the network belongs to another context");
+    require_same_grids(cnn, ctx);
     cnn->net->record_begin(ctx->c);
   });
 }
@@ -487,7 +499,7 @@ int32_t tg_cnn_record_begin(tg_cnn* cnn, tg_ctx* ctx) {
 int32_t tg_cnn_record_end(tg_cnn* cnn, tg_ctx* ctx) {
   if (!cnn || !ctx) return TG_EINVAL;
   return guarded(ctx, [&] {
-    TG_REQUIRE(cnn->owner == ctx, "the network belongs to another context");
+    require_same_grids(cnn, ctx);
     cnn->net->record_end(ctx->c);
   });
 }
@@ -496,6 +508,15 @@ int32_t tg_cnn_train(tg_cnn* cnn, int32_t epochs, double lr, uint64_t seed, doub
   if (!cnn || epochs < 1) return TG_EINVAL;
   return guarded(cnn->owner, [&] {
     const double l = cnn->net->train(epochs, (float)lr, seed);
+    if (final_loss) *final_loss = l;
+  });
+}
+
+int32_t tg_cnn_fit(tg_cnn* cnn, int32_t n, const float* x0s, const float* targets, int32_t epochs,
+                   double lr, uint64_t seed, double* final_loss) {
+  if (!cnn || n < 1 || !x0s || !targets || epochs < 1) return TG_EINVAL;
+  return guarded(cnn->owner, [&] {
+    const double l = cnn->net->fit(n, x0s, targets, epochs, (float)lr, seed);
     if (final_loss) *final_loss = l;
   });
 }

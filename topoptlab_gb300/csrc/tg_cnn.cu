@@ -478,10 +478,12 @@ static unsigned nb(int64_t n) { return (unsigned)cdiv(n, 256); }
 // ---------------------------------------------------------------------------
 // features and targets from the solver state
 // ---------------------------------------------------------------------------
-// x0[I] = (density at fine node 2I, u(2I)/s_u, r(2I)/s_r) with the density
-// averaged over the fine elements touching the node
+// x0[I] = (density at fine node 2I, u(2I)/s_u, (P^T r)(I)/s_r) with the
+// density averaged over the fine elements touching the node and P^T r the
+// residual restricted to the level-1 grid (a smooth coarse picture of the
+// rough fine residual), s_r its norm
 __global__ void k_features(Grid gf, NG g1, const double* __restrict__ xPhys,
-                           const double* __restrict__ u, const float* __restrict__ r,
+                           const double* __restrict__ u, const float* __restrict__ rc,
                            const PCGState* su, const PCGState* sr, float* __restrict__ x0) {
   const int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (I >= g1.n()) return;
@@ -502,7 +504,7 @@ __global__ void k_features(Grid gf, NG g1, const double* __restrict__ xPhys,
   o[0] = (float)(dsum / cnt);
   for (int c = 0; c < 3; ++c) {
     o[1 + c] = (float)u[fn * 3 + c] * iu;
-    o[4 + c] = r[fn * 3 + c] * ir;
+    o[4 + c] = rc[I * 3 + c] * ir;
   }
 }
 // target t[I] = (u_new(2I) - u_prev(2I)) / s_u
@@ -570,10 +572,28 @@ Cnn::Cnn(Ctx& c, int capacity, uint64_t seed) : ctx(&c) {
   uprev.alloc(c.g.ndofs());
   corr.alloc(g1.ndofs());
   r32a.alloc(c.g.ndofs());
-  su.alloc(1); sr.alloc(1); su.zero(c.st); sr.zero(c.st);
+  w32.alloc(c.g.ndofs());
+  w32.zero(c.st);
+  aw32.alloc(c.g.ndofs());
+  aw32.zero(c.st);
+  rc32.alloc(g1.ndofs());
+  su.alloc(1); sr.alloc(1); src.alloc(1); su.zero(c.st); sr.zero(c.st); src.zero(c.st);
   gal.alloc(6); gal.zero(c.st);
   wsb.alloc(4); wsb.zero(c.st);
+  rpart.alloc(RED_BLOCKS);
+  TG_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+  TG_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+  TG_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
   TG_CUDA(cudaStreamSynchronize(c.st));
+}
+
+Cnn::~Cnn() {
+  if (side) {
+    cudaStreamSynchronize(side);
+    cudaStreamDestroy(side);
+  }
+  if (ev_fork) cudaEventDestroy(ev_fork);
+  if (ev_join) cudaEventDestroy(ev_join);
 }
 
 void Cnn::forward(cudaStream_t st, bool split) {
@@ -682,12 +702,16 @@ static void residual32(Ctx& c, const double* u, float* out) {
 
 void Cnn::features(Ctx& c, const double* u_prev) {
   const int64_t n = c.g.ndofs();
+  const Level& l1 = *c.lv[1];
   residual32(c, u_prev, r32a);
   pcg_reset(su, c.st);
-  dot<double, double>(n, u_prev, u_prev, c.part, su, DOT_RR, c.st);
+  dot<double, double>(n, u_prev, u_prev, rpart, su, DOT_RR, c.st);
   pcg_reset(sr, c.st);
-  dot<float, float>(n, r32a.p, r32a.p, c.part, sr, DOT_RR, c.st);
-  k_features<<<nb(A.n()), 256, 0, c.st>>>(c.g, A, c.xPhys, u_prev, r32a, su, sr, x0);
+  dot<float, float>(n, r32a.p, r32a.p, rpart, sr, DOT_RR, c.st);   // the plain start's residual
+  restrict_<float>(c.g, l1.g, l1.fix, r32a, rc32, c.st);
+  pcg_reset(src, c.st);
+  dot<float, float>(l1.g.ndofs(), rc32.p, rc32.p, rpart, src, DOT_RR, c.st);
+  k_features<<<nb(A.n()), 256, 0, c.st>>>(c.g, A, c.xPhys, u_prev, rc32, su, src, x0);
   TG_CHECK_LAUNCH();
 }
 
@@ -731,6 +755,36 @@ double Cnn::train(int epochs, float lr_, uint64_t seed) {
       adam_step(st);
     }
     if (e == epochs - 1) last = sum / nsamples;
+  }
+  TG_CUDA(cudaStreamSynchronize(st));
+  trained = true;
+  return last;
+}
+
+double Cnn::fit(int n, const float* x0s, const float* targets, int epochs, float lr_,
+                uint64_t seed) {
+  TG_REQUIRE(n > 0 && x0s && targets, "tg_cnn_fit: no pairs");
+  lr = lr_;
+  cudaStream_t st = ctx->st;
+  std::mt19937_64 rng(seed);
+  std::vector<int> order(n);
+  const int64_t na = A.n();
+  double last = 0.0;
+  for (int e = 0; e < epochs; ++e) {
+    for (int i = 0; i < n; ++i) order[i] = i;
+    std::shuffle(order.begin(), order.end(), rng);
+    double sum = 0.0;
+    for (int i = 0; i < n; ++i) {
+      const int s = order[i];
+      TG_CUDA(cudaMemcpyAsync(x0.p, x0s + (int64_t)s * na * 7, sizeof(float) * na * 7,
+                              cudaMemcpyHostToDevice, st));
+      TG_CUDA(cudaMemcpyAsync(tgt.p, targets + (int64_t)s * na * 3, sizeof(float) * na * 3,
+                              cudaMemcpyHostToDevice, st));
+      forward(st);
+      sum += backward(st, e == epochs - 1);
+      adam_step(st);
+    }
+    if (e == epochs - 1) last = sum / n;
   }
   TG_CUDA(cudaStreamSynchronize(st));
   trained = true;
@@ -799,94 +853,75 @@ __global__ void __launch_bounds__(RED_THREADS) k_dot5(int64_t n, const float* __
 }
 
 
-// Warm start for the current design.  The network's level-1 correction is
-// prolongated to the fine grid (v2 = P d) and combined with the previous
-// displacement (v1) by the energy-optimal (Galerkin) 2x2 solve
-//   [v_i^T K v_j] c = [v_i^T f],   u0 = c1 v1 + c2 v2,
-// with the products in FP32; u0 replaces u_prev only when its FP32 residual
-// is smaller.  Returns 1 on fallback.
-// The 2x2 Galerkin solve on the device: ws = {c1, c2, valid, accepted}
-__global__ void k_ws_solve(const PCGState* gal, double* ws) {
+// The 2x2 Galerkin solve on the device: ws = {c1, c2, valid}; with
+// `correction` also the deflation scalar pcg->wawinv = 1 / (w^T K w) (0 when
+// the products are not usable)
+__global__ void k_ws_solve(const PCGState* gal, double* ws, PCGState* pcg, int correction) {
   const double g11 = gal[0].bb, g12 = gal[1].bb, g22 = gal[2].bb, f1 = gal[3].bb, f2 = gal[4].bb;
   const double det = g11 * g22 - g12 * g12;
   const bool ok = isfinite(det) && det > 1e-12 * fabs(g11 * g22) && g11 > 0 && g22 > 0;
   ws[0] = ok ? (f1 * g22 - f2 * g12) / det : 0.0;
   ws[1] = ok ? (f2 * g11 - f1 * g12) / det : 0.0;
   ws[2] = ok ? 1.0 : 0.0;
-  ws[3] = 0.0;
+  pcg->wawinv = (correction && isfinite(g22) && g22 > 0.0) ? 1.0 / g22 : 0.0;
+  pcg->wr = pcg->wz = 0.0;
 }
-// ||f - c1 K v1 - c2 K v2||^2 from the products already formed (FP32 vectors,
-// FP64 block and grid sums); the last block accepts the candidate when the
-// solve was valid and this residual is below the previous displacement's
-// (sr.rr), writing the decision to ws[3] and to *accepted
-__global__ void __launch_bounds__(RED_THREADS) k_ws_check(int64_t n, const float* __restrict__ f,
-                                                         const float* __restrict__ kv1,
-                                                         const float* __restrict__ kv2,
-                                                         double* ws, const PCGState* sr,
-                                                         double* part, PCGState* tk,
-                                                         double* accepted) {
-  __shared__ double sh[32];
-  __shared__ int last;
-  const float c1 = (float)ws[0], c2 = (float)ws[1];
-  float acc = 0.f;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const float r = f[i] - c1 * kv1[i] - c2 * kv2[i];
-    acc = fmaf(r, r, acc);
-  }
-  const double bs = block_sum((double)acc, sh);
-  if (threadIdx.x == 0) {
-    part[blockIdx.x] = bs;
-    __threadfence();
-    last = (atomicAdd(&tk->ticket, 1u) == gridDim.x - 1);
-  }
-  __syncthreads();
-  if (!last) return;
-  __threadfence();
-  const double tot = sum_partials(part, (int)gridDim.x, sh);
-  if (threadIdx.x == 0) {
-    const double acc_ok = (ws[2] != 0.0 && isfinite(tot) && tot < sr->rr) ? 1.0 : 0.0;
-    ws[3] = acc_ok;
-    *accepted = acc_ok;
-    tk->ticket = 0;
-  }
-}
-// u <- c1 u + c2 v2 when accepted
+// u <- c1 u + c2 v2 when the 2x2 solve was usable
 __global__ void k_ws_apply(int64_t n, const double* ws, double* u, const double* v2) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i < n && ws[3] != 0.0) u[i] = ws[0] * u[i] + ws[1] * v2[i];
+  if (i < n && ws[2] != 0.0) u[i] = ws[0] * u[i] + ws[1] * v2[i];
 }
 
-// Warm start for the current design.  The network's level-1 correction is
-// prolongated to the fine grid (v2 = P d) and combined with the previous
-// displacement (v1) by the energy-optimal (Galerkin) 2x2 solve
-//   [v_i^T K v_j] c = [v_i^T f],   u0 = c1 v1 + c2 v2,
-// with the products in FP32; u0 replaces u_prev only when its FP32 residual
-// f - c1 K v1 - c2 K v2 is smaller than u_prev's (the fallback rule).  All on
-// the device: the decision (1 = accepted) lands in *accepted.
-void Cnn::warm_start(Ctx& c, double* accepted) {
-  const int64_t n = c.g.ndofs();
-  double* v2 = c.z2.p;
-  features(c, c.u);            // p32 = u_prev, z32 = f, r32a = f - K u_prev
-  forward(c.st, false);        // TF32 inference
-  k_correction<<<nb(c.lv[1]->g.ndofs()), 256, 0, c.st>>>(c.lv[1]->g.ndofs(), y, su, corr);
-  TG_CHECK_LAUNCH();
-  TG_CUDA(cudaMemsetAsync(v2, 0, sizeof(double) * n, c.st));
-  prolong_add<double>(c.g, c.lv[1]->g, c.op.fix, corr, v2, c.st);
-  // d32 = v2, q32 = K v1, r32 = K v2
-  d2f(n, v2, c.d32, c.st);
-  fine_apply<float, float>(c.op, c.s32, c.p32, c.q32, nullptr, nullptr, 0.0, AM_Y, c.st);
-  fine_apply<float, float>(c.op, c.s32, c.d32, c.r32, nullptr, nullptr, 0.0, AM_Y, c.st);
-  const unsigned b5 = std::min<unsigned>(red_blocks(n), (unsigned)DOT5_BLOCKS);
-  k_dot5<<<b5, RED_THREADS, 0, c.st>>>(n, c.p32, c.d32, c.q32, c.r32, c.z32, c.part, gal.p);
-  TG_CHECK_LAUNCH();
-  k_ws_solve<<<1, 1, 0, c.st>>>(gal.p, wsb.p);
-  TG_CHECK_LAUNCH();
-  k_ws_check<<<red_blocks(n), RED_THREADS, 0, c.st>>>(n, c.z32, c.q32, c.r32, wsb.p, sr.p, c.part,
-                                                      gal.p + 5, accepted);
-  TG_CHECK_LAUNCH();
-  k_ws_apply<<<nb(n), 256, 0, c.st>>>(n, wsb.p, c.u.p, v2);
-  TG_CHECK_LAUNCH();
+void Cnn::warm_start_join(Ctx& c) { TG_CUDA(cudaStreamWaitEvent(c.st, ev_join, 0)); }
+
+// Warm start and coarse-grid correction for the current design.  The
+// network's level-1 correction is prolongated to the fine grid (w = P y) and
+// combined with the previous displacement (v1 = u_prev) by the energy-optimal
+// (Galerkin) 2x2 solve
+//   [v_i^T K v_j] c = [v_i^T f],   u0 = c1 v1 + c2 w,
+// with the products in FP32 (the energy error of u0 is at most u_prev's).
+// With `correction` the same w deflates the FP32 PCG of the solve (deflated
+// CG: each pass starts with its residual made orthogonal to w, every search
+// direction is made K-orthogonal to w), a coarse-grid correction by one
+// extra basis vector.  Whether the learned start is kept is decided after the
+// first cycle of the solve, against the plain warm start's residual (solve()).
+void Cnn::warm_start(Ctx& c, bool combine, bool correction) {
+  TG_CUDA(cudaEventRecord(ev_fork, c.st));
+  TG_CUDA(cudaStreamWaitEvent(side, ev_fork, 0));
+  // everything below is enqueued on the side stream (the helpers take the
+  // context's stream member); the context's own stream comes back at the end
+  struct Swap {
+    Ctx& c;
+    cudaStream_t keep;
+    Swap(Ctx& c_, cudaStream_t s) : c(c_), keep(c_.st) { c.st = s; }
+    ~Swap() { c.st = keep; }
+  } swap(c, side);
+  {
+    ProfScope ps(PK_LEARNED, c.st);
+    const int64_t n = c.g.ndofs();
+    double* v2 = c.z2.p;
+    features(c, c.u);            // p32 = u_prev, z32 = f, r32a = f - K u_prev, sr.rr = |r32a|^2
+    forward(c.st, false);        // TF32 inference
+    k_correction<<<nb(c.lv[1]->g.ndofs()), 256, 0, c.st>>>(c.lv[1]->g.ndofs(), y, su, corr);
+    TG_CHECK_LAUNCH();
+    TG_CUDA(cudaMemsetAsync(v2, 0, sizeof(double) * n, c.st));
+    prolong_add<double>(c.g, c.lv[1]->g, c.op.fix, corr, v2, c.st);
+    TG_CUDA(cudaMemcpyAsync(uprev.p, c.u.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, c.st));
+    // w32 = w, q32 = K v1, aw32 = K w
+    d2f(n, v2, w32, c.st);
+    fine_apply<float, float>(c.op, c.s32, c.p32, c.q32, nullptr, nullptr, 0.0, AM_Y, c.st);
+    fine_apply<float, float>(c.op, c.s32, w32, aw32, nullptr, nullptr, 0.0, AM_Y, c.st);
+    const unsigned b5 = std::min<unsigned>(red_blocks(n), (unsigned)DOT5_BLOCKS);
+    k_dot5<<<b5, RED_THREADS, 0, c.st>>>(n, c.p32, w32, c.q32, aw32, c.z32, rpart, gal.p);
+    TG_CHECK_LAUNCH();
+    k_ws_solve<<<1, 1, 0, c.st>>>(gal.p, wsb.p, c.pcg.p, correction ? 1 : 0);
+    TG_CHECK_LAUNCH();
+    if (combine) {
+      k_ws_apply<<<nb(n), 256, 0, c.st>>>(n, wsb.p, c.u.p, v2);
+      TG_CHECK_LAUNCH();
+    }
+  }
+  TG_CUDA(cudaEventRecord(ev_join, c.st));
 }
 
 }  // namespace tg

@@ -30,17 +30,25 @@ struct Cnn {
   // training set recorded from solver runs
   int capacity_ = 0, nsamples = 0;
   DevBuf<float> data_x, data_t;
-  // solver-state scratch
+  // solver-state scratch; w32: the prolongated network output (the deflation
+  // vector of the FP32 PCG in the solve that follows), aw32 = K w32; rc32:
+  // the residual restricted to the level-1 grid, a network input
   DevBuf<double> uprev, corr;
-  DevBuf<float> r32a;
-  DevBuf<PCGState> su, sr;       // norms of u_prev and of its residual
-  DevBuf<PCGState> gal;          // the five products of the 2x2 Galerkin combination (+ a ticket)
-  DevBuf<double> wsb;            // c1, c2, valid, accepted of the last warm start
+  DevBuf<float> r32a, w32, aw32, rc32;
+  DevBuf<PCGState> su, sr, src;  // norms of u_prev, of its residual, of the restricted residual
+  DevBuf<PCGState> gal;          // the five products of the 2x2 Galerkin combination
+  DevBuf<double> wsb;            // c1, c2, valid of the last warm start
+  DevBuf<double> rpart;          // reduction partials of the network's own dots
+  cudaStream_t side = nullptr;   // the warm start's stream
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   float lr = 1e-3f;
   int adam_t = 0;
   bool trained = false;
 
   Cnn(Ctx& c, int capacity, uint64_t seed);
+  ~Cnn();
+  Cnn(const Cnn&) = delete;
+  Cnn& operator=(const Cnn&) = delete;
   // split: FP32-level split-TF32 products (training, checks); otherwise TF32
   void forward(cudaStream_t st, bool split = true);
   double backward(cudaStream_t st, bool want_loss);
@@ -49,7 +57,21 @@ struct Cnn {
   void record_begin(Ctx& c);
   void record_end(Ctx& c);
   double train(int epochs, float lr, uint64_t seed);
-  void warm_start(Ctx& c, double* accepted);   // accepted: device flag (1 = used)
+  // Adam over n caller-provided pairs (host x0s [n][nodes][7], targets
+  // [n][nodes][3]), one step per pair in a seeded shuffled order per epoch
+  double fit(int n, const float* x0s, const float* targets, int epochs, float lr, uint64_t seed);
+  // Candidate warm start and coarse-grid correction for the current design:
+  // uprev <- u; with combine, u <- c1 u + c2 w (w = P y, energy-optimal c);
+  // with correction, c.pcg gets 1 / (w^T K w) and w deflates the FP32 PCG
+  // (else 0).  The plain warm start's residual norm^2 stays in plain_rr()
+  // (device) for the fallback test after the first cycle of the solve.
+  // The work runs on the network's own stream, forked from c.st once the
+  // design's scale factors are set; it does not touch the multigrid
+  // hierarchy, so it overlaps the hierarchy's build, and warm_start_join
+  // makes c.st wait for it before the solve.
+  void warm_start(Ctx& c, bool combine, bool correction);
+  void warm_start_join(Ctx& c);
+  const double* plain_rr() const { return &sr.p->rr; }
 };
 
 }  // namespace tg

@@ -627,21 +627,22 @@ __global__ void k_loop_continue(cudaGraphConditionalHandle h, const PCGState* s)
 }
 
 // Run PCG iterations (body = one iteration, no host read inside) until
-// sqrt(rr) < tol, maxit iterations (counted by the PCG state's iter since
-// its reset) or a non-finite rr: as one WHILE-node graph replay, captured on
-// first use; while a kernel family is event-timed or graphs are off, one
-// iteration at a time from the host.  Leaves the PCG state in h_pcg and
-// returns the number of iterations run.
+// sqrt(rr) < tol, the PCG state's iter (counted since its reset; `start` at
+// entry, so a loop can resume one that stopped) reaches maxit, or rr is not
+// finite: as one WHILE-node graph replay, captured on first use; while a
+// kernel family is event-timed or graphs are off, one iteration at a time
+// from the host.  Leaves the PCG state in h_pcg and returns the number of
+// iterations run by this call.
 template <typename F>
 static int run_loop(Ctx& c, Ctx::IterGraph& gr, Ctx::LoopGraph& lg, double tol, int maxit,
-                    F&& body) {
-  if (maxit <= 0) {
+                    F&& body, int start = 0) {
+  if (maxit - start <= 0) {
     read_pcg(c, c.pcg);
     return 0;
   }
   if (!c.use_graphs || prof_kind() != PK_NONE) {
     int it = 0;
-    while (it < maxit) {
+    while (start + it < maxit) {
       run_iteration(c, gr, [&] {
         body();
         TG_CUDA(cudaMemcpyAsync(c.h_pcg, c.pcg.p, sizeof(PCGState), cudaMemcpyDeviceToHost, c.st));
@@ -690,9 +691,19 @@ static int run_loop(Ctx& c, Ctx::IterGraph& gr, Ctx::LoopGraph& lg, double tol, 
   TG_CHECK_LAUNCH();
   TG_CUDA(cudaGraphLaunch(lg.exec, c.st));
   read_pcg(c, c.pcg);
-  const int it = c.h_pcg->iter;
+  const int it = c.h_pcg->iter - start;
   count_launches(lg.body_launches * it);
   return it;
+}
+
+static void drop_loop_graphs(Ctx::IterGraph& gr, Ctx::LoopGraph& lg) {
+  if (gr.exec) cudaGraphExecDestroy(gr.exec);
+  gr.exec = nullptr;
+  gr.prof.release();
+  if (lg.exec) cudaGraphExecDestroy(lg.exec);
+  if (lg.graph) cudaGraphDestroy(lg.graph);
+  lg.exec = nullptr;
+  lg.graph = nullptr;
 }
 
 // plain FP64 PCG (linear_solvers.py:114-134), x in/out
@@ -730,13 +741,38 @@ static int pcg64(Ctx& c, const double* b, double* x, double tol_abs, int maxiter
   return it;
 }
 
-// FP32 PCG on the unit-norm residual r32 (d32 = 0 initial), FP64 dots
-static int pcg32(Ctx& c, double tol_abs, int maxiter) {
+// the deflation vector of the FP32 PCG (the coarse-grid correction), when
+// the context uses one (a learned network attached with that part enabled)
+static const float* correction_vector(const Ctx& c) {
+  return (c.cnn && (c.learned & TG_LEARNED_COARSE_CORRECTION)) ? c.cnn->w32.p : nullptr;
+}
+
+// FP32 PCG on the unit-norm residual r32 (d32 = 0 initial), FP64 dots:
+// pcg32_begin resets, pcg32_run iterates until the inner tolerance or the
+// state's iteration count reaches maxit (so a second call resumes a first).
+// With a deflation vector w the pass starts from d32 = gamma w, the residual
+// made orthogonal to w (a no-op while the state's wawinv is 0).
+static void pcg32_begin(Ctx& c) {
   const int64_t n = c.g.ndofs();
   TG_CUDA(cudaMemsetAsync(c.d32.p, 0, sizeof(float) * n, c.st));
   pcg_reset(c.pcg, c.st);
-  const int it = run_loop(c, c.g32, c.l32, tol_abs, maxiter, [&] {
-    // z = M r with rho = r . z fused into the cycle's last fine sweep; q = A p
+  if (const float* w = correction_vector(c)) {
+    ProfScope ps(PK_VECTOR, c.st);
+    dot<float, float>(n, w, c.r32.p, c.part, c.pcg, DOT_WR, c.st);
+    deflate_start(n, w, c.cnn->aw32.p, c.d32, c.r32, c.pcg, c.st);
+  }
+}
+static int pcg32_run(Ctx& c, double tol_abs, int maxit, int start) {
+  const int64_t n = c.g.ndofs();
+  const float* w = correction_vector(c);
+  const float* aw = w ? c.cnn->aw32.p : nullptr;
+  if (w != c.g32_corr) {               // the captured iteration is for another vector
+    drop_loop_graphs(c.g32, c.l32);
+    c.g32_corr = w;
+  }
+  const int it = run_loop(c, c.g32, c.l32, tol_abs, maxit, [&] {
+    // z = M r with rho = r . z fused into the cycle's last fine sweep; with a
+    // deflation vector w, Aw . z for the deflated search direction; q = A p
     // with p . q (alpha) fused into the product
     if (c.precond == TG_PRECOND_GMG) {
       vcycle<float>(c, 0, c.r32, c.z32, false, DOT_RHO);
@@ -747,13 +783,18 @@ static int pcg32(Ctx& c, double tol_abs, int maxiter) {
     }
     {
       ProfScope ps(PK_VECTOR, c.st);
-      update_p<float>(n, c.z32, c.p32, c.pcg, c.st);
+      if (w) {
+        dot<float, float>(n, aw, c.z32.p, c.part, c.pcg, DOT_WZ, c.st);
+        update_p_corr(n, c.z32, w, c.p32, c.pcg, c.st);
+      } else {
+        update_p<float>(n, c.z32, c.p32, c.pcg, c.st);
+      }
     }
     fine_apply_dot<float, float>(c.op, c.s32, c.p32, c.q32, nullptr, nullptr, 0.0, AM_Y, c.part,
                                  c.pcg, DOT_ALPHA, c.st);
     ProfScope ps(PK_VECTOR, c.st);
     update_xr<float>(n, c.p32, c.q32, c.d32, c.r32, c.part, c.pcg, c.st);
-  });
+  }, start);
   check_finite(c.h_pcg->rr, "inner PCG residual");
   return it;
 }
@@ -813,8 +854,35 @@ void solve(Ctx& c, const double* b, double* u) {
       // 20-60): an FP32 recurrence that stalls -- seen on one design of a
       // 200-iteration run from random densities -- is restarted from the true
       // FP64 residual by the next pass
-      const int cap = c.precond == TG_PRECOND_GMG ? 200 : c.maxiter;
-      total += pcg32(c, inner, std::min(c.maxiter - total, cap));
+      const int cap = std::min(c.maxiter - total, c.precond == TG_PRECOND_GMG ? 200 : c.maxiter);
+      pcg32_begin(c);
+      int it = 0;
+      if (c.ws_pending) {
+        // the learned start is kept only if the residual after its first
+        // cycle is below the plain warm start's (u_prev's) residual;
+        // otherwise plain PCG from u_prev, without the deflation
+        c.ws_pending = false;
+        it = pcg32_run(c, inner, 1, 0);
+        const double inner1 = std::sqrt(c.h_pcg->rr);
+        const double r1 = std::sqrt(rr) * inner1;
+        TG_CUDA(cudaMemcpyAsync(c.h_scal + 5, c.cnn->plain_rr(), sizeof(double),
+                                cudaMemcpyDeviceToHost, c.st));
+        TG_CUDA(cudaStreamSynchronize(c.st));
+        const double r_plain = std::sqrt(c.h_scal[5]);
+        c.last_warm_ratio = r_plain > 0.0 ? std::sqrt(rr) / r_plain : 0.0;
+        if (!(r1 < r_plain)) {
+          TG_CUDA(cudaMemcpyAsync(u, c.cnn->uprev.p, sizeof(double) * n, cudaMemcpyDeviceToDevice,
+                                  c.st));
+          set_correction(c.pcg, 0.0, c.st);
+          c.last_fallback = 1;
+          total += it;
+          continue;    // the next pass starts from u_prev's true residual
+        }
+        if (inner1 >= inner && it < cap) it += pcg32_run(c, inner, cap, it);
+      } else {
+        it = pcg32_run(c, inner, cap, 0);
+      }
+      total += it;
       ProfScope ps(PK_VECTOR, c.st);
       add_scaled_f32(n, c.d32, c.pcg_out, u, c.st);
       c.last_refine = k + 1;
@@ -847,14 +915,26 @@ void ctx_step(Ctx& c, tg_iter_out& out) {
   const int64_t nel = g.nel();
   set_density(c, c.xPhys);
   TG_CUDA(cudaEventRecord(c.ev0, c.st));
-  build_hierarchy(c);
-  // learned warm start (falls back to the previous displacement when its
-  // residual is not smaller); the solve below is unchanged either way
-  const bool warm = c.learned && c.cnn && c.cnn->trained && c.iter > 0 && c.nload == 1;
+  // learned warm start and coarse-grid correction (kept only if the residual
+  // after the solve's first cycle is below the plain warm start's; else the
+  // solve falls back to plain PCG from the previous displacement); it needs
+  // only the new scale factors, so it runs on the network's stream while
+  // this stream builds the hierarchy
+  const int lmask = c.learned & (TG_LEARNED_WARM_START | TG_LEARNED_COARSE_CORRECTION);
+  const bool warm = lmask && c.cnn && c.cnn->trained && c.iter > 0 && c.nload == 1 &&
+                    c.precision == TG_PREC_MIXED;
+  c.last_fallback = 0;
+  c.last_warm_ratio = 0.0;
+  c.ws_pending = false;
   if (warm) {
-    ProfScope ps(PK_LEARNED, c.st);
-    c.cnn->warm_start(c, c.scal.p + 3);   // decision read back with the scalars below
+    c.cnn->warm_start(c, (lmask & TG_LEARNED_WARM_START) != 0,
+                      (lmask & TG_LEARNED_COARSE_CORRECTION) != 0);
+    c.ws_pending = true;
+  } else if (correction_vector(c)) {
+    set_correction(c.pcg, 0.0, c.st);     // no vector for this design: plain PCG
   }
+  build_hierarchy(c);
+  if (warm) c.cnn->warm_start_join(c);
   // one solve per load case with the same hierarchy (topology_optimization.py:446-459)
   const int64_t nd = g.ndofs();
   int iters = 0, vcycles = 0, refine = 0;
@@ -908,7 +988,7 @@ void ctx_step(Ctx& c, tg_iter_out& out) {
   if (c.h_oc->bar.err) throw Error{ETIMEOUT, "OC bisection: a grid barrier wait timed out"};
   if (!c.h_oc->done) throw Error{ENOTCONV, "OC bisection did not terminate within 256 steps"};
   c.g_oc = c.h_oc->gt;
-  const int fallback = (warm && c.h_scal[3] == 0.0) ? 1 : 0;
+  const int fallback = c.last_fallback;
   const double vol_sum = c.h_scal[1];
   float ms = 0.f;
   TG_CUDA(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
@@ -924,6 +1004,7 @@ void ctx_step(Ctx& c, tg_iter_out& out) {
   out.fallback = fallback;
   out.nlevels = c.L;
   out.t_solve_ms = ms;
+  out.warm_ratio = c.last_warm_ratio;
   check_finite(out.obj, "objective");
   c.iter++;
   out.t_step_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();

@@ -110,6 +110,12 @@ struct Ctx {
   } l64, l32;
   bool use_graphs = true;
   struct Cnn* cnn = nullptr;     // learned warm start (not owned)
+  // the learned start of this step awaits its test after the first cycle;
+  // the FP32 PCG graphs were captured for this deflation vector (null: none)
+  bool ws_pending = false;
+  int last_fallback = 0;
+  double last_warm_ratio = 0.0;
+  const float* g32_corr = nullptr;
   // Helmholtz PDE filter: the screened Poisson problem on the same device
   // grid, one scalar DOF per node, as its own context (owned); events order
   // its stream after this context's and back

@@ -420,6 +420,59 @@ void update_p(int64_t n, const T* z, T* p, const PCGState* st, cudaStream_t s) {
 template void update_p<double>(int64_t, const double*, double*, const PCGState*, cudaStream_t);
 template void update_p<float>(int64_t, const float*, float*, const PCGState*, cudaStream_t);
 
+__global__ void k_update_p_corr(int64_t n, const float* __restrict__ z, const float* __restrict__ w,
+                                float* __restrict__ p, const PCGState* st) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const float beta = (float)st->beta;
+  const float gam = -(float)(st->wz * st->wawinv);
+  const bool first = st->iter == 0;
+  const int64_t n4 = n / 4;
+  if (i < n4) {
+    const float4 zv = reinterpret_cast<const float4*>(z)[i];
+    const float4 wv = reinterpret_cast<const float4*>(w)[i];
+    float4 v;
+    v.x = fmaf(gam, wv.x, zv.x); v.y = fmaf(gam, wv.y, zv.y);
+    v.z = fmaf(gam, wv.z, zv.z); v.w = fmaf(gam, wv.w, zv.w);
+    if (!first) {
+      const float4 pv = reinterpret_cast<const float4*>(p)[i];
+      v.x = fmaf(beta, pv.x, v.x); v.y = fmaf(beta, pv.y, v.y);
+      v.z = fmaf(beta, pv.z, v.z); v.w = fmaf(beta, pv.w, v.w);
+    }
+    reinterpret_cast<float4*>(p)[i] = v;
+  } else if (i < n4 + (n - 4 * n4)) {
+    const int64_t j = 4 * n4 + (i - n4);
+    const float v = fmaf(gam, w[j], z[j]);
+    p[j] = first ? v : fmaf(beta, p[j], v);
+  }
+}
+void update_p_corr(int64_t n, const float* z, const float* w, float* p, const PCGState* st,
+                   cudaStream_t s) {
+  const int64_t nt = n / 4 + (n % 4);
+  k_update_p_corr<<<(unsigned)cdiv(nt, 256), 256, 0, s>>>(n, z, w, p, st);
+  TG_CHECK_LAUNCH();
+}
+__global__ void k_deflate_start(int64_t n, const float* __restrict__ w, const float* __restrict__ aw,
+                                float* __restrict__ d, float* __restrict__ r, const PCGState* st) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float gam = (float)(st->wr * st->wawinv);
+  d[i] = gam * w[i];
+  r[i] = fmaf(-gam, aw[i], r[i]);
+}
+void deflate_start(int64_t n, const float* w, const float* aw, float* d, float* r,
+                   const PCGState* st, cudaStream_t s) {
+  k_deflate_start<<<(unsigned)cdiv(n, 256), 256, 0, s>>>(n, w, aw, d, r, st);
+  TG_CHECK_LAUNCH();
+}
+__global__ void k_set_correction(PCGState* st, double v) {
+  st->wawinv = v;
+  st->wr = st->wz = 0.0;
+}
+void set_correction(PCGState* st, double v, cudaStream_t s) {
+  k_set_correction<<<1, 1, 0, s>>>(st, v);
+  TG_CHECK_LAUNCH();
+}
+
 // x += alpha p ; r -= alpha q ; rr = r.r (finalised by the last block)
 template <typename T>
 __global__ void __launch_bounds__(RED_THREADS) k_update_xr(int64_t n, const T* __restrict__ p,

@@ -23,13 +23,19 @@ struct OCScratch {
 };
 
 // PCG scalars (linear_solvers.py:114-134)
-enum DotOp : int { DOT_RHO = 0, DOT_ALPHA = 1, DOT_RR = 2, DOT_BB = 3 };
+enum DotOp : int { DOT_RHO = 0, DOT_ALPHA = 1, DOT_RR = 2, DOT_BB = 3, DOT_WR = 4, DOT_WZ = 5 };
 struct PCGState {
   double rho, beta, alpha, pq, rr, bb, rnorm, rinv;
   int iter;
   unsigned int ticket;
   double tol;        // device-side PCG loop: continue while sqrt(rr) >= tol
   int maxit;         //   and iter < maxit (and rr finite)
+  // deflation by one vector w (deflated CG, Saad et al. 2000): each pass
+  // starts with the residual made orthogonal to w (wr = w.r, DOT_WR) and
+  // every search direction is made A-orthogonal to w, p = z - mu w + beta p
+  // with mu = (Aw . z) / (w^T A w) (wz = Aw . z, DOT_WZ); wawinv =
+  // 1 / (w^T A w), 0 = no deflation
+  double wr, wz, wawinv;
 };
 
 // PCG scalars from a finished dot product (the last block of a reduction)
@@ -46,6 +52,10 @@ __device__ inline void pcg_dot_finish(PCGState* st, int op, double tot) {
     st->rinv = tot > 0.0 ? 1.0 / st->rnorm : 0.0;
   } else if (op == DOT_BB) {
     st->bb = tot;
+  } else if (op == DOT_WR) {
+    st->wr = tot;
+  } else if (op == DOT_WZ) {
+    st->wz = tot;
   }
 }
 
@@ -76,6 +86,15 @@ template <typename TA, typename TB>
 void dot(int64_t n, const TA* a, const TB* b, double* part, PCGState* st, int op, cudaStream_t s);
 template <typename T>
 void update_p(int64_t n, const T* z, T* p, const PCGState* st, cudaStream_t s);
+// deflated search direction p = (z - mu w) + beta p, mu = st->wz * st->wawinv (FP32)
+void update_p_corr(int64_t n, const float* z, const float* w, float* p, const PCGState* st,
+                   cudaStream_t s);
+// start of a deflated pass: gamma = st->wr * st->wawinv, d = gamma w,
+// r -= gamma Aw (the residual orthogonal to w; FP32)
+void deflate_start(int64_t n, const float* w, const float* aw, float* d, float* r,
+                   const PCGState* st, cudaStream_t s);
+// st->wawinv = v (one thread)
+void set_correction(PCGState* st, double v, cudaStream_t s);
 template <typename T>
 void update_xr(int64_t n, const T* p, const T* q, T* x, T* r, double* part, PCGState* st,
                cudaStream_t s);

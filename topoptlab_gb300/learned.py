@@ -1,13 +1,18 @@
 """Learned warm start for the GPU solver (no counterpart in the reference).
 
 A 3-level 3-D convolutional encoder-decoder (16/32/64 channels, FP32) on the
-multigrid level-1 node grid predicts a displacement correction from the
-filtered density, the previous displacement and its residual; the warm start
-of each solve is ``u_prev + P(correction)``, kept only when its residual is
-smaller than the previous displacement's (otherwise the step falls back to
-the plain warm start and reports ``fallback = 1``).  Training data are
-(features, displacement change) pairs recorded around solver steps; training
-runs on the GPU with the library's own kernels (forward, backward, Adam).
+multigrid level-1 node grid predicts a displacement correction y from the
+filtered density, the previous displacement and its residual restricted to
+the level-1 grid.  With w = P y the warm start of each solve is the
+energy-optimal combination ``c1 u_prev + c2 w``; optionally w also deflates
+the mixed solver's FP32 PCG (the coarse-grid correction, ``learned=
+"coarse_correction"`` or ``"both"`` on the problem).  The learned start is
+kept only when the residual after the solve's first cycle is below the plain
+warm start's (otherwise the step falls back to plain PCG from the previous
+displacement and reports ``fallback = 1``).  Training data are (features,
+displacement change) pairs recorded around solver steps of any context with
+the same grids (or given by the caller, ``fit``); training runs on the GPU
+with the library's own kernels (forward, backward, Adam).
 """
 from __future__ import annotations
 
@@ -63,6 +68,20 @@ class LearnedWarmStart:
     def train(self, epochs: int = 20, lr: float = 1e-3, seed: int = 0) -> float:
         loss = C.c_double()
         self._check(self._lib.tg_cnn_train(self._h, epochs, lr, seed, C.byref(loss)), "tg_cnn_train")
+        return loss.value
+
+    def fit(self, x0s, targets, epochs: int = 1, lr: float = 1e-3, seed: int = 0) -> float:
+        """Adam over caller-provided pairs: x0s (n, nodes, 7), targets (n, nodes, 3)."""
+        g = self.info()["grid"]
+        nn = g[0] * g[1] * g[2]
+        x = np.ascontiguousarray(np.asarray(x0s, dtype=np.float32).reshape(-1, nn, 7))
+        t = np.ascontiguousarray(np.asarray(targets, dtype=np.float32).reshape(-1, nn, 3))
+        if x.shape[0] != t.shape[0]:
+            raise ValueError("fit: as many targets as feature sets are needed")
+        loss = C.c_double()
+        self._check(self._lib.tg_cnn_fit(self._h, x.shape[0], x.ctypes.data_as(_fp),
+                                         t.ctypes.data_as(_fp), epochs, lr, seed, C.byref(loss)),
+                    "tg_cnn_fit")
         return loss.value
 
     def attach(self, prob: GpuProblem | None = None, on: bool = True):

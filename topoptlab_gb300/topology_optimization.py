@@ -25,6 +25,15 @@ Solver selection (``lin_solver_kw["name"]``):
 ``preconditioner_kw``: name "gb300-gmg" (default) or "gb300-jacobi";
 ``nlevels`` (0 = automatic), ``nsmooth`` (2), ``omega`` (0.6),
 ``precision`` ("fp64" or "mixed"), ``inner_rtol`` (1e-4), ``learned`` (False).
+``learned`` carries a trained network (no counterpart in the reference): the
+flat parameter vector of a ``learned.LearnedWarmStart`` (its ``params()``), or
+the path of a ``.npy`` file holding it, optionally as
+``{"params": ..., "mode": "warm_start" | "coarse_correction" | "both"}``
+(default "warm_start").  The network then gives each solve its warm start
+(and with "coarse_correction" the FP32 PCG its deflation vector); it needs a
+3-D elasticity problem with ``precision="mixed"`` and multigrid.
+``learned=True`` without parameters raises ValueError, like the reference's
+unknown-option errors.
 """
 from __future__ import annotations
 
@@ -81,8 +90,27 @@ def solver_options(lin_solver_kw: Dict, preconditioner_kw: Dict) -> Dict:
     if "precision" in preconditioner_kw:
         opts["precision"] = preconditioner_kw["precision"]
     if "learned" in preconditioner_kw:
-        opts["learned"] = bool(preconditioner_kw["learned"])
+        opts["learned"] = preconditioner_kw["learned"]
     return opts
+
+
+def learned_network(spec):
+    """(params, mode) of preconditioner_kw["learned"]; (None, 0) for none."""
+    if spec is None or spec is False:
+        return None, 0
+    mode = "warm_start"
+    if isinstance(spec, dict):
+        mode = spec.get("mode", "warm_start")
+        spec = spec.get("params")
+    if spec is True or spec is None:
+        raise ValueError("preconditioner_kw['learned'] needs trained network parameters "
+                         "(LearnedWarmStart.params() or the path of a .npy file holding them)")
+    if isinstance(spec, str):
+        spec = np.load(spec)
+    params = np.ascontiguousarray(np.asarray(spec, dtype=np.float32).reshape(-1))
+    if params.size == 0:
+        raise ValueError("preconditioner_kw['learned']: empty parameter vector")
+    return params, mode
 
 
 def _name(fn) -> str:
@@ -151,6 +179,11 @@ def main(nelx: int, nely: int,
     if assembly_mode not in ("full", "lower"):
         raise ValueError(f"Unknown assembly_mode {assembly_mode}")
     opts = solver_options(lin_solver_kw, preconditioner_kw)
+    net_params, net_mode = learned_network(opts.pop("learned"))
+    if net_params is not None and (ndim != 3 or opts["precision"] != "mixed"
+                                   or opts["precond"] != "gb300-gmg"):
+        raise ValueError("the learned network needs a 3-D problem with precision='mixed' and "
+                         "the multigrid preconditioner")
     eps = float(matinterpol_kw.get("eps", 1e-9))
     penal = float(matinterpol_kw.get("penal", 3.0))
     # ---- logging (log_utils.SimpleLogger semantics) ----
@@ -186,7 +219,23 @@ def main(nelx: int, nely: int,
     # sensitivities summed (topology_optimization.py:446-500)
     prob = GpuProblem(nelx, nely, nelz, KE, fixed, f, volfrac, rmin, ft=int(ft),
                       eps=eps, penal=penal, el_flags=el_flags, device=device,
-                      filter_mode=filter_mode, filter_l=l, **opts)
+                      filter_mode=filter_mode, filter_l=l,
+                      learned=net_mode if net_params is not None else False, **opts)
+    net = None
+    if net_params is not None:
+        from .learned import LearnedWarmStart
+        try:
+            net = LearnedWarmStart(prob, capacity=0)
+            if net.info()["nparams"] != net_params.size:
+                raise ValueError(f"preconditioner_kw['learned']: {net_params.size} parameters, "
+                                 f"the network has {net.info()['nparams']}")
+            net.set_params(net_params)
+            net.attach(prob)
+        except Exception:
+            if net is not None:
+                net.close()
+            prob.close()
+            raise
     obj = 0.0
 
     def export(name):
@@ -211,6 +260,8 @@ def main(nelx: int, nely: int,
         if output_kw["export"]:
             export(output_kw["file"])
     finally:
+        if net is not None:
+            net.close()
         prob.close()
     if profiler is not None:
         profiler.disable()
