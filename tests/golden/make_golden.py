@@ -22,6 +22,7 @@ Outputs (small .npz files, committed):
                        the 3-D cantilever ladder (20 / 10 / 2 iterations): the
                        grids on which the multigrid hierarchy is deep; also the
                        reference's seconds per design iteration on this host
+  mbb2d_60x20.log  the reference's log file of the MBB 60x20 run (verbosity 20)
   vtk.npz          what the reference's export_vtk hands to meshio (points,
                    cells, point and cell data) for a 2-D and a 3-D grid, seeded
                    fields, and what export_stl hands it for the 2-D grid,
@@ -389,7 +390,22 @@ def gen_ladder():
         print("ladder", nx, ny, nz, r[1], f"{sec:.2f} s/iteration")
 
 
-GENERATORS = {"ladder": lambda: gen_ladder(), "vtk": lambda: gen_vtk(),
+def gen_log():
+    """The reference's log file (SimpleLogger, verbosity 20) of the MBB beam
+    60x20 run with the density filter (tests/test_compliance.py:10 set-up)."""
+    import tempfile
+    with tempfile.TemporaryDirectory() as tmp:
+        base = os.path.join(tmp, "mbb")
+        kw = dict(OUT_KW, write_log=True, file=base, verbosity=20)
+        T.main(nelx=60, nely=20, volfrac=0.5, rmin=2.4, ft=1, bcs=mbb_2d, optimizer="oc",
+               lin_solver_kw={"name": "scipy-direct"}, output_kw=kw)
+        text = open(base + ".log").read()
+    with open(os.path.join(HERE, "mbb2d_60x20.log"), "w") as f:
+        f.write(text)
+    print("log lines", len(text.splitlines()))
+
+
+GENERATORS = {"log": lambda: gen_log(), "ladder": lambda: gen_ladder(), "vtk": lambda: gen_vtk(),
               "helmholtz": lambda: gen_helmholtz(), "stiffness": lambda: gen_stiffness(),
               "convolution": lambda: gen_convolution(),
               "passive": lambda: gen_passive(), "slow": lambda: gen_slow_cantilevers()}
@@ -423,6 +439,7 @@ def main():
                    bcs=cantilever_3d, nouteriter=12)
     print("cant3d", r[1], r[2])
     gen_ladder()
+    gen_log()
 
 
 if __name__ == "__main__":

@@ -26,6 +26,39 @@ def test_mbb_density_filter_full_run(gpu_lib, golden):
     np.testing.assert_allclose(x[:, 0], g["final_x"], atol=1e-8)
 
 
+def test_log_file_matches_reference(gpu_lib, tmp_path):
+    """The log file of main (write_log, verbosity 20) against the reference's
+    own log of the same MBB run (topology_optimization.py:181-199, :669-670):
+    the same lines in the same order, the set-up lines identical, each
+    iteration line in the reference's format with its numbers within the
+    solver tolerance (obj 1e-8 relative, vol and change 1e-9)."""
+    import os
+    import re
+    from topoptlab_gb300 import main
+    from topoptlab_gb300.example_bc import mbb_2d
+    ref = open(os.path.join(os.path.dirname(__file__), "golden", "mbb2d_60x20.log")).read()
+    base = str(tmp_path / "mbb")
+    out = dict(OUT, write_log=True, file=base, verbosity=20)
+    main(nelx=60, nely=20, volfrac=0.5, rmin=2.4, ft=1, filter_mode="matrix", optimizer="oc",
+         bcs=mbb_2d, lin_solver_kw={"name": "scipy-direct"}, output_kw=out)
+    ours = open(base + ".log").read().splitlines()
+    theirs = ref.splitlines()
+    assert len(ours) == len(theirs)
+    pat = re.compile(r"^it\.: (\d+) obj\.: (-?\d+\.\d{10}) vol\.: (-?\d+\.\d{10}) "
+                     r"ch\.: (-?\d+\.\d{10})$")
+    for a, b in zip(ours, theirs):
+        mb = pat.match(b)
+        if mb is None:
+            assert a == b
+            continue
+        ma = pat.match(a)
+        assert ma is not None, a
+        assert ma.group(1) == mb.group(1)
+        np.testing.assert_allclose(float(ma.group(2)), float(mb.group(2)), rtol=1e-8)
+        np.testing.assert_allclose(float(ma.group(3)), float(mb.group(3)), rtol=0, atol=1e-9)
+        np.testing.assert_allclose(float(ma.group(4)), float(mb.group(4)), rtol=0, atol=1e-9)
+
+
 def test_mbb_sensitivity_filter(gpu_lib, golden):
     """tests/test_compliance.py:9 -- 216.81366 (ft=0)."""
     from topoptlab_gb300 import main
