@@ -480,6 +480,319 @@ __global__ void __launch_bounds__(zs::NT, sizeof(T) == 8 ? 2 : 4) k_fine_zstream
   }
 }
 
+// ---------------------------------------------------------------------------
+// 3-D, FP32: z-streaming with two y-adjacent elements per thread.  The CTA's
+// 256 threads cover 16 (x) x 32 (y) elements (15 x 31 owned nodes); a thread's
+// two elements share their middle node face, so per element layer it reads 3
+// node faces instead of 4 and does the x/z butterflies of the reflection
+// transform once per face; the two elements' outputs on the shared face are
+// added in transform space before the inverse x/z butterflies.  Node
+// contributions are merged without the element-output buffer: the face a
+// thread shares with its y-neighbour arrives by a warp shuffle (lane + 1 is
+// the next element pair in y), the x-neighbour's by one small shared-memory
+// exchange, and the z-neighbour's stays in registers until the next layer.
+// Node rows are stored even y first, then odd y, with a pitch of 48 words, so
+// every shared-memory access of a warp (two x-rows of 16 lanes, stride-2 in
+// y) is bank-conflict free.  Every sum runs in a fixed order: results are
+// bit-reproducible.
+// ---------------------------------------------------------------------------
+namespace zp {
+constexpr int EXT = 16, JY = 16;            // threads: element columns in x, pairs in y
+constexpr int EYT = 2 * JY;                 // 32 elements in y
+constexpr int OX = EXT - 1, OY = EYT - 1;   // owned nodes per tile: 15 x 31
+constexpr int PX = EXT + 1, PY = EYT + 1;   // node rows / nodes per row incl. halo: 17 x 33
+constexpr int ODD = 17;                     // odd-y nodes of a row start here (even y: 0..16)
+constexpr int PITCH = 48;
+constexpr int PLANE = PX * PITCH;           // words per component plane
+constexpr int NT = EXT * JY;
+template <int NDOF> __host__ __device__ constexpr int ncopy() { return (NDOF * PX * PY + NT - 1) / NT; }
+template <int NDOF> constexpr size_t smem() {
+  return sizeof(float) * ((size_t)3 * NDOF * PLANE + (size_t)4 * NDOF * NT);
+}
+__host__ __device__ constexpr int ycol(int hy) { return (hy & 1) ? ODD + (hy >> 1) : (hy >> 1); }
+}  // namespace zp
+
+// Element with lower face Fa (dy = 0) and upper face Fb (dy = 1), both after
+// the x/z butterflies (index q = cx | cz << 1): the y butterfly, the sector
+// product with B (in place, group by group) and the inverse y butterfly;
+// returns the element's output faces G[0] (lower), G[1] (upper), still in
+// x/z transform space and without the density.
+template <int NDOF, int KIND>
+__device__ __forceinline__ void pair_element(const float (&Fa)[4][NDOF], const float (&Fb)[4][NDOF],
+                                             const Sector<float>& B, float (&G)[2][4][NDOF]) {
+  float U[8][NDOF];
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+#pragma unroll
+    for (int c = 0; c < NDOF; ++c) {
+      const int lo = (q & 1) | ((q >> 1) << 2);      // chi with cy = 0
+      U[lo][c] = Fa[q][c] + Fb[q][c];
+      U[lo | 2][c] = Fa[q][c] - Fb[q][c];
+    }
+  // y[sig(chi, c)][c] = sum_c2 B[chi][c][c2] u[sig(chi, c2)][c2]: each chi maps
+  // NDOF inputs to NDOF outputs on the same index set, so it runs in place
+#pragma unroll
+  for (int chi = 0; chi < 8; ++chi) {
+    float in[NDOF];
+#pragma unroll
+    for (int c2 = 0; c2 < NDOF; ++c2) in[c2] = U[sig<3, NDOF>(chi, c2)][c2];
+#pragma unroll
+    for (int c = 0; c < NDOF; ++c) {
+      float acc = 0.f;
+#pragma unroll
+      for (int c2 = 0; c2 < NDOF; ++c2)
+        if (KIND != EK_SECTOR_HEX8 || ((hex8_mask(chi) >> (c * 3 + c2)) & 1u))
+          acc += B.b[chi][c][c2] * in[c2];
+      U[sig<3, NDOF>(chi, c)][c] = acc;
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+#pragma unroll
+    for (int c = 0; c < NDOF; ++c) {
+      const int lo = (q & 1) | ((q >> 1) << 2);
+      G[0][q][c] = U[lo][c] + U[lo | 2][c];
+      G[1][q][c] = U[lo][c] - U[lo | 2][c];
+    }
+}
+
+// the x and z butterflies of one face (q = dx | dz << 1 <-> cx | cz << 1)
+template <int NDOF>
+__device__ __forceinline__ void face_xz(float (&F)[4][NDOF]) {
+#pragma unroll
+  for (int c = 0; c < NDOF; ++c) {
+    float t0 = F[0][c], t1 = F[1][c];
+    F[0][c] = t0 + t1;
+    F[1][c] = t0 - t1;
+    t0 = F[2][c];
+    t1 = F[3][c];
+    F[2][c] = t0 + t1;
+    F[3][c] = t0 - t1;
+    t0 = F[0][c];
+    t1 = F[2][c];
+    F[0][c] = t0 + t1;
+    F[2][c] = t0 - t1;
+    t0 = F[1][c];
+    t1 = F[3][c];
+    F[1][c] = t0 + t1;
+    F[3][c] = t0 - t1;
+  }
+}
+
+template <int NDOF, typename S, int KIND, int MODE, int DOTK = -1>
+__global__ void __launch_bounds__(zp::NT, 3) k_fine_zpair(ApplyArgs<float, S> a, int zc) {
+  using namespace zp;
+  using T = float;
+  constexpr int SLOT = NDOF * PLANE;
+  constexpr int NCP = ncopy<NDOF>();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* us = reinterpret_cast<T*>(smem_raw);        // 3 node-plane slots [c][hx][PITCH]
+  T* xch = us + 3 * SLOT;                         // x exchange [(face*2 + dz)*NDOF + c][NT]
+  const Grid& g = a.g;
+  const int tid = threadIdx.x;
+  const int y0 = blockIdx.x * OY, x0 = blockIdx.y * OX;
+  const int zbeg = blockIdx.z * zc, zend = min(zbeg + zc, g.nnz);
+  const int64_t pstride = (int64_t)g.nnx * g.nny * NDOF;
+  const int64_t lstride = (int64_t)g.nex * g.ney;
+
+  int goff[NCP], soff[NCP];
+#pragma unroll
+  for (int k = 0; k < NCP; ++k) {
+    const int i = tid + k * NT;
+    soff[k] = -1;
+    goff[k] = 0;
+    if (i < NDOF * PX * PY) {
+      const int hx = i / (PY * NDOF), j = i % (PY * NDOF);
+      const int hy = j / NDOF, c = j % NDOF;
+      const int gx = x0 - 1 + hx, gy = y0 - 1 + hy;
+      if (gx >= 0 && gx < g.nnx && gy >= 0 && gy < g.nny) {
+        soff[k] = c * PLANE + hx * PITCH + ycol(hy);
+        goff[k] = (gx * g.nny + gy) * NDOF + c;
+      }
+    }
+  }
+  for (int i = tid; i < 3 * SLOT; i += NT) us[i] = T(0);
+  __syncthreads();
+  auto load_plane = [&](int p, int slot) {
+    if (p < 0 || p >= g.nnz) return;
+    const T* src = a.u + p * pstride;
+    T* dst = us + slot * SLOT;
+#pragma unroll
+    for (int k = 0; k < NCP; ++k)
+      if (soff[k] >= 0) cp_async<4>(dst + soff[k], src + goff[k]);
+  };
+
+  // this thread's element pair and owned nodes
+  const int exl = tid / JY, jy = tid % JY;
+  const int ex = x0 - 1 + exl;
+  const int eyA = y0 - 1 + 2 * jy;
+  const bool xin = ex >= 0 && ex < g.nex;
+  const bool vA = xin && eyA >= 0 && eyA < g.ney;
+  const bool vB = xin && eyA + 1 < g.ney;
+  const int64_t eoffA = (int64_t)ex * g.ney + eyA;
+  auto load_rho = [&](int ez, bool v, int64_t eoff) -> T {
+    return (v && ez >= 0 && ez < g.nez) ? load_scale<T, S>(a.scale, ez * lstride + eoff) : T(0);
+  };
+  const int row = exl * PITCH;
+  const int cf0 = jy, cf1 = ODD + jy, cf2 = jy + 1;      // columns of faces y = 2jy, 2jy+1, 2jy+2
+  const int nx = x0 - 1 + exl, ny0 = y0 - 1 + 2 * jy;
+  const bool xown = exl >= 1 && nx < g.nnx;
+  const bool own0 = xown && jy >= 1 && ny0 < g.nny;      // node (nx, ny0)
+  const bool own1 = xown && ny0 + 1 < g.nny;             // node (nx, ny0 + 1)
+
+  int s0 = 0, s1 = 1, s2 = 2;
+  load_plane(zbeg - 1, s0);
+  load_plane(zbeg, s1);
+  cp_async_wait_all();
+  __syncthreads();
+  T rhoA = load_rho(zbeg - 1, vA, eoffA), rhoB = load_rho(zbeg - 1, vB, eoffA + 1);
+  T dacc = T(0);
+  T acc[2][NDOF];
+#pragma unroll
+  for (int f = 0; f < 2; ++f)
+#pragma unroll
+    for (int c = 0; c < NDOF; ++c) acc[f][c] = T(0);
+
+  for (int ez = zbeg - 1; ez < zend; ++ez) {
+    if (ez + 1 < zend) load_plane(ez + 2, s2);
+    const T rnA = load_rho(ez + 1, vA, eoffA), rnB = load_rho(ez + 1, vB, eoffA + 1);
+    const bool owned = ez >= zbeg;
+    const int64_t nid = ((int64_t)ez * g.nnx + nx) * g.nny + ny0;
+    // node values of this layer's elements: O[face][q = dx | dz << 1][c]
+    T O[3][4][NDOF];
+    const bool lvalid = ez >= 0 && ez < g.nez;   // uniform over the CTA
+    if (lvalid) {
+      const T* p0 = us + s0 * SLOT + row;
+      const T* p1 = us + s1 * SLOT + row;
+      auto load_face = [&](int col, T (&F)[4][NDOF]) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+#pragma unroll
+          for (int c = 0; c < NDOF; ++c)
+            F[q][c] = ((q >> 1) ? p1 : p0)[c * PLANE + (q & 1) * PITCH + col];
+        face_xz<NDOF>(F);
+      };
+      T Fa[4][NDOF], Fb[4][NDOF];
+      load_face(cf0, Fa);
+      load_face(cf1, Fb);
+      T G[2][4][NDOF];
+      pair_element<NDOF, KIND>(Fa, Fb, a.B, G);
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int c = 0; c < NDOF; ++c) {
+          O[0][q][c] = rhoA * G[0][q][c];
+          O[1][q][c] = rhoA * G[1][q][c];
+        }
+      load_face(cf2, Fa);                        // face 2 (upper face of element B)
+      pair_element<NDOF, KIND>(Fb, Fa, a.B, G);
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int c = 0; c < NDOF; ++c) {
+          O[1][q][c] = fmaf(rhoB, G[0][q][c], O[1][q][c]);
+          O[2][q][c] = rhoB * G[1][q][c];
+        }
+#pragma unroll
+      for (int f = 0; f < 3; ++f) face_xz<NDOF>(O[f]);
+    } else {
+#pragma unroll
+      for (int f = 0; f < 3; ++f)
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+#pragma unroll
+          for (int c = 0; c < NDOF; ++c) O[f][q][c] = T(0);
+    }
+    // y: face 2 of the previous pair (lane - 1) is this pair's face 0
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+      for (int c = 0; c < NDOF; ++c) {
+        const T v = __shfl_up_sync(0xffffffffu, O[2][q][c], 1);
+        if (jy > 0) O[0][q][c] += v;
+      }
+    // x: the dx = 1 values of faces 0 and 1 go to the next element column
+#pragma unroll
+    for (int f = 0; f < 2; ++f)
+#pragma unroll
+      for (int dz = 0; dz < 2; ++dz)
+#pragma unroll
+        for (int c = 0; c < NDOF; ++c) xch[((f * 2 + dz) * NDOF + c) * NT + tid] = O[f][1 | (dz << 1)][c];
+    // epilogue inputs of node plane ez (their latency overlaps the barrier)
+    T bv[2][NDOF], dv[2][NDOF];
+    uint8_t fx[2] = {0, 0};
+#pragma unroll
+    for (int f = 0; f < 2; ++f) {
+      const bool o = owned && (f == 0 ? own0 : own1);
+      if (o) fx[f] = a.fix[nid + f];
+#pragma unroll
+      for (int c = 0; c < NDOF; ++c) {
+        bv[f][c] = (o && MODE != AM_Y) ? a.b[(nid + f) * NDOF + c] : T(0);
+        dv[f][c] = (o && MODE == AM_JACOBI) ? a.dinv[(nid + f) * NDOF + c] : T(0);
+      }
+    }
+    __syncthreads();
+    if (exl >= 1) {
+#pragma unroll
+      for (int f = 0; f < 2; ++f)
+#pragma unroll
+        for (int dz = 0; dz < 2; ++dz)
+#pragma unroll
+          for (int c = 0; c < NDOF; ++c)
+            O[f][dz << 1][c] += xch[((f * 2 + dz) * NDOF + c) * NT + tid - JY];
+    }
+    // z: dz = 0 completes node plane ez, dz = 1 starts plane ez + 1
+#pragma unroll
+    for (int f = 0; f < 2; ++f) {
+      const bool o = owned && (f == 0 ? own0 : own1);
+      if (o) {
+        const T* pu = us + s0 * SLOT + row + (f == 0 ? cf0 : cf1);
+#pragma unroll
+        for (int c = 0; c < NDOF; ++c) {
+          const T au = acc[f][c] + O[f][0][c];
+          T out;
+          if (MODE == AM_Y) out = au;
+          else if (MODE == AM_RES) out = bv[f][c] - au;
+          else out = pu[c * PLANE] + a.omega * dv[f][c] * (bv[f][c] - au);
+          out = ((fx[f] >> c) & 1) ? T(0) : out;
+          a.y[(nid + f) * NDOF + c] = out;
+          if (DOTK == DOT_ALPHA) dacc = fmaf(pu[c * PLANE], out, dacc);
+          else if (DOTK == DOT_RHO) dacc = fmaf(bv[f][c], out, dacc);
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < NDOF; ++c) acc[f][c] = O[f][2][c];
+    }
+    rhoA = rnA;
+    rhoB = rnB;
+    cp_async_wait_all();
+    __syncthreads();
+    const int t = s0;
+    s0 = s1; s1 = s2; s2 = t;
+  }
+  if constexpr (DOTK >= 0) {
+    __shared__ double sh[32];
+    __shared__ int last;
+    const double bs = block_sum((double)dacc, sh);
+    const unsigned nblk = gridDim.x * gridDim.y * gridDim.z;
+    const unsigned bid = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+    if (tid == 0) {
+      a.part[bid] = bs;
+      __threadfence();
+      last = (atomicAdd(&a.pst->ticket, 1u) == nblk - 1);
+    }
+    __syncthreads();
+    if (last) {
+      __threadfence();
+      const double tot = sum_partials(a.part, (int)nblk, sh);
+      if (tid == 0) {
+        pcg_dot_finish(a.pst, DOTK, tot);
+        a.pst->ticket = 0;
+      }
+    }
+  }
+}
+
 static int sm_count() {
   static const int n = [] {     // thread-safe one-time initialisation
     int dev = 0, v = 0;
@@ -509,8 +822,46 @@ static ZsShape zstream_shape(const Grid& g, bool fp64) {
   return s;
 }
 
+// the paired-element kernel: FP32 with a sector-form element product
+template <typename T, int KIND> constexpr bool use_zpair() {
+  return std::is_same<T, float>::value && KIND != EK_DENSE;
+}
+// its launch shape: 31 x 15 node columns, 3 resident CTAs per SM
+static ZsShape zpair_shape(const Grid& g) {
+  ZsShape s;
+  s.gy = (int)cdiv(g.nny, zp::OY);
+  s.gx = (int)cdiv(g.nnx, zp::OX);
+  const int target = sm_count() * 3;
+  const int cols = s.gx * s.gy;
+  const int chunks = std::max(1, std::min(g.nnz, target / cols));
+  s.zc = (int)cdiv(g.nnz, chunks);
+  s.chunks = (int)cdiv(g.nnz, s.zc);
+  return s;
+}
+// CTAs of the 3-D fine launch for (T, KIND) on g (fused dots need one
+// partial-sum slot per CTA)
+template <typename T, int KIND>
+static int64_t fine3d_ctas(const Grid& g) {
+  return use_zpair<T, KIND>() ? zpair_shape(g).ctas() : zstream_shape(g, sizeof(T) == 8).ctas();
+}
+
 template <int NDOF, typename T, typename S, int KIND, int MODE, int DOTK = -1>
 static void launch_zstream(const ApplyArgs<T, S>& a, cudaStream_t st) {
+  const int pk = std::is_same<T, double>::value ? PK_FINE_F64
+                 : (std::is_same<S, float>::value ? PK_FINE_F32 : PK_FINE_BF16);
+  if constexpr (use_zpair<T, KIND>()) {
+    constexpr size_t smem = zp::smem<NDOF>();
+    auto kern = k_fine_zpair<NDOF, S, KIND, MODE, DOTK>;
+    set_smem_limit((const void*)kern, (int)smem);
+    const ZsShape sh = zpair_shape(a.g);
+    if (DOTK >= 0 && sh.ctas() > RED_BLOCKS)
+      throw Error{EINVAL_, "fused dot: more CTAs than partial-sum slots"};
+    prof_begin(pk, st);
+    kern<<<dim3((unsigned)sh.gy, (unsigned)sh.gx, (unsigned)sh.chunks), zp::NT, smem, st>>>(a, sh.zc);
+    prof_end(pk, st);
+    TG_CHECK_LAUNCH();
+    return;
+  }
   constexpr size_t smem = zs::smem<NDOF, T, KIND>();
   auto kern = k_fine_zstream<NDOF, T, S, KIND, MODE, DOTK>;
   set_smem_limit((const void*)kern, (int)smem);
@@ -518,8 +869,6 @@ static void launch_zstream(const ApplyArgs<T, S>& a, cudaStream_t st) {
   const int gy = sh.gy, gx = sh.gx, chunks = sh.chunks, zc = sh.zc;
   if (DOTK >= 0 && sh.ctas() > RED_BLOCKS)
     throw Error{EINVAL_, "fused dot: more CTAs than partial-sum slots"};
-  const int pk = std::is_same<T, double>::value ? PK_FINE_F64
-                 : (std::is_same<S, float>::value ? PK_FINE_F32 : PK_FINE_BF16);
   prof_begin(pk, st);
   kern<<<dim3((unsigned)gy, (unsigned)gx, (unsigned)chunks), zs::NT, smem, st>>>(a, zc);
   prof_end(pk, st);
@@ -598,7 +947,7 @@ void fine_apply_dot(const FineOp& op, const S* scale, const T* u, T* y, const T*
              "fused dot: DOT_ALPHA with AM_Y or DOT_RHO with AM_JACOBI");
   const bool zstream = op.g.ndim == 3 && op.g.ndof == 3 && op.kind == EK_SECTOR_HEX8 &&
                        (int64_t)op.g.nnx * op.g.nny * 3 < (int64_t(1) << 31) &&
-                       zstream_shape(op.g, sizeof(T) == 8).ctas() <= RED_BLOCKS;
+                       fine3d_ctas<T, EK_SECTOR_HEX8>(op.g) <= RED_BLOCKS;
   if (!zstream) {   // other kernels (or more CTAs than partial slots): product, then dot
     fine_apply<T, S>(op, scale, u, y, b, dinv, omega, mode, st);
     dot<T, T>(op.g.ndofs(), dot_op == DOT_ALPHA ? u : b, y, part, pst, dot_op, st);
