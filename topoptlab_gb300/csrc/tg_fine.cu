@@ -497,11 +497,14 @@ __global__ void __launch_bounds__(zs::NT, sizeof(T) == 8 ? 2 : 4) k_fine_zstream
 // bit-reproducible.
 // ---------------------------------------------------------------------------
 namespace zp {
+// JY = 16: a warp is exactly two x-rows of pairs, so the y-neighbour of every
+// lane but the first of a row is lane - 1 of the same warp (the shuffle)
 constexpr int EXT = 16, JY = 16;            // threads: element columns in x, pairs in y
 constexpr int EYT = 2 * JY;                 // 32 elements in y
 constexpr int OX = EXT - 1, OY = EYT - 1;   // owned nodes per tile: 15 x 31
 constexpr int PX = EXT + 1, PY = EYT + 1;   // node rows / nodes per row incl. halo: 17 x 33
-constexpr int ODD = 17;                     // odd-y nodes of a row start here (even y: 0..16)
+constexpr int ODD = JY + 1;                 // odd-y nodes of a row start here (even y: 0..16)
+// the two x-rows of a warp land 16 banks apart for every face access
 constexpr int PITCH = 48;
 constexpr int PLANE = PX * PITCH;           // words per component plane
 constexpr int NT = EXT * JY;
@@ -579,9 +582,11 @@ __device__ __forceinline__ void face_xz(float (&F)[4][NDOF]) {
   }
 }
 
+// zc unused: blockIdx.z takes node planes [z nnz / gridDim.z, (z+1) nnz / gridDim.z)
 template <int NDOF, typename S, int KIND, int MODE, int DOTK = -1>
 __global__ void __launch_bounds__(zp::NT, 3) k_fine_zpair(ApplyArgs<float, S> a, int zc) {
   using namespace zp;
+  static_assert(32 % JY == 0, "the y shuffle needs warps made of whole rows of pairs");
   using T = float;
   constexpr int SLOT = NDOF * PLANE;
   constexpr int NCP = ncopy<NDOF>();
@@ -591,7 +596,9 @@ __global__ void __launch_bounds__(zp::NT, 3) k_fine_zpair(ApplyArgs<float, S> a,
   const Grid& g = a.g;
   const int tid = threadIdx.x;
   const int y0 = blockIdx.x * OY, x0 = blockIdx.y * OX;
-  const int zbeg = blockIdx.z * zc, zend = min(zbeg + zc, g.nnz);
+  (void)zc;
+  const int zbeg = (int)((int64_t)blockIdx.z * g.nnz / gridDim.z);
+  const int zend = (int)((int64_t)(blockIdx.z + 1) * g.nnz / gridDim.z);
   const int64_t pstride = (int64_t)g.nnx * g.nny * NDOF;
   const int64_t lstride = (int64_t)g.nex * g.ney;
 
@@ -826,16 +833,16 @@ static ZsShape zstream_shape(const Grid& g, bool fp64) {
 template <typename T, int KIND> constexpr bool use_zpair() {
   return std::is_same<T, float>::value && KIND != EK_DENSE;
 }
-// its launch shape: 31 x 15 node columns, 3 resident CTAs per SM
+// its launch shape: 31 x 15 node columns, as many z chunks (balanced plane
+// ranges) as fill one wave of 3 resident CTAs per SM
 static ZsShape zpair_shape(const Grid& g) {
   ZsShape s;
   s.gy = (int)cdiv(g.nny, zp::OY);
   s.gx = (int)cdiv(g.nnx, zp::OX);
   const int target = sm_count() * 3;
   const int cols = s.gx * s.gy;
-  const int chunks = std::max(1, std::min(g.nnz, target / cols));
-  s.zc = (int)cdiv(g.nnz, chunks);
-  s.chunks = (int)cdiv(g.nnz, s.zc);
+  s.chunks = std::max(1, std::min(g.nnz, target / cols));
+  s.zc = (int)cdiv(g.nnz, s.chunks);
   return s;
 }
 // CTAs of the 3-D fine launch for (T, KIND) on g (fused dots need one
