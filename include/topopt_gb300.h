@@ -149,6 +149,17 @@ int32_t tg_kmul(tg_ctx* ctx, const double* xPhys, const double* u, double* y, in
 /* K u = rhs on the free DOFs (solve_linsystem.py:20-365 slot).  u0 may be NULL. */
 int32_t tg_solve(tg_ctx* ctx, const double* xPhys, const double* rhs, const double* u0, double* u,
                  tg_solve_info* info);
+/* Adjoint solve and sensitivity of an objective that is not self-adjoint
+ * (topology_optimization.py:473-500): adj = K^-1 rhs_adj on the free DOFs,
+ * with the scale factors, multigrid hierarchy and coarsest inverse of the
+ * last state solve (tg_step or tg_solve) -- nothing is rebuilt, as the
+ * reference reuses its factorisation / preconditioner -- and, when dobj is
+ * not NULL, dobj_e = simp_dx(xPhys_e) adj_e^T KE u_e for the design of that
+ * solve (the reference's dobj accumulation).  u: the state of that solve
+ * (ndof); rhs_adj: the objective's adjoint right-hand side (the reference
+ * objectives' rhs_adj, e.g. objectives.py:121-157).  Not for padded grids. */
+int32_t tg_adjoint(tg_ctx* ctx, const double* u, const double* rhs_adj, double* adj, double* dobj,
+                   tg_solve_info* info);
 /* PCG on an assembled CSR matrix (indptr int64 [n+1], indices int32, data
  * FP64), Jacobi-preconditioned when jacobi != 0, stopping at
  * ||b - A x|| < max(atol, rtol ||b||): the pcg / solve_lin path for callers

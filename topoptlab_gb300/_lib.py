@@ -95,6 +95,7 @@ SIGNATURES = {
     "tg_cnn_eval": (C.c_int32, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float),
                                 C.POINTER(C.c_float), _dp, C.POINTER(C.c_float)]),
     "tg_cnn_infer": (C.c_int32, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "tg_adjoint": (C.c_int32, [C.c_void_p, _dp, _dp, _dp, _dp, C.POINTER(TgSolveInfo)]),
     "tg_csr_pcg": (C.c_int32, [C.c_int64, _i64p, _i32p, _dp, _dp, _dp, _dp, C.c_double,
                                C.c_double, C.c_int32, C.c_int32, C.POINTER(TgSolveInfo),
                                C.c_int32]),

@@ -202,6 +202,19 @@ class GpuProblem:
                                             _lib.dptr(dc)), "tg_compliance")
         return obj.value, dc
 
+    def adjoint(self, u, rhs_adj):
+        """Adjoint solve K adj = rhs_adj with the operator of the last state
+        solve (step / solve) and the sensitivity simp_dx(xPhys) adj_e^T KE u_e
+        of that design (topology_optimization.py:473-500): (adj, dobj, info)."""
+        uu = _lib.f64(u).reshape(-1)
+        rr = _lib.f64(rhs_adj).reshape(-1)
+        adj = np.empty(self.ndof)
+        dobj = np.empty(self.nel)
+        info = _lib.TgSolveInfo()
+        self._check(self._lib.tg_adjoint(self._h, _lib.dptr(uu), _lib.dptr(rr), _lib.dptr(adj),
+                                         _lib.dptr(dobj), C.byref(info)), "tg_adjoint")
+        return adj, dobj, {k: getattr(info, k) for k, _ in _lib.TgSolveInfo._fields_}
+
     def vcycle(self, xPhys, b, precision="fp64"):
         x = _lib.f64(xPhys).reshape(-1)
         bb = _lib.f64(b).reshape(-1)

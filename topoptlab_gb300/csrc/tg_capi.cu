@@ -252,6 +252,41 @@ int32_t tg_solve(tg_ctx* ctx, const double* xPhys, const double* rhs, const doub
   return rc;
 }
 
+int32_t tg_adjoint(tg_ctx* ctx, const double* u, const double* rhs_adj, double* adj, double* dobj,
+                   tg_solve_info* info) {
+  if (!ctx || !u || !rhs_adj || !adj) return TG_EINVAL;
+  tg::Ctx& c = ctx->c;
+  const int32_t rc = guarded(ctx, [&] {
+    require_unpadded(c, "tg_adjoint");
+    TG_REQUIRE(c.built, "tg_adjoint reuses the operator of a state solve: call tg_step or "
+                        "tg_solve first");
+    const int64_t nd = c.g.ndofs(), nel = c.g.nel();
+    tg::DevBuf<double> uu, b, x;
+    uu.alloc(nd);
+    b.alloc(nd);
+    x.alloc(nd);
+    h2d(uu.p, u, nd, c.st);
+    h2d(b.p, rhs_adj, nd, c.st);
+    tg::mask_vec_f64(c.g.nnodes(), c.g.ndof, c.op.fix, b, c.st);
+    tg::mask_vec_f64(c.g.nnodes(), c.g.ndof, c.op.fix, uu, c.st);
+    x.zero(c.st);
+    tg::solve(c, b, x);                 // the state solve's scale factors and hierarchy
+    d2h(adj, x.p, nd, c.st);
+    if (dobj) {
+      tg::fine_adjoint_sens(c.op, c.xsolved, uu, x, c.eps, c.penal, c.dc, c.st, c.flags.p);
+      d2h(dobj, c.dc.p, nel, c.st);
+    }
+  });
+  if (info) {
+    info->iters = c.last_iters;
+    info->vcycles = c.last_vcycles;
+    info->refinements = c.last_refine;
+    info->converged = c.last_converged;
+    info->rel_res = c.last_relres;
+  }
+  return rc;
+}
+
 int32_t tg_filter(tg_ctx* ctx, const double* x, const double* d, double* y, int32_t mode) {
   const bool pde = mode == 6 || mode == 7;
   if (!ctx || !y || mode < 0 || (mode > 3 && !pde) || (mode != 3 && !x) ||

@@ -327,7 +327,7 @@ void ctx_init(Ctx& c, const tg_problem& p) {
   if (c.padded) c.emb.alloc(std::max(rnd, rnel));
   // vectors
   c.f.alloc(nd * c.nload); c.u.alloc(nd * c.nload);
-  c.x.alloc(nel); c.xPhys.alloc(nel); c.xold.alloc(nel); c.xnew.alloc(nel);
+  c.x.alloc(nel); c.xPhys.alloc(nel); c.xold.alloc(nel); c.xnew.alloc(nel); c.xsolved.alloc(nel);
   c.dc.alloc(nel); c.dcf.alloc(nel); c.dv.alloc(nel); c.Hs.alloc(nel); c.S.alloc(3 * nel);
   c.s64.alloc(nel);
   if (mixed) { c.s32.alloc(nel); c.s16.alloc(nel); }
@@ -404,6 +404,8 @@ void ctx_init(Ctx& c, const tg_problem& p) {
 void set_density(Ctx& c, const double* xPhys) {
   ProfScope ps(PK_COARSE_BUILD, c.st);
   simp_scale(c.g.nel(), xPhys, c.eps, c.penal, c.s64, c.s32.p, c.s16.p, c.st, c.flags.p);
+  TG_CUDA(cudaMemcpyAsync(c.xsolved.p, xPhys, sizeof(double) * c.g.nel(), cudaMemcpyDeviceToDevice,
+                          c.st));
 }
 
 void build_hierarchy(Ctx& c) {
@@ -413,7 +415,10 @@ void build_hierarchy(Ctx& c) {
   ProfScope ps(PK_COARSE_BUILD, c.st);
   fine_dinv<double, double>(c.op, c.s64, f.dinv64, c.st);
   if (mixed) fine_dinv<float, __nv_bfloat16>(c.op, c.s16, f.dinv32, c.st);
-  if (c.precond != TG_PRECOND_GMG) return;
+  if (c.precond != TG_PRECOND_GMG) {
+    c.built = true;
+    return;
+  }
   // mixed: level operators in FP32 (they only serve the FP32 V-cycle, which
   // would round FP64 ones to FP32 anyway); the coarsest matrix is inverted in FP64
   for (int l = 1; l < c.L; ++l) {
@@ -440,6 +445,7 @@ void build_hierarchy(Ctx& c) {
   }
   ProfScope ps(PK_COARSE_INV, c.st);
   gj_inverse(c.Dc, c.nc, c.ldc, c.gjwork, c.st);
+  c.built = true;
 }
 
 // ---------------------------------------------------------------------------

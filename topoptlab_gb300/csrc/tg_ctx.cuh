@@ -68,6 +68,8 @@ struct Ctx {
   DevBuf<float> Q32;            // Q in FP32 (mixed: coarse operators built in FP32)
   DevBuf<float> KE32;
   DevBuf<double> f, u, x, xPhys, xold, xnew, dc, dcf, dv, Hs, S, s64;
+  DevBuf<double> xsolved;       // the design the scale factors and hierarchy were built for
+  bool built = false;           // a hierarchy exists (tg_adjoint reuses it)
   DevBuf<float> s32;
   DevBuf<__nv_bfloat16> s16;
   DevBuf<double> fw;            // filter weights

@@ -1123,4 +1123,61 @@ void fine_compliance(const FineOp& op, const double* xPhys, const double* u, dou
   TG_CHECK_LAUNCH();
 }
 
+// ---------------------------------------------------------------------------
+// adjoint sensitivity (FP64, dense element product)
+// ---------------------------------------------------------------------------
+template <int NDIM, int NDOF>
+__global__ void __launch_bounds__(256) k_adjoint_sens(Grid g, const double* __restrict__ xPhys,
+                                                     const double* __restrict__ u,
+                                                     const double* __restrict__ v,
+                                                     const double* __restrict__ KE, double eps,
+                                                     double penal, double* __restrict__ dobj,
+                                                     const int8_t* __restrict__ flags) {
+  constexpr int NC = 1 << NDIM;
+  constexpr int NE = NC * NDOF;
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= g.nel()) return;
+  if (flags && flags[e] == EL_OUTSIDE) {
+    dobj[e] = 0.0;
+    return;
+  }
+  const int ey = (int)(e % g.ney);
+  const int ex = (int)((e / g.ney) % g.nex);
+  const int ez = (int)(e / ((int64_t)g.ney * g.nex));
+  double ue[NE], ve[NE];
+#pragma unroll
+  for (int d = 0; d < NC; ++d) {
+    const int64_t n = g.node(ex + (d & 1), ey + ((d >> 1) & 1), (NDIM == 3) ? ez + ((d >> 2) & 1) : 0);
+#pragma unroll
+    for (int c = 0; c < NDOF; ++c) {
+      ue[d * NDOF + c] = u[n * NDOF + c];
+      ve[d * NDOF + c] = v[n * NDOF + c];
+    }
+  }
+  double s = 0.0;
+  for (int i = 0; i < NE; ++i) {
+    double t = 0.0;
+#pragma unroll
+    for (int j = 0; j < NE; ++j) t += __ldg(KE + i * NE + j) * ue[j];
+    s += ve[i] * t;
+  }
+  const double xv = xPhys[e];
+  const double dx = penal * (1.0 - eps) * ((penal == 3.0) ? xv * xv : pow(xv, penal - 1.0));
+  dobj[e] = dx * s;
+}
+
+void fine_adjoint_sens(const FineOp& op, const double* xPhys, const double* u, const double* v,
+                       double eps, double penal, double* dobj, cudaStream_t st,
+                       const int8_t* flags) {
+  const unsigned blocks = (unsigned)cdiv(op.g.nel(), 256);
+  switch (op.g.ndim * 10 + op.g.ndof) {
+    case 33: k_adjoint_sens<3, 3><<<blocks, 256, 0, st>>>(op.g, xPhys, u, v, op.KE64, eps, penal, dobj, flags); break;
+    case 31: k_adjoint_sens<3, 1><<<blocks, 256, 0, st>>>(op.g, xPhys, u, v, op.KE64, eps, penal, dobj, flags); break;
+    case 22: k_adjoint_sens<2, 2><<<blocks, 256, 0, st>>>(op.g, xPhys, u, v, op.KE64, eps, penal, dobj, flags); break;
+    case 21: k_adjoint_sens<2, 1><<<blocks, 256, 0, st>>>(op.g, xPhys, u, v, op.KE64, eps, penal, dobj, flags); break;
+    default: throw Error{EINVAL_, "unsupported (ndim, nnode_dof) combination"};
+  }
+  TG_CHECK_LAUNCH();
+}
+
 }  // namespace tg

@@ -57,6 +57,11 @@ constexpr int8_t EL_OUTSIDE = 3;
 // partial[b] = sum over the block's elements of simp(x_e) ce_e (padding
 // elements, flag EL_OUTSIDE, contribute nothing and get dc = 0)
 // (accumulate: dc and partial are added to, for a further load case)
+// dobj_e = simp_dx(xPhys_e) * v_e^T KE u_e (FP64): the sensitivity of an
+// objective with adjoint solution v (topology_optimization.py:473-500)
+void fine_adjoint_sens(const FineOp& op, const double* xPhys, const double* u, const double* v,
+                       double eps, double penal, double* dobj, cudaStream_t st,
+                       const int8_t* flags = nullptr);
 void fine_compliance(const FineOp& op, const double* xPhys, const double* u, double eps,
                      double penal, double* dc, double* partial, cudaStream_t st,
                      const int8_t* flags = nullptr, bool accumulate = false);
