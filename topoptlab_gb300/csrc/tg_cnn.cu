@@ -581,19 +581,7 @@ Cnn::Cnn(Ctx& c, int capacity, uint64_t seed) : ctx(&c) {
   gal.alloc(6); gal.zero(c.st);
   wsb.alloc(4); wsb.zero(c.st);
   rpart.alloc(RED_BLOCKS);
-  TG_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
-  TG_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
-  TG_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
   TG_CUDA(cudaStreamSynchronize(c.st));
-}
-
-Cnn::~Cnn() {
-  if (side) {
-    cudaStreamSynchronize(side);
-    cudaStreamDestroy(side);
-  }
-  if (ev_fork) cudaEventDestroy(ev_fork);
-  if (ev_join) cudaEventDestroy(ev_join);
 }
 
 void Cnn::forward(cudaStream_t st, bool split) {
@@ -872,8 +860,6 @@ __global__ void k_ws_apply(int64_t n, const double* ws, double* u, const double*
   if (i < n && ws[2] != 0.0) u[i] = ws[0] * u[i] + ws[1] * v2[i];
 }
 
-void Cnn::warm_start_join(Ctx& c) { TG_CUDA(cudaStreamWaitEvent(c.st, ev_join, 0)); }
-
 // Warm start and coarse-grid correction for the current design.  The
 // network's level-1 correction is prolongated to the fine grid (w = P y) and
 // combined with the previous displacement (v1 = u_prev) by the energy-optimal
@@ -885,9 +871,7 @@ void Cnn::warm_start_join(Ctx& c) { TG_CUDA(cudaStreamWaitEvent(c.st, ev_join, 0
 // direction is made K-orthogonal to w), a coarse-grid correction by one
 // extra basis vector.  Whether the learned start is kept is decided after the
 // first cycle of the solve, against the plain warm start's residual (solve()).
-void Cnn::warm_start(Ctx& c, bool combine, bool correction) {
-  TG_CUDA(cudaEventRecord(ev_fork, c.st));
-  TG_CUDA(cudaStreamWaitEvent(side, ev_fork, 0));
+void Cnn::warm_start(Ctx& c, bool combine, bool correction, cudaStream_t side) {
   // everything below is enqueued on the side stream (the helpers take the
   // context's stream member); the context's own stream comes back at the end
   struct Swap {
@@ -921,7 +905,6 @@ void Cnn::warm_start(Ctx& c, bool combine, bool correction) {
       TG_CHECK_LAUNCH();
     }
   }
-  TG_CUDA(cudaEventRecord(ev_join, c.st));
 }
 
 }  // namespace tg

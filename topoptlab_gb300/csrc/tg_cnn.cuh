@@ -39,14 +39,11 @@ struct Cnn {
   DevBuf<PCGState> gal;          // the five products of the 2x2 Galerkin combination
   DevBuf<double> wsb;            // c1, c2, valid of the last warm start
   DevBuf<double> rpart;          // reduction partials of the network's own dots
-  cudaStream_t side = nullptr;   // the warm start's stream
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   float lr = 1e-3f;
   int adam_t = 0;
   bool trained = false;
 
   Cnn(Ctx& c, int capacity, uint64_t seed);
-  ~Cnn();
   Cnn(const Cnn&) = delete;
   Cnn& operator=(const Cnn&) = delete;
   // split: FP32-level split-TF32 products (training, checks); otherwise TF32
@@ -65,12 +62,10 @@ struct Cnn {
   // with correction, c.pcg gets 1 / (w^T K w) and w deflates the FP32 PCG
   // (else 0).  The plain warm start's residual norm^2 stays in plain_rr()
   // (device) for the fallback test after the first cycle of the solve.
-  // The work runs on the network's own stream, forked from c.st once the
-  // design's scale factors are set; it does not touch the multigrid
-  // hierarchy, so it overlaps the hierarchy's build, and warm_start_join
-  // makes c.st wait for it before the solve.
-  void warm_start(Ctx& c, bool combine, bool correction);
-  void warm_start_join(Ctx& c);
+  // The work is enqueued on stream s (the context's side stream, which the
+  // caller has made wait for the design's scale factors); it does not touch
+  // the multigrid hierarchy, so it overlaps the hierarchy's build.
+  void warm_start(Ctx& c, bool combine, bool correction, cudaStream_t s);
   const double* plain_rr() const { return &sr.p->rr; }
 };
 

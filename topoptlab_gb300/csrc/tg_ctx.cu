@@ -32,6 +32,12 @@ Ctx::~Ctx() {
   if (ev1) cudaEventDestroy(ev1);
   if (tev0) cudaEventDestroy(tev0);
   if (tev1) cudaEventDestroy(tev1);
+  if (side) {
+    cudaStreamSynchronize(side);
+    cudaStreamDestroy(side);
+  }
+  if (sev_fork) cudaEventDestroy(sev_fork);
+  if (sev_join) cudaEventDestroy(sev_join);
   if (st) cudaStreamDestroy(st);
 }
 
@@ -208,6 +214,9 @@ void ctx_init(Ctx& c, const tg_problem& p) {
   c.dev = p.device;
   TG_CUDA(cudaSetDevice(c.dev));
   TG_CUDA(cudaStreamCreateWithFlags(&c.st, cudaStreamNonBlocking));
+  TG_CUDA(cudaStreamCreateWithFlags(&c.side, cudaStreamNonBlocking));
+  TG_CUDA(cudaEventCreateWithFlags(&c.sev_fork, cudaEventDisableTiming));
+  TG_CUDA(cudaEventCreateWithFlags(&c.sev_join, cudaEventDisableTiming));
   TG_CUDA(cudaEventCreate(&c.ev0));
   TG_CUDA(cudaEventCreate(&c.ev1));
   TG_CUDA(cudaEventCreate(&c.tev0));
@@ -807,6 +816,10 @@ static int pcg32_run(Ctx& c, double tol_abs, int maxit, int start) {
 
 void solve(Ctx& c, const double* b, double* u) {
   const int64_t n = c.g.ndofs();
+  // c.r / c.pcg_out already hold b - K u and its norm (formed beside the
+  // hierarchy build by ctx_step); consumed by this call only
+  const bool r_ready = c.r_ready;
+  c.r_ready = false;
   double bb;
   {
     pcg_reset(c.pcg_out, c.st);
@@ -838,8 +851,8 @@ void solve(Ctx& c, const double* b, double* u) {
     bool conv = false;
     double rr = 0.0;
     for (int k = 0; k < 64 && total < c.maxiter; ++k) {
-      fine_apply<double, double>(c.op, c.s64, u, c.r, b, nullptr, 0.0, AM_RES, c.st);
-      {
+      if (!(k == 0 && r_ready)) {      // else formed on the side stream during the build
+        fine_apply<double, double>(c.op, c.s64, u, c.r, b, nullptr, 0.0, AM_RES, c.st);
         ProfScope ps(PK_VECTOR, c.st);
         pcg_reset(c.pcg_out, c.st);
         dot<double, double>(n, c.r.p, c.r.p, c.part, c.pcg_out, DOT_RR, c.st);
@@ -932,15 +945,32 @@ void ctx_step(Ctx& c, tg_iter_out& out) {
   c.last_fallback = 0;
   c.last_warm_ratio = 0.0;
   c.ws_pending = false;
-  if (warm) {
-    c.cnn->warm_start(c, (lmask & TG_LEARNED_WARM_START) != 0,
-                      (lmask & TG_LEARNED_COARSE_CORRECTION) != 0);
-    c.ws_pending = true;
-  } else if (correction_vector(c)) {
-    set_correction(c.pcg, 0.0, c.st);     // no vector for this design: plain PCG
+  c.r_ready = false;
+  if (!warm && correction_vector(c)) set_correction(c.pcg, 0.0, c.st);   // plain PCG
+  // the mixed solve's first FP64 residual f - K u needs only the scale
+  // factors too: on the side stream (after the warm start, which changes u)
+  const bool side = c.precision == TG_PREC_MIXED && c.nload == 1;
+  if (side) {
+    TG_CUDA(cudaEventRecord(c.sev_fork, c.st));
+    TG_CUDA(cudaStreamWaitEvent(c.side, c.sev_fork, 0));
+    if (warm) {
+      c.cnn->warm_start(c, (lmask & TG_LEARNED_WARM_START) != 0,
+                        (lmask & TG_LEARNED_COARSE_CORRECTION) != 0, c.side);
+      c.ws_pending = true;
+    }
+    fine_apply<double, double>(c.op, c.s64, c.u, c.r, c.f, nullptr, 0.0, AM_RES, c.side);
+    {
+      ProfScope ps(PK_VECTOR, c.side);
+      pcg_reset(c.pcg_out, c.side);
+      dot<double, double>(g.ndofs(), c.r.p, c.r.p, c.part, c.pcg_out, DOT_RR, c.side);
+    }
+    TG_CUDA(cudaEventRecord(c.sev_join, c.side));
   }
   build_hierarchy(c);
-  if (warm) c.cnn->warm_start_join(c);
+  if (side) {
+    TG_CUDA(cudaStreamWaitEvent(c.st, c.sev_join, 0));
+    c.r_ready = true;
+  }
   // one solve per load case with the same hierarchy (topology_optimization.py:446-459)
   const int64_t nd = g.ndofs();
   int iters = 0, vcycles = 0, refine = 0;

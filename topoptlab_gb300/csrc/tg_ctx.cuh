@@ -115,6 +115,12 @@ struct Ctx {
   // the learned start of this step awaits its test after the first cycle;
   // the FP32 PCG graphs were captured for this deflation vector (null: none)
   bool ws_pending = false;
+  // side stream of a design step (learned warm start, then the first FP64
+  // residual of the mixed solve, beside the hierarchy build); r_ready: c.r
+  // and c.pcg_out hold f - K u and its norm for the solve that follows
+  cudaStream_t side = nullptr;
+  cudaEvent_t sev_fork = nullptr, sev_join = nullptr;
+  bool r_ready = false;
   int last_fallback = 0;
   double last_warm_ratio = 0.0;
   const float* g32_corr = nullptr;
