@@ -161,7 +161,8 @@ def _problem(precision, device, size=None, volfrac=None):
 FAMILIES = [(1, "fine_f64_residual"), (2, "fine_f32_kmul"), (3, "fine_bf16_jacobi"),
             (8, "stencil_level1_f32"), (4, "stencil_levels2plus_f32"), (5, "stencil_f64"),
             (6, "filter"), (7, "oc"), (9, "coarse_build"), (10, "coarse_inverse"),
-            (11, "vector"), (12, "transfer"), (13, "compliance"), (14, "learned_warm_start")]
+            (11, "vector"), (12, "transfer"), (13, "compliance"), (14, "learned_warm_start"),
+            (15, "coarse_tail")]
 ROOFLINE_KERNEL = {1: "k_fine_zstream FP64 residual b - K u",
                    2: "k_fine_zstream FP32 K.u (inner PCG)",
                    3: "k_fine_zstream FP32 damped-Jacobi sweep (BF16 densities)",

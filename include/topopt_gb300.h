@@ -266,8 +266,11 @@ int32_t tg_cnn_infer(tg_cnn* cnn, const float* x0, float* y);
  * elapsed milliseconds to *ms. */
 int32_t tg_timer(tg_ctx* ctx, int32_t op, double* ms);
 /* Event timing of one kernel family (0 off, 1 fine FP64 K.u, 2 fine FP32
- * K.u, 3 fine FP32 K.u with BF16 densities, 4 FP32 coarse stencil, 5 FP64
- * coarse stencil, 6 filter, 7 OC step); resets the accumulated time. */
+ * K.u, 3 fine FP32 K.u with BF16 densities, 4 FP32 coarse stencil (levels
+ * >= 2), 5 FP64 coarse stencil, 6 filter, 7 OC step, 8 FP32 level-1
+ * stencil, 9 coarse operator build, 10 coarsest inverse, 11 vector kernels,
+ * 12 transfers, 13 compliance, 14 learned warm start, 15 the V-cycle's
+ * cooperative bottom); resets the accumulated time. */
 int32_t tg_profile_kernel(int32_t kind);
 /* Kernel launches made by the library (all contexts) and the accumulated
  * device time / launch count of the profiled family; reset != 0 zeroes them. */
@@ -280,8 +283,21 @@ int32_t tg_stats(int32_t reset, int64_t* launches, double* prof_ms, int64_t* pro
  * TG_TUNE_OC_BARRIER_TIMEOUT: value != 0 makes the next OC bisection's grid
  * barrier wait for one block more than its grid holds, so every block's
  * bounded wait runs out (seconds) and the call returns TG_ETIMEOUT;
- * the switch clears itself.  Unknown keys or bad values return TG_EINVAL. */
-enum { TG_TUNE_STENCIL_SMALL_PAIRS = 1, TG_TUNE_OC_BARRIER_TIMEOUT = 2 };
+ * the switch clears itself.  TG_TUNE_COARSE_TAIL: value 1 runs the bottom
+ * of every V-cycle -- restriction into the last smoothed level, its sweeps,
+ * the coarsest dense solve and both prolongations -- as one cooperative
+ * launch with bounded grid barriers, one block per SM (value > 1: that many
+ * blocks); 0 (default) runs the separate kernels.  Same arithmetic, same
+ * results; on GB300 the separate launches inside the PCG graph are faster.
+ * TG_TUNE_TAIL_BARRIER_TIMEOUT:
+ * like TG_TUNE_OC_BARRIER_TIMEOUT for the next such launch (the solve or
+ * tg_vcycle call returns TG_ETIMEOUT).  Unknown keys return TG_EINVAL. */
+enum {
+  TG_TUNE_STENCIL_SMALL_PAIRS = 1,
+  TG_TUNE_OC_BARRIER_TIMEOUT = 2,
+  TG_TUNE_COARSE_TAIL = 3,
+  TG_TUNE_TAIL_BARRIER_TIMEOUT = 4
+};
 int32_t tg_tune(int32_t key, int64_t value);
 /* edofMat (elements/bilinear_quadrilateral.py:7-48, trilinear_hexahedron.py:7-58)
  * generated on the device; out has nel*(2^ndim*nnode_dof) int32 entries */

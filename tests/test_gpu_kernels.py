@@ -277,6 +277,70 @@ def test_vcycle_matches_oracle(gpu_lib, nelx, nely, nelz, kind):
     np.testing.assert_allclose(z, zr, rtol=0, atol=1e-10 * np.abs(zr).max())
 
 
+def _vcycle_tail(prob, x, b, precision, on):
+    from topoptlab_gb300 import _lib
+    lib = _lib.load()
+    assert lib.tg_tune(_lib.TG_TUNE_COARSE_TAIL, 1 if on else 0) == _lib.TG_OK
+    try:
+        return prob.vcycle(x, b, precision=precision)
+    finally:
+        lib.tg_tune(_lib.TG_TUNE_COARSE_TAIL, 0)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("nlevels", [3, 4])
+@pytest.mark.parametrize("nelx,nely,nelz,kind", [(32, 16, None, "elast"), (32, 32, None, "poisson"),
+                                                 (16, 8, 8, "elast"), (16, 16, 8, "poisson")])
+def test_coarse_tail_matches_separate_kernels(gpu_lib, precision, nlevels, nelx, nely, nelz, kind):
+    """The V-cycle's bottom two levels as one cooperative launch (restriction
+    into the last smoothed level, its sweeps, the coarsest dense solve, both
+    prolongations) compute the same values in the same order as the separate
+    kernels: the cycles agree bit for bit."""
+    rng = np.random.default_rng(17)
+    prob, KE, fixed, f, x, ndof = _setup(nelx, nely, nelz, kind, rng, nlevels=nlevels,
+                                         precision=precision)
+    mask = np.zeros(ndof, bool)
+    mask[fixed] = True
+    b = rng.standard_normal(ndof) * ~mask
+    try:
+        z_sep = _vcycle_tail(prob, x, b, precision, False)
+        z_tail = _vcycle_tail(prob, x, b, precision, True)
+    finally:
+        prob.close()
+    assert np.abs(z_sep).max() > 0
+    np.testing.assert_array_equal(z_tail, z_sep)
+
+
+def test_coarse_tail_barrier_wait_runs_out(gpu_lib):
+    """The cooperative V-cycle bottom's grid barriers are bounded: tg_tune
+    makes the next launch's first barrier wait for one block more than the
+    grid holds, every block polls until its limit, the error flag is set and
+    the call returns TG_ETIMEOUT (RuntimeError).  The barrier is reset, and
+    the next cycle on the same context is the separate kernels' cycle."""
+    import time
+    from topoptlab_gb300 import _lib
+    lib = _lib.load()
+    rng = np.random.default_rng(18)
+    prob, KE, fixed, f, x, ndof = _setup(16, 8, 8, "elast", rng, nlevels=3)
+    mask = np.zeros(ndof, bool)
+    mask[fixed] = True
+    b = rng.standard_normal(ndof) * ~mask
+    try:
+        assert lib.tg_tune(_lib.TG_TUNE_COARSE_TAIL, 1) == _lib.TG_OK
+        assert lib.tg_tune(_lib.TG_TUNE_TAIL_BARRIER_TIMEOUT, 1) == _lib.TG_OK
+        t0 = time.perf_counter()
+        with pytest.raises(RuntimeError, match="timed out"):
+            prob.vcycle(x, b)
+        assert time.perf_counter() - t0 < 60.0
+        z = prob.vcycle(x, b)
+        z_sep = _vcycle_tail(prob, x, b, "fp64", False)
+    finally:
+        lib.tg_tune(_lib.TG_TUNE_TAIL_BARRIER_TIMEOUT, 0)
+        lib.tg_tune(_lib.TG_TUNE_COARSE_TAIL, 0)
+        prob.close()
+    np.testing.assert_array_equal(z, z_sep)
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("nelx,nely,nelz,kind", [(32, 16, None, "elast"), (32, 32, None, "poisson"),
                                                  (16, 8, 8, "elast")])

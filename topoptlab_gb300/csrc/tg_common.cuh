@@ -97,7 +97,8 @@ enum ProfKind : int {
   PK_TRANSFER = 12,       // restriction, prolongation, coarsest dense apply
   PK_COMPLIANCE = 13,     // compliance and sensitivities
   PK_LEARNED = 14,        // learned warm start inference
-  PK_NKINDS = 15
+  PK_TAIL = 15,           // the V-cycle's bottom levels in one cooperative launch
+  PK_NKINDS = 16
 };
 void prof_begin(int kind, cudaStream_t st);
 void prof_end(int kind, cudaStream_t st);
@@ -136,6 +137,12 @@ int64_t launch_count();       // kernels launched so far
 // wait for one block more than its grid holds (its bounded wait runs out).
 int64_t tune_stencil_small_pairs();
 bool tune_take_oc_barrier_timeout();
+// the V-cycle's bottom (the last smoothed level and the coarsest solve) as
+// one cooperative launch (default off: on GB300 its nine grid barriers cost
+// more than the ten separate launches they replace inside the PCG graph),
+// and the one-shot barrier-timeout request for its next launch
+int tune_coarse_tail();         // 0 off, 1 one block per SM, > 1 that many blocks
+bool tune_take_tail_barrier_timeout();
 
 #define TG_REQUIRE(cond, msg)                                                \
   do {                                                                       \

@@ -297,6 +297,8 @@ void ctx_init(Ctx& c, const tg_problem& p) {
     c.ldc = cdiv(c.nc, 32) * 32;
     c.Dc.alloc(c.ldc * c.ldc);
     c.gjwork.alloc(32 * 32 + 2 * 32 * c.ldc);   // pivot tile, row panel R, saved panel X
+    c.tailbar.alloc(1);
+    TG_CUDA(cudaMemsetAsync(c.tailbar.p, 0, sizeof(GridBar), c.st));
   }
   const bool mixed = c.precision == TG_PREC_MIXED;
   for (int l = 0; l < c.L; ++l) {
@@ -525,18 +527,39 @@ template <typename T> void vcycle(Ctx& c, int l, const T* b, T* x, bool prescale
   level_apply<T>(c, l, bufs[cur], r, b, AM_RES);
   Level& w = *c.lv[l + 1];
   const bool fuse = l + 1 < c.L - 1;       // the coarsest level has no smoother
-  {
-    ProfScope ps(PK_TRANSFER, c.st);
-    if (fuse)
-      restrict_<T>(v.g, w.g, w.fix, r, LvBufs<T>::b(w), c.st, LvBufs<T>::dinv(w), LvBufs<T>::t(w),
-                   c.omega);
-    else
-      restrict_<T>(v.g, w.g, w.fix, r, LvBufs<T>::b(w), c.st);
-  }
-  vcycle<T>(c, l + 1, LvBufs<T>::b(w), LvBufs<T>::x(w), fuse);
-  {
-    ProfScope ps(PK_TRANSFER, c.st);
-    prolong_add<T>(v.g, w.g, v.fix, LvBufs<T>::x(w), bufs[cur], c.st);
+  // the two levels below this one (the last smoothed level, on the small-grid
+  // stencil, and the coarsest solve) in one cooperative launch
+  const int64_t tail_pairs = w.g.nnodes() * w.g.ndof;
+  if (l + 3 == c.L && tune_coarse_tail() && tail_pairs < tune_stencil_small_pairs() &&
+      tail_pairs <= TAIL_MAX_PAIRS) {
+    Level& k = *c.lv[c.L - 1];
+    TailArgs<T> a;
+    a.gp = v.g; a.gt = w.g; a.gc = k.g;
+    a.fixt = w.fix; a.fixc = k.fix; a.fixp = v.fix;
+    a.rp = r; a.xp = bufs[cur];
+    a.At = LvBufs<T>::A(w); a.dinvt = LvBufs<T>::dinv(w);
+    a.bt = LvBufs<T>::b(w); a.xt = LvBufs<T>::x(w); a.tt = LvBufs<T>::t(w);
+    a.rt = LvBufs<T>::r(w);
+    a.bc = LvBufs<T>::b(k); a.xc = LvBufs<T>::x(k);
+    a.Dc = c.Dc; a.nc = c.nc; a.ldc = c.ldc; a.part = c.gjwork;
+    a.omega = (T)c.omega; a.nsmooth = c.nsmooth; a.bar = c.tailbar;
+    a.blocks = tune_coarse_tail() > 1 ? tune_coarse_tail() : 0;
+    ProfScope ps(PK_TAIL, c.st);
+    coarse_tail<T>(a, c.st);
+  } else {
+    {
+      ProfScope ps(PK_TRANSFER, c.st);
+      if (fuse)
+        restrict_<T>(v.g, w.g, w.fix, r, LvBufs<T>::b(w), c.st, LvBufs<T>::dinv(w),
+                     LvBufs<T>::t(w), c.omega);
+      else
+        restrict_<T>(v.g, w.g, w.fix, r, LvBufs<T>::b(w), c.st);
+    }
+    vcycle<T>(c, l + 1, LvBufs<T>::b(w), LvBufs<T>::x(w), fuse);
+    {
+      ProfScope ps(PK_TRANSFER, c.st);
+      prolong_add<T>(v.g, w.g, v.fix, LvBufs<T>::x(w), bufs[cur], c.st);
+    }
   }
   // the fine level's last sweep of the FP32 cycle also forms the PCG dot b . x
   const bool fused_dot = dot_op >= 0 && l == 0 && std::is_same<T, float>::value;
@@ -814,6 +837,18 @@ static int pcg32_run(Ctx& c, double tol_abs, int maxit, int start) {
   return it;
 }
 
+void check_tail(Ctx& c) {
+  if (!c.tailbar.p) return;
+  int err = 0;
+  TG_CUDA(cudaMemcpyAsync(&err, &c.tailbar.p->err, sizeof(int), cudaMemcpyDeviceToHost, c.st));
+  TG_CUDA(cudaStreamSynchronize(c.st));
+  if (err) {
+    TG_CUDA(cudaMemsetAsync(c.tailbar.p, 0, sizeof(GridBar), c.st));
+    TG_CUDA(cudaStreamSynchronize(c.st));
+    throw Error{ETIMEOUT, "multigrid V-cycle: a grid barrier wait of the coarse levels timed out"};
+  }
+}
+
 void solve(Ctx& c, const double* b, double* u) {
   const int64_t n = c.g.ndofs();
   // c.r / c.pcg_out already hold b - K u and its norm (formed beside the
@@ -919,6 +954,7 @@ void solve(Ctx& c, const double* b, double* u) {
     read_pcg(c, c.pcg_out);
     c.last_relres = std::sqrt(c.h_pcg->rr) / bnorm;
   }
+  if (c.precond == TG_PRECOND_GMG) check_tail(c);
   if (!c.last_converged)
     throw Error{ENOTCONV, "gb300 pcg iteration did not converge (iterations: " +
                               std::to_string(c.last_iters) +

@@ -22,6 +22,8 @@
 //    design iteration by the block sweep operator in FP64 (16-wide pivots)
 //    and applied as one dense mat-vec per V-cycle.
 #include <algorithm>
+#include <atomic>
+
 #include "tg_ops.cuh"
 
 namespace tg {
@@ -130,6 +132,15 @@ __global__ void __launch_bounds__(NDOF * 256) k_stencil_apply(Grid g, int TY, in
   y[k] = out;
 }
 
+// Loads of vectors: through the read-only cache in separate launches; at L2
+// (coherent) inside the cooperative tail kernel, where the vector was written
+// by other blocks earlier in the same launch.
+template <bool CG, typename T>
+__device__ __forceinline__ T ldv(const T* p) {
+  if constexpr (CG) return __ldcg(p);
+  else return __ldg(p);
+}
+
 // Small levels (too few (row, node) pairs to hide the coefficient-load
 // latency): three threads per pair, each summing the 9 directions of one
 // neighbour plane (dz = -1, 0, +1; in 2-D three columns dx), the partial sums
@@ -137,7 +148,7 @@ __global__ void __launch_bounds__(NDOF * 256) k_stencil_apply(Grid g, int TY, in
 constexpr int SMALL_PAIRS = 128;
 // one block's work: pairs [vb * SMALL_PAIRS, (vb + 1) * SMALL_PAIRS) with
 // 3 * SMALL_PAIRS threads; ends with a barrier, so part can be reused
-template <int NDIM, int NDOF, typename T, int MODE>
+template <int NDIM, int NDOF, typename T, int MODE, bool CG = false>
 __device__ __forceinline__ void stencil_small_vb(const Grid& g, const T* __restrict__ A,
                                                  const T* __restrict__ u, T* __restrict__ y,
                                                  const T* __restrict__ b,
@@ -167,7 +178,7 @@ __device__ __forceinline__ void stencil_small_vb(const Grid& g, const T* __restr
       const int64_t m = v ? n + dz * sz + dx * sx + dy : n;
 #pragma unroll
       for (int cj = 0; cj < NDOF; ++cj) {
-        const T uu = __ldg(u + m * NDOF + cj);
+        const T uu = ldv<CG>(u + m * NDOF + cj);
         acc = fma(coef<NDIM, NDOF, T>(A, ld, d, ci, cj, n, m), v ? uu : T(0), acc);
       }
     }
@@ -179,8 +190,8 @@ __device__ __forceinline__ void stencil_small_vb(const Grid& g, const T* __restr
     const int64_t k = n * NDOF + ci;
     T out;
     if (MODE == AM_Y) out = s;
-    else if (MODE == AM_RES) out = b[k] - s;
-    else out = u[k] + omega * dinv[k] * (b[k] - s);
+    else if (MODE == AM_RES) out = ldv<CG>(b + k) - s;
+    else out = ldv<CG>(u + k) + omega * dinv[k] * (ldv<CG>(b + k) - s);
     y[k] = out;
   }
   __syncthreads();
@@ -574,7 +585,7 @@ template void stencil_expand<float>(const Grid&, const float*, double*, cudaStre
 // the 3^ndim fine nodes of the coarse node's support
 // (optionally fused with the coarse level's first smoothing step from a zero
 // guess, xc = omega * dinvc * bc)
-template <int NDIM, int NDOF, typename T>
+template <int NDIM, int NDOF, typename T, bool CG = false>
 __device__ __forceinline__ void restrict_one(const Grid& gf, const Grid& gc, const uint8_t* fixc,
                                              const T* __restrict__ rf, T* __restrict__ bc,
                                              const T* __restrict__ dinvc, T* __restrict__ xc,
@@ -592,7 +603,7 @@ __device__ __forceinline__ void restrict_one(const Grid& gf, const Grid& gc, con
     const int fx = 2 * ix + ax, fy = 2 * iy + ay, fz = 2 * iz + az;
     if (!in_grid(gf, fx, fy, fz)) continue;
     const T w = T((ax ? 0.5 : 1.0) * (ay ? 0.5 : 1.0) * (az ? 0.5 : 1.0));
-    acc += w * __ldg(rf + gf.node(fx, fy, fz) * NDOF + c);
+    acc += w * ldv<CG>(rf + gf.node(fx, fy, fz) * NDOF + c);
   }
   const T bv = ((fixc[I] >> c) & 1) ? T(0) : acc;
   bc[I * NDOF + c] = bv;
@@ -627,7 +638,7 @@ template void restrict_<float>(const Grid&, const Grid&, const uint8_t*, const f
 
 // prolongation: one thread per fine node, all components; the 1, 2, 4 or 8
 // coarse parents follow from the parity of the fine coordinates
-template <int NDIM, int NDOF, typename T>
+template <int NDIM, int NDOF, typename T, bool CG = false>
 __device__ __forceinline__ void prolong_one(const Grid& gf, const Grid& gc, const uint8_t* fixf,
                                             const T* __restrict__ xc, T* __restrict__ xf,
                                             int64_t i) {
@@ -645,7 +656,7 @@ __device__ __forceinline__ void prolong_one(const Grid& gf, const Grid& gc, cons
     if ((a && !ox) || (b && !oy) || (d && !oz)) continue;
     const int64_t I = gc.node(cx0 + a, cy0 + b, cz0 + d);
 #pragma unroll
-    for (int c = 0; c < NDOF; ++c) acc[c] += __ldg(xc + I * NDOF + c);
+    for (int c = 0; c < NDOF; ++c) acc[c] += ldv<CG>(xc + I * NDOF + c);
   }
   const uint8_t m = fixf[i];
 #pragma unroll
@@ -896,7 +907,7 @@ void gj_inverse(double* D, int64_t n, int64_t ld, double* work, cudaStream_t st)
 // Fixed rows of Dinv hold the identity and b is 0 there.
 constexpr int DA_CHUNKS = 8;
 // one warp: the partial sum of row `row` over column chunk `chunk`
-template <typename T>
+template <typename T, bool CG = false>
 __device__ __forceinline__ void dense_partial_one(const double* __restrict__ Dinv, int64_t n,
                                                   int64_t ld, const T* __restrict__ b,
                                                   double* __restrict__ part, int64_t row,
@@ -905,16 +916,16 @@ __device__ __forceinline__ void dense_partial_one(const double* __restrict__ Din
   const int64_t j0 = chunk * w, j1 = min(n, j0 + w);
   double acc = 0.0;
 #pragma unroll 4
-  for (int64_t j = j0 + lane; j < j1; j += 32) acc = fma(Dinv[row * ld + j], (double)b[j], acc);
+  for (int64_t j = j0 + lane; j < j1; j += 32) acc = fma(Dinv[row * ld + j], (double)ldv<CG>(b + j), acc);
   acc = warp_sum(acc);
   if (lane == 0) part[chunk * n + row] = acc;
 }
-template <typename T>
+template <typename T, bool CG = false>
 __device__ __forceinline__ void dense_sum_one(const double* __restrict__ part, int64_t n,
                                               T* __restrict__ x, int64_t row) {
   double s = 0.0;
 #pragma unroll
-  for (int k = 0; k < DA_CHUNKS; ++k) s += part[k * n + row];
+  for (int k = 0; k < DA_CHUNKS; ++k) s += ldv<CG>(part + k * n + row);
   x[row] = (T)s;
 }
 template <typename T>
@@ -940,5 +951,121 @@ void dense_apply(const double* Dinv, int64_t n, int64_t ld, const T* b, T* x, do
 }
 template void dense_apply<double>(const double*, int64_t, int64_t, const double*, double*, double*, cudaStream_t);
 template void dense_apply<float>(const double*, int64_t, int64_t, const float*, float*, double*, cudaStream_t);
+
+// ---------------------------------------------------------------------------
+// the bottom of the V-cycle in one cooperative launch
+// ---------------------------------------------------------------------------
+// Every phase is a grid-stride loop over the same work units as the separate
+// kernels (restrict_one, stencil_small_vb, dense_partial_one, dense_sum_one,
+// prolong_one), so each value is computed in the same order as with those
+// launches; grid_sync separates the phases.  One block per SM: the tail and
+// coarsest levels are small (a few thousand rows), so the launch and drain of
+// ~10 separate kernels per V-cycle, not their work, was the cost.
+template <int NDIM, int NDOF, typename T>
+__global__ void __launch_bounds__(3 * SMALL_PAIRS) k_coarse_tail(TailArgs<T> a) {
+  __shared__ T spart[3][SMALL_PAIRS];
+  const int64_t gtid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t gsz = (int64_t)gridDim.x * blockDim.x;
+  const int64_t rows_t = a.gt.nnodes() * NDOF;
+  const int64_t nvb = cdiv(rows_t, SMALL_PAIRS);
+  auto sweep = [&](const T* in, T* out, int mode) {
+    for (int64_t vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
+      if (mode == AM_JACOBI)
+        stencil_small_vb<NDIM, NDOF, T, AM_JACOBI, true>(a.gt, a.At, in, out, a.bt, a.dinvt, a.omega, vb, spart);
+      else
+        stencil_small_vb<NDIM, NDOF, T, AM_RES, true>(a.gt, a.At, in, out, a.bt, a.dinvt, a.omega, vb, spart);
+    }
+  };
+  // restriction into the tail level with its first step from zero (t = omega D^-1 b)
+  for (int64_t t = gtid; t < rows_t; t += gsz)
+    restrict_one<NDIM, NDOF, T, true>(a.gp, a.gt, a.fixt, a.rp, a.bt, a.dinvt, a.tt, a.omega, t);
+  if (!grid_sync(a.bar)) return;
+  T* bufs[2] = {a.xt, a.tt};
+  int cur = 1;
+  for (int s = 1; s < a.nsmooth; ++s) {
+    sweep(bufs[cur], bufs[1 - cur], AM_JACOBI);
+    cur = 1 - cur;
+    if (!grid_sync(a.bar)) return;
+  }
+  sweep(bufs[cur], a.rt, AM_RES);
+  if (!grid_sync(a.bar)) return;
+  // restriction to the coarsest level
+  const int64_t rows_c = a.gc.nnodes() * NDOF;
+  for (int64_t t = gtid; t < rows_c; t += gsz)
+    restrict_one<NDIM, NDOF, T, true>(a.gt, a.gc, a.fixc, a.rt, a.bc, nullptr, nullptr, T(0), t);
+  if (!grid_sync(a.bar)) return;
+  // coarsest solve: a warp per (row, column chunk), then the fixed-order sums
+  {
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = gtid >> 5, nw = gsz >> 5;
+    for (int64_t w = w0; w < a.nc * DA_CHUNKS; w += nw)
+      dense_partial_one<T, true>(a.Dc, a.nc, a.ldc, a.bc, a.part, w % a.nc, (int)(w / a.nc), lane);
+  }
+  if (!grid_sync(a.bar)) return;
+  for (int64_t r = gtid; r < a.nc; r += gsz) dense_sum_one<T, true>(a.part, a.nc, a.xc, r);
+  if (!grid_sync(a.bar)) return;
+  for (int64_t i = gtid; i < a.gt.nnodes(); i += gsz)
+    prolong_one<NDIM, NDOF, T, true>(a.gt, a.gc, a.fixt, a.xc, bufs[cur], i);
+  if (!grid_sync(a.bar)) return;
+  for (int s = 0; s < a.nsmooth; ++s) {
+    sweep(bufs[cur], bufs[1 - cur], AM_JACOBI);
+    cur = 1 - cur;
+    if (!grid_sync(a.bar)) return;
+  }
+  // the tail level's result (ends in xt for an even number of steps; the
+  // parent reads bufs[cur])
+  for (int64_t i = gtid; i < a.gp.nnodes(); i += gsz)
+    prolong_one<NDIM, NDOF, T, true>(a.gp, a.gt, a.fixp, bufs[cur], a.xp, i);
+}
+
+template <typename T>
+void coarse_tail(const TailArgs<T>& a, cudaStream_t st) {
+  TG_REQUIRE(a.gt.nnodes() * a.gt.ndof <= TAIL_MAX_PAIRS, "coarse_tail: tail level too large");
+  TG_REQUIRE(a.nsmooth >= 1, "coarse_tail: nsmooth >= 1");
+  TG_REQUIRE(a.gc.ndofs() == a.nc && a.ldc >= a.nc, "coarse_tail: coarsest matrix size");
+  int dev = 0, nsm = 0;
+  TG_CUDA(cudaGetDevice(&dev));
+  TG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const void* fn = nullptr;
+  int slot = 0;
+  switch (a.gt.ndim * 10 + a.gt.ndof) {
+    case 33: fn = (const void*)k_coarse_tail<3, 3, T>; slot = 0; break;
+    case 31: fn = (const void*)k_coarse_tail<3, 1, T>; slot = 1; break;
+    case 22: fn = (const void*)k_coarse_tail<2, 2, T>; slot = 2; break;
+    case 21: fn = (const void*)k_coarse_tail<2, 1, T>; slot = 3; break;
+    default: throw Error{EINVAL_, "unsupported (ndim, nnode_dof)"};
+  }
+  static std::atomic<int> fits[4] = {};      // resident blocks per SM, found once per variant
+  int per_sm = fits[slot].load(std::memory_order_relaxed);
+  if (!per_sm) {
+    TG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 3 * SMALL_PAIRS, 0));
+    TG_REQUIRE(per_sm >= 1, "coarse_tail: kernel does not fit on an SM");
+    fits[slot].store(per_sm, std::memory_order_relaxed);
+  }
+  if (tune_take_tail_barrier_timeout()) {
+    // the first barrier waits for one block more than the grid holds (the
+    // same count OC's bounded-wait test uses), so every wait runs out
+    static const unsigned int big = 0x40000000u;
+    TG_CUDA(cudaMemcpyAsync(&a.bar->count, &big, sizeof(big), cudaMemcpyHostToDevice, st));
+  }
+  // all blocks co-resident (the cooperative launch refuses more)
+  const unsigned blocks = (unsigned)std::min(a.blocks > 0 ? a.blocks : nsm, nsm * per_sm);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(blocks);
+  cfg.blockDim = dim3(3 * SMALL_PAIRS);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  TailArgs<T> args = a;
+  void* kargs[] = {(void*)&args};
+  TG_CUDA(cudaLaunchKernelExC(&cfg, fn, kargs));
+  TG_CHECK_LAUNCH();
+}
+template void coarse_tail<float>(const TailArgs<float>&, cudaStream_t);
+template void coarse_tail<double>(const TailArgs<double>&, cudaStream_t);
 
 }  // namespace tg

@@ -104,6 +104,35 @@ template <typename T>
 void prolong_add(const Grid& gf, const Grid& gc, const uint8_t* fixf, const T* xc, T* xf,
                  cudaStream_t st);
 
+// The bottom of a V-cycle in one cooperative launch: restriction of the
+// parent level's residual rp into the tail level (with its first smoothing
+// step from zero), nsmooth - 1 Jacobi sweeps, the residual, restriction to
+// the coarsest level, the coarsest solve (dense FP64 inverse), prolongation,
+// nsmooth Jacobi sweeps, and prolongation of the tail level's iterate into
+// the parent's xp -- phases separated by bounded grid barriers (bar->err set
+// when one times out).  The tail level must use the small-grid stencil.
+template <typename T> struct TailArgs {
+  Grid gp, gt, gc;                         // parent, tail and coarsest grids
+  const uint8_t *fixt, *fixc, *fixp;
+  const T* rp;                             // parent residual
+  T* xp;                                   // parent iterate (+= P x_t)
+  const T* At;                             // tail stencil (half-stored)
+  const T* dinvt;
+  T *bt, *xt, *tt, *rt;                    // tail vectors
+  T *bc, *xc;                              // coarsest vectors
+  const double* Dc;                        // coarsest inverse
+  int64_t nc, ldc;
+  double* part;                            // >= 8 * nc doubles
+  T omega;
+  int nsmooth;
+  int blocks;                              // 0: one per SM
+  GridBar* bar;
+};
+template <typename T>
+void coarse_tail(const TailArgs<T>& a, cudaStream_t st);
+// the largest (node, DOF) row count of a tail level the fused kernel takes
+constexpr int64_t TAIL_MAX_PAIRS = 65536;
+
 // coarsest level: dense matrix (fixed DOFs -> identity) and its inverse
 template <typename T>
 void stencil_to_dense(const Grid& g, const uint8_t* fix, const T* A, double* D, int64_t n,

@@ -64,9 +64,13 @@ int prof_kind() { return g_kind; }
 namespace {
 std::atomic<int64_t> g_small_pairs{150000};
 std::atomic<int> g_oc_timeout{0};
+std::atomic<int> g_tail{0};
+std::atomic<int> g_tail_timeout{0};
 }  // namespace
 int64_t tune_stencil_small_pairs() { return g_small_pairs.load(std::memory_order_relaxed); }
 bool tune_take_oc_barrier_timeout() { return g_oc_timeout.exchange(0) != 0; }
+int tune_coarse_tail() { return g_tail.load(std::memory_order_relaxed); }
+bool tune_take_tail_barrier_timeout() { return g_tail_timeout.exchange(0) != 0; }
 
 namespace {
 thread_local ProfCapture* g_cap = nullptr;
@@ -175,6 +179,13 @@ extern "C" int32_t tg_tune(int32_t key, int64_t value) {
       return TG_OK;
     case TG_TUNE_OC_BARRIER_TIMEOUT:
       tg::g_oc_timeout.store(value != 0 ? 1 : 0);
+      return TG_OK;
+    case TG_TUNE_COARSE_TAIL:
+      if (value < 0 || value > 4096) return TG_EINVAL;
+      tg::g_tail.store((int)value);
+      return TG_OK;
+    case TG_TUNE_TAIL_BARRIER_TIMEOUT:
+      tg::g_tail_timeout.store(value != 0 ? 1 : 0);
       return TG_OK;
     default:
       return TG_EINVAL;
