@@ -277,6 +277,35 @@ def test_vcycle_matches_oracle(gpu_lib, nelx, nely, nelz, kind):
     np.testing.assert_allclose(z, zr, rtol=0, atol=1e-10 * np.abs(zr).max())
 
 
+@pytest.mark.parametrize("n", [37, 300, 1188])
+@pytest.mark.parametrize("cond", [1e2, 1e6, 1e9])
+def test_dense_inverse_fp64_and_double_word(gpu_lib, n, cond):
+    """The coarsest-level inverse (symmetric block sweep) in FP64 and in
+    double-word FP32 arithmetic against LAPACK on SPD matrices of a given
+    condition number.  Bound on the largest entry error of the inverse,
+    relative to its largest entry: cond * 2^-42 for double-word (about 48
+    significant bits), cond * 2^-46 for FP64 (LAPACK's own inverse is off by
+    about cond * 2^-53 as well)."""
+    import ctypes as C
+    from topoptlab_gb300 import _lib
+    lib = _lib.load()
+    rng = np.random.default_rng(int(n + np.log10(cond)))
+    Q, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    lam = np.logspace(0, -np.log10(cond), n)
+    A = (Q * lam) @ Q.T
+    A = 0.5 * (A + A.T)
+    ref = np.linalg.inv(A)
+    nrm = np.abs(ref).max()
+    for mode, bound in ((0, 2.0 ** -46), (1, 2.0 ** -42)):
+        X = np.empty((n, n))
+        rc = lib.tg_dense_inverse(_lib.dptr(np.ascontiguousarray(A)), n, _lib.dptr(X), mode, 0)
+        assert rc == _lib.TG_OK, lib.tg_last_error(None)
+        err = np.abs(X - ref).max() / nrm
+        print(f"n={n} cond={cond:.0e} mode={mode} err={err:.3e} err/cond={err / cond:.3e}")
+        assert err < cond * bound, (mode, err)
+        np.testing.assert_array_equal(X, X.T)
+
+
 def _vcycle_tail(prob, x, b, precision, on):
     from topoptlab_gb300 import _lib
     lib = _lib.load()

@@ -105,6 +105,7 @@ SIGNATURES = {
     "tg_profile_kernel": (C.c_int32, [C.c_int32]),
     "tg_stats": (C.c_int32, [C.c_int32, _i64p, _dp, _i64p]),
     "tg_tune": (C.c_int32, [C.c_int32, C.c_int64]),
+    "tg_dense_inverse": (C.c_int32, [_dp, C.c_int64, _dp, C.c_int32, C.c_int32]),
     "tg_edofmat": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _i32p,
                                C.c_int32]),
 }

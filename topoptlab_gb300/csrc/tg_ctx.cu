@@ -455,7 +455,8 @@ void build_hierarchy(Ctx& c) {
   }
   }
   ProfScope ps(PK_COARSE_INV, c.st);
-  gj_inverse(c.Dc, c.nc, c.ldc, c.gjwork, c.st);
+  if (mixed && c.L > 1) gj_inverse_dw(c.Dc, c.nc, c.ldc, c.gjwork, c.st);
+  else gj_inverse(c.Dc, c.nc, c.ldc, c.gjwork, c.st);
   c.built = true;
 }
 

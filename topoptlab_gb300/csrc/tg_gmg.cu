@@ -901,6 +901,208 @@ void gj_inverse(double* D, int64_t n, int64_t ld, double* work, cudaStream_t st)
   TG_CHECK_LAUNCH();
 }
 
+// ---------------------------------------------------------------------------
+// the same block sweep in double-word arithmetic on the FP32 pipes
+// ---------------------------------------------------------------------------
+// GB300 issues about 2 FP64 FMAs per SM per clock against 128 FP32 ones.  A
+// double-word number is the unevaluated sum h + l of two FP32 numbers (about
+// 48 significant bits); its error-free building blocks are Knuth's TwoSum,
+// Dekker's FastTwoSum and the FMA-based TwoProd, and the accurate DW + DW
+// and DW x DW of Joldes, Muller and Popescu, "Tight and rigorous error bounds
+// for basic building blocks of double-word arithmetic" (ACM TOMS 44, 2017,
+// Algorithms 6 and 12).  The update's 16-term sums follow the compensated
+// dot product of Ogita, Rump and Oishi ("Accurate sum and dot product", SIAM
+// J. Sci. Comput. 26, 2005), extended by the cross terms of DW operands.
+// Every operation is an explicit round-to-nearest intrinsic, so none is
+// contracted into an FMA.  A matrix element is a float2 (h, l) in the same
+// 8 bytes as the FP64 element it replaces.
+struct DW {
+  float h, l;
+};
+__device__ __forceinline__ DW two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ DW fast_two_sum(float a, float b) {   // |a| >= |b| or a == 0
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ DW dw_add(DW x, DW y) {
+  const DW s = two_sum(x.h, y.h);
+  const DW t = two_sum(x.l, y.l);
+  const DW v = fast_two_sum(s.h, __fadd_rn(s.l, t.h));
+  return fast_two_sum(v.h, __fadd_rn(t.l, v.l));
+}
+__device__ __forceinline__ DW dw_neg(DW x) { return {-x.h, -x.l}; }
+__device__ __forceinline__ DW dw_mul(DW x, DW y) {
+  const float ch = __fmul_rn(x.h, y.h);
+  const float cl1 = __fmaf_rn(x.h, y.h, -ch);
+  const float tl1 = __fmaf_rn(x.h, y.l, __fmul_rn(x.l, y.l));
+  const float cl2 = __fmaf_rn(x.l, y.h, tl1);
+  return fast_two_sum(ch, __fadd_rn(cl1, cl2));
+}
+// 1 / a: the correctly rounded FP32 reciprocal r0 of a.h, then one Newton
+// step r0 + r0 (1 - a r0) with the residual 1 - a r0 formed in DW
+__device__ __forceinline__ DW dw_rcp(DW a) {
+  const float r0 = __frcp_rn(a.h);
+  const DW p = dw_mul(a, DW{r0, 0.f});
+  const DW e = dw_add(DW{1.f, 0.f}, dw_neg(p));
+  return fast_two_sum(r0, __fmul_rn(r0, __fadd_rn(e.h, e.l)));
+}
+// compensated sum of products: (sh, sl) += x y
+__device__ __forceinline__ void dw_dot_step(float& sh, float& sl, DW x, DW y) {
+  const float p = __fmul_rn(x.h, y.h);
+  float pe = __fmaf_rn(x.h, y.h, -p);
+  pe = __fmaf_rn(x.h, y.l, pe);
+  pe = __fmaf_rn(x.l, y.h, pe);
+  const DW s = two_sum(sh, p);
+  sh = s.h;
+  sl = __fadd_rn(sl, __fadd_rn(s.l, pe));
+}
+__device__ __forceinline__ DW ld_dw(const float2* p) {
+  const float2 v = *p;
+  return {v.x, v.y};
+}
+__device__ __forceinline__ void st_dw(float2* p, DW v) { *p = make_float2(v.h, v.l); }
+
+// gj_tile_inverse in DW (same step structure and barriers)
+template <int TB>
+__device__ __forceinline__ void dw_tile_inverse(float2 (&a)[TB][TB + 1], float2 (&b)[TB][TB + 1],
+                                                DW (&rpiv)[2], int i, int j) {
+  if (i == 0 && j == 0) rpiv[0] = dw_rcp(ld_dw(&a[0][0]));
+  __syncthreads();
+  for (int p = 0; p < TB; p += 2) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      float2 (&src)[TB][TB + 1] = h ? b : a;
+      float2 (&dst)[TB][TB + 1] = h ? a : b;
+      const int q = p + h;
+      const DW rp = rpiv[h];
+      const DW aiq = ld_dw(&src[i][q]), aqj = ld_dw(&src[q][j]);
+      DW v;
+      if (i == q && j == q) v = rp;
+      else if (i == q) v = dw_mul(aqj, rp);
+      else if (j == q) v = dw_neg(dw_mul(aiq, rp));
+      else v = dw_add(ld_dw(&src[i][j]), dw_neg(dw_mul(aiq, dw_mul(aqj, rp))));
+      st_dw(&dst[i][j], v);
+      if (i == q + 1 && j == q + 1) rpiv[h ^ 1] = dw_rcp(v);
+      __syncthreads();
+    }
+  }
+}
+
+// k_sw_panel / k_sw_update in DW on float2 storage
+template <int TB>
+__global__ void __launch_bounds__(TB * TB) k_dw_panel(const float2* D, int64_t ld, int k,
+                                                     float2* P, float2* R, float2* Xb) {
+  __shared__ float2 a[TB][TB + 1], xs[TB][TB + 1], tb[TB][TB + 1];
+  __shared__ DW rpiv[2];
+  const int jb = blockIdx.x;
+  const int i = threadIdx.y, j = threadIdx.x;
+  a[i][j] = D[(int64_t)(k * TB + i) * ld + k * TB + j];
+  if (jb != k) {
+    if (k < jb) xs[i][j] = D[(int64_t)(k * TB + i) * ld + jb * TB + j];
+    else xs[j][i] = D[(int64_t)(jb * TB + i) * ld + k * TB + j];
+  }
+  __syncthreads();
+  dw_tile_inverse<TB>(a, tb, rpiv, i, j);
+  if (jb == k) {
+    P[i * TB + j] = a[i][j];
+    return;
+  }
+  float sh = 0.f, sl = 0.f;
+#pragma unroll
+  for (int m = 0; m < TB; ++m) dw_dot_step(sh, sl, ld_dw(&a[i][m]), ld_dw(&xs[m][j]));
+  st_dw(&R[(int64_t)i * ld + jb * TB + j], two_sum(sh, sl));
+  Xb[(int64_t)i * ld + jb * TB + j] = xs[i][j];
+}
+
+template <int TB>
+__global__ void __launch_bounds__(TB * TB) k_dw_update(float2* D, int64_t ld, int k,
+                                                      const float2* P, const float2* R,
+                                                      const float2* Xb) {
+  int ib, jb;
+  tri_tile(blockIdx.x, ib, jb);
+  const int i = threadIdx.y, j = threadIdx.x;
+  if (ib == k && jb == k) {
+    const float2 v = P[i * TB + j];
+    D[(int64_t)(k * TB + i) * ld + k * TB + j] = make_float2(-v.x, -v.y);
+    return;
+  }
+  if (ib == k) {
+    D[(int64_t)(k * TB + i) * ld + jb * TB + j] = R[(int64_t)i * ld + jb * TB + j];
+    return;
+  }
+  __shared__ float2 xs[TB][TB + 1], rs[TB][TB + 1];
+  if (jb == k) {
+    rs[i][j] = R[(int64_t)i * ld + ib * TB + j];
+    __syncthreads();
+    D[(int64_t)(ib * TB + i) * ld + k * TB + j] = rs[j][i];
+    return;
+  }
+  xs[i][j] = Xb[(int64_t)i * ld + ib * TB + j];
+  rs[i][j] = R[(int64_t)i * ld + jb * TB + j];
+  __syncthreads();
+  float sh = 0.f, sl = 0.f;
+#pragma unroll
+  for (int m = 0; m < TB; ++m) dw_dot_step(sh, sl, ld_dw(&xs[m][i]), ld_dw(&rs[m][j]));
+  float2* d = D + (int64_t)(ib * TB + i) * ld + jb * TB + j;
+  st_dw(d, dw_add(ld_dw(d), dw_neg(two_sum(sh, sl))));
+}
+
+// FP64 -> DW in place (h = the FP64 value rounded to FP32, l = the rounded rest)
+__global__ void k_dw_split(double* D, int64_t n) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const double v = D[e];
+  const float h = __double2float_rn(v);
+  const float l = __double2float_rn(v - (double)h);
+  reinterpret_cast<float2*>(D)[e] = make_float2(h, l);
+}
+// k_sw_mirror reading DW and writing FP64 in place: each block reads only its
+// own upper tile (before its barrier) and the lower tiles it writes are read
+// by no block
+__global__ void __launch_bounds__(GJB * GJB) k_dw_mirror(double* D, int64_t ld) {
+  const int ib = blockIdx.y, jb = blockIdx.x;
+  if (ib > jb) return;
+  __shared__ double ts[GJB][GJB + 1];
+  const int i = threadIdx.y, j = threadIdx.x;
+  const int64_t e = (int64_t)(ib * GJB + i) * ld + jb * GJB + j;
+  const float2 f = reinterpret_cast<const float2*>(D)[e];
+  const double v = -((double)f.x + (double)f.y);
+  ts[i][j] = v;
+  __syncthreads();
+  if (ib == jb) {
+    const int ri = i / SWB, cj = j / SWB;
+    const double w = ri > cj ? ts[j][i] : (ri < cj ? v : 0.5 * (v + ts[j][i]));
+    D[e] = w;
+  } else {
+    D[e] = v;
+    D[(int64_t)(jb * GJB + i) * ld + ib * GJB + j] = ts[j][i];
+  }
+}
+
+void gj_inverse_dw(double* D, int64_t n, int64_t ld, double* work, cudaStream_t st) {
+  TG_REQUIRE(ld % GJB == 0, "dense leading dimension must be a multiple of 32");
+  const int nb = (int)(ld / SWB);
+  float2* Df = reinterpret_cast<float2*>(D);
+  float2* P = reinterpret_cast<float2*>(work);
+  float2* R = P + SWB * SWB;
+  float2* Xb = R + SWB * ld;
+  k_dw_split<<<(unsigned)cdiv(ld * ld, 256), 256, 0, st>>>(D, ld * ld);
+  const dim3 thr(SWB, SWB);
+  const unsigned tiles = (unsigned)(nb * (nb + 1) / 2);
+  for (int k = 0; k < nb; ++k) {
+    k_dw_panel<SWB><<<nb, thr, 0, st>>>(Df, ld, k, P, R, Xb);
+    k_dw_update<SWB><<<tiles, thr, 0, st>>>(Df, ld, k, P, R, Xb);
+  }
+  const int nm = (int)(ld / GJB);
+  k_dw_mirror<<<dim3(nm, nm), dim3(GJB, GJB), 0, st>>>(D, ld);
+  count_launches(2 * (int64_t)nb + 1);   // and the split; the mirror is counted below
+  TG_CHECK_LAUNCH();
+}
+
 // x = Dinv b: a warp per (row, column chunk) writes a partial sum, a second
 // kernel adds the DA_CHUNKS partials of a row in fixed order (deterministic;
 // 8x the parallelism of a warp per row on the ~1200-row coarsest matrix).

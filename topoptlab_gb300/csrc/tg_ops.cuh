@@ -139,6 +139,10 @@ void stencil_to_dense(const Grid& g, const uint8_t* fix, const T* A, double* D, 
                       int64_t ld, cudaStream_t st);
 // work: 32 * 32 + 2 * 32 * ld doubles (enough for pivot blocks up to 32)
 void gj_inverse(double* D, int64_t n, int64_t ld, double* work, cudaStream_t st);
+// the same in double-word FP32 arithmetic (about 48 significant bits; same
+// work buffer): mixed-precision contexts, whose coarsest matrix holds FP32
+// values and whose V-cycle runs in FP32
+void gj_inverse_dw(double* D, int64_t n, int64_t ld, double* work, cudaStream_t st);
 template <typename T>
 void dense_apply(const double* Dinv, int64_t n, int64_t ld, const T* b, T* x,
                  double* work /* >= 8*n */, cudaStream_t st);
