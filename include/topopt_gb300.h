@@ -285,10 +285,15 @@ int32_t tg_stats(int32_t reset, int64_t* launches, double* prof_ms, int64_t* pro
  * bounded wait runs out (seconds) and the call returns TG_ETIMEOUT;
  * the switch clears itself.  TG_TUNE_COARSE_TAIL: value 1 runs the bottom
  * of every V-cycle -- restriction into the last smoothed level, its sweeps,
- * the coarsest dense solve and both prolongations -- as one cooperative
- * launch with bounded grid barriers, one block per SM (value > 1: that many
- * blocks); 0 (default) runs the separate kernels.  Same arithmetic, same
- * results; on GB300 the separate launches inside the PCG graph are faster.
+ * the coarsest dense solve and both prolongations -- as one launch of one
+ * thread-block cluster (up to 16 CTAs, hardware cluster barriers between
+ * the phases); 2 as one cooperative launch with bounded grid barriers, one
+ * block per SM (value > 2: that many blocks); 0 runs the separate kernels.
+ * Same arithmetic, same results.
+ * TG_TUNE_STENCIL_TMA: value 1 runs the FP32 3-D coarse sweeps of levels
+ * too large for the small-grid kernel with TMA-staged coefficients (value
+ * > 1: at most value - 1 node rows per CTA); 0 (default) runs the
+ * register-path kernel.  Same results.
  * TG_TUNE_TAIL_BARRIER_TIMEOUT:
  * like TG_TUNE_OC_BARRIER_TIMEOUT for the next such launch (the solve or
  * tg_vcycle call returns TG_ETIMEOUT).  Unknown keys return TG_EINVAL. */
@@ -296,7 +301,8 @@ enum {
   TG_TUNE_STENCIL_SMALL_PAIRS = 1,
   TG_TUNE_OC_BARRIER_TIMEOUT = 2,
   TG_TUNE_COARSE_TAIL = 3,
-  TG_TUNE_TAIL_BARRIER_TIMEOUT = 4
+  TG_TUNE_TAIL_BARRIER_TIMEOUT = 4,
+  TG_TUNE_STENCIL_TMA = 5
 };
 int32_t tg_tune(int32_t key, int64_t value);
 /* edofMat (elements/bilinear_quadrilateral.py:7-48, trilinear_hexahedron.py:7-58)

@@ -306,25 +306,58 @@ def test_dense_inverse_fp64_and_double_word(gpu_lib, n, cond):
         np.testing.assert_array_equal(X, X.T)
 
 
-def _vcycle_tail(prob, x, b, precision, on):
+@pytest.mark.parametrize("nlevels", [2, 3])
+@pytest.mark.parametrize("nelx,nely,nelz,kind", [(16, 8, 8, "elast"), (32, 16, 16, "elast"),
+                                                 (24, 16, 8, "poisson"), (8, 124, 4, "poisson")])
+def test_stencil_tma_matches_register_path(gpu_lib, nlevels, nelx, nely, nelz, kind):
+    """FP32 3-D coarse sweeps with TMA-staged coefficients (every coarse level
+    forced onto the large-grid path) compute the same products in the same
+    order as the register-path kernel: mixed V-cycles agree bit for bit."""
     from topoptlab_gb300 import _lib
     lib = _lib.load()
-    assert lib.tg_tune(_lib.TG_TUNE_COARSE_TAIL, 1 if on else 0) == _lib.TG_OK
+    rng = np.random.default_rng(19)
+    prob, KE, fixed, f, x, ndof = _setup(nelx, nely, nelz, kind, rng, nlevels=nlevels,
+                                         precision="mixed")
+    mask = np.zeros(ndof, bool)
+    mask[fixed] = True
+    b = rng.standard_normal(ndof) * ~mask
+    out = {}
+    try:
+        assert lib.tg_tune(_lib.TG_TUNE_STENCIL_SMALL_PAIRS, 0) == _lib.TG_OK
+        for on in (0, 1):
+            assert lib.tg_tune(_lib.TG_TUNE_STENCIL_TMA, on) == _lib.TG_OK
+            out[on] = prob.vcycle(x, b, precision="mixed")
+    finally:
+        lib.tg_tune(_lib.TG_TUNE_STENCIL_TMA, 1)
+        lib.tg_tune(_lib.TG_TUNE_STENCIL_SMALL_PAIRS, 150000)
+        prob.close()
+    assert np.abs(out[0]).max() > 0
+    np.testing.assert_array_equal(out[1], out[0])
+
+
+def _vcycle_tail(prob, x, b, precision, mode):
+    from topoptlab_gb300 import _lib
+    lib = _lib.load()
+    assert lib.tg_tune(_lib.TG_TUNE_COARSE_TAIL, mode) == _lib.TG_OK
     try:
         return prob.vcycle(x, b, precision=precision)
     finally:
         lib.tg_tune(_lib.TG_TUNE_COARSE_TAIL, 0)
 
 
+@pytest.mark.parametrize("mode", [1, 2])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("nlevels", [3, 4])
 @pytest.mark.parametrize("nelx,nely,nelz,kind", [(32, 16, None, "elast"), (32, 32, None, "poisson"),
                                                  (16, 8, 8, "elast"), (16, 16, 8, "poisson")])
-def test_coarse_tail_matches_separate_kernels(gpu_lib, precision, nlevels, nelx, nely, nelz, kind):
-    """The V-cycle's bottom two levels as one cooperative launch (restriction
-    into the last smoothed level, its sweeps, the coarsest dense solve, both
-    prolongations) compute the same values in the same order as the separate
-    kernels: the cycles agree bit for bit."""
+def test_coarse_tail_matches_separate_kernels(gpu_lib, mode, precision, nlevels, nelx, nely, nelz,
+                                              kind):
+    """The V-cycle's bottom two levels as one launch (restriction into the
+    last smoothed level, its sweeps, the coarsest dense solve, both
+    prolongations), phases separated by a thread-block cluster's barrier
+    (mode 1) or a cooperative grid's bounded barrier (mode 2), compute the
+    same values in the same order as the separate kernels: the cycles agree
+    bit for bit."""
     rng = np.random.default_rng(17)
     prob, KE, fixed, f, x, ndof = _setup(nelx, nely, nelz, kind, rng, nlevels=nlevels,
                                          precision=precision)
@@ -332,8 +365,8 @@ def test_coarse_tail_matches_separate_kernels(gpu_lib, precision, nlevels, nelx,
     mask[fixed] = True
     b = rng.standard_normal(ndof) * ~mask
     try:
-        z_sep = _vcycle_tail(prob, x, b, precision, False)
-        z_tail = _vcycle_tail(prob, x, b, precision, True)
+        z_sep = _vcycle_tail(prob, x, b, precision, 0)
+        z_tail = _vcycle_tail(prob, x, b, precision, mode)
     finally:
         prob.close()
     assert np.abs(z_sep).max() > 0
@@ -341,7 +374,7 @@ def test_coarse_tail_matches_separate_kernels(gpu_lib, precision, nlevels, nelx,
 
 
 def test_coarse_tail_barrier_wait_runs_out(gpu_lib):
-    """The cooperative V-cycle bottom's grid barriers are bounded: tg_tune
+    """The cooperative V-cycle bottom's grid barriers (mode 2) are bounded: tg_tune
     makes the next launch's first barrier wait for one block more than the
     grid holds, every block polls until its limit, the error flag is set and
     the call returns TG_ETIMEOUT (RuntimeError).  The barrier is reset, and
@@ -355,14 +388,14 @@ def test_coarse_tail_barrier_wait_runs_out(gpu_lib):
     mask[fixed] = True
     b = rng.standard_normal(ndof) * ~mask
     try:
-        assert lib.tg_tune(_lib.TG_TUNE_COARSE_TAIL, 1) == _lib.TG_OK
+        assert lib.tg_tune(_lib.TG_TUNE_COARSE_TAIL, 2) == _lib.TG_OK
         assert lib.tg_tune(_lib.TG_TUNE_TAIL_BARRIER_TIMEOUT, 1) == _lib.TG_OK
         t0 = time.perf_counter()
         with pytest.raises(RuntimeError, match="timed out"):
             prob.vcycle(x, b)
         assert time.perf_counter() - t0 < 60.0
         z = prob.vcycle(x, b)
-        z_sep = _vcycle_tail(prob, x, b, "fp64", False)
+        z_sep = _vcycle_tail(prob, x, b, "fp64", 0)
     finally:
         lib.tg_tune(_lib.TG_TUNE_TAIL_BARRIER_TIMEOUT, 0)
         lib.tg_tune(_lib.TG_TUNE_COARSE_TAIL, 0)

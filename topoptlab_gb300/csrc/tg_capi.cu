@@ -396,7 +396,7 @@ int32_t tg_vcycle(tg_ctx* ctx, const double* xPhys, const double* b, double* x, 
                  "an FP64 V-cycle needs an fp64 context (mixed contexts build FP32 levels)");
       tg::vcycle<double>(c, 0, c.r, c.z);
       d2h(x, c.z.p, nd, c.st);
-      tg::check_tail(c);
+      tg::check_waits(c);
     } else {
       TG_REQUIRE(c.precision == TG_PREC_MIXED, "FP32 V-cycle needs a mixed-precision context");
       tg::d2f(nd, c.r, c.r32, c.st);
@@ -404,7 +404,7 @@ int32_t tg_vcycle(tg_ctx* ctx, const double* xPhys, const double* b, double* x, 
       std::vector<float> tmp(nd);
       d2h(tmp.data(), c.z32.p, nd, c.st);
       for (int64_t i = 0; i < nd; ++i) x[i] = tmp[i];
-      tg::check_tail(c);
+      tg::check_waits(c);
     }
   });
 }

@@ -28,6 +28,9 @@ struct Grid {
   int nex, ney, nez;     // elements per axis (nez = 1 in 2-D)
   int nnx, nny, nnz;     // nodes per axis (nnz = 1 in 2-D)
   __host__ __device__ int64_t nnodes() const { return (int64_t)nnx * nny * nnz; }
+  // stride between the coefficient arrays of an assembled stencil: nnodes
+  // rounded up to 32, so every array starts 128-byte aligned (TMA copies)
+  __host__ __device__ int64_t slds() const { return (nnodes() + 31) / 32 * 32; }
   __host__ __device__ int64_t ndofs() const { return nnodes() * ndof; }
   __host__ __device__ int64_t nel() const { return (int64_t)nex * ney * nez; }
   __host__ __device__ int64_t node(int x, int y, int z) const {
@@ -141,7 +144,7 @@ bool tune_take_oc_barrier_timeout();
 // one cooperative launch (default off: on GB300 its nine grid barriers cost
 // more than the ten separate launches they replace inside the PCG graph),
 // and the one-shot barrier-timeout request for its next launch
-int tune_coarse_tail();         // 0 off, 1 one block per SM, > 1 that many blocks
+int tune_coarse_tail();   // 0 off, 1 one cluster, 2 cooperative (one block per SM), > 2 that many blocks
 bool tune_take_tail_barrier_timeout();
 
 #define TG_REQUIRE(cond, msg)                                                \

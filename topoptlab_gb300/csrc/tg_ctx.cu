@@ -306,7 +306,7 @@ void ctx_init(Ctx& c, const tg_problem& p) {
     const int64_t n = v.g.ndofs();
     v.fix.alloc(v.g.nnodes());
     TG_CUDA(cudaMemcpy(v.fix.p, fixl[l].data(), fixl[l].size(), cudaMemcpyHostToDevice));
-    const int64_t ns = v.g.nnodes() * stencil_half_dirs(g.ndim) * g.ndof * g.ndof;
+    const int64_t ns = v.g.slds() * stencil_half_dirs(g.ndim) * g.ndof * g.ndof;
     // mixed precision: the coarse operators (levels >= 1) exist in FP32 only,
     // built in FP32 for the FP32 V-cycle; the fine level keeps its FP64 data
     const bool last = (l == c.L - 1) && c.precond == TG_PRECOND_GMG;
@@ -544,7 +544,9 @@ template <typename T> void vcycle(Ctx& c, int l, const T* b, T* x, bool prescale
     a.bc = LvBufs<T>::b(k); a.xc = LvBufs<T>::x(k);
     a.Dc = c.Dc; a.nc = c.nc; a.ldc = c.ldc; a.part = c.gjwork;
     a.omega = (T)c.omega; a.nsmooth = c.nsmooth; a.bar = c.tailbar;
-    a.blocks = tune_coarse_tail() > 1 ? tune_coarse_tail() : 0;
+    const int mode = tune_coarse_tail();
+    a.cluster = mode == 1 ? 16 : 0;
+    a.blocks = mode > 2 ? mode : 0;
     ProfScope ps(PK_TAIL, c.st);
     coarse_tail<T>(a, c.st);
   } else {
@@ -838,7 +840,9 @@ static int pcg32_run(Ctx& c, double tol_abs, int maxit, int start) {
   return it;
 }
 
-void check_tail(Ctx& c) {
+void check_waits(Ctx& c) {
+  if (take_wait_error(c.st))
+    throw Error{ETIMEOUT, "multigrid V-cycle: a bounded wait for a TMA copy timed out"};
   if (!c.tailbar.p) return;
   int err = 0;
   TG_CUDA(cudaMemcpyAsync(&err, &c.tailbar.p->err, sizeof(int), cudaMemcpyDeviceToHost, c.st));
@@ -955,7 +959,7 @@ void solve(Ctx& c, const double* b, double* u) {
     read_pcg(c, c.pcg_out);
     c.last_relres = std::sqrt(c.h_pcg->rr) / bnorm;
   }
-  if (c.precond == TG_PRECOND_GMG) check_tail(c);
+  if (c.precond == TG_PRECOND_GMG) check_waits(c);
   if (!c.last_converged)
     throw Error{ENOTCONV, "gb300 pcg iteration did not converge (iterations: " +
                               std::to_string(c.last_iters) +

@@ -144,9 +144,10 @@ void build_hierarchy(Ctx& c);     // uses c.s64 / c.s32 / c.s16 of the current x
 void set_density(Ctx& c, const double* xPhys_dev);   // scale factors for xPhys
 // solve K u = b (b, u device FP64, u holds the warm start)
 void solve(Ctx& c, const double* b, double* u);
-// TG_ETIMEOUT (and a reset barrier) if a grid barrier of the V-cycle's
-// cooperative bottom timed out since the last check; synchronises c.st
-void check_tail(Ctx& c);
+// TG_ETIMEOUT (and a reset flag or barrier) if a bounded wait of a V-cycle
+// kernel (TMA copy, grid barrier of the cooperative bottom) ran out since the
+// last check; synchronises c.st
+void check_waits(Ctx& c);
 // prescaled: the level's scratch buffer already holds omega D^-1 b (fused
 // into the restriction that produced b); dot_op >= 0: also the PCG dot b . x
 // of the result into c.pcg (DOT_RHO), fused into the last fine sweep

@@ -23,6 +23,7 @@
 //    and applied as one dense mat-vec per V-cycle.
 #include <algorithm>
 #include <atomic>
+#include <cuda.h>
 
 #include "tg_ops.cuh"
 
@@ -90,7 +91,7 @@ __global__ void __launch_bounds__(NDOF * 256) k_stencil_apply(Grid g, int TY, in
   T* us = reinterpret_cast<T*>(smem_raw);
   const int RY = TY + 2, PL = (TX + 2) * RY;
   const int y0 = blockIdx.x * TY, x0 = blockIdx.y * TX, z = blockIdx.z;
-  const int64_t ld = g.nnodes();
+  const int64_t ld = g.slds();
   const int tid = threadIdx.x;
   // stage u (global order: component fastest)
   for (int i = tid; i < NDOF * NP * PL; i += blockDim.x) {
@@ -155,7 +156,7 @@ __device__ __forceinline__ void stencil_small_vb(const Grid& g, const T* __restr
                                                  const T* __restrict__ dinv, T omega, int64_t vb,
                                                  T (&part)[3][SMALL_PAIRS]) {
   const int slot = threadIdx.x % SMALL_PAIRS, pz = threadIdx.x / SMALL_PAIRS;
-  const int64_t ld = g.nnodes();
+  const int64_t ld = g.nnodes(), lda = g.slds();
   const int64_t t = vb * SMALL_PAIRS + slot;
   const bool active = t < ld * NDOF;
   T acc = T(0);
@@ -179,7 +180,7 @@ __device__ __forceinline__ void stencil_small_vb(const Grid& g, const T* __restr
 #pragma unroll
       for (int cj = 0; cj < NDOF; ++cj) {
         const T uu = ldv<CG>(u + m * NDOF + cj);
-        acc = fma(coef<NDIM, NDOF, T>(A, ld, d, ci, cj, n, m), v ? uu : T(0), acc);
+        acc = fma(coef<NDIM, NDOF, T>(A, lda, d, ci, cj, n, m), v ? uu : T(0), acc);
       }
     }
   }
@@ -207,6 +208,256 @@ __global__ void __launch_bounds__(3 * SMALL_PAIRS) k_stencil_small(Grid g, const
   stencil_small_vb<NDIM, NDOF, T, MODE>(g, A, u, y, b, dinv, omega, blockIdx.x, part);
 }
 
+// ---------------------------------------------------------------------------
+// 3-D FP32 stencil sweep with TMA-staged coefficients
+// ---------------------------------------------------------------------------
+// k_stencil_apply waits on its 81 coefficient loads per row one after another
+// (long-scoreboard stalls).  Here one thread of the CTA issues, per direction
+// d, one 2-D TMA copy of the NDOF^2 coefficient arrays of that direction over
+// the CTA's node range into shared memory: a CTA owns TX whole y-rows of a
+// plane, nodes [n0, n0 + P) contiguous, and a lower direction's blocks are
+// read at the neighbour range [n0 + off(d), n0 + off(d) + P).  The tensor map
+// views the stencil as (node, array) with the 128-byte-aligned array stride
+// slds; each copy starts at the range start rounded down to a multiple of 4
+// nodes (the TMA rule for 4-byte elements) and reads BX >= P + 3 nodes, zeros
+// beyond the grid.  Three mbarriers (dz = -1, 0, +1) let the rows start on the
+// first nine directions while the rest arrive; u is staged as in
+// k_stencil_apply.  Same products in the same order as k_stencil_apply, so
+// the results are bit-identical.  Every wait is bounded (about a second of
+// %globaltimer); a wait that runs out sets the library's wait-error flag,
+// waits once more for the copies in flight and leaves.
+__device__ int g_wait_err = 0;
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint64_t limit_ns) {
+  const uint32_t a = smem_u32(bar);
+  const uint64_t t0 = global_ns();
+  while (true) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done) : "r"(a), "r"(parity) : "memory");
+    if (done) return true;
+    if (global_ns() - t0 > limit_ns) return false;
+  }
+}
+
+constexpr int STMA_PT = 128;           // node slots per CTA at most (threads = NDOF * PT)
+constexpr int STMA_SMEM_MAX = 112 * 1024;
+
+template <int NDOF, int MODE, int PT>
+__global__ void __launch_bounds__(NDOF * PT) k_stencil_tma(const __grid_constant__ CUtensorMap tmA,
+                                                                Grid g, int TX, int BX, int tstride,
+                                                                const float* __restrict__ u,
+                                                                float* __restrict__ y,
+                                                                const float* __restrict__ b,
+                                                                const float* __restrict__ dinv,
+                                                                float omega) {
+  constexpr int NB = NDOF * NDOF;
+  constexpr int C = 13;
+  extern __shared__ __align__(128) unsigned char stma_smem[];
+  // 128-byte aligned start (the launch adds 128 bytes for this)
+  unsigned char* base = stma_smem + ((128u - (smem_u32(stma_smem) & 127u)) & 127u);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(base);
+  float* tiles = reinterpret_cast<float*>(base + 128);
+  float* us = tiles + 27 * tstride;
+  const int x0 = blockIdx.x * TX, z = blockIdx.y;
+  const int TXe = min(TX, g.nnx - x0);
+  const int P = TXe * g.nny;
+  const int64_t n0 = g.node(x0, 0, z);
+  const int64_t sx = g.nny, sz = (int64_t)g.nny * g.nnx;
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bar[k])) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (tid == 0) {
+    const uint32_t bytes = (uint32_t)(BX * NB * 4);
+    for (int gz = 0; gz < 3; ++gz) {
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                   ::"r"(smem_u32(&bar[gz])), "r"(9 * bytes) : "memory");
+      for (int e = 0; e < 9; ++e) {
+        const int d = gz * 9 + e;
+        int dx, dy, dz;
+        dir_xyz(d, 3, dx, dy, dz);
+        const int64_t off = (d >= C) ? 0 : dz * sz + dx * sx + dy;
+        const int xs = (int)((n0 + off) & ~(int64_t)3);
+        const int krow = (d >= C ? d - C : C - d) * NB;
+        asm volatile(
+            "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+            " [%0], [%1, {%2, %3}], [%4];"
+            ::"r"(smem_u32(tiles + d * tstride)), "l"(reinterpret_cast<uint64_t>(&tmA)),
+              "r"(xs), "r"(krow), "r"(smem_u32(&bar[gz]))
+            : "memory");
+      }
+    }
+  }
+  // u of planes z-1..z+1, rows x0-1..x0+TX, y -1..nny (zeros outside the grid)
+  const int RY = g.nny + 2, PL = (TX + 2) * RY;
+  for (int i = tid; i < NDOF * 3 * PL; i += blockDim.x) {
+    const int c = i % NDOF, hy = (i / NDOF) % RY, hx = (i / (NDOF * RY)) % (TX + 2);
+    const int pz = i / (NDOF * PL);
+    const int gx = x0 - 1 + hx, gy = -1 + hy, gz = z - 1 + pz;
+    float v = 0.f;
+    if (in_grid(g, gx, gy, gz)) v = __ldg(u + g.node(gx, gy, gz) * NDOF + c);
+    us[(c * 3 + pz) * PL + hx * RY + hy] = v;
+  }
+  __syncthreads();
+  const int ci = tid / PT, p = tid % PT;
+  const bool active = p < P;
+  const int tx = p / g.nny, ty = p % g.nny;
+  const float* uc = us + PL + (tx + 1) * RY + (ty + 1);     // centre, plane z
+  float acc = 0.f;
+  bool ok = true;
+#pragma unroll
+  for (int gz = 0; gz < 3; ++gz) {
+    if (!mbar_wait_bounded(&bar[gz], 0, 1000000000ull)) {
+      ok = false;
+      break;
+    }
+    if (active) {
+#pragma unroll
+      for (int e = 0; e < 9; ++e) {
+        const int d = gz * 9 + e;
+        int dx, dy, dz;
+        dir_xyz(d, 3, dx, dy, dz);
+        const int64_t off = (d >= C) ? 0 : dz * sz + dx * sx + dy;
+        const int xi = p + (int)((n0 + off) & 3);
+        const float* tl = tiles + d * tstride + xi;
+        const int so = dz * PL + dx * RY + dy;
+#pragma unroll
+        for (int cj = 0; cj < NDOF; ++cj) {
+          const int r = (d >= C) ? ci * NDOF + cj : cj * NDOF + ci;
+          acc = fmaf(tl[r * BX], uc[cj * 3 * PL + so], acc);
+        }
+      }
+    }
+  }
+  if (!ok) {
+    if (tid == 0) atomicExch(&g_wait_err, 1);
+    for (int gz = 0; gz < 3; ++gz) mbar_wait_bounded(&bar[gz], 0, 1000000000ull);
+    return;
+  }
+  if (!active) return;
+  const int64_t n = n0 + p;
+  const int64_t k = n * NDOF + ci;
+  float out;
+  if (MODE == AM_Y) out = acc;
+  else if (MODE == AM_RES) out = b[k] - acc;
+  else out = uc[ci * 3 * PL] + omega * dinv[k] * (b[k] - acc);
+  y[k] = out;
+}
+
+namespace {
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                   const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                   const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    TG_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                             cudaEnableDefault, &q));
+    TG_REQUIRE(q == cudaDriverEntryPointSuccess && p, "cuTensorMapEncodeTiled unavailable");
+    return reinterpret_cast<EncodeTiledFn>(p);
+  }();
+  return fn;
+}
+// rows TX per CTA and the copy width BX for the TMA sweep, 0 when it does not apply
+struct StmaShape {
+  int TX = 0, BX = 0, tstride = 0, PT = 0;
+  size_t smem = 0;
+};
+std::atomic<int> g_stma_on{0};
+StmaShape stma_shape(const Grid& g) {
+  StmaShape s;
+  if (g.ndim != 3 || (g.ndof != 3 && g.ndof != 1)) return s;
+  const int nb = g.ndof * g.ndof;
+  const int cap = g_stma_on.load(std::memory_order_relaxed) > 1 ? g_stma_on.load() - 1 : 1 << 20;
+  for (int tx = std::min(std::min(STMA_PT / g.nny, g.nnx), cap); tx >= 1; --tx) {
+    const int bx = (tx * g.nny + 3 + 3) / 4 * 4;
+    if (bx > 256) continue;
+    const int ts = (bx * nb + 31) / 32 * 32;
+    const size_t sm = 256 + sizeof(float) * (27 * (size_t)ts + (size_t)g.ndof * 3 * (tx + 2) * (g.nny + 2));
+    if (sm <= (size_t)STMA_SMEM_MAX) {
+      s.TX = tx; s.BX = bx; s.tstride = ts; s.smem = sm;
+      s.PT = tx * g.nny <= 64 ? 64 : 128;
+      return s;
+    }
+  }
+  return s;
+}
+}  // namespace
+
+void tune_set_stencil_tma(int on) { g_stma_on.store(on); }
+
+int take_wait_error(cudaStream_t st) {
+  int v = 0;
+  TG_CUDA(cudaMemcpyFromSymbolAsync(&v, g_wait_err, sizeof(int), 0, cudaMemcpyDeviceToHost, st));
+  TG_CUDA(cudaStreamSynchronize(st));
+  if (v) {
+    static const int z = 0;
+    TG_CUDA(cudaMemcpyToSymbolAsync(g_wait_err, &z, sizeof(int), 0, cudaMemcpyHostToDevice, st));
+    TG_CUDA(cudaStreamSynchronize(st));
+  }
+  return v;
+}
+
+static bool stencil_apply_tma(const Grid& g, const float* A, const float* u, float* y,
+                              const float* b, const float* dinv, double omega, int mode,
+                              cudaStream_t st) {
+  if (!g_stma_on.load(std::memory_order_relaxed)) return false;
+  const StmaShape s = stma_shape(g);
+  if (!s.TX) return false;
+  TG_REQUIRE((reinterpret_cast<uintptr_t>(A) & 127) == 0, "stencil arrays must be 128-byte aligned");
+  CUtensorMap tm;
+  const cuuint64_t dims[2] = {(cuuint64_t)g.nnodes(), (cuuint64_t)(14 * g.ndof * g.ndof)};
+  const cuuint64_t strides[1] = {(cuuint64_t)g.slds() * sizeof(float)};
+  const cuuint32_t box[2] = {(cuuint32_t)s.BX, (cuuint32_t)(g.ndof * g.ndof)};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUresult r = encode_tiled()(&tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(A),
+                                    dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                    CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  TG_REQUIRE(r == CUDA_SUCCESS, "cuTensorMapEncodeTiled failed for the stencil");
+  const dim3 grid((unsigned)cdiv(g.nnx, s.TX), (unsigned)g.nnz);
+  const unsigned nt = (unsigned)(g.ndof * s.PT);
+  const float om = (float)omega;
+#define TG_ST(NF, M, PTV)                                                                      \
+  {                                                                                            \
+    static bool attr = false;                                                                  \
+    if (!attr) {                                                                               \
+      TG_CUDA(cudaFuncSetAttribute(k_stencil_tma<NF, M, PTV>,                                  \
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, STMA_SMEM_MAX)); \
+      attr = true;                                                                             \
+    }                                                                                          \
+    k_stencil_tma<NF, M, PTV><<<grid, nt, s.smem, st>>>(tm, g, s.TX, s.BX, s.tstride, u, y, b, dinv, om); \
+  }
+#define TG_STM(NF, PTV)                                                                        \
+  if (mode == AM_Y) TG_ST(NF, AM_Y, PTV) else if (mode == AM_RES) TG_ST(NF, AM_RES, PTV) else TG_ST(NF, AM_JACOBI, PTV)
+  if (g.ndof == 3) {
+    if (s.PT == 64) { TG_STM(3, 64) } else { TG_STM(3, 128) }
+  } else {
+    if (s.PT == 64) { TG_STM(1, 64) } else { TG_STM(1, 128) }
+  }
+#undef TG_STM
+#undef TG_ST
+  TG_CHECK_LAUNCH();
+  return true;
+}
+
 template <typename T>
 void stencil_apply(const Grid& g, const T* A, const T* u, T* y, const T* b, const T* dinv,
                    double omega, int mode, cudaStream_t st) {
@@ -227,6 +478,9 @@ void stencil_apply(const Grid& g, const T* A, const T* u, T* y, const T* b, cons
 #undef TG_SS
     TG_CHECK_LAUNCH();
     return;
+  }
+  if constexpr (std::is_same<T, float>::value) {
+    if (stencil_apply_tma(g, A, u, y, b, dinv, omega, mode, st)) return;
   }
   const int TY = std::min(g.nny, 256);
   const int TX = std::max(1, std::min(g.nnx, 256 / TY));
@@ -256,8 +510,8 @@ template void stencil_apply<float>(const Grid&, const float*, const float*, floa
 template <int NDIM, int NDOF, typename T>
 __global__ void k_stencil_dinv(Grid g, const uint8_t* fix, const T* A, T* dinv) {
   const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int64_t ld = g.nnodes();
-  if (n >= ld) return;
+  if (n >= g.nnodes()) return;
+  const int64_t ld = g.slds();
 #pragma unroll
   for (int c = 0; c < NDOF; ++c) {
     const T dg = A[(c * NDOF + c) * ld + n];     // centre block (half index 0)
@@ -377,7 +631,7 @@ __global__ void __launch_bounds__(256) k_build_level1(Grid gf, Grid gc, const T*
 #pragma unroll
   for (int ci = 0; ci < NDOF; ++ci)
 #pragma unroll
-    for (int cj = 0; cj < NDOF; ++cj) Ac[((DH * NDOF + ci) * NDOF + cj) * ldc + I] = acc[ci][cj];
+    for (int cj = 0; cj < NDOF; ++cj) Ac[((DH * NDOF + ci) * NDOF + cj) * gc.slds() + I] = acc[ci][cj];
 }
 
 template <typename T>
@@ -450,7 +704,7 @@ __global__ void __launch_bounds__(256) k_build_fine(Grid g, const double* __rest
 #pragma unroll
   for (int ci = 0; ci < NDOF; ++ci)
 #pragma unroll
-    for (int cj = 0; cj < NDOF; ++cj) A[((DH * NDOF + ci) * NDOF + cj) * ld + I] = acc[ci][cj];
+    for (int cj = 0; cj < NDOF; ++cj) A[((DH * NDOF + ci) * NDOF + cj) * g.slds() + I] = acc[ci][cj];
 }
 
 void build_fine_stencil(const FineOp& op, const double* scale, double* A, cudaStream_t st) {
@@ -470,50 +724,89 @@ void build_fine_stencil(const FineOp& op, const double* scale, double* A, cudaSt
 // ---------------------------------------------------------------------------
 // Galerkin product of an assembled stencil
 // ---------------------------------------------------------------------------
+// Valid (a, b) pairs per axis for coarse offset d = j - i: fine nodes 2i + a
+// and 2j + b (a, b in {-1, 0, 1}) that lie within one fine cell of each other
+// (r = 2d + b - a in {-1, 0, 1}): 3, 7 and 3 pairs for d = -1, 0, 1.
+__constant__ int8_t c_gal_a[3][7] = {{-1, -1, 0, 0, 0, 0, 0}, {-1, -1, 0, 0, 0, 1, 1}, {0, 1, 1, 0, 0, 0, 0}};
+__constant__ int8_t c_gal_b[3][7] = {{0, 1, 1, 0, 0, 0, 0}, {-1, 0, -1, 0, 1, 0, 1}, {-1, -1, 0, 0, 0, 0, 0}};
+__host__ __device__ constexpr int gal_pairs(int d) { return d == 0 ? 7 : 3; }
+
+// Galerkin product of a half-stored stencil, Ac(I, J) = sum P(f, I) Af(f, g)
+// P(g, J): a group of 8 threads per (coarse node I, upper direction D), lane
+// k taking the k-th valid pair of the slowest axis (z in 3-D, x in 2-D) and
+// looping over the valid pairs of the other axes, so only contributing fine
+// pairs are visited (1270 of 27 x 27 per node in 3-D) and the small coarse
+// levels get 8x the threads; the group's partial blocks are added by a fixed
+// shuffle tree.
+constexpr int GAL_LANES = 8;
 template <int NDIM, int NDOF, typename T>
 __global__ void __launch_bounds__(256) k_galerkin(Grid gf, const T* __restrict__ Af, Grid gc,
                                                   const uint8_t* __restrict__ fixc,
                                                   T* __restrict__ Ac) {
-  const int64_t ldc = gc.nnodes(), ldf = gf.nnodes();
+  const int64_t ldc = gc.nnodes();
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t >= ldc * ndir_half<NDIM>()) return;
-  const int64_t I = t % ldc;
-  const int DH = (int)(t / ldc), D = DH + ndir<NDIM>() / 2;
+  const int lane = threadIdx.x % GAL_LANES;
+  const int64_t grp = t / GAL_LANES;
+  const bool active = grp < ldc * ndir_half<NDIM>();
+  const int64_t I = active ? grp % ldc : 0;
+  const int DH = active ? (int)(grp / ldc) : 0, D = DH + ndir<NDIM>() / 2;
   int ix, iy, iz, dx, dy, dz;
   node_xyz(gc, I, ix, iy, iz);
   dir_xyz(D, NDIM, dx, dy, dz);
   const int jx = ix + dx, jy = iy + dy, jz = iz + dz;
+  const bool jin = active && in_grid(gc, jx, jy, jz);
   T acc[NDOF][NDOF];
 #pragma unroll
   for (int a = 0; a < NDOF; ++a)
 #pragma unroll
     for (int b = 0; b < NDOF; ++b) acc[a][b] = T(0);
-  if (in_grid(gc, jx, jy, jz)) {
-    const int64_t J = gc.node(jx, jy, jz);
-    for (int al = 0; al < ndir<NDIM>(); ++al) {
-      int ax, ay, az;
-      dir_xyz(al, NDIM, ax, ay, az);
-      const int fx = 2 * ix + ax, fy = 2 * iy + ay, fz = 2 * iz + az;
-      if (!in_grid(gf, fx, fy, fz)) continue;
-      const T wi = T((ax ? 0.5 : 1.0) * (ay ? 0.5 : 1.0) * (az ? 0.5 : 1.0));
-      const int64_t fi = gf.node(fx, fy, fz);
-      for (int be = 0; be < ndir<NDIM>(); ++be) {
-        int bx, by, bz;
-        dir_xyz(be, NDIM, bx, by, bz);
-        const int gx = 2 * jx + bx, gy = 2 * jy + by, gz = 2 * jz + bz;
-        const int rx = gx - fx, ry = gy - fy, rz = gz - fz;
-        if (rx < -1 || rx > 1 || ry < -1 || ry > 1 || rz < -1 || rz > 1) continue;
-        if (!in_grid(gf, gx, gy, gz)) continue;
-        const T w = wi * T((bx ? 0.5 : 1.0) * (by ? 0.5 : 1.0) * (bz ? 0.5 : 1.0));
-        const int dd = dir_index(rx, ry, rz, NDIM);
-        const int64_t gi = gf.node(gx, gy, gz);
+  // slowest axis of the lane: z in 3-D, x in 2-D
+  const int ds = (NDIM == 3) ? dz : dx;
+  if (jin && lane < gal_pairs(ds)) {
+    const int as = c_gal_a[ds + 1][lane], bs = c_gal_b[ds + 1][lane];
+    const int fs = 2 * ((NDIM == 3) ? iz : ix) + as, gs = 2 * ((NDIM == 3) ? jz : jx) + bs;
+    const int ns = (NDIM == 3) ? gf.nnz : gf.nnx;
+    if (fs >= 0 && fs < ns && gs >= 0 && gs < ns) {
+      const T ws = T((as ? 0.5 : 1.0) * (bs ? 0.5 : 1.0));
+      const int rs = gs - fs;
+      // the middle axis (x in 3-D; none in 2-D) and y
+      const int nm = (NDIM == 3) ? gal_pairs(dx) : 1;
+      for (int km = 0; km < nm; ++km) {
+        const int am = (NDIM == 3) ? c_gal_a[dx + 1][km] : 0;
+        const int bm = (NDIM == 3) ? c_gal_b[dx + 1][km] : 0;
+        const int fx = (NDIM == 3) ? 2 * ix + am : fs, gx = (NDIM == 3) ? 2 * jx + bm : gs;
+        if (fx < 0 || fx >= gf.nnx || gx < 0 || gx >= gf.nnx) continue;
+        const T wm = ws * T((am ? 0.5 : 1.0) * (bm ? 0.5 : 1.0));
+        const int fz = (NDIM == 3) ? fs : 0, gz = (NDIM == 3) ? gs : 0;
+        const int rx = gx - fx, rz = (NDIM == 3) ? rs : 0;
 #pragma unroll
-        for (int ci = 0; ci < NDOF; ++ci)
+        for (int ky = 0; ky < 7; ++ky) {
+          if (ky >= gal_pairs(dy)) break;
+          const int ay = c_gal_a[dy + 1][ky], by = c_gal_b[dy + 1][ky];
+          const int fy = 2 * iy + ay, gy = 2 * jy + by;
+          if (fy < 0 || fy >= gf.nny || gy < 0 || gy >= gf.nny) continue;
+          const T w = wm * T((ay ? 0.5 : 1.0) * (by ? 0.5 : 1.0));
+          const int dd = dir_index(rx, gy - fy, rz, NDIM);
+          const int64_t fi = gf.node(fx, fy, fz), gi = gf.node(gx, gy, gz);
 #pragma unroll
-          for (int cj = 0; cj < NDOF; ++cj)
-            acc[ci][cj] += w * coef<NDIM, NDOF, T>(Af, ldf, dd, ci, cj, fi, gi);
+          for (int ci = 0; ci < NDOF; ++ci)
+#pragma unroll
+            for (int cj = 0; cj < NDOF; ++cj)
+              acc[ci][cj] += w * coef<NDIM, NDOF, T>(Af, gf.slds(), dd, ci, cj, fi, gi);
+        }
       }
     }
+  }
+#pragma unroll
+  for (int off = GAL_LANES / 2; off > 0; off >>= 1)
+#pragma unroll
+    for (int ci = 0; ci < NDOF; ++ci)
+#pragma unroll
+      for (int cj = 0; cj < NDOF; ++cj)
+        acc[ci][cj] += __shfl_xor_sync(0xffffffffu, acc[ci][cj], off);
+  if (!active || lane != 0) return;
+  if (jin) {
+    const int64_t J = gc.node(jx, jy, jz);
     const uint8_t mi = fixc[I], mj = fixc[J];
 #pragma unroll
     for (int ci = 0; ci < NDOF; ++ci)
@@ -524,13 +817,13 @@ __global__ void __launch_bounds__(256) k_galerkin(Grid gf, const T* __restrict__
 #pragma unroll
   for (int ci = 0; ci < NDOF; ++ci)
 #pragma unroll
-    for (int cj = 0; cj < NDOF; ++cj) Ac[((DH * NDOF + ci) * NDOF + cj) * ldc + I] = acc[ci][cj];
+    for (int cj = 0; cj < NDOF; ++cj) Ac[((DH * NDOF + ci) * NDOF + cj) * gc.slds() + I] = acc[ci][cj];
 }
 
 template <typename T>
 void build_galerkin(const Grid& gf, const T* Af, const Grid& gc, const uint8_t* fixc, T* Ac,
                     cudaStream_t st) {
-  const int64_t nt = gc.nnodes() * (gf.ndim == 3 ? 14 : 5);
+  const int64_t nt = gc.nnodes() * (gf.ndim == 3 ? 14 : 5) * GAL_LANES;
   const unsigned blocks = (unsigned)cdiv(nt, 256);
   const int key = gf.ndim * 10 + gf.ndof;
   switch (key) {
@@ -559,7 +852,7 @@ __global__ void k_stencil_expand(Grid g, const T* __restrict__ Ah, double* __res
   node_xyz(g, n, x, y, z);
   dir_xyz(d, NDIM, dx, dy, dz);
   Af[t] = in_grid(g, x + dx, y + dy, z + dz)
-              ? (double)coef<NDIM, NDOF, T>(Ah, ld, d, ci, cj, n, g.node(x + dx, y + dy, z + dz))
+              ? (double)coef<NDIM, NDOF, T>(Ah, g.slds(), d, ci, cj, n, g.node(x + dx, y + dy, z + dz))
               : 0.0;
 }
 
@@ -707,7 +1000,7 @@ __global__ void k_stencil_to_dense(Grid g, const uint8_t* fix, const T* __restri
   dir_xyz(C + dh, g.ndim, dx, dy, dz);
   if (!in_grid(g, ix + dx, iy + dy, iz + dz)) return;
   const int64_t J = g.node(ix + dx, iy + dy, iz + dz);
-  const double v = (double)A[(int64_t)k * ldA + I];
+  const double v = (double)A[(int64_t)k * g.slds() + I];
   D[(I * ndof + ci) * ld + J * ndof + cj] = v;
   if (dh > 0) D[(J * ndof + cj) * ld + I * ndof + ci] = v;   // mirrored lower block
 }
@@ -1163,7 +1456,21 @@ template void dense_apply<float>(const double*, int64_t, int64_t, const float*, 
 // launches; grid_sync separates the phases.  One block per SM: the tail and
 // coarsest levels are small (a few thousand rows), so the launch and drain of
 // ~10 separate kernels per V-cycle, not their work, was the cost.
-template <int NDIM, int NDOF, typename T>
+// phase barrier: the hardware cluster barrier (release / acquire at cluster
+// scope) when the launch is one thread-block cluster, else the bounded grid
+// barrier of a cooperative launch
+template <bool CLUSTER>
+__device__ __forceinline__ bool tail_sync(GridBar* bar) {
+  if constexpr (CLUSTER) {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;"
+                 ::: "memory");
+    return true;
+  } else {
+    return grid_sync(bar);
+  }
+}
+
+template <int NDIM, int NDOF, typename T, bool CLUSTER>
 __global__ void __launch_bounds__(3 * SMALL_PAIRS) k_coarse_tail(TailArgs<T> a) {
   __shared__ T spart[3][SMALL_PAIRS];
   const int64_t gtid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -1181,21 +1488,21 @@ __global__ void __launch_bounds__(3 * SMALL_PAIRS) k_coarse_tail(TailArgs<T> a) 
   // restriction into the tail level with its first step from zero (t = omega D^-1 b)
   for (int64_t t = gtid; t < rows_t; t += gsz)
     restrict_one<NDIM, NDOF, T, true>(a.gp, a.gt, a.fixt, a.rp, a.bt, a.dinvt, a.tt, a.omega, t);
-  if (!grid_sync(a.bar)) return;
+  if (!tail_sync<CLUSTER>(a.bar)) return;
   T* bufs[2] = {a.xt, a.tt};
   int cur = 1;
   for (int s = 1; s < a.nsmooth; ++s) {
     sweep(bufs[cur], bufs[1 - cur], AM_JACOBI);
     cur = 1 - cur;
-    if (!grid_sync(a.bar)) return;
+    if (!tail_sync<CLUSTER>(a.bar)) return;
   }
   sweep(bufs[cur], a.rt, AM_RES);
-  if (!grid_sync(a.bar)) return;
+  if (!tail_sync<CLUSTER>(a.bar)) return;
   // restriction to the coarsest level
   const int64_t rows_c = a.gc.nnodes() * NDOF;
   for (int64_t t = gtid; t < rows_c; t += gsz)
     restrict_one<NDIM, NDOF, T, true>(a.gt, a.gc, a.fixc, a.rt, a.bc, nullptr, nullptr, T(0), t);
-  if (!grid_sync(a.bar)) return;
+  if (!tail_sync<CLUSTER>(a.bar)) return;
   // coarsest solve: a warp per (row, column chunk), then the fixed-order sums
   {
     const int lane = threadIdx.x & 31;
@@ -1203,16 +1510,16 @@ __global__ void __launch_bounds__(3 * SMALL_PAIRS) k_coarse_tail(TailArgs<T> a) 
     for (int64_t w = w0; w < a.nc * DA_CHUNKS; w += nw)
       dense_partial_one<T, true>(a.Dc, a.nc, a.ldc, a.bc, a.part, w % a.nc, (int)(w / a.nc), lane);
   }
-  if (!grid_sync(a.bar)) return;
+  if (!tail_sync<CLUSTER>(a.bar)) return;
   for (int64_t r = gtid; r < a.nc; r += gsz) dense_sum_one<T, true>(a.part, a.nc, a.xc, r);
-  if (!grid_sync(a.bar)) return;
+  if (!tail_sync<CLUSTER>(a.bar)) return;
   for (int64_t i = gtid; i < a.gt.nnodes(); i += gsz)
     prolong_one<NDIM, NDOF, T, true>(a.gt, a.gc, a.fixt, a.xc, bufs[cur], i);
-  if (!grid_sync(a.bar)) return;
+  if (!tail_sync<CLUSTER>(a.bar)) return;
   for (int s = 0; s < a.nsmooth; ++s) {
     sweep(bufs[cur], bufs[1 - cur], AM_JACOBI);
     cur = 1 - cur;
-    if (!grid_sync(a.bar)) return;
+    if (!tail_sync<CLUSTER>(a.bar)) return;
   }
   // the tail level's result (ends in xt for an even number of steps; the
   // parent reads bufs[cur])
@@ -1228,40 +1535,68 @@ void coarse_tail(const TailArgs<T>& a, cudaStream_t st) {
   int dev = 0, nsm = 0;
   TG_CUDA(cudaGetDevice(&dev));
   TG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const bool cl = a.cluster > 0;
   const void* fn = nullptr;
   int slot = 0;
   switch (a.gt.ndim * 10 + a.gt.ndof) {
-    case 33: fn = (const void*)k_coarse_tail<3, 3, T>; slot = 0; break;
-    case 31: fn = (const void*)k_coarse_tail<3, 1, T>; slot = 1; break;
-    case 22: fn = (const void*)k_coarse_tail<2, 2, T>; slot = 2; break;
-    case 21: fn = (const void*)k_coarse_tail<2, 1, T>; slot = 3; break;
+    case 33: fn = cl ? (const void*)k_coarse_tail<3, 3, T, true> : (const void*)k_coarse_tail<3, 3, T, false>; slot = 0; break;
+    case 31: fn = cl ? (const void*)k_coarse_tail<3, 1, T, true> : (const void*)k_coarse_tail<3, 1, T, false>; slot = 1; break;
+    case 22: fn = cl ? (const void*)k_coarse_tail<2, 2, T, true> : (const void*)k_coarse_tail<2, 2, T, false>; slot = 2; break;
+    case 21: fn = cl ? (const void*)k_coarse_tail<2, 1, T, true> : (const void*)k_coarse_tail<2, 1, T, false>; slot = 3; break;
     default: throw Error{EINVAL_, "unsupported (ndim, nnode_dof)"};
   }
-  static std::atomic<int> fits[4] = {};      // resident blocks per SM, found once per variant
-  int per_sm = fits[slot].load(std::memory_order_relaxed);
-  if (!per_sm) {
-    TG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 3 * SMALL_PAIRS, 0));
-    TG_REQUIRE(per_sm >= 1, "coarse_tail: kernel does not fit on an SM");
-    fits[slot].store(per_sm, std::memory_order_relaxed);
-  }
-  if (tune_take_tail_barrier_timeout()) {
-    // the first barrier waits for one block more than the grid holds (the
-    // same count OC's bounded-wait test uses), so every wait runs out
-    static const unsigned int big = 0x40000000u;
-    TG_CUDA(cudaMemcpyAsync(&a.bar->count, &big, sizeof(big), cudaMemcpyHostToDevice, st));
-  }
-  // all blocks co-resident (the cooperative launch refuses more)
-  const unsigned blocks = (unsigned)std::min(a.blocks > 0 ? a.blocks : nsm, nsm * per_sm);
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(blocks);
   cfg.blockDim = dim3(3 * SMALL_PAIRS);
   cfg.dynamicSmemBytes = 0;
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeCooperative;
-  attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
+  if (cl) {
+    // one cluster of 16 CTAs (non-portable size) where the GPU can place it, else 8
+    static std::atomic<int> csize[4] = {};
+    int cs = csize[slot].load(std::memory_order_relaxed);
+    if (!cs) {
+      TG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+      for (cs = 16; cs >= 2; cs /= 2) {
+        cfg.gridDim = dim3((unsigned)cs);
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = (unsigned)cs;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        int nclusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&nclusters, fn, &cfg) == cudaSuccess && nclusters >= 1)
+          break;
+        (void)cudaGetLastError();
+      }
+      TG_REQUIRE(cs >= 2, "coarse_tail: no thread-block cluster fits");
+      csize[slot].store(cs, std::memory_order_relaxed);
+    }
+    cs = std::min(cs, a.cluster);
+    cfg.gridDim = dim3((unsigned)cs);
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)cs;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+  } else {
+    static std::atomic<int> fits[4] = {};      // resident blocks per SM, found once per variant
+    int per_sm = fits[slot].load(std::memory_order_relaxed);
+    if (!per_sm) {
+      TG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 3 * SMALL_PAIRS, 0));
+      TG_REQUIRE(per_sm >= 1, "coarse_tail: kernel does not fit on an SM");
+      fits[slot].store(per_sm, std::memory_order_relaxed);
+    }
+    if (tune_take_tail_barrier_timeout()) {
+      // the first barrier waits for one block more than the grid holds (the
+      // same count OC's bounded-wait test uses), so every wait runs out
+      static const unsigned int big = 0x40000000u;
+      TG_CUDA(cudaMemcpyAsync(&a.bar->count, &big, sizeof(big), cudaMemcpyHostToDevice, st));
+    }
+    // all blocks co-resident (the cooperative launch refuses more)
+    cfg.gridDim = dim3((unsigned)std::min(a.blocks > 0 ? a.blocks : nsm, nsm * per_sm));
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+  }
   TailArgs<T> args = a;
   void* kargs[] = {(void*)&args};
   TG_CUDA(cudaLaunchKernelExC(&cfg, fn, kargs));

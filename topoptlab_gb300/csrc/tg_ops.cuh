@@ -68,7 +68,8 @@ void fine_compliance(const FineOp& op, const double* xPhys, const double* u, dou
 
 // ---------------------------------------------------------------------------
 // assembled 3^ndim-point block stencils (coarse levels)
-// layout: A[(dir * ndof + ci) * ndof + cj][node]   (structure of arrays)
+// layout: A[(dir * ndof + ci) * ndof + cj][node]   (structure of arrays, each
+// array of stride g.slds(): nnodes rounded up to 32)
 // ---------------------------------------------------------------------------
 // Stencils are symmetric and stored half: the centre block and the 3^ndim/2
 // upper direction blocks per node, [(dh*ndof+ci)*ndof+cj][node]
@@ -76,6 +77,13 @@ inline int stencil_half_dirs(int ndim) { return ndim == 3 ? 14 : 5; }
 template <typename T>
 void stencil_apply(const Grid& g, const T* A, const T* u, T* y, const T* b, const T* dinv,
                    double omega, int mode, cudaStream_t st);
+// FP32 3-D sweeps on grids too large for the small-grid kernel stage their
+// coefficients in shared memory by TMA (on by default); 0 selects the
+// register-path kernel (same results)
+void tune_set_stencil_tma(int on);
+// 1 (and cleared) if a bounded wait of a TMA-fed stencil sweep ran out since
+// the last call; synchronises st
+int take_wait_error(cudaStream_t st);
 template <typename T>
 void stencil_dinv(const Grid& g, const uint8_t* fix, const T* A, T* dinv, cudaStream_t st);
 
@@ -109,8 +117,10 @@ void prolong_add(const Grid& gf, const Grid& gc, const uint8_t* fixf, const T* x
 // step from zero), nsmooth - 1 Jacobi sweeps, the residual, restriction to
 // the coarsest level, the coarsest solve (dense FP64 inverse), prolongation,
 // nsmooth Jacobi sweeps, and prolongation of the tail level's iterate into
-// the parent's xp -- phases separated by bounded grid barriers (bar->err set
-// when one times out).  The tail level must use the small-grid stencil.
+// the parent's xp -- phases separated by the cluster barrier of one
+// thread-block cluster (up to 16 SMs), or by bounded grid barriers of a
+// cooperative launch (bar->err set when one times out).  The tail level must
+// use the small-grid stencil.
 template <typename T> struct TailArgs {
   Grid gp, gt, gc;                         // parent, tail and coarsest grids
   const uint8_t *fixt, *fixc, *fixp;
@@ -125,7 +135,8 @@ template <typename T> struct TailArgs {
   double* part;                            // >= 8 * nc doubles
   T omega;
   int nsmooth;
-  int blocks;                              // 0: one per SM
+  int cluster;                             // > 0: one thread-block cluster of at most this many CTAs
+  int blocks;                              // cooperative launch: 0 one block per SM
   GridBar* bar;
 };
 template <typename T>

@@ -9,6 +9,7 @@
 #include <utility>
 #include <vector>
 #include "tg_common.cuh"
+#include "tg_ops.cuh"
 #include "../../include/topopt_gb300.h"
 
 namespace tg {
@@ -186,6 +187,10 @@ extern "C" int32_t tg_tune(int32_t key, int64_t value) {
       return TG_OK;
     case TG_TUNE_TAIL_BARRIER_TIMEOUT:
       tg::g_tail_timeout.store(value != 0 ? 1 : 0);
+      return TG_OK;
+    case TG_TUNE_STENCIL_TMA:
+      if (value < 0 || value > 64) return TG_EINVAL;
+      tg::tune_set_stencil_tma((int)value);
       return TG_OK;
     default:
       return TG_EINVAL;
