@@ -60,6 +60,10 @@ def test_noalloc_oc_matches_allocating_entry_and_oracle(gpu_lib):
         torch.cuda.synchronize()
         xn = out.cpu().numpy()
         np.testing.assert_allclose(xn, xref, rtol=0, atol=1e-13)
+        # the allocating entry screens each bisection decision in FP32 (with an
+        # error bound, FP64 where it cannot decide); the allocation-free one
+        # evaluates every step in FP64: same decisions, the same densities
+        np.testing.assert_array_equal(xn, xref)
         np.testing.assert_allclose(gt.value, gtref, rtol=1e-9, atol=1e-12)
         np.testing.assert_allclose(xn, xo, rtol=0, atol=1e-13)
         np.testing.assert_allclose(gt.value, gto, rtol=1e-9, atol=1e-12)

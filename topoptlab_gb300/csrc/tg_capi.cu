@@ -333,7 +333,7 @@ int32_t tg_oc(tg_ctx* ctx, const double* x, const double* dc, const double* dv, 
     h2d(xd.p, x, nel, c.st);
     h2d(dcd.p, dc, nel, c.st);
     h2d(dvd.p, dv, nel, c.st);
-    const tg::OCScratch ocs{c.S.p, c.S.p + nel, c.S.p + 2 * nel};
+    const tg::OCScratch ocs{c.S.p, c.S.p + nel, c.S.p + 2 * nel, c.S32.p};
     tg::oc_begin(nel, xd, dcd, dvd, c.flags.p, c.move, ocs, c.oc, g, c.st);
     tg::oc_steps(nel, xd, ocs, dvd, c.flags.p, c.move, c.part2, c.oc, 256, c.st);
     d2h(c.h_oc, c.oc.p, 1, c.st);
@@ -354,9 +354,11 @@ int32_t tg_oc_raw(int64_t n, const double* x, const double* dc, const double* dv
     TG_CUDA(cudaSetDevice(device));
     cudaStream_t st = 0;
     tg::DevBuf<double> xd, dcd, dvd, xn, S, part;
+    tg::DevBuf<float> S32;
     tg::DevBuf<int8_t> fl;
     tg::DevBuf<tg::OCState> oc;
     xd.alloc(n); dcd.alloc(n); dvd.alloc(n); xn.alloc(n); S.alloc(3 * n); part.alloc(tg::RED_BLOCKS);
+    S32.alloc(5 * n);
     oc.alloc(1);
     h2d(xd.p, x, n, st);
     h2d(dcd.p, dc, n, st);
@@ -366,7 +368,7 @@ int32_t tg_oc_raw(int64_t n, const double* x, const double* dc, const double* dv
       h2d(fl.p, el_flags, n, st);
     }
     tg::OCState h;
-    const tg::OCScratch ocs{S.p, S.p + n, S.p + 2 * n};
+    const tg::OCScratch ocs{S.p, S.p + n, S.p + 2 * n, S32.p};
     tg::oc_begin(n, xd, dcd, dvd, fl.p, move, ocs, oc, g, st, l1, l2);
     tg::oc_steps(n, xd, ocs, dvd, fl.p, move, part, oc, 256, st);
     d2h(&h, oc.p, 1, st);

@@ -340,6 +340,7 @@ void ctx_init(Ctx& c, const tg_problem& p) {
   c.f.alloc(nd * c.nload); c.u.alloc(nd * c.nload);
   c.x.alloc(nel); c.xPhys.alloc(nel); c.xold.alloc(nel); c.xnew.alloc(nel); c.xsolved.alloc(nel);
   c.dc.alloc(nel); c.dcf.alloc(nel); c.dv.alloc(nel); c.Hs.alloc(nel); c.S.alloc(3 * nel);
+  c.S32.alloc(5 * nel);
   c.s64.alloc(nel);
   if (mixed) { c.s32.alloc(nel); c.s16.alloc(nel); }
   c.part.alloc(RED_BLOCKS); c.part2.alloc(RED_BLOCKS); c.scal.alloc(8);
@@ -1042,7 +1043,7 @@ void ctx_step(Ctx& c, tg_iter_out& out) {
   else if (c.ft == 0) filter_apply(g, c.fs, c.x, c.dc, c.Hs, c.dcf, 2, c.st);
   else TG_CUDA(cudaMemcpyAsync(c.dcf.p, c.dc.p, sizeof(double) * nel, cudaMemcpyDeviceToDevice, c.st));
   // OC
-  const OCScratch ocs{c.S.p, c.S.p + nel, c.S.p + 2 * nel};
+  const OCScratch ocs{c.S.p, c.S.p + nel, c.S.p + 2 * nel, c.S32.p};
   // the whole bisection in one launch; its state is read back with the
   // iteration's scalars at the end (no host round trip in between)
   oc_begin(nel, c.x, c.dcf, c.dv, c.flags.p, c.move, ocs, c.oc, c.g_oc, c.st);

@@ -69,6 +69,7 @@ struct Ctx {
   DevBuf<float> KE32;
   DevBuf<double> f, u, x, xPhys, xold, xnew, dc, dcf, dv, Hs, S, s64;
   DevBuf<double> xsolved;       // the design the scale factors and hierarchy were built for
+  DevBuf<float> S32;            // FP32 copies screening the OC bisection (5 nel)
   bool built = false;           // a hierarchy exists (tg_adjoint reuses it)
   DevBuf<float> s32;
   DevBuf<__nv_bfloat16> s16;

@@ -170,6 +170,7 @@ __global__ void k_oc_init(OCState* s, double g, double l1, double l2, unsigned i
   s->g = g;
   s->gt = g;
   s->nsteps = 0;
+  s->nsteps64 = 0;
   s->done = ((l2 - l1) / (l1 + l2) > 1e-3) ? 0 : 1;
   s->lmid = 0.5 * (l2 + l1);
   s->sc = 1.0 / sqrt(s->lmid);
@@ -193,7 +194,8 @@ __global__ void __launch_bounds__(RED_THREADS) k_oc_prep(int64_t n, const double
   if (i >= n) return;
   const double xi = x[i];
   const bool outside = flags && flags[i] == EL_OUTSIDE;
-  sc.P[i] = outside ? 0.0 : xi * sqrt(-dc[i] / dv[i]);
+  const double P = outside ? 0.0 : xi * sqrt(-dc[i] / dv[i]);
+  sc.P[i] = P;
   if (sc.lo) {
     double lo = fmax(0.0, xi - move), hi = fmin(1.0, xi + move);
     if (flags) {
@@ -202,6 +204,13 @@ __global__ void __launch_bounds__(RED_THREADS) k_oc_prep(int64_t n, const double
     }
     sc.lo[i] = lo;
     sc.hi[i] = hi;
+    if (sc.f32) {
+      sc.f32[i] = (float)P;
+      sc.f32[n + i] = (float)lo;
+      sc.f32[2 * n + i] = (float)hi;
+      sc.f32[3 * n + i] = (float)xi;
+      sc.f32[4 * n + i] = (float)dv[i];
+    }
   }
 }
 
@@ -225,10 +234,24 @@ __device__ __forceinline__ double oc_value(int64_t i, double xi, const OCScratch
 // parity, meets the others at a grid barrier and then sums all partials in
 // the same fixed order, so every block takes the same decision on (l1, l2)
 // without another launch or a host round trip.  Double-buffered partials need
-// one barrier per step: a block writes step k+1's partials only after every
-// block has passed step k's barrier, i.e. finished reading step k-1's.
-// Block 0 writes the final state.  Runs at most max_steps steps.
-template <bool BOUNDS>
+// one barrier per reduction: a block writes reduction k+1's partials only
+// after every block has passed reduction k's barrier, i.e. finished reading
+// reduction k-1's.  Block 0 writes the final state.  Runs at most max_steps
+// steps.
+//
+// SCREEN (GB300 issues ~64 FP32 operations per FP64 one): each step first
+// evaluates the sum in FP32 from FP32 copies of P, lo, hi, x, dv, together
+// with a bound on its distance from the FP64 sum.  Per element the FP32 term
+// differs from the FP64 one by at most 4u (|dv| (P s + 1 + |x| + 2 |d|) + |t|)
+// (u = 2^-24: the roundings of P, s, their product, lo / hi (both in [0, 1]),
+// x, the difference d, dv and the product t = dv d; the clamp is 1-Lipschitz),
+// and a thread's sum of m terms adds at most m u sum |t|; the FP64 sum's own
+// rounding is far below.  With A = sum (|dv| (P s + 1 + |x| + 2 |d|) + |t|),
+// |g + T32| > (16 + 2m) u A means the FP64 evaluation has the same sign: the
+// decision is the FP64 decision.  Otherwise (near the root) the step is
+// evaluated in FP64 as without SCREEN.  The carry gt of the last step is
+// always an FP64 sum.
+template <bool BOUNDS, bool SCREEN>
 __global__ void __launch_bounds__(RED_THREADS) k_oc_bisect(int64_t n, const double* __restrict__ x,
                                                           OCScratch sc,
                                                           const double* __restrict__ dv,
@@ -236,29 +259,84 @@ __global__ void __launch_bounds__(RED_THREADS) k_oc_bisect(int64_t n, const doub
                                                           double move, double* part, OCState* st,
                                                           int max_steps) {
   __shared__ double sh[32];
-  __shared__ double tot_s;
+  __shared__ double tot_s, tot_a;
   double l1 = st->l1, l2 = st->l2, lmid = st->lmid, s = st->sc, s_last = st->sc_last;
   double gt = st->gt;
   const double g = st->g;
-  int done = st->done, steps = 0;
+  int done = st->done, steps = 0, steps64 = 0;
+  bool gt_exact = true;
   const unsigned int nb = gridDim.x;
-  while (!done && steps < max_steps) {
+  const int64_t t0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t ts = (int64_t)gridDim.x * blockDim.x;
+  int red = 0;                                   // reductions so far (partials parity)
+  // one FP64 reduction of g + sum dv (xnew(s) - x); false: a barrier timed out
+  auto fp64_sum = [&](double sv, double& out) -> bool {
     double acc = 0.0;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-         i += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t i = t0; i < n; i += ts) {
       const double xi = x[i];
-      acc += dv[i] * (oc_value<BOUNDS>(i, xi, sc, flags, move, s) - xi);
+      acc += dv[i] * (oc_value<BOUNDS>(i, xi, sc, flags, move, sv) - xi);
     }
-    double* pp = part + (steps & 1) * nb;
+    double* pp = part + (red & 1) * (SCREEN ? 2 : 1) * nb;
     const double bs = block_sum(acc, sh);
     if (threadIdx.x == 0) pp[blockIdx.x] = bs;
-    if (!grid_sync(&st->bar)) return;
-    const double t0 = sum_partials(pp, (int)nb, sh);
-    if (threadIdx.x == 0) tot_s = t0;
+    if (!grid_sync(&st->bar)) return false;
+    ++red;
+    const double t = sum_partials(pp, (int)nb, sh);
+    if (threadIdx.x == 0) tot_s = t;
     __syncthreads();
-    gt = g + tot_s;
+    out = g + tot_s;
+    return true;
+  };
+  while (!done && steps < max_steps) {
+    bool decided = false, up = false;
+    if constexpr (SCREEN) {
+      const float s32 = (float)s;
+      const float* P32 = sc.f32;
+      const float* lo32 = sc.f32 + n;
+      const float* hi32 = sc.f32 + 2 * n;
+      const float* x32 = sc.f32 + 3 * n;
+      const float* dv32 = sc.f32 + 4 * n;
+      float tsum = 0.f, asum = 0.f;
+      for (int64_t i = t0; i < n; i += ts) {
+        const float ps = P32[i] * s32;
+        const float xi = x32[i], di = dv32[i];
+        const float d = fmaxf(lo32[i], fminf(hi32[i], ps)) - xi;
+        const float t = di * d;
+        tsum += t;
+        asum += fabsf(di) * (ps + 1.f + fabsf(xi) + 2.f * fabsf(d)) + fabsf(t);
+      }
+      double* pp = part + (red & 1) * 2 * nb;
+      const double bt = block_sum((double)tsum, sh);
+      const double ba = block_sum((double)asum, sh);
+      if (threadIdx.x == 0) {
+        pp[blockIdx.x] = bt;
+        pp[nb + blockIdx.x] = ba;
+      }
+      if (!grid_sync(&st->bar)) return;
+      ++red;
+      const double tt = sum_partials(pp, (int)nb, sh);
+      if (threadIdx.x == 0) tot_s = tt;
+      const double ta = sum_partials(pp + nb, (int)nb, sh);
+      if (threadIdx.x == 0) tot_a = ta;
+      __syncthreads();
+      const double m = (double)((n + ts - 1) / ts);
+      const double g32 = g + tot_s;
+      const double margin = ldexp(tot_a, -24) * (16.0 + 2.0 * m);
+      if (fabs(g32) > margin) {        // false for NaN or infinite values: FP64 below
+        decided = true;
+        up = g32 > 0;
+        gt = g32;
+        gt_exact = false;
+      }
+    }
+    if (!decided) {
+      if (!fp64_sum(s, gt)) return;
+      up = gt > 0;
+      gt_exact = true;
+      ++steps64;
+    }
     s_last = s;
-    if (gt > 0) l1 = lmid;
+    if (up) l1 = lmid;
     else l2 = lmid;
     ++steps;
     if ((l2 - l1) / (l1 + l2) > 1e-3) {
@@ -267,6 +345,9 @@ __global__ void __launch_bounds__(RED_THREADS) k_oc_bisect(int64_t n, const doub
     } else {
       done = 1;
     }
+  }
+  if (SCREEN && !gt_exact) {
+    if (!fp64_sum(s_last, gt)) return;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     st->l1 = l1;
@@ -277,6 +358,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_oc_bisect(int64_t n, const doub
     st->gt = gt;
     st->done = done;
     st->nsteps += steps;
+    st->nsteps64 += steps64;
   }
 }
 
@@ -308,9 +390,13 @@ void oc_steps(int64_t n, const double* x, OCScratch sc, const double* dv, const 
   int dev = 0, nsm = 0, per_sm = 0;
   TG_CUDA(cudaGetDevice(&dev));
   TG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  const void* fn = sc.lo ? (const void*)k_oc_bisect<true> : (const void*)k_oc_bisect<false>;
+  const bool screen = sc.lo && sc.f32;
+  const void* fn = screen ? (const void*)k_oc_bisect<true, true>
+                   : sc.lo ? (const void*)k_oc_bisect<true, false>
+                           : (const void*)k_oc_bisect<false, false>;
   TG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, RED_THREADS, 0));
-  const int64_t cap = std::min<int64_t>(RED_BLOCKS / 2, (int64_t)nsm * std::max(per_sm, 1));
+  // double-buffered partials: 2 (4 with the screen's second sum) per block
+  const int64_t cap = std::min<int64_t>(RED_BLOCKS / (screen ? 4 : 2), (int64_t)nsm * std::max(per_sm, 1));
   const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(cdiv(n, RED_THREADS), cap));
   void* args[] = {(void*)&n, (void*)&x, (void*)&sc, (void*)&dv, (void*)&flags, (void*)&move,
                   (void*)&part, (void*)&st, (void*)&nsteps};

@@ -11,6 +11,7 @@ struct OCState {
   double sc;         // 1/sqrt(lmid) of the next step (computed once per step)
   double sc_last;    // 1/sqrt(lmid) of the last evaluated step
   int done, nsteps;
+  int nsteps64;      // steps decided by an FP64 pass (the rest by the FP32 screen)
   unsigned int ticket;
   GridBar bar;       // barrier of the one-launch bisection (bar.err: a wait timed out)
 };
@@ -20,6 +21,9 @@ struct OCScratch {
   double* P;
   double* lo;
   double* hi;
+  // optional (with lo/hi): 5 n floats, the FP32 copies of P, lo, hi, x and dv
+  // that screen each bisection decision (null: every step in FP64)
+  float* f32 = nullptr;
 };
 
 // PCG scalars (linear_solvers.py:114-134)
