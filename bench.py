@@ -41,6 +41,12 @@ METRIC = "design iters/s, 3D hex8 1M elems: learned+mixed vs plain GMG-PCG at re
 UNIT = "design iters/s"
 SIZE = (160, 80, 80)
 VOLFRAC, RMIN, PENAL = 0.12, 1.5, 3.0
+# V-cycle smoothing of both GPU arms (learned+mixed and plain FP64): one
+# damped-Jacobi sweep before and after the coarse correction with omega 0.65.
+# Measured on GB300 at 160x80x80 against the library default (2 sweeps, 0.6):
+# 21 % more PCG iterations but 15 % less time per design iteration (mixed),
+# 22 % less (FP64); 0.7 and above stall the FP32 PCG.
+NSMOOTH, OMEGA = 1, 0.65
 CPU_SAMPLE = (24, 12, 12)
 # grids of the reference arm: one design iteration of one grid per step, in
 # turn; the seconds per iteration are fitted as a * nel^b
@@ -154,7 +160,8 @@ def _problem(precision, device, size=None, volfrac=None):
     ndof = 3 * (nx + 1) * (ny + 1) * (nz + 1)
     _, f, fixed, _, _ = cantilever_3d(nx, ny, nz, ndof)
     return GpuProblem(nx, ny, nz, lk_linear_elast_3d(), fixed, f[:, 0], volfrac or VOLFRAC, RMIN, ft=1,
-                      penal=PENAL, precision=precision, rtol=1e-8, device=device)
+                      penal=PENAL, precision=precision, rtol=1e-8, device=device,
+                      nsmooth=NSMOOTH, omega=OMEGA)
 
 
 # kernel families timed one at a time with CUDA events (library profiling kinds)
@@ -164,13 +171,15 @@ FAMILIES = [(1, "fine_f64_residual"), (2, "fine_f32_kmul"), (3, "fine_bf16_jacob
             (11, "vector"), (12, "transfer"), (13, "compliance"), (14, "learned_warm_start"),
             (15, "coarse_tail")]
 ROOFLINE_KERNEL = {1: "k_fine_zstream FP64 residual b - K u",
-                   2: "k_fine_zstream FP32 K.u (inner PCG)",
-                   3: "k_fine_zstream FP32 damped-Jacobi sweep (BF16 densities)",
+                   2: "k_fine_zpair FP32 K.u (inner PCG)",
+                   3: "k_fine_zpair FP32 fine sweep (BF16 densities): damped Jacobi and the "
+                      "V-cycle residual",
                    8: "k_stencil_apply FP32 level 1 (3 Jacobi sweeps + 1 residual per V-cycle)"}
 
-# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum, mean of
-# three launches of one ncu capture of this bench's 160x80x80 workload)
-NCU_TRAFFIC = {(3, (160, 80, 80)): 41154048}
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum of one
+# ncu --set full capture of the k_fine_zpair Jacobi sweep on this bench's
+# 160x80x80 workload: 41.16 MB read, 0.02 MB written)
+NCU_TRAFFIC = {(3, (160, 80, 80)): 41180000}
 
 
 def _fine_bytes(kind, size=None):
@@ -471,7 +480,8 @@ def run_ours(args, dist, rank, ws, local):
                                "3,168,963 DOFs), volfrac 0.12, rmin 1.5, ft=1, OC, "
                                "FP64 relative residual 1e-8",
                    "solver": "mixed-precision GMG-PCG (FP32 V-cycle, BF16 smoother densities, "
-                             "FP64 refinement), 5 levels, 2 damped-Jacobi sweeps omega 0.6, "
+                             f"FP64 refinement), 5 levels, {NSMOOTH} damped-Jacobi sweep(s) "
+                             f"omega {OMEGA} before and after, FP32-screened OC, "
                              "learned warm start (3-level 16/32/64 conv encoder-decoder, FP32, "
                              "on its own stream beside the hierarchy build)",
                    "learned_warm_start": train_info,
