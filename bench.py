@@ -387,15 +387,16 @@ def run_ours(args, dist, rank, ws, local):
     for _ in range(nsteps_e2e):
         prob.set(_lib.TG_FIELD_X, xh)                 # H2D: the design
         prob.step()
-        xp[:] = prob.get(_lib.TG_FIELD_XPHYS)         # D2H: the physical densities
-        xh[:] = prob.get(_lib.TG_FIELD_X)             # D2H: the updated design
+        prob.get(_lib.TG_FIELD_XPHYS, out=xp)         # D2H: the physical densities
+        prob.get(_lib.TG_FIELD_X, out=xh)             # D2H: the updated design
     t_e2e = _max_over_ranks(dist, time.perf_counter() - t0)
     # the state after design iteration warmup + steps, for the errors against FP64
     fields_mixed = {"x": xh.copy(), "xPhys": xp.copy(), "dc": prob.get(_lib.TG_FIELD_DC),
                     "u": prob.get(_lib.TG_FIELD_U)}
     e2e = {"value": nsteps_e2e * ws / t_e2e, "unit": UNIT,
            "h2d_bytes_per_step": 8 * prob.nel, "d2h_bytes_per_step": 16 * prob.nel,
-           "api": "GpuProblem.set/step/get over the C ABI (tg_set, tg_step, tg_get)",
+           "api": "GpuProblem.set/step/get over the C ABI (tg_set, tg_step, tg_get), "
+                  "host buffers page-locked, get into them with out=",
            "design_iterations": f"{args.warmup + 1}..{args.warmup + args.steps}, as value"}
     if net is not None:
         net.close()

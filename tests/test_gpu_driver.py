@@ -217,6 +217,32 @@ def test_nan_density_raises(gpu_lib):
         prob.close()
 
 
+def test_get_into_page_locked_buffer(gpu_lib):
+    """get(field, out=...) copies into the caller's array (page-locked host
+    memory in the end-to-end bench) with the values of get(field); a wrong
+    dtype, size or layout raises ValueError."""
+    torch = pytest.importorskip("torch")
+    from topoptlab_gb300.context import GpuProblem
+    from topoptlab_gb300.elements import lk_linear_elast_2d
+    from topoptlab_gb300 import _lib
+    fixed, f = O.bc_mbb_2d(24, 12)
+    prob = GpuProblem(24, 12, None, lk_linear_elast_2d(), fixed, f, 0.5, 1.5)
+    try:
+        prob.step()
+        for field, n in ((_lib.TG_FIELD_XPHYS, 24 * 12), (_lib.TG_FIELD_U, prob.ndof)):
+            buf = torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+            assert prob.get(field, out=buf) is buf
+            np.testing.assert_array_equal(buf, prob.get(field))
+        with pytest.raises(ValueError):
+            prob.get(_lib.TG_FIELD_X, out=np.empty(24 * 12, dtype=np.float32))
+        with pytest.raises(ValueError):
+            prob.get(_lib.TG_FIELD_X, out=np.empty(24 * 12 + 1))
+        with pytest.raises(ValueError):
+            prob.get(_lib.TG_FIELD_X, out=np.empty((24 * 12, 2))[:, 0])
+    finally:
+        prob.close()
+
+
 def test_main_exports_vtk(gpu_lib, tmp_path):
     """output_kw export / output_movie write the reference's VTK files: one per
     design iteration, named file_<iteration>, and the final design as file.vtk,

@@ -144,13 +144,25 @@ class GpuProblem:
         self._check(self._lib.tg_step(self._h, C.byref(out)), "tg_step")
         return IterResult(*(getattr(out, k) for k, _ in _lib.TgIterOut._fields_))
 
-    def get(self, field: int) -> np.ndarray:
+    def get(self, field: int, out: np.ndarray = None) -> np.ndarray:
         """Element fields: (nel,); u and f: (ndof,) for one load case, else
-        (ndof, nload)."""
+        (ndof, nload).  `out`: a C-contiguous float64 array of the field's
+        size to copy into (for one load case), e.g. page-locked host memory,
+        which the device copies into directly."""
         nodes = field in (_lib.TG_FIELD_U, _lib.TG_FIELD_F)
         n = self.ndof * self.nload if nodes else self.nel
-        a = np.empty(n)
+        if out is not None:
+            if nodes and self.nload > 1:
+                raise ValueError("get(out=...) takes one load case")
+            if (out.dtype != np.float64 or out.size != n or not out.flags["C_CONTIGUOUS"]
+                    or not out.flags["WRITEABLE"]):
+                raise ValueError(f"get(out=...) needs a writeable C-contiguous float64 array of {n}")
+            a = out.reshape(-1)
+        else:
+            a = np.empty(n)
         self._check(self._lib.tg_get(self._h, field, _lib.dptr(a), n), "tg_get")
+        if out is not None:
+            return out
         if nodes and self.nload > 1:
             return np.ascontiguousarray(a.reshape(self.nload, self.ndof).T)
         return a
