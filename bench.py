@@ -42,11 +42,16 @@ UNIT = "design iters/s"
 SIZE = (160, 80, 80)
 VOLFRAC, RMIN, PENAL = 0.12, 1.5, 3.0
 # V-cycle smoothing of both GPU arms (learned+mixed and plain FP64): one
-# damped-Jacobi sweep before and after the coarse correction with omega 0.65.
-# Measured on GB300 at 160x80x80 against the library default (2 sweeps, 0.6):
-# 21 % more PCG iterations but 15 % less time per design iteration (mixed),
-# 22 % less (FP64); 0.7 and above stall the FP32 PCG.
-NSMOOTH, OMEGA = 1, 0.65
+# damped-Jacobi sweep (omega 0.6) before and after the coarse correction, and
+# none on level 1 (its right-hand side restricted straight on to level 2,
+# bit 1 of tg_problem.unsmoothed).  Measured on GB300 at 160x80x80 against
+# the library default (2 sweeps on every level): one sweep, 21 % more PCG
+# iterations but 15 % less time per design iteration (mixed), 22 % less
+# (FP64); level 1 unsmoothed on top, 7 % more iterations and 13 % less time.
+# Leaving level 2 or 3 unsmoothed costs more iterations than it saves; omega
+# 0.65 was 1.5 % faster here but stalls the FP32 PCG on a random-density
+# 32x16x16 design once level 1 is unsmoothed (omega 0.6 converges there).
+NSMOOTH, OMEGA, UNSMOOTHED = 1, 0.6, 1 << 1
 CPU_SAMPLE = (24, 12, 12)
 # grids of the reference arm: one design iteration of one grid per step, in
 # turn; the seconds per iteration are fitted as a * nel^b
@@ -161,7 +166,7 @@ def _problem(precision, device, size=None, volfrac=None):
     _, f, fixed, _, _ = cantilever_3d(nx, ny, nz, ndof)
     return GpuProblem(nx, ny, nz, lk_linear_elast_3d(), fixed, f[:, 0], volfrac or VOLFRAC, RMIN, ft=1,
                       penal=PENAL, precision=precision, rtol=1e-8, device=device,
-                      nsmooth=NSMOOTH, omega=OMEGA)
+                      nsmooth=NSMOOTH, omega=OMEGA, unsmoothed=UNSMOOTHED)
 
 
 # kernel families timed one at a time with CUDA events (library profiling kinds)
@@ -482,7 +487,8 @@ def run_ours(args, dist, rank, ws, local):
                                "FP64 relative residual 1e-8",
                    "solver": "mixed-precision GMG-PCG (FP32 V-cycle, BF16 smoother densities, "
                              f"FP64 refinement), 5 levels, {NSMOOTH} damped-Jacobi sweep(s) "
-                             f"omega {OMEGA} before and after, FP32-screened OC, "
+                             f"omega {OMEGA} before and after (level 1 unsmoothed), "
+                             "FP32-screened OC, "
                              "learned warm start (3-level 16/32/64 conv encoder-decoder, FP32, "
                              "on its own stream beside the hierarchy build)",
                    "learned_warm_start": train_info,

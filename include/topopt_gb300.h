@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define TG_ABI_VERSION 4
+#define TG_ABI_VERSION 5
 
 enum {
   TG_OK = 0,
@@ -87,6 +87,12 @@ typedef struct tg_problem {
   const double* KF;      /* filter_pde: screened Poisson element matrix, (2^ndim)^2 row
                             major, reference local node order (lk_screened_poisson_2d/_3d
                             with k = (rmin / (2 sqrt 3))^2, elements/screenedpoisson_2d.py:8) */
+  int32_t unsmoothed;    /* multigrid: bit l set (0 < l < nlevels - 1) = level l is not
+                            smoothed: its right-hand side is restricted on as it is and
+                            the coarser correction prolongated back (the Galerkin coarse
+                            correction through the composite interpolation of levels
+                            l-1 -> l+1); 0 = every level smoothed (TG_EINVAL for other
+                            bits) */
 } tg_problem;
 
 typedef struct tg_iter_out {

@@ -82,11 +82,15 @@ class Hierarchy:
     formed instead of K -- the mixed-precision cycle smooths with BF16
     densities on the fine level but builds the coarse levels from FP32
     densities.  coarse_ops (if given): the operators of levels 1, 2, ...
-    themselves, used in place of the Galerkin products."""
+    themselves, used in place of the Galerkin products.  unsmoothed: levels
+    (0 < l < nlevels - 1) the V-cycle does not smooth: their right-hand side
+    is restricted on as it is and the coarser correction prolongated back
+    (the GPU context's tg_problem.unsmoothed bits)."""
 
     def __init__(self, K, fixed_mask, dims, ndof, nlevels, omega=0.6, nsmooth=2, K_build=None,
-                 coarse_ops=None):
+                 coarse_ops=None, unsmoothed=()):
         self.omega, self.nsmooth = omega, nsmooth
+        self.unsmoothed = set(unsmoothed)
         free = (~fixed_mask).astype(float)
         M = sp.diags(free)
         self.A = [(M @ K @ M).tocsr()]
@@ -127,6 +131,8 @@ class Hierarchy:
     def vcycle(self, b, lvl=0):
         if lvl == len(self.A) - 1:
             return self.Ac_inv @ b
+        if lvl in self.unsmoothed:
+            return self.P[lvl] @ self.vcycle(self.P[lvl].T @ b, lvl + 1)
         A, Dinv, w = self.A[lvl], self.Dinv[lvl], self.omega
         x = w * Dinv * b
         for _ in range(self.nsmooth - 1):

@@ -403,6 +403,60 @@ def test_coarse_tail_barrier_wait_runs_out(gpu_lib):
     np.testing.assert_array_equal(z, z_sep)
 
 
+@pytest.mark.parametrize("unsmoothed", [(1,), (2,), (1, 2)])
+@pytest.mark.parametrize("nelx,nely,nelz,kind", [(32, 16, None, "elast"), (16, 8, 8, "elast"),
+                                                 (32, 16, 16, "elast"), (16, 16, 8, "poisson")])
+def test_vcycle_unsmoothed_levels_match_oracle(gpu_lib, unsmoothed, nelx, nely, nelz, kind):
+    """Levels left unsmoothed (tg_problem.unsmoothed): the cycle restricts
+    their right-hand side on and prolongates the coarser correction back,
+    as the oracle's Hierarchy(unsmoothed=...) does (FP64, 4 levels)."""
+    rng = np.random.default_rng(21)
+    mask_bits = sum(1 << l for l in unsmoothed)
+    prob, KE, fixed, f, x, ndof = _setup(nelx, nely, nelz, kind, rng, nlevels=4,
+                                         unsmoothed=mask_bits)
+    ndim = 2 if nelz is None else 3
+    dims = (nelx, nely) if ndim == 2 else (nelx, nely, nelz)
+    nnd = KE.shape[0] // 2 ** ndim
+    K = O.assemble(KE, O.edofmat(nelx, nely, nelz, nnd), O.simp(x), ndof)
+    mask = np.zeros(ndof, bool)
+    mask[fixed] = True
+    h = G.Hierarchy(K, mask, dims, nnd, 4, omega=0.6, nsmooth=2, unsmoothed=unsmoothed)
+    b = rng.standard_normal(ndof) * ~mask
+    try:
+        z = prob.vcycle(x, b)
+    finally:
+        prob.close()
+    zr = h.vcycle(b)
+    np.testing.assert_allclose(z, zr, rtol=0, atol=1e-10 * np.abs(zr).max())
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_solve_unsmoothed_level1_reaches_direct_solution(gpu_lib, precision):
+    """One smoothing sweep (omega 0.6) with level 1 unsmoothed -- the bench's
+    V-cycle -- still converges to the direct solution on a random-density
+    design."""
+    rng = np.random.default_rng(22)
+    prob, KE, fixed, f, x, ndof = _setup(32, 16, 16, "elast", rng, precision=precision,
+                                         rtol=1e-10, nlevels=4, nsmooth=1, omega=0.6,
+                                         unsmoothed=2)
+    try:
+        u, info = prob.solve(x, f)
+    finally:
+        prob.close()
+    assert info["converged"] == 1 and info["rel_res"] < 1e-10
+    K = O.assemble(KE, O.edofmat(32, 16, 16, 3), O.simp(x), ndof)
+    free = np.setdiff1d(np.arange(ndof), fixed)
+    ud = O.solve_direct(K, f, free)
+    np.testing.assert_allclose(u, ud, rtol=0, atol=1e-7 * np.abs(ud).max())
+
+
+def test_unsmoothed_bits_are_checked(gpu_lib):
+    rng = np.random.default_rng(23)
+    for bits in (1, 1 << 3, 1 << 5):          # the fine level, the coarsest (4 levels), beyond
+        with pytest.raises(ValueError, match="unsmoothed"):
+            _setup(16, 8, 8, "elast", rng, nlevels=4, unsmoothed=bits)
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("nelx,nely,nelz,kind", [(32, 16, None, "elast"), (32, 32, None, "poisson"),
                                                  (16, 8, 8, "elast")])

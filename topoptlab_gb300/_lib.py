@@ -39,7 +39,7 @@ class TgProblem(C.Structure):
         ("nsmooth", C.c_int32), ("omega", C.c_double), ("rtol", C.c_double),
         ("maxiter", C.c_int32), ("inner_rtol", C.c_double), ("learned", C.c_int32),
         ("device", C.c_int32), ("nload", C.c_int32),
-        ("filter_pde", C.c_int32), ("KF", _dp),
+        ("filter_pde", C.c_int32), ("KF", _dp), ("unsmoothed", C.c_int32),
     ]
 
 

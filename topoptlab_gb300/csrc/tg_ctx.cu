@@ -274,6 +274,11 @@ void ctx_init(Ctx& c, const tg_problem& p) {
   // L == 1 with multigrid: the fine grid is the coarsest level and the
   // "V-cycle" is the dense direct solve of the fine operator
   c.L = (c.precond == TG_PRECOND_GMG) ? choose_levels(g, p.nlevels) : 1;
+  c.unsmoothed = p.unsmoothed;
+  TG_REQUIRE(c.unsmoothed == 0 ||
+                 (c.precond == TG_PRECOND_GMG && (c.unsmoothed & 1) == 0 &&
+                  (c.unsmoothed >> std::max(c.L - 1, 0)) == 0),
+             "unsmoothed: only levels 1 .. nlevels-2 can be left unsmoothed");
   std::vector<std::vector<uint8_t>> fixl{fix};
   c.lv.push_back(new Level());
   c.lv[0]->g = g;
@@ -513,6 +518,25 @@ template <typename T> void vcycle(Ctx& c, int l, const T* b, T* x, bool prescale
     }
     return;
   }
+  auto smoothed = [&](int k) { return k < c.L - 1 && !((c.unsmoothed >> k) & 1); };
+  if (l > 0 && !smoothed(l)) {
+    // no smoothing on this level (x = 0, residual = b): restrict b on, take
+    // the coarser correction and prolongate it back
+    Level& w = *c.lv[l + 1];
+    const bool fuse = smoothed(l + 1);
+    {
+      ProfScope ps(PK_TRANSFER, c.st);
+      if (fuse)
+        restrict_<T>(v.g, w.g, w.fix, b, LvBufs<T>::b(w), c.st, LvBufs<T>::dinv(w),
+                     LvBufs<T>::t(w), c.omega);
+      else
+        restrict_<T>(v.g, w.g, w.fix, b, LvBufs<T>::b(w), c.st);
+    }
+    vcycle<T>(c, l + 1, LvBufs<T>::b(w), LvBufs<T>::x(w), fuse);
+    ProfScope ps(PK_TRANSFER, c.st);
+    prolong_set<T>(v.g, w.g, v.fix, LvBufs<T>::x(w), x, c.st);
+    return;
+  }
   // 2*nsmooth - 1 sweeps swap the buffers an odd number of times: starting in
   // the scratch buffer ends in x (no copy at the end of the level)
   T* bufs[2] = {x, LvBufs<T>::t(v)};
@@ -528,12 +552,12 @@ template <typename T> void vcycle(Ctx& c, int l, const T* b, T* x, bool prescale
   T* r = LvBufs<T>::r(v);
   level_apply<T>(c, l, bufs[cur], r, b, AM_RES);
   Level& w = *c.lv[l + 1];
-  const bool fuse = l + 1 < c.L - 1;       // the coarsest level has no smoother
+  const bool fuse = smoothed(l + 1);       // the coarsest level has no smoother
   // the two levels below this one (the last smoothed level, on the small-grid
   // stencil, and the coarsest solve) in one cooperative launch
   const int64_t tail_pairs = w.g.nnodes() * w.g.ndof;
   if (l + 3 == c.L && tune_coarse_tail() && tail_pairs < tune_stencil_small_pairs() &&
-      tail_pairs <= TAIL_MAX_PAIRS) {
+      tail_pairs <= TAIL_MAX_PAIRS && smoothed(l + 1)) {
     Level& k = *c.lv[c.L - 1];
     TailArgs<T> a;
     a.gp = v.g; a.gt = w.g; a.gc = k.g;

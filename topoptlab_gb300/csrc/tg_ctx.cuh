@@ -56,6 +56,7 @@ struct Ctx {
   double volfrac = 0.5, rmin = 1.5, eps = 1e-9, penal = 3.0, move = 0.2;
   int ft = 1;
   int precond = 0, precision = 0, nsmooth = 2, maxiter = 2000, learned = 0;
+  int unsmoothed = 0;           // bit l: level l not smoothed (tg_problem.unsmoothed)
   double omega = 0.6, rtol = 1e-8, inner_rtol = 1e-4;
   double bnorm = 0.0;           // ||M f|| of load case 0
   int nload = 1;                // load cases: f and u hold nload vectors each

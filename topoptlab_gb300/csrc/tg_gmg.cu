@@ -931,7 +931,7 @@ template void restrict_<float>(const Grid&, const Grid&, const uint8_t*, const f
 
 // prolongation: one thread per fine node, all components; the 1, 2, 4 or 8
 // coarse parents follow from the parity of the fine coordinates
-template <int NDIM, int NDOF, typename T, bool CG = false>
+template <int NDIM, int NDOF, typename T, bool CG = false, bool SET = false>
 __device__ __forceinline__ void prolong_one(const Grid& gf, const Grid& gc, const uint8_t* fixf,
                                             const T* __restrict__ xc, T* __restrict__ xf,
                                             int64_t i) {
@@ -953,32 +953,46 @@ __device__ __forceinline__ void prolong_one(const Grid& gf, const Grid& gc, cons
   }
   const uint8_t m = fixf[i];
 #pragma unroll
-  for (int c = 0; c < NDOF; ++c)
-    if (!((m >> c) & 1)) xf[i * NDOF + c] += w * acc[c];
+  for (int c = 0; c < NDOF; ++c) {
+    if (SET) xf[i * NDOF + c] = ((m >> c) & 1) ? T(0) : w * acc[c];
+    else if (!((m >> c) & 1)) xf[i * NDOF + c] += w * acc[c];
+  }
 }
-template <int NDIM, int NDOF, typename T>
+template <int NDIM, int NDOF, typename T, bool SET>
 __global__ void __launch_bounds__(256) k_prolong_add(Grid gf, Grid gc, const uint8_t* fixf,
                                                      const T* __restrict__ xc,
                                                      T* __restrict__ xf) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i < gf.nnodes()) prolong_one<NDIM, NDOF, T>(gf, gc, fixf, xc, xf, i);
+  if (i < gf.nnodes()) prolong_one<NDIM, NDOF, T, false, SET>(gf, gc, fixf, xc, xf, i);
 }
 
-template <typename T>
-void prolong_add(const Grid& gf, const Grid& gc, const uint8_t* fixf, const T* xc, T* xf,
-                 cudaStream_t st) {
+template <typename T, bool SET>
+static void prolong_launch(const Grid& gf, const Grid& gc, const uint8_t* fixf, const T* xc, T* xf,
+                           cudaStream_t st) {
   const unsigned blocks = (unsigned)cdiv(gf.nnodes(), 256);
   switch (gf.ndim * 10 + gf.ndof) {
-    case 33: k_prolong_add<3, 3, T><<<blocks, 256, 0, st>>>(gf, gc, fixf, xc, xf); break;
-    case 31: k_prolong_add<3, 1, T><<<blocks, 256, 0, st>>>(gf, gc, fixf, xc, xf); break;
-    case 22: k_prolong_add<2, 2, T><<<blocks, 256, 0, st>>>(gf, gc, fixf, xc, xf); break;
-    case 21: k_prolong_add<2, 1, T><<<blocks, 256, 0, st>>>(gf, gc, fixf, xc, xf); break;
+    case 33: k_prolong_add<3, 3, T, SET><<<blocks, 256, 0, st>>>(gf, gc, fixf, xc, xf); break;
+    case 31: k_prolong_add<3, 1, T, SET><<<blocks, 256, 0, st>>>(gf, gc, fixf, xc, xf); break;
+    case 22: k_prolong_add<2, 2, T, SET><<<blocks, 256, 0, st>>>(gf, gc, fixf, xc, xf); break;
+    case 21: k_prolong_add<2, 1, T, SET><<<blocks, 256, 0, st>>>(gf, gc, fixf, xc, xf); break;
     default: throw Error{EINVAL_, "unsupported (ndim, nnode_dof)"};
   }
   TG_CHECK_LAUNCH();
 }
+template <typename T>
+void prolong_add(const Grid& gf, const Grid& gc, const uint8_t* fixf, const T* xc, T* xf,
+                 cudaStream_t st) {
+  prolong_launch<T, false>(gf, gc, fixf, xc, xf, st);
+}
+template <typename T>
+void prolong_set(const Grid& gf, const Grid& gc, const uint8_t* fixf, const T* xc, T* xf,
+                 cudaStream_t st) {
+  prolong_launch<T, true>(gf, gc, fixf, xc, xf, st);
+}
 template void prolong_add<double>(const Grid&, const Grid&, const uint8_t*, const double*, double*, cudaStream_t);
 template void prolong_add<float>(const Grid&, const Grid&, const uint8_t*, const float*, float*, cudaStream_t);
+template void prolong_set<double>(const Grid&, const Grid&, const uint8_t*, const double*, double*, cudaStream_t);
+template void prolong_set<float>(const Grid&, const Grid&, const uint8_t*, const float*, float*, cudaStream_t);
 
 // ---------------------------------------------------------------------------
 // coarsest level: dense matrix and blocked Gauss-Jordan inverse (FP64)

@@ -111,6 +111,10 @@ void restrict_(const Grid& gf, const Grid& gc, const uint8_t* fixc, const T* rf,
 template <typename T>
 void prolong_add(const Grid& gf, const Grid& gc, const uint8_t* fixf, const T* xc, T* xf,
                  cudaStream_t st);
+// xf = Mf P xc (fixed DOFs 0)
+template <typename T>
+void prolong_set(const Grid& gf, const Grid& gc, const uint8_t* fixf, const T* xc, T* xf,
+                 cudaStream_t st);
 
 // The bottom of a V-cycle in one cooperative launch: restriction of the
 // parent level's residual rp into the tail level (with its first smoothing
