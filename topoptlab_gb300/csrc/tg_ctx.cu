@@ -301,6 +301,7 @@ void ctx_init(Ctx& c, const tg_problem& p) {
                              "preconditioner gb300-jacobi)");
     c.ldc = cdiv(c.nc, 32) * 32;
     c.Dc.alloc(c.ldc * c.ldc);
+    if (c.precision == TG_PREC_MIXED && c.L > 1) c.Dc32.alloc(c.ldc * c.ldc);
     c.gjwork.alloc(32 * 32 + 2 * 32 * c.ldc);   // pivot tile, row panel R, saved panel X
     c.tailbar.alloc(1);
     TG_CUDA(cudaMemsetAsync(c.tailbar.p, 0, sizeof(GridBar), c.st));
@@ -463,6 +464,7 @@ void build_hierarchy(Ctx& c) {
   ProfScope ps(PK_COARSE_INV, c.st);
   if (mixed && c.L > 1) gj_inverse_dw(c.Dc, c.nc, c.ldc, c.gjwork, c.st);
   else gj_inverse(c.Dc, c.nc, c.ldc, c.gjwork, c.st);
+  if (c.Dc32.p) d2f(c.ldc * c.ldc, c.Dc, c.Dc32, c.st);
   c.built = true;
 }
 
@@ -510,7 +512,13 @@ template <typename T> void vcycle(Ctx& c, int l, const T* b, T* x, bool prescale
   if (l == c.L - 1) {
     {
       ProfScope ps(PK_TRANSFER, c.st);
-      dense_apply<T>(c.Dc, c.nc, c.ldc, b, x, c.gjwork, c.st);   // GJ scratch is idle here
+      // GJ scratch is idle here
+      if constexpr (std::is_same<T, float>::value) {
+        if (c.Dc32.p) dense_apply(c.Dc32.p, c.nc, c.ldc, b, x, c.gjwork, c.st);
+        else dense_apply<T>(c.Dc, c.nc, c.ldc, b, x, c.gjwork, c.st);
+      } else {
+        dense_apply<T>(c.Dc, c.nc, c.ldc, b, x, c.gjwork, c.st);
+      }
     }
     if (dot_op >= 0) {
       ProfScope ps(PK_VECTOR, c.st);
@@ -568,6 +576,7 @@ template <typename T> void vcycle(Ctx& c, int l, const T* b, T* x, bool prescale
     a.rt = LvBufs<T>::r(w);
     a.bc = LvBufs<T>::b(k); a.xc = LvBufs<T>::x(k);
     a.Dc = c.Dc; a.nc = c.nc; a.ldc = c.ldc; a.part = c.gjwork;
+    a.Dc32 = std::is_same<T, float>::value ? c.Dc32.p : nullptr;
     a.omega = (T)c.omega; a.nsmooth = c.nsmooth; a.bar = c.tailbar;
     const int mode = tune_coarse_tail();
     a.cluster = mode == 1 ? 16 : 0;

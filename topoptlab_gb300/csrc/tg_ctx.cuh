@@ -88,6 +88,7 @@ struct Ctx {
   int L = 1;
   int64_t nc = 0, ldc = 0;
   DevBuf<double> Dc, gjwork;
+  DevBuf<float> Dc32;           // mixed contexts: the coarsest inverse in FP32 for the FP32 V-cycle
   DevBuf<GridBar> tailbar;      // barrier of the cooperative V-cycle bottom
   double g_oc = 0.0;            // OC carry
   int iter = 0;

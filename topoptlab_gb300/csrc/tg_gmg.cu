@@ -1437,6 +1437,22 @@ __device__ __forceinline__ void dense_sum_one(const double* __restrict__ part, i
   for (int k = 0; k < DA_CHUNKS; ++k) s += ldv<CG>(part + k * n + row);
   x[row] = (T)s;
 }
+// the same with the inverse stored in FP32 (the FP32 V-cycle of mixed
+// contexts): half the bytes per cycle, FP32 products summed per lane in FP32,
+// the warp and chunk sums in FP64
+template <bool CG = false>
+__device__ __forceinline__ void dense_partial32_one(const float* __restrict__ Dinv, int64_t n,
+                                                    int64_t ld, const float* __restrict__ b,
+                                                    double* __restrict__ part, int64_t row,
+                                                    int chunk, int lane) {
+  const int64_t w = (n + DA_CHUNKS - 1) / DA_CHUNKS;
+  const int64_t j0 = chunk * w, j1 = min(n, j0 + w);
+  float acc = 0.f;
+#pragma unroll 4
+  for (int64_t j = j0 + lane; j < j1; j += 32) acc = fmaf(Dinv[row * ld + j], ldv<CG>(b + j), acc);
+  const double s = warp_sum((double)acc);
+  if (lane == 0) part[chunk * n + row] = s;
+}
 template <typename T>
 __global__ void __launch_bounds__(256) k_dense_partial(const double* __restrict__ Dinv, int64_t n,
                                                       int64_t ld, const T* __restrict__ b,
@@ -1460,6 +1476,20 @@ void dense_apply(const double* Dinv, int64_t n, int64_t ld, const T* b, T* x, do
 }
 template void dense_apply<double>(const double*, int64_t, int64_t, const double*, double*, double*, cudaStream_t);
 template void dense_apply<float>(const double*, int64_t, int64_t, const float*, float*, double*, cudaStream_t);
+
+__global__ void __launch_bounds__(256) k_dense_partial_f32(const float* __restrict__ Dinv, int64_t n,
+                                                          int64_t ld, const float* __restrict__ b,
+                                                          double* __restrict__ part) {
+  const int64_t row = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (row < n) dense_partial32_one<false>(Dinv, n, ld, b, part, row, blockIdx.y, threadIdx.x & 31);
+}
+void dense_apply(const float* Dinv, int64_t n, int64_t ld, const float* b, float* x, double* work,
+                 cudaStream_t st) {
+  k_dense_partial_f32<<<dim3((unsigned)cdiv(n, 8), DA_CHUNKS), 256, 0, st>>>(Dinv, n, ld, b, work);
+  TG_CHECK_LAUNCH();
+  k_dense_sum<float><<<(unsigned)cdiv(n, 256), 256, 0, st>>>(work, n, x);
+  TG_CHECK_LAUNCH();
+}
 
 // ---------------------------------------------------------------------------
 // the bottom of the V-cycle in one cooperative launch
@@ -1521,8 +1551,15 @@ __global__ void __launch_bounds__(3 * SMALL_PAIRS) k_coarse_tail(TailArgs<T> a) 
   {
     const int lane = threadIdx.x & 31;
     const int64_t w0 = gtid >> 5, nw = gsz >> 5;
-    for (int64_t w = w0; w < a.nc * DA_CHUNKS; w += nw)
+    for (int64_t w = w0; w < a.nc * DA_CHUNKS; w += nw) {
+      if constexpr (std::is_same<T, float>::value) {
+        if (a.Dc32) {
+          dense_partial32_one<true>(a.Dc32, a.nc, a.ldc, a.bc, a.part, w % a.nc, (int)(w / a.nc), lane);
+          continue;
+        }
+      }
       dense_partial_one<T, true>(a.Dc, a.nc, a.ldc, a.bc, a.part, w % a.nc, (int)(w / a.nc), lane);
+    }
   }
   if (!tail_sync<CLUSTER>(a.bar)) return;
   for (int64_t r = gtid; r < a.nc; r += gsz) dense_sum_one<T, true>(a.part, a.nc, a.xc, r);

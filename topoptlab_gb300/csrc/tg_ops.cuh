@@ -135,6 +135,7 @@ template <typename T> struct TailArgs {
   T *bt, *xt, *tt, *rt;                    // tail vectors
   T *bc, *xc;                              // coarsest vectors
   const double* Dc;                        // coarsest inverse
+  const float* Dc32;                       // the same in FP32 (T = float; null: Dc)
   int64_t nc, ldc;
   double* part;                            // >= 8 * nc doubles
   T omega;
@@ -160,6 +161,9 @@ void gj_inverse(double* D, int64_t n, int64_t ld, double* work, cudaStream_t st)
 void gj_inverse_dw(double* D, int64_t n, int64_t ld, double* work, cudaStream_t st);
 template <typename T>
 void dense_apply(const double* Dinv, int64_t n, int64_t ld, const T* b, T* x,
+                 double* work /* >= 8*n */, cudaStream_t st);
+// the inverse stored in FP32 (mixed contexts' FP32 V-cycle)
+void dense_apply(const float* Dinv, int64_t n, int64_t ld, const float* b, float* x,
                  double* work /* >= 8*n */, cudaStream_t st);
 
 // ---------------------------------------------------------------------------
