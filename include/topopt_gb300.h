@@ -300,6 +300,10 @@ int32_t tg_stats(int32_t reset, int64_t* launches, double* prof_ms, int64_t* pro
  * too large for the small-grid kernel with TMA-staged coefficients (value
  * > 1: at most value - 1 node rows per CTA); 0 (default) runs the
  * register-path kernel.  Same results.
+ * TG_TUNE_PDL: value != 0 (default) launches the kernels of the PCG iteration
+ * with programmatic dependent launch (a kernel is scheduled while its
+ * predecessor finishes and waits for it before touching memory); 0 launches
+ * them one after another.  Same results.
  * TG_TUNE_TAIL_BARRIER_TIMEOUT:
  * like TG_TUNE_OC_BARRIER_TIMEOUT for the next such launch (the solve or
  * tg_vcycle call returns TG_ETIMEOUT).  Unknown keys return TG_EINVAL. */
@@ -308,7 +312,8 @@ enum {
   TG_TUNE_OC_BARRIER_TIMEOUT = 2,
   TG_TUNE_COARSE_TAIL = 3,
   TG_TUNE_TAIL_BARRIER_TIMEOUT = 4,
-  TG_TUNE_STENCIL_TMA = 5
+  TG_TUNE_STENCIL_TMA = 5,
+  TG_TUNE_PDL = 6
 };
 int32_t tg_tune(int32_t key, int64_t value);
 /* edofMat (elements/bilinear_quadrilateral.py:7-48, trilinear_hexahedron.py:7-58)

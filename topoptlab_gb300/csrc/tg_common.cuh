@@ -85,6 +85,35 @@ void set_smem_limit(const void* func, int bytes);
     TG_CUDA(cudaGetLastError());          \
   } while (0)
 
+// Programmatic dependent launch for the small kernels of the PCG iteration:
+// launched with launch_pdl, a kernel may be scheduled while its predecessor
+// on the stream still runs (once every block of the predecessor has passed
+// pdl_trigger), which hides the launch and block ramp-up between dependent
+// kernels.  Every kernel launched this way calls pdl_wait() first, in every
+// thread, before any global memory access: it returns once the predecessor
+// grid has completed and its writes are visible, so the stream order of the
+// data is unchanged.  Both are no-ops for a kernel launched normally.
+bool pdl_on();            // tg_tune(TG_TUNE_PDL), default on
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+template <typename... ExpTypes, typename... ActTypes>
+inline void launch_pdl(void (*kernel)(ExpTypes...), dim3 grid, dim3 block, size_t smem,
+                       cudaStream_t st, ActTypes&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl_on() ? 1 : 0;
+  TG_CUDA(cudaLaunchKernelEx(&cfg, kernel, std::forward<ActTypes>(args)...));
+}
+
 // Optional event timing of one kernel family (see tg_profile_kernel):
 // prof_begin/prof_end bracket the launches of family `kind` on stream st.
 // Families are disjoint; a composite region (e.g. the coarsest inverse) is

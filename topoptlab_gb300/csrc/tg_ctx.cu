@@ -690,6 +690,8 @@ static void run_iteration(Ctx& c, Ctx::IterGraph& gr, F&& body) {
 }
 
 __global__ void k_loop_ctl(PCGState* s, double tol, int maxit) {
+  pdl_wait();
+  pdl_trigger();
   s->tol = tol;
   s->maxit = maxit;
 }
@@ -698,6 +700,7 @@ __device__ __host__ inline bool pcg_continue(const PCGState& s) {
   return isfinite(s.rr) && sqrt(s.rr) >= s.tol && s.iter < s.maxit;
 }
 __global__ void k_loop_continue(cudaGraphConditionalHandle h, const PCGState* s) {
+  pdl_wait();
   cudaGraphSetConditional(h, pcg_continue(*s) ? 1u : 0u);
 }
 
@@ -746,7 +749,7 @@ static int run_loop(Ctx& c, Ctx::IterGraph& gr, Ctx::LoopGraph& lg, double tol, 
                                           cudaStreamCaptureModeThreadLocal));
     try {
       body();
-      k_loop_continue<<<1, 1, 0, c.st>>>(lg.h, c.pcg);
+      launch_pdl(k_loop_continue, dim3(1), dim3(1), 0, c.st, lg.h, (const PCGState*)c.pcg.p);
       TG_CHECK_LAUNCH();
     } catch (...) {
       cudaGraph_t g2 = nullptr;

@@ -425,6 +425,8 @@ template <typename TA, typename TB>
 __global__ void __launch_bounds__(RED_THREADS) k_dot(int64_t n, const TA* __restrict__ a,
                                                     const TB* __restrict__ b, double* part,
                                                     PCGState* st, int op) {
+  pdl_wait();
+  pdl_trigger();
   __shared__ double sh[32];
   __shared__ int last;
   TA acc = TA(0);
@@ -467,7 +469,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_dot(int64_t n, const TA* __rest
 
 template <typename TA, typename TB>
 void dot(int64_t n, const TA* a, const TB* b, double* part, PCGState* st, int op, cudaStream_t s) {
-  k_dot<TA, TB><<<red_blocks(n), RED_THREADS, 0, s>>>(n, a, b, part, st, op);
+  launch_pdl(k_dot<TA, TB>, dim3(red_blocks(n)), dim3(RED_THREADS), 0, s, n, a, b, part, st, op);
   TG_CHECK_LAUNCH();
 }
 template void dot<double, double>(int64_t, const double*, const double*, double*, PCGState*, int, cudaStream_t);
@@ -475,6 +477,8 @@ template void dot<float, float>(int64_t, const float*, const float*, double*, PC
 
 template <typename T>
 __global__ void k_update_p(int64_t n, const T* __restrict__ z, T* __restrict__ p, const PCGState* st) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const T beta = (T)st->beta;
   const bool first = st->iter == 0;
@@ -500,7 +504,7 @@ __global__ void k_update_p(int64_t n, const T* __restrict__ z, T* __restrict__ p
 template <typename T>
 void update_p(int64_t n, const T* z, T* p, const PCGState* st, cudaStream_t s) {
   const int64_t nt = sizeof(T) == 4 ? n / 4 + (n % 4) : n;
-  k_update_p<T><<<(unsigned)cdiv(nt, 256), 256, 0, s>>>(n, z, p, st);
+  launch_pdl(k_update_p<T>, dim3((unsigned)cdiv(nt, 256)), dim3(256), 0, s, n, z, p, st);
   TG_CHECK_LAUNCH();
 }
 template void update_p<double>(int64_t, const double*, double*, const PCGState*, cudaStream_t);
@@ -508,6 +512,8 @@ template void update_p<float>(int64_t, const float*, float*, const PCGState*, cu
 
 __global__ void k_update_p_corr(int64_t n, const float* __restrict__ z, const float* __restrict__ w,
                                 float* __restrict__ p, const PCGState* st) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const float beta = (float)st->beta;
   const float gam = -(float)(st->wz * st->wawinv);
@@ -534,7 +540,7 @@ __global__ void k_update_p_corr(int64_t n, const float* __restrict__ z, const fl
 void update_p_corr(int64_t n, const float* z, const float* w, float* p, const PCGState* st,
                    cudaStream_t s) {
   const int64_t nt = n / 4 + (n % 4);
-  k_update_p_corr<<<(unsigned)cdiv(nt, 256), 256, 0, s>>>(n, z, w, p, st);
+  launch_pdl(k_update_p_corr, dim3((unsigned)cdiv(nt, 256)), dim3(256), 0, s, n, z, w, p, st);
   TG_CHECK_LAUNCH();
 }
 __global__ void k_deflate_start(int64_t n, const float* __restrict__ w, const float* __restrict__ aw,
@@ -564,6 +570,8 @@ template <typename T>
 __global__ void __launch_bounds__(RED_THREADS) k_update_xr(int64_t n, const T* __restrict__ p,
                                                           const T* __restrict__ q, T* __restrict__ x,
                                                           T* __restrict__ r, double* part, PCGState* st) {
+  pdl_wait();
+  pdl_trigger();
   __shared__ double sh[32];
   __shared__ int last;
   const T alpha = (T)st->alpha;
@@ -618,7 +626,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_update_xr(int64_t n, const T* _
 template <typename T>
 void update_xr(int64_t n, const T* p, const T* q, T* x, T* r, double* part, PCGState* st,
                cudaStream_t s) {
-  k_update_xr<T><<<red_blocks(n), RED_THREADS, 0, s>>>(n, p, q, x, r, part, st);
+  launch_pdl(k_update_xr<T>, dim3(red_blocks(n)), dim3(RED_THREADS), 0, s, n, p, q, x, r, part, st);
   TG_CHECK_LAUNCH();
 }
 template void update_xr<double>(int64_t, const double*, const double*, double*, double*, double*, PCGState*, cudaStream_t);
@@ -662,6 +670,8 @@ void add_scaled_f32(int64_t n, const float* d, const PCGState* st, double* x, cu
 template <typename T>
 __global__ void k_scale_mul(int64_t n, T a, const T* __restrict__ d, const T* __restrict__ b,
                             T* __restrict__ x) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if constexpr (sizeof(T) == 4) {         // thread per 4 values, 16-byte accesses
     const int64_t n4 = n / 4;
@@ -681,7 +691,7 @@ __global__ void k_scale_mul(int64_t n, T a, const T* __restrict__ d, const T* __
 template <typename T>
 void scale_mul(int64_t n, double a, const T* d, const T* b, T* x, cudaStream_t s) {
   const int64_t nt = sizeof(T) == 4 ? n / 4 + (n % 4) : n;
-  k_scale_mul<T><<<(unsigned)cdiv(nt, 256), 256, 0, s>>>(n, (T)a, d, b, x);
+  launch_pdl(k_scale_mul<T>, dim3((unsigned)cdiv(nt, 256)), dim3(256), 0, s, n, (T)a, d, b, x);
   TG_CHECK_LAUNCH();
 }
 template void scale_mul<double>(int64_t, double, const double*, const double*, double*, cudaStream_t);

@@ -162,6 +162,8 @@ constexpr size_t apply_smem_v2() {
 
 template <int NDIM, int NDOF, typename T, typename S, int KIND, int MODE>
 __global__ void __launch_bounds__(256, sizeof(T) == 8 ? 2 : 4) k_fine_apply(ApplyArgs<T, S> a) {
+  pdl_wait();
+  pdl_trigger();
   using TL = Tile<NDIM>;
   using L = SLayout<NDIM>;
   constexpr int TX = TL::X, TY = TL::Y, TZ = TL::Z;
@@ -307,6 +309,8 @@ template <int NDOF, typename T, int KIND> constexpr size_t smem() {
 template <int NDOF, typename T, typename S, int KIND, int MODE, int DOTK = -1>
 __global__ void __launch_bounds__(zs::NT, sizeof(T) == 8 ? 2 : 4) k_fine_zstream(ApplyArgs<T, S> a,
                                                                                 int zc) {
+  pdl_wait();
+  pdl_trigger();
   using namespace zs;
   constexpr int NC = 8;
   constexpr int NE = NC * NDOF;
@@ -585,6 +589,8 @@ __device__ __forceinline__ void face_xz(float (&F)[4][NDOF]) {
 // zc unused: blockIdx.z takes node planes [z nnz / gridDim.z, (z+1) nnz / gridDim.z)
 template <int NDOF, typename S, int KIND, int MODE, int DOTK = -1>
 __global__ void __launch_bounds__(zp::NT, 3) k_fine_zpair(ApplyArgs<float, S> a, int zc) {
+  pdl_wait();
+  pdl_trigger();
   using namespace zp;
   static_assert(32 % JY == 0, "the y shuffle needs warps made of whole rows of pairs");
   using T = float;
@@ -864,7 +870,8 @@ static void launch_zstream(const ApplyArgs<T, S>& a, cudaStream_t st) {
     if (DOTK >= 0 && sh.ctas() > RED_BLOCKS)
       throw Error{EINVAL_, "fused dot: more CTAs than partial-sum slots"};
     prof_begin(pk, st);
-    kern<<<dim3((unsigned)sh.gy, (unsigned)sh.gx, (unsigned)sh.chunks), zp::NT, smem, st>>>(a, sh.zc);
+    launch_pdl(kern, dim3((unsigned)sh.gy, (unsigned)sh.gx, (unsigned)sh.chunks), dim3(zp::NT),
+               smem, st, a, sh.zc);
     prof_end(pk, st);
     TG_CHECK_LAUNCH();
     return;
@@ -877,7 +884,8 @@ static void launch_zstream(const ApplyArgs<T, S>& a, cudaStream_t st) {
   if (DOTK >= 0 && sh.ctas() > RED_BLOCKS)
     throw Error{EINVAL_, "fused dot: more CTAs than partial-sum slots"};
   prof_begin(pk, st);
-  kern<<<dim3((unsigned)gy, (unsigned)gx, (unsigned)chunks), zs::NT, smem, st>>>(a, zc);
+  launch_pdl(kern, dim3((unsigned)gy, (unsigned)gx, (unsigned)chunks), dim3(zs::NT), smem, st, a,
+             zc);
   prof_end(pk, st);
   TG_CHECK_LAUNCH();
 }
@@ -900,7 +908,7 @@ static void launch_apply(const ApplyArgs<T, S>& a, cudaStream_t st) {
   const int pk = std::is_same<T, double>::value ? PK_FINE_F64
                  : (std::is_same<S, float>::value ? PK_FINE_F32 : PK_FINE_BF16);
   prof_begin(pk, st);
-  kern<<<grid, 256, smem, st>>>(a);
+  launch_pdl(kern, grid, dim3(256), smem, st, a);
   prof_end(pk, st);
   TG_CHECK_LAUNCH();
 }

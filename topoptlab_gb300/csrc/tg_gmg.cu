@@ -86,6 +86,8 @@ __global__ void __launch_bounds__(NDOF * 256) k_stencil_apply(Grid g, int TY, in
                                                              T* __restrict__ y,
                                                              const T* __restrict__ b,
                                                              const T* __restrict__ dinv, T omega) {
+  pdl_wait();
+  pdl_trigger();
   constexpr int NP = (NDIM == 3) ? 3 : 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* us = reinterpret_cast<T*>(smem_raw);
@@ -204,6 +206,8 @@ __global__ void __launch_bounds__(3 * SMALL_PAIRS) k_stencil_small(Grid g, const
                                                                   const T* __restrict__ b,
                                                                   const T* __restrict__ dinv,
                                                                   T omega) {
+  pdl_wait();
+  pdl_trigger();
   __shared__ T part[3][SMALL_PAIRS];
   stencil_small_vb<NDIM, NDOF, T, MODE>(g, A, u, y, b, dinv, omega, blockIdx.x, part);
 }
@@ -465,9 +469,9 @@ void stencil_apply(const Grid& g, const T* A, const T* u, T* y, const T* b, cons
   if (pairs < tune_stencil_small_pairs()) {
     const unsigned blocks = (unsigned)cdiv(pairs, SMALL_PAIRS);
 #define TG_SS(ND, NF)                                                                          \
-  if (mode == AM_Y) k_stencil_small<ND, NF, T, AM_Y><<<blocks, 3 * SMALL_PAIRS, 0, st>>>(g, A, u, y, b, dinv, (T)omega); \
-  else if (mode == AM_RES) k_stencil_small<ND, NF, T, AM_RES><<<blocks, 3 * SMALL_PAIRS, 0, st>>>(g, A, u, y, b, dinv, (T)omega); \
-  else k_stencil_small<ND, NF, T, AM_JACOBI><<<blocks, 3 * SMALL_PAIRS, 0, st>>>(g, A, u, y, b, dinv, (T)omega);
+  if (mode == AM_Y) launch_pdl(k_stencil_small<ND, NF, T, AM_Y>, dim3(blocks), dim3(3 * SMALL_PAIRS), 0, st, g, A, u, y, b, dinv, (T)omega); \
+  else if (mode == AM_RES) launch_pdl(k_stencil_small<ND, NF, T, AM_RES>, dim3(blocks), dim3(3 * SMALL_PAIRS), 0, st, g, A, u, y, b, dinv, (T)omega); \
+  else launch_pdl(k_stencil_small<ND, NF, T, AM_JACOBI>, dim3(blocks), dim3(3 * SMALL_PAIRS), 0, st, g, A, u, y, b, dinv, (T)omega);
     switch (g.ndim * 10 + g.ndof) {
       case 33: TG_SS(3, 3) break;
       case 31: TG_SS(3, 1) break;
@@ -489,9 +493,9 @@ void stencil_apply(const Grid& g, const T* A, const T* u, T* y, const T* b, cons
   const unsigned nt = 256u * (unsigned)g.ndof;
   const int key = g.ndim * 10 + g.ndof;
 #define TG_SA(ND, NF)                                                                          \
-  if (mode == AM_Y) k_stencil_apply<ND, NF, T, AM_Y><<<grid, nt, smem, st>>>(g, TY, TX, A, u, y, b, dinv, (T)omega); \
-  else if (mode == AM_RES) k_stencil_apply<ND, NF, T, AM_RES><<<grid, nt, smem, st>>>(g, TY, TX, A, u, y, b, dinv, (T)omega); \
-  else k_stencil_apply<ND, NF, T, AM_JACOBI><<<grid, nt, smem, st>>>(g, TY, TX, A, u, y, b, dinv, (T)omega);
+  if (mode == AM_Y) launch_pdl(k_stencil_apply<ND, NF, T, AM_Y>, dim3(grid), dim3(nt), smem, st, g, TY, TX, A, u, y, b, dinv, (T)omega); \
+  else if (mode == AM_RES) launch_pdl(k_stencil_apply<ND, NF, T, AM_RES>, dim3(grid), dim3(nt), smem, st, g, TY, TX, A, u, y, b, dinv, (T)omega); \
+  else launch_pdl(k_stencil_apply<ND, NF, T, AM_JACOBI>, dim3(grid), dim3(nt), smem, st, g, TY, TX, A, u, y, b, dinv, (T)omega);
   switch (key) {
     case 33: TG_SA(3, 3) break;
     case 31: TG_SA(3, 1) break;
@@ -907,6 +911,8 @@ __global__ void __launch_bounds__(256) k_restrict(Grid gf, Grid gc, const uint8_
                                                   const T* __restrict__ rf, T* __restrict__ bc,
                                                   const T* __restrict__ dinvc, T* __restrict__ xc,
                                                   T omega) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t < gc.nnodes() * NDOF) restrict_one<NDIM, NDOF, T>(gf, gc, fixc, rf, bc, dinvc, xc, omega, t);
 }
@@ -916,10 +922,10 @@ void restrict_(const Grid& gf, const Grid& gc, const uint8_t* fixc, const T* rf,
                cudaStream_t st, const T* dinvc, T* xc, double omega) {
   const unsigned blocks = (unsigned)cdiv(gc.nnodes() * gc.ndof, 256);
   switch (gf.ndim * 10 + gf.ndof) {
-    case 33: k_restrict<3, 3, T><<<blocks, 256, 0, st>>>(gf, gc, fixc, rf, bc, dinvc, xc, (T)omega); break;
-    case 31: k_restrict<3, 1, T><<<blocks, 256, 0, st>>>(gf, gc, fixc, rf, bc, dinvc, xc, (T)omega); break;
-    case 22: k_restrict<2, 2, T><<<blocks, 256, 0, st>>>(gf, gc, fixc, rf, bc, dinvc, xc, (T)omega); break;
-    case 21: k_restrict<2, 1, T><<<blocks, 256, 0, st>>>(gf, gc, fixc, rf, bc, dinvc, xc, (T)omega); break;
+    case 33: launch_pdl(k_restrict<3, 3, T>, dim3(blocks), dim3(256), 0, st, gf, gc, fixc, rf, bc, dinvc, xc, (T)omega); break;
+    case 31: launch_pdl(k_restrict<3, 1, T>, dim3(blocks), dim3(256), 0, st, gf, gc, fixc, rf, bc, dinvc, xc, (T)omega); break;
+    case 22: launch_pdl(k_restrict<2, 2, T>, dim3(blocks), dim3(256), 0, st, gf, gc, fixc, rf, bc, dinvc, xc, (T)omega); break;
+    case 21: launch_pdl(k_restrict<2, 1, T>, dim3(blocks), dim3(256), 0, st, gf, gc, fixc, rf, bc, dinvc, xc, (T)omega); break;
     default: throw Error{EINVAL_, "unsupported (ndim, nnode_dof)"};
   }
   TG_CHECK_LAUNCH();
@@ -962,6 +968,8 @@ template <int NDIM, int NDOF, typename T, bool SET>
 __global__ void __launch_bounds__(256) k_prolong_add(Grid gf, Grid gc, const uint8_t* fixf,
                                                      const T* __restrict__ xc,
                                                      T* __restrict__ xf) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < gf.nnodes()) prolong_one<NDIM, NDOF, T, false, SET>(gf, gc, fixf, xc, xf, i);
 }
@@ -971,10 +979,10 @@ static void prolong_launch(const Grid& gf, const Grid& gc, const uint8_t* fixf, 
                            cudaStream_t st) {
   const unsigned blocks = (unsigned)cdiv(gf.nnodes(), 256);
   switch (gf.ndim * 10 + gf.ndof) {
-    case 33: k_prolong_add<3, 3, T, SET><<<blocks, 256, 0, st>>>(gf, gc, fixf, xc, xf); break;
-    case 31: k_prolong_add<3, 1, T, SET><<<blocks, 256, 0, st>>>(gf, gc, fixf, xc, xf); break;
-    case 22: k_prolong_add<2, 2, T, SET><<<blocks, 256, 0, st>>>(gf, gc, fixf, xc, xf); break;
-    case 21: k_prolong_add<2, 1, T, SET><<<blocks, 256, 0, st>>>(gf, gc, fixf, xc, xf); break;
+    case 33: launch_pdl(k_prolong_add<3, 3, T, SET>, dim3(blocks), dim3(256), 0, st, gf, gc, fixf, xc, xf); break;
+    case 31: launch_pdl(k_prolong_add<3, 1, T, SET>, dim3(blocks), dim3(256), 0, st, gf, gc, fixf, xc, xf); break;
+    case 22: launch_pdl(k_prolong_add<2, 2, T, SET>, dim3(blocks), dim3(256), 0, st, gf, gc, fixf, xc, xf); break;
+    case 21: launch_pdl(k_prolong_add<2, 1, T, SET>, dim3(blocks), dim3(256), 0, st, gf, gc, fixf, xc, xf); break;
     default: throw Error{EINVAL_, "unsupported (ndim, nnode_dof)"};
   }
   TG_CHECK_LAUNCH();
@@ -1457,11 +1465,15 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_dense_partial(const double* __restrict__ Dinv, int64_t n,
                                                       int64_t ld, const T* __restrict__ b,
                                                       double* __restrict__ part) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t row = blockIdx.x * 8 + (threadIdx.x >> 5);
   if (row < n) dense_partial_one<T>(Dinv, n, ld, b, part, row, blockIdx.y, threadIdx.x & 31);
 }
 template <typename T>
 __global__ void k_dense_sum(const double* __restrict__ part, int64_t n, T* __restrict__ x) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (row < n) dense_sum_one<T>(part, n, x, row);
 }
@@ -1469,9 +1481,9 @@ __global__ void k_dense_sum(const double* __restrict__ part, int64_t n, T* __res
 template <typename T>
 void dense_apply(const double* Dinv, int64_t n, int64_t ld, const T* b, T* x, double* work,
                  cudaStream_t st) {
-  k_dense_partial<T><<<dim3((unsigned)cdiv(n, 8), DA_CHUNKS), 256, 0, st>>>(Dinv, n, ld, b, work);
+  launch_pdl(k_dense_partial<T>, dim3(dim3((unsigned)cdiv(n, 8), DA_CHUNKS)), dim3(256), 0, st, Dinv, n, ld, b, work);
   TG_CHECK_LAUNCH();
-  k_dense_sum<T><<<(unsigned)cdiv(n, 256), 256, 0, st>>>(work, n, x);
+  launch_pdl(k_dense_sum<T>, dim3((unsigned)cdiv(n, 256)), dim3(256), 0, st, work, n, x);
   TG_CHECK_LAUNCH();
 }
 template void dense_apply<double>(const double*, int64_t, int64_t, const double*, double*, double*, cudaStream_t);
@@ -1480,14 +1492,16 @@ template void dense_apply<float>(const double*, int64_t, int64_t, const float*, 
 __global__ void __launch_bounds__(256) k_dense_partial_f32(const float* __restrict__ Dinv, int64_t n,
                                                           int64_t ld, const float* __restrict__ b,
                                                           double* __restrict__ part) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t row = blockIdx.x * 8 + (threadIdx.x >> 5);
   if (row < n) dense_partial32_one<false>(Dinv, n, ld, b, part, row, blockIdx.y, threadIdx.x & 31);
 }
 void dense_apply(const float* Dinv, int64_t n, int64_t ld, const float* b, float* x, double* work,
                  cudaStream_t st) {
-  k_dense_partial_f32<<<dim3((unsigned)cdiv(n, 8), DA_CHUNKS), 256, 0, st>>>(Dinv, n, ld, b, work);
+  launch_pdl(k_dense_partial_f32, dim3(dim3((unsigned)cdiv(n, 8), DA_CHUNKS)), dim3(256), 0, st, Dinv, n, ld, b, work);
   TG_CHECK_LAUNCH();
-  k_dense_sum<float><<<(unsigned)cdiv(n, 256), 256, 0, st>>>(work, n, x);
+  launch_pdl(k_dense_sum<float>, dim3((unsigned)cdiv(n, 256)), dim3(256), 0, st, work, n, x);
   TG_CHECK_LAUNCH();
 }
 

@@ -66,11 +66,13 @@ namespace {
 std::atomic<int64_t> g_small_pairs{150000};
 std::atomic<int> g_oc_timeout{0};
 std::atomic<int> g_tail{0};
+std::atomic<int> g_pdl{1};
 std::atomic<int> g_tail_timeout{0};
 }  // namespace
 int64_t tune_stencil_small_pairs() { return g_small_pairs.load(std::memory_order_relaxed); }
 bool tune_take_oc_barrier_timeout() { return g_oc_timeout.exchange(0) != 0; }
 int tune_coarse_tail() { return g_tail.load(std::memory_order_relaxed); }
+bool pdl_on() { return g_pdl.load(std::memory_order_relaxed) != 0; }
 bool tune_take_tail_barrier_timeout() { return g_tail_timeout.exchange(0) != 0; }
 
 namespace {
@@ -187,6 +189,9 @@ extern "C" int32_t tg_tune(int32_t key, int64_t value) {
       return TG_OK;
     case TG_TUNE_TAIL_BARRIER_TIMEOUT:
       tg::g_tail_timeout.store(value != 0 ? 1 : 0);
+      return TG_OK;
+    case TG_TUNE_PDL:
+      tg::g_pdl.store(value != 0 ? 1 : 0);
       return TG_OK;
     case TG_TUNE_STENCIL_TMA:
       if (value < 0 || value > 64) return TG_EINVAL;
