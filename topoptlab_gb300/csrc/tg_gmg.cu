@@ -1112,6 +1112,8 @@ __device__ __forceinline__ void gj_tile_inverse(double (&a)[TB][TB + 1], double 
 template <int TB>
 __global__ void __launch_bounds__(TB * TB) k_sw_panel(const double* D, int64_t ld, int k,
                                                      double* P, double* R, double* Xb) {
+  pdl_wait();
+  pdl_trigger();
   __shared__ double a[TB][TB + 1], xs[TB][TB + 1], tb[TB][TB + 1];
   __shared__ double rpiv[2];
   const int jb = blockIdx.x;
@@ -1150,6 +1152,8 @@ template <int TB>
 __global__ void __launch_bounds__(TB * TB) k_sw_update(double* D, int64_t ld, int k,
                                                       const double* P, const double* R,
                                                       const double* Xb) {
+  pdl_wait();
+  pdl_trigger();
   int ib, jb;
   tri_tile(blockIdx.x, ib, jb);
   const int i = threadIdx.y, j = threadIdx.x;
@@ -1179,6 +1183,8 @@ __global__ void __launch_bounds__(TB * TB) k_sw_update(double* D, int64_t ld, in
 // D <- -D on the upper blocks, mirrored into the lower ones: the full A^-1
 // (GJB is a multiple of SWB)
 __global__ void __launch_bounds__(GJB * GJB) k_sw_mirror(double* D, int64_t ld) {
+  pdl_wait();
+  pdl_trigger();
   const int ib = blockIdx.y, jb = blockIdx.x;
   if (ib > jb) return;
   __shared__ double ts[GJB][GJB + 1];
@@ -1207,11 +1213,11 @@ void gj_inverse(double* D, int64_t n, int64_t ld, double* work, cudaStream_t st)
   const dim3 thr(SWB, SWB);
   const unsigned tiles = (unsigned)(nb * (nb + 1) / 2);
   for (int k = 0; k < nb; ++k) {
-    k_sw_panel<SWB><<<nb, thr, 0, st>>>(D, ld, k, P, R, Xb);
-    k_sw_update<SWB><<<tiles, thr, 0, st>>>(D, ld, k, P, R, Xb);
+    launch_pdl(k_sw_panel<SWB>, dim3(nb), thr, 0, st, (const double*)D, ld, k, P, R, Xb);
+    launch_pdl(k_sw_update<SWB>, dim3(tiles), thr, 0, st, D, ld, k, (const double*)P, (const double*)R, (const double*)Xb);
   }
   const int nm = (int)(ld / GJB);
-  k_sw_mirror<<<dim3(nm, nm), dim3(GJB, GJB), 0, st>>>(D, ld);
+  launch_pdl(k_sw_mirror, dim3(nm, nm), dim3(GJB, GJB), 0, st, D, ld);
   count_launches(2 * (int64_t)nb);   // + the mirror, counted below
   TG_CHECK_LAUNCH();
 }
@@ -1311,6 +1317,8 @@ __device__ __forceinline__ void dw_tile_inverse(float2 (&a)[TB][TB + 1], float2 
 template <int TB>
 __global__ void __launch_bounds__(TB * TB) k_dw_panel(const float2* D, int64_t ld, int k,
                                                      float2* P, float2* R, float2* Xb) {
+  pdl_wait();
+  pdl_trigger();
   __shared__ float2 a[TB][TB + 1], xs[TB][TB + 1], tb[TB][TB + 1];
   __shared__ DW rpiv[2];
   const int jb = blockIdx.x;
@@ -1337,6 +1345,8 @@ template <int TB>
 __global__ void __launch_bounds__(TB * TB) k_dw_update(float2* D, int64_t ld, int k,
                                                       const float2* P, const float2* R,
                                                       const float2* Xb) {
+  pdl_wait();
+  pdl_trigger();
   int ib, jb;
   tri_tile(blockIdx.x, ib, jb);
   const int i = threadIdx.y, j = threadIdx.x;
@@ -1368,6 +1378,8 @@ __global__ void __launch_bounds__(TB * TB) k_dw_update(float2* D, int64_t ld, in
 
 // FP64 -> DW in place (h = the FP64 value rounded to FP32, l = the rounded rest)
 __global__ void k_dw_split(double* D, int64_t n) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (e >= n) return;
   const double v = D[e];
@@ -1379,6 +1391,8 @@ __global__ void k_dw_split(double* D, int64_t n) {
 // own upper tile (before its barrier) and the lower tiles it writes are read
 // by no block
 __global__ void __launch_bounds__(GJB * GJB) k_dw_mirror(double* D, int64_t ld) {
+  pdl_wait();
+  pdl_trigger();
   const int ib = blockIdx.y, jb = blockIdx.x;
   if (ib > jb) return;
   __shared__ double ts[GJB][GJB + 1];
@@ -1405,15 +1419,15 @@ void gj_inverse_dw(double* D, int64_t n, int64_t ld, double* work, cudaStream_t 
   float2* P = reinterpret_cast<float2*>(work);
   float2* R = P + SWB * SWB;
   float2* Xb = R + SWB * ld;
-  k_dw_split<<<(unsigned)cdiv(ld * ld, 256), 256, 0, st>>>(D, ld * ld);
+  launch_pdl(k_dw_split, dim3((unsigned)cdiv(ld * ld, 256)), dim3(256), 0, st, D, ld * ld);
   const dim3 thr(SWB, SWB);
   const unsigned tiles = (unsigned)(nb * (nb + 1) / 2);
   for (int k = 0; k < nb; ++k) {
-    k_dw_panel<SWB><<<nb, thr, 0, st>>>(Df, ld, k, P, R, Xb);
-    k_dw_update<SWB><<<tiles, thr, 0, st>>>(Df, ld, k, P, R, Xb);
+    launch_pdl(k_dw_panel<SWB>, dim3(nb), thr, 0, st, Df, ld, k, P, R, Xb);
+    launch_pdl(k_dw_update<SWB>, dim3(tiles), thr, 0, st, Df, ld, k, (const float2*)P, (const float2*)R, (const float2*)Xb);
   }
   const int nm = (int)(ld / GJB);
-  k_dw_mirror<<<dim3(nm, nm), dim3(GJB, GJB), 0, st>>>(D, ld);
+  launch_pdl(k_dw_mirror, dim3(nm, nm), dim3(GJB, GJB), 0, st, D, ld);
   count_launches(2 * (int64_t)nb + 1);   // and the split; the mirror is counted below
   TG_CHECK_LAUNCH();
 }
