@@ -26,6 +26,8 @@ __global__ void __launch_bounds__(RED_THREADS) k_filter(Grid g, int R, int rex, 
                                                        double* __restrict__ y,
                                                        const double* __restrict__ xold,
                                                        double* part_sum, double* part_max) {
+  pdl_wait();
+  pdl_trigger();
   __shared__ double sh[32];
   const int64_t nel = g.nel();
   const int W = 2 * R + 1;
@@ -82,6 +84,8 @@ __global__ void __launch_bounds__(RED_THREADS) k_filter(Grid g, int R, int rex, 
 
 __global__ void k_div(int64_t n, const double* __restrict__ a, const double* __restrict__ b,
                       double* __restrict__ q) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < n) q[i] = a[i] / b[i];
 }
@@ -94,12 +98,12 @@ void filter_apply_ex(const Grid& g, const FilterStencil& fs, const double* x, co
   if (mode == 1 && fs.tmp) {
     // H (x / Hs): the quotient once per element (GB300's FP64 divide is a
     // multi-instruction sequence on the narrow FP64 pipe), then a plain sum
-    k_div<<<(unsigned)cdiv(g.nel(), 256), 256, 0, st>>>(g.nel(), x, Hs, fs.tmp);
+    launch_pdl(k_div, dim3((unsigned)cdiv(g.nel(), 256)), dim3(256), 0, st, g.nel(), x, Hs, fs.tmp);
     TG_CHECK_LAUNCH();
     x = fs.tmp;
     mode = 5;
   }
-#define TG_F(ND, M) k_filter<ND, M><<<blocks, RED_THREADS, 0, st>>>(g, fs.R, fs.rex, fs.rey, fs.rez, fs.w, x, d, Hs, y, xold, part_sum, part_max)
+#define TG_F(ND, M) launch_pdl(k_filter<ND, M>, dim3(blocks), dim3(RED_THREADS), 0, st, g, fs.R, fs.rex, fs.rey, fs.rez, fs.w, x, d, Hs, y, xold, part_sum, part_max)
   if (g.ndim == 3) {
     if (mode == 0) TG_F(3, 0); else if (mode == 1) TG_F(3, 1); else if (mode == 2) TG_F(3, 2);
     else if (mode == 3) TG_F(3, 3); else if (mode == 5) TG_F(3, 5); else TG_F(3, 4);
@@ -122,6 +126,8 @@ void filter_apply(const Grid& g, const FilterStencil& fs, const double* x, const
 // ---------------------------------------------------------------------------
 __global__ void k_simp(int64_t n, const double* __restrict__ x, double eps, double penal,
                        double* s64, float* s32, __nv_bfloat16* s16, const int8_t* flags) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double xv = x[i];
@@ -135,7 +141,7 @@ __global__ void k_simp(int64_t n, const double* __restrict__ x, double eps, doub
 
 void simp_scale(int64_t n, const double* x, double eps, double penal, double* s64, float* s32,
                 __nv_bfloat16* s16, cudaStream_t st, const int8_t* flags) {
-  k_simp<<<(unsigned)cdiv(n, 256), 256, 0, st>>>(n, x, eps, penal, s64, s32, s16, flags);
+  launch_pdl(k_simp, dim3((unsigned)cdiv(n, 256)), dim3(256), 0, st, n, x, eps, penal, s64, s32, s16, flags);
   TG_CHECK_LAUNCH();
 }
 
@@ -149,13 +155,15 @@ __device__ double max_partials(const double* part, int nb, double* sh) {
 }
 
 __global__ void k_reduce_to(const double* part, int nb, double* out, int is_max) {
+  pdl_wait();
+  pdl_trigger();
   __shared__ double sh[32];
   const double v = is_max ? max_partials(part, nb, sh) : sum_partials(part, nb, sh);
   if (threadIdx.x == 0) *out = v;
 }
 
 void reduce_partials(const double* part, int nb, double* out, bool is_max, cudaStream_t st) {
-  k_reduce_to<<<1, RED_THREADS, 0, st>>>(part, nb, out, is_max ? 1 : 0);
+  launch_pdl(k_reduce_to, dim3(1), dim3(RED_THREADS), 0, st, part, nb, out, is_max ? 1 : 0);
   TG_CHECK_LAUNCH();
 }
 
@@ -165,6 +173,8 @@ void reduce_partials(const double* part, int nb, double* out, bool is_max, cudaS
 // bar_count0 = 0; a value no arrival sequence of the grid reaches (a test of
 // the bounded barrier wait) keeps every block waiting until its limit
 __global__ void k_oc_init(OCState* s, double g, double l1, double l2, unsigned int bar_count0) {
+  pdl_wait();
+  pdl_trigger();
   s->l1 = l1;
   s->l2 = l2;
   s->g = g;
@@ -190,6 +200,8 @@ __global__ void __launch_bounds__(RED_THREADS) k_oc_prep(int64_t n, const double
                                                         const double* __restrict__ dv,
                                                         const int8_t* __restrict__ flags,
                                                         double move, OCScratch sc) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double xi = x[i];
@@ -368,6 +380,8 @@ __global__ void __launch_bounds__(RED_THREADS) k_oc_finish(int64_t n, const doub
                                                           const int8_t* __restrict__ flags,
                                                           double move, double* __restrict__ xnew,
                                                           const OCState* st) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < n) xnew[i] = oc_value<BOUNDS>(i, x[i], sc, flags, move, st->sc_last);
 }
@@ -376,8 +390,8 @@ void oc_begin(int64_t n, const double* x, const double* dc, const double* dv, co
               double move, OCScratch sc, OCState* st, double g, cudaStream_t s, double l1,
               double l2) {
   prof_begin(PK_OC, s);
-  k_oc_prep<<<(unsigned)cdiv(n, RED_THREADS), RED_THREADS, 0, s>>>(n, x, dc, dv, flags, move, sc);
-  k_oc_init<<<1, 1, 0, s>>>(st, g, l1, l2, tune_take_oc_barrier_timeout() ? 0x40000000u : 0u);
+  launch_pdl(k_oc_prep, dim3((unsigned)cdiv(n, RED_THREADS)), dim3(RED_THREADS), 0, s, n, x, dc, dv, flags, move, sc);
+  launch_pdl(k_oc_init, dim3(1), dim3(1), 0, s, st, g, l1, l2, tune_take_oc_barrier_timeout() ? 0x40000000u : 0u);
   prof_end(PK_OC, s);
   count_launches(1);
   TG_CHECK_LAUNCH();
@@ -409,8 +423,8 @@ void oc_finish(int64_t n, const double* x, OCScratch sc, const int8_t* flags, do
                double* xnew, const OCState* st, cudaStream_t s) {
   const unsigned blocks = (unsigned)cdiv(n, RED_THREADS);
   prof_begin(PK_OC, s);
-  if (sc.lo) k_oc_finish<true><<<blocks, RED_THREADS, 0, s>>>(n, x, sc, flags, move, xnew, st);
-  else k_oc_finish<false><<<blocks, RED_THREADS, 0, s>>>(n, x, sc, flags, move, xnew, st);
+  if (sc.lo) launch_pdl(k_oc_finish<true>, dim3(blocks), dim3(RED_THREADS), 0, s, n, x, sc, flags, move, xnew, st);
+  else launch_pdl(k_oc_finish<false>, dim3(blocks), dim3(RED_THREADS), 0, s, n, x, sc, flags, move, xnew, st);
   prof_end(PK_OC, s);
   TG_CHECK_LAUNCH();
 }
@@ -633,34 +647,40 @@ template void update_xr<double>(int64_t, const double*, const double*, double*, 
 template void update_xr<float>(int64_t, const float*, const float*, float*, float*, double*, PCGState*, cudaStream_t);
 
 __global__ void k_pcg_reset(PCGState* st) {
+  pdl_wait();
+  pdl_trigger();
   st->iter = 0;
   st->rho = st->beta = st->alpha = st->pq = 0.0;
   st->ticket = 0;
 }
 void pcg_reset(PCGState* st, cudaStream_t s) {
-  k_pcg_reset<<<1, 1, 0, s>>>(st);
+  launch_pdl(k_pcg_reset, dim3(1), dim3(1), 0, s, st);
   TG_CHECK_LAUNCH();
 }
 
 // r32 = r64 / ||r64|| ;   x64 += ||r64|| * d32   (the norm comes from DOT_RR)
 __global__ void k_to_unit_f32(int64_t n, const double* __restrict__ r, const PCGState* st,
                               float* __restrict__ r32) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
   r32[i] = (float)r[i] * (float)st->rinv;
 }
 __global__ void k_add_scaled_f32(int64_t n, const float* __restrict__ d, const PCGState* st,
                                  double* __restrict__ x) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
   x[i] = fma(st->rnorm, (double)d[i], x[i]);
 }
 void to_unit_f32(int64_t n, const double* r, const PCGState* st, float* r32, cudaStream_t s) {
-  k_to_unit_f32<<<(unsigned)cdiv(n, 256), 256, 0, s>>>(n, r, st, r32);
+  launch_pdl(k_to_unit_f32, dim3((unsigned)cdiv(n, 256)), dim3(256), 0, s, n, r, st, r32);
   TG_CHECK_LAUNCH();
 }
 void add_scaled_f32(int64_t n, const float* d, const PCGState* st, double* x, cudaStream_t s) {
-  k_add_scaled_f32<<<(unsigned)cdiv(n, 256), 256, 0, s>>>(n, d, st, x);
+  launch_pdl(k_add_scaled_f32, dim3((unsigned)cdiv(n, 256)), dim3(256), 0, s, n, d, st, x);
   TG_CHECK_LAUNCH();
 }
 
@@ -698,11 +718,13 @@ template void scale_mul<double>(int64_t, double, const double*, const double*, d
 template void scale_mul<float>(int64_t, double, const float*, const float*, float*, cudaStream_t);
 
 __global__ void k_d2f(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < n) b[i] = (float)a[i];
 }
 void d2f(int64_t n, const double* a, float* b, cudaStream_t s) {
-  k_d2f<<<(unsigned)cdiv(n, 256), 256, 0, s>>>(n, a, b);
+  launch_pdl(k_d2f, dim3((unsigned)cdiv(n, 256)), dim3(256), 0, s, n, a, b);
   TG_CHECK_LAUNCH();
 }
 
@@ -720,6 +742,8 @@ template void axpby<double>(int64_t, double, const double*, double, double*, cud
 template void axpby<float>(int64_t, double, const float*, double, float*, cudaStream_t);
 
 __global__ void k_mask(int64_t nnodes, int ndof, const uint8_t* fix, double* v) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= nnodes * ndof) return;
   if ((fix[i / ndof] >> (i % ndof)) & 1) v[i] = 0.0;
@@ -750,7 +774,7 @@ void embed_copy(const Grid& rg, const Grid& g, bool nodes, const double* src, do
 }
 
 void mask_vec_f64(int64_t nnodes, int ndof, const uint8_t* fix, double* v, cudaStream_t st) {
-  k_mask<<<(unsigned)cdiv(nnodes * ndof, 256), 256, 0, st>>>(nnodes, ndof, fix, v);
+  launch_pdl(k_mask, dim3((unsigned)cdiv(nnodes * ndof, 256)), dim3(256), 0, st, nnodes, ndof, fix, v);
   TG_CHECK_LAUNCH();
 }
 

@@ -996,6 +996,8 @@ template void fine_apply<float, __nv_bfloat16>(const FineOp&, const __nv_bfloat1
 // ---------------------------------------------------------------------------
 template <int NDIM, int NDOF, typename T, typename S>
 __global__ void k_fine_dinv(Grid g, const uint8_t* fix, const S* scale, T* dinv, FineOp op) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (n >= g.nnodes()) return;
   const int y = (int)(n % g.nny);
@@ -1023,10 +1025,10 @@ void fine_dinv(const FineOp& op, const S* scale, T* dinv, cudaStream_t st) {
   const unsigned blocks = (unsigned)cdiv(nn, 256);
   const int key = op.g.ndim * 10 + op.g.ndof;
   switch (key) {
-    case 33: k_fine_dinv<3, 3, T, S><<<blocks, 256, 0, st>>>(op.g, op.fix, scale, dinv, op); break;
-    case 31: k_fine_dinv<3, 1, T, S><<<blocks, 256, 0, st>>>(op.g, op.fix, scale, dinv, op); break;
-    case 22: k_fine_dinv<2, 2, T, S><<<blocks, 256, 0, st>>>(op.g, op.fix, scale, dinv, op); break;
-    case 21: k_fine_dinv<2, 1, T, S><<<blocks, 256, 0, st>>>(op.g, op.fix, scale, dinv, op); break;
+    case 33: launch_pdl(k_fine_dinv<3, 3, T, S>, dim3(blocks), dim3(256), 0, st, op.g, op.fix, scale, dinv, op); break;
+    case 31: launch_pdl(k_fine_dinv<3, 1, T, S>, dim3(blocks), dim3(256), 0, st, op.g, op.fix, scale, dinv, op); break;
+    case 22: launch_pdl(k_fine_dinv<2, 2, T, S>, dim3(blocks), dim3(256), 0, st, op.g, op.fix, scale, dinv, op); break;
+    case 21: launch_pdl(k_fine_dinv<2, 1, T, S>, dim3(blocks), dim3(256), 0, st, op.g, op.fix, scale, dinv, op); break;
     default: throw Error{EINVAL_, "unsupported (ndim, nnode_dof) combination"};
   }
   TG_CHECK_LAUNCH();
@@ -1048,6 +1050,8 @@ __global__ void __launch_bounds__(RED_THREADS) k_compliance(Grid g, const double
                                                            double* partial,
                                                            const int8_t* __restrict__ flags,
                                                            int accumulate) {
+  pdl_wait();
+  pdl_trigger();
   constexpr int NC = 1 << NDIM;
   constexpr int NE = NC * NDOF;
   __shared__ double sh[32];
@@ -1115,10 +1119,10 @@ void fine_compliance(const FineOp& op, const double* xPhys, const double* u, dou
   const int key = op.g.ndim * 10 + op.g.ndof;
 #define TG_COMP(ND, NF)                                                                     \
   if (op.sector)                                                                            \
-    k_compliance<ND, NF, true><<<blocks, RED_THREADS, 0, st>>>(op.g, xPhys, u, op.KE64,      \
+    launch_pdl(k_compliance<ND, NF, true>, dim3(blocks), dim3(RED_THREADS), 0, st, op.g, xPhys, u, op.KE64,      \
                                                               op.B64, eps, penal, dc, partial, flags, accumulate ? 1 : 0); \
   else                                                                                      \
-    k_compliance<ND, NF, false><<<blocks, RED_THREADS, 0, st>>>(op.g, xPhys, u, op.KE64,     \
+    launch_pdl(k_compliance<ND, NF, false>, dim3(blocks), dim3(RED_THREADS), 0, st, op.g, xPhys, u, op.KE64,     \
                                                                op.B64, eps, penal, dc, partial, flags, accumulate ? 1 : 0);
   switch (key) {
     case 33: TG_COMP(3, 3) break;

@@ -513,6 +513,8 @@ template void stencil_apply<float>(const Grid&, const float*, const float*, floa
 
 template <int NDIM, int NDOF, typename T>
 __global__ void k_stencil_dinv(Grid g, const uint8_t* fix, const T* A, T* dinv) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (n >= g.nnodes()) return;
   const int64_t ld = g.slds();
@@ -528,10 +530,10 @@ void stencil_dinv(const Grid& g, const uint8_t* fix, const T* A, T* dinv, cudaSt
   const unsigned blocks = (unsigned)cdiv(g.nnodes(), 256);
   const int key = g.ndim * 10 + g.ndof;
   switch (key) {
-    case 33: k_stencil_dinv<3, 3, T><<<blocks, 256, 0, st>>>(g, fix, A, dinv); break;
-    case 31: k_stencil_dinv<3, 1, T><<<blocks, 256, 0, st>>>(g, fix, A, dinv); break;
-    case 22: k_stencil_dinv<2, 2, T><<<blocks, 256, 0, st>>>(g, fix, A, dinv); break;
-    case 21: k_stencil_dinv<2, 1, T><<<blocks, 256, 0, st>>>(g, fix, A, dinv); break;
+    case 33: launch_pdl(k_stencil_dinv<3, 3, T>, dim3(blocks), dim3(256), 0, st, g, fix, A, dinv); break;
+    case 31: launch_pdl(k_stencil_dinv<3, 1, T>, dim3(blocks), dim3(256), 0, st, g, fix, A, dinv); break;
+    case 22: launch_pdl(k_stencil_dinv<2, 2, T>, dim3(blocks), dim3(256), 0, st, g, fix, A, dinv); break;
+    case 21: launch_pdl(k_stencil_dinv<2, 1, T>, dim3(blocks), dim3(256), 0, st, g, fix, A, dinv); break;
     default: throw Error{EINVAL_, "unsupported (ndim, nnode_dof)"};
   }
   TG_CHECK_LAUNCH();
@@ -561,6 +563,8 @@ __global__ void __launch_bounds__(256) k_build_level1(Grid gf, Grid gc, const T*
                                                       const T* __restrict__ KE,
                                                       const uint8_t* __restrict__ fixc,
                                                       T* __restrict__ Ac) {
+  pdl_wait();
+  pdl_trigger();
   constexpr int NC = 1 << NDIM;
   constexpr int NE = NC * NDOF;
   const int64_t ldc = gc.nnodes();
@@ -645,10 +649,10 @@ void build_level1(const FineOp& op, const T* scale, const uint8_t* touch, const 
   const unsigned blocks = (unsigned)cdiv(nt, 256);
   const int key = op.g.ndim * 10 + op.g.ndof;
   switch (key) {
-    case 33: k_build_level1<3, 3, T><<<blocks, 256, 0, st>>>(op.g, gc, scale, touch, op.fix, Q, KE, fixc, Ac); break;
-    case 31: k_build_level1<3, 1, T><<<blocks, 256, 0, st>>>(op.g, gc, scale, touch, op.fix, Q, KE, fixc, Ac); break;
-    case 22: k_build_level1<2, 2, T><<<blocks, 256, 0, st>>>(op.g, gc, scale, touch, op.fix, Q, KE, fixc, Ac); break;
-    case 21: k_build_level1<2, 1, T><<<blocks, 256, 0, st>>>(op.g, gc, scale, touch, op.fix, Q, KE, fixc, Ac); break;
+    case 33: launch_pdl(k_build_level1<3, 3, T>, dim3(blocks), dim3(256), 0, st, op.g, gc, scale, touch, op.fix, Q, KE, fixc, Ac); break;
+    case 31: launch_pdl(k_build_level1<3, 1, T>, dim3(blocks), dim3(256), 0, st, op.g, gc, scale, touch, op.fix, Q, KE, fixc, Ac); break;
+    case 22: launch_pdl(k_build_level1<2, 2, T>, dim3(blocks), dim3(256), 0, st, op.g, gc, scale, touch, op.fix, Q, KE, fixc, Ac); break;
+    case 21: launch_pdl(k_build_level1<2, 1, T>, dim3(blocks), dim3(256), 0, st, op.g, gc, scale, touch, op.fix, Q, KE, fixc, Ac); break;
     default: throw Error{EINVAL_, "unsupported (ndim, nnode_dof)"};
   }
   TG_CHECK_LAUNCH();
@@ -747,6 +751,8 @@ template <int NDIM, int NDOF, typename T>
 __global__ void __launch_bounds__(256) k_galerkin(Grid gf, const T* __restrict__ Af, Grid gc,
                                                   const uint8_t* __restrict__ fixc,
                                                   T* __restrict__ Ac) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t ldc = gc.nnodes();
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int lane = threadIdx.x % GAL_LANES;
@@ -831,10 +837,10 @@ void build_galerkin(const Grid& gf, const T* Af, const Grid& gc, const uint8_t* 
   const unsigned blocks = (unsigned)cdiv(nt, 256);
   const int key = gf.ndim * 10 + gf.ndof;
   switch (key) {
-    case 33: k_galerkin<3, 3, T><<<blocks, 256, 0, st>>>(gf, Af, gc, fixc, Ac); break;
-    case 31: k_galerkin<3, 1, T><<<blocks, 256, 0, st>>>(gf, Af, gc, fixc, Ac); break;
-    case 22: k_galerkin<2, 2, T><<<blocks, 256, 0, st>>>(gf, Af, gc, fixc, Ac); break;
-    case 21: k_galerkin<2, 1, T><<<blocks, 256, 0, st>>>(gf, Af, gc, fixc, Ac); break;
+    case 33: launch_pdl(k_galerkin<3, 3, T>, dim3(blocks), dim3(256), 0, st, gf, Af, gc, fixc, Ac); break;
+    case 31: launch_pdl(k_galerkin<3, 1, T>, dim3(blocks), dim3(256), 0, st, gf, Af, gc, fixc, Ac); break;
+    case 22: launch_pdl(k_galerkin<2, 2, T>, dim3(blocks), dim3(256), 0, st, gf, Af, gc, fixc, Ac); break;
+    case 21: launch_pdl(k_galerkin<2, 1, T>, dim3(blocks), dim3(256), 0, st, gf, Af, gc, fixc, Ac); break;
     default: throw Error{EINVAL_, "unsupported (ndim, nnode_dof)"};
   }
   TG_CHECK_LAUNCH();
@@ -1008,6 +1014,8 @@ template void prolong_set<float>(const Grid&, const Grid&, const uint8_t*, const
 template <typename T>
 __global__ void k_stencil_to_dense(Grid g, const uint8_t* fix, const T* __restrict__ A,
                                    double* D, int64_t n, int64_t ld) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t ldA = g.nnodes();
   const int C = g.ndim == 3 ? 13 : 4;
   const int nh = C + 1;
@@ -1027,6 +1035,8 @@ __global__ void k_stencil_to_dense(Grid g, const uint8_t* fix, const T* __restri
   if (dh > 0) D[(J * ndof + cj) * ld + I * ndof + ci] = v;   // mirrored lower block
 }
 __global__ void k_dense_fix_diag(Grid g, const uint8_t* fix, double* D, int64_t n, int64_t ld) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (r >= ld) return;
   if (r >= n) {
@@ -1043,9 +1053,9 @@ void stencil_to_dense(const Grid& g, const uint8_t* fix, const T* A, double* D, 
                       int64_t ld, cudaStream_t st) {
   TG_CUDA(cudaMemsetAsync(D, 0, sizeof(double) * ld * ld, st));
   const int64_t nt = g.nnodes() * (g.ndim == 3 ? 14 : 5) * g.ndof * g.ndof;
-  k_stencil_to_dense<T><<<(unsigned)cdiv(nt, 256), 256, 0, st>>>(g, fix, A, D, n, ld);
+  launch_pdl(k_stencil_to_dense<T>, dim3((unsigned)cdiv(nt, 256)), dim3(256), 0, st, g, fix, A, D, n, ld);
   TG_CHECK_LAUNCH();
-  k_dense_fix_diag<<<(unsigned)cdiv(ld, 256), 256, 0, st>>>(g, fix, D, n, ld);
+  launch_pdl(k_dense_fix_diag, dim3((unsigned)cdiv(ld, 256)), dim3(256), 0, st, g, fix, D, n, ld);
   TG_CHECK_LAUNCH();
 }
 template void stencil_to_dense<double>(const Grid&, const uint8_t*, const double*, double*,
