@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define TG_ABI_VERSION 5
+#define TG_ABI_VERSION 6
 
 enum {
   TG_OK = 0,
@@ -93,6 +93,8 @@ typedef struct tg_problem {
                             correction through the composite interpolation of levels
                             l-1 -> l+1); 0 = every level smoothed (TG_EINVAL for other
                             bits) */
+  int32_t nsmooth_coarse;/* multigrid: damped-Jacobi sweeps before / after on the coarse
+                            levels (1 .. nlevels-2); 0 = nsmooth */
 } tg_problem;
 
 typedef struct tg_iter_out {

@@ -88,8 +88,9 @@ class Hierarchy:
     (the GPU context's tg_problem.unsmoothed bits)."""
 
     def __init__(self, K, fixed_mask, dims, ndof, nlevels, omega=0.6, nsmooth=2, K_build=None,
-                 coarse_ops=None, unsmoothed=()):
+                 coarse_ops=None, unsmoothed=(), nsmooth_coarse=None):
         self.omega, self.nsmooth = omega, nsmooth
+        self.nsmooth_coarse = nsmooth if not nsmooth_coarse else nsmooth_coarse
         self.unsmoothed = set(unsmoothed)
         free = (~fixed_mask).astype(float)
         M = sp.diags(free)
@@ -134,13 +135,14 @@ class Hierarchy:
         if lvl in self.unsmoothed:
             return self.P[lvl] @ self.vcycle(self.P[lvl].T @ b, lvl + 1)
         A, Dinv, w = self.A[lvl], self.Dinv[lvl], self.omega
+        ns = self.nsmooth if lvl == 0 else self.nsmooth_coarse
         x = w * Dinv * b
-        for _ in range(self.nsmooth - 1):
+        for _ in range(ns - 1):
             x = x + w * Dinv * (b - A @ x)
         r = b - A @ x
         xc = self.vcycle(self.P[lvl].T @ r, lvl + 1)
         x = x + self.P[lvl] @ xc
-        for _ in range(self.nsmooth):
+        for _ in range(ns):
             x = x + w * Dinv * (b - A @ x)
         return x
 

@@ -403,24 +403,29 @@ def test_coarse_tail_barrier_wait_runs_out(gpu_lib):
     np.testing.assert_array_equal(z, z_sep)
 
 
-@pytest.mark.parametrize("unsmoothed", [(1,), (2,), (1, 2)])
+@pytest.mark.parametrize("unsmoothed,nsmooth,nsmooth_coarse",
+                         [((1,), 2, 0), ((2,), 2, 0), ((1, 2), 2, 0), ((1,), 1, 2), ((), 1, 3)])
 @pytest.mark.parametrize("nelx,nely,nelz,kind", [(32, 16, None, "elast"), (16, 8, 8, "elast"),
                                                  (32, 16, 16, "elast"), (16, 16, 8, "poisson")])
-def test_vcycle_unsmoothed_levels_match_oracle(gpu_lib, unsmoothed, nelx, nely, nelz, kind):
+def test_vcycle_unsmoothed_levels_match_oracle(gpu_lib, unsmoothed, nsmooth, nsmooth_coarse,
+                                               nelx, nely, nelz, kind):
     """Levels left unsmoothed (tg_problem.unsmoothed): the cycle restricts
     their right-hand side on and prolongates the coarser correction back,
-    as the oracle's Hierarchy(unsmoothed=...) does (FP64, 4 levels)."""
+    as the oracle's Hierarchy(unsmoothed=...) does; with nsmooth_coarse, the
+    coarse levels take that many sweeps (FP64, 4 levels)."""
     rng = np.random.default_rng(21)
     mask_bits = sum(1 << l for l in unsmoothed)
     prob, KE, fixed, f, x, ndof = _setup(nelx, nely, nelz, kind, rng, nlevels=4,
-                                         unsmoothed=mask_bits)
+                                         unsmoothed=mask_bits, nsmooth=nsmooth,
+                                         nsmooth_coarse=nsmooth_coarse)
     ndim = 2 if nelz is None else 3
     dims = (nelx, nely) if ndim == 2 else (nelx, nely, nelz)
     nnd = KE.shape[0] // 2 ** ndim
     K = O.assemble(KE, O.edofmat(nelx, nely, nelz, nnd), O.simp(x), ndof)
     mask = np.zeros(ndof, bool)
     mask[fixed] = True
-    h = G.Hierarchy(K, mask, dims, nnd, 4, omega=0.6, nsmooth=2, unsmoothed=unsmoothed)
+    h = G.Hierarchy(K, mask, dims, nnd, 4, omega=0.6, nsmooth=nsmooth, unsmoothed=unsmoothed,
+                    nsmooth_coarse=nsmooth_coarse)
     b = rng.standard_normal(ndof) * ~mask
     try:
         z = prob.vcycle(x, b)
@@ -432,13 +437,13 @@ def test_vcycle_unsmoothed_levels_match_oracle(gpu_lib, unsmoothed, nelx, nely, 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_solve_unsmoothed_level1_reaches_direct_solution(gpu_lib, precision):
-    """One smoothing sweep (omega 0.6) with level 1 unsmoothed -- the bench's
-    V-cycle -- still converges to the direct solution on a random-density
-    design."""
+    """One smoothing sweep (omega 0.6) on the fine level, two on levels 2-3,
+    level 1 unsmoothed -- the bench's V-cycle -- still converges to the
+    direct solution on a random-density design."""
     rng = np.random.default_rng(22)
     prob, KE, fixed, f, x, ndof = _setup(32, 16, 16, "elast", rng, precision=precision,
                                          rtol=1e-10, nlevels=4, nsmooth=1, omega=0.6,
-                                         unsmoothed=2)
+                                         unsmoothed=2, nsmooth_coarse=2)
     try:
         u, info = prob.solve(x, f)
     finally:

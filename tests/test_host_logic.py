@@ -121,7 +121,7 @@ def test_library_loads_and_exports_every_symbol():
     lib = ctypes.CDLL(path)
     for name in _declared_symbols():
         assert hasattr(lib, name), name
-    assert _lib.load().tg_abi_version() == 5
+    assert _lib.load().tg_abi_version() == 6
 
 
 @pytest.mark.parametrize("case", ["nelx0", "ke_shape", "fixed_range", "f_length", "ft", "precision",

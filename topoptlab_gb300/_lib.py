@@ -41,6 +41,7 @@ class TgProblem(C.Structure):
         ("maxiter", C.c_int32), ("inner_rtol", C.c_double), ("learned", C.c_int32),
         ("device", C.c_int32), ("nload", C.c_int32),
         ("filter_pde", C.c_int32), ("KF", _dp), ("unsmoothed", C.c_int32),
+        ("nsmooth_coarse", C.c_int32),
     ]
 
 

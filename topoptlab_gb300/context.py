@@ -60,7 +60,8 @@ class GpuProblem:
     def __init__(self, nelx, nely, nelz, KE, fixed, f, volfrac, rmin, ft=1, eps=1e-9,
                  penal=3.0, move=0.2, el_flags=None, precond="gb300-gmg", precision="fp64",
                  nlevels=0, nsmooth=2, omega=0.6, rtol=1e-8, maxiter=2000, inner_rtol=1e-4,
-                 learned=False, device=0, filter_mode="matrix", filter_l=None, unsmoothed=0):
+                 learned=False, device=0, filter_mode="matrix", filter_l=None, unsmoothed=0,
+                 nsmooth_coarse=0):
         self._lib = _lib.load()
         self.ndim = 2 if nelz is None else 3
         self.nelx, self.nely, self.nelz = nelx, nely, nelz
@@ -106,6 +107,7 @@ class GpuProblem:
         p.precision = PRECISIONS[precision]
         p.nlevels, p.nsmooth, p.omega = nlevels, nsmooth, omega
         p.unsmoothed = int(unsmoothed)
+        p.nsmooth_coarse = int(nsmooth_coarse)
         p.rtol, p.maxiter, p.inner_rtol = rtol, maxiter, inner_rtol
         p.learned = learned_mask(learned)
         p.device = device

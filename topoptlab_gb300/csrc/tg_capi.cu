@@ -17,8 +17,18 @@ struct tg_ctx {
 namespace {
 thread_local std::string g_last_error;
 
+// programmatic dependent launch for mixed-precision contexts only (restored
+// on every exit)
+struct PdlScope {
+  int prev;
+  explicit PdlScope(tg_ctx* ctx)
+      : prev(tg::pdl_scope(!ctx || ctx->c.precision == TG_PREC_MIXED ? 1 : 0)) {}
+  ~PdlScope() { tg::pdl_scope(prev); }
+};
+
 template <typename F>
 int32_t guarded(tg_ctx* ctx, F&& fn) {
+  PdlScope pdl(ctx);
   try {
     if (ctx) TG_CUDA(cudaSetDevice(ctx->c.dev));
     fn();

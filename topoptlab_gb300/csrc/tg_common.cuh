@@ -93,7 +93,12 @@ void set_smem_limit(const void* func, int bytes);
 // thread, before any global memory access: it returns once the predecessor
 // grid has completed and its writes are visible, so the stream order of the
 // data is unchanged.  Both are no-ops for a kernel launched normally.
-bool pdl_on();            // tg_tune(TG_TUNE_PDL), default on
+bool pdl_on();            // tg_tune(TG_TUNE_PDL) (default on) and the calling thread's scope
+// the calling thread's scope: the library turns programmatic dependent launch
+// off while it works for an FP64 context (its long FP64 kernels gain nothing,
+// and blocks parked early cost concurrently stepped designs SM slots);
+// returns the previous setting
+int pdl_scope(int on);
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void pdl_trigger() {
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");

@@ -228,6 +228,7 @@ void ctx_init(Ctx& c, const tg_problem& p) {
   c.move = p.move > 0 ? p.move : 0.2;
   c.ft = p.ft; c.precond = p.precond; c.precision = p.precision;
   c.nsmooth = p.nsmooth > 0 ? p.nsmooth : 2;
+  c.nsmooth_coarse = p.nsmooth_coarse > 0 ? p.nsmooth_coarse : c.nsmooth;
   c.omega = p.omega > 0 ? p.omega : 0.6;
   c.rtol = p.rtol > 0 ? p.rtol : 1e-8;
   c.maxiter = p.maxiter > 0 ? p.maxiter : 2000;
@@ -545,7 +546,8 @@ template <typename T> void vcycle(Ctx& c, int l, const T* b, T* x, bool prescale
     prolong_set<T>(v.g, w.g, v.fix, LvBufs<T>::x(w), x, c.st);
     return;
   }
-  // 2*nsmooth - 1 sweeps swap the buffers an odd number of times: starting in
+  const int nsm = l == 0 ? c.nsmooth : c.nsmooth_coarse;
+  // 2*nsm - 1 sweeps swap the buffers an odd number of times: starting in
   // the scratch buffer ends in x (no copy at the end of the level)
   T* bufs[2] = {x, LvBufs<T>::t(v)};
   int cur = 1;
@@ -553,7 +555,7 @@ template <typename T> void vcycle(Ctx& c, int l, const T* b, T* x, bool prescale
     ProfScope ps(PK_VECTOR, c.st);
     scale_mul<T>(n, c.omega, LvBufs<T>::dinv(v), b, bufs[cur], c.st);
   }
-  for (int s = 1; s < c.nsmooth; ++s) {
+  for (int s = 1; s < nsm; ++s) {
     level_apply<T>(c, l, bufs[cur], bufs[1 - cur], b, AM_JACOBI);
     cur = 1 - cur;
   }
@@ -577,7 +579,7 @@ template <typename T> void vcycle(Ctx& c, int l, const T* b, T* x, bool prescale
     a.bc = LvBufs<T>::b(k); a.xc = LvBufs<T>::x(k);
     a.Dc = c.Dc; a.nc = c.nc; a.ldc = c.ldc; a.part = c.gjwork;
     a.Dc32 = std::is_same<T, float>::value ? c.Dc32.p : nullptr;
-    a.omega = (T)c.omega; a.nsmooth = c.nsmooth; a.bar = c.tailbar;
+    a.omega = (T)c.omega; a.nsmooth = c.nsmooth_coarse; a.bar = c.tailbar;
     const int mode = tune_coarse_tail();
     a.cluster = mode == 1 ? 16 : 0;
     a.blocks = mode > 2 ? mode : 0;
@@ -600,8 +602,8 @@ template <typename T> void vcycle(Ctx& c, int l, const T* b, T* x, bool prescale
   }
   // the fine level's last sweep of the FP32 cycle also forms the PCG dot b . x
   const bool fused_dot = dot_op >= 0 && l == 0 && std::is_same<T, float>::value;
-  for (int s = 0; s < c.nsmooth; ++s) {
-    if (fused_dot && s == c.nsmooth - 1)
+  for (int s = 0; s < nsm; ++s) {
+    if (fused_dot && s == nsm - 1)
       fine_apply_dot<float, __nv_bfloat16>(c.op, c.s16, (const float*)bufs[cur],
                                            (float*)bufs[1 - cur], (const float*)b,
                                            (const float*)LvBufs<T>::dinv(v), c.omega, AM_JACOBI,

@@ -57,6 +57,7 @@ struct Ctx {
   int ft = 1;
   int precond = 0, precision = 0, nsmooth = 2, maxiter = 2000, learned = 0;
   int unsmoothed = 0;           // bit l: level l not smoothed (tg_problem.unsmoothed)
+  int nsmooth_coarse = 2;       // sweeps before / after on levels >= 1
   double omega = 0.6, rtol = 1e-8, inner_rtol = 1e-4;
   double bnorm = 0.0;           // ||M f|| of load case 0
   int nload = 1;                // load cases: f and u hold nload vectors each

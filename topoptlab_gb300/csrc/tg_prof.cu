@@ -72,7 +72,15 @@ std::atomic<int> g_tail_timeout{0};
 int64_t tune_stencil_small_pairs() { return g_small_pairs.load(std::memory_order_relaxed); }
 bool tune_take_oc_barrier_timeout() { return g_oc_timeout.exchange(0) != 0; }
 int tune_coarse_tail() { return g_tail.load(std::memory_order_relaxed); }
-bool pdl_on() { return g_pdl.load(std::memory_order_relaxed) != 0; }
+namespace {
+thread_local int tl_pdl = 1;
+}
+bool pdl_on() { return tl_pdl != 0 && g_pdl.load(std::memory_order_relaxed) != 0; }
+int pdl_scope(int on) {
+  const int prev = tl_pdl;
+  tl_pdl = on;
+  return prev;
+}
 bool tune_take_tail_barrier_timeout() { return g_tail_timeout.exchange(0) != 0; }
 
 namespace {

@@ -64,7 +64,8 @@ def solver_options(lin_solver_kw: Dict, preconditioner_kw: Dict) -> Dict:
     name = lin_solver_kw.get("name", "gb300-gmgpcg")
     pname = preconditioner_kw.get("name", None)
     opts = dict(precond="gb300-gmg", precision="fp64", nlevels=0, nsmooth=2, omega=0.6,
-                rtol=1e-8, maxiter=2000, inner_rtol=1e-4, learned=False, unsmoothed=0)
+                rtol=1e-8, maxiter=2000, inner_rtol=1e-4, learned=False, unsmoothed=0,
+                nsmooth_coarse=0)
     if name in _DIRECT:
         opts["rtol"] = 1e-12
     elif name in ("gb300-gmgpcg", "gb300-pcg") or name in _ITERATIVE:
@@ -81,7 +82,7 @@ def solver_options(lin_solver_kw: Dict, preconditioner_kw: Dict) -> Dict:
         opts["precond"] = "gb300-jacobi"
     elif pname not in (None, "gb300-gmg") and not str(pname).startswith(("pyamg-", "scipy-")):
         raise ValueError("Unknown preconditioner: ", pname)
-    for key in ("nlevels", "nsmooth", "maxiter", "unsmoothed"):
+    for key in ("nlevels", "nsmooth", "maxiter", "unsmoothed", "nsmooth_coarse"):
         if key in preconditioner_kw:
             opts[key] = int(preconditioner_kw[key])
     for key in ("omega", "inner_rtol"):
