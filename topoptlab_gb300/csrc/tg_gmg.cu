@@ -556,7 +556,7 @@ __device__ __forceinline__ double pweight(int o, int p, int a, int ndim) {
 }
 
 template <int NDIM, int NDOF, typename T>
-__global__ void __launch_bounds__(256) k_build_level1(Grid gf, Grid gc, const T* __restrict__ scale,
+__global__ void __launch_bounds__(256, 3) k_build_level1(Grid gf, Grid gc, const T* __restrict__ scale,
                                                       const uint8_t* __restrict__ touch,
                                                       const uint8_t* __restrict__ fixf,
                                                       const T* __restrict__ Q,
@@ -592,6 +592,27 @@ __global__ void __launch_bounds__(256) k_build_level1(Grid gf, Grid gc, const T*
         for (int ey = eyl; ey <= eyh; ++ey) {
           const int ca = (ix - ex) | ((iy - ey) << 1) | ((NDIM == 3 ? iz - ez : 0) << 2);
           const int cb = (jx - ex) | ((jy - ey) << 1) | ((NDIM == 3 ? jz - ez : 0) << 2);
+          // children touching no fixed DOF, the common case, in one unrolled
+          // pass (their density and table loads independent of each other)
+          const int64_t fe0 = gf.elem(2 * ex, 2 * ey, (NDIM == 3) ? 2 * ez : 0);
+          const int64_t fsx = gf.ney, fsz = (int64_t)gf.nex * gf.ney;
+          bool any_touch = false;
+#pragma unroll
+          for (int o = 0; o < NC; ++o)
+            any_touch |= touch[fe0 + (o & 1) * fsx + ((o >> 1) & 1) + ((o >> 2) & 1) * fsz] != 0;
+          if (!any_touch) {
+#pragma unroll
+            for (int o = 0; o < NC; ++o) {
+              const T rho = scale[fe0 + (o & 1) * fsx + ((o >> 1) & 1) + ((o >> 2) & 1) * fsz];
+              const T* Qo = Q + (int64_t)o * NE * NE;
+#pragma unroll
+              for (int ci = 0; ci < NDOF; ++ci)
+#pragma unroll
+                for (int cj = 0; cj < NDOF; ++cj)
+                  acc[ci][cj] += rho * __ldg(Qo + (ca * NDOF + ci) * NE + cb * NDOF + cj);
+            }
+            continue;
+          }
 #pragma unroll 1
           for (int o = 0; o < NC; ++o) {
             const int fx = 2 * ex + (o & 1), fy = 2 * ey + ((o >> 1) & 1);
