@@ -323,8 +323,10 @@ int32_t tg_tune(int32_t key, int64_t value);
 /* Inverse of a dense SPD matrix A (row-major n x n, n <= 8192) by the
  * library's coarsest-level method, the symmetric block sweep operator:
  * mode 0 in FP64, mode 1 in double-word FP32 arithmetic (about 48
- * significant bits; what mixed-precision contexts use).  Diagnostic (no
- * reference counterpart); synchronous. */
+ * significant bits; what mixed-precision contexts use: each step's update
+ * launch also forms the next step's panel), mode 2 the same double-word
+ * sweep with panel and update as separate launches (same result as mode 1).
+ * Diagnostic (no reference counterpart); synchronous. */
 int32_t tg_dense_inverse(const double* A, int64_t n, double* Ainv, int32_t mode, int32_t device);
 int32_t tg_edofmat(int32_t ndim, int32_t nelx, int32_t nely, int32_t nelz, int32_t nnode_dof,
                    int32_t* out, int32_t device);

@@ -281,8 +281,8 @@ def test_vcycle_matches_oracle(gpu_lib, nelx, nely, nelz, kind):
 @pytest.mark.parametrize("cond", [1e2, 1e6, 1e9])
 def test_dense_inverse_fp64_and_double_word(gpu_lib, n, cond):
     """The coarsest-level inverse (symmetric block sweep) in FP64 and in
-    double-word FP32 arithmetic against LAPACK on SPD matrices of a given
-    condition number.  Bound on the largest entry error of the inverse,
+    double-word FP32 arithmetic (with and without the look-ahead panel)
+    against LAPACK on SPD matrices of a given condition number.  Bound on the largest entry error of the inverse,
     relative to its largest entry: cond * 2^-42 for double-word (about 48
     significant bits), cond * 2^-46 for FP64 (LAPACK's own inverse is off by
     about cond * 2^-53 as well)."""
@@ -296,7 +296,8 @@ def test_dense_inverse_fp64_and_double_word(gpu_lib, n, cond):
     A = 0.5 * (A + A.T)
     ref = np.linalg.inv(A)
     nrm = np.abs(ref).max()
-    for mode, bound in ((0, 2.0 ** -46), (1, 2.0 ** -42)):
+    out = {}
+    for mode, bound in ((0, 2.0 ** -46), (1, 2.0 ** -42), (2, 2.0 ** -42)):
         X = np.empty((n, n))
         rc = lib.tg_dense_inverse(_lib.dptr(np.ascontiguousarray(A)), n, _lib.dptr(X), mode, 0)
         assert rc == _lib.TG_OK, lib.tg_last_error(None)
@@ -304,6 +305,10 @@ def test_dense_inverse_fp64_and_double_word(gpu_lib, n, cond):
         print(f"n={n} cond={cond:.0e} mode={mode} err={err:.3e} err/cond={err / cond:.3e}")
         assert err < cond * bound, (mode, err)
         np.testing.assert_array_equal(X, X.T)
+        out[mode] = X
+    # the double-word sweep with the next panel formed inside each update
+    # launch (mode 1) computes the same values as separate launches (mode 2)
+    np.testing.assert_array_equal(out[1], out[2])
 
 
 @pytest.mark.parametrize("nlevels", [2, 3])

@@ -468,7 +468,7 @@ int32_t tg_timer(tg_ctx* ctx, int32_t op, double* ms) {
 }
 
 int32_t tg_dense_inverse(const double* A, int64_t n, double* Ainv, int32_t mode, int32_t device) {
-  if (!A || !Ainv || n <= 0 || n > 8192 || (mode != 0 && mode != 1)) return TG_EINVAL;
+  if (!A || !Ainv || n <= 0 || n > 8192 || mode < 0 || mode > 2) return TG_EINVAL;
   return guarded(nullptr, [&] {
     TG_CUDA(cudaSetDevice(device));
     const int64_t ld = tg::cdiv(n, 32) * 32;
@@ -482,7 +482,7 @@ int32_t tg_dense_inverse(const double* A, int64_t n, double* Ainv, int32_t mode,
     work.alloc(32 * 32 + 2 * 32 * ld);
     TG_CUDA(cudaMemcpy(D.p, h.data(), sizeof(double) * ld * ld, cudaMemcpyHostToDevice));
     if (mode == 0) tg::gj_inverse(D, n, ld, work, 0);
-    else tg::gj_inverse_dw(D, n, ld, work, 0);
+    else tg::gj_inverse_dw(D, n, ld, work, 0, mode == 1);
     TG_CUDA(cudaMemcpy(h.data(), D.p, sizeof(double) * ld * ld, cudaMemcpyDeviceToHost));
     for (int64_t i = 0; i < n; ++i)
       for (int64_t j = 0; j < n; ++j) Ainv[i * n + j] = h[(size_t)(i * ld + j)];

@@ -1407,6 +1407,102 @@ __global__ void __launch_bounds__(TB * TB) k_dw_update(float2* D, int64_t ld, in
   st_dw(d, dw_add(ld_dw(d), dw_neg(two_sum(sh, sl))));
 }
 
+// Step k of the sweep together with step k+1's panel (look-ahead), one
+// launch: the first nb CTAs form panel column J of pivot block K = k+1 from
+// the matrix as step k leaves it -- the pivot tile and tile (K, J), each
+// updated in the CTA by the same double-word expression k_dw_update applies
+// (tile (K, k) is step k's R) --, invert the pivot tile and write P, R, Xb of
+// step K into the other buffer; the other CTAs update the upper tiles as
+// k_dw_update does, except those of row / column K, which step K overwrites
+// anyway.  Same values as the two-launch sweep; the panel's serial chain
+// (pivot-tile inverse) runs beside the update instead of after it.
+template <int TB>
+__global__ void __launch_bounds__(TB * TB) k_dw_update_la(float2* D, int64_t ld, int k, int nb,
+                                                         const float2* P, const float2* R,
+                                                         const float2* Xb, float2* Pn, float2* Rn,
+                                                         float2* Xbn) {
+  pdl_wait();
+  pdl_trigger();
+  const int i = threadIdx.y, j = threadIdx.x;
+  const int K = k + 1;
+  __shared__ float2 xs[TB][TB + 1], rs[TB][TB + 1];
+  if ((int)blockIdx.x < nb) {
+    __shared__ float2 a[TB][TB + 1], tb[TB][TB + 1], xk[TB][TB + 1], ys[TB][TB + 1];
+    __shared__ DW rpiv[2];
+    const int J = blockIdx.x;
+    // X_K and R_K of step k (k_dw_update's xs / rs for block K)
+    xs[i][j] = Xb[(int64_t)i * ld + K * TB + j];
+    rs[i][j] = R[(int64_t)i * ld + K * TB + j];
+    if (J != K && J != k) ys[i][j] = (K < J) ? R[(int64_t)i * ld + J * TB + j]     // R_J
+                                             : Xb[(int64_t)i * ld + J * TB + j];   // X_J
+    __syncthreads();
+    {
+      // pivot tile (K, K) after step k
+      float sh = 0.f, sl = 0.f;
+#pragma unroll
+      for (int m = 0; m < TB; ++m) dw_dot_step(sh, sl, ld_dw(&xs[m][i]), ld_dw(&rs[m][j]));
+      const float2* d = D + (int64_t)(K * TB + i) * ld + K * TB + j;
+      st_dw(&a[i][j], dw_add(ld_dw(d), dw_neg(two_sum(sh, sl))));
+    }
+    if (J == k) {
+      // tile (k, K) is step k's R at block K: A'(K*TB+i, k*TB+j) = R[j][K*TB+i]
+      xk[i][j] = R[(int64_t)j * ld + K * TB + i];
+    } else if (K < J) {
+      // tile (K, J) after step k
+      float sh = 0.f, sl = 0.f;
+#pragma unroll
+      for (int m = 0; m < TB; ++m) dw_dot_step(sh, sl, ld_dw(&xs[m][i]), ld_dw(&ys[m][j]));
+      const float2* d = D + (int64_t)(K * TB + i) * ld + J * TB + j;
+      st_dw(&xk[i][j], dw_add(ld_dw(d), dw_neg(two_sum(sh, sl))));
+    } else if (J < K) {
+      // tile (J, K) after step k, element (j, i) of the upper tile
+      float sh = 0.f, sl = 0.f;
+#pragma unroll
+      for (int m = 0; m < TB; ++m) dw_dot_step(sh, sl, ld_dw(&ys[m][j]), ld_dw(&rs[m][i]));
+      const float2* d = D + (int64_t)(J * TB + j) * ld + K * TB + i;
+      st_dw(&xk[i][j], dw_add(ld_dw(d), dw_neg(two_sum(sh, sl))));
+    }
+    __syncthreads();
+    dw_tile_inverse<TB>(a, tb, rpiv, i, j);
+    if (J == K) {
+      Pn[i * TB + j] = a[i][j];
+      return;
+    }
+    float sh = 0.f, sl = 0.f;
+#pragma unroll
+    for (int m = 0; m < TB; ++m) dw_dot_step(sh, sl, ld_dw(&a[i][m]), ld_dw(&xk[m][j]));
+    st_dw(&Rn[(int64_t)i * ld + J * TB + j], two_sum(sh, sl));
+    Xbn[(int64_t)i * ld + J * TB + j] = xk[i][j];
+    return;
+  }
+  int ib, jb;
+  tri_tile((int)blockIdx.x - nb, ib, jb);
+  if (ib == K || jb == K) return;
+  if (ib == k && jb == k) {
+    const float2 v = P[i * TB + j];
+    D[(int64_t)(k * TB + i) * ld + k * TB + j] = make_float2(-v.x, -v.y);
+    return;
+  }
+  if (ib == k) {
+    D[(int64_t)(k * TB + i) * ld + jb * TB + j] = R[(int64_t)i * ld + jb * TB + j];
+    return;
+  }
+  if (jb == k) {
+    rs[i][j] = R[(int64_t)i * ld + ib * TB + j];
+    __syncthreads();
+    D[(int64_t)(ib * TB + i) * ld + k * TB + j] = rs[j][i];
+    return;
+  }
+  xs[i][j] = Xb[(int64_t)i * ld + ib * TB + j];
+  rs[i][j] = R[(int64_t)i * ld + jb * TB + j];
+  __syncthreads();
+  float sh = 0.f, sl = 0.f;
+#pragma unroll
+  for (int m = 0; m < TB; ++m) dw_dot_step(sh, sl, ld_dw(&xs[m][i]), ld_dw(&rs[m][j]));
+  float2* d = D + (int64_t)(ib * TB + i) * ld + jb * TB + j;
+  st_dw(d, dw_add(ld_dw(d), dw_neg(two_sum(sh, sl))));
+}
+
 // FP64 -> DW in place (h = the FP64 value rounded to FP32, l = the rounded rest)
 __global__ void k_dw_split(double* D, int64_t n) {
   pdl_wait();
@@ -1443,24 +1539,46 @@ __global__ void __launch_bounds__(GJB * GJB) k_dw_mirror(double* D, int64_t ld) 
   }
 }
 
-void gj_inverse_dw(double* D, int64_t n, int64_t ld, double* work, cudaStream_t st) {
+void gj_inverse_dw(double* D, int64_t n, int64_t ld, double* work, cudaStream_t st, bool lookahead) {
   TG_REQUIRE(ld % GJB == 0, "dense leading dimension must be a multiple of 32");
   const int nb = (int)(ld / SWB);
   float2* Df = reinterpret_cast<float2*>(D);
-  float2* P = reinterpret_cast<float2*>(work);
-  float2* R = P + SWB * SWB;
-  float2* Xb = R + SWB * ld;
+  // two (P, R, Xb) sets: the look-ahead writes step k+1's while step k reads its own
+  const int64_t set = SWB * SWB + 2 * SWB * ld;
+  float2* P[2];
+  float2* R[2];
+  float2* Xb[2];
+  for (int b = 0; b < 2; ++b) {
+    P[b] = reinterpret_cast<float2*>(work) + b * set;
+    R[b] = P[b] + SWB * SWB;
+    Xb[b] = R[b] + SWB * ld;
+  }
   launch_pdl(k_dw_split, dim3((unsigned)cdiv(ld * ld, 256)), dim3(256), 0, st, D, ld * ld);
   const dim3 thr(SWB, SWB);
   const unsigned tiles = (unsigned)(nb * (nb + 1) / 2);
-  for (int k = 0; k < nb; ++k) {
-    launch_pdl(k_dw_panel<SWB>, dim3(nb), thr, 0, st, Df, ld, k, P, R, Xb);
-    launch_pdl(k_dw_update<SWB>, dim3(tiles), thr, 0, st, Df, ld, k, (const float2*)P, (const float2*)R, (const float2*)Xb);
+  if (lookahead) {
+    launch_pdl(k_dw_panel<SWB>, dim3(nb), thr, 0, st, Df, ld, 0, P[0], R[0], Xb[0]);
+    for (int k = 0; k + 1 < nb; ++k) {
+      const int b = k & 1;
+      launch_pdl(k_dw_update_la<SWB>, dim3(nb + tiles), thr, 0, st, Df, ld, k, nb,
+                 (const float2*)P[b], (const float2*)R[b], (const float2*)Xb[b], P[b ^ 1], R[b ^ 1],
+                 Xb[b ^ 1]);
+    }
+    const int b = (nb - 1) & 1;
+    launch_pdl(k_dw_update<SWB>, dim3(tiles), thr, 0, st, Df, ld, nb - 1, (const float2*)P[b],
+               (const float2*)R[b], (const float2*)Xb[b]);
+    count_launches((int64_t)nb + 2);     // panel, nb - 1 fused steps, last update, split
+  } else {
+    for (int k = 0; k < nb; ++k) {
+      launch_pdl(k_dw_panel<SWB>, dim3(nb), thr, 0, st, Df, ld, k, P[0], R[0], Xb[0]);
+      launch_pdl(k_dw_update<SWB>, dim3(tiles), thr, 0, st, Df, ld, k, (const float2*)P[0],
+                 (const float2*)R[0], (const float2*)Xb[0]);
+    }
+    count_launches(2 * (int64_t)nb + 1);   // and the split
   }
   const int nm = (int)(ld / GJB);
   launch_pdl(k_dw_mirror, dim3(nm, nm), dim3(GJB, GJB), 0, st, D, ld);
-  count_launches(2 * (int64_t)nb + 1);   // and the split; the mirror is counted below
-  TG_CHECK_LAUNCH();
+  TG_CHECK_LAUNCH();                     // the mirror
 }
 
 // x = Dinv b: a warp per (row, column chunk) writes a partial sum, a second

@@ -158,7 +158,12 @@ void gj_inverse(double* D, int64_t n, int64_t ld, double* work, cudaStream_t st)
 // the same in double-word FP32 arithmetic (about 48 significant bits; same
 // work buffer): mixed-precision contexts, whose coarsest matrix holds FP32
 // values and whose V-cycle runs in FP32
-void gj_inverse_dw(double* D, int64_t n, int64_t ld, double* work, cudaStream_t st);
+// lookahead: each step's update launch also forms the next step's panel
+// (same values, ~half the launches, the panel chain off the critical path);
+// work then needs two sets of 16*16 + 2*16*ld doubles (the 32*32 + 2*32*ld
+// of gj_inverse suffice)
+void gj_inverse_dw(double* D, int64_t n, int64_t ld, double* work, cudaStream_t st,
+                   bool lookahead = true);
 template <typename T>
 void dense_apply(const double* Dinv, int64_t n, int64_t ld, const T* b, T* x,
                  double* work /* >= 8*n */, cudaStream_t st);
