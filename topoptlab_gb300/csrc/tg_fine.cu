@@ -513,8 +513,8 @@ constexpr int PITCH = 48;
 constexpr int PLANE = PX * PITCH;           // words per component plane
 constexpr int NT = EXT * JY;
 template <int NDOF> __host__ __device__ constexpr int ncopy() { return (NDOF * PX * PY + NT - 1) / NT; }
-template <int NDOF> constexpr size_t smem() {
-  return sizeof(float) * ((size_t)3 * NDOF * PLANE + (size_t)4 * NDOF * NT);
+template <int NDOF, typename T> constexpr size_t smem() {
+  return sizeof(T) * ((size_t)3 * NDOF * PLANE + (size_t)4 * NDOF * NT);
 }
 __host__ __device__ constexpr int ycol(int hy) { return (hy & 1) ? ODD + (hy >> 1) : (hy >> 1); }
 }  // namespace zp
@@ -524,10 +524,10 @@ __host__ __device__ constexpr int ycol(int hy) { return (hy & 1) ? ODD + (hy >> 
 // product with B (in place, group by group) and the inverse y butterfly;
 // returns the element's output faces G[0] (lower), G[1] (upper), still in
 // x/z transform space and without the density.
-template <int NDOF, int KIND>
-__device__ __forceinline__ void pair_element(const float (&Fa)[4][NDOF], const float (&Fb)[4][NDOF],
-                                             const Sector<float>& B, float (&G)[2][4][NDOF]) {
-  float U[8][NDOF];
+template <int NDOF, int KIND, typename T>
+__device__ __forceinline__ void pair_element(const T (&Fa)[4][NDOF], const T (&Fb)[4][NDOF],
+                                             const Sector<T>& B, T (&G)[2][4][NDOF]) {
+  T U[8][NDOF];
 #pragma unroll
   for (int q = 0; q < 4; ++q)
 #pragma unroll
@@ -540,12 +540,12 @@ __device__ __forceinline__ void pair_element(const float (&Fa)[4][NDOF], const f
   // NDOF inputs to NDOF outputs on the same index set, so it runs in place
 #pragma unroll
   for (int chi = 0; chi < 8; ++chi) {
-    float in[NDOF];
+    T in[NDOF];
 #pragma unroll
     for (int c2 = 0; c2 < NDOF; ++c2) in[c2] = U[sig<3, NDOF>(chi, c2)][c2];
 #pragma unroll
     for (int c = 0; c < NDOF; ++c) {
-      float acc = 0.f;
+      T acc = T(0);
 #pragma unroll
       for (int c2 = 0; c2 < NDOF; ++c2)
         if (KIND != EK_SECTOR_HEX8 || ((hex8_mask(chi) >> (c * 3 + c2)) & 1u))
@@ -564,11 +564,11 @@ __device__ __forceinline__ void pair_element(const float (&Fa)[4][NDOF], const f
 }
 
 // the x and z butterflies of one face (q = dx | dz << 1 <-> cx | cz << 1)
-template <int NDOF>
-__device__ __forceinline__ void face_xz(float (&F)[4][NDOF]) {
+template <int NDOF, typename T>
+__device__ __forceinline__ void face_xz(T (&F)[4][NDOF]) {
 #pragma unroll
   for (int c = 0; c < NDOF; ++c) {
-    float t0 = F[0][c], t1 = F[1][c];
+    T t0 = F[0][c], t1 = F[1][c];
     F[0][c] = t0 + t1;
     F[1][c] = t0 - t1;
     t0 = F[2][c];
@@ -587,13 +587,13 @@ __device__ __forceinline__ void face_xz(float (&F)[4][NDOF]) {
 }
 
 // zc unused: blockIdx.z takes node planes [z nnz / gridDim.z, (z+1) nnz / gridDim.z)
-template <int NDOF, typename S, int KIND, int MODE, int DOTK = -1>
-__global__ void __launch_bounds__(zp::NT, 3) k_fine_zpair(ApplyArgs<float, S> a, int zc) {
+template <int NDOF, typename T, typename S, int KIND, int MODE, int DOTK = -1>
+__global__ void __launch_bounds__(zp::NT, sizeof(T) == 8 ? 1 : 3) k_fine_zpair(ApplyArgs<T, S> a,
+                                                                              int zc) {
   pdl_wait();
   pdl_trigger();
   using namespace zp;
   static_assert(32 % JY == 0, "the y shuffle needs warps made of whole rows of pairs");
-  using T = float;
   constexpr int SLOT = NDOF * PLANE;
   constexpr int NCP = ncopy<NDOF>();
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -632,7 +632,7 @@ __global__ void __launch_bounds__(zp::NT, 3) k_fine_zpair(ApplyArgs<float, S> a,
     T* dst = us + slot * SLOT;
 #pragma unroll
     for (int k = 0; k < NCP; ++k)
-      if (soff[k] >= 0) cp_async<4>(dst + soff[k], src + goff[k]);
+      if (soff[k] >= 0) cp_async<sizeof(T)>(dst + soff[k], src + goff[k]);
   };
 
   // this thread's element pair and owned nodes
@@ -683,13 +683,13 @@ __global__ void __launch_bounds__(zp::NT, 3) k_fine_zpair(ApplyArgs<float, S> a,
 #pragma unroll
           for (int c = 0; c < NDOF; ++c)
             F[q][c] = ((q >> 1) ? p1 : p0)[c * PLANE + (q & 1) * PITCH + col];
-        face_xz<NDOF>(F);
+        face_xz<NDOF, T>(F);
       };
       T Fa[4][NDOF], Fb[4][NDOF];
       load_face(cf0, Fa);
       load_face(cf1, Fb);
       T G[2][4][NDOF];
-      pair_element<NDOF, KIND>(Fa, Fb, a.B, G);
+      pair_element<NDOF, KIND, T>(Fa, Fb, a.B, G);
 #pragma unroll
       for (int q = 0; q < 4; ++q)
 #pragma unroll
@@ -698,16 +698,16 @@ __global__ void __launch_bounds__(zp::NT, 3) k_fine_zpair(ApplyArgs<float, S> a,
           O[1][q][c] = rhoA * G[1][q][c];
         }
       load_face(cf2, Fa);                        // face 2 (upper face of element B)
-      pair_element<NDOF, KIND>(Fb, Fa, a.B, G);
+      pair_element<NDOF, KIND, T>(Fb, Fa, a.B, G);
 #pragma unroll
       for (int q = 0; q < 4; ++q)
 #pragma unroll
         for (int c = 0; c < NDOF; ++c) {
-          O[1][q][c] = fmaf(rhoB, G[0][q][c], O[1][q][c]);
+          O[1][q][c] = fma(rhoB, G[0][q][c], O[1][q][c]);
           O[2][q][c] = rhoB * G[1][q][c];
         }
 #pragma unroll
-      for (int f = 0; f < 3; ++f) face_xz<NDOF>(O[f]);
+      for (int f = 0; f < 3; ++f) face_xz<NDOF, T>(O[f]);
     } else {
 #pragma unroll
       for (int f = 0; f < 3; ++f)
@@ -769,8 +769,8 @@ __global__ void __launch_bounds__(zp::NT, 3) k_fine_zpair(ApplyArgs<float, S> a,
           else out = pu[c * PLANE] + a.omega * dv[f][c] * (bv[f][c] - au);
           out = ((fx[f] >> c) & 1) ? T(0) : out;
           a.y[(nid + f) * NDOF + c] = out;
-          if (DOTK == DOT_ALPHA) dacc = fmaf(pu[c * PLANE], out, dacc);
-          else if (DOTK == DOT_RHO) dacc = fmaf(bv[f][c], out, dacc);
+          if (DOTK == DOT_ALPHA) dacc = fma(pu[c * PLANE], out, dacc);
+          else if (DOTK == DOT_RHO) dacc = fma(bv[f][c], out, dacc);
         }
       }
 #pragma unroll
@@ -835,17 +835,17 @@ static ZsShape zstream_shape(const Grid& g, bool fp64) {
   return s;
 }
 
-// the paired-element kernel: FP32 with a sector-form element product
-template <typename T, int KIND> constexpr bool use_zpair() {
-  return std::is_same<T, float>::value && KIND != EK_DENSE;
-}
+// the paired-element kernel: every sector-form element product, FP32 and
+// FP64 (in FP64 its shared faces and 1.10 instead of 1.26 evaluations per
+// element cut the FP64-pipe work of the residual by a fifth)
+template <typename T, int KIND> constexpr bool use_zpair() { return KIND != EK_DENSE; }
 // its launch shape: 31 x 15 node columns, as many z chunks (balanced plane
-// ranges) as fill one wave of 3 resident CTAs per SM
-static ZsShape zpair_shape(const Grid& g) {
+// ranges) as fill one wave of resident CTAs (3 per SM in FP32, 1 in FP64)
+static ZsShape zpair_shape(const Grid& g, bool fp64) {
   ZsShape s;
   s.gy = (int)cdiv(g.nny, zp::OY);
   s.gx = (int)cdiv(g.nnx, zp::OX);
-  const int target = sm_count() * 3;
+  const int target = sm_count() * (fp64 ? 1 : 3);
   const int cols = s.gx * s.gy;
   s.chunks = std::max(1, std::min(g.nnz, target / cols));
   s.zc = (int)cdiv(g.nnz, s.chunks);
@@ -855,7 +855,8 @@ static ZsShape zpair_shape(const Grid& g) {
 // partial-sum slot per CTA)
 template <typename T, int KIND>
 static int64_t fine3d_ctas(const Grid& g) {
-  return use_zpair<T, KIND>() ? zpair_shape(g).ctas() : zstream_shape(g, sizeof(T) == 8).ctas();
+  return use_zpair<T, KIND>() ? zpair_shape(g, sizeof(T) == 8).ctas()
+                              : zstream_shape(g, sizeof(T) == 8).ctas();
 }
 
 template <int NDOF, typename T, typename S, int KIND, int MODE, int DOTK = -1>
@@ -863,10 +864,10 @@ static void launch_zstream(const ApplyArgs<T, S>& a, cudaStream_t st) {
   const int pk = std::is_same<T, double>::value ? PK_FINE_F64
                  : (std::is_same<S, float>::value ? PK_FINE_F32 : PK_FINE_BF16);
   if constexpr (use_zpair<T, KIND>()) {
-    constexpr size_t smem = zp::smem<NDOF>();
-    auto kern = k_fine_zpair<NDOF, S, KIND, MODE, DOTK>;
+    constexpr size_t smem = zp::smem<NDOF, T>();
+    auto kern = k_fine_zpair<NDOF, T, S, KIND, MODE, DOTK>;
     set_smem_limit((const void*)kern, (int)smem);
-    const ZsShape sh = zpair_shape(a.g);
+    const ZsShape sh = zpair_shape(a.g, sizeof(T) == 8);
     if (DOTK >= 0 && sh.ctas() > RED_BLOCKS)
       throw Error{EINVAL_, "fused dot: more CTAs than partial-sum slots"};
     prof_begin(pk, st);
