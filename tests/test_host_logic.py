@@ -50,6 +50,13 @@ def test_solver_options_mapping():
     assert o["rtol"] == 1e-6 and o["precision"] == "mixed" and o["nlevels"] == 3
     o = solver_options({"name": "gb300-pcg"}, {"name": "gb300-jacobi"})
     assert o["precond"] == "gb300-jacobi"
+    # the V-cycle's smoothing options pass through to the context
+    o = solver_options({"name": "gb300-gmgpcg"},
+                       {"name": "gb300-gmg", "nsmooth": 1, "nsmooth_coarse": 2, "unsmoothed": 2,
+                        "omega": 0.6})
+    assert (o["nsmooth"], o["nsmooth_coarse"], o["unsmoothed"], o["omega"]) == (1, 2, 2, 0.6)
+    o = solver_options({"name": "gb300-gmgpcg"}, {"name": "gb300-gmg"})
+    assert (o["nsmooth"], o["nsmooth_coarse"], o["unsmoothed"]) == (2, 0, 0)
     with pytest.raises(ValueError):
         solver_options({"name": "no-such-solver"}, {"name": None})
     with pytest.raises(ValueError):
