@@ -62,3 +62,34 @@ def test_shifted_filter_equals_matrix_filter():
     v = np.random.default_rng(5).uniform(size=nx * ny * nz)
     np.testing.assert_allclose(apply(v), H @ v, rtol=1e-14)
     np.testing.assert_allclose(hs, Hs, rtol=1e-14)
+
+
+@pytest.mark.parametrize("unsmoothed,nsmooth,nsmooth_coarse", [((1,), 1, 2), ((1, 2), 2, 0),
+                                                                ((), 1, 3)])
+def test_oracle_vcycle_variants_are_spd_preconditioners(unsmoothed, nsmooth, nsmooth_coarse):
+    """The oracle's V-cycle with unsmoothed levels and a separate coarse sweep
+    count (the GPU context's tg_problem.unsmoothed / nsmooth_coarse, which
+    the GPU tests compare against it) is a symmetric positive definite
+    operator, so PCG with it converges to the direct solution."""
+    nx, ny, nz = 16, 8, 8
+    rng = np.random.default_rng(5)
+    KE = O.ke_elast(3)
+    x = rng.uniform(0.05, 1.0, nx * ny * nz)
+    fixed, f = O.bc_cantilever_3d(nx, ny, nz)
+    ndof = f.shape[0]
+    K = O.assemble(KE, O.edofmat(nx, ny, nz, 3), O.simp(x), ndof)
+    mask = np.zeros(ndof, bool)
+    mask[fixed] = True
+    h = G.Hierarchy(K, mask, (nx, ny, nz), 3, 4, omega=0.6, nsmooth=nsmooth,
+                    unsmoothed=unsmoothed, nsmooth_coarse=nsmooth_coarse)
+    b1 = rng.standard_normal(ndof) * ~mask
+    b2 = rng.standard_normal(ndof) * ~mask
+    z1, z2 = h.vcycle(b1), h.vcycle(b2)
+    assert abs(z1 @ b2 - z2 @ b1) <= 1e-10 * abs(z1 @ b2)
+    assert z1 @ b1 > 0 and z2 @ b2 > 0
+    A = h.A[0]
+    u, it = G.pcg(A, f * ~mask, h.vcycle, rtol=1e-10, maxiter=500)
+    assert it < 500
+    free = np.setdiff1d(np.arange(ndof), fixed)
+    ud = O.solve_direct(K, f, free)
+    np.testing.assert_allclose(u, ud, rtol=0, atol=1e-7 * np.abs(ud).max())
