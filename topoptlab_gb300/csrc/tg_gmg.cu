@@ -145,21 +145,27 @@ __device__ __forceinline__ T ldv(const T* p) {
 }
 
 // Small levels (too few (row, node) pairs to hide the coefficient-load
-// latency): three threads per pair, each summing the 9 directions of one
-// neighbour plane (dz = -1, 0, +1; in 2-D three columns dx), the partial sums
-// added in fixed order through shared memory.
-constexpr int SMALL_PAIRS = 128;
-// one block's work: pairs [vb * SMALL_PAIRS, (vb + 1) * SMALL_PAIRS) with
-// 3 * SMALL_PAIRS threads; ends with a barrier, so part can be reused
+// latency): several threads per pair, each summing the 3 directions of one
+// neighbour row (dz, dx fixed, dy = -1, 0, +1; 9 rows in 3-D, 3 in 2-D), the
+// partial sums added in fixed order through shared memory -- a short load
+// chain per thread and more CTAs on grids too small to fill the GPU.
+template <int NDIM> __host__ __device__ constexpr int small_split() { return NDIM == 3 ? 9 : 3; }
+template <int NDIM> __host__ __device__ constexpr int small_pairs() { return NDIM == 3 ? 64 : 128; }
+template <int NDIM> __host__ __device__ constexpr int small_threads() {
+  return small_split<NDIM>() * small_pairs<NDIM>();
+}
+// one block's work: pairs [vb * SP, (vb + 1) * SP) with small_threads
+// threads; ends with a barrier, so part can be reused
 template <int NDIM, int NDOF, typename T, int MODE, bool CG = false>
 __device__ __forceinline__ void stencil_small_vb(const Grid& g, const T* __restrict__ A,
                                                  const T* __restrict__ u, T* __restrict__ y,
                                                  const T* __restrict__ b,
                                                  const T* __restrict__ dinv, T omega, int64_t vb,
-                                                 T (&part)[3][SMALL_PAIRS]) {
-  const int slot = threadIdx.x % SMALL_PAIRS, pz = threadIdx.x / SMALL_PAIRS;
+                                                 T (&part)[small_split<NDIM>()][small_pairs<NDIM>()]) {
+  constexpr int SP = small_pairs<NDIM>(), NS = small_split<NDIM>();
+  const int slot = threadIdx.x % SP, pz = threadIdx.x / SP;
   const int64_t ld = g.nnodes(), lda = g.slds();
-  const int64_t t = vb * SMALL_PAIRS + slot;
+  const int64_t t = vb * SP + slot;
   const bool active = t < ld * NDOF;
   T acc = T(0);
   int ci = 0;
@@ -171,10 +177,9 @@ __device__ __forceinline__ void stencil_small_vb(const Grid& g, const T* __restr
     node_xyz(g, n, x, yy, z);
     const int64_t sx = g.nny, sz = (int64_t)g.nny * g.nnx;
 #pragma unroll
-    for (int e = 0; e < 9; ++e) {
-      // 3-D: directions pz*9 + e (dz = pz - 1); 2-D: directions pz*3 + e (dx = pz - 1)
-      if (NDIM == 2 && e >= 3) break;
-      const int d = (NDIM == 3) ? pz * 9 + e : pz * 3 + e;
+    for (int e = 0; e < 3; ++e) {
+      // the row pz: 3-D (dz, dx) = (pz / 3 - 1, pz % 3 - 1), 2-D dx = pz - 1
+      const int d = pz * 3 + e;
       int dx, dy, dz;
       dir_xyz(d, NDIM, dx, dy, dz);
       const bool v = in_grid(g, x + dx, yy + dy, z + dz);
@@ -189,7 +194,9 @@ __device__ __forceinline__ void stencil_small_vb(const Grid& g, const T* __restr
   part[pz][slot] = acc;
   __syncthreads();
   if (pz == 0 && active) {
-    const T s = (part[0][slot] + part[1][slot]) + part[2][slot];
+    T s = part[0][slot];
+#pragma unroll
+    for (int r = 1; r < NS; ++r) s += part[r][slot];
     const int64_t k = n * NDOF + ci;
     T out;
     if (MODE == AM_Y) out = s;
@@ -200,7 +207,7 @@ __device__ __forceinline__ void stencil_small_vb(const Grid& g, const T* __restr
   __syncthreads();
 }
 template <int NDIM, int NDOF, typename T, int MODE>
-__global__ void __launch_bounds__(3 * SMALL_PAIRS) k_stencil_small(Grid g, const T* __restrict__ A,
+__global__ void __launch_bounds__(small_threads<NDIM>()) k_stencil_small(Grid g, const T* __restrict__ A,
                                                                   const T* __restrict__ u,
                                                                   T* __restrict__ y,
                                                                   const T* __restrict__ b,
@@ -208,7 +215,7 @@ __global__ void __launch_bounds__(3 * SMALL_PAIRS) k_stencil_small(Grid g, const
                                                                   T omega) {
   pdl_wait();
   pdl_trigger();
-  __shared__ T part[3][SMALL_PAIRS];
+  __shared__ T part[small_split<NDIM>()][small_pairs<NDIM>()];
   stencil_small_vb<NDIM, NDOF, T, MODE>(g, A, u, y, b, dinv, omega, blockIdx.x, part);
 }
 
@@ -467,11 +474,13 @@ void stencil_apply(const Grid& g, const T* A, const T* u, T* y, const T* b, cons
                    double omega, int mode, cudaStream_t st) {
   const int64_t pairs = g.nnodes() * g.ndof;
   if (pairs < tune_stencil_small_pairs()) {
-    const unsigned blocks = (unsigned)cdiv(pairs, SMALL_PAIRS);
 #define TG_SS(ND, NF)                                                                          \
-  if (mode == AM_Y) launch_pdl(k_stencil_small<ND, NF, T, AM_Y>, dim3(blocks), dim3(3 * SMALL_PAIRS), 0, st, g, A, u, y, b, dinv, (T)omega); \
-  else if (mode == AM_RES) launch_pdl(k_stencil_small<ND, NF, T, AM_RES>, dim3(blocks), dim3(3 * SMALL_PAIRS), 0, st, g, A, u, y, b, dinv, (T)omega); \
-  else launch_pdl(k_stencil_small<ND, NF, T, AM_JACOBI>, dim3(blocks), dim3(3 * SMALL_PAIRS), 0, st, g, A, u, y, b, dinv, (T)omega);
+  {                                                                                            \
+    const dim3 grid((unsigned)cdiv(pairs, small_pairs<ND>())), blk(small_threads<ND>());      \
+    if (mode == AM_Y) launch_pdl(k_stencil_small<ND, NF, T, AM_Y>, grid, blk, 0, st, g, A, u, y, b, dinv, (T)omega); \
+    else if (mode == AM_RES) launch_pdl(k_stencil_small<ND, NF, T, AM_RES>, grid, blk, 0, st, g, A, u, y, b, dinv, (T)omega); \
+    else launch_pdl(k_stencil_small<ND, NF, T, AM_JACOBI>, grid, blk, 0, st, g, A, u, y, b, dinv, (T)omega); \
+  }
     switch (g.ndim * 10 + g.ndof) {
       case 33: TG_SS(3, 3) break;
       case 31: TG_SS(3, 1) break;
@@ -1692,12 +1701,12 @@ __device__ __forceinline__ bool tail_sync(GridBar* bar) {
 }
 
 template <int NDIM, int NDOF, typename T, bool CLUSTER>
-__global__ void __launch_bounds__(3 * SMALL_PAIRS) k_coarse_tail(TailArgs<T> a) {
-  __shared__ T spart[3][SMALL_PAIRS];
+__global__ void __launch_bounds__(small_threads<NDIM>()) k_coarse_tail(TailArgs<T> a) {
+  __shared__ T spart[small_split<NDIM>()][small_pairs<NDIM>()];
   const int64_t gtid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t gsz = (int64_t)gridDim.x * blockDim.x;
   const int64_t rows_t = a.gt.nnodes() * NDOF;
-  const int64_t nvb = cdiv(rows_t, SMALL_PAIRS);
+  const int64_t nvb = cdiv(rows_t, small_pairs<NDIM>());
   auto sweep = [&](const T* in, T* out, int mode) {
     for (int64_t vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
       if (mode == AM_JACOBI)
@@ -1774,7 +1783,8 @@ void coarse_tail(const TailArgs<T>& a, cudaStream_t st) {
     default: throw Error{EINVAL_, "unsupported (ndim, nnode_dof)"};
   }
   cudaLaunchConfig_t cfg = {};
-  cfg.blockDim = dim3(3 * SMALL_PAIRS);
+  const int nthr = a.gt.ndim == 3 ? small_threads<3>() : small_threads<2>();
+  cfg.blockDim = dim3((unsigned)nthr);
   cfg.dynamicSmemBytes = 0;
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
@@ -1810,7 +1820,7 @@ void coarse_tail(const TailArgs<T>& a, cudaStream_t st) {
     static std::atomic<int> fits[4] = {};      // resident blocks per SM, found once per variant
     int per_sm = fits[slot].load(std::memory_order_relaxed);
     if (!per_sm) {
-      TG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 3 * SMALL_PAIRS, 0));
+      TG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, nthr, 0));
       TG_REQUIRE(per_sm >= 1, "coarse_tail: kernel does not fit on an SM");
       fits[slot].store(per_sm, std::memory_order_relaxed);
     }
