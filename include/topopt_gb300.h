@@ -308,14 +308,24 @@ int32_t tg_stats(int32_t reset, int64_t* launches, double* prof_ms, int64_t* pro
  * them one after another.  Same results.
  * TG_TUNE_TAIL_BARRIER_TIMEOUT:
  * like TG_TUNE_OC_BARRIER_TIMEOUT for the next such launch (the solve or
- * tg_vcycle call returns TG_ETIMEOUT).  Unknown keys return TG_EINVAL. */
+ * tg_vcycle call returns TG_ETIMEOUT).  TG_TUNE_CONV_UMMA: value != 0
+ * (default) runs the learned warm start's TF32 inference convolutions on the
+ * 5th-generation tensor cores (tcgen05, accumulators in tensor memory); 0 on
+ * warp-level mma.sync.  Both round the operands to TF32 the same way and
+ * accumulate in FP32 (the sums in another order).  TG_TUNE_CONV_TIMEOUT:
+ * value != 0 makes the next tensor-core convolution launch wait on a barrier
+ * phase that never completes, so its bounded waits run out (about a second)
+ * and the call that ran it returns TG_ETIMEOUT; the switch clears itself.
+ * Unknown keys return TG_EINVAL. */
 enum {
   TG_TUNE_STENCIL_SMALL_PAIRS = 1,
   TG_TUNE_OC_BARRIER_TIMEOUT = 2,
   TG_TUNE_COARSE_TAIL = 3,
   TG_TUNE_TAIL_BARRIER_TIMEOUT = 4,
   TG_TUNE_STENCIL_TMA = 5,
-  TG_TUNE_PDL = 6
+  TG_TUNE_PDL = 6,
+  TG_TUNE_CONV_UMMA = 7,
+  TG_TUNE_CONV_TIMEOUT = 8
 };
 int32_t tg_tune(int32_t key, int64_t value);
 /* edofMat (elements/bilinear_quadrilateral.py:7-48, trilinear_hexahedron.py:7-58)

@@ -86,6 +86,72 @@ def test_tf32_inference_matches_oracle(gpu_lib):
     np.testing.assert_allclose(y_tf32, y_ref, rtol=0, atol=1e-2 * scale)
 
 
+def _infer_net(nx, ny, nz, seed):
+    from topoptlab_gb300.learned import LearnedWarmStart
+    prob = _problem(nx, ny, nz)
+    net = LearnedWarmStart(prob, capacity=1, seed=seed)
+    info = net.info()
+    grid = info["grid"]
+    rng = np.random.default_rng(seed + 6)
+    net.set_params((rng.standard_normal(info["nparams"]) * 0.05).astype(np.float32))
+    x0 = rng.standard_normal((grid[0] * grid[1] * grid[2], 7)).astype(np.float32)
+    return prob, net, x0
+
+
+def test_tensor_core_inference_matches_mma_sync(gpu_lib):
+    """The warm start's inference convolutions on the 5th-generation tensor
+    cores (tcgen05: operands in shared memory, FP32 accumulators in tensor
+    memory, one thread issuing the MMAs) and on warp-level mma.sync round the
+    operands to TF32 the same way and accumulate in FP32 in different orders:
+    the outputs agree to 1e-4 of the largest output, on a level-1 grid of
+    25 x 13 x 13 nodes (partial 8 x 16 node tiles in y and x, 16 -> 32 -> 64
+    channels and back); both are within 1e-2 of the FP32-level forward."""
+    from topoptlab_gb300 import _lib
+    lib = _lib.load()
+    prob, net, x0 = _infer_net(48, 24, 24, 5)
+    out = {}
+    try:
+        assert net.info()["grid"] == (25, 13, 13)
+        for on in (1, 0):
+            assert lib.tg_tune(_lib.TG_TUNE_CONV_UMMA, on) == _lib.TG_OK
+            out[on] = net.infer(x0)
+        ref = net.eval(x0)
+    finally:
+        lib.tg_tune(_lib.TG_TUNE_CONV_UMMA, 1)
+        net.close()
+        prob.close()
+    scale = np.abs(ref).max()
+    assert scale > 0 and np.abs(out[1]).max() > 0.5 * scale
+    np.testing.assert_allclose(out[1], out[0], rtol=0, atol=1e-4 * scale)
+    np.testing.assert_allclose(out[1], ref, rtol=0, atol=1e-2 * scale)
+
+
+def test_tensor_core_convolution_wait_runs_out(gpu_lib):
+    """The tcgen05 convolution's mbarrier waits are bounded: tg_tune makes one
+    CTA of the next launch wait on a barrier phase that nothing completes; its
+    wait gives up after about a second, the CTA frees its tensor memory and
+    leaves, and the call returns TG_ETIMEOUT (RuntimeError).  The next call
+    on the same network gives the same output as before, bit for bit."""
+    import time
+    from topoptlab_gb300 import _lib
+    lib = _lib.load()
+    prob, net, x0 = _infer_net(16, 8, 8, 9)
+    try:
+        y0 = net.infer(x0)
+        assert lib.tg_tune(_lib.TG_TUNE_CONV_TIMEOUT, 1) == _lib.TG_OK
+        t0 = time.perf_counter()
+        with pytest.raises(RuntimeError, match="timed out"):
+            net.infer(x0)
+        assert time.perf_counter() - t0 < 60.0
+        y1 = net.infer(x0)
+    finally:
+        lib.tg_tune(_lib.TG_TUNE_CONV_TIMEOUT, 0)
+        net.close()
+        prob.close()
+    assert np.abs(y0).max() > 0
+    np.testing.assert_array_equal(y1, y0)
+
+
 def test_adam_steps_match_oracle(gpu_lib):
     """Two Adam steps of the network's optimiser (tg_cnn_fit on one pair)
     against the oracle's FP32 Adam fed with the GPU's own gradients at p0 and

@@ -20,7 +20,7 @@ TG_PRECOND_GMG, TG_PRECOND_JACOBI = 0, 1
 (TG_FIELD_X, TG_FIELD_XPHYS, TG_FIELD_U, TG_FIELD_DC, TG_FIELD_DV, TG_FIELD_F) = range(6)
 TG_TUNE_STENCIL_SMALL_PAIRS, TG_TUNE_OC_BARRIER_TIMEOUT = 1, 2
 TG_TUNE_COARSE_TAIL, TG_TUNE_TAIL_BARRIER_TIMEOUT, TG_TUNE_STENCIL_TMA = 3, 4, 5
-TG_TUNE_PDL = 6
+TG_TUNE_PDL, TG_TUNE_CONV_UMMA, TG_TUNE_CONV_TIMEOUT = 6, 7, 8
 
 _dp = C.POINTER(C.c_double)
 _i64p = C.POINTER(C.c_int64)

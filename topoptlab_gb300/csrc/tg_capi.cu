@@ -650,6 +650,8 @@ int32_t tg_cnn_infer(tg_cnn* cnn, const float* x0, float* y) {
     net.forward(st, false);
     d2h(y, net.y.p, na * 3, st);
     TG_CUDA(cudaStreamSynchronize(st));
+    if (tg::take_conv_error(st))
+      throw tg::Error{tg::ETIMEOUT, "tensor-core convolution: a bounded wait timed out"};
   });
 }
 

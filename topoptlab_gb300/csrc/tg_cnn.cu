@@ -244,9 +244,380 @@ static void conv3_launch(const NG& g, const float* in, const float* W, int cout,
   TG_CHECK_LAUNCH();
 }
 
+// ---------------------------------------------------------------------------
+// The same convolution on the 5th-generation tensor cores (tcgen05), for the
+// warm start's TF32 inference.
+// ---------------------------------------------------------------------------
+// A CTA of 4 warps computes 128 output nodes -- 8 (y) x 16 (x) of one z plane
+// -- times NN output channels (blockIdx.z / nz selects the chunk) as one
+// M = 128, N = NN FP32 accumulator in tensor memory (TMEM): tile row r is
+// TMEM lane r, node (y0 + r % 8, x0 + r / 8); column n is output channel
+// co0 + n.  Both operands sit in shared memory in the MMA's K-major layout
+// without swizzle: core matrices of 8 rows x 16 bytes (4 TF32 values), the 8
+// rows 16 bytes apart, neighbouring core matrices along K `lbo` bytes apart
+// and along M (or N) `sbo` bytes apart.
+//  * A (input): the tile's input block with a one-node halo, 3 (z) x 18 (x)
+//    x 10 (y) nodes, as planes [chunk of 8 channels][half of 4] of [z][x][y]
+//    16-byte entries (zero outside the grid and past CIN), staged once by all
+//    threads.  For a tap (dz, dx, dy) the 128 rows are 16 runs of 8
+//    consecutive y entries, one run per x, so the tap's A matrix is a view of
+//    the block: start at the shifted entry, sbo = one x column (10 entries),
+//    lbo = one plane.
+//  * B (one tap's weights): the image [chunk][half][n] of 16-byte entries (4
+//    input channels of output channel co0 + n; sbo = 8 entries, lbo = NN
+//    entries), packed in global memory once per forward pass (k_pack_umma)
+//    and streamed by bulk copies (cp.async.bulk) into a ring of WSTAGES
+//    stages: a stage's "full" barrier completes when its copy has landed, its
+//    "empty" barrier when the MMAs that read it have completed.
+// One thread drives the ring and the tensor core: per tap it waits for the
+// stage to be full, issues the NCH MMAs (K = 8 each), commits them to the
+// stage's empty barrier, and refills the previous tap's stage once those
+// MMAs are done.  A last commit completes the "done" barrier, on which the
+// other threads wait before they read their 32 TMEM lanes (tcgen05.ld) and
+// apply bias, skip and relu.  Operands are rounded to TF32 as the mma.sync
+// kernel rounds them (cvt.rna) and accumulated in FP32 in the same order
+// (tap, chunk of 8 channels), so the two kernels give the same results.
+// Every wait is bounded (about a second of %globaltimer): a wait that runs
+// out makes the CTA issue nothing more, wait once more (bounded) for its
+// copies and MMAs in flight, free its TMEM and leave without storing; the
+// convolution error flag tells the host (TG_ETIMEOUT).
+__device__ int g_conv_err = 0;
+
+namespace um {
+constexpr int TY = 8, TX = 16, HY = TY + 2, HX = TX + 2, HZ = 3;
+constexpr int HN = HZ * HX * HY;                 // 540 halo entries per plane
+// bytes per [chunk][half] plane: one entry of padding puts the 8 planes that
+// a quarter warp stores to in distinct 16-byte bank groups
+constexpr int PLANE = (HN + 1) * 16;
+constexpr int WSTAGES = 4;
+constexpr uint64_t WAIT_NS = 1000000000ull;
+// mbarriers: full[WSTAGES], empty[WSTAGES], done, stall (never completes)
+constexpr int B_FULL = 0, B_EMPTY = WSTAGES, B_DONE = 2 * WSTAGES, B_STALL = 2 * WSTAGES + 1;
+constexpr int NBARS = 2 * WSTAGES + 2;
+}  // namespace um
+
+// output channels per CTA for a layer of cout channels (the MMA's N)
+inline int umma_nn(int cout) { return cout <= 16 ? 16 : cout <= 32 ? 32 : 64; }
+
+template <int CIN, int NN>
+struct UmmaConv {
+  static constexpr int CP = (CIN + 7) / 8 * 8;
+  static constexpr int NCH = CP / 8;
+  static constexpr int A_BYTES = NCH * 2 * um::PLANE;
+  static constexpr int W_BYTES = NCH * 2 * NN * 16;        // one tap's weight image
+  static constexpr int TCOLS = NN < 32 ? 32 : NN;          // TMEM columns: a power of 2, >= 32
+  // 128 bytes of alignment slack, 128 of mbarriers, TMEM address and flag
+  static constexpr size_t smem() {
+    return 256 + (size_t)A_BYTES + (size_t)um::WSTAGES * W_BYTES;
+  }
+};
+
+// shared-memory matrix descriptor: start address, leading (K) and stride
+// (M / N) byte offsets, each in 16-byte units; bits 46-48 hold the fixed
+// value 0b001; base offset 0, no swizzle
+__device__ __forceinline__ uint64_t umma_sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+// instruction descriptor of kind::tf32: D FP32 (bits 4-5 = 1), A and B TF32
+// (bits 7-9 and 10-12 = 2), both K-major, N >> 3 at bit 17, M >> 4 at bit 24
+__host__ __device__ constexpr uint32_t umma_idesc_tf32(int m, int n) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) |
+         ((uint32_t)(m >> 4) << 24);
+}
+__device__ __forceinline__ void umma_tf32(uint32_t dtmem, uint64_t adesc, uint64_t bdesc,
+                                          uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n"
+      :: "r"(dtmem), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate) : "memory");
+}
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+               ::"r"(smem_u32(bar)) : "memory");
+}
+// bulk copy of `bytes` (a multiple of 16, both addresses 16-byte aligned)
+// from global to shared memory, completing on `bar` with its byte count
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+               ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+      ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
+}
+// 16 consecutive 32-bit TMEM columns of this thread's lane; the wait carries
+// the registers, so nothing reads them before the load has completed
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
+      "%15}, [%16];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+        "=r"(v[14]), "=r"(v[15])
+      : "r"(taddr) : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(v[0]), "+r"(v[1]), "+r"(v[2]), "+r"(v[3]), "+r"(v[4]), "+r"(v[5]),
+                 "+r"(v[6]), "+r"(v[7]), "+r"(v[8]), "+r"(v[9]), "+r"(v[10]), "+r"(v[11]),
+                 "+r"(v[12]), "+r"(v[13]), "+r"(v[14]), "+r"(v[15])
+               :: "memory");
+}
+__device__ __forceinline__ float tf32r(float v) { return __uint_as_float(f2tf32(v)); }
+
+// weight images of the tensor-core kernel: out[((chunk * 27 + k) * NCH2 + p)
+// * NN + n][j] = tf32(W[k][4 p + j][chunk * NN + n]), zero past cin / cout
+struct PackJob {
+  const float* W;
+  float* out;
+  int cin, cout, nn, nch2, chunks;
+};
+struct PackJobs {
+  PackJob j[6];
+};
+__global__ void k_pack_umma(PackJobs jobs) {
+  const PackJob& jb = jobs.j[blockIdx.y];
+  const int64_t per_tap = (int64_t)jb.nch2 * jb.nn * 4;
+  const int64_t total = (int64_t)jb.chunks * 27 * per_tap;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int j = (int)(i & 3), n = (int)((i >> 2) % jb.nn);
+    const int p = (int)((i / (4 * jb.nn)) % jb.nch2);
+    const int k = (int)((i / per_tap) % 27), ch = (int)(i / (per_tap * 27));
+    const int ci = 4 * p + j, co = ch * jb.nn + n;
+    jb.out[i] = (ci < jb.cin && co < jb.cout) ? tf32r(jb.W[((int64_t)k * jb.cin + ci) * jb.cout + co])
+                                               : 0.f;
+  }
+}
+
+template <int CIN, int NN>
+__global__ void __launch_bounds__(128) k_conv3_umma(NG g, const float* __restrict__ in,
+                                                    const float* __restrict__ Wp, int cout,
+                                                    const float* __restrict__ bias,
+                                                    const float* __restrict__ skip, int relu,
+                                                    float* __restrict__ out, int stall) {
+  using U = UmmaConv<CIN, NN>;
+  constexpr int NCH = U::NCH, NS = um::WSTAGES;
+  extern __shared__ __align__(128) unsigned char um_smem[];
+  unsigned char* base = um_smem + ((128u - (smem_u32(um_smem) & 127u)) & 127u);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(base);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(base + 8 * um::NBARS);
+  int* s_fail = reinterpret_cast<int*>(base + 8 * um::NBARS + 4);
+  unsigned char* As = base + 128;
+  unsigned char* Ws = As + U::A_BYTES;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int z = (int)(blockIdx.z % (unsigned)g.nz), chunk = (int)(blockIdx.z / (unsigned)g.nz);
+  const int co0 = chunk * NN;
+  const int y0 = blockIdx.x * um::TY, x0 = blockIdx.y * um::TX;
+  const float* wimg = Wp + (int64_t)chunk * 27 * (U::W_BYTES / 4);
+  auto tap_image = [&](int k) { return wimg + (int64_t)k * (U::W_BYTES / 4); };
+
+  if (tid == 0) {
+    *s_fail = 0;
+#pragma unroll
+    for (int k = 0; k < um::NBARS; ++k)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bar[k])) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    // the first WSTAGES taps' weights start moving while the block is staged
+#pragma unroll
+    for (int k = 0; k < NS; ++k)
+      bulk_g2s(Ws + k * U::W_BYTES, tap_image(k), U::W_BYTES, &bar[um::B_FULL + k]);
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                 ::"r"(smem_u32(tslot)), "r"((uint32_t)U::TCOLS) : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  // input block, (chunk, half) fastest so that a warp reads whole node rows;
+  // four entries in flight per thread
+  constexpr int NE = NCH * 2 * um::HN;
+  auto load_entry = [&](int i) {
+    const int p = i % (NCH * 2), e = i / (NCH * 2);
+    const int hy = e % um::HY, hx = (e / um::HY) % um::HX, hz = e / (um::HY * um::HX);
+    const int X = x0 - 1 + hx, Y = y0 - 1 + hy, Z = z - 1 + hz;
+    const int c0 = p * 4;
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (X >= 0 && X < g.nx && Y >= 0 && Y < g.ny && Z >= 0 && Z < g.nz && c0 < CIN) {
+      const float* src = in + ng_idx(g, X, Y, Z) * CIN + c0;
+      if constexpr (CIN % 4 == 0) {
+        v = __ldg(reinterpret_cast<const float4*>(src));
+      } else {
+        v.x = __ldg(src);
+        v.y = c0 + 1 < CIN ? __ldg(src + 1) : 0.f;
+        v.z = c0 + 2 < CIN ? __ldg(src + 2) : 0.f;
+        v.w = c0 + 3 < CIN ? __ldg(src + 3) : 0.f;
+      }
+    }
+    return v;
+  };
+  for (int i0 = tid; i0 < NE; i0 += 4 * 128) {
+    float4 v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      v[u] = (i0 + u * 128 < NE) ? load_entry(i0 + u * 128) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int i = i0 + u * 128;
+      if (i < NE)
+        *reinterpret_cast<float4*>(As + (i % (NCH * 2)) * um::PLANE + (i / (NCH * 2)) * 16) =
+            make_float4(tf32r(v[u].x), tf32r(v[u].y), tf32r(v[u].z), tf32r(v[u].w));
+    }
+  }
+  // generic-proxy stores -> visible to the tensor core's (async-proxy) reads;
+  // the TMEM address written by the allocation
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tslot;
+  bool failed = false;
+  if (tid == 0) {
+    constexpr uint32_t IDESC = umma_idesc_tf32(128, NN);
+    const uint32_t a0 = smem_u32(As), w0 = smem_u32(Ws);
+    int issued = NS - 1;          // the last tap whose weight copy was issued
+    int consumed = -1;            // the last tap whose copy was waited for
+    int committed = -1;           // the last tap whose MMAs were committed
+    if (stall) failed = !mbar_wait_bounded(&bar[um::B_STALL], 0, um::WAIT_NS);
+#pragma unroll 1
+    for (int k = 0; k < 27 && !failed; ++k) {
+      const int s = k % NS;
+      if (!mbar_wait_bounded(&bar[um::B_FULL + s], (k / NS) & 1, um::WAIT_NS)) {
+        failed = true;
+        break;
+      }
+      consumed = k;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const int dy = k % 3 - 1, dx = (k / 3) % 3 - 1, dz = k / 9 - 1;
+      const uint32_t aoff = (uint32_t)((((1 + dz) * um::HX + (1 + dx)) * um::HY + (1 + dy)) * 16);
+#pragma unroll
+      for (int c = 0; c < NCH; ++c) {
+        const uint64_t ad = umma_sdesc(a0 + 2 * c * um::PLANE + aoff, um::PLANE, um::HY * 16);
+        const uint64_t bd = umma_sdesc(w0 + s * U::W_BYTES + 2 * c * NN * 16, NN * 16, 128);
+        umma_tf32(tmem, ad, bd, IDESC, (k | c) != 0 ? 1u : 0u);
+      }
+      umma_commit(&bar[um::B_EMPTY + s]);
+      committed = k;
+      // refill the previous tap's stage once its MMAs are done (this tap's
+      // MMAs keep the tensor core busy meanwhile)
+      const int kp = k - 1, kn = kp + NS;
+      if (kp >= 0 && kn < 27) {
+        const int sp = kp % NS;
+        if (!mbar_wait_bounded(&bar[um::B_EMPTY + sp], (kp / NS) & 1, um::WAIT_NS)) {
+          failed = true;
+          break;
+        }
+        bulk_g2s(Ws + sp * U::W_BYTES, tap_image(kn), U::W_BYTES, &bar[um::B_FULL + sp]);
+        issued = kn;
+      }
+    }
+    if (!failed) {
+      umma_commit(&bar[um::B_DONE]);     // completes when every MMA above has
+    } else {
+      // nothing more is issued; wait (bounded) for what is in flight, then
+      // release the other threads
+      for (int j = consumed + 1; j <= issued; ++j)
+        (void)mbar_wait_bounded(&bar[um::B_FULL + j % NS], (j / NS) & 1, um::WAIT_NS);
+      if (committed >= 0)
+        (void)mbar_wait_bounded(&bar[um::B_EMPTY + committed % NS], (committed / NS) & 1,
+                                um::WAIT_NS);
+      *s_fail = 1;
+      asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}\n"
+                   ::"r"(smem_u32(&bar[um::B_DONE])) : "memory");
+    }
+  }
+  // thread 0 arrives within a few of its own bounded waits, even on failure
+  if (!mbar_wait_bounded(&bar[um::B_DONE], 0, 8 * um::WAIT_NS)) failed = true;
+  failed = __syncthreads_or(failed || *s_fail != 0) != 0;
+  if (!failed) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const int r = warp * 32 + lane;
+    const int Y = y0 + (r & 7), X = x0 + (r >> 3);
+    const bool valid = X < g.nx && Y < g.ny;
+    const int64_t node = valid ? ng_idx(g, X, Y, z) : 0;
+#pragma unroll
+    for (int cb = 0; cb < NN; cb += 16) {
+      uint32_t v[16];
+      tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)cb, v);
+      if (!valid) continue;
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        const int co = co0 + cb + j;
+        if (co >= cout) continue;
+        float val = __uint_as_float(v[j]) + (bias ? bias[co] : 0.f);
+        if (skip) val += skip[node * cout + co];
+        if (relu) val = fmaxf(val, 0.f);
+        out[node * cout + co] = val;
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;"
+                 ::"r"(tmem), "r"((uint32_t)U::TCOLS) : "memory");
+  }
+  if (failed && tid == 0) atomicExch(&g_conv_err, 1);
+}
+
+int take_conv_error(cudaStream_t st) {
+  int v = 0;
+  TG_CUDA(cudaMemcpyFromSymbolAsync(&v, g_conv_err, sizeof(int), 0, cudaMemcpyDeviceToHost, st));
+  TG_CUDA(cudaStreamSynchronize(st));
+  if (v) {
+    static const int zero = 0;
+    TG_CUDA(cudaMemcpyToSymbolAsync(g_conv_err, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, st));
+    TG_CUDA(cudaStreamSynchronize(st));
+  }
+  return v;
+}
+
+template <int CIN, int NN>
+static void conv3_umma_launch(const NG& g, const float* in, const float* Wp, int cout,
+                              const float* bias, const float* skip, int relu, float* out,
+                              cudaStream_t st) {
+  using U = UmmaConv<CIN, NN>;
+  const dim3 grid((unsigned)cdiv(g.ny, um::TY), (unsigned)cdiv(g.nx, um::TX),
+                  (unsigned)(g.nz * cdiv(cout, NN)));
+  set_smem_limit((const void*)k_conv3_umma<CIN, NN>, (int)U::smem());
+  const int stall = tune_take_conv_timeout() ? 1 : 0;
+  k_conv3_umma<CIN, NN><<<grid, 128, U::smem(), st>>>(g, in, Wp, cout, bias, skip, relu, out, stall);
+  TG_CHECK_LAUNCH();
+}
+
+// Wp: the layer's weight images (k_pack_umma); false: no tensor-core variant
+// for this shape (the caller uses mma.sync)
+static bool conv3_umma(const NG& g, int cin, const float* in, const float* Wp, int cout,
+                       const float* bias, const float* skip, int relu, float* out,
+                       cudaStream_t st) {
+  if (cout > 64) return false;
+  auto go = [&](auto cin_tag) {
+    constexpr int CI = decltype(cin_tag)::value;
+    switch (umma_nn(cout)) {
+      case 16: conv3_umma_launch<CI, 16>(g, in, Wp, cout, bias, skip, relu, out, st); break;
+      case 32: conv3_umma_launch<CI, 32>(g, in, Wp, cout, bias, skip, relu, out, st); break;
+      default: conv3_umma_launch<CI, 64>(g, in, Wp, cout, bias, skip, relu, out, st); break;
+    }
+  };
+  switch (cin) {
+    case 7: go(std::integral_constant<int, 7>{}); return true;
+    case 16: go(std::integral_constant<int, 16>{}); return true;
+    case 32: go(std::integral_constant<int, 32>{}); return true;
+    case 64: go(std::integral_constant<int, 64>{}); return true;
+    default: return false;
+  }
+}
+
+// floats of one layer's weight images
+static int64_t umma_pack_size(int cin, int cout) {
+  const int nn = umma_nn(cout);
+  return (int64_t)cdiv(cout, nn) * 27 * ((cin + 7) / 8 * 2) * nn * 4;
+}
+
+// Wp: the layer's tensor-core weight images (TF32 inference only), or null
 static void conv3(const NG& g, int cin, const float* in, const float* W, int cout,
                   const float* bias, const float* skip, int relu, const float* mask, float* out,
-                  cudaStream_t st, bool split = true) {
+                  cudaStream_t st, bool split = true, const float* Wp = nullptr) {
+  if (Wp && !split && !mask && conv3_umma(g, cin, in, Wp, cout, bias, skip, relu, out, st))
+    return;
 #define TG_C3(CI)                                                                                \
   if (split) conv3_launch<CI, true>(g, in, W, cout, bias, skip, relu, mask, out, st);            \
   else conv3_launch<CI, false>(g, in, W, cout, bias, skip, relu, mask, out, st);
@@ -546,6 +917,12 @@ Cnn::Cnn(Ctx& c, int capacity, uint64_t seed) : ctx(&c) {
   nparams = off;
   params.alloc(nparams); grads.alloc(nparams); adam_m.alloc(nparams); adam_v.alloc(nparams);
   wt.alloc((int64_t)27 * 64 * 64);
+  int64_t poff = 0;
+  for (size_t i = 0; i < layers.size(); ++i) {
+    wpack_off[i] = poff;
+    poff += umma_pack_size(layers[i].cin, layers[i].cout);
+  }
+  wpack.alloc(poff);
   adam_m.zero(c.st);
   adam_v.zero(c.st);
   // He-normal initialisation from a seeded generator
@@ -584,24 +961,44 @@ Cnn::Cnn(Ctx& c, int capacity, uint64_t seed) : ctx(&c) {
   TG_CUDA(cudaStreamSynchronize(c.st));
 }
 
+// the tensor-core weight images of every layer, from the current parameters
+void Cnn::pack_umma(cudaStream_t st) {
+  PackJobs jobs{};
+  int64_t most = 0;
+  for (size_t i = 0; i < layers.size(); ++i) {
+    const Layer& l = layers[i];
+    const int nn = umma_nn(l.cout);
+    jobs.j[i] = PackJob{params.p + l.w_off, wpack.p + wpack_off[i], l.cin, l.cout, nn,
+                        (l.cin + 7) / 8 * 2, (int)cdiv(l.cout, nn)};
+    most = std::max(most, umma_pack_size(l.cin, l.cout));
+  }
+  k_pack_umma<<<dim3((unsigned)std::min<int64_t>(cdiv(most, 256), 128), (unsigned)layers.size()),
+                256, 0, st>>>(jobs);
+  TG_CHECK_LAUNCH();
+}
+
 void Cnn::forward(cudaStream_t st, bool split) {
   const float* P = params.p;
   auto W = [&](int i) { return P + layers[i].w_off; };
   auto b = [&](int i) { return P + layers[i].b_off; };
-  conv3(A, 7, x0, W(0), 16, b(0), nullptr, 1, nullptr, e1, st, split);
+  // TF32 inference on the tensor cores (tcgen05) unless switched off
+  const bool tc = !split && tune_conv_umma();
+  if (tc) pack_umma(st);
+  auto Wp = [&](int i) { return tc ? wpack.p + wpack_off[i] : nullptr; };
+  conv3(A, 7, x0, W(0), 16, b(0), nullptr, 1, nullptr, e1, st, split, Wp(0));
   k_pool<<<nb(B.n() * 16), 256, 0, st>>>(A, B, 16, e1, p1);
   TG_CHECK_LAUNCH();
-  conv3(B, 16, p1, W(1), 32, b(1), nullptr, 1, nullptr, e2, st, split);
+  conv3(B, 16, p1, W(1), 32, b(1), nullptr, 1, nullptr, e2, st, split, Wp(1));
   k_pool<<<nb(Cg.n() * 32), 256, 0, st>>>(B, Cg, 32, e2, p2);
   TG_CHECK_LAUNCH();
-  conv3(Cg, 32, p2, W(2), 64, b(2), nullptr, 1, nullptr, e3, st, split);
+  conv3(Cg, 32, p2, W(2), 64, b(2), nullptr, 1, nullptr, e3, st, split, Wp(2));
   k_up<<<nb(B.n() * 64), 256, 0, st>>>(B, Cg, 64, e3, u2);
   TG_CHECK_LAUNCH();
-  conv3(B, 64, u2, W(3), 32, b(3), e2, 1, nullptr, d2, st, split);
+  conv3(B, 64, u2, W(3), 32, b(3), e2, 1, nullptr, d2, st, split, Wp(3));
   k_up<<<nb(A.n() * 32), 256, 0, st>>>(A, B, 32, d2, u1);
   TG_CHECK_LAUNCH();
-  conv3(A, 32, u1, W(4), 16, b(4), e1, 1, nullptr, d1, st, split);
-  conv3(A, 16, d1, W(5), 3, b(5), nullptr, 0, nullptr, y, st, split);
+  conv3(A, 32, u1, W(4), 16, b(4), e1, 1, nullptr, d1, st, split, Wp(4));
+  conv3(A, 16, d1, W(5), 3, b(5), nullptr, 0, nullptr, y, st, split, Wp(5));
 }
 
 // loss against tgt, gradients into grads (forward must have run)

@@ -22,6 +22,10 @@ struct Cnn {
   std::vector<Layer> layers;
   int64_t nparams = 0;
   DevBuf<float> params, grads, adam_m, adam_v, wt;
+  // per layer the TF32 weight images the tensor-core convolution streams
+  // into shared memory (rebuilt from params by every TF32 forward)
+  DevBuf<float> wpack;
+  int64_t wpack_off[6] = {};
   // activations (channels-last) and their gradients
   DevBuf<float> x0, e1, p1, e2, p2, e3, u2, d2, u1, d1, y, tgt;
   DevBuf<float> g_a16, g_a32, g_b64, g_b32, g_b16, g_c64, g_c32, g_e1, g_e2, g_y;
@@ -48,6 +52,7 @@ struct Cnn {
   Cnn& operator=(const Cnn&) = delete;
   // split: FP32-level split-TF32 products (training, checks); otherwise TF32
   void forward(cudaStream_t st, bool split = true);
+  void pack_umma(cudaStream_t st);
   double backward(cudaStream_t st, bool want_loss);
   void adam_step(cudaStream_t st);
   void features(Ctx& c, const double* u_prev);

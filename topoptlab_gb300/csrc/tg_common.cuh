@@ -180,6 +180,8 @@ bool tune_take_oc_barrier_timeout();
 // and the one-shot barrier-timeout request for its next launch
 int tune_coarse_tail();   // 0 off, 1 one cluster, 2 cooperative (one block per SM), > 2 that many blocks
 bool tune_take_tail_barrier_timeout();
+bool tune_conv_umma();           // warm-start inference convolutions on tcgen05 (default on)
+bool tune_take_conv_timeout();   // one-shot: the next tcgen05 convolution's waits run out
 
 #define TG_REQUIRE(cond, msg)                                                \
   do {                                                                       \
@@ -290,6 +292,31 @@ __device__ __forceinline__ bool grid_sync(GridBar* b) {
   }
   __syncthreads();
   return ok != 0;
+}
+
+// mbarrier helpers: the shared-window address of a shared-memory pointer, the
+// global nanosecond timer, and a parity wait that gives up after limit_ns
+// (false: the phase did not complete in time).
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint64_t limit_ns) {
+  const uint32_t a = smem_u32(bar);
+  const uint64_t t0 = global_ns();
+  while (true) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done) : "r"(a), "r"(parity) : "memory");
+    if (done) return true;
+    if (global_ns() - t0 > limit_ns) return false;
+  }
 }
 
 // Number of partial-sum slots used by every grid-wide reduction.  Grids that

@@ -882,6 +882,8 @@ static int pcg32_run(Ctx& c, double tol_abs, int maxit, int start) {
 void check_waits(Ctx& c) {
   if (take_wait_error(c.st))
     throw Error{ETIMEOUT, "multigrid V-cycle: a bounded wait for a TMA copy timed out"};
+  if (c.cnn && take_conv_error(c.st))
+    throw Error{ETIMEOUT, "learned warm start: a bounded wait of the tensor-core convolution timed out"};
   if (!c.tailbar.p) return;
   int err = 0;
   TG_CUDA(cudaMemcpyAsync(&err, &c.tailbar.p->err, sizeof(int), cudaMemcpyDeviceToHost, c.st));

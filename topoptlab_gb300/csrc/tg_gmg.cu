@@ -239,27 +239,6 @@ __global__ void __launch_bounds__(small_threads<NDIM>()) k_stencil_small(Grid g,
 // waits once more for the copies in flight and leaves.
 __device__ int g_wait_err = 0;
 
-__device__ __forceinline__ uint64_t global_ns() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint64_t limit_ns) {
-  const uint32_t a = smem_u32(bar);
-  const uint64_t t0 = global_ns();
-  while (true) {
-    uint32_t done;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-        " selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done) : "r"(a), "r"(parity) : "memory");
-    if (done) return true;
-    if (global_ns() - t0 > limit_ns) return false;
-  }
-}
 
 constexpr int STMA_PT = 128;           // node slots per CTA at most (threads = NDOF * PT)
 constexpr int STMA_SMEM_MAX = 112 * 1024;

@@ -84,6 +84,8 @@ void tune_set_stencil_tma(int on);
 // 1 (and cleared) if a bounded wait of a TMA-fed stencil sweep ran out since
 // the last call; synchronises st
 int take_wait_error(cudaStream_t st);
+// the tensor-core convolution's wait-error flag (read and cleared)
+int take_conv_error(cudaStream_t st);
 template <typename T>
 void stencil_dinv(const Grid& g, const uint8_t* fix, const T* A, T* dinv, cudaStream_t st);
 

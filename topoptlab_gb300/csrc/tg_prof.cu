@@ -68,7 +68,11 @@ std::atomic<int> g_oc_timeout{0};
 std::atomic<int> g_tail{0};
 std::atomic<int> g_pdl{1};
 std::atomic<int> g_tail_timeout{0};
+std::atomic<int> g_conv_umma{1};
+std::atomic<int> g_conv_timeout{0};
 }  // namespace
+bool tune_conv_umma() { return g_conv_umma.load(std::memory_order_relaxed) != 0; }
+bool tune_take_conv_timeout() { return g_conv_timeout.exchange(0) != 0; }
 int64_t tune_stencil_small_pairs() { return g_small_pairs.load(std::memory_order_relaxed); }
 bool tune_take_oc_barrier_timeout() { return g_oc_timeout.exchange(0) != 0; }
 int tune_coarse_tail() { return g_tail.load(std::memory_order_relaxed); }
@@ -204,6 +208,12 @@ extern "C" int32_t tg_tune(int32_t key, int64_t value) {
     case TG_TUNE_STENCIL_TMA:
       if (value < 0 || value > 64) return TG_EINVAL;
       tg::tune_set_stencil_tma((int)value);
+      return TG_OK;
+    case TG_TUNE_CONV_UMMA:
+      tg::g_conv_umma.store(value != 0 ? 1 : 0);
+      return TG_OK;
+    case TG_TUNE_CONV_TIMEOUT:
+      tg::g_conv_timeout.store(value != 0 ? 1 : 0);
       return TG_OK;
     default:
       return TG_EINVAL;
