@@ -538,8 +538,8 @@ def _cpu_step_factory(size=CPU_SAMPLE):
     nx, ny, nz = size
     KE = O.ke_elast(3)
     fixed, f = O.bc_cantilever_3d(nx, ny, nz)
-    edof = O.edofmat(nx, ny, nz, 3)
-    H, Hs = O.filter_matrix(nx, ny, nz, RMIN)
+    edof = O.edofmat_vec(nx, ny, nz, 3)
+    H, Hs = O.filter_matrix_vec(nx, ny, nz, RMIN)
     ndof = f.shape[0]
     nel = nx * ny * nz
     free = np.setdiff1d(np.arange(ndof), fixed)
@@ -592,6 +592,52 @@ def cpu_baseline(steps=2, warmup=1):
             "host": _host_info()}
 
 
+def _ref_nonsolve_at_workload(size=None):
+    """The reference algorithm's functions of one design iteration other than
+    the solve, each timed once at the full grid on the host (oracle port,
+    single-threaded NumPy / SciPy like the reference): edofMat
+    (trilinear_hexahedron.py:7-58), COO assembly + CSR conversion
+    (fem.py:141-178), Dirichlet slicing K[free][:, free] (fem.py:208-237),
+    compliance + sensitivities (objectives.py:51-55,
+    topology_optimization.py:491-500), the distance-filter matrix
+    (matrix_filter.py:101-232), the sensitivity filter, the OC bisection
+    (optimality_criterion.py:59-79) and the density filter, at the uniform
+    start with a seeded random displacement (the solve's output is not
+    needed for timing)."""
+    from oracle import topopt as O
+    nx, ny, nz = size or SIZE
+    nel = nx * ny * nz
+    KE = O.ke_elast(3)
+    fixed, f = O.bc_cantilever_3d(nx, ny, nz)
+    ndof = f.shape[0]
+    free = np.setdiff1d(np.arange(ndof), fixed)
+    x = np.full(nel, VOLFRAC)
+    t = {}
+
+    def timed(key, fn):
+        t0 = time.perf_counter()
+        r = fn()
+        t[key] = time.perf_counter() - t0
+        return r
+    edof = timed("edofmat", lambda: O.edofmat_vec(nx, ny, nz, 3))
+    K = timed("assembly", lambda: O.assemble(KE, edof, O.simp(x), ndof))
+    timed("dirichlet_slicing", lambda: K[free][:, free])
+    del K
+    u = np.random.default_rng(0).standard_normal(ndof)
+    _, dc, _ = timed("compliance_and_sensitivities", lambda: O.compliance_sens(x, u, KE, edof))
+    H, Hs = timed("filter_matrix", lambda: O.filter_matrix_vec(nx, ny, nz, RMIN))
+    dv = np.ones(nel)
+    dcf, dvf = timed("sensitivity_filter", lambda: (np.asarray(H @ (dc / Hs)),
+                                                   np.asarray(H @ (dv / Hs))))
+    xn, _, nsteps = timed("oc_bisection", lambda: O.oc_top88(x, dcf, dvf, 0.0))
+    timed("density_filter", lambda: np.asarray(H @ xn) / Hs)
+    per_iter = (t["assembly"] + t["dirichlet_slicing"] + t["compliance_and_sensitivities"]
+                + t["sensitivity_filter"] + t["oc_bisection"] + t["density_filter"])
+    return {"grid": f"{nx}x{ny}x{nz}", "seconds": t, "oc_steps": nsteps, "cores": 1,
+            "seconds_per_design_iteration_without_solve": per_iter,
+            "set_up_once": ["edofmat", "filter_matrix"]}
+
+
 def run_reference(args, rank):
     """The reference algorithm's CPU path (oracle port: COO assembly, SciPy
     SuperLU, compliance, filter, OC) on the host cores.  The 160x80x80
@@ -618,6 +664,7 @@ def run_reference(args, rank):
             per[s].append(t)
             t_timed += t
     t_run = time.perf_counter() - t_run0
+    nonsolve = None if args.no_ref_nonsolve else _ref_nonsolve_at_workload()
     nel = np.array([float(np.prod(s)) for s in REF_LADDER])
     sec = np.array([statistics.median(per[s]) if per[s] else float("nan") for s in REF_LADDER])
     ok = np.isfinite(sec)
@@ -647,6 +694,7 @@ def run_reference(args, rank):
                    "fit_seconds_at_workload": t_full,
                    "ms_per_step_is": "measured mean wall time of the timed ladder steps",
                    "timed_seconds": t_timed, "run_seconds": t_run, "setup_seconds": t_setup,
+                   "nonsolve_at_workload": nonsolve,
                    "host": _host_info()},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
                          "sample": sample},
@@ -661,6 +709,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-ref-nonsolve", action="store_true",
+                    help="reference arm: skip timing the non-solve functions at 160x80x80")
     ap.add_argument("--train-iters", type=int, default=200,
                     help="design iterations recorded to train the warm-start network")
     ap.add_argument("--train-uniform", type=int, default=40,

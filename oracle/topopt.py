@@ -48,6 +48,24 @@ def edofmat(nelx, nely, nelz=None, ndof=1):
     return out
 
 
+def edofmat_vec(nelx, nely, nelz=None, ndof=1):
+    """edofmat with the elements vectorised, as the reference builds it
+    (elements/bilinear_quadrilateral.py:7-48, trilinear_hexahedron.py:7-58):
+    the same matrix, for grids where the per-element loop is too slow."""
+    corners = CORNERS_2D if nelz is None else CORNERS_3D
+    nz = 1 if nelz is None else nelz
+    e = np.arange(nelx * nely * nz, dtype=np.int64)
+    ez, rest = np.divmod(e, nelx * nely)
+    ex, ey = np.divmod(rest, nely)
+    out = np.empty((e.size, len(corners) * ndof), dtype=np.int32)
+    for k, c in enumerate(corners):
+        dz = c[2] if nelz is not None else 0
+        n = node_id(ex + c[0], ey + c[1], ez + dz, nelx, nely)
+        for d in range(ndof):
+            out[:, k * ndof + d] = n * ndof + d
+    return out
+
+
 # --------------------------------------------------------------------------
 # element matrices by 3-point Gauss quadrature (exact for these elements)
 # (elements/linear_elasticity_2d.py:69-229 plane stress,
@@ -217,6 +235,41 @@ def filter_matrix(nelx, nely, nelz, rmin):
             cols.append(j)
             vals.append(w)
     H = sp.csr_matrix((vals, (rows, cols)), shape=(nel, nel))
+    Hs = np.asarray(H.sum(1)).ravel()
+    return H, Hs
+
+
+def filter_matrix_vec(nelx, nely, nelz, rmin):
+    """filter_matrix with the loop over offsets only, all elements of an
+    offset at once (the reference builds H the same way,
+    filter/matrix_filter.py:170-231): the same entries, explicit zero
+    weights included, for grids where the per-element loop is too slow."""
+    ndim = 2 if nelz is None else 3
+    dims = (nelx, nely) if ndim == 2 else (nelx, nely, nelz)
+    R = int(np.ceil(rmin)) - 1
+    nel = int(np.prod(dims))
+    e = np.arange(nel, dtype=np.int64)
+    if ndim == 2:
+        ex, ey = np.divmod(e, nely)
+        c = (ex, ey)
+    else:
+        ez, rest = np.divmod(e, nelx * nely)
+        ex, ey = np.divmod(rest, nely)
+        c = (ex, ey, ez)
+    rows, cols, vals = [], [], []
+    for off in np.ndindex(*(2 * R + 1,) * ndim):
+        d = [o - R for o in off]
+        w = max(0.0, rmin - float(np.sqrt(sum(di * di for di in d))))
+        nb = [c[i] + d[i] for i in range(ndim)]
+        ok = np.ones(nel, dtype=bool)
+        for i in range(ndim):
+            ok &= (nb[i] >= 0) & (nb[i] < dims[i])
+        j = nb[0] * nely + nb[1] + (nb[2] * nelx * nely if ndim == 3 else 0)
+        rows.append(e[ok])
+        cols.append(j[ok])
+        vals.append(np.full(int(ok.sum()), w))
+    H = sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
+                      shape=(nel, nel))
     Hs = np.asarray(H.sum(1)).ravel()
     return H, Hs
 

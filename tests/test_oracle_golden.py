@@ -14,10 +14,12 @@ def test_edofmat(golden):
             _, dims, nd = k.split("_")
             nx, ny = map(int, dims.split("x"))
             np.testing.assert_array_equal(O.edofmat(nx, ny, None, int(nd)), d[k])
+            np.testing.assert_array_equal(O.edofmat_vec(nx, ny, None, int(nd)), d[k])
         elif k.startswith("edof3d"):
             _, dims, nd = k.split("_")
             nx, ny, nz = map(int, dims.split("x"))
             np.testing.assert_array_equal(O.edofmat(nx, ny, nz, int(nd)), d[k])
+            np.testing.assert_array_equal(O.edofmat_vec(nx, ny, nz, int(nd)), d[k])
 
 
 def test_element_matrices(golden):
@@ -38,6 +40,11 @@ def test_filter_matrix(golden):
         H, Hs = O.filter_matrix(int(a[0]), int(a[1]), nz, float(a[3]))
         np.testing.assert_allclose(H.toarray(), f["H_" + key], atol=1e-15)
         np.testing.assert_allclose(Hs, f["Hs_" + key], rtol=1e-14)
+        # the offset-vectorised builder (full-size timings) gives the same matrix
+        Hv, Hsv = O.filter_matrix_vec(int(a[0]), int(a[1]), nz, float(a[3]))
+        assert Hv.nnz == H.nnz
+        np.testing.assert_array_equal(Hv.toarray(), H.toarray())
+        np.testing.assert_array_equal(Hsv, Hs)
 
 
 def test_boundary_conditions(golden):
