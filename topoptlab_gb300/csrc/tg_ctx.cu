@@ -238,6 +238,7 @@ void ctx_init(Ctx& c, const tg_problem& p) {
   const Grid& g = c.g;
   const int64_t nn = g.nnodes(), nd = g.ndofs(), nel = g.nel();
   c.op.g = g;
+  c.op.flat64 = c.precision == TG_PREC_FP64;
   setup_element(c, p.KE);
 
   // fixed-DOF bits per node (caller's DOF numbers mapped to the device grid;

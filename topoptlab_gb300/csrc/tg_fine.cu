@@ -102,6 +102,7 @@ template <typename T, typename S> struct ApplyArgs {
   Sector<T> B;
   double* part;     // fused PCG dot: per-CTA partial sums
   PCGState* pst;    //   and the state it finalises
+  bool flat64;      // FineOp::flat64
 };
 
 template <int NDIM, int NDOF, typename T, bool SECTOR>
@@ -587,9 +588,8 @@ __device__ __forceinline__ void face_xz(T (&F)[4][NDOF]) {
 }
 
 // zc unused: blockIdx.z takes node planes [z nnz / gridDim.z, (z+1) nnz / gridDim.z)
-template <int NDOF, typename T, typename S, int KIND, int MODE, int DOTK = -1>
-__global__ void __launch_bounds__(zp::NT, sizeof(T) == 8 ? 1 : 3) k_fine_zpair(ApplyArgs<T, S> a,
-                                                                              int zc) {
+template <int NDOF, typename T, typename S, int KIND, int MODE, int DOTK = -1, bool FLAT = false>
+__global__ void __launch_bounds__(zp::NT, sizeof(T) == 8 ? 1 : 3) k_fine_zpair(ApplyArgs<T, S> a) {
   pdl_wait();
   pdl_trigger();
   using namespace zp;
@@ -601,12 +601,30 @@ __global__ void __launch_bounds__(zp::NT, sizeof(T) == 8 ? 1 : 3) k_fine_zpair(A
   T* xch = us + 3 * SLOT;                         // x exchange [(face*2 + dz)*NDOF + c][NT]
   const Grid& g = a.g;
   const int tid = threadIdx.x;
-  const int y0 = blockIdx.x * OY, x0 = blockIdx.y * OX;
-  (void)zc;
-  const int zbeg = (int)((int64_t)blockIdx.z * g.nnz / gridDim.z);
-  const int zend = (int)((int64_t)(blockIdx.z + 1) * g.nnz / gridDim.z);
   const int64_t pstride = (int64_t)g.nnx * g.nny * NDOF;
   const int64_t lstride = (int64_t)g.nex * g.ney;
+  // work units: (node column, node plane), column-major; a CTA owns the
+  // units [u0, u1) -- one column's z chunk (grid = columns x z chunks), or
+  // with FLAT an equal share of all units over a 1-D grid, which may run
+  // into the next column (a second segment; without FLAT the kernel
+  // compiles to a single segment, without the loop's registers)
+  const int gyn = (int)cdiv(g.nny, OY);
+  int64_t u0, u1;
+  if (FLAT) {
+    const int64_t U = (int64_t)gyn * cdiv(g.nnx, OX) * g.nnz;
+    u0 = (int64_t)blockIdx.x * U / gridDim.x;
+    u1 = (int64_t)(blockIdx.x + 1) * U / gridDim.x;
+  } else {
+    const int64_t col = (int64_t)blockIdx.y * gyn + blockIdx.x;
+    u0 = col * g.nnz + (int64_t)blockIdx.z * g.nnz / gridDim.z;
+    u1 = col * g.nnz + (int64_t)(blockIdx.z + 1) * g.nnz / gridDim.z;
+  }
+  T dacc = T(0);
+  do {
+  const int col = (int)(u0 / g.nnz);
+  const int zbeg = (int)(u0 - (int64_t)col * g.nnz);
+  const int zend = (int)min((int64_t)g.nnz, zbeg + (u1 - u0));
+  const int y0 = (col % gyn) * OY, x0 = (col / gyn) * OX;
 
   int goff[NCP], soff[NCP];
 #pragma unroll
@@ -659,7 +677,6 @@ __global__ void __launch_bounds__(zp::NT, sizeof(T) == 8 ? 1 : 3) k_fine_zpair(A
   cp_async_wait_all();
   __syncthreads();
   T rhoA = load_rho(zbeg - 1, vA, eoffA), rhoB = load_rho(zbeg - 1, vB, eoffA + 1);
-  T dacc = T(0);
   T acc[2][NDOF];
 #pragma unroll
   for (int f = 0; f < 2; ++f)
@@ -783,6 +800,8 @@ __global__ void __launch_bounds__(zp::NT, sizeof(T) == 8 ? 1 : 3) k_fine_zpair(A
     const int t = s0;
     s0 = s1; s1 = s2; s2 = t;
   }
+  u0 += zend - zbeg;
+  } while (FLAT && u0 < u1);
   if constexpr (DOTK >= 0) {
     __shared__ double sh[32];
     __shared__ int last;
@@ -821,6 +840,7 @@ static int sm_count() {
 // FP32, 2 in FP64), so that no second partial wave doubles the kernel time
 struct ZsShape {
   int gy, gx, chunks, zc;
+  bool flat = false;         // paired kernel: 1-D grid over (column, plane) units
   int64_t ctas() const { return (int64_t)gy * gx * chunks; }
 };
 static ZsShape zstream_shape(const Grid& g, bool fp64) {
@@ -841,7 +861,7 @@ static ZsShape zstream_shape(const Grid& g, bool fp64) {
 template <typename T, int KIND> constexpr bool use_zpair() { return KIND != EK_DENSE; }
 // its launch shape: 31 x 15 node columns, as many z chunks (balanced plane
 // ranges) as fill one wave of resident CTAs (3 per SM in FP32, 1 in FP64)
-static ZsShape zpair_shape(const Grid& g, bool fp64) {
+static ZsShape zpair_shape(const Grid& g, bool fp64, bool flat_ok) {
   ZsShape s;
   s.gy = (int)cdiv(g.nny, zp::OY);
   s.gx = (int)cdiv(g.nnx, zp::OX);
@@ -849,13 +869,22 @@ static ZsShape zpair_shape(const Grid& g, bool fp64) {
   const int cols = s.gx * s.gy;
   s.chunks = std::max(1, std::min(g.nnz, target / cols));
   s.zc = (int)cdiv(g.nnz, s.chunks);
+  s.flat = false;
+  if (fp64 && flat_ok && (int64_t)cols * s.chunks < target) {
+    // one CTA per SM: an equal share of the (column, plane) units each
+    // instead of whole-column chunks that leave SMs idle
+    const int64_t units = (int64_t)cols * g.nnz;
+    s.gy = (int)std::min<int64_t>(target, units);
+    s.gx = s.chunks = 1;
+    s.flat = true;
+  }
   return s;
 }
 // CTAs of the 3-D fine launch for (T, KIND) on g (fused dots need one
 // partial-sum slot per CTA)
 template <typename T, int KIND>
-static int64_t fine3d_ctas(const Grid& g) {
-  return use_zpair<T, KIND>() ? zpair_shape(g, sizeof(T) == 8).ctas()
+static int64_t fine3d_ctas(const Grid& g, bool flat64) {
+  return use_zpair<T, KIND>() ? zpair_shape(g, sizeof(T) == 8, flat64).ctas()
                               : zstream_shape(g, sizeof(T) == 8).ctas();
 }
 
@@ -865,16 +894,24 @@ static void launch_zstream(const ApplyArgs<T, S>& a, cudaStream_t st) {
                  : (std::is_same<S, float>::value ? PK_FINE_F32 : PK_FINE_BF16);
   if constexpr (use_zpair<T, KIND>()) {
     constexpr size_t smem = zp::smem<NDOF, T>();
-    auto kern = k_fine_zpair<NDOF, T, S, KIND, MODE, DOTK>;
-    set_smem_limit((const void*)kern, (int)smem);
-    const ZsShape sh = zpair_shape(a.g, sizeof(T) == 8);
+    const ZsShape sh = zpair_shape(a.g, sizeof(T) == 8, a.flat64);
     if (DOTK >= 0 && sh.ctas() > RED_BLOCKS)
       throw Error{EINVAL_, "fused dot: more CTAs than partial-sum slots"};
-    prof_begin(pk, st);
-    launch_pdl(kern, dim3((unsigned)sh.gy, (unsigned)sh.gx, (unsigned)sh.chunks), dim3(zp::NT),
-               smem, st, a, sh.zc);
-    prof_end(pk, st);
-    TG_CHECK_LAUNCH();
+    auto go = [&](auto kern) {
+      set_smem_limit((const void*)kern, (int)smem);
+      prof_begin(pk, st);
+      launch_pdl(kern, dim3((unsigned)sh.gy, (unsigned)sh.gx, (unsigned)sh.chunks), dim3(zp::NT),
+                 smem, st, a);
+      prof_end(pk, st);
+      TG_CHECK_LAUNCH();
+    };
+    if constexpr (sizeof(T) == 8) {
+      if (sh.flat) {
+        go(k_fine_zpair<NDOF, T, S, KIND, MODE, DOTK, true>);
+        return;
+      }
+    }
+    go(k_fine_zpair<NDOF, T, S, KIND, MODE, DOTK, false>);
     return;
   }
   constexpr size_t smem = zs::smem<NDOF, T, KIND>();
@@ -944,7 +981,7 @@ void fine_apply(const FineOp& op, const S* scale, const T* u, T* y, const T* b, 
   ApplyArgs<T, S> a;
   a.g = op.g; a.fix = op.fix; a.scale = scale; a.u = u; a.y = y; a.b = b; a.dinv = dinv;
   a.omega = (T)omega; a.KE = ke_ptr<T>(op); a.B = sec_ref<T>(op);
-  a.part = nullptr; a.pst = nullptr;
+  a.part = nullptr; a.pst = nullptr; a.flat64 = op.flat64;
   const int key = op.g.ndim * 10 + op.g.ndof;
   switch (key) {
     case 33: dispatch_apply<3, 3, T, S>(a, op.kind, mode, st); break;
@@ -963,7 +1000,7 @@ void fine_apply_dot(const FineOp& op, const S* scale, const T* u, T* y, const T*
              "fused dot: DOT_ALPHA with AM_Y or DOT_RHO with AM_JACOBI");
   const bool zstream = op.g.ndim == 3 && op.g.ndof == 3 && op.kind == EK_SECTOR_HEX8 &&
                        (int64_t)op.g.nnx * op.g.nny * 3 < (int64_t(1) << 31) &&
-                       fine3d_ctas<T, EK_SECTOR_HEX8>(op.g) <= RED_BLOCKS;
+                       fine3d_ctas<T, EK_SECTOR_HEX8>(op.g, op.flat64) <= RED_BLOCKS;
   if (!zstream) {   // other kernels (or more CTAs than partial slots): product, then dot
     fine_apply<T, S>(op, scale, u, y, b, dinv, omega, mode, st);
     dot<T, T>(op.g.ndofs(), dot_op == DOT_ALPHA ? u : b, y, part, pst, dot_op, st);
@@ -972,7 +1009,7 @@ void fine_apply_dot(const FineOp& op, const S* scale, const T* u, T* y, const T*
   ApplyArgs<T, S> a;
   a.g = op.g; a.fix = op.fix; a.scale = scale; a.u = u; a.y = y; a.b = b; a.dinv = dinv;
   a.omega = (T)omega; a.KE = ke_ptr<T>(op); a.B = sec_ref<T>(op);
-  a.part = part; a.pst = pst;
+  a.part = part; a.pst = pst; a.flat64 = op.flat64;
   if (dot_op == DOT_ALPHA) launch_zstream<3, T, S, EK_SECTOR_HEX8, AM_Y, DOT_ALPHA>(a, st);
   else launch_zstream<3, T, S, EK_SECTOR_HEX8, AM_JACOBI, DOT_RHO>(a, st);
 }

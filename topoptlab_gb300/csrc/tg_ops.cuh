@@ -35,6 +35,10 @@ struct FineOp {
   bool sector;              // use the sector path
   int kind;                 // element product: 0 dense, 1 sector, 2 sector with the hex8 zero pattern
   double KEdiag[24];        // diagonal of KE, corner-bit order
+  // 3-D FP64 paired products over an equal share of (column, plane) units
+  // per SM instead of whole-column chunks (the FP64 solver's contexts; the
+  // mixed solver's FP64 residual leaves SMs to the hierarchy build beside it)
+  bool flat64 = false;
 };
 
 enum ApplyMode : int { AM_Y = 0, AM_RES = 1, AM_JACOBI = 2 };
