@@ -128,7 +128,24 @@ def test_library_loads_and_exports_every_symbol():
     lib = ctypes.CDLL(path)
     for name in _declared_symbols():
         assert hasattr(lib, name), name
-    assert _lib.load().tg_abi_version() == 6
+    assert _lib.load().tg_abi_version() == _lib.TG_ABI_VERSION == 6
+
+
+def test_header_constants_match_binding():
+    """Every constant the header defines (status codes, precisions, fields,
+    learned bits, tg_tune keys, the ABI version, the allocation-free entry's
+    size limit) has the same value in the Python binding."""
+    txt = open(os.path.join(ROOT, "include", "topopt_gb300.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    vals = {}
+    for body in re.findall(r"enum\s*\{(.*?)\}", txt, flags=re.S):
+        for m in re.finditer(r"(TG_[A-Z0-9_]+)\s*=\s*(-?\d+)", body):
+            vals[m.group(1)] = int(m.group(2))
+    for m in re.finditer(r"#define\s+(TG_[A-Z0-9_]+)\s+(\d+)", txt):
+        vals[m.group(1)] = int(m.group(2))
+    assert len(vals) >= 29
+    for name, v in vals.items():
+        assert getattr(_lib, name) == v, name
 
 
 @pytest.mark.parametrize("case", ["nelx0", "ke_shape", "fixed_range", "f_length", "ft", "precision",

@@ -75,7 +75,7 @@ def test_noalloc_rejects_oversize(gpu_lib):
     lib = _lib.load()
     gt = C.c_double()
     ns = C.c_int32()
-    rc = lib.tg_oc_noalloc(2097152 + 1, 1, 1, 1, 0.0, None, 0.2, 0.0, 1e9, 1,
+    rc = lib.tg_oc_noalloc(_lib.TG_NOALLOC_MAX_N + 1, 1, 1, 1, 0.0, None, 0.2, 0.0, 1e9, 1,
                            C.byref(gt), C.byref(ns), None)
     assert rc == _lib.TG_EINVAL
     assert "exceeds" in lib.tg_noalloc_last_error().decode()

@@ -21,6 +21,9 @@ TG_PRECOND_GMG, TG_PRECOND_JACOBI = 0, 1
 TG_TUNE_STENCIL_SMALL_PAIRS, TG_TUNE_OC_BARRIER_TIMEOUT = 1, 2
 TG_TUNE_COARSE_TAIL, TG_TUNE_TAIL_BARRIER_TIMEOUT, TG_TUNE_STENCIL_TMA = 3, 4, 5
 TG_TUNE_PDL, TG_TUNE_CONV_UMMA, TG_TUNE_CONV_TIMEOUT = 6, 7, 8
+TG_LEARNED_WARM_START, TG_LEARNED_COARSE_CORRECTION = 1, 2
+TG_ABI_VERSION = 6            # the header this binding follows
+TG_NOALLOC_MAX_N = 2097152    # design variables tg_oc_noalloc's static scratch holds
 
 _dp = C.POINTER(C.c_double)
 _i64p = C.POINTER(C.c_int64)

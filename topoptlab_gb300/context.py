@@ -32,7 +32,9 @@ class IterResult:
 
 # parts of a learned network a problem uses once one is attached
 # (tg_problem.learned bits: 1 warm start, 2 coarse-grid correction)
-LEARNED_MODES = {"warm_start": 1, "coarse_correction": 2, "both": 3}
+LEARNED_MODES = {"warm_start": _lib.TG_LEARNED_WARM_START,
+                 "coarse_correction": _lib.TG_LEARNED_COARSE_CORRECTION,
+                 "both": _lib.TG_LEARNED_WARM_START | _lib.TG_LEARNED_COARSE_CORRECTION}
 
 
 def learned_mask(learned) -> int:
