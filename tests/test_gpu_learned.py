@@ -273,7 +273,7 @@ def test_coarse_correction_keeps_the_solution(gpu_lib):
 def test_learned_network_through_main(gpu_lib):
     """preconditioner_kw["learned"] carries trained parameters into the
     drop-in main: same design as main without the network (the solve's FP64
-    residual is the judge in both)."""
+    residual decides convergence in both)."""
     from topoptlab_gb300 import main
     from topoptlab_gb300.example_bc import cantilever_3d
     from topoptlab_gb300.elements import lk_linear_elast_3d

@@ -1,6 +1,6 @@
 """Modified SIMP interpolation (material_interpolation.py:6-62).
 
-These host functions identify the interpolation scheme the driver passes to
+These host functions identify the interpolation scheme that main passes to
 the GPU (eps, penal); the GPU kernels evaluate the same formulas in FP64."""
 from __future__ import annotations
 
