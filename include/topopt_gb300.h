@@ -312,7 +312,7 @@ int32_t tg_stats(int32_t reset, int64_t* launches, double* prof_ms, int64_t* pro
  * (default) runs the learned warm start's TF32 inference convolutions on the
  * 5th-generation tensor cores (tcgen05, accumulators in tensor memory); 0 on
  * warp-level mma.sync.  Both round the operands to TF32 the same way and
- * accumulate in FP32 (the sums in another order).  TG_TUNE_CONV_TIMEOUT:
+ * accumulate in FP32 in the same order (bit-identical outputs).  TG_TUNE_CONV_TIMEOUT:
  * value != 0 makes the next tensor-core convolution launch wait on a barrier
  * phase that never completes, so its bounded waits run out (about a second)
  * and the call that ran it returns TG_ETIMEOUT; the switch clears itself.

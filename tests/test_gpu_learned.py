@@ -102,10 +102,11 @@ def test_tensor_core_inference_matches_mma_sync(gpu_lib):
     """The warm start's inference convolutions on the 5th-generation tensor
     cores (tcgen05: operands in shared memory, FP32 accumulators in tensor
     memory, one thread issuing the MMAs) and on warp-level mma.sync round the
-    operands to TF32 the same way and accumulate in FP32 in different orders:
-    the outputs agree to 1e-4 of the largest output, on a level-1 grid of
-    25 x 13 x 13 nodes (partial 8 x 16 node tiles in y and x, 16 -> 32 -> 64
-    channels and back); both are within 1e-2 of the FP32-level forward."""
+    operands to TF32 the same way and add the K = 8 products per tap and
+    channel chunk in the same order (bit-identical outputs on GB300); asserted:
+    agreement to 1e-4 of the largest output, on a level-1 grid of 25 x 13 x 13
+    nodes (partial 8 x 16 node tiles in y and x, 16 -> 32 -> 64 channels and
+    back), and both within 1e-2 of the FP32-level forward."""
     from topoptlab_gb300 import _lib
     lib = _lib.load()
     prob, net, x0 = _infer_net(48, 24, 24, 5)
