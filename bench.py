@@ -664,7 +664,12 @@ def run_reference(args, rank):
             per[s].append(t)
             t_timed += t
     t_run = time.perf_counter() - t_run0
-    nonsolve = None if args.no_ref_nonsolve else _ref_nonsolve_at_workload()
+    nonsolve = None
+    if not args.no_ref_nonsolve:
+        try:
+            nonsolve = _ref_nonsolve_at_workload()
+        except (MemoryError, ValueError, RuntimeError) as e:   # the ladder line stands
+            nonsolve = {"unavailable": f"{type(e).__name__}: {e}"}
     nel = np.array([float(np.prod(s)) for s in REF_LADDER])
     sec = np.array([statistics.median(per[s]) if per[s] else float("nan") for s in REF_LADDER])
     ok = np.isfinite(sec)
