@@ -149,6 +149,39 @@ def test_compliance_and_sensitivity(gpu_lib, nelx, nely, nelz, kind):
     np.testing.assert_allclose(dc, dc_ref, rtol=1e-11, atol=1e-13 * np.abs(dc_ref).max())
 
 
+@pytest.mark.parametrize("nelx,nely,nelz,kind", [(20, 8, None, "elast"), (12, 6, 4, "elast"),
+                                                  (9, 7, None, "poisson")])
+def test_objectives_compliance_reference_signature(gpu_lib, nelx, nely, nelz, kind):
+    """objectives.compliance called as the reference calls it
+    (objectives.py:7-15: no grid sizes, u with one column per load case, the
+    SIMP parameters in matinterpol_kw): the grid comes from edofMat, the value
+    is the oracle's, a second call reuses the context, and rhs_adj = -u."""
+    from topoptlab_gb300 import objectives
+    from topoptlab_gb300.material_interpolation import simp
+    rng = np.random.default_rng(6)
+    ndim = 2 if nelz is None else 3
+    KE = O.ke_elast(ndim) if kind == "elast" else O.ke_poisson(ndim)
+    nd = KE.shape[0] // (4 if ndim == 2 else 8)
+    edof = O.edofmat(nelx, nely, nelz, nd)
+    nel = edof.shape[0]
+    ndof = nd * int(np.prod(np.array([nelx, nely] + ([nelz] if nelz else [])) + 1))
+    x = rng.uniform(0.05, 1.0, nel)
+    u = rng.standard_normal((ndof, 2))
+    kw = {"eps": 1e-9, "penal": 3.0}
+    try:
+        for i in (0, 1):
+            obj, rhs_adj, self_adj = objectives.compliance(x, u, KE, edof, i, simp, kw, 0.5)
+            obj_ref, _, _ = O.compliance_sens(x, u[:, i], KE, edof)
+            np.testing.assert_allclose(obj, 0.5 + obj_ref, rtol=1e-12)
+            assert self_adj is True
+            np.testing.assert_array_equal(rhs_adj, -u)
+            assert len(objectives._CTX) == 1
+    finally:
+        for p in objectives._CTX.values():
+            p.close()
+        objectives._CTX.clear()
+
+
 def test_oc_against_reference_steps(gpu_lib, golden):
     from topoptlab_gb300.optimizer import oc_top88
     g = golden("mbb2d_60x20.npz")

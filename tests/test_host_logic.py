@@ -187,3 +187,23 @@ def test_reference_solver_names_map(solver, precond):
     accepted and runs the GPU multigrid PCG with the caller's tolerance."""
     o = solver_options({"name": solver, "rtol": 1e-10, "maxiter": 10000}, {"name": precond})
     assert o["precond"] == "gb300-gmg" and o["rtol"] == 1e-10 and o["maxiter"] == 10000
+
+
+@pytest.mark.parametrize("nelx,nely,nelz,kind", [(60, 20, None, "elast"), (7, 5, None, "poisson"),
+                                                  (12, 6, 4, "elast"), (5, 4, 3, "poisson"),
+                                                  (1, 1, None, "elast"), (3, 1, 2, "poisson")])
+def test_compliance_infers_grid_from_edofmat(nelx, nely, nelz, kind):
+    """objectives.compliance takes the reference's signature (no grid sizes,
+    objectives.py:7-15): the grid and DOFs per node come from edofMat (the
+    reference numbering, pinned by the oracle's edofMat fixtures)."""
+    from oracle import topopt as O
+    from topoptlab_gb300.objectives import grid_from_edofmat
+    ndim = 2 if nelz is None else 3
+    nd = (ndim if kind == "elast" else 1)
+    ed = O.edofmat(nelx, nely, nelz, nd)
+    assert grid_from_edofmat(ed, ed.shape[1]) == (nelx, nely, nelz, nd)
+    with pytest.raises(ValueError):
+        grid_from_edofmat(ed, ed.shape[1] + 1)
+    if ed.shape[0] > 1:                      # elements out of order
+        with pytest.raises(ValueError):
+            grid_from_edofmat(ed[::-1], ed.shape[1])
