@@ -313,9 +313,10 @@ int32_t tg_stats(int32_t reset, int64_t* launches, double* prof_ms, int64_t* pro
  * 5th-generation tensor cores (tcgen05, accumulators in tensor memory); 0 on
  * warp-level mma.sync.  Both round the operands to TF32 the same way and
  * accumulate in FP32 in the same order (bit-identical outputs).  TG_TUNE_CONV_TIMEOUT:
- * value != 0 makes the next tensor-core convolution launch wait on a barrier
- * phase that never completes, so its bounded waits run out (about a second)
- * and the call that ran it returns TG_ETIMEOUT; the switch clears itself.
+ * value != 0 makes one CTA of the next tensor-core convolution launch wait on
+ * a barrier phase that never completes, so its bounded wait runs out (about
+ * a second), it frees its tensor memory and leaves, and the call that ran the
+ * launch returns TG_ETIMEOUT; the switch clears itself.
  * Unknown keys return TG_EINVAL. */
 enum {
   TG_TUNE_STENCIL_SMALL_PAIRS = 1,
